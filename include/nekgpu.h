@@ -1,0 +1,149 @@
+/*
+ * nekgpu.h -- C ABI of the GB300 Helmholtz/Poisson solve path for Nek5000.
+ *
+ * Drop-in replacements for the reference's matrix-free Helmholtz operator
+ * (axhelm), direct-stiffness sum (dssum -> gslib gs_op), Jacobi
+ * preconditioner (setprec) and Jacobi-PCG solver (cggo / hmholtz).  Every
+ * entry point takes its arguments by pointer, exactly as Fortran passes them,
+ * so a Fortran caller binds them with ISO_C_BINDING `bind(C)` interfaces and
+ * no name mangling; arrays are the reference's element-major layout
+ * (lx1,ly1,lz1,nel), x fastest.  The caller keeps ownership of every array it
+ * passes; the library copies what it needs.
+ *
+ * Status: every function returns 0 (NEKGPU_OK) or a negative NEKGPU_E* code;
+ * nekgpu_last_error() gives the message.  Nothing calls exit() and no device
+ * code traps.  A handle owns one CUDA stream on one device and is not
+ * thread-safe; separate handles may be used concurrently.
+ *
+ * Unless a name ends in _dev, array arguments are HOST pointers and the call
+ * moves them to and from the device inside the call.  The _dev variants take
+ * device pointers (cudaMalloc'ed, or torch tensors' data_ptr) and copy
+ * nothing; they run on the handle's stream and return when the work is
+ * complete.
+ */
+#ifndef NEKGPU_H
+#define NEKGPU_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NEKGPU_OK 0
+#define NEKGPU_EINVAL (-1)    /* bad argument: N, nel, null pointer, size   */
+#define NEKGPU_EHANDLE (-2)   /* unknown or finalized handle                */
+#define NEKGPU_ECUDA (-3)     /* CUDA runtime error                         */
+#define NEKGPU_ENOMEM (-4)    /* device allocation failed                   */
+#define NEKGPU_ENOTCONV (-5)  /* PCG stopped at maxit without converging    */
+#define NEKGPU_ENOSETUP (-6)  /* mesh / geometry not set up on the handle   */
+#define NEKGPU_ENAN (-7)      /* non-finite value met in the solve          */
+
+/* Largest polynomial order served (lx1 = N+1 <= NEKGPU_MAX_LX1). */
+#define NEKGPU_MAX_LX1 12
+
+/* Options for nekgpu_set_option */
+#define NEKGPU_OPT_EXACT 1   /* 1: FP64 products and sums rounded one by one in the
+                                reference's order (bit-faithful operator); 0: fused
+                                multiply-adds (default)                           */
+#define NEKGPU_OPT_TIMING 2  /* 1: time the solve and its operator kernels with
+                                CUDA events (nekgpu_last_timing)                  */
+#define NEKGPU_OPT_CHUNK 3   /* PCG iterations launched between host convergence
+                                checks (default 16)                               */
+#define NEKGPU_OPT_ISTEP 4   /* time-step index the reference's cggo sees; with
+                                istep <= 5 the first iteration may already stop
+                                (core/hmholtz.f:778)                              */
+
+/* ---- life cycle ---------------------------------------------------------- */
+/* Create a handle on CUDA device *device.  Replaces the per-rank setup the
+ * reference does once in nek_init (core/drive1.f:2-178). */
+int nekgpu_init(const int *device, int64_t *handle);
+int nekgpu_finalize(int64_t *handle);
+/* Copy the last error message (NUL-terminated, truncated to *buflen). */
+int nekgpu_last_error(const int64_t *handle, char *buf, const int *buflen);
+
+/* Set a handle option (NEKGPU_OPT_*). */
+int nekgpu_set_option(const int64_t *handle, const int *key, const int *value);
+
+/* ---- mesh data ----------------------------------------------------------- */
+/* Upload the operator data the reference keeps in COMMON blocks and build the
+ * gather-scatter maps:
+ *   dxm1(lx1,lx1)            -- /DXYZ/ (core/DXYZ, genwz core/coef.f:1-355)
+ *   g1..g6(lx1^3*nel)        -- /GMFACT/ g1m1..g6m1 (core/GEOM, geodat1 core/coef.f:633-784)
+ *   bm1(lx1^3*nel)           -- /MASS/ bm1 (core/MASS)
+ *   glo_num(lx1^3*nel)       -- global ids from set_vert (core/navier8.f:3-33);
+ *                               0 = not shared (element interior)
+ * Replaces setupds -> fgslib_gs_setup (core/dssum.f:1-31) plus the geometry
+ * COMMON-block setup.  Any earlier mesh on the handle is released. */
+int nekgpu_setup(const int64_t *handle, const int *lx1, const int *nel, const double *dxm1,
+                 const double *g1, const double *g2, const double *g3, const double *g4,
+                 const double *g5, const double *g6, const double *bm1, const int64_t *glo_num);
+
+/* Number of shared groups and of local copies in them (gs_setup's maps);
+ * with non-null outputs, copies the CSR maps: seg_start[nseg+1], idx[nidx]
+ * (0-based local indices, ascending inside a group, groups by ascending id). */
+int nekgpu_gs_maps(const int64_t *handle, int64_t *nseg, int64_t *nidx, int64_t *seg_start,
+                   int64_t *idx);
+
+/* ---- operator ------------------------------------------------------------ */
+/* au = h1 * A u + h2 * B u  (core/hmholtz.f:72-259, 3-D deformed path).
+ * imesh / isd are accepted for signature parity (imesh selects nelv/nelt in
+ * the reference; one element count is served here; isd only matters for the
+ * axisymmetric branch, which is not served). */
+int nekgpu_axhelm(const int64_t *handle, double *au, const double *u, const double *h1,
+                  const double *h2, const int *imesh, const int *isd);
+int nekgpu_axhelm_dev(const int64_t *handle, double *au, const double *u, const double *h1,
+                      const double *h2, const int *imesh, const int *isd);
+
+/* u <- dssum(u): sum of all local copies of every shared node, written back
+ * to each copy (core/dssum.f:33-98 -> fgslib_gs_op(gsh,u,1,1,0)). */
+int nekgpu_dssum(const int64_t *handle, double *u);
+int nekgpu_dssum_dev(const int64_t *handle, double *u);
+/* gs_op with op '+', '*', 'M' (max) or 'm' (min)  (core/dssum.f:100-160 dsop) */
+int nekgpu_dsop_dev(const int64_t *handle, double *u, const char *op);
+
+/* d = 1 / dssum(diag approx of h1*A + h2*B)  (core/hmholtz.f:380-524) */
+int nekgpu_setprec(const int64_t *handle, double *d, const double *h1, const double *h2,
+                   const int *imsh, const int *isd);
+int nekgpu_setprec_dev(const int64_t *handle, double *d, const double *h1, const double *h2,
+                       const int *imsh, const int *isd);
+
+/* ---- Jacobi-PCG ---------------------------------------------------------- */
+/* cggo (core/hmholtz.f:611-846): x solves H x = f with H = h1 A + h2 B,
+ * Jacobi preconditioner, masked by mask, dot products weighted by mult,
+ * residual norm sqrt(sum r^2 mult binv / vol).  tin < 0 means relative
+ * tolerance |tin| * (iteration-1 norm).  The reference's hard cap of 900
+ * iterations (maxcg) is applied when *maxcg is NULL; pass a pointer to lift
+ * it.  Outputs: *niter, *rbn0 (first norm), *rbn2 (last norm).  Returns
+ * NEKGPU_ENOTCONV (with x = the last iterate) when the cap is reached. */
+int nekgpu_cggo(const int64_t *handle, double *x, const double *f, const double *h1,
+                const double *h2, const double *mask, const double *mult, const int *imsh,
+                const double *tin, const int *maxit, const int *isd, const double *binv,
+                const int *maxcg, int *niter, double *rbn0, double *rbn2);
+int nekgpu_cggo_dev(const int64_t *handle, double *x, const double *f, const double *h1,
+                    const double *h2, const double *mask, const double *mult, const int *imsh,
+                    const double *tin, const int *maxit, const int *isd, const double *binv,
+                    const int *maxcg, int *niter, double *rbn0, double *rbn2);
+
+/* hmholtz (core/hmholtz.f:2-69): rhs <- mask * dssum(rhs) (in place, as the
+ * reference does), tolerance guard chktcg1 (:527-609), then cggo. */
+int nekgpu_hmholtz(const int64_t *handle, double *u, double *rhs, const double *h1,
+                   const double *h2, const double *mask, const double *mult, const int *imsh,
+                   const double *tli, const int *maxit, const int *isd, const double *binv,
+                   const int *maxcg, int *niter, double *rbn0, double *rbn2);
+int nekgpu_hmholtz_dev(const int64_t *handle, double *u, double *rhs, const double *h1,
+                       const double *h2, const double *mask, const double *mult,
+                       const int *imsh, const double *tli, const int *maxit, const int *isd,
+                       const double *binv, const int *maxcg, int *niter, double *rbn0,
+                       double *rbn2);
+
+/* ---- timing of the last solve (device time, CUDA events) ----------------- */
+/* ms_total: whole call on the device; ms_axhelm: summed axhelm-kernel time of
+ * the last cggo when the handle's kernel timing is on (nekgpu_set_timing). */
+int nekgpu_set_timing(const int64_t *handle, const int *on);
+int nekgpu_last_timing(const int64_t *handle, double *ms_total, double *ms_axhelm,
+                       int *n_axhelm);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,10 @@
+"""GB300-native Helmholtz/Poisson solve path for Nek5000.
+
+The compute path is libnekgpu.so (hand-written CUDA for sm_103a behind the C
+ABI of include/nekgpu.h).  This package holds its sources (csrc/), the build
+recipe (build.py), a ctypes binding (_capi.py), a front end with the
+reference's routine names (solver.py) and a synthetic box mesher (mesh.py).
+"""
+from .solver import NekGpu  # noqa: F401
+
+__all__ = ["NekGpu"]

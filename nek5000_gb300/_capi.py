@@ -1,0 +1,85 @@
+"""ctypes binding of libnekgpu.so (the C ABI declared in include/nekgpu.h).
+
+The library is the product: this module only loads it and declares the
+argument types.  If the shared object is missing the import fails loudly --
+there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libnekgpu.so")
+
+OK = 0
+EINVAL, EHANDLE, ECUDA, ENOMEM, ENOTCONV, ENOSETUP, ENAN = -1, -2, -3, -4, -5, -6, -7
+OPT_EXACT, OPT_TIMING, OPT_CHUNK, OPT_ISTEP = 1, 2, 3, 4
+MAX_LX1 = 12
+
+STATUS_NAMES = {
+    0: "NEKGPU_OK", -1: "NEKGPU_EINVAL", -2: "NEKGPU_EHANDLE", -3: "NEKGPU_ECUDA",
+    -4: "NEKGPU_ENOMEM", -5: "NEKGPU_ENOTCONV", -6: "NEKGPU_ENOSETUP", -7: "NEKGPU_ENAN",
+}
+
+# Every exported entry point and its argument types.  Pointer arguments are
+# passed as c_void_p so that host buffers (numpy) and device buffers (torch
+# data_ptr) go through the same declaration.
+_P = C.c_void_p
+_I64P = C.POINTER(C.c_int64)
+_IP = C.POINTER(C.c_int)
+_DP = C.POINTER(C.c_double)
+SIGNATURES = {
+    "nekgpu_init": [_IP, _I64P],
+    "nekgpu_finalize": [_I64P],
+    "nekgpu_last_error": [_I64P, C.c_char_p, _IP],
+    "nekgpu_set_option": [_I64P, _IP, _IP],
+    "nekgpu_setup": [_I64P, _IP, _IP, _P, _P, _P, _P, _P, _P, _P, _P, _P],
+    "nekgpu_gs_maps": [_I64P, _I64P, _I64P, _P, _P],
+    "nekgpu_axhelm": [_I64P, _P, _P, _P, _P, _IP, _IP],
+    "nekgpu_axhelm_dev": [_I64P, _P, _P, _P, _P, _IP, _IP],
+    "nekgpu_dssum": [_I64P, _P],
+    "nekgpu_dssum_dev": [_I64P, _P],
+    "nekgpu_dsop_dev": [_I64P, _P, C.c_char_p],
+    "nekgpu_setprec": [_I64P, _P, _P, _P, _IP, _IP],
+    "nekgpu_setprec_dev": [_I64P, _P, _P, _P, _IP, _IP],
+    "nekgpu_cggo": [_I64P, _P, _P, _P, _P, _P, _P, _IP, _DP, _IP, _IP, _P, _IP, _IP, _DP, _DP],
+    "nekgpu_cggo_dev": [_I64P, _P, _P, _P, _P, _P, _P, _IP, _DP, _IP, _IP, _P, _IP, _IP, _DP, _DP],
+    "nekgpu_hmholtz": [_I64P, _P, _P, _P, _P, _P, _P, _IP, _DP, _IP, _IP, _P, _IP, _IP, _DP, _DP],
+    "nekgpu_hmholtz_dev": [_I64P, _P, _P, _P, _P, _P, _P, _IP, _DP, _IP, _IP, _P, _IP, _IP, _DP,
+                           _DP],
+    "nekgpu_set_timing": [_I64P, _IP],
+    "nekgpu_last_timing": [_I64P, _DP, _DP, _IP],
+}
+
+_lib = None
+_lock = threading.Lock()
+
+
+def lib_path() -> str:
+    return LIB_PATH
+
+
+def load():
+    """Load libnekgpu.so (raises if it has not been built)."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(LIB_PATH):
+                raise RuntimeError(
+                    f"{LIB_PATH} is missing: build it with `python -m nek5000_gb300.build` "
+                    "(nvcc, sm_103a); there is no CPU fallback")
+            L = C.CDLL(LIB_PATH)
+            for name, args in SIGNATURES.items():
+                fn = getattr(L, name)
+                fn.argtypes = args
+                fn.restype = C.c_int
+            _lib = L
+    return _lib
+
+
+class NekGpuError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{STATUS_NAMES.get(code, code)}: {msg}")
+        self.code = code

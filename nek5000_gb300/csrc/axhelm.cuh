@@ -1,0 +1,214 @@
+// axhelm.cuh -- matrix-free Helmholtz operator, 3-D deformed elements.
+//
+//   au = h1 * sum_ij D_i^T (G_ij D_j u) + h2 * B u           (per element)
+//
+// Restates core/hmholtz.f:72-259 (3-D deformed branch :191-217, h2 term :225)
+// for one element per thread-slab: an lx1 x lx1 slab of threads owns the
+// element, thread (i,j) walks the z-column k = 0..lx1-1.  The element's field
+// is staged once in shared memory (row-padded against bank conflicts); D and
+// D^T live in shared memory and are read as warp broadcasts; the t-direction
+// transposed contraction accumulates in registers, so only the r and s
+// intermediates go through shared memory.  G is read once, coalesced
+// (consecutive i are consecutive addresses inside G[e][m][:]).
+//
+// Contraction order is the reference's mxm -> mxf<n> order
+// (core/mxm_std.f:139-230): sum over the inner index l = 0..lx1-1 left to
+// right.  With EXACT = true every product and sum is rounded separately, in
+// the reference's order, so FP64 results equal an unfused evaluation of the
+// Fortran bit for bit; EXACT = false uses fused multiply-adds.
+//
+// FUSED = true is the PCG form (hmholtz.f:795-801 folded together): the load
+// stage forms p <- r*d + beta*p (col3 + add2s1, :730, :795) and stores it,
+// the operator is applied to the new p, and the element-interior part of
+// rho = sum w*p*mult (glsc3 :801; interior points have mult = 1 and are not
+// touched by dssum/mask) is reduced into one FP64 partial per block.
+#pragma once
+#include "common.cuh"
+
+namespace nekgpu {
+
+template <typename T>
+struct AxArgs {
+  T* au;           // out: w
+  const T* u;      // in: field (plain) / old p (fused; may alias p)
+  const T* G;      // G[e][6][P]
+  const T* bm1;    // mass (read when h2mode != 0)
+  const T* h1;     // h1 array (h1mode 1)
+  const T* h2;     // h2 array (h2mode 2)
+  T h1s, h2s;      // uniform h1 (h1mode 0) / h2 (h2mode 1)
+  int h1mode, h2mode;
+  const T* D;      // lx1*lx1 row-major, D[i][j]
+  int nel;
+  // fused PCG operands
+  T* p;
+  const T* r;
+  const T* d;
+  const CgScalars* cg;
+  double* partial; // one per block
+};
+
+template <int NX>
+struct AxShape {
+  static constexpr int R = NX + 1;           // padded row
+  static constexpr int LP = NX * NX * R;     // padded element slab
+  static constexpr int P = NX * NX * NX;
+};
+
+template <int NX, typename T>
+__host__ __device__ constexpr size_t axhelm_smem_bytes(int epb) {
+  return (size_t)(2 * NX * (NX + 1) + epb * 3 * AxShape<NX>::LP) * sizeof(T);
+}
+
+template <int NX, typename T, bool EXACT, bool FUSED>
+__global__ void __launch_bounds__(256) axhelm_kernel(const AxArgs<T> a) {
+  constexpr int R = AxShape<NX>::R, LP = AxShape<NX>::LP, P = AxShape<NX>::P;
+  constexpr int NXY = NX * NX;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ double red[32];
+  T* sD = reinterpret_cast<T*>(smem_raw);  // sD[i*R+l]  = D[i][l]
+  T* sDT = sD + NX * R;                    // sDT[i*R+l] = D[l][i]
+  T* su = sDT + NX * R + threadIdx.y * 3 * LP;
+  T* st1 = su + LP;
+  T* st2 = st1 + LP;
+
+  if constexpr (FUSED) {
+    if (a.cg->done) return;  // uniform over the grid: nothing to do after convergence
+  }
+  const int tid = threadIdx.x;
+  const int i = tid % NX, j = tid / NX;
+  const int ft = tid + NXY * threadIdx.y, nthr = NXY * blockDim.y;
+  for (int q = ft; q < NXY; q += nthr) {
+    const int r = q / NX, c = q % NX;
+    const T v = a.D[q];
+    sD[r * R + c] = v;
+    sDT[c * R + r] = v;
+  }
+  const int e = blockIdx.x * blockDim.y + threadIdx.y;
+  const bool act = e < a.nel;
+  const size_t eo = (size_t)(act ? e : 0) * P;
+
+  T beta = T(0);
+  if constexpr (FUSED) beta = (T)a.cg->beta;
+
+  T ru[NX];
+#pragma unroll
+  for (int k = 0; k < NX; ++k) {
+    const int pt = k * NXY + j * NX + i;
+    T v = T(0);
+    if (act) {
+      if constexpr (FUSED) {
+        const T z = EXACT ? mul_x(a.r[eo + pt], a.d[eo + pt]) : a.r[eo + pt] * a.d[eo + pt];
+        v = madd<EXACT>(beta, a.u[eo + pt], z);  // add2s1: p = beta*p + z
+        a.p[eo + pt] = v;
+      } else {
+        v = a.u[eo + pt];
+      }
+    }
+    ru[k] = v;
+    su[k * NX * R + j * R + i] = v;
+  }
+  __syncthreads();
+
+  T rau[NX];
+#pragma unroll
+  for (int m = 0; m < NX; ++m) rau[m] = T(0);
+
+  const T* __restrict__ g = a.G + (size_t)(act ? e : 0) * 6 * P;
+#pragma unroll
+  for (int k = 0; k < NX; ++k) {
+    const T* slab = su + k * NX * R;
+    // dudr(i,jk) = sum_l D(i,l) u(l,jk)      (mxm(dxm1,lx1,u,lx1,dudr,nyz))
+    T ur = EXACT ? mul_x(sD[i * R], slab[j * R]) : sD[i * R] * slab[j * R];
+#pragma unroll
+    for (int l = 1; l < NX; ++l) ur = madd<EXACT>(sD[i * R + l], slab[j * R + l], ur);
+    // duds(i,j,k) = sum_l u(i,l,k) D(j,l)     (mxm(u(1,1,iz),lx1,dytm1,ly1,duds,ly1))
+    T us = EXACT ? mul_x(slab[i], sD[j * R]) : slab[i] * sD[j * R];
+#pragma unroll
+    for (int l = 1; l < NX; ++l) us = madd<EXACT>(slab[l * R + i], sD[j * R + l], us);
+    // dudt(ij,k) = sum_l u(ij,l) D(k,l)       (mxm(u,nxy,dztm1,lz1,dudt,lz1))
+    T ut = EXACT ? mul_x(ru[0], sD[k * R]) : ru[0] * sD[k * R];
+#pragma unroll
+    for (int l = 1; l < NX; ++l) ut = madd<EXACT>(ru[l], sD[k * R + l], ut);
+
+    const int pt = k * NXY + j * NX + i;
+    T g1 = 0, g2 = 0, g3 = 0, g4 = 0, g5 = 0, g6 = 0, h = a.h1s;
+    if (act) {
+      g1 = __ldg(g + pt);
+      g2 = __ldg(g + P + pt);
+      g3 = __ldg(g + 2 * P + pt);
+      g4 = __ldg(g + 3 * P + pt);
+      g5 = __ldg(g + 4 * P + pt);
+      g6 = __ldg(g + 5 * P + pt);
+      if (a.h1mode) h = __ldg(a.h1 + eo + pt);
+    }
+    // col3 / addcol3 order of hmholtz.f:199-206, then col2 by h1 (:207-209)
+    T t1 = EXACT ? mul_x(ur, g1) : ur * g1;
+    T t2 = EXACT ? mul_x(us, g2) : us * g2;
+    T t3 = EXACT ? mul_x(ut, g3) : ut * g3;
+    t1 = madd<EXACT>(us, g4, t1);
+    t1 = madd<EXACT>(ut, g5, t1);
+    t2 = madd<EXACT>(ur, g4, t2);
+    t2 = madd<EXACT>(ut, g6, t2);
+    t3 = madd<EXACT>(ur, g5, t3);
+    t3 = madd<EXACT>(us, g6, t3);
+    if (EXACT) {
+      t1 = mul_x(t1, h);
+      t2 = mul_x(t2, h);
+      t3 = mul_x(t3, h);
+    } else {
+      t1 *= h;
+      t2 *= h;
+      t3 *= h;
+    }
+    st1[k * NX * R + j * R + i] = t1;
+    st2[k * NX * R + j * R + i] = t2;
+    // tm3(ij,m) = sum_k tmp3(ij,k) D(k,m)      (mxm(tmp3,nxy,dzm1,lz1,tm3,lz1))
+#pragma unroll
+    for (int m = 0; m < NX; ++m) {
+      if (k == 0) rau[m] = EXACT ? mul_x(t3, sD[m]) : t3 * sD[m];
+      else rau[m] = madd<EXACT>(t3, sD[k * R + m], rau[m]);
+    }
+  }
+  __syncthreads();
+
+  T dot = T(0);  // interior w*p of this column, in field precision
+#pragma unroll
+  for (int k = 0; k < NX; ++k) {
+    const T* s1 = st1 + k * NX * R;
+    const T* s2 = st2 + k * NX * R;
+    // tm1(i,jk) = sum_l D(l,i) tmp1(l,jk)     (mxm(dxtm1,lx1,tmp1,lx1,tm1,nyz))
+    T tm1 = EXACT ? mul_x(sDT[i * R], s1[j * R]) : sDT[i * R] * s1[j * R];
+#pragma unroll
+    for (int l = 1; l < NX; ++l) tm1 = madd<EXACT>(sDT[i * R + l], s1[j * R + l], tm1);
+    // tm2(i,j,k) = sum_l tmp2(i,l,k) D(l,j)   (mxm(tmp2(1,1,iz),lx1,dym1,ly1,tm2,ly1))
+    T tm2 = EXACT ? mul_x(s2[i], sDT[j * R]) : s2[i] * sDT[j * R];
+#pragma unroll
+    for (int l = 1; l < NX; ++l) tm2 = madd<EXACT>(s2[l * R + i], sDT[j * R + l], tm2);
+    // au = ((0 + tm1) + tm2) + tm3   (rzero + add2 x3, :125, :215-217)
+    T s = EXACT ? add_x(add_x(tm1, tm2), rau[k]) : (tm1 + tm2) + rau[k];
+    const int pt = k * NXY + j * NX + i;
+    if (act) {
+      if (a.h2mode) {  // addcol4(au,helm2,bm1,u): au + helm2*bm1*u  (:225)
+        const T hh = (a.h2mode == 1) ? a.h2s : __ldg(a.h2 + eo + pt);
+        const T bm = __ldg(a.bm1 + eo + pt);
+        s = EXACT ? add_x(s, mul_x(mul_x(hh, bm), ru[k])) : fma(hh * bm, ru[k], s);
+      }
+      a.au[eo + pt] = s;
+      if constexpr (FUSED) {
+        if (i > 0 && i < NX - 1 && j > 0 && j < NX - 1 && k > 0 && k < NX - 1)
+          dot = fma(s, ru[k], dot);
+      }
+    }
+  }
+  if constexpr (FUSED) {
+    const double bsum = block_sum((double)dot, red);
+    if (threadIdx.x == 0 && threadIdx.y == 0) a.partial[blockIdx.x] = bsum;
+  }
+}
+
+// Elements per block for a given lx1 (about 256 threads, at least one element).
+__host__ __device__ constexpr int axhelm_epb(int nx) {
+  return (256 / (nx * nx)) > 0 ? (256 / (nx * nx)) : 1;
+}
+
+}  // namespace nekgpu

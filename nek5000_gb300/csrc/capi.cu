@@ -1,0 +1,561 @@
+// capi.cu -- the extern "C" entry points declared in include/nekgpu.h.
+//
+// Handles are small integers mapped to Handle objects; every call validates
+// its handle and arguments, records a message on failure and returns a
+// negative status.  Nothing here exits or traps.
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <mutex>
+
+#include "impl.cuh"
+#include "nekgpu.h"
+
+using namespace nekgpu;
+
+namespace {
+
+std::mutex g_mu;
+std::map<int64_t, std::unique_ptr<Handle>> g_handles;
+int64_t g_next = 1;
+thread_local std::string g_orphan_err;
+
+Handle* get(const int64_t* h) {
+  if (!h) return nullptr;
+  std::lock_guard<std::mutex> lk(g_mu);
+  auto it = g_handles.find(*h);
+  return it == g_handles.end() ? nullptr : it->second.get();
+}
+
+int fail(Handle* H, int code, const std::string& msg) {
+  if (H) H->err = msg;
+  else g_orphan_err = msg;
+  return code;
+}
+
+int cuda_fail(Handle* H, cudaError_t e, const char* where) {
+  return fail(H, NEKGPU_ECUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define GET_HANDLE(hp)                                                   \
+  Handle* H = get(hp);                                                   \
+  if (!H) return fail(nullptr, NEKGPU_EHANDLE, "unknown handle");        \
+  if (cudaSetDevice(H->device) != cudaSuccess)                           \
+    return fail(H, NEKGPU_ECUDA, "cudaSetDevice failed");
+
+#define NEED_MESH()                                                      \
+  if (!H->has_mesh) return fail(H, NEKGPU_ENOSETUP, "mesh not set up (nekgpu_setup)");
+
+__global__ void pack_g_kernel(double* __restrict__ G, const double* __restrict__ gm, int m, int P,
+                              int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t e = i / P;
+    const int p = (int)(i % P);
+    G[(e * 6 + m) * P + p] = gm[i];
+  }
+}
+
+__global__ void mul_kernel(double* __restrict__ a, const double* __restrict__ b, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    a[i] = a[i] * b[i];
+}
+
+__global__ void fill_kernel(double* __restrict__ a, double v, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    a[i] = v;
+}
+
+inline int nblk(int64_t n) {
+  int64_t b = (n + 255) / 256;
+  return (int)std::min<int64_t>(std::max<int64_t>(b, 1), 152 * 16);
+}
+
+// Device-side coefficient descriptor for host or device h1/h2.
+int make_coef(Handle* H, const double* h1, const double* h2, Coef<double>& c) {
+  if (!h1 || !h2) return fail(H, NEKGPU_EINVAL, "h1/h2 must not be null");
+  int st = detect_coef<double>(*H, h1, h2, H->mesh.n, c);
+  if (st) return fail(H, NEKGPU_ECUDA, "coefficient scan failed");
+  return 0;
+}
+
+int axhelm_dev(Handle* H, double* au, const double* u, const Coef<double>& c) {
+  cudaError_t e = H->exact ? launch_axhelm<double, true>(H->mesh, H->mesh.f64, au, u, c, H->stream)
+                           : launch_axhelm<double, false>(H->mesh, H->mesh.f64, au, u, c, H->stream);
+  if (e != cudaSuccess) return cuda_fail(H, e, "axhelm launch");
+  e = cudaStreamSynchronize(H->stream);
+  if (e != cudaSuccess) return cuda_fail(H, e, "axhelm");
+  return 0;
+}
+
+int h2d(Handle* H, DevBuf<double>& b, const double* src, int64_t n) {
+  if (b.ensure(n) != cudaSuccess) return fail(H, NEKGPU_ENOMEM, "staging allocation failed");
+  cudaError_t e = cudaMemcpyAsync(b.ptr, src, n * sizeof(double), cudaMemcpyHostToDevice, H->stream);
+  if (e != cudaSuccess) return cuda_fail(H, e, "host to device copy");
+  return 0;
+}
+
+int d2h(Handle* H, double* dst, const double* src, int64_t n) {
+  cudaError_t e = cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToHost, H->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(H->stream);
+  if (e != cudaSuccess) return cuda_fail(H, e, "device to host copy");
+  return 0;
+}
+
+// chktcg1 (core/hmholtz.f:527-609) on device arrays; EIGAA = 0 -> ACONDNO = 10
+int chktcg1_dev(Handle* H, double* tol, const double* res, const Coef<double>& c,
+                const double* mask, const double* mult, const double* binv) {
+  const int64_t n = H->mesh.n;
+  const double eps = 1.0e-13, acondno = 10.0, vol = H->mesh.vol;
+  int st = 0;
+  const double r2 = device_sum(*H, 4, binv, res, mult, n, &st);
+  if (st) return fail(H, st, "chktcg1: reduction failed");
+  const double rinit = std::sqrt(r2 / vol);
+  const double rmin = eps * rinit;
+  if (*tol < rmin) *tol = rmin;
+  const double bcneu1 = device_sum(*H, 5, mask, mult, nullptr, n, &st);
+  const double bcneu2 = device_sum(*H, 0, mult, nullptr, nullptr, n, &st);
+  const double bctest = std::fabs(bcneu1 - bcneu2);
+  DevBuf<double>& w1 = H->io5;
+  DevBuf<double>& w2 = H->io6;
+  if (w1.ensure(n) || w2.ensure(n)) return fail(H, NEKGPU_ENOMEM, "chktcg1: allocation failed");
+  fill_kernel<<<nblk(n), 256, 0, H->stream>>>(w1.ptr, 1.0, n);
+  int rc = axhelm_dev(H, w2.ptr, w1.ptr, c);
+  if (rc) return rc;
+  const double s = device_sum(*H, 2, w2.ptr, H->mesh.f64.bm1, nullptr, n, &st);
+  if (st) return fail(H, st, "chktcg1: reduction failed");
+  const double bcrob = std::sqrt(s / vol);
+  if (bctest < 0.1 && bcrob < eps * acondno) {
+    const double tolmin = rinit * eps * 10.0;
+    if (*tol < tolmin) *tol = tolmin;
+  }
+  return 0;
+}
+
+// cggo on device arrays.  Returns status; outputs niter/rbn0/rbn2.
+int cggo_dev(Handle* H, double* x, const double* f, const double* h1, const double* h2,
+             const double* mask, const double* mult, double tin, int maxit, int maxcg,
+             const double* binv, int* niter, double* rbn0, double* rbn2) {
+  Coef<double> c;
+  int rc = make_coef(H, h1, h2, c);
+  if (rc) return rc;
+  // non-trivial null space (no Dirichlet point, h2 == 0) needs the mean
+  // correction of hmholtz.f:705-750, which this solver does not provide
+  int st = 0;
+  if (c.h2mode == 0) {
+    DevBuf<double> tmp;
+    const int64_t n = H->mesh.n;
+    if (tmp.ensure(n)) return fail(H, NEKGPU_ENOMEM, "allocation failed");
+    // min(mask) > 0  <=>  max(1 - mask) < 1 ; use max|mask - 1| via kind 3 on (1-mask)
+    cudaMemcpyAsync(tmp.ptr, mask, n * sizeof(double), cudaMemcpyDeviceToDevice, H->stream);
+    const double mmax = device_sum(*H, 6, tmp.ptr, nullptr, nullptr, n, &st);  // min(mask)
+    if (!st && mmax > 0.0)
+      return fail(H, NEKGPU_EINVAL,
+                  "cggo: singular operator (no Dirichlet point and h2 = 0) is not supported");
+  }
+  const int maxiter = std::min(maxit, maxcg);
+  PcgResult r = pcg_solve<double>(*H, H->mesh.f64, H->w64, x, f, c, mask, mult, binv, tin,
+                                  maxiter, H->istep, H->exact);
+  if (niter) *niter = r.niter;
+  if (rbn0) *rbn0 = r.rbn0;
+  if (rbn2) *rbn2 = r.rbn2;
+  if (r.status == -5) return NEKGPU_ENOTCONV;
+  if (r.status == -7) return NEKGPU_ENAN;
+  if (r.status) return fail(H, r.status, H->err.empty() ? "pcg failed" : H->err);
+  return 0;
+}
+
+int hmholtz_dev(Handle* H, double* u, double* rhs, const double* h1, const double* h2,
+                const double* mask, const double* mult, double tli, int maxit, int maxcg,
+                const double* binv, int* niter, double* rbn0, double* rbn2) {
+  const int64_t n = H->mesh.n;
+  double tol = std::fabs(tli);
+  gs_op<double>(H->mesh.gs, rhs, 0, H->stream);                       // dssum(rhs)
+  mul_kernel<<<nblk(n), 256, 0, H->stream>>>(rhs, mask, n);           // col2(rhs,mask)
+  Coef<double> c;
+  int rc = make_coef(H, h1, h2, c);
+  if (rc) return rc;
+  rc = chktcg1_dev(H, &tol, rhs, c, mask, mult, binv);
+  if (rc) return rc;
+  if (tli < 0) tol = tli;
+  return cggo_dev(H, u, rhs, h1, h2, mask, mult, tol, maxit, maxcg, binv, niter, rbn0, rbn2);
+}
+
+int check_n(Handle* H, const void* p) {
+  if (!p) return fail(H, NEKGPU_EINVAL, "null array argument");
+  return 0;
+}
+
+}  // namespace
+
+namespace nekgpu {
+// extra reductions used above (kinds 4, 5, 6), defined in pcg.cu's sum kernel
+}
+
+extern "C" {
+
+int nekgpu_init(const int* device, int64_t* handle) {
+  if (!device || !handle) return fail(nullptr, NEKGPU_EINVAL, "null argument");
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0) return fail(nullptr, NEKGPU_ECUDA, "no CUDA device");
+  if (*device < 0 || *device >= ndev) return fail(nullptr, NEKGPU_EINVAL, "device out of range");
+  auto H = std::make_unique<Handle>();
+  H->device = *device;
+  if ((e = cudaSetDevice(H->device)) != cudaSuccess) return cuda_fail(nullptr, e, "cudaSetDevice");
+  if ((e = cudaStreamCreateWithFlags(&H->stream, cudaStreamNonBlocking)) != cudaSuccess)
+    return cuda_fail(nullptr, e, "stream");
+  if ((e = cudaMalloc(&H->cg, sizeof(CgScalars))) != cudaSuccess) return cuda_fail(nullptr, e, "alloc");
+  if ((e = cudaMallocHost(&H->cg_host, sizeof(CgScalars))) != cudaSuccess)
+    return cuda_fail(nullptr, e, "alloc");
+  if ((e = cudaMalloc(&H->flag, sizeof(int) * 4)) != cudaSuccess) return cuda_fail(nullptr, e, "alloc");
+  cudaMemset(H->cg, 0, sizeof(CgScalars));
+  cudaEventCreate(&H->ev0);
+  cudaEventCreate(&H->ev1);
+  cudaEventCreate(&H->evt0);
+  cudaEventCreate(&H->evt1);
+  std::lock_guard<std::mutex> lk(g_mu);
+  *handle = g_next++;
+  g_handles[*handle] = std::move(H);
+  return NEKGPU_OK;
+}
+
+int nekgpu_finalize(int64_t* handle) {
+  Handle* H = get(handle);
+  if (!H) return fail(nullptr, NEKGPU_EHANDLE, "unknown handle");
+  cudaSetDevice(H->device);
+  cudaStreamSynchronize(H->stream);
+  gs_free(H->mesh.gs);
+  H->mesh.f64.release();
+  H->mesh.f32.release();
+  cudaFree(H->cg);
+  cudaFreeHost(H->cg_host);
+  cudaFree(H->flag);
+  cudaEventDestroy(H->ev0);
+  cudaEventDestroy(H->ev1);
+  cudaEventDestroy(H->evt0);
+  cudaEventDestroy(H->evt1);
+  cudaStreamDestroy(H->stream);
+  std::lock_guard<std::mutex> lk(g_mu);
+  g_handles.erase(*handle);
+  *handle = 0;
+  return NEKGPU_OK;
+}
+
+int nekgpu_last_error(const int64_t* handle, char* buf, const int* buflen) {
+  if (!buf || !buflen || *buflen <= 0) return NEKGPU_EINVAL;
+  Handle* H = get(handle);
+  const std::string& m = H ? H->err : g_orphan_err;
+  const size_t k = std::min<size_t>(m.size(), (size_t)*buflen - 1);
+  std::memcpy(buf, m.data(), k);
+  buf[k] = '\0';
+  return NEKGPU_OK;
+}
+
+int nekgpu_set_option(const int64_t* handle, const int* key, const int* value) {
+  GET_HANDLE(handle);
+  if (!key || !value) return fail(H, NEKGPU_EINVAL, "null argument");
+  switch (*key) {
+    case NEKGPU_OPT_EXACT: H->exact = (*value != 0); break;
+    case NEKGPU_OPT_TIMING: H->timing = (*value != 0); break;
+    case NEKGPU_OPT_CHUNK:
+      if (*value < 1) return fail(H, NEKGPU_EINVAL, "chunk must be >= 1");
+      H->graph_chunk = *value;
+      break;
+    case NEKGPU_OPT_ISTEP: H->istep = *value; break;
+    default: return fail(H, NEKGPU_EINVAL, "unknown option");
+  }
+  return NEKGPU_OK;
+}
+
+int nekgpu_setup(const int64_t* handle, const int* lx1, const int* nel, const double* dxm1,
+                 const double* g1, const double* g2, const double* g3, const double* g4,
+                 const double* g5, const double* g6, const double* bm1, const int64_t* glo_num) {
+  GET_HANDLE(handle);
+  if (!lx1 || !nel || !dxm1 || !g1 || !g2 || !g3 || !g4 || !g5 || !g6 || !bm1 || !glo_num)
+    return fail(H, NEKGPU_EINVAL, "null argument");
+  if (*lx1 < 2 || *lx1 > NEKGPU_MAX_LX1)
+    return fail(H, NEKGPU_EINVAL, "lx1 out of range [2, " + std::to_string(NEKGPU_MAX_LX1) + "]");
+  if (*nel < 1) return fail(H, NEKGPU_EINVAL, "nel must be positive");
+  cudaStreamSynchronize(H->stream);
+  Mesh& m = H->mesh;
+  gs_free(m.gs);
+  m.f64.release();
+  m.f32.release();
+  m.has_f32 = false;
+  H->has_mesh = false;
+  m.nx1 = *lx1;
+  m.nel = *nel;
+  const int P = m.nx1 * m.nx1 * m.nx1;
+  m.n = (int64_t)P * m.nel;
+  const int64_t n = m.n;
+  cudaError_t e;
+  if ((e = cudaMalloc(&m.f64.G, 6 * n * sizeof(double))) != cudaSuccess ||
+      (e = cudaMalloc(&m.f64.bm1, n * sizeof(double))) != cudaSuccess ||
+      (e = cudaMalloc(&m.f64.D, m.nx1 * m.nx1 * sizeof(double))) != cudaSuccess) {
+    m.f64.release();
+    return fail(H, NEKGPU_ENOMEM, "mesh allocation failed");
+  }
+  // D row-major from the Fortran-ordered dxm1(i,j) = dxm1[i + j*lx1]
+  m.h_D.assign((size_t)m.nx1 * m.nx1, 0.0);
+  for (int i = 0; i < m.nx1; ++i)
+    for (int j = 0; j < m.nx1; ++j) m.h_D[i * m.nx1 + j] = dxm1[i + j * m.nx1];
+  cudaMemcpy(m.f64.D, m.h_D.data(), m.h_D.size() * sizeof(double), cudaMemcpyHostToDevice);
+  const double* gs6[6] = {g1, g2, g3, g4, g5, g6};
+  DevBuf<double> stage;
+  if (stage.ensure(n)) return fail(H, NEKGPU_ENOMEM, "staging allocation failed");
+  for (int q = 0; q < 6; ++q) {
+    if ((e = cudaMemcpy(stage.ptr, gs6[q], n * sizeof(double), cudaMemcpyHostToDevice)) !=
+        cudaSuccess)
+      return cuda_fail(H, e, "geometry upload");
+    pack_g_kernel<<<nblk(n), 256, 0, 0>>>(m.f64.G, stage.ptr, q, P, n);
+    if ((e = cudaDeviceSynchronize()) != cudaSuccess) return cuda_fail(H, e, "geometry pack");
+  }
+  if ((e = cudaMemcpy(m.f64.bm1, bm1, n * sizeof(double), cudaMemcpyHostToDevice)) != cudaSuccess)
+    return cuda_fail(H, e, "mass upload");
+  // volvm1 = glsum(bm1): serial left-to-right, as one rank of the reference
+  double vol = 0.0;
+  for (int64_t i = 0; i < n; ++i) vol = vol + bm1[i];
+  m.vol = vol;
+  std::string err;
+  int rc = gs_setup(m.gs, glo_num, n, err);
+  if (rc) return fail(H, rc == -4 ? NEKGPU_ENOMEM : NEKGPU_EINVAL, err);
+  H->has_mesh = true;
+  return NEKGPU_OK;
+}
+
+int nekgpu_gs_maps(const int64_t* handle, int64_t* nseg, int64_t* nidx, int64_t* seg_start,
+                   int64_t* idx) {
+  GET_HANDLE(handle);
+  NEED_MESH();
+  const GsMaps& g = H->mesh.gs;
+  if (nseg) *nseg = g.nseg;
+  if (nidx) *nidx = g.nidx;
+  if (seg_start) std::memcpy(seg_start, g.h_start.data(), g.h_start.size() * sizeof(int64_t));
+  if (idx) std::memcpy(idx, g.h_idx.data(), g.h_idx.size() * sizeof(int64_t));
+  return NEKGPU_OK;
+}
+
+int nekgpu_axhelm_dev(const int64_t* handle, double* au, const double* u, const double* h1,
+                      const double* h2, const int* imesh, const int* isd) {
+  GET_HANDLE(handle);
+  NEED_MESH();
+  (void)imesh;
+  (void)isd;
+  if (check_n(H, au) || check_n(H, u)) return NEKGPU_EINVAL;
+  Coef<double> c;
+  int rc = make_coef(H, h1, h2, c);
+  if (rc) return rc;
+  if (H->timing) cudaEventRecord(H->evt0, H->stream);
+  rc = axhelm_dev(H, au, u, c);
+  if (H->timing && !rc) {
+    cudaEventRecord(H->evt1, H->stream);
+    cudaEventSynchronize(H->evt1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, H->evt0, H->evt1);
+    H->ms_total = ms;
+    H->ms_axhelm = ms;
+    H->n_axhelm = 1;
+  }
+  return rc;
+}
+
+int nekgpu_axhelm(const int64_t* handle, double* au, const double* u, const double* h1,
+                  const double* h2, const int* imesh, const int* isd) {
+  GET_HANDLE(handle);
+  NEED_MESH();
+  if (check_n(H, au) || check_n(H, u) || check_n(H, h1) || check_n(H, h2)) return NEKGPU_EINVAL;
+  const int64_t n = H->mesh.n;
+  int rc;
+  if ((rc = h2d(H, H->io0, u, n)) || (rc = h2d(H, H->io1, h1, n)) || (rc = h2d(H, H->io2, h2, n)))
+    return rc;
+  if (H->io3.ensure(n)) return fail(H, NEKGPU_ENOMEM, "staging allocation failed");
+  rc = nekgpu_axhelm_dev(handle, H->io3.ptr, H->io0.ptr, H->io1.ptr, H->io2.ptr, imesh, isd);
+  if (rc) return rc;
+  return d2h(H, au, H->io3.ptr, n);
+}
+
+int nekgpu_dssum_dev(const int64_t* handle, double* u) {
+  GET_HANDLE(handle);
+  NEED_MESH();
+  if (check_n(H, u)) return NEKGPU_EINVAL;
+  gs_op<double>(H->mesh.gs, u, 0, H->stream);
+  cudaError_t e = cudaStreamSynchronize(H->stream);
+  if (e != cudaSuccess) return cuda_fail(H, e, "dssum");
+  return NEKGPU_OK;
+}
+
+int nekgpu_dssum(const int64_t* handle, double* u) {
+  GET_HANDLE(handle);
+  NEED_MESH();
+  if (check_n(H, u)) return NEKGPU_EINVAL;
+  int rc = h2d(H, H->io0, u, H->mesh.n);
+  if (rc) return rc;
+  rc = nekgpu_dssum_dev(handle, H->io0.ptr);
+  if (rc) return rc;
+  return d2h(H, u, H->io0.ptr, H->mesh.n);
+}
+
+int nekgpu_dsop_dev(const int64_t* handle, double* u, const char* op) {
+  GET_HANDLE(handle);
+  NEED_MESH();
+  if (check_n(H, u) || !op) return fail(H, NEKGPU_EINVAL, "null argument");
+  int code;
+  switch (op[0]) {
+    case '+': code = 0; break;
+    case '*': code = 1; break;
+    case 'M': code = 2; break;
+    case 'm': code = 3; break;
+    default: return fail(H, NEKGPU_EINVAL, "dsop: op must be one of + * M m");
+  }
+  gs_op<double>(H->mesh.gs, u, code, H->stream);
+  cudaError_t e = cudaStreamSynchronize(H->stream);
+  if (e != cudaSuccess) return cuda_fail(H, e, "dsop");
+  return NEKGPU_OK;
+}
+
+int nekgpu_setprec_dev(const int64_t* handle, double* d, const double* h1, const double* h2,
+                       const int* imsh, const int* isd) {
+  GET_HANDLE(handle);
+  NEED_MESH();
+  (void)imsh;
+  (void)isd;
+  if (check_n(H, d)) return NEKGPU_EINVAL;
+  Coef<double> c;
+  int rc = make_coef(H, h1, h2, c);
+  if (rc) return rc;
+  if (setprec_f64(*H, d, c)) return fail(H, NEKGPU_ECUDA, "setprec launch");
+  cudaError_t e = cudaStreamSynchronize(H->stream);
+  if (e != cudaSuccess) return cuda_fail(H, e, "setprec");
+  return NEKGPU_OK;
+}
+
+int nekgpu_setprec(const int64_t* handle, double* d, const double* h1, const double* h2,
+                   const int* imsh, const int* isd) {
+  GET_HANDLE(handle);
+  NEED_MESH();
+  if (check_n(H, d) || check_n(H, h1) || check_n(H, h2)) return NEKGPU_EINVAL;
+  const int64_t n = H->mesh.n;
+  int rc;
+  if ((rc = h2d(H, H->io1, h1, n)) || (rc = h2d(H, H->io2, h2, n))) return rc;
+  if (H->io3.ensure(n)) return fail(H, NEKGPU_ENOMEM, "staging allocation failed");
+  rc = nekgpu_setprec_dev(handle, H->io3.ptr, H->io1.ptr, H->io2.ptr, imsh, isd);
+  if (rc) return rc;
+  return d2h(H, d, H->io3.ptr, n);
+}
+
+int nekgpu_cggo_dev(const int64_t* handle, double* x, const double* f, const double* h1,
+                    const double* h2, const double* mask, const double* mult, const int* imsh,
+                    const double* tin, const int* maxit, const int* isd, const double* binv,
+                    const int* maxcg, int* niter, double* rbn0, double* rbn2) {
+  GET_HANDLE(handle);
+  NEED_MESH();
+  (void)imsh;
+  (void)isd;
+  if (check_n(H, x) || check_n(H, f) || check_n(H, mask) || check_n(H, mult) ||
+      check_n(H, binv) || !tin || !maxit)
+    return fail(H, NEKGPU_EINVAL, "null argument");
+  if (H->timing) cudaEventRecord(H->evt0, H->stream);
+  int rc = cggo_dev(H, x, f, h1, h2, mask, mult, *tin, *maxit, maxcg ? *maxcg : 900, binv, niter,
+                    rbn0, rbn2);
+  if (H->timing) {
+    cudaEventRecord(H->evt1, H->stream);
+    cudaEventSynchronize(H->evt1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, H->evt0, H->evt1);
+    H->ms_total = ms;
+  }
+  return rc;
+}
+
+int nekgpu_cggo(const int64_t* handle, double* x, const double* f, const double* h1,
+                const double* h2, const double* mask, const double* mult, const int* imsh,
+                const double* tin, const int* maxit, const int* isd, const double* binv,
+                const int* maxcg, int* niter, double* rbn0, double* rbn2) {
+  GET_HANDLE(handle);
+  NEED_MESH();
+  if (check_n(H, x) || check_n(H, f) || check_n(H, h1) || check_n(H, h2) || check_n(H, mask) ||
+      check_n(H, mult) || check_n(H, binv))
+    return NEKGPU_EINVAL;
+  const int64_t n = H->mesh.n;
+  int rc;
+  if ((rc = h2d(H, H->io0, f, n)) || (rc = h2d(H, H->io1, h1, n)) || (rc = h2d(H, H->io2, h2, n)) ||
+      (rc = h2d(H, H->io4, mask, n)) || (rc = h2d(H, H->io5, mult, n)) ||
+      (rc = h2d(H, H->io6, binv, n)))
+    return rc;
+  if (H->io3.ensure(n)) return fail(H, NEKGPU_ENOMEM, "staging allocation failed");
+  rc = nekgpu_cggo_dev(handle, H->io3.ptr, H->io0.ptr, H->io1.ptr, H->io2.ptr, H->io4.ptr,
+                       H->io5.ptr, imsh, tin, maxit, isd, H->io6.ptr, maxcg, niter, rbn0, rbn2);
+  if (rc && rc != NEKGPU_ENOTCONV) return rc;
+  int rc2 = d2h(H, x, H->io3.ptr, n);
+  return rc2 ? rc2 : rc;
+}
+
+int nekgpu_hmholtz_dev(const int64_t* handle, double* u, double* rhs, const double* h1,
+                       const double* h2, const double* mask, const double* mult,
+                       const int* imsh, const double* tli, const int* maxit, const int* isd,
+                       const double* binv, const int* maxcg, int* niter, double* rbn0,
+                       double* rbn2) {
+  GET_HANDLE(handle);
+  NEED_MESH();
+  (void)imsh;
+  (void)isd;
+  if (check_n(H, u) || check_n(H, rhs) || check_n(H, mask) || check_n(H, mult) ||
+      check_n(H, binv) || !tli || !maxit)
+    return fail(H, NEKGPU_EINVAL, "null argument");
+  if (H->timing) cudaEventRecord(H->evt0, H->stream);
+  int rc = hmholtz_dev(H, u, rhs, h1, h2, mask, mult, *tli, *maxit, maxcg ? *maxcg : 900, binv,
+                       niter, rbn0, rbn2);
+  if (H->timing) {
+    cudaEventRecord(H->evt1, H->stream);
+    cudaEventSynchronize(H->evt1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, H->evt0, H->evt1);
+    H->ms_total = ms;
+  }
+  return rc;
+}
+
+int nekgpu_hmholtz(const int64_t* handle, double* u, double* rhs, const double* h1,
+                   const double* h2, const double* mask, const double* mult, const int* imsh,
+                   const double* tli, const int* maxit, const int* isd, const double* binv,
+                   const int* maxcg, int* niter, double* rbn0, double* rbn2) {
+  GET_HANDLE(handle);
+  NEED_MESH();
+  if (check_n(H, u) || check_n(H, rhs) || check_n(H, h1) || check_n(H, h2) || check_n(H, mask) ||
+      check_n(H, mult) || check_n(H, binv))
+    return NEKGPU_EINVAL;
+  const int64_t n = H->mesh.n;
+  int rc;
+  if ((rc = h2d(H, H->io0, rhs, n)) || (rc = h2d(H, H->io1, h1, n)) ||
+      (rc = h2d(H, H->io2, h2, n)) || (rc = h2d(H, H->io4, mask, n)) ||
+      (rc = h2d(H, H->io7, mult, n)) || (rc = h2d(H, H->io8, binv, n)))
+    return rc;
+  if (H->io3.ensure(n)) return fail(H, NEKGPU_ENOMEM, "staging allocation failed");
+  rc = nekgpu_hmholtz_dev(handle, H->io3.ptr, H->io0.ptr, H->io1.ptr, H->io2.ptr, H->io4.ptr,
+                          H->io7.ptr, imsh, tli, maxit, isd, H->io8.ptr, maxcg, niter, rbn0, rbn2);
+  if (rc && rc != NEKGPU_ENOTCONV) return rc;
+  int rc2 = d2h(H, u, H->io3.ptr, n);
+  if (!rc2) rc2 = d2h(H, rhs, H->io0.ptr, n);
+  return rc2 ? rc2 : rc;
+}
+
+int nekgpu_set_timing(const int64_t* handle, const int* on) {
+  GET_HANDLE(handle);
+  if (!on) return fail(H, NEKGPU_EINVAL, "null argument");
+  H->timing = (*on != 0);
+  return NEKGPU_OK;
+}
+
+int nekgpu_last_timing(const int64_t* handle, double* ms_total, double* ms_axhelm,
+                       int* n_axhelm) {
+  GET_HANDLE(handle);
+  if (ms_total) *ms_total = H->ms_total;
+  if (ms_axhelm) *ms_axhelm = H->ms_axhelm;
+  if (n_axhelm) *n_axhelm = H->n_axhelm;
+  return NEKGPU_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,75 @@
+// common.cuh -- internal types and device helpers of the nekgpu library.
+//
+// Data layout in HBM (one mesh per handle):
+//   geometric factors  G[e][m][p], m = 0..5 (G1..G6), p = 0..lx1^3-1
+//                      (element-blocked: one element's six factors form one
+//                      contiguous 6*lx1^3 block, read once per operator apply)
+//   fields             f[e*lx1^3 + p], the reference's element-major layout
+//   derivative matrix  D[i][j] row-major (D[i][j] = dl_j/dr at z_i)
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+namespace nekgpu {
+
+constexpr int kMaxLx1 = 12;
+
+// ---- reductions: deterministic (fixed tree, no floating-point atomics) ----
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Sum over the whole block; the result is valid in every thread.
+// `scratch` must hold 32 values of T.
+template <typename T>
+__device__ __forceinline__ T block_sum(T v, T* scratch) {
+  const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+  const int nthr = blockDim.x * blockDim.y * blockDim.z;
+  const int lane = tid & 31, wid = tid >> 5, nw = (nthr + 31) >> 5;
+  v = warp_sum(v);
+  __syncthreads();
+  if (lane == 0) scratch[wid] = v;
+  __syncthreads();
+  T t = (tid < nw) ? scratch[tid] : T(0);
+  if (wid == 0) t = warp_sum(t);
+  if (tid == 0) scratch[0] = t;
+  __syncthreads();
+  t = scratch[0];
+  __syncthreads();
+  return t;
+}
+
+// Scalars of one PCG solve, resident on the device (no host round trip per
+// iteration).  All FP64, whatever the field precision.
+struct CgScalars {
+  double rtz1, rtz2, rho, alpha, beta;
+  double rbn0, rbn2, tol, tin, vol;
+  double s1, s2;
+  int iter;       // iteration index of the last completed convergence check
+  int niter;      // reported iteration count (cggo's niter)
+  int done;       // 1 = converged (or stopped), kernels return immediately
+  int maxiter;    // min(maxit, maxcg)
+  int istep;      // reference istep (for the "at least one iteration" rule)
+  int nonfinite;  // set when a non-finite norm is met
+  unsigned int counter[4];  // last-block tickets, one per reduction site
+};
+
+// Exact-order helpers: products and sums are rounded separately (no fused
+// multiply-add), reproducing an unfused left-to-right evaluation.
+__device__ __forceinline__ double mul_x(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double add_x(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float mul_x(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float add_x(float a, float b) { return __fadd_rn(a, b); }
+
+template <bool EXACT, typename T>
+__device__ __forceinline__ T madd(T a, T b, T c) {  // a*b + c
+  if constexpr (EXACT) return add_x(mul_x(a, b), c);
+  else return fma(a, b, c);
+}
+
+}  // namespace nekgpu

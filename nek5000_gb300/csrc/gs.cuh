@@ -1,0 +1,60 @@
+// gs.cuh -- direct-stiffness summation (gslib gs_setup / gs_op semantics).
+//
+// gs_setup (called from core/dssum.f:20) groups the local copies of every
+// non-zero global id; gs_op(+) (core/dssum.f:79) replaces each copy by the
+// sum over its group.  Ids of 0 (element interiors, core/navier8.f:2317-2346)
+// are never touched.  Here the groups are sorted segments: the (id, local
+// index) pairs sorted by id then index give CSR maps
+//   start[s] .. start[s+1]-1  ->  idx[]  (ascending local index)
+// and one thread owns one segment: gather in ascending index order, reduce,
+// scatter back.  Two map sets are kept:
+//   shared  -- groups with >= 2 copies (what dssum/dsop changes)
+//   bound   -- every non-zero id, singletons included (the PCG form, which
+//              also applies the Dirichlet mask and forms the element-boundary
+//              part of rho = sum w*p*mult there)
+#pragma once
+#include <vector>
+
+#include "common.cuh"
+
+namespace nekgpu {
+
+struct GsMaps {
+  int64_t n = 0;
+  int nseg = 0, nidx = 0;    // shared groups
+  int* start = nullptr;      // device, nseg+1
+  int* idx = nullptr;        // device, nidx
+  int nbseg = 0, nbidx = 0;  // all boundary groups
+  int* bstart = nullptr;
+  int* bidx = nullptr;
+  std::vector<int64_t> h_start, h_idx;  // host copy of the shared maps (export)
+};
+
+// Host: build maps from glo_num (sort by (id, local index)).  Returns 0 or an
+// error code; fills err.
+int gs_setup(GsMaps& gs, const int64_t* glo_num, int64_t n, std::string& err);
+void gs_free(GsMaps& gs);
+
+// u <- gs_op(u, op): op 0 '+', 1 '*', 2 max, 3 min
+template <typename T>
+void gs_op(const GsMaps& gs, T* u, int op, cudaStream_t s);
+
+// PCG form: for every boundary group g, s = mask_g * sum w; w <- s on all
+// copies; rho partial += s * p_g * msum_g.  The last block adds these
+// partials to the interior partials left by the fused axhelm (nA of them)
+// and sets rho, alpha = rtz1/rho.
+template <typename T>
+void gs_cg(const GsMaps& gs, T* w, const T* p, const T* segmask, const double* segmsum,
+           CgScalars* cg, double* partialA, int nA, double* partialB, cudaStream_t s);
+
+// Per-segment mask value (mask at the first copy) and sum of mult over the
+// copies, for the bound maps.  Returns via `nonuniform` (device int) whether
+// any group has copies with different mask values.
+template <typename T>
+void gs_cg_weights(const GsMaps& gs, const T* mask, const T* mult, T* segmask, double* segmsum,
+                   int* nonuniform, cudaStream_t s);
+
+constexpr int kGsThreads = 256;
+inline int gs_cg_blocks(const GsMaps& gs) { return (gs.nbseg + kGsThreads - 1) / kGsThreads; }
+
+}  // namespace nekgpu

@@ -1,0 +1,151 @@
+// impl.cuh -- handle, mesh and solver internals shared by the library's TUs.
+#pragma once
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "axhelm.cuh"
+#include "common.cuh"
+#include "gs.cuh"
+
+namespace nekgpu {
+
+// Device copy of a field buffer, grown on demand.
+template <typename T>
+struct DevBuf {
+  T* ptr = nullptr;
+  size_t cap = 0;
+  cudaError_t ensure(size_t n) {
+    if (n <= cap) return cudaSuccess;
+    cudaFree(ptr);
+    ptr = nullptr;
+    cap = 0;
+    cudaError_t e = cudaMalloc(&ptr, std::max<size_t>(n, 1) * sizeof(T));
+    if (e == cudaSuccess) cap = n;
+    return e;
+  }
+  void release() {
+    cudaFree(ptr);
+    ptr = nullptr;
+    cap = 0;
+  }
+  ~DevBuf() { cudaFree(ptr); }
+};
+
+// Operator data in one precision.
+template <typename T>
+struct OpData {
+  T* G = nullptr;    // [nel][6][P]
+  T* bm1 = nullptr;  // [n]
+  T* D = nullptr;    // [lx1*lx1] row-major
+  void release() {
+    cudaFree(G);
+    cudaFree(bm1);
+    cudaFree(D);
+    G = bm1 = D = nullptr;
+  }
+};
+
+struct Mesh {
+  int nx1 = 0, nel = 0;
+  int64_t n = 0;
+  OpData<double> f64;
+  OpData<float> f32;  // built on first mixed-precision use
+  bool has_f32 = false;
+  GsMaps gs;
+  double vol = 0.0;  // glsum(bm1) (core/coef.f:1181)
+  std::vector<double> h_D;  // lx1*lx1 row-major (host copy)
+};
+
+// Coefficient descriptor after uniformity detection.
+template <typename T>
+struct Coef {
+  int h1mode = 0, h2mode = 0;  // see AxArgs
+  T h1s = T(1), h2s = T(0);
+  const T* h1 = nullptr;
+  const T* h2 = nullptr;
+};
+
+// Work space of one PCG precision.
+template <typename T>
+struct PcgWork {
+  DevBuf<T> r, w, p, d, mult, binv, mask, segmask, x, f, h1, h2;
+  DevBuf<double> segmsum;
+};
+
+struct Handle {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  Mesh mesh;
+  bool has_mesh = false;
+  std::string err;
+  CgScalars* cg = nullptr;       // device
+  CgScalars* cg_host = nullptr;  // pinned mirror
+  DevBuf<double> partialA, partialB, partialC, red;
+  int* flag = nullptr;           // device int scratch
+  PcgWork<double> w64;
+  PcgWork<float> w32;
+  DevBuf<double> io0, io1, io2, io3, io4, io5, io6, io7, io8;  // host-path staging
+  bool exact = false;  // unfused FP64 arithmetic in the reference's order
+  int istep = 0;       // reference time-step index (cggo's "at least one iteration" rule)
+  // timing
+  bool timing = false;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, evt0 = nullptr, evt1 = nullptr;
+  double ms_total = 0.0, ms_axhelm = 0.0;
+  int n_axhelm = 0;
+  // graph cache for the PCG iteration chunk
+  struct GraphKey {
+    const void* x = nullptr;
+    int prec = -1;
+    int h1mode = -1, h2mode = -1;
+    double h1s = 0, h2s = 0;
+    const void* h1 = nullptr;
+    const void* h2 = nullptr;
+    const void* f = nullptr;
+    bool operator==(const GraphKey& o) const {
+      return x == o.x && prec == o.prec && h1mode == o.h1mode && h2mode == o.h2mode &&
+             h1s == o.h1s && h2s == o.h2s && h1 == o.h1 && h2 == o.h2 && f == o.f;
+    }
+  };
+  GraphKey gkey;
+  cudaGraphExec_t gexec = nullptr;
+  int graph_chunk = 16;
+  bool use_graph = true;
+};
+
+// ---- operator entry points (axhelm_*.cu) ---------------------------------
+// Plain operator: au = A u.  Returns cudaError_t of the launch.
+template <typename T, bool EXACT>
+cudaError_t launch_axhelm(const Mesh& m, const OpData<T>& op, T* au, const T* u, const Coef<T>& c,
+                          cudaStream_t s);
+// Fused PCG form (see axhelm.cuh).  Returns number of blocks (partials written).
+template <typename T, bool EXACT>
+cudaError_t launch_axhelm_cg(const Mesh& m, const OpData<T>& op, T* w, T* p, const T* r,
+                             const T* d, const Coef<T>& c, const CgScalars* cg, double* partial,
+                             int* nblocks, cudaStream_t s);
+int axhelm_blocks(int nx1, int nel);
+
+// ---- solver / vector kernels (pcg.cu) ---------------------------------------
+template <typename T>
+int detect_coef(Handle& h, const T* h1, const T* h2, int64_t n, Coef<T>& c);
+template <typename T>
+cudaError_t setprec(Handle& h, const OpData<T>& op, T* d, const Coef<T>& c);
+int setprec_f64(Handle& h, double* d, const Coef<double>& c);
+double device_sum(Handle& h, int kind, const double* a, const double* b, const double* c,
+                  int64_t n, int* status);
+
+struct PcgResult {
+  int niter = 0;
+  double rbn0 = 0, rbn2 = 0;
+  int status = 0;
+};
+
+// cggo on device arrays (f: masked, assembled rhs; x: out).  Precision T.
+template <typename T>
+PcgResult pcg_solve(Handle& h, const OpData<T>& op, PcgWork<T>& wk, T* x, const T* f,
+                    const Coef<T>& c, const T* mask, const T* mult, const T* binv, double tin,
+                    int maxiter, int istep, bool exact);
+
+void set_error(Handle& h, const std::string& msg);
+
+}  // namespace nekgpu

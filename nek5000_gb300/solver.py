@@ -1,0 +1,164 @@
+"""Python front end mirroring the reference's Helmholtz interface.
+
+Method names, argument order and meaning follow the Fortran routines they
+replace (core/hmholtz.f: hmholtz :2, axhelm :72, setprec :380, cggo :611;
+core/dssum.f: dssum :33, dsop :100).  Every call goes through the C ABI of
+libnekgpu.so.  Arrays may be
+
+  * numpy float64 host arrays -> the host entry points (copies inside the call)
+  * torch float64 CUDA tensors -> the *_dev entry points (no copies)
+
+Output arrays are written in place, as the Fortran routines do; the solver
+calls also return (niter, rbn0, rbn2).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _capi
+
+_cdouble = C.c_double
+_cint = C.c_int
+
+
+def _is_dev(a) -> bool:
+    return hasattr(a, "is_cuda") and a.is_cuda
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    if _is_dev(a):
+        if str(a.dtype) != "torch.float64" or not a.is_contiguous():
+            raise TypeError("device arrays must be contiguous torch.float64 CUDA tensors")
+        return C.c_void_p(a.data_ptr())
+    if not isinstance(a, np.ndarray) or a.dtype != np.float64 or not a.flags.c_contiguous:
+        raise TypeError("host arrays must be C-contiguous numpy float64 arrays")
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class NekGpu:
+    """One library handle: one device, one stream, one mesh."""
+
+    def __init__(self, device: int = 0):
+        self._L = _capi.load()
+        self._h = C.c_int64(0)
+        self._check(self._L.nekgpu_init(C.byref(_cint(device)), C.byref(self._h)), orphan=True)
+        self.n = 0
+        self.lx1 = 0
+        self.nel = 0
+
+    # ---- plumbing ---------------------------------------------------------
+    def last_error(self) -> str:
+        buf = C.create_string_buffer(1024)
+        self._L.nekgpu_last_error(C.byref(self._h), buf, C.byref(_cint(1024)))
+        return buf.value.decode(errors="replace")
+
+    def _check(self, rc: int, orphan: bool = False, allow=()):
+        if rc != 0 and rc not in allow:
+            raise _capi.NekGpuError(rc, self.last_error())
+        return rc
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._L.nekgpu_finalize(C.byref(self._h))
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_option(self, key: int, value: int):
+        self._check(self._L.nekgpu_set_option(C.byref(self._h), C.byref(_cint(key)),
+                                              C.byref(_cint(int(value)))))
+
+    def set_exact(self, on: bool = True):
+        """Round every FP64 product and sum separately, in the reference's order."""
+        self.set_option(_capi.OPT_EXACT, int(on))
+
+    def set_timing(self, on: bool = True):
+        self.set_option(_capi.OPT_TIMING, int(on))
+
+    def last_timing(self):
+        t, a, k = _cdouble(0), _cdouble(0), _cint(0)
+        self._check(self._L.nekgpu_last_timing(C.byref(self._h), C.byref(t), C.byref(a),
+                                               C.byref(k)))
+        return t.value, a.value, k.value
+
+    # ---- mesh -------------------------------------------------------------
+    def setup(self, lx1: int, nel: int, D, g, bm1, glo_num):
+        """D: (lx1,lx1) numpy with D[i,j] = dl_j/dr(z_i) (the reference's dxm1);
+        g: (6, n) geometric factors G1..G6; bm1: (n,); glo_num: (n,) int64."""
+        n = lx1 ** 3 * nel
+        D = np.asarray(D, dtype=np.float64)
+        dxm1 = np.ascontiguousarray(D.T)  # Fortran order: dxm1(i,j) at [i + j*lx1]
+        g = np.ascontiguousarray(np.asarray(g, dtype=np.float64).reshape(6, n))
+        bm1 = np.ascontiguousarray(bm1, dtype=np.float64)
+        glo = np.ascontiguousarray(glo_num, dtype=np.int64)
+        if bm1.size != n or glo.size != n:
+            raise ValueError("bm1 / glo_num must have lx1^3*nel entries")
+        gp = [g[q].ctypes.data_as(C.c_void_p) for q in range(6)]
+        self._check(self._L.nekgpu_setup(C.byref(self._h), C.byref(_cint(lx1)),
+                                         C.byref(_cint(nel)), dxm1.ctypes.data_as(C.c_void_p),
+                                         *gp, bm1.ctypes.data_as(C.c_void_p),
+                                         glo.ctypes.data_as(C.c_void_p)))
+        self.n, self.lx1, self.nel = n, lx1, nel
+
+    def gs_maps(self):
+        ns, ni = C.c_int64(0), C.c_int64(0)
+        self._check(self._L.nekgpu_gs_maps(C.byref(self._h), C.byref(ns), C.byref(ni), None, None))
+        start = np.zeros(ns.value + 1, dtype=np.int64)
+        idx = np.zeros(max(ni.value, 1), dtype=np.int64)
+        self._check(self._L.nekgpu_gs_maps(C.byref(self._h), C.byref(ns), C.byref(ni),
+                                           start.ctypes.data_as(C.c_void_p),
+                                           idx.ctypes.data_as(C.c_void_p)))
+        return start, idx[: ni.value]
+
+    # ---- operator ---------------------------------------------------------
+    def axhelm(self, au, u, helm1, helm2, imesh: int = 1, isd: int = 1):
+        fn = self._L.nekgpu_axhelm_dev if _is_dev(u) else self._L.nekgpu_axhelm
+        self._check(fn(C.byref(self._h), _ptr(au), _ptr(u), _ptr(helm1), _ptr(helm2),
+                       C.byref(_cint(imesh)), C.byref(_cint(isd))))
+        return au
+
+    def dssum(self, u):
+        fn = self._L.nekgpu_dssum_dev if _is_dev(u) else self._L.nekgpu_dssum
+        self._check(fn(C.byref(self._h), _ptr(u)))
+        return u
+
+    def dsop(self, u, op: str):
+        if not _is_dev(u):
+            raise TypeError("dsop takes a device array")
+        self._check(self._L.nekgpu_dsop_dev(C.byref(self._h), _ptr(u), op.encode()[:1]))
+        return u
+
+    def setprec(self, dpcm1, helm1, helm2, imsh: int = 1, isd: int = 1):
+        fn = self._L.nekgpu_setprec_dev if _is_dev(dpcm1) else self._L.nekgpu_setprec
+        self._check(fn(C.byref(self._h), _ptr(dpcm1), _ptr(helm1), _ptr(helm2),
+                       C.byref(_cint(imsh)), C.byref(_cint(isd))))
+        return dpcm1
+
+    # ---- solvers ----------------------------------------------------------
+    def _solve(self, fn, a, b, h1, h2, mask, mult, imsh, tol, maxit, isd, binv, maxcg):
+        niter, r0, r2 = _cint(0), _cdouble(0), _cdouble(0)
+        mc = C.byref(_cint(int(maxcg))) if maxcg is not None else None
+        rc = fn(C.byref(self._h), _ptr(a), _ptr(b), _ptr(h1), _ptr(h2), _ptr(mask), _ptr(mult),
+                C.byref(_cint(imsh)), C.byref(_cdouble(tol)), C.byref(_cint(int(maxit))),
+                C.byref(_cint(isd)), _ptr(binv), mc, C.byref(niter), C.byref(r0), C.byref(r2))
+        self._check(rc, allow=(_capi.ENOTCONV,))
+        return niter.value, r0.value, r2.value, rc
+
+    def cggo(self, x, f, h1, h2, mask, mult, imsh, tin, maxit, isd, binv, maxcg=900):
+        """x: out.  Returns (niter, rbn0, rbn2, status)."""
+        fn = self._L.nekgpu_cggo_dev if _is_dev(x) else self._L.nekgpu_cggo
+        return self._solve(fn, x, f, h1, h2, mask, mult, imsh, tin, maxit, isd, binv, maxcg)
+
+    def hmholtz(self, name, u, rhs, h1, h2, mask, mult, imsh, tli, maxit, isd, binv, maxcg=900):
+        """name is accepted for signature parity (the reference uses it only for
+        the pressure branch and log lines).  rhs is dssum'd and masked in place."""
+        del name
+        fn = self._L.nekgpu_hmholtz_dev if _is_dev(u) else self._L.nekgpu_hmholtz
+        return self._solve(fn, u, rhs, h1, h2, mask, mult, imsh, tli, maxit, isd, binv, maxcg)

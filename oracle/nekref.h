@@ -1,0 +1,100 @@
+/*
+ * nekref.h -- CPU oracle for the Nek5000 Helmholtz/Poisson solve path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is a C restatement of the reference
+ * Fortran (Nek5000 core/ *.f files) in the same loop and accumulation order, used
+ * by the test-suite as the parity checker and by bench.py as the timed CPU
+ * baseline.  The product library (nek5000_gb300/csrc) never links, loads or
+ * calls it.
+ *
+ * Array conventions follow the Fortran: every field is (lx1,ly1,lz1,nel)
+ * column-major (x fastest, element slowest), 0-based here.  D(i,j) is stored
+ * d[i + j*nx].  All arithmetic is FP64, compiled with -ffp-contract=off so no
+ * multiply-add is fused (gfortran's default for these loops).
+ */
+#ifndef NEKREF_H
+#define NEKREF_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- spectral library (core/speclib.f) ---------------------------------- */
+void ref_zwgll(double *z, double *w, int np);                          /* ZWGLL  speclib.f:107 */
+void ref_dgll(double *d, double *dt, const double *z, int nz);         /* DGLL   speclib.f:811 */
+
+/* ---- synthetic deformed box (harness input, not on the solve path) ------- */
+/* kx*ky*kz hex elements on the unit cube, element e = ex + kx*(ey + ky*ez).
+ * GLL nodes by the trilinear map, then x -> x + amp*sin(pi x)sin(pi y)sin(pi z)*v.
+ * vertex(8,nel): hypercube-ordered lattice ids, wrapped in y/z when periodic. */
+void ref_box_mesh(int nx1, int kx, int ky, int kz, int periodic_y, int periodic_z,
+                  double amp, const double *v3, double *xm1, double *ym1, double *zm1,
+                  int64_t *vertex);
+
+/* ---- geometry (core/coef.f xyzrst/glmapm1/geodat1) ----------------------- */
+/* g6 holds G1..G6 as six consecutive arrays of n = nx1^3*nel. */
+void ref_geom(int nx1, int nel, const double *xm1, const double *ym1, const double *zm1,
+              double *g6, double *bm1, double *jacm1);
+
+/* ---- global numbering (core/navier8.f setvert3d) ------------------------- */
+void ref_setvert3d(int64_t *glo_num, int64_t *ngv, int nx, int nel, const int64_t *vertex);
+
+/* ---- gather-scatter (gslib gs_setup/gs_op semantics) --------------------- */
+typedef struct ref_gs ref_gs;
+ref_gs *ref_gs_setup(const int64_t *glo_num, int64_t n);
+void ref_gs_free(ref_gs *gs);
+/* op: 0 '+', 1 '*', 2 'M' (max), 3 'm' (min) */
+void ref_gs_op(const ref_gs *gs, double *u, int op);
+/* number of shared groups / total members in them; fills CSR maps when non-null */
+int64_t ref_gs_nseg(const ref_gs *gs);
+int64_t ref_gs_nidx(const ref_gs *gs);
+void ref_gs_maps(const ref_gs *gs, int64_t *seg_start, int64_t *idx, int64_t *seg_id);
+
+/* ---- operator state ------------------------------------------------------ */
+typedef struct ref_ops ref_ops;
+/* Pointers are borrowed (caller keeps them alive).  d/dt: D and D^T. */
+ref_ops *ref_ops_create(int nx1, int nel, const double *d, const double *dt,
+                        const double *g6, const double *bm1, const int64_t *glo_num,
+                        int nthreads);
+void ref_ops_free(ref_ops *ops);
+const ref_gs *ref_ops_gs(const ref_ops *ops);
+
+void ref_axhelm(const ref_ops *ops, double *au, const double *u, const double *h1,
+                const double *h2);                                   /* hmholtz.f:72  */
+void ref_dssum(const ref_ops *ops, double *u);                       /* dssum.f:33    */
+void ref_dsop(const ref_ops *ops, double *u, int op);                 /* dssum.f:100   */
+void ref_setprec(const ref_ops *ops, double *d, const double *h1, const double *h2); /* :380 */
+double ref_glsc3(const ref_ops *ops, const double *a, const double *b, const double *m);
+void ref_chktcg1(const ref_ops *ops, double *tol, const double *res, const double *h1,
+                 const double *h2, const double *mask, const double *mult,
+                 const double *binv);                                /* hmholtz.f:527 */
+/* cggo (hmholtz.f:611).  maxcg = the reference's 900 cap (pass a large value
+ * to lift it).  istep feeds the "take at least one iteration" rule.
+ * Returns niter; rbn0/rbn2 out. */
+int ref_cggo(const ref_ops *ops, double *x, const double *f, const double *h1,
+             const double *h2, const double *mask, const double *mult, double tin,
+             int maxit, int maxcg, int istep, const double *binv, double *rbn0,
+             double *rbn2);
+/* hmholtz (hmholtz.f:2): dssum+mask the rhs (in place), chktcg1, cggo. */
+int ref_hmholtz(const ref_ops *ops, double *u, double *rhs, const double *h1,
+                const double *h2, const double *mask, const double *mult, double tli,
+                int maxit, int maxcg, int istep, const double *binv, double *rbn0,
+                double *rbn2);
+
+/* local_grad3 (navier5.f:428) / local_grad3_t (navier1.f:4669), one element */
+void ref_local_grad3(double *ur, double *us, double *ut, const double *u, int N,
+                     const double *d, const double *dt);
+void ref_local_grad3_t(double *u, const double *ur, const double *us, const double *ut,
+                       int N, const double *d, const double *dt, double *w);
+
+/* mxm (mxm_wrapper.f:1 -> mxf<n2>): c(n1,n3) = a(n1,n2) b(n2,n3) */
+void ref_mxm(const double *a, int n1, const double *b, int n2, double *c, int n3);
+
+/* threads actually used by the OpenMP loops (1 without OpenMP) */
+int ref_max_threads(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,303 @@
+"""ctypes front end of the CPU oracle (oracle/nekref.c).
+
+TEST INFRASTRUCTURE ONLY.  The parity tests, ``__graft_entry__.smoke()`` and
+the CPU-baseline leg of ``bench.py`` import this module as the checker / the
+timed CPU restatement of the reference.  The product package
+(``nek5000_gb300``) never imports it.
+
+Every routine mirrors one reference routine; see nekref.c for the file:line
+citations.  Arrays are numpy float64 / int64 in the reference's element-major
+layout (lx1, ly1, lz1, nel) flattened with x fastest.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "libnekref.so")
+_lock = threading.Lock()
+_lib = None
+
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_ip = np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")
+_vp = C.c_void_p
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with its Makefile (gcc, OpenMP, -ffp-contract=off)."""
+    src = os.path.join(_HERE, "nekref.c")
+    if force or not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < os.path.getmtime(src):
+        subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    with _lock:
+        if _lib is None:
+            build()
+            L = C.CDLL(_LIB_PATH)
+            L.ref_zwgll.argtypes = [_dp, _dp, C.c_int]
+            L.ref_dgll.argtypes = [_dp, _dp, _dp, C.c_int]
+            L.ref_box_mesh.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                       C.c_double, _dp, _dp, _dp, _dp, _ip]
+            L.ref_geom.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp]
+            L.ref_setvert3d.argtypes = [_ip, C.POINTER(C.c_int64), C.c_int, C.c_int, _ip]
+            L.ref_gs_setup.argtypes = [_ip, C.c_int64]
+            L.ref_gs_setup.restype = _vp
+            L.ref_gs_free.argtypes = [_vp]
+            L.ref_gs_op.argtypes = [_vp, _dp, C.c_int]
+            L.ref_gs_nseg.argtypes = [_vp]
+            L.ref_gs_nseg.restype = C.c_int64
+            L.ref_gs_nidx.argtypes = [_vp]
+            L.ref_gs_nidx.restype = C.c_int64
+            L.ref_gs_maps.argtypes = [_vp, _ip, _ip, _ip]
+            L.ref_ops_create.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp, _dp, _ip, C.c_int]
+            L.ref_ops_create.restype = _vp
+            L.ref_ops_free.argtypes = [_vp]
+            L.ref_ops_gs.argtypes = [_vp]
+            L.ref_ops_gs.restype = _vp
+            L.ref_axhelm.argtypes = [_vp, _dp, _dp, _dp, _dp]
+            L.ref_dssum.argtypes = [_vp, _dp]
+            L.ref_dsop.argtypes = [_vp, _dp, C.c_int]
+            L.ref_setprec.argtypes = [_vp, _dp, _dp, _dp]
+            L.ref_glsc3.argtypes = [_vp, _dp, _dp, _dp]
+            L.ref_glsc3.restype = C.c_double
+            L.ref_chktcg1.argtypes = [_vp, C.POINTER(C.c_double), _dp, _dp, _dp, _dp, _dp, _dp]
+            L.ref_cggo.argtypes = [_vp, _dp, _dp, _dp, _dp, _dp, _dp, C.c_double, C.c_int, C.c_int,
+                                   C.c_int, _dp, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+            L.ref_cggo.restype = C.c_int
+            L.ref_hmholtz.argtypes = [_vp, _dp, _dp, _dp, _dp, _dp, _dp, C.c_double, C.c_int,
+                                      C.c_int, C.c_int, _dp, C.POINTER(C.c_double),
+                                      C.POINTER(C.c_double)]
+            L.ref_hmholtz.restype = C.c_int
+            L.ref_local_grad3.argtypes = [_dp, _dp, _dp, _dp, C.c_int, _dp, _dp]
+            L.ref_local_grad3_t.argtypes = [_dp, _dp, _dp, _dp, C.c_int, _dp, _dp, _dp]
+            L.ref_mxm.argtypes = [_dp, C.c_int, _dp, C.c_int, _dp, C.c_int]
+            L.ref_max_threads.restype = C.c_int
+            _lib = L
+    return _lib
+
+
+def _c(a, dt=np.float64):
+    return np.ascontiguousarray(a, dtype=dt)
+
+
+# ---- spectral library -------------------------------------------------------
+def zwgll(np_: int):
+    z = np.zeros(np_)
+    w = np.zeros(np_)
+    lib().ref_zwgll(z, w, np_)
+    return z, w
+
+
+def dgll(z):
+    nz = len(z)
+    d = np.zeros(nz * nz)
+    dt = np.zeros(nz * nz)
+    lib().ref_dgll(d, dt, _c(z), nz)
+    # Fortran D(i,j) = d[i + j*nz]  ->  numpy D[i, j]
+    return d.reshape(nz, nz).T.copy(), dt.reshape(nz, nz).T.copy()
+
+
+def mxm(a, b):
+    """C = A B with the reference's mxf<n> left-to-right sums (2-D numpy in)."""
+    n1, n2 = a.shape
+    n3 = b.shape[1]
+    c = np.zeros(n1 * n3)
+    lib().ref_mxm(_c(a.T.ravel()), n1, _c(b.T.ravel()), n2, c, n3)
+    return c.reshape(n3, n1).T
+
+
+# ---- mesh / geometry / numbering -------------------------------------------
+def box_mesh(nx1, kx, ky, kz, periodic=(False, False, False), amp=0.05, v=(0.0, 0.0, 1.0)):
+    nel = kx * ky * kz
+    n = nx1 ** 3 * nel
+    x = np.zeros(n)
+    y = np.zeros(n)
+    z = np.zeros(n)
+    vert = np.zeros(8 * nel, dtype=np.int64)
+    if periodic[0]:
+        raise ValueError("periodic x is not supported by the box mesher")
+    lib().ref_box_mesh(nx1, kx, ky, kz, int(periodic[1]), int(periodic[2]), float(amp),
+                       _c(v), x, y, z, vert)
+    return x, y, z, vert
+
+
+def geom(nx1, nel, x, y, z):
+    n = nx1 ** 3 * nel
+    g = np.zeros(6 * n)
+    bm1 = np.zeros(n)
+    jac = np.zeros(n)
+    lib().ref_geom(nx1, nel, _c(x), _c(y), _c(z), g, bm1, jac)
+    return g.reshape(6, n), bm1, jac
+
+
+def setvert3d(nx, nel, vertex):
+    glo = np.zeros(nx ** 3 * nel, dtype=np.int64)
+    ngv = C.c_int64(0)
+    lib().ref_setvert3d(glo, C.byref(ngv), nx, nel, _c(vertex, np.int64))
+    return glo, int(ngv.value)
+
+
+class GS:
+    """gs_setup / gs_op semantics; maps exported for bit-exact comparison."""
+
+    def __init__(self, glo_num):
+        self._glo = _c(glo_num, np.int64)
+        self.h = lib().ref_gs_setup(self._glo, len(self._glo))
+
+    def op(self, u, op="+"):
+        lib().ref_gs_op(self.h, u, {"+": 0, "*": 1, "M": 2, "m": 3}[op])
+
+    def maps(self):
+        L = lib()
+        ns, ni = L.ref_gs_nseg(self.h), L.ref_gs_nidx(self.h)
+        start = np.zeros(ns + 1, dtype=np.int64)
+        idx = np.zeros(max(ni, 1), dtype=np.int64)
+        ids = np.zeros(max(ns, 1), dtype=np.int64)
+        L.ref_gs_maps(self.h, start, idx, ids)
+        return start, idx[:ni], ids[:ns]
+
+    def __del__(self):
+        try:
+            lib().ref_gs_free(self.h)
+        except Exception:
+            pass
+
+
+class Ops:
+    """Operator state for axhelm / dssum / setprec / cggo (borrowed arrays kept alive)."""
+
+    def __init__(self, nx1, nel, D, g, bm1, glo_num, nthreads=1):
+        self.nx1, self.nel = nx1, nel
+        self.n = nx1 ** 3 * nel
+        self._d = _c(D.T.ravel())      # Fortran order D(i,j) at [i + j*nx]
+        self._dt = _c(D.ravel())       # D^T in Fortran order
+        self._g = _c(g.reshape(-1))
+        self._bm1 = _c(bm1)
+        self._glo = _c(glo_num, np.int64)
+        self.nthreads = nthreads
+        self.h = lib().ref_ops_create(nx1, nel, self._d, self._dt, self._g, self._bm1, self._glo,
+                                      int(nthreads))
+
+    def __del__(self):
+        try:
+            lib().ref_ops_free(self.h)
+        except Exception:
+            pass
+
+    def axhelm(self, u, h1, h2):
+        au = np.zeros(self.n)
+        lib().ref_axhelm(self.h, au, _c(u), _c(h1), _c(h2))
+        return au
+
+    def dssum(self, u):
+        u = np.array(u, dtype=np.float64, copy=True)
+        lib().ref_dssum(self.h, u)
+        return u
+
+    def dsop(self, u, op):
+        u = np.array(u, dtype=np.float64, copy=True)
+        lib().ref_dsop(self.h, u, {"+": 0, "*": 1, "M": 2, "m": 3}[op])
+        return u
+
+    def setprec(self, h1, h2):
+        d = np.zeros(self.n)
+        lib().ref_setprec(self.h, d, _c(h1), _c(h2))
+        return d
+
+    def glsc3(self, a, b, m):
+        return lib().ref_glsc3(self.h, _c(a), _c(b), _c(m))
+
+    def chktcg1(self, tol, res, h1, h2, mask, mult, binv):
+        t = C.c_double(tol)
+        lib().ref_chktcg1(self.h, C.byref(t), _c(res), _c(h1), _c(h2), _c(mask), _c(mult), _c(binv))
+        return t.value
+
+    def cggo(self, f, h1, h2, mask, mult, binv, tin, maxit=10 ** 9, maxcg=900, istep=0):
+        x = np.zeros(self.n)
+        r0, r2 = C.c_double(0), C.c_double(0)
+        it = lib().ref_cggo(self.h, x, _c(f), _c(h1), _c(h2), _c(mask), _c(mult), float(tin),
+                            int(min(maxit, 2 ** 31 - 1)), int(min(maxcg, 2 ** 31 - 1)), int(istep),
+                            _c(binv), C.byref(r0), C.byref(r2))
+        return x, it, r0.value, r2.value
+
+    def hmholtz(self, rhs, h1, h2, mask, mult, binv, tli, maxit=10 ** 9, maxcg=900, istep=0):
+        """Returns (u, rhs_after_dssum_mask, niter, rbn0, rbn2)."""
+        u = np.zeros(self.n)
+        rhs = np.array(rhs, dtype=np.float64, copy=True)
+        r0, r2 = C.c_double(0), C.c_double(0)
+        it = lib().ref_hmholtz(self.h, u, rhs, _c(h1), _c(h2), _c(mask), _c(mult), float(tli),
+                               int(min(maxit, 2 ** 31 - 1)), int(min(maxcg, 2 ** 31 - 1)),
+                               int(istep), _c(binv), C.byref(r0), C.byref(r2))
+        return u, rhs, it, r0.value, r2.value
+
+
+def local_grad3(u, D):
+    N = D.shape[0] - 1
+    m3 = (N + 1) ** 3
+    ur, us, ut = np.zeros(m3), np.zeros(m3), np.zeros(m3)
+    lib().ref_local_grad3(ur, us, ut, _c(u), N, _c(D.T.ravel()), _c(D.ravel()))
+    return ur, us, ut
+
+
+def local_grad3_t(ur, us, ut, D):
+    N = D.shape[0] - 1
+    m3 = (N + 1) ** 3
+    u, w = np.zeros(m3), np.zeros(m3)
+    lib().ref_local_grad3_t(u, _c(ur), _c(us), _c(ut), N, _c(D.T.ravel()), _c(D.ravel()), w)
+    return u
+
+
+def max_threads():
+    return lib().ref_max_threads()
+
+
+# ---- problem assembly (what Nek's setup produces for a box case) ------------
+def box_problem(nx1, kx, ky, kz, periodic=(False, False, False), dirichlet=None, amp=0.05,
+                v=(0.0, 0.0, 1.0), nthreads=1):
+    """Mesh + geometry + numbering + masks + multiplicity + inverse mass.
+
+    dirichlet: 6 flags for the domain faces (x-, x+, y-, y+, z-, z+); default:
+    every non-periodic face.  The mask follows bcmask (bdry.f:317): zero on
+    Dirichlet faces (facev) then dsop 'MUL'.  vmult = 1/dssum(1)
+    (connect1.f:126-135), binvm1 = 1/dssum(bm1) (coef.f:1500-1545).
+    """
+    nel = kx * ky * kz
+    nxyz = nx1 ** 3
+    n = nxyz * nel
+    x, y, z, vert = box_mesh(nx1, kx, ky, kz, periodic, amp, v)
+    g, bm1, jac = geom(nx1, nel, x, y, z)
+    glo, ngv = setvert3d(nx1, nel, vert)
+    z1, w1 = zwgll(nx1)
+    D, DT = dgll(z1)
+    ops = Ops(nx1, nel, D, g, bm1, glo, nthreads)
+    if dirichlet is None:
+        dirichlet = (not periodic[0],) * 2 + (not periodic[1],) * 2 + (not periodic[2],) * 2
+    mask = np.ones((nel, nx1, nx1, nx1))  # [e, iz, iy, ix]
+    e = np.arange(nel)
+    ex, ey, ez = e % kx, (e // kx) % ky, e // (kx * ky)
+    if dirichlet[0]:
+        mask[ex == 0, :, :, 0] = 0.0
+    if dirichlet[1]:
+        mask[ex == kx - 1, :, :, -1] = 0.0
+    if dirichlet[2]:
+        mask[ey == 0, :, 0, :] = 0.0
+    if dirichlet[3]:
+        mask[ey == ky - 1, :, -1, :] = 0.0
+    if dirichlet[4]:
+        mask[ez == 0, 0, :, :] = 0.0
+    if dirichlet[5]:
+        mask[ez == kz - 1, -1, :, :] = 0.0
+    mask = ops.dsop(mask.reshape(-1), "*")
+    mult = 1.0 / ops.dssum(np.ones(n))
+    binv = 1.0 / ops.dssum(bm1)
+    return dict(nx1=nx1, nel=nel, n=n, kx=kx, ky=ky, kz=kz, x=x, y=y, z=z, vertex=vert, g=g,
+                bm1=bm1, jac=jac, glo_num=glo, ngv=ngv, zgll=z1, wgll=w1, D=D, mask=mask,
+                mult=mult, binv=binv, ops=ops)

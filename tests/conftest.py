@@ -1,0 +1,38 @@
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300) and the built libnekgpu.so")
+
+
+@pytest.fixture(scope="session")
+def oracle():
+    from oracle import nekref
+    nekref.build()
+    return nekref
+
+
+def rng_unit_vector(seed):
+    r = np.random.default_rng(seed)
+    v = r.standard_normal(3)
+    return v / np.linalg.norm(v)
+
+
+@pytest.fixture(scope="session")
+def gpu_lib():
+    """Build (if needed) and load libnekgpu.so; skip when no GPU is visible."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from nek5000_gb300 import build
+    build.build()
+    from nek5000_gb300 import NekGpu
+    return NekGpu

@@ -1,0 +1,55 @@
+"""The C ABI library: builds, loads without a GPU, exports every declared symbol,
+and reports errors by status code (no GPU compute is called here)."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    src = open(os.path.join(ROOT, "include", "nekgpu.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\bint\s+(nekgpu_\w+)\s*\(", src)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from nek5000_gb300 import _capi, build
+    build.build()
+    return _capi.load()
+
+
+def test_header_declares_the_reference_boundary():
+    syms = declared_symbols()
+    for must in ("nekgpu_axhelm", "nekgpu_dssum", "nekgpu_setprec", "nekgpu_cggo", "nekgpu_hmholtz",
+                 "nekgpu_setup", "nekgpu_init", "nekgpu_finalize"):
+        assert must in syms
+
+
+def test_library_exports_every_declared_symbol(lib):
+    from nek5000_gb300 import _capi
+    for s in declared_symbols():
+        assert hasattr(lib, s), s
+        assert s in _capi.SIGNATURES, f"{s} has no ctypes signature"
+
+
+def test_bad_handle_is_an_error_code(lib):
+    h = C.c_int64(987654)
+    out = C.c_double(0)
+    rc = lib.nekgpu_dssum(C.byref(h), C.c_void_p(C.addressof(out)))
+    assert rc == -2  # NEKGPU_EHANDLE
+    buf = C.create_string_buffer(256)
+    assert lib.nekgpu_last_error(C.byref(h), buf, C.byref(C.c_int(256))) == 0
+    assert b"handle" in buf.value
+
+
+def test_init_without_gpu_fails_cleanly(lib):
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    h = C.c_int64(0)
+    rc = lib.nekgpu_init(C.byref(C.c_int(0)), C.byref(h))
+    assert rc in (-3, -1)
