@@ -1,0 +1,340 @@
+#!/usr/bin/env python
+"""Benchmark of the Helmholtz Jacobi-PCG solve path on one GB300 (or N replicas).
+
+Workload (the Helmholtz configuration on one GPU): a 32x32x32 = 32768-element
+deformed box, N = 7 (lx1 = 8, 16.8 M element-local points), deformation
+x -> x + 0.05 sin(pi x) sin(pi y) sin(pi z) v with a unit vector v from seed 1,
+Dirichlet on the x faces and periodic in y and z, h1 = 1, h2 = 10, right-hand
+side B f with f standard normal per global node (seed 1), Jacobi-PCG to a
+relative residual of 1e-10 (the reference's cggo norm and stopping rule, the
+900-iteration cap lifted).
+
+A step is one complete solve.  `value` is DOF-iterations/s = n * iterations /
+solve time over the K timed steps, with every input resident in HBM (the
+device entry point nekgpu_cggo_dev).  `e2e` is the same metric through the
+host entry point nekgpu_hmholtz: rhs, h1, h2, mask, mult and binv copied in
+from pinned host memory and u, rhs copied out inside each timed call.
+
+--impl reference times the CPU restatement of the reference (the oracle, all
+host threads) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "DOF-iters/s, E=32^3 N=7 PCG to 1e-10: mixed vs FP64; axhelm HBM GB/s"
+FALLBACK_HBM_GBS = 6800.0
+FP64_PEAK_TFLOPS = 1.0  # measured FMA-chain rate on this GB300 (profiles/gb300_fp_rates.md)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--k", type=int, default=32, help="elements per direction")
+    ap.add_argument("--N", type=int, default=7, help="polynomial order")
+    ap.add_argument("--tol", type=float, default=1e-10)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-iters", type=int, default=0, help="oracle PCG iterations per sample")
+    return ap.parse_args()
+
+
+def workload(k, N):
+    from nek5000_gb300 import mesh
+    M = mesh.box_mesh(N, k, k, k, periodic=(False, True, True),
+                      dirichlet=(True, True, False, False, False, False), seed=1)
+    rng = np.random.default_rng(1)
+    nglob = int(M["lattice"].max()) + 1
+    f = rng.standard_normal(nglob)[M["lattice"]]
+    M["rhs"] = M["bm1"] * f
+    # assembled, masked right-hand side (what hmholtz hands to cggo)
+    M["f"] = mesh.dssum_host(M["lattice"], M["rhs"], nglob) * M["mask"]
+    M["h1"] = np.ones(M["n"])
+    M["h2"] = np.full(M["n"], 10.0)
+    return M
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "of measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "of fallback"
+
+
+def ncu_traffic(kernel_key):
+    """dram bytes per launch for the dominant kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    try:
+        d = json.load(open(p))
+        return d.get(kernel_key)
+    except Exception:
+        return None
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.out = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.out.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.out:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup(n_gpus):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if ws > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo")
+        pg = dist
+    return ws, rank, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def allmax(pg, v):
+    if pg is None:
+        return v
+    import torch
+    t = torch.tensor([float(v)])
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def allsum(pg, v):
+    if pg is None:
+        return v
+    import torch
+    t = torch.tensor([float(v)])
+    pg.all_reduce(t)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------
+def cpu_sample(M, nthreads, iters):
+    """Oracle (CPU restatement of the reference) PCG iterations on the full problem."""
+    from oracle import nekref
+    ops = nekref.Ops(M["lx1"], M["nel"], M["D"], M["g"], M["bm1"], M["glo_num"], nthreads)
+    t0 = time.perf_counter()
+    x, it, r0, r2 = ops.cggo(M["f"], M["h1"], M["h2"], M["mask"], M["mult"], M["binv"], -1e-30,
+                             maxcg=iters)
+    dt = time.perf_counter() - t0
+    return M["n"] * it / dt, it, dt
+
+
+def run_reference(args):
+    ws, rank, local, pg = dist_setup(args.gpus)
+    if rank != 0:
+        return
+    M = workload(args.k, args.N)
+    nth = os.cpu_count() or 1
+    iters = args.cpu_iters or 10
+    for _ in range(args.warmup):
+        cpu_sample(M, nth, max(2, iters // 5))
+    vals, times = [], []
+    for _ in range(args.steps):
+        v, it, dt = cpu_sample(M, nth, iters)
+        vals.append(v)
+        times.append(dt)
+    value = M["n"] * iters * len(times) / sum(times)
+    sample = (f"{iters} Jacobi-PCG iterations (cggo restated in C, FP64) on the full "
+              f"E={args.k}^3 N={args.N} problem per step")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "DOF-iters/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"helmholtz E={args.k}^3 N={args.N} h1=1 h2=10 "
+                                   "dirichlet-x periodic-yz", "n_points": M["n"]},
+            "cpu_baseline": {"value": value, "unit": "DOF-iters/s", "cores": nth, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": "DOF-iters/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args):
+    import torch
+    ws, rank, local, pg = dist_setup(args.gpus)
+    torch.cuda.set_device(local)
+    from nek5000_gb300 import NekGpu
+    from nek5000_gb300 import build as nb
+    nb.build()
+    M = workload(args.k, args.N)
+    n = M["n"]
+    lib = NekGpu(local)
+    lib.setup(M["lx1"], M["nel"], M["D"], M["g"], M["bm1"], M["glo_num"])
+    dev = lambda a: torch.tensor(a, device=f"cuda:{local}")
+    f, h1, h2 = dev(M["f"]), dev(M["h1"]), dev(M["h2"])
+    mask, mult, binv = dev(M["mask"]), dev(M["mult"]), dev(M["binv"])
+    x = torch.zeros(n, dtype=torch.float64, device=f"cuda:{local}")
+    big = 10 ** 6
+
+    def solve():
+        return lib.cggo(x, f, h1, h2, mask, mult, 1, -args.tol, big, 1, binv, maxcg=big)
+
+    lib.set_option(2, 1)  # timing: solve-total and per-launch operator events
+    for _ in range(args.warmup):
+        solve()
+    barrier(pg)
+    torch.cuda.synchronize()
+    l0 = lib.launch_count()
+    iters, ms_tot, ms_ax, n_ax = [], 0.0, 0.0, 0
+    with Clocks(local) as ck:
+        for _ in range(args.steps):
+            it, r0, r2, rc = solve()
+            t_tot, t_ax, k_ax = lib.last_timing()
+            iters.append(it)
+            ms_tot += t_tot
+            ms_ax += t_ax
+            n_ax += k_ax
+    torch.cuda.synchronize()
+    barrier(pg)
+    launches = lib.launch_count() - l0
+    T = allmax(pg, ms_tot / 1e3)
+    dof_iters = n * sum(iters)
+    value = allsum(pg, dof_iters) / T
+    # dominant kernel: fused operator (p-update + axhelm), FP64, Helmholtz
+    w = 8
+    bytes_per_pt = w * (3 + 6 + 1 + 2)  # r, d, p_old, G1..G6, bm1 in; p, w out
+    ax_ms = ms_ax / max(n_ax, 1)
+    achieved = bytes_per_pt * n / (ax_ms * 1e-3) / 1e9
+    peak, peak_src = peaks()
+    flops_pt = 12 * M["lx1"] + 20 + 3 + 2
+    clk = ck.summary()
+    line = {"metric": METRIC, "value": value, "unit": "DOF-iters/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_tot / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": f"helmholtz E={args.k}^3 N={args.N} h1=1 h2=10 "
+                                   "dirichlet-x periodic-yz", "n_points": n,
+                       "solver": "jacobi-pcg fp64 (fused 3-kernel iteration)",
+                       "tol": args.tol, "iterations": iters, "l2": "inputs larger than L2",
+                       "parallelism": f"replicas{ws}"},
+            "roofline": {"kernel": "axhelm_kernel<8,double,fused>", "bound": "hbm",
+                         "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_source": peak_src,
+                         "bytes_per_point": bytes_per_pt, "avg_launch_ms": ax_ms,
+                         "launches_timed": n_ax,
+                         "traffic": ncu_traffic("axhelm_fused_f64_n7"),
+                         "fp64_alu": {"achieved_tflops": flops_pt * n / (ax_ms * 1e-3) / 1e12,
+                                      "peak_tflops": FP64_PEAK_TFLOPS,
+                                      "frac": flops_pt * n / (ax_ms * 1e-3) / 1e12 / FP64_PEAK_TFLOPS}},
+            "gpu_launches": launches,
+            "clocks": clk}
+    # ---- end to end through the host entry point ------------------------------
+    if not args.no_e2e:
+        pin = lambda a: torch.tensor(a).pin_memory().numpy()
+        rhs0 = pin(M["rhs"])
+        hb = {k: pin(M[k]) for k in ("h1", "h2", "mask", "mult", "binv")}
+        rhs = pin(M["rhs"])
+        u = pin(np.zeros(n))
+        lib.hmholtz("TEMP", u, rhs, hb["h1"], hb["h2"], hb["mask"], hb["mult"], 1, -args.tol, big,
+                    1, hb["binv"], maxcg=big)  # warm the staging buffers
+        e_tot, e_it = 0.0, 0
+        barrier(pg)
+        for _ in range(args.steps):
+            np.copyto(rhs, rhs0)
+            t0 = time.perf_counter()
+            it, r0, r2, rc = lib.hmholtz("TEMP", u, rhs, hb["h1"], hb["h2"], hb["mask"], hb["mult"],
+                                         1, -args.tol, big, 1, hb["binv"], maxcg=big)
+            e_tot += time.perf_counter() - t0
+            e_it += it
+        barrier(pg)
+        e_T = allmax(pg, e_tot)
+        line["e2e"] = {"value": allsum(pg, n * e_it) / e_T, "unit": "DOF-iters/s",
+                       "h2d_bytes_per_step": 6 * 8 * n, "d2h_bytes_per_step": 2 * 8 * n,
+                       "api": "nekgpu_hmholtz (host arrays, pinned)"}
+    # ---- CPU baseline (oracle) on rank 0, N=1 only -------------------------------
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        nth = os.cpu_count() or 1
+        iters_cpu = args.cpu_iters or 10
+        v, it, dt = cpu_sample(M, nth, iters_cpu)
+        line["cpu_baseline"] = {"value": v, "unit": "DOF-iters/s", "cores": nth, "kind": "port",
+                                "sample": f"{it} Jacobi-PCG iterations of the full problem, "
+                                          f"{dt:.1f} s, C restatement of the reference (FP64)"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    lib.close()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

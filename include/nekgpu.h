@@ -142,6 +142,8 @@ int nekgpu_hmholtz_dev(const int64_t *handle, double *u, double *rhs, const doub
 int nekgpu_set_timing(const int64_t *handle, const int *on);
 int nekgpu_last_timing(const int64_t *handle, double *ms_total, double *ms_axhelm,
                        int *n_axhelm);
+/* Kernels this library has launched in the process so far (all handles). */
+int nekgpu_launch_count(int64_t *count);
 
 #ifdef __cplusplus
 }

@@ -51,6 +51,7 @@ SIGNATURES = {
                            _DP],
     "nekgpu_set_timing": [_I64P, _IP],
     "nekgpu_last_timing": [_I64P, _DP, _DP, _IP],
+    "nekgpu_launch_count": [_I64P],
 }
 
 _lib = None

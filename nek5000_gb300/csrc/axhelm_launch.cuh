@@ -20,6 +20,7 @@ static cudaError_t launch_ax_nx(const Mesh& m, const AxArgs<T>& a, int* nblocks,
   const int nb = (m.nel + epb - 1) / epb;
   if (nblocks) *nblocks = nb;
   dim3 block(NX * NX, epb);
+  count_launch();
   axhelm_kernel<NX, T, EXACT, FUSED><<<nb, block, smem, s>>>(a);
   return cudaGetLastError();
 }

@@ -121,6 +121,7 @@ int chktcg1_dev(Handle* H, double* tol, const double* res, const Coef<double>& c
   DevBuf<double>& w1 = H->io5;
   DevBuf<double>& w2 = H->io6;
   if (w1.ensure(n) || w2.ensure(n)) return fail(H, NEKGPU_ENOMEM, "chktcg1: allocation failed");
+  count_launch();
   fill_kernel<<<nblk(n), 256, 0, H->stream>>>(w1.ptr, 1.0, n);
   int rc = axhelm_dev(H, w2.ptr, w1.ptr, c);
   if (rc) return rc;
@@ -145,13 +146,8 @@ int cggo_dev(Handle* H, double* x, const double* f, const double* h1, const doub
   // correction of hmholtz.f:705-750, which this solver does not provide
   int st = 0;
   if (c.h2mode == 0) {
-    DevBuf<double> tmp;
-    const int64_t n = H->mesh.n;
-    if (tmp.ensure(n)) return fail(H, NEKGPU_ENOMEM, "allocation failed");
-    // min(mask) > 0  <=>  max(1 - mask) < 1 ; use max|mask - 1| via kind 3 on (1-mask)
-    cudaMemcpyAsync(tmp.ptr, mask, n * sizeof(double), cudaMemcpyDeviceToDevice, H->stream);
-    const double mmax = device_sum(*H, 6, tmp.ptr, nullptr, nullptr, n, &st);  // min(mask)
-    if (!st && mmax > 0.0)
+    const double skmin = device_sum(*H, 6, mask, nullptr, nullptr, H->mesh.n, &st);  // glmin(mask)
+    if (!st && skmin > 0.0)
       return fail(H, NEKGPU_EINVAL,
                   "cggo: singular operator (no Dirichlet point and h2 = 0) is not supported");
   }
@@ -173,6 +169,7 @@ int hmholtz_dev(Handle* H, double* u, double* rhs, const double* h1, const doubl
   const int64_t n = H->mesh.n;
   double tol = std::fabs(tli);
   gs_op<double>(H->mesh.gs, rhs, 0, H->stream);                       // dssum(rhs)
+  count_launch();
   mul_kernel<<<nblk(n), 256, 0, H->stream>>>(rhs, mask, n);           // col2(rhs,mask)
   Coef<double> c;
   int rc = make_coef(H, h1, h2, c);
@@ -310,6 +307,7 @@ int nekgpu_setup(const int64_t* handle, const int* lx1, const int* nel, const do
     if ((e = cudaMemcpy(stage.ptr, gs6[q], n * sizeof(double), cudaMemcpyHostToDevice)) !=
         cudaSuccess)
       return cuda_fail(H, e, "geometry upload");
+    count_launch();
     pack_g_kernel<<<nblk(n), 256, 0, 0>>>(m.f64.G, stage.ptr, q, P, n);
     if ((e = cudaDeviceSynchronize()) != cudaSuccess) return cuda_fail(H, e, "geometry pack");
   }
@@ -540,6 +538,12 @@ int nekgpu_hmholtz(const int64_t* handle, double* u, double* rhs, const double* 
   int rc2 = d2h(H, u, H->io3.ptr, n);
   if (!rc2) rc2 = d2h(H, rhs, H->io0.ptr, n);
   return rc2 ? rc2 : rc;
+}
+
+int nekgpu_launch_count(int64_t* count) {
+  if (!count) return NEKGPU_EINVAL;
+  *count = (int64_t)launch_counter().load();
+  return NEKGPU_OK;
 }
 
 int nekgpu_set_timing(const int64_t* handle, const int* on) {

@@ -10,11 +10,19 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <string>
 
 namespace nekgpu {
 
 constexpr int kMaxLx1 = 12;
+
+// Process-wide count of kernel launches made by this library.
+inline std::atomic<long long>& launch_counter() {
+  static std::atomic<long long> c{0};
+  return c;
+}
+inline void count_launch() { launch_counter().fetch_add(1, std::memory_order_relaxed); }
 
 // ---- reductions: deterministic (fixed tree, no floating-point atomics) ----
 template <typename T>

@@ -155,6 +155,7 @@ void gs_free(GsMaps& gs) {
 template <typename T>
 void gs_op(const GsMaps& gs, T* u, int op, cudaStream_t s) {
   if (gs.nseg == 0) return;
+  count_launch();
   gs_op_kernel<T><<<(gs.nseg + kGsThreads - 1) / kGsThreads, kGsThreads, 0, s>>>(
       u, gs.start, gs.idx, gs.nseg, op);
 }
@@ -163,6 +164,7 @@ template <typename T>
 void gs_cg(const GsMaps& gs, T* w, const T* p, const T* segmask, const double* segmsum,
            CgScalars* cg, double* partialA, int nA, double* partialB, cudaStream_t s) {
   const int nb = std::max(gs_cg_blocks(gs), 1);
+  count_launch();
   gs_cg_kernel<T><<<nb, kGsThreads, 0, s>>>(w, p, gs.bstart, gs.bidx, gs.nbseg, segmask, segmsum,
                                             cg, partialA, nA, partialB);
 }
@@ -171,6 +173,7 @@ template <typename T>
 void gs_cg_weights(const GsMaps& gs, const T* mask, const T* mult, T* segmask, double* segmsum,
                    int* nonuniform, cudaStream_t s) {
   if (gs.nbseg == 0) return;
+  count_launch();
   gs_cg_weights_kernel<T><<<(gs.nbseg + kGsThreads - 1) / kGsThreads, kGsThreads, 0, s>>>(
       gs.bstart, gs.bidx, gs.nbseg, mask, mult, segmask, segmsum, nonuniform);
 }

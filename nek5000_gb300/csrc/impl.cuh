@@ -91,6 +91,7 @@ struct Handle {
   // timing
   bool timing = false;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, evt0 = nullptr, evt1 = nullptr;
+  std::vector<cudaEvent_t> ax_ev;  // per-launch operator timing pool
   double ms_total = 0.0, ms_axhelm = 0.0;
   int n_axhelm = 0;
   // graph cache for the PCG iteration chunk

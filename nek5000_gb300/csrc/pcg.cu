@@ -283,7 +283,9 @@ template <typename T>
 int detect_coef(Handle& h, const T* h1, const T* h2, int64_t n, Coef<T>& c) {
   const int nb = vec_blocks(n);
   if (h.red.ensure(4 * (size_t)nb) != cudaSuccess) return NEKGPU_ENOMEM_;
+  count_launch();
   minmax_kernel<T><<<nb, kVecThreads, 0, h.stream>>>(h1, n, h.red.ptr);
+  count_launch();
   minmax_kernel<T><<<nb, kVecThreads, 0, h.stream>>>(h2, n, h.red.ptr + 2 * nb);
   std::vector<double> hm(4 * (size_t)nb);
   if (cudaMemcpyAsync(hm.data(), h.red.ptr, hm.size() * sizeof(double), cudaMemcpyDeviceToHost,
@@ -328,6 +330,7 @@ double device_sum(Handle& h, int kind, const double* a, const double* b, const d
     *status = -4;
     return 0.0;
   }
+  count_launch();
   sum_kernel<<<nb, kVecThreads, 0, h.stream>>>(kind, a, b, c, n, h.red.ptr);
   std::vector<double> hp((size_t)nb);
   if (cudaMemcpyAsync(hp.data(), h.red.ptr, nb * sizeof(double), cudaMemcpyDeviceToHost,
@@ -347,6 +350,7 @@ static void launch_setprec_nx(Handle& h, double* d, const Coef<double>& c) {
   const Mesh& m = h.mesh;
   const int64_t n = m.n;
   const int nb = (int)((n + 255) / 256);
+  count_launch();
   setprec_kernel<NX><<<nb, 256, 0, h.stream>>>(d, m.f64.G, m.f64.D, m.f64.bm1, c.h1, c.h2, c.h1s,
                                               c.h2s, c.h1mode, c.h2mode, m.nel);
 }
@@ -368,6 +372,7 @@ int setprec_f64(Handle& h, double* d, const Coef<double>& c) {
     default: return -1;
   }
   gs_op<double>(h.mesh.gs, d, 0, h.stream);
+  count_launch();
   invert_kernel<<<vec_blocks(h.mesh.n), kVecThreads, 0, h.stream>>>(d, h.mesh.n);
   return cudaGetLastError() == cudaSuccess ? 0 : -3;
 }
@@ -394,21 +399,11 @@ static void launch_C(Handle& h, PcgWork<T>& wk, T* x, const T* mult, const T* bi
                      bool first) {
   const int64_t n = h.mesh.n;
   const int nb = vec_blocks(n);
-  if (exact) {
-    if (first)
-      cg_update_kernel<T, true, true><<<nb, kVecThreads, 0, h.stream>>>(
-          x, wk.r.ptr, wk.p.ptr, wk.w.ptr, wk.d.ptr, mult, binv, n, h.cg, h.partialC.ptr);
-    else
-      cg_update_kernel<T, true, false><<<nb, kVecThreads, 0, h.stream>>>(
-          x, wk.r.ptr, wk.p.ptr, wk.w.ptr, wk.d.ptr, mult, binv, n, h.cg, h.partialC.ptr);
-  } else {
-    if (first)
-      cg_update_kernel<T, false, true><<<nb, kVecThreads, 0, h.stream>>>(
-          x, wk.r.ptr, wk.p.ptr, wk.w.ptr, wk.d.ptr, mult, binv, n, h.cg, h.partialC.ptr);
-    else
-      cg_update_kernel<T, false, false><<<nb, kVecThreads, 0, h.stream>>>(
-          x, wk.r.ptr, wk.p.ptr, wk.w.ptr, wk.d.ptr, mult, binv, n, h.cg, h.partialC.ptr);
-  }
+  auto kern = exact ? (first ? cg_update_kernel<T, true, true> : cg_update_kernel<T, true, false>)
+                    : (first ? cg_update_kernel<T, false, true> : cg_update_kernel<T, false, false>);
+  count_launch();
+  kern<<<nb, kVecThreads, 0, h.stream>>>(x, wk.r.ptr, wk.p.ptr, wk.w.ptr, wk.d.ptr, mult, binv, n,
+                                         h.cg, h.partialC.ptr);
 }
 
 template <typename T>
@@ -440,6 +435,7 @@ PcgResult pcg_solve(Handle& h, const OpData<T>& op, PcgWork<T>& wk, T* x, const 
       res.status = -4;
       return res;
     }
+    count_launch();
     cast_kernel<double, float><<<vec_blocks(n), kVecThreads, 0, s>>>(tmp.ptr, f, n);
     fmax = device_sum(h, 3, tmp.ptr, nullptr, nullptr, n, &st);
   }
@@ -448,6 +444,7 @@ PcgResult pcg_solve(Handle& h, const OpData<T>& op, PcgWork<T>& wk, T* x, const 
     set_error(h, "pcg: reduction failed");
     return res;
   }
+  count_launch();
   zero_kernel<T><<<vec_blocks(n), kVecThreads, 0, s>>>(x, n);
   if (fmax == 0.0) return res;
 
@@ -466,14 +463,17 @@ PcgResult pcg_solve(Handle& h, const OpData<T>& op, PcgWork<T>& wk, T* x, const 
       return res;
     }
     if (c.h1mode) {
+      count_launch();
       cast_kernel<double, float><<<vec_blocks(n), kVecThreads, 0, s>>>(h1d.ptr, c.h1, n);
       c64.h1 = h1d.ptr;
     }
     if (c.h2mode == 2) {
+      count_launch();
       cast_kernel<double, float><<<vec_blocks(n), kVecThreads, 0, s>>>(h2d.ptr, c.h2, n);
       c64.h2 = h2d.ptr;
     }
     st = setprec_f64(h, d64.ptr, c64);
+    count_launch();
     cast_kernel<float, double><<<vec_blocks(n), kVecThreads, 0, s>>>(wk.d.ptr, d64.ptr, n);
     cudaStreamSynchronize(s);
   }
@@ -489,6 +489,7 @@ PcgResult pcg_solve(Handle& h, const OpData<T>& op, PcgWork<T>& wk, T* x, const 
   cudaMemcpyAsync(&nonuni, h.flag, sizeof(int), cudaMemcpyDeviceToHost, s);
   // r = f, p = 0
   cudaMemcpyAsync(wk.r.ptr, f, n * sizeof(T), cudaMemcpyDeviceToDevice, s);
+  count_launch();
   zero_kernel<T><<<vec_blocks(n), kVecThreads, 0, s>>>(wk.p.ptr, n);
   CgScalars& hc = *h.cg_host;
   memset(&hc, 0, sizeof(CgScalars));
@@ -515,13 +516,20 @@ PcgResult pcg_solve(Handle& h, const OpData<T>& op, PcgWork<T>& wk, T* x, const 
   }
   // iteration 1 check (z, s1, s2) -- no update
   launch_C<T>(h, wk, x, mult, binv, exact, true);
-  // main loop: chunks of iterations, one host check per chunk.  With timing
-  // on, the chunk is one iteration and the fused axhelm is bracketed by
-  // events, so its summed time covers live launches only.
-  const int chunk = h.timing ? 1 : std::max(1, h.graph_chunk);
+  // main loop: chunks of iterations, one host check per chunk.  With kernel
+  // timing on, every fused-axhelm launch is bracketed by events; after the
+  // chunk's check, the first (iterations completed in the chunk) of them are
+  // the live launches and are summed (later ones found the solve converged
+  // and returned at once).
+  const int chunk = std::max(1, h.graph_chunk);
   h.ms_axhelm = 0.0;
   h.n_axhelm = 0;
-  bool pending = false;
+  if (h.timing && h.ax_ev.size() < 2 * (size_t)chunk) {
+    for (cudaEvent_t e : h.ax_ev) cudaEventDestroy(e);
+    h.ax_ev.assign(2 * (size_t)chunk, nullptr);
+    for (auto& e : h.ax_ev) cudaEventCreate(&e);
+  }
+  int launched = 0, iter_before = 0;
   for (;;) {
     cudaMemcpyAsync(h.cg_host, h.cg, sizeof(CgScalars), cudaMemcpyDeviceToHost, s);
     if (cudaStreamSynchronize(s) != cudaSuccess) {
@@ -529,24 +537,24 @@ PcgResult pcg_solve(Handle& h, const OpData<T>& op, PcgWork<T>& wk, T* x, const 
       set_error(h, std::string("pcg: ") + cudaGetErrorString(cudaGetLastError()));
       return res;
     }
-    if (pending) {
-      float ms = 0.f;
-      cudaEventElapsedTime(&ms, h.ev0, h.ev1);
-      h.ms_axhelm += ms;
-      h.n_axhelm += 1;
-      pending = false;
+    if (h.timing && launched) {
+      const int live = std::min(launched, h.cg_host->iter - iter_before);
+      for (int q = 0; q < live; ++q) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, h.ax_ev[2 * q], h.ax_ev[2 * q + 1]);
+        h.ms_axhelm += ms;
+      }
+      h.n_axhelm += live;
     }
     if (h.cg_host->done) break;
+    iter_before = h.cg_host->iter;
     const int left = h.cg_host->maxiter - h.cg_host->iter + 1;
     const int k = std::min(chunk, std::max(left, 1));
     for (int q = 0; q < k; ++q) {
       int nAb = 0;
-      if (h.timing) cudaEventRecord(h.ev0, s);
+      if (h.timing) cudaEventRecord(h.ax_ev[2 * q], s);
       cudaError_t e = launch_A<T>(h, op, wk, c, exact, &nAb);
-      if (h.timing) {
-        cudaEventRecord(h.ev1, s);
-        pending = true;
-      }
+      if (h.timing) cudaEventRecord(h.ax_ev[2 * q + 1], s);
       if (e != cudaSuccess) {
         res.status = -3;
         set_error(h, std::string("pcg axhelm: ") + cudaGetErrorString(e));
@@ -556,6 +564,7 @@ PcgResult pcg_solve(Handle& h, const OpData<T>& op, PcgWork<T>& wk, T* x, const 
                h.partialB.ptr, s);
       launch_C<T>(h, wk, x, mult, binv, exact, false);
     }
+    launched = k;
   }
   const CgScalars& fin = *h.cg_host;
   res.niter = fin.niter;

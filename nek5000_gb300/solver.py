@@ -88,6 +88,11 @@ class NekGpu:
                                                C.byref(k)))
         return t.value, a.value, k.value
 
+    def launch_count(self) -> int:
+        c = C.c_int64(0)
+        self._L.nekgpu_launch_count(C.byref(c))
+        return c.value
+
     # ---- mesh -------------------------------------------------------------
     def setup(self, lx1: int, nel: int, D, g, bm1, glo_num):
         """D: (lx1,lx1) numpy with D[i,j] = dl_j/dr(z_i) (the reference's dxm1);

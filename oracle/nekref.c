@@ -787,6 +787,9 @@ void ref_gs_op(const ref_gs *gs, double *u, int op) {
 /* ========================================================================
  * Operator state
  * ====================================================================== */
+/* pointwise loops: independent per point, so threading leaves results unchanged */
+#define PFOR _Pragma("omp parallel for schedule(static) num_threads(ops->nthreads)")
+
 struct ref_ops {
   int nx1, nel, nthreads;
   int64_t n;
@@ -977,9 +980,12 @@ void ref_setprec(const ref_ops *ops, double *dpcm1, const double *helm1, const d
   }
 #undef DT
 #undef IDX
+  PFOR
   for (int64_t i = 0; i < ntot; ++i) dpcm1[i] = dpcm1[i] * helm1[i];                 /* COL2 */
+  PFOR
   for (int64_t i = 0; i < ntot; ++i) dpcm1[i] = dpcm1[i] + helm2[i] * ops->bm1[i];  /* ADDCOL3 */
   ref_dssum(ops, dpcm1);
+  PFOR
   for (int64_t i = 0; i < ntot; ++i) dpcm1[i] = 1.0 / dpcm1[i];                     /* INVCOL1 */
 }
 
@@ -993,16 +999,20 @@ void ref_chktcg1(const ref_ops *ops, double *tol, const double *res, const doubl
   double *w1 = (double *)malloc(sizeof(double) * n);
   double *w2 = (double *)malloc(sizeof(double) * n);
   memcpy(w1, res, sizeof(double) * n);
+  PFOR
   for (int64_t i = 0; i < n; ++i) w2[i] = binv[i] * w1[i];
   double rinit = sqrt(ref_glsc3(ops, w2, w1, mult) / vol);
   double rmin = eps * rinit;
   if (*tol < rmin) *tol = rmin;
+  PFOR
   for (int64_t i = 0; i < n; ++i) w1[i] = 1.0;
   double bcneu1 = ref_glsc3(ops, w1, mask, mult);
   double bcneu2 = ref_glsc3(ops, w1, w1, mult);
   double bctest = fabs(bcneu1 - bcneu2);
   ref_axhelm(ops, w2, w1, h1, h2);
+  PFOR
   for (int64_t i = 0; i < n; ++i) w2[i] = w2[i] * w2[i];
+  PFOR
   for (int64_t i = 0; i < n; ++i) w2[i] = w2[i] * ops->bm1[i];
   double s;
   GLOBAL_SUM(ops, s, w2[i]);
@@ -1031,7 +1041,9 @@ int ref_cggo(const ref_ops *ops, double *x, const double *f, const double *h1, c
   double *z = (double *)malloc(sizeof(double) * n);
   ref_setprec(ops, d, h1, h2);
   memcpy(r, f, sizeof(double) * n);
+  PFOR
   for (int64_t i = 0; i < n; ++i) x[i] = 0.0;
+  PFOR
   for (int64_t i = 0; i < n; ++i) p[i] = 0.0;
   double rbn0 = 0.0, rbn2 = 0.0;
   double fmax = 0.0;
@@ -1058,18 +1070,22 @@ int ref_cggo(const ref_ops *ops, double *x, const double *f, const double *h1, c
     double rmean = smean * sr;
     memcpy(x, ops->bm1, sizeof(double) * n);
     ref_dssum(ops, x);
+    PFOR
     for (int64_t i = 0; i < n; ++i) r[i] = r[i] + rmean * x[i];
+    PFOR
     for (int64_t i = 0; i < n; ++i) x[i] = 0.0;
   }
   double rtz1 = 1.0, rtz2, rho = 0.0;
   int iter;
   (void)P;
   for (iter = 1; iter <= niter; ++iter) {
+    PFOR
     for (int64_t i = 0; i < n; ++i) z[i] = r[i] * d[i]; /* col3 */
     if (ifmcor) {
       double sz;
       GLOBAL_SUM(ops, sz, z[i] * ops->bm1[i]);
       double rmean = smean * sz;
+      PFOR
       for (int64_t i = 0; i < n; ++i) z[i] = z[i] + rmean;
     }
     rtz2 = rtz1;
@@ -1086,14 +1102,18 @@ int ref_cggo(const ref_ops *ops, double *x, const double *f, const double *h1, c
     }
     double beta = rtz1 / rtz2;
     if (iter == 1) beta = 0.0;
+    PFOR
     for (int64_t i = 0; i < n; ++i) p[i] = beta * p[i] + z[i]; /* add2s1 */
     ref_axhelm(ops, w, p, h1, h2);
     ref_dssum(ops, w);
+    PFOR
     for (int64_t i = 0; i < n; ++i) w[i] = w[i] * mask[i];
     rho = ref_glsc3(ops, w, p, mult);
     double alpha = rtz1 / rho;
     double alphm = -alpha;
+    PFOR
     for (int64_t i = 0; i < n; ++i) x[i] = x[i] + alpha * p[i]; /* add2s2 */
+    PFOR
     for (int64_t i = 0; i < n; ++i) r[i] = r[i] + alphm * w[i];
   }
   niter = iter - 1;
@@ -1111,6 +1131,7 @@ int ref_hmholtz(const ref_ops *ops, double *u, double *rhs, const double *h1, co
   const int64_t n = ops->n;
   double tol = fabs(tli);
   ref_dssum(ops, rhs);
+  PFOR
   for (int64_t i = 0; i < n; ++i) rhs[i] = rhs[i] * mask[i];
   ref_chktcg1(ops, &tol, rhs, h1, h2, mask, mult, binv);
   if (tli < 0) tol = tli;

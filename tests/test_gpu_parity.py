@@ -6,8 +6,12 @@ Tolerances:
   * default mode (fused multiply-adds): axhelm within 1e-13 relative (max
     norm).
   * PCG: the same iteration count as the oracle (+-1 allowed only at the
-    stopping threshold), final solution within 1e-12 relative (L2) of the
-    oracle's, rbn0 within 1e-13 relative.
+    stopping threshold), rbn0 within 1e-13 relative, and the solution within
+    max(1e-12, 2 * spread) relative (L2) of the single-rank oracle, where
+    spread is how far the reference's own solution moves when its dot
+    products are summed as P ranks would (P = 2, 3, 4, 7, 8): the GPU sums in
+    a tree, which no serial order reproduces, and CG carries that rounding
+    into the iterates at the 1e-12 level.
 """
 import numpy as np
 import pytest
@@ -33,6 +37,16 @@ def cfg1(oracle):
 def cfgp(oracle):
     """Config-2 shape at small size: Dirichlet x, periodic y/z, N=5."""
     return oracle.box_problem(6, 3, 4, 3, periodic=(False, True, True), v=rng_unit_vector(1))
+
+
+def rank_spread(oracle, P, solve):
+    """Largest relative change of the oracle's solution over P-rank sum orders."""
+    base = solve(P["ops"])
+    worst = 0.0
+    for nt in (2, 3, 4, 7, 8):
+        ops = oracle.Ops(P["nx1"], P["nel"], P["D"], P["g"], P["bm1"], P["glo_num"], nt)
+        worst = max(worst, np.linalg.norm(solve(ops) - base) / np.linalg.norm(base))
+    return base, worst
 
 
 def rel(a, b):
@@ -143,7 +157,11 @@ def test_hmholtz_poisson_config1(gpu_lib, oracle, cfg1, exact):
     assert abs(r0 - r0_ref) <= 1e-13 * r0_ref
     assert abs(it - it_ref) <= 1, (it, it_ref)
     assert r2 <= 1e-10 * r0
-    assert np.linalg.norm(u - u_ref) <= 1e-12 * np.linalg.norm(u_ref)
+    base, spread = rank_spread(oracle, P, lambda ops: ops.hmholtz(
+        rhs, h1, h2, P["mask"], P["mult"], P["binv"], -1e-10, maxcg=10 ** 6)[0])
+    assert np.array_equal(base, u_ref)
+    err = np.linalg.norm(u - u_ref) / np.linalg.norm(u_ref)
+    assert err <= max(1e-12, 2 * spread), (err, spread)
 
 
 def test_cggo_helmholtz_periodic(gpu_lib, oracle, cfgp):
@@ -161,7 +179,10 @@ def test_cggo_helmholtz_periodic(gpu_lib, oracle, cfgp):
                               10 ** 6, 1, dev(P["binv"]), maxcg=10 ** 6)
     assert rc == 0
     assert abs(it - it_ref) <= 1
-    assert np.linalg.norm(x.cpu().numpy() - x_ref) <= 1e-12 * np.linalg.norm(x_ref)
+    _, spread = rank_spread(oracle, P, lambda ops: ops.cggo(
+        f, h1, h2, P["mask"], P["mult"], P["binv"], -1e-10, maxcg=10 ** 6)[0])
+    err = np.linalg.norm(x.cpu().numpy() - x_ref) / np.linalg.norm(x_ref)
+    assert err <= max(1e-12, 2 * spread), (err, spread)
 
 
 def test_cggo_iteration_cap_reports_not_converged(gpu_lib, oracle, cfg1):
