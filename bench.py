@@ -9,11 +9,14 @@ side B f with f standard normal per global node (seed 1), Jacobi-PCG to a
 relative residual of 1e-10 (the reference's cggo norm and stopping rule, the
 900-iteration cap lifted).
 
-A step is one complete solve.  `value` is DOF-iterations/s = n * iterations /
-solve time over the K timed steps, with every input resident in HBM (the
-device entry point nekgpu_cggo_dev).  `e2e` is the same metric through the
-host entry point nekgpu_hmholtz: rhs, h1, h2, mask, mult and binv copied in
-from pinned host memory and u, rhs copied out inside each timed call.
+A step is one complete solve.  `value` is the mixed-precision solve (FP32
+inner Jacobi-PCG in FP64 defect correction) as time-to-solution
+DOF-iterations/s: n * (iteration count of the plain FP64 solve) / mixed solve
+time, over the K timed steps, every input resident in HBM (device entry
+points).  The plain FP64 solve (nekgpu_cggo_dev) is reported beside it under
+"fp64".  `e2e` is the same metric through the host entry point
+nekgpu_hmholtz_mixed: rhs, h1, h2, mask, mult and binv copied in from pinned
+host memory and u, rhs copied out inside each timed call.
 
 --impl reference times the CPU restatement of the reference (the oracle, all
 host threads) on a bounded sample of the same workload.
@@ -36,7 +39,6 @@ sys.path.insert(0, ROOT)
 
 METRIC = "DOF-iters/s, E=32^3 N=7 PCG to 1e-10: mixed vs FP64; axhelm HBM GB/s"
 FALLBACK_HBM_GBS = 6800.0
-FP64_PEAK_TFLOPS = 1.0  # measured FMA-chain rate on this GB300 (profiles/gb300_fp_rates.md)
 
 
 def parse():
@@ -51,6 +53,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-iters", type=int, default=0, help="oracle PCG iterations per sample")
+    ap.add_argument("--inner-tol", type=float, default=1e-5, help="mixed: inner FP32 tolerance")
+    ap.add_argument("--only-mixed", action="store_true", help="skip the plain FP64 solve")
     return ap.parse_args()
 
 
@@ -78,12 +82,11 @@ def peaks():
         return FALLBACK_HBM_GBS, "of fallback"
 
 
-def ncu_traffic(kernel_key):
-    """dram bytes per launch for the dominant kernel from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+def ncu_summary(kernel_key):
+    """Figures from the committed ncu capture of a kernel (profiles/ncu_summary.json)."""
+    p = os.path.join(ROOT, "profiles", "ncu_summary.json")
     try:
-        d = json.load(open(p))
-        return d.get(kernel_key)
+        return json.load(open(p)).get(kernel_key)
     except Exception:
         return None
 
@@ -199,9 +202,9 @@ def run_reference(args):
         return
     M = workload(args.k, args.N)
     nth = os.cpu_count() or 1
-    iters = args.cpu_iters or 10
+    iters = args.cpu_iters or 100
     for _ in range(args.warmup):
-        cpu_sample(M, nth, max(2, iters // 5))
+        cpu_sample(M, nth, max(2, iters // 10))
     vals, times = [], []
     for _ in range(args.steps):
         v, it, dt = cpu_sample(M, nth, iters)
@@ -239,90 +242,127 @@ def run_gpu(args):
     mask, mult, binv = dev(M["mask"]), dev(M["mult"]), dev(M["binv"])
     x = torch.zeros(n, dtype=torch.float64, device=f"cuda:{local}")
     big = 10 ** 6
-
-    def solve():
-        return lib.cggo(x, f, h1, h2, mask, mult, 1, -args.tol, big, 1, binv, maxcg=big)
-
     lib.set_option(2, 1)  # timing: solve-total and per-launch operator events
-    for _ in range(args.warmup):
-        solve()
-    barrier(pg)
-    torch.cuda.synchronize()
-    l0 = lib.launch_count()
-    iters, ms_tot, ms_ax, n_ax = [], 0.0, 0.0, 0
-    with Clocks(local) as ck:
-        for _ in range(args.steps):
-            it, r0, r2, rc = solve()
-            t_tot, t_ax, k_ax = lib.last_timing()
-            iters.append(it)
-            ms_tot += t_tot
-            ms_ax += t_ax
-            n_ax += k_ax
-    torch.cuda.synchronize()
-    barrier(pg)
-    launches = lib.launch_count() - l0
-    T = allmax(pg, ms_tot / 1e3)
-    dof_iters = n * sum(iters)
-    value = allsum(pg, dof_iters) / T
-    # dominant kernel: fused operator (p-update + axhelm), FP64, Helmholtz
-    w = 8
-    bytes_per_pt = w * (3 + 6 + 1 + 2)  # r, d, p_old, G1..G6, bm1 in; p, w out
-    ax_ms = ms_ax / max(n_ax, 1)
-    achieved = bytes_per_pt * n / (ax_ms * 1e-3) / 1e9
+
+    def fp64():
+        it, r0, r2, rc = lib.cggo(x, f, h1, h2, mask, mult, 1, -args.tol, big, 1, binv, maxcg=big)
+        return it, rc
+
+    def mixed():
+        no, ni, r0, r2, rc = lib.cggo_mixed(x, f, h1, h2, mask, mult, 1, -args.tol, big, 1, binv,
+                                            inner_tol=args.inner_tol)
+        return (no, ni), rc
+
+    def timed(solve):
+        for _ in range(args.warmup):
+            solve()
+        barrier(pg)
+        torch.cuda.synchronize()
+        l0 = lib.launch_count()
+        its, ms_tot, ms_ax, n_ax = [], 0.0, 0.0, 0
+        with Clocks(local) as ck:
+            for _ in range(args.steps):
+                it, rc = solve()
+                if rc != 0:
+                    raise RuntimeError(f"solve did not converge: {lib.last_error()}")
+                t_tot, t_ax, k_ax = lib.last_timing()
+                its.append(it)
+                ms_tot += t_tot
+                ms_ax += t_ax
+                n_ax += k_ax
+        torch.cuda.synchronize()
+        barrier(pg)
+        return dict(iters=its, T=allmax(pg, ms_tot / 1e3), ms_ax=ms_ax / max(n_ax, 1), n_ax=n_ax,
+                    launches=lib.launch_count() - l0, clocks=ck.summary())
+
     peak, peak_src = peaks()
-    flops_pt = 12 * M["lx1"] + 20 + 3 + 2
-    clk = ck.summary()
-    line = {"metric": METRIC, "value": value, "unit": "DOF-iters/s", "n_gpus": ws,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_tot / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+    flops_pt = 12 * M["lx1"] + 25
+    if args.only_mixed:  # profiling runs: iteration count of the FP64 solve not measured
+        r64 = dict(iters=[0], T=1.0, ms_ax=0.0, launches=0, clocks=None)
+    else:
+        r64 = timed(fp64)
+    it64 = r64["iters"][0]
+    v64 = allsum(pg, n * sum(r64["iters"])) / r64["T"]
+    b64 = 8 * 12  # fused operator: r, d, p_old, G1..G6, bm1 in; p, w out (FP64 words)
+    ns64 = ncu_summary("axhelm_fused_f64_n7")
+    fp64_block = {
+        "value": v64, "unit": "DOF-iters/s", "iterations": r64["iters"],
+        "ms_per_solve": 1e3 * r64["T"] / args.steps,
+        "axhelm": {"kernel": "axhelm_kernel<8,double,fused>", "avg_launch_ms": r64["ms_ax"],
+                   "GB/s": b64 * n / (r64["ms_ax"] * 1e-3) / 1e9, "bytes_per_point": b64,
+                   "fp64_tflops": flops_pt * n / (r64["ms_ax"] * 1e-3) / 1e12,
+                   "ncu_fp64_pipe_active_pct": (ns64 or {}).get("fp64_pipe_active_pct")},
+        "gpu_launches": r64["launches"], "clocks": r64["clocks"]}
+    rmx = timed(mixed)
+    outer = [o for o, i in rmx["iters"]]
+    inner = [i for o, i in rmx["iters"]]
+    # time to solution, counted with the FP64 solve's iteration count
+    vmx = allsum(pg, n * it64 * args.steps) / rmx["T"]
+    b32 = 4 * 12
+    ax_gbs = b32 * n / (rmx["ms_ax"] * 1e-3) / 1e9
+    ns32 = ncu_summary("axhelm_fused_f32_n7")
+    line = {"metric": METRIC, "value": vmx, "unit": "DOF-iters/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * rmx["T"] / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 inner / f64 outer",
             "data": "synthetic",
             "config": {"workload": f"helmholtz E={args.k}^3 N={args.N} h1=1 h2=10 "
                                    "dirichlet-x periodic-yz", "n_points": n,
-                       "solver": "jacobi-pcg fp64 (fused 3-kernel iteration)",
-                       "tol": args.tol, "iterations": iters, "l2": "inputs larger than L2",
-                       "parallelism": f"replicas{ws}"},
-            "roofline": {"kernel": "axhelm_kernel<8,double,fused>", "bound": "hbm",
-                         "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "peak_source": peak_src,
-                         "bytes_per_point": bytes_per_pt, "avg_launch_ms": ax_ms,
-                         "launches_timed": n_ax,
-                         "traffic": ncu_traffic("axhelm_fused_f64_n7"),
-                         "fp64_alu": {"achieved_tflops": flops_pt * n / (ax_ms * 1e-3) / 1e12,
-                                      "peak_tflops": FP64_PEAK_TFLOPS,
-                                      "frac": flops_pt * n / (ax_ms * 1e-3) / 1e12 / FP64_PEAK_TFLOPS}},
-            "gpu_launches": launches,
-            "clocks": clk}
-    # ---- end to end through the host entry point ------------------------------
+                       "solver": "mixed: fp32 jacobi-pcg (inner tol "
+                                 f"{args.inner_tol:g}) in fp64 defect correction",
+                       "value_definition": "n * (FP64 PCG iteration count) / mixed solve time",
+                       "tol": args.tol, "outer_steps": outer, "inner_iterations": inner,
+                       "inner_rate_dof_iters_per_s": allsum(pg, n * sum(inner)) / rmx["T"],
+                       "l2": "inputs larger than L2", "parallelism": f"replicas{ws}"},
+            "fp64": fp64_block,
+            "speedup_mixed_vs_fp64": vmx / v64,
+            "roofline": {"kernel": "axhelm_kernel<8,float,fused> (inner solve)", "bound": "hbm",
+                         "achieved": ax_gbs, "peak": peak, "unit": "GB/s", "frac": ax_gbs / peak,
+                         "peak_source": peak_src, "bytes_per_point": b32,
+                         "avg_launch_ms": rmx["ms_ax"], "launches_timed": rmx["n_ax"],
+                         "traffic": ns32["dram_bytes_per_point"] * n if ns32 else None},
+            "gpu_launches": rmx["launches"],
+            "clocks": rmx["clocks"]}
+    # ---- end to end through the host entry points -------------------------------
     if not args.no_e2e:
         pin = lambda a: torch.tensor(a).pin_memory().numpy()
         rhs0 = pin(M["rhs"])
         hb = {k: pin(M[k]) for k in ("h1", "h2", "mask", "mult", "binv")}
         rhs = pin(M["rhs"])
         u = pin(np.zeros(n))
-        lib.hmholtz("TEMP", u, rhs, hb["h1"], hb["h2"], hb["mask"], hb["mult"], 1, -args.tol, big,
-                    1, hb["binv"], maxcg=big)  # warm the staging buffers
-        e_tot, e_it = 0.0, 0
-        barrier(pg)
-        for _ in range(args.steps):
+
+        def e2e(call):
             np.copyto(rhs, rhs0)
-            t0 = time.perf_counter()
-            it, r0, r2, rc = lib.hmholtz("TEMP", u, rhs, hb["h1"], hb["h2"], hb["mask"], hb["mult"],
-                                         1, -args.tol, big, 1, hb["binv"], maxcg=big)
-            e_tot += time.perf_counter() - t0
-            e_it += it
-        barrier(pg)
-        e_T = allmax(pg, e_tot)
-        line["e2e"] = {"value": allsum(pg, n * e_it) / e_T, "unit": "DOF-iters/s",
+            call()  # warm the staging buffers
+            tot, cnt = 0.0, 0
+            barrier(pg)
+            for _ in range(args.steps):
+                np.copyto(rhs, rhs0)
+                t0 = time.perf_counter()
+                call()
+                tot += time.perf_counter() - t0
+                cnt += 1
+            barrier(pg)
+            return allmax(pg, tot)
+
+        tm = e2e(lambda: lib.hmholtz_mixed("TEMP", u, rhs, hb["h1"], hb["h2"], hb["mask"],
+                                           hb["mult"], 1, -args.tol, big, 1, hb["binv"],
+                                           inner_tol=args.inner_tol))
+        t6 = e2e(lambda: lib.hmholtz("TEMP", u, rhs, hb["h1"], hb["h2"], hb["mask"], hb["mult"], 1,
+                                     -args.tol, big, 1, hb["binv"], maxcg=big))
+        line["e2e"] = {"value": allsum(pg, n * it64 * args.steps) / tm, "unit": "DOF-iters/s",
                        "h2d_bytes_per_step": 6 * 8 * n, "d2h_bytes_per_step": 2 * 8 * n,
-                       "api": "nekgpu_hmholtz (host arrays, pinned)"}
-    # ---- CPU baseline (oracle) on rank 0, N=1 only -------------------------------
+                       "api": "nekgpu_hmholtz_mixed (host arrays, pinned)"}
+        fp64_block["e2e"] = {"value": allsum(pg, n * it64 * args.steps) / t6,
+                             "unit": "DOF-iters/s", "api": "nekgpu_hmholtz (host arrays, pinned)"}
+    # ---- CPU baseline (oracle) on rank 0, N=1 only ------------------------------
     if rank == 0 and ws == 1 and not args.no_cpu:
         nth = os.cpu_count() or 1
-        iters_cpu = args.cpu_iters or 10
+        iters_cpu = args.cpu_iters or 200
         v, it, dt = cpu_sample(M, nth, iters_cpu)
         line["cpu_baseline"] = {"value": v, "unit": "DOF-iters/s", "cores": nth, "kind": "port",
-                                "sample": f"{it} Jacobi-PCG iterations of the full problem, "
-                                          f"{dt:.1f} s, C restatement of the reference (FP64)"}
+                                "sample": f"{it} Jacobi-PCG iterations of the full problem "
+                                          f"({dt:.1f} s), C restatement of the reference, FP64"}
     if rank == 0:
         print(json.dumps(line), flush=True)
     lib.close()

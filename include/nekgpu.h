@@ -136,6 +136,28 @@ int nekgpu_hmholtz_dev(const int64_t *handle, double *u, double *rhs, const doub
                        const double *binv, const int *maxcg, int *niter, double *rbn0,
                        double *rbn2);
 
+/* ---- mixed precision --------------------------------------------------- */
+/* Same system and FP64 stopping rule as cggo, solved by FP64 defect
+ * correction around an FP32 Jacobi-PCG: each outer step solves A e = r in
+ * FP32 (G, D, fields, diagonal stored FP32) to *inner_tol relative (default
+ * 1e-5 when NULL), adds e to x in FP64 and recomputes r = f - A x with the
+ * FP64 operator.  Stops when the FP64 norm sqrt(sum r^2 mult binv / vol)
+ * reaches |tin| (tin >= 0) or |tin| * its initial value (tin < 0).  *maxit
+ * caps each inner solve.  Outputs: outer steps, total inner iterations, first
+ * and last FP64 norms.  No reference counterpart: it replaces cggo
+ * (core/hmholtz.f:611) for callers that accept FP32 inner arithmetic. */
+int nekgpu_cggo_mixed_dev(const int64_t *handle, double *x, const double *f, const double *h1,
+                          const double *h2, const double *mask, const double *mult,
+                          const int *imsh, const double *tin, const int *maxit, const int *isd,
+                          const double *binv, const double *inner_tol, int *niter_outer,
+                          int *niter_inner, double *rbn0, double *rbn2);
+/* hmholtz (core/hmholtz.f:2-69) with the mixed-precision solve, host arrays. */
+int nekgpu_hmholtz_mixed(const int64_t *handle, double *u, double *rhs, const double *h1,
+                         const double *h2, const double *mask, const double *mult,
+                         const int *imsh, const double *tli, const int *maxit, const int *isd,
+                         const double *binv, const double *inner_tol, int *niter_outer,
+                         int *niter_inner, double *rbn0, double *rbn2);
+
 /* ---- timing of the last solve (device time, CUDA events) ----------------- */
 /* ms_total: whole call on the device; ms_axhelm: summed axhelm-kernel time of
  * the last cggo when the handle's kernel timing is on (nekgpu_set_timing). */

@@ -52,6 +52,10 @@ SIGNATURES = {
     "nekgpu_set_timing": [_I64P, _IP],
     "nekgpu_last_timing": [_I64P, _DP, _DP, _IP],
     "nekgpu_launch_count": [_I64P],
+    "nekgpu_cggo_mixed_dev": [_I64P, _P, _P, _P, _P, _P, _P, _IP, _DP, _IP, _IP, _P, _DP, _IP, _IP,
+                              _DP, _DP],
+    "nekgpu_hmholtz_mixed": [_I64P, _P, _P, _P, _P, _P, _P, _IP, _DP, _IP, _IP, _P, _DP, _IP, _IP,
+                             _DP, _DP],
 }
 
 _lib = None

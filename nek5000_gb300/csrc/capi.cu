@@ -455,6 +455,8 @@ int nekgpu_cggo_dev(const int64_t* handle, double* x, const double* f, const dou
   if (check_n(H, x) || check_n(H, f) || check_n(H, mask) || check_n(H, mult) ||
       check_n(H, binv) || !tin || !maxit)
     return fail(H, NEKGPU_EINVAL, "null argument");
+  H->ms_axhelm = 0.0;
+  H->n_axhelm = 0;
   if (H->timing) cudaEventRecord(H->evt0, H->stream);
   int rc = cggo_dev(H, x, f, h1, h2, mask, mult, *tin, *maxit, maxcg ? *maxcg : 900, binv, niter,
                     rbn0, rbn2);
@@ -503,6 +505,8 @@ int nekgpu_hmholtz_dev(const int64_t* handle, double* u, double* rhs, const doub
   if (check_n(H, u) || check_n(H, rhs) || check_n(H, mask) || check_n(H, mult) ||
       check_n(H, binv) || !tli || !maxit)
     return fail(H, NEKGPU_EINVAL, "null argument");
+  H->ms_axhelm = 0.0;
+  H->n_axhelm = 0;
   if (H->timing) cudaEventRecord(H->evt0, H->stream);
   int rc = hmholtz_dev(H, u, rhs, h1, h2, mask, mult, *tli, *maxit, maxcg ? *maxcg : 900, binv,
                        niter, rbn0, rbn2);
@@ -534,6 +538,78 @@ int nekgpu_hmholtz(const int64_t* handle, double* u, double* rhs, const double* 
   if (H->io3.ensure(n)) return fail(H, NEKGPU_ENOMEM, "staging allocation failed");
   rc = nekgpu_hmholtz_dev(handle, H->io3.ptr, H->io0.ptr, H->io1.ptr, H->io2.ptr, H->io4.ptr,
                           H->io7.ptr, imsh, tli, maxit, isd, H->io8.ptr, maxcg, niter, rbn0, rbn2);
+  if (rc && rc != NEKGPU_ENOTCONV) return rc;
+  int rc2 = d2h(H, u, H->io3.ptr, n);
+  if (!rc2) rc2 = d2h(H, rhs, H->io0.ptr, n);
+  return rc2 ? rc2 : rc;
+}
+
+int nekgpu_cggo_mixed_dev(const int64_t* handle, double* x, const double* f, const double* h1,
+                          const double* h2, const double* mask, const double* mult,
+                          const int* imsh, const double* tin, const int* maxit, const int* isd,
+                          const double* binv, const double* inner_tol, int* niter_outer,
+                          int* niter_inner, double* rbn0, double* rbn2) {
+  GET_HANDLE(handle);
+  NEED_MESH();
+  (void)imsh;
+  (void)isd;
+  if (check_n(H, x) || check_n(H, f) || check_n(H, h1) || check_n(H, h2) || check_n(H, mask) ||
+      check_n(H, mult) || check_n(H, binv) || !tin || !maxit)
+    return fail(H, NEKGPU_EINVAL, "null argument");
+  const double itol = inner_tol ? *inner_tol : 1e-5;
+  if (!(itol > 0.0 && itol < 1.0)) return fail(H, NEKGPU_EINVAL, "inner_tol must be in (0, 1)");
+  H->ms_axhelm = 0.0;
+  H->n_axhelm = 0;
+  if (H->timing) cudaEventRecord(H->evt0, H->stream);
+  MixedResult r = mixed_solve(*H, x, f, h1, h2, mask, mult, binv, *tin, *maxit, itol);
+  if (H->timing) {
+    cudaEventRecord(H->evt1, H->stream);
+    cudaEventSynchronize(H->evt1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, H->evt0, H->evt1);
+    H->ms_total = ms;
+  }
+  if (niter_outer) *niter_outer = r.outer;
+  if (niter_inner) *niter_inner = r.inner;
+  if (rbn0) *rbn0 = r.rbn0;
+  if (rbn2) *rbn2 = r.rbn2;
+  if (r.status == -5) return NEKGPU_ENOTCONV;
+  if (r.status == -7) return NEKGPU_ENAN;
+  if (r.status) return fail(H, r.status, H->err.empty() ? "mixed solve failed" : H->err);
+  return NEKGPU_OK;
+}
+
+int nekgpu_hmholtz_mixed(const int64_t* handle, double* u, double* rhs, const double* h1,
+                         const double* h2, const double* mask, const double* mult,
+                         const int* imsh, const double* tli, const int* maxit, const int* isd,
+                         const double* binv, const double* inner_tol, int* niter_outer,
+                         int* niter_inner, double* rbn0, double* rbn2) {
+  GET_HANDLE(handle);
+  NEED_MESH();
+  if (check_n(H, u) || check_n(H, rhs) || check_n(H, h1) || check_n(H, h2) || check_n(H, mask) ||
+      check_n(H, mult) || check_n(H, binv) || !tli)
+    return NEKGPU_EINVAL;
+  const int64_t n = H->mesh.n;
+  int rc;
+  if ((rc = h2d(H, H->io0, rhs, n)) || (rc = h2d(H, H->io1, h1, n)) ||
+      (rc = h2d(H, H->io2, h2, n)) || (rc = h2d(H, H->io4, mask, n)) ||
+      (rc = h2d(H, H->io7, mult, n)) || (rc = h2d(H, H->io8, binv, n)))
+    return rc;
+  if (H->io3.ensure(n)) return fail(H, NEKGPU_ENOMEM, "staging allocation failed");
+  // hmholtz (core/hmholtz.f:50-57): dssum + mask the rhs; a relative tolerance
+  // (tli < 0) is used as given, an absolute one goes through chktcg1.
+  gs_op<double>(H->mesh.gs, H->io0.ptr, 0, H->stream);
+  count_launch();
+  mul_kernel<<<nblk(n), 256, 0, H->stream>>>(H->io0.ptr, H->io4.ptr, n);
+  double tol = *tli;
+  if (tol >= 0) {
+    Coef<double> c;
+    if ((rc = make_coef(H, H->io1.ptr, H->io2.ptr, c))) return rc;
+    if ((rc = chktcg1_dev(H, &tol, H->io0.ptr, c, H->io4.ptr, H->io7.ptr, H->io8.ptr))) return rc;
+  }
+  rc = nekgpu_cggo_mixed_dev(handle, H->io3.ptr, H->io0.ptr, H->io1.ptr, H->io2.ptr, H->io4.ptr,
+                             H->io7.ptr, imsh, &tol, maxit, isd, H->io8.ptr, inner_tol,
+                             niter_outer, niter_inner, rbn0, rbn2);
   if (rc && rc != NEKGPU_ENOTCONV) return rc;
   int rc2 = d2h(H, u, H->io3.ptr, n);
   if (!rc2) rc2 = d2h(H, rhs, H->io0.ptr, n);

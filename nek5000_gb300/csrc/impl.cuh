@@ -142,10 +142,24 @@ struct PcgResult {
 };
 
 // cggo on device arrays (f: masked, assembled rhs; x: out).  Precision T.
+// dpre: precomputed Jacobi diagonal (device, precision T), or nullptr to
+// run setprec (FP64 only).
 template <typename T>
 PcgResult pcg_solve(Handle& h, const OpData<T>& op, PcgWork<T>& wk, T* x, const T* f,
                     const Coef<T>& c, const T* mask, const T* mult, const T* binv, double tin,
-                    int maxiter, int istep, bool exact);
+                    int maxiter, int istep, bool exact, const T* dpre = nullptr);
+template <typename T>
+double device_absmax(Handle& h, const T* a, int64_t n, int* status);
+
+// Mixed precision (mixed.cu): FP32 inner PCG in an FP64 defect-correction loop.
+struct MixedResult {
+  int outer = 0, inner = 0;
+  double rbn0 = 0, rbn2 = 0;
+  int status = 0;
+};
+MixedResult mixed_solve(Handle& h, double* x, const double* f, const double* h1,
+                        const double* h2, const double* mask, const double* mult,
+                        const double* binv, double tin, int maxit, double inner_tol);
 
 void set_error(Handle& h, const std::string& msg);
 

@@ -1,0 +1,242 @@
+// mixed.cu -- mixed-precision Helmholtz solve: FP32 inner Jacobi-PCG inside an
+// FP64 defect-correction loop.
+//
+//   x = 0, r = f                                       (FP64)
+//   repeat:  rbn = sqrt(sum r^2 mult binv / vol)       (FP64, cggo's norm)
+//            stop when rbn <= tol (tin < 0: |tin| * rbn of r = f)
+//            e = PCG32(A, r / s) to inner_tol (relative; s = power of two
+//                near max|r|, so the FP32 iterate stays O(1))
+//            x += s * e                                (FP64)
+//            r = f - mask * dssum(A x)                 (FP64 operator)
+//
+// The inner solve stores G, D, the fields and the Jacobi diagonal in FP32 and
+// runs the same fused three-kernel iteration as the FP64 solver; its dot
+// products are accumulated with compensated FP32 sums per thread and FP64
+// across threads and blocks.  The outer residual, the solution and the
+// stopping test are FP64, so the result meets the same FP64 tolerance as the
+// plain solve.
+#include <algorithm>
+#include <cmath>
+
+#include "impl.cuh"
+
+namespace nekgpu {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kMaxOuter = 30;
+
+inline int blocks(int64_t n) {
+  int64_t b = (n + kThreads - 1) / kThreads;
+  return (int)std::min<int64_t>(std::max<int64_t>(b, 1), 152 * 8);
+}
+
+template <typename TO, typename TI>
+__global__ void cast_scale_kernel(TO* __restrict__ o, const TI* __restrict__ a, double sc,
+                                  int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    o[i] = (TO)((double)a[i] * sc);
+}
+
+__global__ void axpy_kernel(double* __restrict__ x, const float* __restrict__ e, double sc,
+                            int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    x[i] = fma(sc, (double)e[i], x[i]);
+}
+
+// r = f - mask*w ; partial sums of mult*binv*r^2
+__global__ void residual_kernel(double* __restrict__ r, const double* __restrict__ f,
+                                const double* __restrict__ w, const double* __restrict__ mask,
+                                const double* __restrict__ mult, const double* __restrict__ binv,
+                                int64_t n, double* __restrict__ partial) {
+  __shared__ double red[32];
+  double acc = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double ri = f[i] - mask[i] * w[i];
+    r[i] = ri;
+    acc += mult[i] * binv[i] * ri * ri;
+  }
+  acc = block_sum(acc, red);
+  if (threadIdx.x == 0) partial[blockIdx.x] = acc;
+}
+
+__global__ void norm_kernel(const double* __restrict__ r, const double* __restrict__ mult,
+                            const double* __restrict__ binv, int64_t n,
+                            double* __restrict__ partial) {
+  __shared__ double red[32];
+  double acc = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    acc += mult[i] * binv[i] * r[i] * r[i];
+  acc = block_sum(acc, red);
+  if (threadIdx.x == 0) partial[blockIdx.x] = acc;
+}
+
+double host_sum(Handle& h, int nb, int* st) {
+  std::vector<double> hp((size_t)nb);
+  if (cudaMemcpyAsync(hp.data(), h.red.ptr, nb * sizeof(double), cudaMemcpyDeviceToHost,
+                      h.stream) != cudaSuccess ||
+      cudaStreamSynchronize(h.stream) != cudaSuccess) {
+    *st = -3;
+    return 0.0;
+  }
+  double s = 0.0;
+  for (double v : hp) s += v;
+  return s;
+}
+
+int ensure_f32(Handle& h) {
+  Mesh& m = h.mesh;
+  if (m.has_f32) return 0;
+  const int64_t n = m.n;
+  if (cudaMalloc(&m.f32.G, 6 * n * sizeof(float)) != cudaSuccess ||
+      cudaMalloc(&m.f32.bm1, n * sizeof(float)) != cudaSuccess ||
+      cudaMalloc(&m.f32.D, m.nx1 * m.nx1 * sizeof(float)) != cudaSuccess) {
+    m.f32.release();
+    return -4;
+  }
+  count_launch();
+  cast_scale_kernel<float, double><<<blocks(6 * n), kThreads, 0, h.stream>>>(m.f32.G, m.f64.G, 1.0,
+                                                                            6 * n);
+  count_launch();
+  cast_scale_kernel<float, double><<<blocks(n), kThreads, 0, h.stream>>>(m.f32.bm1, m.f64.bm1, 1.0,
+                                                                        n);
+  count_launch();
+  cast_scale_kernel<float, double><<<1, kThreads, 0, h.stream>>>(m.f32.D, m.f64.D, 1.0,
+                                                                 m.nx1 * m.nx1);
+  if (cudaStreamSynchronize(h.stream) != cudaSuccess) return -3;
+  m.has_f32 = true;
+  return 0;
+}
+
+}  // namespace
+
+MixedResult mixed_solve(Handle& h, double* x, const double* f, const double* h1,
+                        const double* h2, const double* mask, const double* mult,
+                        const double* binv, double tin, int maxit, double inner_tol) {
+  MixedResult res;
+  Mesh& m = h.mesh;
+  const int64_t n = m.n;
+  cudaStream_t s = h.stream;
+  const int nb = blocks(n);
+  if ((res.status = ensure_f32(h))) {
+    set_error(h, "mixed: FP32 operator data allocation failed");
+    return res;
+  }
+  PcgWork<float>& wk = h.w32;
+  PcgWork<double>& w64 = h.w64;
+  if (wk.mask.ensure(n) || wk.mult.ensure(n) || wk.binv.ensure(n) || wk.x.ensure(n) ||
+      wk.f.ensure(n) || wk.d.ensure(n) || wk.h1.ensure(n) || wk.h2.ensure(n) || w64.r.ensure(n) ||
+      w64.w.ensure(n) || w64.d.ensure(n) || h.red.ensure(nb)) {
+    res.status = -4;
+    set_error(h, "mixed: device allocation failed");
+    return res;
+  }
+  Coef<double> c64;
+  if (detect_coef<double>(h, h1, h2, n, c64)) {
+    res.status = -3;
+    set_error(h, "mixed: coefficient scan failed");
+    return res;
+  }
+  Coef<float> c32;
+  c32.h1mode = c64.h1mode;
+  c32.h2mode = c64.h2mode;
+  c32.h1s = (float)c64.h1s;
+  c32.h2s = (float)c64.h2s;
+  auto cast = [&](float* o, const double* a, double sc) {
+    count_launch();
+    cast_scale_kernel<float, double><<<nb, kThreads, 0, s>>>(o, a, sc, n);
+  };
+  if (c64.h1mode) {
+    cast(wk.h1.ptr, h1, 1.0);
+    c32.h1 = wk.h1.ptr;
+  }
+  if (c64.h2mode == 2) {
+    cast(wk.h2.ptr, h2, 1.0);
+    c32.h2 = wk.h2.ptr;
+  }
+  cast(wk.mask.ptr, mask, 1.0);
+  cast(wk.mult.ptr, mult, 1.0);
+  cast(wk.binv.ptr, binv, 1.0);
+  // Jacobi diagonal once, in FP64, then FP32
+  if (setprec_f64(h, w64.d.ptr, c64)) {
+    res.status = -3;
+    set_error(h, "mixed: setprec failed");
+    return res;
+  }
+  cast(wk.d.ptr, w64.d.ptr, 1.0);
+  // x = 0, r = f
+  cudaMemsetAsync(x, 0, n * sizeof(double), s);
+  cudaMemcpyAsync(w64.r.ptr, f, n * sizeof(double), cudaMemcpyDeviceToDevice, s);
+  int st = 0;
+  count_launch();
+  norm_kernel<<<nb, kThreads, 0, s>>>(w64.r.ptr, mult, binv, n, h.red.ptr);
+  const double rbn0 = std::sqrt(host_sum(h, nb, &st) / m.vol);
+  if (st) {
+    res.status = st;
+    set_error(h, "mixed: reduction failed");
+    return res;
+  }
+  res.rbn0 = res.rbn2 = rbn0;
+  if (rbn0 == 0.0) return res;
+  if (!std::isfinite(rbn0)) {
+    res.status = -7;
+    set_error(h, "mixed: non-finite residual norm");
+    return res;
+  }
+  const double tol = tin < 0 ? std::fabs(tin) * rbn0 : std::fabs(tin);
+  double rbn = rbn0;
+  const bool exact = false;
+  for (int outer = 1; outer <= kMaxOuter; ++outer) {
+    if (rbn <= tol) break;
+    const double amax = device_absmax<double>(h, w64.r.ptr, n, &st);
+    if (st || amax == 0.0) break;
+    const double scale = std::ldexp(1.0, std::ilogb(amax));  // power of two: exact rescale
+    cast(wk.f.ptr, w64.r.ptr, 1.0 / scale);
+    PcgResult pr = pcg_solve<float>(h, m.f32, wk, wk.x.ptr, wk.f.ptr, c32, wk.mask.ptr,
+                                    wk.mult.ptr, wk.binv.ptr, -inner_tol, maxit, 0, exact,
+                                    wk.d.ptr);
+    if (pr.status && pr.status != -5) {
+      res.status = pr.status;
+      return res;
+    }
+    res.outer = outer;
+    res.inner += pr.niter;
+    count_launch();
+    axpy_kernel<<<nb, kThreads, 0, s>>>(x, wk.x.ptr, scale, n);
+    // r = f - mask * dssum(A x) in FP64
+    cudaError_t e = launch_axhelm<double, false>(m, m.f64, w64.w.ptr, x, c64, s);
+    if (e != cudaSuccess) {
+      res.status = -3;
+      set_error(h, std::string("mixed: axhelm ") + cudaGetErrorString(e));
+      return res;
+    }
+    gs_op<double>(m.gs, w64.w.ptr, 0, s);
+    count_launch();
+    residual_kernel<<<nb, kThreads, 0, s>>>(w64.r.ptr, f, w64.w.ptr, mask, mult, binv, n,
+                                            h.red.ptr);
+    const double rnew = std::sqrt(host_sum(h, nb, &st) / m.vol);
+    if (st || !std::isfinite(rnew)) {
+      res.status = st ? st : -7;
+      set_error(h, "mixed: non-finite outer residual");
+      return res;
+    }
+    if (rnew >= rbn) {  // no progress: FP32 inner solve cannot reduce further
+      rbn = rnew;
+      break;
+    }
+    rbn = rnew;
+  }
+  res.rbn2 = rbn;
+  if (!(rbn <= tol)) {
+    res.status = -5;
+    set_error(h, "mixed: outer defect correction did not reach the tolerance");
+  }
+  return res;
+}
+
+}  // namespace nekgpu

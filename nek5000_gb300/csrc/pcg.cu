@@ -246,6 +246,13 @@ __global__ void __launch_bounds__(kVecThreads)
     cg->counter[1] = 0u;
     const int iter = cg->iter + 1;
     cg->iter = iter;
+    if (iter > cg->maxiter) {
+      // the reference's loop has ended (do iter=1,niter): no further check,
+      // rbn2 stays the norm of the last checked iterate
+      cg->niter = cg->maxiter;
+      cg->done = 1;
+      return;
+    }
     cg->s1 = s1;
     cg->s2 = s2;
     cg->rtz2 = cg->rtz1;
@@ -260,9 +267,6 @@ __global__ void __launch_bounds__(kVecThreads)
       cg->done = 1;
     } else if (rbn2 <= cg->tol && (iter > 1 || cg->istep <= 5)) {
       cg->niter = iter - 1;
-      cg->done = 1;
-    } else if (iter > cg->maxiter) {
-      cg->niter = cg->maxiter;
       cg->done = 1;
     }
     cg->beta = (iter == 1) ? 0.0 : s1 / cg->rtz2;
@@ -407,9 +411,33 @@ static void launch_C(Handle& h, PcgWork<T>& wk, T* x, const T* mult, const T* bi
 }
 
 template <typename T>
+double device_absmax(Handle& h, const T* a, int64_t n, int* status) {
+  const int nb = vec_blocks(n);
+  *status = 0;
+  if (h.red.ensure(2 * (size_t)nb) != cudaSuccess) {
+    *status = -4;
+    return 0.0;
+  }
+  count_launch();
+  minmax_kernel<T><<<nb, kVecThreads, 0, h.stream>>>(a, n, h.red.ptr);
+  std::vector<double> hm(2 * (size_t)nb);
+  if (cudaMemcpyAsync(hm.data(), h.red.ptr, hm.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                      h.stream) != cudaSuccess ||
+      cudaStreamSynchronize(h.stream) != cudaSuccess) {
+    *status = -3;
+    return 0.0;
+  }
+  double m = 0.0;
+  for (int b = 0; b < nb; ++b) m = std::max(m, std::max(std::fabs(hm[2 * b]), std::fabs(hm[2 * b + 1])));
+  return m;
+}
+template double device_absmax<double>(Handle&, const double*, int64_t, int*);
+template double device_absmax<float>(Handle&, const float*, int64_t, int*);
+
+template <typename T>
 PcgResult pcg_solve(Handle& h, const OpData<T>& op, PcgWork<T>& wk, T* x, const T* f,
                     const Coef<T>& c, const T* mask, const T* mult, const T* binv, double tin,
-                    int maxiter, int istep, bool exact) {
+                    int maxiter, int istep, bool exact, const T* dpre) {
   PcgResult res;
   Mesh& m = h.mesh;
   const int64_t n = m.n;
@@ -426,19 +454,7 @@ PcgResult pcg_solve(Handle& h, const OpData<T>& op, PcgWork<T>& wk, T* x, const 
   }
   // fmax = glamax(f): an all-zero rhs returns x = 0 at once (hmholtz.f:699-701)
   int st = 0;
-  double fmax;
-  if constexpr (std::is_same<T, double>::value) {
-    fmax = device_sum(h, 3, f, nullptr, nullptr, n, &st);
-  } else {
-    DevBuf<double> tmp;
-    if (tmp.ensure(n)) {
-      res.status = -4;
-      return res;
-    }
-    count_launch();
-    cast_kernel<double, float><<<vec_blocks(n), kVecThreads, 0, s>>>(tmp.ptr, f, n);
-    fmax = device_sum(h, 3, tmp.ptr, nullptr, nullptr, n, &st);
-  }
+  const double fmax = device_absmax<T>(h, f, n, &st);
   if (st) {
     res.status = st;
     set_error(h, "pcg: reduction failed");
@@ -448,34 +464,15 @@ PcgResult pcg_solve(Handle& h, const OpData<T>& op, PcgWork<T>& wk, T* x, const 
   zero_kernel<T><<<vec_blocks(n), kVecThreads, 0, s>>>(x, n);
   if (fmax == 0.0) return res;
 
-  // Jacobi diagonal in FP64, cast for an FP32 solve
-  if constexpr (std::is_same<T, double>::value) {
+  // Jacobi diagonal: given by the caller (FP32 inner solves get the FP64
+  // diagonal cast once), or setprec in FP64 here.
+  if (dpre) {
+    if (dpre != wk.d.ptr)
+      cudaMemcpyAsync(wk.d.ptr, dpre, n * sizeof(T), cudaMemcpyDeviceToDevice, s);
+  } else if constexpr (std::is_same<T, double>::value) {
     st = setprec_f64(h, wk.d.ptr, c);
   } else {
-    DevBuf<double> d64, h1d, h2d;
-    Coef<double> c64;
-    c64.h1mode = c.h1mode;
-    c64.h2mode = c.h2mode;
-    c64.h1s = c.h1s;
-    c64.h2s = c.h2s;
-    if (d64.ensure(n) || (c.h1mode && h1d.ensure(n)) || (c.h2mode == 2 && h2d.ensure(n))) {
-      res.status = -4;
-      return res;
-    }
-    if (c.h1mode) {
-      count_launch();
-      cast_kernel<double, float><<<vec_blocks(n), kVecThreads, 0, s>>>(h1d.ptr, c.h1, n);
-      c64.h1 = h1d.ptr;
-    }
-    if (c.h2mode == 2) {
-      count_launch();
-      cast_kernel<double, float><<<vec_blocks(n), kVecThreads, 0, s>>>(h2d.ptr, c.h2, n);
-      c64.h2 = h2d.ptr;
-    }
-    st = setprec_f64(h, d64.ptr, c64);
-    count_launch();
-    cast_kernel<float, double><<<vec_blocks(n), kVecThreads, 0, s>>>(wk.d.ptr, d64.ptr, n);
-    cudaStreamSynchronize(s);
+    st = -1;
   }
   if (st) {
     res.status = st;
@@ -522,8 +519,6 @@ PcgResult pcg_solve(Handle& h, const OpData<T>& op, PcgWork<T>& wk, T* x, const 
   // the live launches and are summed (later ones found the solve converged
   // and returned at once).
   const int chunk = std::max(1, h.graph_chunk);
-  h.ms_axhelm = 0.0;
-  h.n_axhelm = 0;
   if (h.timing && h.ax_ev.size() < 2 * (size_t)chunk) {
     for (cudaEvent_t e : h.ax_ev) cudaEventDestroy(e);
     h.ax_ev.assign(2 * (size_t)chunk, nullptr);
@@ -582,9 +577,10 @@ PcgResult pcg_solve(Handle& h, const OpData<T>& op, PcgWork<T>& wk, T* x, const 
 
 template PcgResult pcg_solve<double>(Handle&, const OpData<double>&, PcgWork<double>&, double*,
                                      const double*, const Coef<double>&, const double*,
-                                     const double*, const double*, double, int, int, bool);
+                                     const double*, const double*, double, int, int, bool,
+                                     const double*);
 template PcgResult pcg_solve<float>(Handle&, const OpData<float>&, PcgWork<float>&, float*,
                                     const float*, const Coef<float>&, const float*, const float*,
-                                    const float*, double, int, int, bool);
+                                    const float*, double, int, int, bool, const float*);
 
 }  // namespace nekgpu

@@ -167,3 +167,27 @@ class NekGpu:
         del name
         fn = self._L.nekgpu_hmholtz_dev if _is_dev(u) else self._L.nekgpu_hmholtz
         return self._solve(fn, u, rhs, h1, h2, mask, mult, imsh, tli, maxit, isd, binv, maxcg)
+
+    def _solve_mixed(self, fn, a, b, h1, h2, mask, mult, imsh, tol, maxit, isd, binv, inner_tol):
+        no, ni, r0, r2 = _cint(0), _cint(0), _cdouble(0), _cdouble(0)
+        rc = fn(C.byref(self._h), _ptr(a), _ptr(b), _ptr(h1), _ptr(h2), _ptr(mask), _ptr(mult),
+                C.byref(_cint(imsh)), C.byref(_cdouble(tol)), C.byref(_cint(int(maxit))),
+                C.byref(_cint(isd)), _ptr(binv), C.byref(_cdouble(inner_tol)), C.byref(no),
+                C.byref(ni), C.byref(r0), C.byref(r2))
+        self._check(rc, allow=(_capi.ENOTCONV,))
+        return no.value, ni.value, r0.value, r2.value, rc
+
+    def cggo_mixed(self, x, f, h1, h2, mask, mult, imsh, tin, maxit, isd, binv, inner_tol=1e-5):
+        """FP32-inner / FP64-defect-correction form of cggo (device arrays).
+        Returns (outer steps, inner iterations, rbn0, rbn2, status)."""
+        if not _is_dev(x):
+            raise TypeError("cggo_mixed takes device arrays")
+        return self._solve_mixed(self._L.nekgpu_cggo_mixed_dev, x, f, h1, h2, mask, mult, imsh,
+                                 tin, maxit, isd, binv, inner_tol)
+
+    def hmholtz_mixed(self, name, u, rhs, h1, h2, mask, mult, imsh, tli, maxit, isd, binv,
+                      inner_tol=1e-5):
+        """hmholtz with the mixed-precision solve (host arrays)."""
+        del name
+        return self._solve_mixed(self._L.nekgpu_hmholtz_mixed, u, rhs, h1, h2, mask, mult, imsh,
+                                 tli, maxit, isd, binv, inner_tol)

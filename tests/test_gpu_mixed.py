@@ -1,0 +1,75 @@
+"""Mixed precision: FP32 inner PCG inside FP64 defect correction, against the
+FP64 oracle on the same seeded mesh and right-hand side.
+
+Pass criteria (per solve):
+  * the FP64 residual of the returned x, recomputed by the oracle's operator
+    (r = f - mask*dssum(A x), cggo's norm), is <= 1.05 * 1e-10 * rbn0;
+  * the error against the oracle's FP64 solution is reported and bounded by
+    1e-8 relative (both solutions satisfy the same 1e-10 residual bound; their
+    difference is the conditioning of A times that bound, not rounding).
+"""
+import numpy as np
+import pytest
+
+from conftest import rng_unit_vector
+
+pytestmark = pytest.mark.gpu
+
+
+def fp64_residual_norm(P, x, f, h1, h2):
+    ops = P["ops"]
+    w = ops.dssum(ops.axhelm(x, h1, h2)) * P["mask"]
+    r = f - w
+    return np.sqrt(np.sum(P["mult"] * P["binv"] * r * r) / np.sum(P["bm1"]))
+
+
+@pytest.mark.parametrize("case", [
+    dict(nx1=10, k=(3, 3, 3), periodic=(False, False, False), h2=0.0, seed=2),   # N=9 Poisson
+    dict(nx1=8, k=(3, 4, 3), periodic=(False, True, True), h2=10.0, seed=1),     # Helmholtz, periodic
+    dict(nx1=6, k=(2, 2, 2), periodic=(False, False, False), h2=1500.0, seed=3), # velocity-like h2
+])
+def test_mixed_meets_fp64_tolerance(gpu_lib, oracle, case):
+    torch = pytest.importorskip("torch")
+    kx, ky, kz = case["k"]
+    P = oracle.box_problem(case["nx1"], kx, ky, kz, periodic=case["periodic"],
+                           v=rng_unit_vector(case["seed"]))
+    n = P["n"]
+    rng = np.random.default_rng(case["seed"])
+    f = P["ops"].dssum(P["bm1"] * (P["ops"].dssum(rng.standard_normal(n)) * P["mult"])) * P["mask"]
+    h1, h2 = np.ones(n), np.full(n, case["h2"])
+    x_ref, it_ref, r0_ref, r2_ref = P["ops"].cggo(f, h1, h2, P["mask"], P["mult"], P["binv"], -1e-10,
+                                                  maxcg=10 ** 6)
+    lib = gpu_lib(0)
+    lib.setup(P["nx1"], P["nel"], P["D"], P["g"], P["bm1"], P["glo_num"])
+    dev = lambda a: torch.tensor(a, device="cuda")
+    x = torch.zeros(n, dtype=torch.float64, device="cuda")
+    outer, inner, r0, r2, rc = lib.cggo_mixed(x, dev(f), dev(h1), dev(h2), dev(P["mask"]),
+                                              dev(P["mult"]), 1, -1e-10, 10 ** 6, 1, dev(P["binv"]),
+                                              inner_tol=1e-5)
+    assert rc == 0, lib.last_error()
+    xs = x.cpu().numpy()
+    assert abs(r0 - r0_ref) <= 1e-12 * r0_ref
+    rn = fp64_residual_norm(P, xs, f, h1, h2)
+    assert rn <= 1.05e-10 * r0_ref, (rn / r0_ref, outer, inner)
+    err = np.linalg.norm(xs - x_ref) / np.linalg.norm(x_ref)
+    print(f"mixed: outer {outer} inner {inner} (FP64 cggo {it_ref}), rel. error vs FP64 oracle {err:.2e}")
+    assert err <= 1e-8
+    assert 2 <= outer <= 6
+
+
+def test_mixed_host_entry_point(gpu_lib, oracle):
+    P = oracle.box_problem(8, 2, 2, 2, v=rng_unit_vector(5))
+    n = P["n"]
+    rhs = P["bm1"] * (P["ops"].dssum(np.random.default_rng(5).uniform(-1, 1, n)) * P["mult"])
+    lib = gpu_lib(0)
+    lib.setup(P["nx1"], P["nel"], P["D"], P["g"], P["bm1"], P["glo_num"])
+    u = np.zeros(n)
+    r = rhs.copy()
+    h1, h2 = np.ones(n), np.zeros(n)
+    outer, inner, r0, r2, rc = lib.hmholtz_mixed("TEMP", u, r, h1, h2, P["mask"], P["mult"], 1,
+                                                 -1e-10, 10 ** 6, 1, P["binv"])
+    u_ref, rhs_ref, it_ref, r0_ref, _ = P["ops"].hmholtz(rhs, h1, h2, P["mask"], P["mult"],
+                                                         P["binv"], -1e-10, maxcg=10 ** 6)
+    assert rc == 0
+    assert np.array_equal(r, rhs_ref)
+    assert fp64_residual_norm(P, u, rhs_ref, h1, h2) <= 1.05e-10 * r0_ref
