@@ -52,6 +52,8 @@ extern "C" {
 #define NEKGPU_OPT_ISTEP 4   /* time-step index the reference's cggo sees; with
                                 istep <= 5 the first iteration may already stop
                                 (core/hmholtz.f:778)                              */
+#define NEKGPU_OPT_TMA 5     /* 1 (default): stage element blocks with bulk async
+                                copies where lx1 is even; 0: plain loads         */
 
 /* ---- life cycle ---------------------------------------------------------- */
 /* Create a handle on CUDA device *device.  Replaces the per-rank setup the

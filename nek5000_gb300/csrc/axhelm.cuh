@@ -45,6 +45,7 @@ struct AxArgs {
   const T* d;
   const CgScalars* cg;
   double* partial; // one per block
+  int* err;        // device flag: set if a bounded wait expired
 };
 
 template <int NX>

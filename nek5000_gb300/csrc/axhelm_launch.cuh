@@ -2,6 +2,7 @@
 // Included by one translation unit per precision so the instantiations
 // compile in parallel.
 #pragma once
+#include "axhelm_tma.cuh"
 #include "impl.cuh"
 
 namespace nekgpu {
@@ -25,8 +26,54 @@ static cudaError_t launch_ax_nx(const Mesh& m, const AxArgs<T>& a, int* nblocks,
   return cudaGetLastError();
 }
 
+// TMA-staged form: even lx1 (so one element's slice is a multiple of 16
+// bytes) and 16-byte aligned arrays.
+template <int NX, typename T, bool FUSED>
+static cudaError_t launch_tma_nx(const Mesh& m, const AxArgs<T>& a, int* nblocks, cudaStream_t s) {
+  constexpr int EPB = tma_epb<NX>();
+  const size_t smem = tma_smem_bytes<NX, T>(FUSED, a.h1mode, a.h2mode);
+  static bool configured = false;
+  if (!configured) {
+    const int maxb = (int)tma_smem_bytes<NX, T>(true, 1, 2);
+    cudaError_t e = cudaFuncSetAttribute(axhelm_tma_kernel<NX, T, FUSED>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, maxb);
+    if (e != cudaSuccess) return e;
+    cudaFuncSetAttribute(axhelm_tma_kernel<NX, T, FUSED>,
+                         cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    configured = true;
+  }
+  const int nb = (m.nel + EPB - 1) / EPB;
+  if (nblocks) *nblocks = nb;
+  count_launch();
+  axhelm_tma_kernel<NX, T, FUSED><<<nb, dim3(NX * NX, EPB), smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+inline bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
+
+template <typename T, bool FUSED>
+static bool tma_ok(const AxArgs<T>& a) {
+  bool ok = aligned16(a.u) && aligned16(a.G) && aligned16(a.D);
+  if (a.h2mode) ok = ok && aligned16(a.bm1);
+  if (a.h1mode == 1) ok = ok && aligned16(a.h1);
+  if (a.h2mode == 2) ok = ok && aligned16(a.h2);
+  if (FUSED) ok = ok && aligned16(a.r) && aligned16(a.d);
+  return ok;
+}
+
 template <typename T, bool EXACT, bool FUSED>
 static cudaError_t launch_ax(const Mesh& m, const AxArgs<T>& a, int* nblocks, cudaStream_t s) {
+  if (!EXACT && m.use_tma && tma_ok<T, FUSED>(a)) {
+    switch (m.nx1) {
+      case 2: return launch_tma_nx<2, T, FUSED>(m, a, nblocks, s);
+      case 4: return launch_tma_nx<4, T, FUSED>(m, a, nblocks, s);
+      case 6: return launch_tma_nx<6, T, FUSED>(m, a, nblocks, s);
+      case 8: return launch_tma_nx<8, T, FUSED>(m, a, nblocks, s);
+      case 10: return launch_tma_nx<10, T, FUSED>(m, a, nblocks, s);
+      case 12: return launch_tma_nx<12, T, FUSED>(m, a, nblocks, s);
+      default: break;
+    }
+  }
   switch (m.nx1) {
     case 2: return launch_ax_nx<2, T, EXACT, FUSED>(m, a, nblocks, s);
     case 3: return launch_ax_nx<3, T, EXACT, FUSED>(m, a, nblocks, s);
@@ -59,6 +106,7 @@ static AxArgs<T> make_args(const Mesh& m, const OpData<T>& op, T* au, const T* u
   a.h2mode = c.h2mode;
   a.D = op.D;
   a.nel = m.nel;
+  a.err = m.dev_err;
   return a;
 }
 

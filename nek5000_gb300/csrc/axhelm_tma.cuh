@@ -1,0 +1,252 @@
+// axhelm_tma.cuh -- the operator with TMA-staged element blocks.
+//
+// Same mathematics and contraction order as axhelm.cuh (core/hmholtz.f:72-259,
+// 3-D deformed path), organised for HBM bandwidth:
+//
+//  * one block owns EPB consecutive elements; since every array is
+//    element-major, their u (or p, r, d), G, bm1 and coefficient slices are
+//    each one contiguous range, staged into shared memory by a handful of
+//    1-D bulk asynchronous copies (cp.async.bulk) completing on one mbarrier
+//    -- every byte the block needs is in flight at once;
+//  * thread (i,j) of an element keeps the rows D(i,:), D(j,:) and the columns
+//    D(:,i), D(:,j) in registers; rows of the staged field are read as 8- or
+//    16-byte vectors (warp broadcasts), columns as conflict-free scalars;
+//  * the t-direction transposed contraction accumulates in registers.
+//
+// Valid when lx1^3 * sizeof(T) is a multiple of 16 bytes (even lx1) and the
+// arrays are 16-byte aligned; otherwise axhelm.cuh's kernel is used.
+#pragma once
+#include "axhelm.cuh"
+#include "tma.cuh"
+
+namespace nekgpu {
+
+template <int NX>
+__host__ __device__ constexpr int tma_epb() {
+  return (128 / (NX * NX)) > 0 ? (128 / (NX * NX)) : 1;
+}
+
+// Number of staged field slices (of EPB*P values) besides G and the work slabs.
+__host__ __device__ constexpr int tma_nslices(bool fused, int h1mode, int h2mode) {
+  return 1 + (fused ? 2 : 0) + (h2mode ? 1 : 0) + (h1mode == 1 ? 1 : 0) + (h2mode == 2 ? 1 : 0);
+}
+
+template <int NX, typename T>
+__host__ __device__ constexpr size_t tma_smem_bytes(bool fused, int h1mode, int h2mode) {
+  constexpr int P = NX * NX * NX;
+  return 64 /* mbarrier + pad */ + (size_t)NX * NX * sizeof(T) /* D */ +
+         (size_t)tma_epb<NX>() * P * sizeof(T) * (tma_nslices(fused, h1mode, h2mode) + 6 + 2);
+}
+
+template <typename T>
+struct Vec16;
+template <>
+struct Vec16<float> {
+  using type = float4;
+};
+template <>
+struct Vec16<double> {
+  using type = double2;
+};
+
+// Load NX consecutive values of T from shared memory with the widest aligned
+// vector width that NX*sizeof(T) allows.
+template <int NX, typename T>
+__device__ __forceinline__ void load_row(const T* __restrict__ p, T (&v)[NX]) {
+  if constexpr ((NX * sizeof(T)) % 16 == 0) {
+    using V = typename Vec16<T>::type;
+    constexpr int W = 16 / sizeof(T);
+#pragma unroll
+    for (int c = 0; c < NX / W; ++c) {
+      const V x = reinterpret_cast<const V*>(p)[c];
+      if constexpr (W == 4) {
+        v[4 * c] = x.x;
+        v[4 * c + 1] = x.y;
+        v[4 * c + 2] = x.z;
+        v[4 * c + 3] = x.w;
+      } else {
+        v[2 * c] = x.x;
+        v[2 * c + 1] = x.y;
+      }
+    }
+  } else if constexpr (sizeof(T) == 4 && (NX * sizeof(T)) % 8 == 0) {
+#pragma unroll
+    for (int c = 0; c < NX / 2; ++c) {
+      const float2 x = reinterpret_cast<const float2*>(p)[c];
+      v[2 * c] = x.x;
+      v[2 * c + 1] = x.y;
+    }
+  } else {
+#pragma unroll
+    for (int l = 0; l < NX; ++l) v[l] = p[l];
+  }
+}
+
+// Block sum of a per-thread value: warp sums in T, one FP64 value per warp.
+template <typename T>
+__device__ __forceinline__ double block_sum_warps(T v, double* scratch) {
+  v = warp_sum(v);
+  const int tid = threadIdx.x + blockDim.x * threadIdx.y;
+  const int nw = (blockDim.x * blockDim.y + 31) >> 5;
+  if ((tid & 31) == 0) scratch[tid >> 5] = (double)v;
+  __syncthreads();
+  double s = 0.0;
+  if (tid == 0)
+    for (int q = 0; q < nw; ++q) s += scratch[q];
+  return s;  // valid in thread 0
+}
+
+template <int NX, typename T, bool FUSED>
+__global__ void __launch_bounds__(NX* NX* tma_epb<NX>())
+    axhelm_tma_kernel(const AxArgs<T> a) {
+  constexpr int P = NX * NX * NX, NXY = NX * NX, EPB = tma_epb<NX>();
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  __shared__ double red[32];
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
+  T* sD = reinterpret_cast<T*>(smem_raw + 64);  // D[i][l] row-major
+  // staged slices, each EPB*P values, 16-byte aligned (P*sizeof(T) % 16 == 0)
+  T* base = reinterpret_cast<T*>(smem_raw + 64 + ((NX * NX * sizeof(T) + 15) / 16) * 16);
+  const int hb = a.h2mode ? 1 : 0, hh1 = a.h1mode == 1 ? 1 : 0, hh2 = a.h2mode == 2 ? 1 : 0;
+  T* sU = base;
+  T* sR = sU + EPB * P;
+  T* sDg = sR + (FUSED ? EPB * P : 0);
+  T* sB = sDg + (FUSED ? EPB * P : 0);
+  T* sH1 = sB + hb * EPB * P;
+  T* sH2 = sH1 + hh1 * EPB * P;
+  T* sG = sH2 + hh2 * EPB * P;
+  T* st1 = sG + 6 * EPB * P;
+  T* st2 = st1 + EPB * P;
+
+  if constexpr (FUSED) {
+    if (a.cg->done) return;
+  }
+  const int tid = threadIdx.x + NXY * threadIdx.y;
+  const int e0 = blockIdx.x * EPB;
+  const int ne = min(EPB, a.nel - e0);  // elements of this block
+  if (tid == 0) {
+    mbar_init(bar, 1);
+    mbar_fence_init();
+  }
+  for (int q = tid; q < NXY; q += NXY * EPB) sD[q] = a.D[q];
+  __syncthreads();
+  if (tid == 0) {
+    const uint32_t fb = (uint32_t)(ne * P * sizeof(T));
+    const size_t off = (size_t)e0 * P;
+    const uint32_t total = fb * (1 + (FUSED ? 2 : 0) + hb + hh1 + hh2 + 6);
+    mbar_expect_tx(bar, total);
+    bulk_g2s(sU, a.u + off, fb, bar);
+    if constexpr (FUSED) {
+      bulk_g2s(sR, a.r + off, fb, bar);
+      bulk_g2s(sDg, a.d + off, fb, bar);
+    }
+    if (hb) bulk_g2s(sB, a.bm1 + off, fb, bar);
+    if (hh1) bulk_g2s(sH1, a.h1 + off, fb, bar);
+    if (hh2) bulk_g2s(sH2, a.h2 + off, fb, bar);
+    bulk_g2s(sG, a.G + 6 * off, 6 * fb, bar);
+  }
+  // D rows / columns of this thread while the copies fly
+  const int i = threadIdx.x % NX, j = threadIdx.x / NX, el = threadIdx.y;
+  T Di[NX], Dj[NX], DTi[NX], DTj[NX];
+#pragma unroll
+  for (int l = 0; l < NX; ++l) {
+    Di[l] = a.D[i * NX + l];
+    Dj[l] = a.D[j * NX + l];
+    DTi[l] = a.D[l * NX + i];
+    DTj[l] = a.D[l * NX + j];
+  }
+  const bool ok = mbar_wait_bounded(bar, 0, a.err);
+  const bool act = ok && el < ne;
+  const int lo = el * P;  // element offset inside the staged slices
+  const size_t eo = (size_t)(e0 + (el < ne ? el : 0)) * P;
+
+  T beta = T(0);
+  if constexpr (FUSED) beta = (T)a.cg->beta;
+  T ru[NX];
+#pragma unroll
+  for (int k = 0; k < NX; ++k) {
+    const int pt = k * NXY + j * NX + i;
+    T v = act ? sU[lo + pt] : T(0);
+    if constexpr (FUSED) {
+      if (act) {
+        v = fma(beta, v, sR[lo + pt] * sDg[lo + pt]);  // add2s1: p = beta*p + r*d
+        sU[lo + pt] = v;
+        a.p[eo + pt] = v;
+      }
+    }
+    ru[k] = v;
+  }
+  __syncthreads();
+
+  T rau[NX];
+#pragma unroll
+  for (int m = 0; m < NX; ++m) rau[m] = T(0);
+  const T* gE = sG + 6 * lo;
+#pragma unroll
+  for (int k = 0; k < NX; ++k) {
+    const T* slab = sU + lo + k * NXY;
+    T row[NX], dk[NX];
+    load_row<NX, T>(slab + j * NX, row);
+    load_row<NX, T>(sD + k * NX, dk);
+    T ur = Di[0] * row[0];
+#pragma unroll
+    for (int l = 1; l < NX; ++l) ur = fma(Di[l], row[l], ur);
+    T us = slab[i] * Dj[0];
+#pragma unroll
+    for (int l = 1; l < NX; ++l) us = fma(slab[l * NX + i], Dj[l], us);
+    T ut = ru[0] * dk[0];
+#pragma unroll
+    for (int l = 1; l < NX; ++l) ut = fma(ru[l], dk[l], ut);
+    const int pt = k * NXY + j * NX + i;
+    const T g1 = gE[pt], g2 = gE[P + pt], g3 = gE[2 * P + pt], g4 = gE[3 * P + pt],
+            g5 = gE[4 * P + pt], g6 = gE[5 * P + pt];
+    const T h = hh1 ? sH1[lo + pt] : a.h1s;
+    T t1 = ur * g1, t2 = us * g2, t3 = ut * g3;
+    t1 = fma(us, g4, t1);
+    t1 = fma(ut, g5, t1);
+    t2 = fma(ur, g4, t2);
+    t2 = fma(ut, g6, t2);
+    t3 = fma(ur, g5, t3);
+    t3 = fma(us, g6, t3);
+    st1[lo + pt] = t1 * h;
+    st2[lo + pt] = t2 * h;
+    t3 *= h;
+#pragma unroll
+    for (int m = 0; m < NX; ++m) rau[m] = (k == 0) ? t3 * dk[m] : fma(t3, dk[m], rau[m]);
+  }
+  __syncthreads();
+
+  T dot = T(0);
+#pragma unroll
+  for (int k = 0; k < NX; ++k) {
+    const T* s1 = st1 + lo + k * NXY;
+    const T* s2 = st2 + lo + k * NXY;
+    T row[NX];
+    load_row<NX, T>(s1 + j * NX, row);
+    T tm1 = DTi[0] * row[0];
+#pragma unroll
+    for (int l = 1; l < NX; ++l) tm1 = fma(DTi[l], row[l], tm1);
+    T tm2 = s2[i] * DTj[0];
+#pragma unroll
+    for (int l = 1; l < NX; ++l) tm2 = fma(s2[l * NX + i], DTj[l], tm2);
+    T s = (tm1 + tm2) + rau[k];
+    const int pt = k * NXY + j * NX + i;
+    if (act) {
+      if (hb) {
+        const T hv = hh2 ? sH2[lo + pt] : a.h2s;
+        s = fma(hv * sB[lo + pt], ru[k], s);
+      }
+      a.au[eo + pt] = s;
+      if constexpr (FUSED) {
+        if (i > 0 && i < NX - 1 && j > 0 && j < NX - 1 && k > 0 && k < NX - 1)
+          dot = fma(s, ru[k], dot);
+      }
+    }
+  }
+  if constexpr (FUSED) {
+    const double bsum = block_sum_warps(dot, red);
+    if (tid == 0) a.partial[blockIdx.x] = bsum;
+  }
+  if (tid == 0 && ok) mbar_inval(bar);
+}
+
+}  // namespace nekgpu

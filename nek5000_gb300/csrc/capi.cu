@@ -227,6 +227,8 @@ int nekgpu_finalize(int64_t* handle) {
   gs_free(H->mesh.gs);
   H->mesh.f64.release();
   H->mesh.f32.release();
+  cudaFree(H->mesh.dev_err);
+  for (cudaEvent_t e : H->ax_ev) cudaEventDestroy(e);
   cudaFree(H->cg);
   cudaFreeHost(H->cg_host);
   cudaFree(H->flag);
@@ -262,6 +264,7 @@ int nekgpu_set_option(const int64_t* handle, const int* key, const int* value) {
       H->graph_chunk = *value;
       break;
     case NEKGPU_OPT_ISTEP: H->istep = *value; break;
+    case NEKGPU_OPT_TMA: H->mesh.use_tma = (*value != 0); break;
     default: return fail(H, NEKGPU_EINVAL, "unknown option");
   }
   return NEKGPU_OK;
@@ -317,6 +320,9 @@ int nekgpu_setup(const int64_t* handle, const int* lx1, const int* nel, const do
   double vol = 0.0;
   for (int64_t i = 0; i < n; ++i) vol = vol + bm1[i];
   m.vol = vol;
+  if (!m.dev_err && cudaMalloc(&m.dev_err, sizeof(int)) != cudaSuccess)
+    return fail(H, NEKGPU_ENOMEM, "flag allocation failed");
+  cudaMemset(m.dev_err, 0, sizeof(int));
   std::string err;
   int rc = gs_setup(m.gs, glo_num, n, err);
   if (rc) return fail(H, rc == -4 ? NEKGPU_ENOMEM : NEKGPU_EINVAL, err);

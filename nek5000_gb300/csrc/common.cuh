@@ -52,6 +52,48 @@ __device__ __forceinline__ T block_sum(T v, T* scratch) {
   return t;
 }
 
+// ---- reductions with one FP64 value per warp ---------------------------------
+// Compensated (TwoSum) accumulator in field precision.  For float, the
+// per-thread sums and the warp tree stay in FP32 with an error term, and only
+// the warp result is widened to FP64; on this GPU FP64 issue is 64x slower
+// than FP32, so FP64 work per point is avoided in the FP32 kernels.
+template <typename T>
+struct CompAcc {
+  T s = T(0), c = T(0);
+  __device__ __forceinline__ void add(T v) {
+    const T t = s + v;
+    const T bp = t - s;
+    c += (s - (t - bp)) + (v - bp);
+    s = t;
+  }
+  __device__ __forceinline__ void add(const CompAcc& o) {
+    add(o.s);
+    c += o.c;
+  }
+};
+
+// Sum of CompAcc over the block, valid in thread 0.  `scratch`: 32 doubles.
+template <typename T>
+__device__ __forceinline__ double block_sum_comp(CompAcc<T> a, double* scratch) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    CompAcc<T> b;
+    b.s = __shfl_xor_sync(0xffffffffu, a.s, o);
+    b.c = __shfl_xor_sync(0xffffffffu, a.c, o);
+    a.add(b);
+  }
+  const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+  const int nw = (blockDim.x * blockDim.y * blockDim.z + 31) >> 5;
+  __syncthreads();
+  if ((tid & 31) == 0) scratch[tid >> 5] = (double)a.s + (double)a.c;
+  __syncthreads();
+  double r = 0.0;
+  if (tid == 0)
+    for (int q = 0; q < nw; ++q) r += scratch[q];
+  __syncthreads();
+  return r;
+}
+
 // Scalars of one PCG solve, resident on the device (no host round trip per
 // iteration).  All FP64, whatever the field precision.
 struct CgScalars {

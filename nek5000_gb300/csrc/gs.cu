@@ -28,23 +28,23 @@ __global__ void gs_op_kernel(T* __restrict__ u, const int* __restrict__ start,
 template <typename T>
 __global__ void gs_cg_kernel(T* __restrict__ w, const T* __restrict__ p,
                              const int* __restrict__ start, const int* __restrict__ idx, int nseg,
-                             const T* __restrict__ segmask, const double* __restrict__ segmsum,
+                             const T* __restrict__ segmask, const T* __restrict__ segmsum,
                              CgScalars* cg, const double* __restrict__ partialA, int nA,
                              double* __restrict__ partialB) {
   __shared__ double red[32];
   __shared__ int am_last;
   if (cg->done) return;
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  double dot = 0.0;
+  CompAcc<T> acc;
   if (s < nseg) {
     const int a = start[s], b = start[s + 1];
     T t = w[idx[a]];
     for (int c = a + 1; c < b; ++c) t = t + w[idx[c]];
     t = t * segmask[s];
     for (int c = a; c < b; ++c) w[idx[c]] = t;
-    dot = (double)t * (double)p[idx[a]] * segmsum[s];
+    acc.add(t * p[idx[a]] * segmsum[s]);
   }
-  dot = block_sum(dot, red);
+  const double dot = block_sum_comp(acc, red);
   if (threadIdx.x == 0) {
     partialB[blockIdx.x] = dot;
     __threadfence();
@@ -55,12 +55,12 @@ __global__ void gs_cg_kernel(T* __restrict__ w, const T* __restrict__ p,
   if (!am_last) return;
   // Last block: rho = interior partials (fused axhelm) + boundary partials,
   // each summed in a fixed order.
-  double acc = 0.0;
-  for (int q = threadIdx.x; q < nA; q += blockDim.x) acc += __ldcg(partialA + q);
-  double rhoA = block_sum(acc, red);
-  acc = 0.0;
-  for (int q = threadIdx.x; q < (int)gridDim.x; q += blockDim.x) acc += __ldcg(partialB + q);
-  double rhoB = block_sum(acc, red);
+  double pa = 0.0;
+  for (int q = threadIdx.x; q < nA; q += blockDim.x) pa += __ldcg(partialA + q);
+  const double rhoA = block_sum(pa, red);
+  double pb = 0.0;
+  for (int q = threadIdx.x; q < (int)gridDim.x; q += blockDim.x) pb += __ldcg(partialB + q);
+  const double rhoB = block_sum(pb, red);
   if (threadIdx.x == 0) {
     const double rho = rhoA + rhoB;
     cg->rho = rho;
@@ -73,7 +73,7 @@ template <typename T>
 __global__ void gs_cg_weights_kernel(const int* __restrict__ start, const int* __restrict__ idx,
                                      int nseg, const T* __restrict__ mask,
                                      const T* __restrict__ mult, T* __restrict__ segmask,
-                                     double* __restrict__ segmsum, int* nonuniform) {
+                                     T* __restrict__ segmsum, int* nonuniform) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nseg) return;
   const int a = start[s], b = start[s + 1];
@@ -84,7 +84,7 @@ __global__ void gs_cg_weights_kernel(const int* __restrict__ start, const int* _
     ms += (double)mult[idx[c]];
   }
   segmask[s] = m0;
-  segmsum[s] = ms;
+  segmsum[s] = (T)ms;
 }
 
 }  // namespace
@@ -161,7 +161,7 @@ void gs_op(const GsMaps& gs, T* u, int op, cudaStream_t s) {
 }
 
 template <typename T>
-void gs_cg(const GsMaps& gs, T* w, const T* p, const T* segmask, const double* segmsum,
+void gs_cg(const GsMaps& gs, T* w, const T* p, const T* segmask, const T* segmsum,
            CgScalars* cg, double* partialA, int nA, double* partialB, cudaStream_t s) {
   const int nb = std::max(gs_cg_blocks(gs), 1);
   count_launch();
@@ -170,7 +170,7 @@ void gs_cg(const GsMaps& gs, T* w, const T* p, const T* segmask, const double* s
 }
 
 template <typename T>
-void gs_cg_weights(const GsMaps& gs, const T* mask, const T* mult, T* segmask, double* segmsum,
+void gs_cg_weights(const GsMaps& gs, const T* mask, const T* mult, T* segmask, T* segmsum,
                    int* nonuniform, cudaStream_t s) {
   if (gs.nbseg == 0) return;
   count_launch();
@@ -182,11 +182,11 @@ template void gs_op<double>(const GsMaps&, double*, int, cudaStream_t);
 template void gs_op<float>(const GsMaps&, float*, int, cudaStream_t);
 template void gs_cg<double>(const GsMaps&, double*, const double*, const double*, const double*,
                             CgScalars*, double*, int, double*, cudaStream_t);
-template void gs_cg<float>(const GsMaps&, float*, const float*, const float*, const double*,
+template void gs_cg<float>(const GsMaps&, float*, const float*, const float*, const float*,
                            CgScalars*, double*, int, double*, cudaStream_t);
 template void gs_cg_weights<double>(const GsMaps&, const double*, const double*, double*, double*,
                                     int*, cudaStream_t);
-template void gs_cg_weights<float>(const GsMaps&, const float*, const float*, float*, double*,
+template void gs_cg_weights<float>(const GsMaps&, const float*, const float*, float*, float*,
                                    int*, cudaStream_t);
 
 }  // namespace nekgpu

@@ -44,14 +44,14 @@ void gs_op(const GsMaps& gs, T* u, int op, cudaStream_t s);
 // partials to the interior partials left by the fused axhelm (nA of them)
 // and sets rho, alpha = rtz1/rho.
 template <typename T>
-void gs_cg(const GsMaps& gs, T* w, const T* p, const T* segmask, const double* segmsum,
+void gs_cg(const GsMaps& gs, T* w, const T* p, const T* segmask, const T* segmsum,
            CgScalars* cg, double* partialA, int nA, double* partialB, cudaStream_t s);
 
 // Per-segment mask value (mask at the first copy) and sum of mult over the
 // copies, for the bound maps.  Returns via `nonuniform` (device int) whether
 // any group has copies with different mask values.
 template <typename T>
-void gs_cg_weights(const GsMaps& gs, const T* mask, const T* mult, T* segmask, double* segmsum,
+void gs_cg_weights(const GsMaps& gs, const T* mask, const T* mult, T* segmask, T* segmsum,
                    int* nonuniform, cudaStream_t s);
 
 constexpr int kGsThreads = 256;

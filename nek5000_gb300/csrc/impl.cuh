@@ -54,6 +54,8 @@ struct Mesh {
   bool has_f32 = false;
   GsMaps gs;
   double vol = 0.0;  // glsum(bm1) (core/coef.f:1181)
+  int* dev_err = nullptr;  // device flag raised by a kernel whose bounded wait expired
+  bool use_tma = true;     // TMA-staged operator where lx1 and alignment allow
   std::vector<double> h_D;  // lx1*lx1 row-major (host copy)
 };
 
@@ -69,8 +71,7 @@ struct Coef {
 // Work space of one PCG precision.
 template <typename T>
 struct PcgWork {
-  DevBuf<T> r, w, p, d, mult, binv, mask, segmask, x, f, h1, h2;
-  DevBuf<double> segmsum;
+  DevBuf<T> r, w, p, d, mult, binv, mask, segmask, segmsum, x, f, h1, h2;
 };
 
 struct Handle {

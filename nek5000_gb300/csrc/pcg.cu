@@ -29,33 +29,6 @@ inline int vec_blocks(int64_t n) {
   return (int)std::min<int64_t>(std::max<int64_t>(b, 1), 152 * 8);
 }
 
-// ---- compensated accumulation for FP32 partial sums -------------------------
-struct Acc32 {
-  float s = 0.f, c = 0.f;
-  __device__ __forceinline__ void add(float v) {  // TwoSum-compensated
-    const float t = s + v;
-    const float bp = t - s;
-    c += (s - (t - bp)) + (v - bp);
-    s = t;
-  }
-  __device__ __forceinline__ double value() const { return (double)s + (double)c; }
-};
-struct Acc64 {
-  double s = 0.0;
-  __device__ __forceinline__ void add(double v) { s += v; }
-  __device__ __forceinline__ double value() const { return s; }
-};
-template <typename T>
-struct AccOf;
-template <>
-struct AccOf<float> {
-  using type = Acc32;
-};
-template <>
-struct AccOf<double> {
-  using type = Acc64;
-};
-
 // ---- min/max of h1 and h2 (uniformity detection) ---------------------------
 template <typename T>
 __global__ void minmax_kernel(const T* __restrict__ a, int64_t n, double* out) {
@@ -203,7 +176,7 @@ __global__ void __launch_bounds__(kVecThreads)
   __shared__ int am_last;
   if (cg->done) return;
   const T alpha = FIRST ? T(0) : (T)cg->alpha;
-  typename AccOf<T>::type a1, a2;
+  CompAcc<T> a1, a2;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     T ri = r[i];
@@ -224,8 +197,8 @@ __global__ void __launch_bounds__(kVecThreads)
       a2.add(m * binv[i] * ri * ri);
     }
   }
-  const double b1 = block_sum(a1.value(), red);
-  const double b2 = block_sum(a2.value(), red);
+  const double b1 = block_sum_comp(a1, red);
+  const double b2 = block_sum_comp(a2, red);
   if (threadIdx.x == 0) {
     partial[blockIdx.x] = b1;
     partial[gridDim.x + blockIdx.x] = b2;

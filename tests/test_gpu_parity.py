@@ -92,15 +92,21 @@ def test_axhelm_exact_bitwise_all_orders(gpu_lib, oracle, nx1):
         assert np.array_equal(au, P["ops"].axhelm(u, h1, h2))
 
 
-def test_axhelm_fma_within_tolerance(gpu_lib, oracle, cfg1):
-    P = cfg1
+@pytest.mark.parametrize("tma", [1, 0])
+@pytest.mark.parametrize("nx1", [2, 3, 4, 6, 8, 9, 10, 12])
+def test_axhelm_fma_within_tolerance(gpu_lib, oracle, nx1, tma):
+    """Default (fused multiply-add) operator, TMA-staged (even lx1) or plain loads."""
+    P = oracle.box_problem(nx1, 3, 2, 2, v=rng_unit_vector(20 + nx1))
     lib = _setup(gpu_lib, P)
+    lib.set_option(5, tma)
     n = P["n"]
-    u = np.random.default_rng(11).standard_normal(n)
-    h1, h2 = np.ones(n), np.full(n, 10.0)
-    au = np.zeros(n)
-    lib.axhelm(au, u, h1, h2)
-    assert rel(au, P["ops"].axhelm(u, h1, h2)) < 1e-13
+    rng = np.random.default_rng(11)
+    u = rng.standard_normal(n)
+    for h1, h2 in ((np.ones(n), np.zeros(n)), (np.ones(n), np.full(n, 10.0)),
+                   (np.exp(0.3 * rng.standard_normal(n)), rng.uniform(0, 5, n))):
+        au = np.zeros(n)
+        lib.axhelm(au, u, h1, h2)
+        assert rel(au, P["ops"].axhelm(u, h1, h2)) < 1e-13
 
 
 def test_axhelm_device_path_equals_host_path(gpu_lib, oracle, cfg1):
