@@ -63,7 +63,9 @@ static bool tma_ok(const AxArgs<T>& a) {
 
 template <typename T, bool EXACT, bool FUSED>
 static cudaError_t launch_ax(const Mesh& m, const AxArgs<T>& a, int* nblocks, cudaStream_t s) {
-  if (!EXACT && m.use_tma && tma_ok<T, FUSED>(a)) {
+  // FP64 is bound by the FP64 pipe, where the plain-load kernel (D in shared
+  // memory, higher occupancy) is faster; the TMA form serves FP32.
+  if (!EXACT && sizeof(T) == 4 && m.use_tma && tma_ok<T, FUSED>(a)) {
     switch (m.nx1) {
       case 2: return launch_tma_nx<2, T, FUSED>(m, a, nblocks, s);
       case 4: return launch_tma_nx<4, T, FUSED>(m, a, nblocks, s);

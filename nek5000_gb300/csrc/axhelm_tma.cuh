@@ -38,17 +38,6 @@ __host__ __device__ constexpr size_t tma_smem_bytes(bool fused, int h1mode, int 
          (size_t)tma_epb<NX>() * P * sizeof(T) * (tma_nslices(fused, h1mode, h2mode) + 6 + 2);
 }
 
-template <typename T>
-struct Vec16;
-template <>
-struct Vec16<float> {
-  using type = float4;
-};
-template <>
-struct Vec16<double> {
-  using type = double2;
-};
-
 // Load NX consecutive values of T from shared memory with the widest aligned
 // vector width that NX*sizeof(T) allows.
 template <int NX, typename T>

@@ -72,6 +72,14 @@ struct CompAcc {
   }
 };
 
+// FP64 fields need no compensation: plain accumulation (FP64 issue is scarce).
+template <>
+struct CompAcc<double> {
+  double s = 0.0, c = 0.0;
+  __device__ __forceinline__ void add(double v) { s += v; }
+  __device__ __forceinline__ void add(const CompAcc& o) { s += o.s; }
+};
+
 // Sum of CompAcc over the block, valid in thread 0.  `scratch`: 32 doubles.
 template <typename T>
 __device__ __forceinline__ double block_sum_comp(CompAcc<T> a, double* scratch) {
@@ -85,13 +93,35 @@ __device__ __forceinline__ double block_sum_comp(CompAcc<T> a, double* scratch) 
   const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
   const int nw = (blockDim.x * blockDim.y * blockDim.z + 31) >> 5;
   __syncthreads();
-  if ((tid & 31) == 0) scratch[tid >> 5] = (double)a.s + (double)a.c;
+  if ((tid & 31) == 0) scratch[tid >> 5] = (double)a.s + (double)a.c;  // c == 0 for FP64
   __syncthreads();
   double r = 0.0;
   if (tid == 0)
     for (int q = 0; q < nw; ++q) r += scratch[q];
   __syncthreads();
   return r;
+}
+
+// 16-byte vector of T, loaded / stored as one access.
+template <typename T>
+struct Vec16;
+template <>
+struct Vec16<float> {
+  using type = float4;
+};
+template <>
+struct Vec16<double> {
+  using type = double2;
+};
+template <typename T>
+__device__ __forceinline__ void ld16(T* v, const T* base, int64_t iv) {
+  using V = typename Vec16<T>::type;
+  *reinterpret_cast<V*>(v) = reinterpret_cast<const V*>(base)[iv];
+}
+template <typename T>
+__device__ __forceinline__ void st16(T* base, const T* v, int64_t iv) {
+  using V = typename Vec16<T>::type;
+  reinterpret_cast<V*>(base)[iv] = *reinterpret_cast<const V*>(v);
 }
 
 // Scalars of one PCG solve, resident on the device (no host round trip per

@@ -125,6 +125,26 @@ int gs_setup(GsMaps& gs, const int64_t* glo_num, int64_t n, std::string& err) {
   gs.nbidx = (int)bix.size();
   gs.h_start.assign(st.begin(), st.end());
   gs.h_idx.assign(ix.begin(), ix.end());
+  // The PCG-form maps are processed in order of each group's first local
+  // index: neighbouring threads then gather and scatter within the same few
+  // elements (the order of groups does not change any group's sum).
+  {
+    const size_t ns = bst.size() - 1;
+    std::vector<int> ord(ns);
+    std::iota(ord.begin(), ord.end(), 0);
+    std::stable_sort(ord.begin(), ord.end(),
+                     [&](int a, int b) { return bix[bst[a]] < bix[bst[b]]; });
+    std::vector<int> nst, nix;
+    nst.reserve(bst.size());
+    nix.reserve(bix.size());
+    for (int g : ord) {
+      nst.push_back((int)nix.size());
+      for (int c = bst[g]; c < bst[g + 1]; ++c) nix.push_back(bix[c]);
+    }
+    nst.push_back((int)nix.size());
+    bst.swap(nst);
+    bix.swap(nix);
+  }
   auto up = [&](int** dst, const std::vector<int>& v) -> bool {
     size_t bytes = std::max<size_t>(v.size(), 1) * sizeof(int);
     if (cudaMalloc(dst, bytes) != cudaSuccess) return false;

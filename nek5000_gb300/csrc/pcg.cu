@@ -167,6 +167,28 @@ __global__ void sum_kernel(int kind, const double* __restrict__ a, const double*
 
 // ---- PCG update / convergence kernel ---------------------------------------
 template <typename T, bool EXACT, bool FIRST>
+struct UpdatePoint {
+  // x += alpha p ; r -= alpha w ; z = r d ; s1 += z r mult ; s2 += mult binv r r
+  __device__ __forceinline__ static void run(T& x, T& r, T p, T w, T d, T m, T b, T alpha,
+                                             CompAcc<T>& a1, CompAcc<T>& a2) {
+    if (!FIRST) {
+      x = madd<EXACT>(alpha, p, x);   // add2s2(x,p,alpha)   (hmholtz.f:804)
+      r = madd<EXACT>(-alpha, w, r);  // add2s2(r,w,-alpha)  (hmholtz.f:805)
+    }
+    if (EXACT) {
+      const T z = mul_x(r, d);                         // col3 (:730)
+      a1.add(mul_x(mul_x(z, r), m));                   // vlsc3 (:754)
+      a2.add(mul_x(mul_x(mul_x(m, b), r), r));         // vlsc32 (:758, :848)
+    } else {
+      const T z = r * d;
+      a1.add(z * r * m);
+      a2.add(m * b * r * r);
+    }
+  }
+};
+
+// VEC: 16-byte vector accesses (all seven arrays 16-byte aligned).
+template <typename T, bool EXACT, bool FIRST, bool VEC>
 __global__ void __launch_bounds__(kVecThreads)
     cg_update_kernel(T* __restrict__ x, T* __restrict__ r, const T* __restrict__ p,
                      const T* __restrict__ w, const T* __restrict__ d,
@@ -177,24 +199,35 @@ __global__ void __launch_bounds__(kVecThreads)
   if (cg->done) return;
   const T alpha = FIRST ? T(0) : (T)cg->alpha;
   CompAcc<T> a1, a2;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    T ri = r[i];
+  using P = UpdatePoint<T, EXACT, FIRST>;
+  const int64_t gtid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  constexpr int W = 16 / sizeof(T);
+  const int64_t nv = VEC ? n / W : 0;
+  for (int64_t iv = gtid; iv < nv; iv += stride) {
+    T xx[W], rr[W], pp[W], ww[W], dd[W], mm[W], bb[W];
+    ld16(rr, r, iv);
+    ld16(dd, d, iv);
+    ld16(mm, mult, iv);
+    ld16(bb, binv, iv);
     if (!FIRST) {
-      // add2s2(x,p,alpha) ; add2s2(r,w,-alpha)   (hmholtz.f:804-805)
-      x[i] = madd<EXACT>(alpha, p[i], x[i]);
-      ri = madd<EXACT>(-alpha, w[i], ri);
-      r[i] = ri;
+      ld16(xx, x, iv);
+      ld16(pp, p, iv);
+      ld16(ww, w, iv);
     }
-    const T m = mult[i];
-    if (EXACT) {
-      const T z = mul_x(ri, d[i]);                          // col3 (:730)
-      a1.add(mul_x(mul_x(z, ri), m));                       // vlsc3 (:754)
-      a2.add(mul_x(mul_x(mul_x(m, binv[i]), ri), ri));      // vlsc32 (:758, :848)
-    } else {
-      const T z = ri * d[i];
-      a1.add(z * ri * m);
-      a2.add(m * binv[i] * ri * ri);
+#pragma unroll
+    for (int q = 0; q < W; ++q) P::run(xx[q], rr[q], pp[q], ww[q], dd[q], mm[q], bb[q], alpha, a1, a2);
+    if (!FIRST) {
+      st16(x, xx, iv);
+      st16(r, rr, iv);
+    }
+  }
+  for (int64_t i = nv * W + gtid; i < n; i += stride) {
+    T xi = FIRST ? T(0) : x[i], ri = r[i];
+    P::run(xi, ri, FIRST ? T(0) : p[i], FIRST ? T(0) : w[i], d[i], mult[i], binv[i], alpha, a1, a2);
+    if (!FIRST) {
+      x[i] = xi;
+      r[i] = ri;
     }
   }
   const double b1 = block_sum_comp(a1, red);
@@ -376,8 +409,17 @@ static void launch_C(Handle& h, PcgWork<T>& wk, T* x, const T* mult, const T* bi
                      bool first) {
   const int64_t n = h.mesh.n;
   const int nb = vec_blocks(n);
-  auto kern = exact ? (first ? cg_update_kernel<T, true, true> : cg_update_kernel<T, true, false>)
-                    : (first ? cg_update_kernel<T, false, true> : cg_update_kernel<T, false, false>);
+  auto al = [](const void* q) { return ((uintptr_t)q & 15u) == 0; };
+  const bool vec = al(x) && al(wk.r.ptr) && al(wk.p.ptr) && al(wk.w.ptr) && al(wk.d.ptr) &&
+                   al(mult) && al(binv);
+  auto kern = vec ? (exact ? (first ? cg_update_kernel<T, true, true, true>
+                                    : cg_update_kernel<T, true, false, true>)
+                           : (first ? cg_update_kernel<T, false, true, true>
+                                    : cg_update_kernel<T, false, false, true>))
+                  : (exact ? (first ? cg_update_kernel<T, true, true, false>
+                                    : cg_update_kernel<T, true, false, false>)
+                           : (first ? cg_update_kernel<T, false, true, false>
+                                    : cg_update_kernel<T, false, false, false>));
   count_launch();
   kern<<<nb, kVecThreads, 0, h.stream>>>(x, wk.r.ptr, wk.p.ptr, wk.w.ptr, wk.d.ptr, mult, binv, n,
                                          h.cg, h.partialC.ptr);
