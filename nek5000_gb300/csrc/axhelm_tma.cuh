@@ -31,11 +31,14 @@ __host__ __device__ constexpr int tma_nslices(bool fused, int h1mode, int h2mode
   return 1 + (fused ? 2 : 0) + (h2mode ? 1 : 0) + (h1mode == 1 ? 1 : 0) + (h2mode == 2 ? 1 : 0);
 }
 
+// The fused form reuses the r and d slices (consumed by the p update) as the
+// two work slabs; the plain form needs two more.
 template <int NX, typename T>
 __host__ __device__ constexpr size_t tma_smem_bytes(bool fused, int h1mode, int h2mode) {
   constexpr int P = NX * NX * NX;
   return 64 /* mbarrier + pad */ + (size_t)NX * NX * sizeof(T) /* D */ +
-         (size_t)tma_epb<NX>() * P * sizeof(T) * (tma_nslices(fused, h1mode, h2mode) + 6 + 2);
+         (size_t)tma_epb<NX>() * P * sizeof(T) *
+             (tma_nslices(fused, h1mode, h2mode) + 6 + (fused ? 0 : 2));
 }
 
 // Load NX consecutive values of T from shared memory with the widest aligned
@@ -103,8 +106,8 @@ __global__ void __launch_bounds__(NX* NX* tma_epb<NX>())
   T* sH1 = sB + hb * EPB * P;
   T* sH2 = sH1 + hh1 * EPB * P;
   T* sG = sH2 + hh2 * EPB * P;
-  T* st1 = sG + 6 * EPB * P;
-  T* st2 = st1 + EPB * P;
+  T* st1 = FUSED ? sR : sG + 6 * EPB * P;
+  T* st2 = FUSED ? sDg : sG + 7 * EPB * P;
 
   if constexpr (FUSED) {
     if (a.cg->done) return;

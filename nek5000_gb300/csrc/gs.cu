@@ -25,18 +25,21 @@ __global__ void gs_op_kernel(T* __restrict__ u, const int* __restrict__ start,
   for (int c = a; c < b; ++c) u[idx[c]] = t;
 }
 
+// Grid-stride over boundary groups with a fixed, small grid; every block also
+// folds a strided slice of the operator's interior partials into its own
+// partial, so the last block sums only gridDim.x values.
 template <typename T>
-__global__ void gs_cg_kernel(T* __restrict__ w, const T* __restrict__ p,
-                             const int* __restrict__ start, const int* __restrict__ idx, int nseg,
-                             const T* __restrict__ segmask, const T* __restrict__ segmsum,
-                             CgScalars* cg, const double* __restrict__ partialA, int nA,
-                             double* __restrict__ partialB) {
+__global__ void __launch_bounds__(kGsThreads)
+    gs_cg_kernel(T* __restrict__ w, const T* __restrict__ p, const int* __restrict__ start,
+                 const int* __restrict__ idx, int nseg, const T* __restrict__ segmask,
+                 const T* __restrict__ segmsum, CgScalars* cg,
+                 const double* __restrict__ partialA, int nA, double* __restrict__ partialB) {
   __shared__ double red[32];
   __shared__ int am_last;
   if (cg->done) return;
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
   CompAcc<T> acc;
-  if (s < nseg) {
+  const int stride = gridDim.x * blockDim.x;
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nseg; s += stride) {
     const int a = start[s], b = start[s + 1];
     T t = w[idx[a]];
     for (int c = a + 1; c < b; ++c) t = t + w[idx[c]];
@@ -44,25 +47,24 @@ __global__ void gs_cg_kernel(T* __restrict__ w, const T* __restrict__ p,
     for (int c = a; c < b; ++c) w[idx[c]] = t;
     acc.add(t * p[idx[a]] * segmsum[s]);
   }
-  const double dot = block_sum_comp(acc, red);
+  double dot = block_sum_comp(acc, red);  // thread 0
+  // this block's share of the interior partials: q = blockIdx.x + k*gridDim.x
+  double pa = 0.0;
+  for (int q = blockIdx.x + gridDim.x * threadIdx.x; q < nA; q += gridDim.x * blockDim.x)
+    pa += __ldcg(partialA + q);
+  pa = block_sum(pa, red);
   if (threadIdx.x == 0) {
-    partialB[blockIdx.x] = dot;
+    partialB[blockIdx.x] = dot + pa;
     __threadfence();
     const unsigned int ticket = atomicAdd(&cg->counter[0], 1u);
     am_last = (ticket == gridDim.x - 1);
   }
   __syncthreads();
   if (!am_last) return;
-  // Last block: rho = interior partials (fused axhelm) + boundary partials,
-  // each summed in a fixed order.
-  double pa = 0.0;
-  for (int q = threadIdx.x; q < nA; q += blockDim.x) pa += __ldcg(partialA + q);
-  const double rhoA = block_sum(pa, red);
   double pb = 0.0;
   for (int q = threadIdx.x; q < (int)gridDim.x; q += blockDim.x) pb += __ldcg(partialB + q);
-  const double rhoB = block_sum(pb, red);
+  const double rho = block_sum(pb, red);
   if (threadIdx.x == 0) {
-    const double rho = rhoA + rhoB;
     cg->rho = rho;
     cg->alpha = cg->rtz1 / rho;
     cg->counter[0] = 0u;
@@ -183,7 +185,7 @@ void gs_op(const GsMaps& gs, T* u, int op, cudaStream_t s) {
 template <typename T>
 void gs_cg(const GsMaps& gs, T* w, const T* p, const T* segmask, const T* segmsum,
            CgScalars* cg, double* partialA, int nA, double* partialB, cudaStream_t s) {
-  const int nb = std::max(gs_cg_blocks(gs), 1);
+  const int nb = gs_cg_blocks(gs);
   count_launch();
   gs_cg_kernel<T><<<nb, kGsThreads, 0, s>>>(w, p, gs.bstart, gs.bidx, gs.nbseg, segmask, segmsum,
                                             cg, partialA, nA, partialB);

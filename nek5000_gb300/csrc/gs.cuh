@@ -55,6 +55,11 @@ void gs_cg_weights(const GsMaps& gs, const T* mask, const T* mult, T* segmask, T
                    int* nonuniform, cudaStream_t s);
 
 constexpr int kGsThreads = 256;
-inline int gs_cg_blocks(const GsMaps& gs) { return (gs.nbseg + kGsThreads - 1) / kGsThreads; }
+// Fixed grid of the PCG-form kernel (grid-stride over groups): two blocks per
+// SM, fewer when there are few groups.
+inline int gs_cg_blocks(const GsMaps& gs) {
+  const int need = (gs.nbseg + kGsThreads - 1) / kGsThreads;
+  return need < 1 ? 1 : (need < 2 * 152 ? need : 2 * 152);
+}
 
 }  // namespace nekgpu

@@ -26,7 +26,7 @@ constexpr int NEKGPU_ENOMEM_ = -4;
 
 inline int vec_blocks(int64_t n) {
   int64_t b = (n + kVecThreads - 1) / kVecThreads;
-  return (int)std::min<int64_t>(std::max<int64_t>(b, 1), 152 * 8);
+  return (int)std::min<int64_t>(std::max<int64_t>(b, 1), 152 * 4);
 }
 
 // ---- min/max of h1 and h2 (uniformity detection) ---------------------------
@@ -242,6 +242,7 @@ __global__ void __launch_bounds__(kVecThreads)
   __syncthreads();
   if (!am_last) return;
   double t1 = 0.0, t2 = 0.0;
+#pragma unroll 4
   for (int q = threadIdx.x; q < (int)gridDim.x; q += blockDim.x) {
     t1 += __ldcg(partial + q);
     t2 += __ldcg(partial + gridDim.x + q);
