@@ -25,30 +25,78 @@ __global__ void gs_op_kernel(T* __restrict__ u, const int* __restrict__ start,
   for (int c = a; c < b; ++c) u[idx[c]] = t;
 }
 
-// Grid-stride over boundary groups with a fixed, small grid; every block also
-// folds a strided slice of the operator's interior partials into its own
-// partial, so the last block sums only gridDim.x values.
+// One group of C copies (C in 1, 2, 4, 8): indices in one vector load, all
+// gathers issued together, sum in ascending local-index order.
+template <typename T, int C>
+__device__ __forceinline__ void gs_group(const int* __restrict__ cidx, int s, T* __restrict__ w,
+                                         const T* __restrict__ p, T mask, T msum,
+                                         CompAcc<T>& acc) {
+  int id[C];
+  if constexpr (C == 1) {
+    id[0] = cidx[s];
+  } else if constexpr (C == 2) {
+    const int2 v = reinterpret_cast<const int2*>(cidx)[s];
+    id[0] = v.x;
+    id[1] = v.y;
+  } else {
+#pragma unroll
+    for (int h = 0; h < C / 4; ++h) {
+      const int4 v = reinterpret_cast<const int4*>(cidx)[(C / 4) * s + h];
+      id[4 * h] = v.x;
+      id[4 * h + 1] = v.y;
+      id[4 * h + 2] = v.z;
+      id[4 * h + 3] = v.w;
+    }
+  }
+  T v[C];
+#pragma unroll
+  for (int q = 0; q < C; ++q) v[q] = w[id[q]];
+  const T p0 = p[id[0]];
+  T t = v[0];
+#pragma unroll
+  for (int q = 1; q < C; ++q) t = t + v[q];
+  t = t * mask;
+#pragma unroll
+  for (int q = 0; q < C; ++q) w[id[q]] = t;
+  acc.add(t * p0 * msum);
+}
+
+// One thread per boundary group; the blocks of each size class are
+// contiguous in the grid, so a block runs one class.  Every block also folds
+// a strided slice of the operator's interior partials into its partial.
 template <typename T>
 __global__ void __launch_bounds__(kGsThreads)
     gs_cg_kernel(T* __restrict__ w, const T* __restrict__ p, const int* __restrict__ start,
-                 const int* __restrict__ idx, int nseg, const T* __restrict__ segmask,
-                 const T* __restrict__ segmsum, CgScalars* cg,
+                 const int* __restrict__ idx, const GsClasses cls,
+                 const T* __restrict__ segmask, const T* __restrict__ segmsum, CgScalars* cg,
                  const double* __restrict__ partialA, int nA, double* __restrict__ partialB) {
   __shared__ double red[32];
   __shared__ int am_last;
   if (cg->done) return;
+  int k = 0;
+  while (k < kGsClasses - 1 && (int)blockIdx.x >= cls.boff[k + 1]) ++k;
+  const int sl = ((int)blockIdx.x - cls.boff[k]) * blockDim.x + threadIdx.x;  // group in class
   CompAcc<T> acc;
-  const int stride = gridDim.x * blockDim.x;
-  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nseg; s += stride) {
-    const int a = start[s], b = start[s + 1];
-    T t = w[idx[a]];
-    for (int c = a + 1; c < b; ++c) t = t + w[idx[c]];
-    t = t * segmask[s];
-    for (int c = a; c < b; ++c) w[idx[c]] = t;
-    acc.add(t * p[idx[a]] * segmsum[s]);
+  if (sl < cls.cnt[k]) {
+    const int g = cls.soff[k] + sl;
+    const T mk = segmask[g], ms = segmsum[g];
+    const int* ci = idx + cls.ioff[k];
+    switch (k) {
+      case 0: gs_group<T, 1>(ci, sl, w, p, mk, ms, acc); break;
+      case 1: gs_group<T, 2>(ci, sl, w, p, mk, ms, acc); break;
+      case 2: gs_group<T, 4>(ci, sl, w, p, mk, ms, acc); break;
+      case 3: gs_group<T, 8>(ci, sl, w, p, mk, ms, acc); break;
+      default: {
+        const int a = start[g], b = start[g + 1];
+        T t = w[idx[a]];
+        for (int c = a + 1; c < b; ++c) t = t + w[idx[c]];
+        t = t * mk;
+        for (int c = a; c < b; ++c) w[idx[c]] = t;
+        acc.add(t * p[idx[a]] * ms);
+      }
+    }
   }
   double dot = block_sum_comp(acc, red);  // thread 0
-  // this block's share of the interior partials: q = blockIdx.x + k*gridDim.x
   double pa = 0.0;
   for (int q = blockIdx.x + gridDim.x * threadIdx.x; q < nA; q += gridDim.x * blockDim.x)
     pa += __ldcg(partialA + q);
@@ -62,6 +110,7 @@ __global__ void __launch_bounds__(kGsThreads)
   __syncthreads();
   if (!am_last) return;
   double pb = 0.0;
+#pragma unroll 8
   for (int q = threadIdx.x; q < (int)gridDim.x; q += blockDim.x) pb += __ldcg(partialB + q);
   const double rho = block_sum(pb, red);
   if (threadIdx.x == 0) {
@@ -123,30 +172,57 @@ int gs_setup(GsMaps& gs, const int64_t* glo_num, int64_t n, std::string& err) {
   bst.push_back((int)bix.size());
   gs.nseg = (int)st.size() - 1;
   gs.nidx = (int)ix.size();
-  gs.nbseg = (int)bst.size() - 1;
-  gs.nbidx = (int)bix.size();
   gs.h_start.assign(st.begin(), st.end());
   gs.h_idx.assign(ix.begin(), ix.end());
-  // The PCG-form maps are processed in order of each group's first local
-  // index: neighbouring threads then gather and scatter within the same few
-  // elements (the order of groups does not change any group's sum).
   {
+    // PCG-form maps: by size class (1, 2, 4, 8, other), then first index;
+    // each class's idx run starts on a 4-entry (16-byte) boundary.
     const size_t ns = bst.size() - 1;
+    auto cls_of = [&](int g) {
+      const int sz = bst[g + 1] - bst[g];
+      return sz == 1 ? 0 : sz == 2 ? 1 : sz == 4 ? 2 : sz == 8 ? 3 : 4;
+    };
     std::vector<int> ord(ns);
     std::iota(ord.begin(), ord.end(), 0);
-    std::stable_sort(ord.begin(), ord.end(),
-                     [&](int a, int b) { return bix[bst[a]] < bix[bst[b]]; });
+    std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) {
+      const int ca = cls_of(a), cb = cls_of(b);
+      if (ca != cb) return ca < cb;
+      return bix[bst[a]] < bix[bst[b]];
+    });
     std::vector<int> nst, nix;
     nst.reserve(bst.size());
-    nix.reserve(bix.size());
-    for (int g : ord) {
+    nix.reserve(bix.size() + 16);
+    GsClasses& C = gs.cls;
+    for (int k = 0; k < kGsClasses; ++k) C.cnt[k] = 0;
+    int cur = -1;
+    for (size_t q = 0; q < ns; ++q) {
+      const int g = ord[q];
+      const int k = cls_of(g);
+      while (cur < k) {  // open the next class region(s)
+        ++cur;
+        while (nix.size() % 4) nix.push_back(0);
+        C.soff[cur] = (int)q;
+        C.ioff[cur] = (int)nix.size();
+      }
+      ++C.cnt[k];
       nst.push_back((int)nix.size());
       for (int c = bst[g]; c < bst[g + 1]; ++c) nix.push_back(bix[c]);
     }
+    while (cur < kGsClasses - 1) {
+      ++cur;
+      while (nix.size() % 4) nix.push_back(0);
+      C.soff[cur] = (int)ns;
+      C.ioff[cur] = (int)nix.size();
+    }
     nst.push_back((int)nix.size());
+    C.boff[0] = 0;
+    for (int k = 0; k < kGsClasses; ++k)
+      C.boff[k + 1] = C.boff[k] + (C.cnt[k] + kGsThreads - 1) / kGsThreads;
     bst.swap(nst);
     bix.swap(nix);
   }
+  gs.nbseg = (int)bst.size() - 1;
+  gs.nbidx = (int)bix.size();
   auto up = [&](int** dst, const std::vector<int>& v) -> bool {
     size_t bytes = std::max<size_t>(v.size(), 1) * sizeof(int);
     if (cudaMalloc(dst, bytes) != cudaSuccess) return false;
@@ -187,7 +263,7 @@ void gs_cg(const GsMaps& gs, T* w, const T* p, const T* segmask, const T* segmsu
            CgScalars* cg, double* partialA, int nA, double* partialB, cudaStream_t s) {
   const int nb = gs_cg_blocks(gs);
   count_launch();
-  gs_cg_kernel<T><<<nb, kGsThreads, 0, s>>>(w, p, gs.bstart, gs.bidx, gs.nbseg, segmask, segmsum,
+  gs_cg_kernel<T><<<nb, kGsThreads, 0, s>>>(w, p, gs.bstart, gs.bidx, gs.cls, segmask, segmsum,
                                             cg, partialA, nA, partialB);
 }
 

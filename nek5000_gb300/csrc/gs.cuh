@@ -19,6 +19,19 @@
 
 namespace nekgpu {
 
+// The PCG-form ("bound") maps are ordered by size class -- groups of 1, 2, 4
+// and 8 copies, then all other sizes -- and inside a class by first local
+// index.  A class's copies form one packed, 16-byte aligned run of idx, so a
+// thread loads its group's indices with one vector access and issues every
+// gather at once.
+constexpr int kGsClasses = 5;  // sizes 1, 2, 4, 8, other
+struct GsClasses {
+  int cnt[kGsClasses];      // groups per class
+  int soff[kGsClasses];     // first group index of the class
+  int ioff[kGsClasses];     // first idx entry of the class (multiple of 4)
+  int boff[kGsClasses + 1]; // first block of the class in the launch
+};
+
 struct GsMaps {
   int64_t n = 0;
   int nseg = 0, nidx = 0;    // shared groups
@@ -27,6 +40,7 @@ struct GsMaps {
   int nbseg = 0, nbidx = 0;  // all boundary groups
   int* bstart = nullptr;
   int* bidx = nullptr;
+  GsClasses cls{};
   std::vector<int64_t> h_start, h_idx;  // host copy of the shared maps (export)
 };
 
@@ -54,12 +68,8 @@ template <typename T>
 void gs_cg_weights(const GsMaps& gs, const T* mask, const T* mult, T* segmask, T* segmsum,
                    int* nonuniform, cudaStream_t s);
 
-constexpr int kGsThreads = 256;
-// Fixed grid of the PCG-form kernel (grid-stride over groups): two blocks per
-// SM, fewer when there are few groups.
-inline int gs_cg_blocks(const GsMaps& gs) {
-  const int need = (gs.nbseg + kGsThreads - 1) / kGsThreads;
-  return need < 1 ? 1 : (need < 2 * 152 ? need : 2 * 152);
-}
+constexpr int kGsThreads = 512;
+// Blocks of the PCG-form kernel: one thread per group, classes block-aligned.
+inline int gs_cg_blocks(const GsMaps& gs) { return gs.cls.boff[kGsClasses] > 0 ? gs.cls.boff[kGsClasses] : 1; }
 
 }  // namespace nekgpu

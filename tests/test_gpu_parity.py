@@ -235,3 +235,37 @@ def test_errors_are_status_codes(gpu_lib, oracle, cfg1):
         lib.cggo(np.zeros(n), f, np.ones(n), np.zeros(n), P["mask"], P["mult"], 1, -1e-10, 100, 1,
                  P["binv"])
     assert e.value.code == _capi.ENAN
+
+
+def test_cggo_irregular_group_sizes(gpu_lib, oracle):
+    """Groups of 3 and 5 copies (as unstructured meshes have) take the generic
+    path of the boundary-group kernel; the solve still matches the oracle."""
+    torch = pytest.importorskip("torch")
+    P0 = oracle.box_problem(6, 3, 3, 3, v=rng_unit_vector(9))
+    nx, nel = P0["nx1"], P0["nel"]
+    glo = P0["glo_num"].copy().reshape(nel, nx, nx, nx)
+    rng = np.random.default_rng(9)
+    # give interior points of some elements the id of a node on an interior
+    # face of the same element: that group grows from 2 to 3 (or 4 -> 5)
+    for e in rng.choice(nel, 10, replace=False):
+        glo[e, 2, 2, 2] = glo[e, 2, 2, 0] if glo[e, 2, 2, 0] else glo[e, 2, 2, -1]
+        glo[e, 3, 1, 1] = glo[e, 3, 0, 0]
+    glo = glo.reshape(-1)
+    ops = oracle.Ops(nx, nel, P0["D"], P0["g"], P0["bm1"], glo, 1)
+    n = P0["n"]
+    mask = ops.dsop(P0["mask"], "*")
+    mult = 1.0 / ops.dssum(np.ones(n))
+    binv = 1.0 / ops.dssum(P0["bm1"])
+    sizes = np.bincount(np.unique(glo[glo > 0], return_counts=True)[1])
+    assert sizes[3:].sum() - sizes[4] - (sizes[8] if len(sizes) > 8 else 0) > 0
+    f = ops.dssum(P0["bm1"] * rng.standard_normal(n)) * mask
+    h1, h2 = np.ones(n), np.full(n, 3.0)
+    x_ref, it_ref, _, _ = ops.cggo(f, h1, h2, mask, mult, binv, -1e-10, maxcg=10 ** 6)
+    lib = gpu_lib(0)
+    lib.setup(nx, nel, P0["D"], P0["g"], P0["bm1"], glo)
+    dev = lambda a: torch.tensor(a, device="cuda")
+    x = torch.zeros(n, dtype=torch.float64, device="cuda")
+    it, r0, r2, rc = lib.cggo(x, dev(f), dev(h1), dev(h2), dev(mask), dev(mult), 1, -1e-10,
+                              10 ** 6, 1, dev(binv), maxcg=10 ** 6)
+    assert rc == 0 and abs(it - it_ref) <= 1
+    assert np.linalg.norm(x.cpu().numpy() - x_ref) <= 1e-11 * np.linalg.norm(x_ref)
