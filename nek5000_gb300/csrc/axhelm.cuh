@@ -46,6 +46,7 @@ struct AxArgs {
   const CgScalars* cg;
   double* partial; // one per block
   int* err;        // device flag: set if a bounded wait expired
+  const unsigned char* skip;  // interior points owned by the boundary-group kernel
 };
 
 template <int NX>
@@ -196,7 +197,8 @@ __global__ void __launch_bounds__(256) axhelm_kernel(const AxArgs<T> a) {
       }
       a.au[eo + pt] = s;
       if constexpr (FUSED) {
-        if (i > 0 && i < NX - 1 && j > 0 && j < NX - 1 && k > 0 && k < NX - 1)
+        if (i > 0 && i < NX - 1 && j > 0 && j < NX - 1 && k > 0 && k < NX - 1 &&
+            (!a.skip || !a.skip[eo + pt]))
           dot = fma(s, ru[k], dot);
       }
     }

@@ -109,6 +109,7 @@ static AxArgs<T> make_args(const Mesh& m, const OpData<T>& op, T* au, const T* u
   a.D = op.D;
   a.nel = m.nel;
   a.err = m.dev_err;
+  a.skip = m.gs.skip;
   return a;
 }
 

@@ -229,7 +229,8 @@ __global__ void __launch_bounds__(NX* NX* tma_epb<NX>())
       }
       a.au[eo + pt] = s;
       if constexpr (FUSED) {
-        if (i > 0 && i < NX - 1 && j > 0 && j < NX - 1 && k > 0 && k < NX - 1)
+        if (i > 0 && i < NX - 1 && j > 0 && j < NX - 1 && k > 0 && k < NX - 1 &&
+            (!a.skip || !a.skip[eo + pt]))
           dot = fma(s, ru[k], dot);
       }
     }

@@ -324,7 +324,7 @@ int nekgpu_setup(const int64_t* handle, const int* lx1, const int* nel, const do
     return fail(H, NEKGPU_ENOMEM, "flag allocation failed");
   cudaMemset(m.dev_err, 0, sizeof(int));
   std::string err;
-  int rc = gs_setup(m.gs, glo_num, n, err);
+  int rc = gs_setup(m.gs, glo_num, n, m.nx1, err);
   if (rc) return fail(H, rc == -4 ? NEKGPU_ENOMEM : NEKGPU_EINVAL, err);
   H->has_mesh = true;
   return NEKGPU_OK;

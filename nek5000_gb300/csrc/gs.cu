@@ -140,7 +140,7 @@ __global__ void gs_cg_weights_kernel(const int* __restrict__ start, const int* _
 
 }  // namespace
 
-int gs_setup(GsMaps& gs, const int64_t* glo_num, int64_t n, std::string& err) {
+int gs_setup(GsMaps& gs, const int64_t* glo_num, int64_t n, int nx1, std::string& err) {
   gs_free(gs);
   if (n >= (int64_t)INT32_MAX) {
     err = "gs_setup: more than 2^31-1 local points";
@@ -157,17 +157,35 @@ int gs_setup(GsMaps& gs, const int64_t* glo_num, int64_t n, std::string& err) {
   ix.reserve(pr.size());
   bst.reserve(pr.size() / 2 + 1);
   bix.reserve(pr.size());
+  const int P = nx1 * nx1 * nx1;
+  auto interior = [&](int64_t i) {
+    const int p = (int)(i % P), x = p % nx1, y = (p / nx1) % nx1, z = p / (nx1 * nx1);
+    return x > 0 && x < nx1 - 1 && y > 0 && y < nx1 - 1 && z > 0 && z < nx1 - 1;
+  };
+  std::vector<unsigned char> skip;
   for (size_t a = 0; a < pr.size();) {
     size_t b = a + 1;
     while (b < pr.size() && pr[b].first == pr[a].first) ++b;
     bst.push_back((int)bix.size());
-    for (size_t c = a; c < b; ++c) bix.push_back(pr[c].second);
+    for (size_t c = a; c < b; ++c) {
+      bix.push_back(pr[c].second);
+      if (interior(pr[c].second)) {
+        if (skip.empty()) skip.assign((size_t)n, 0);
+        skip[(size_t)pr[c].second] = 1;
+      }
+    }
     if (b - a >= 2) {
       st.push_back((int)ix.size());
       for (size_t c = a; c < b; ++c) ix.push_back(pr[c].second);
     }
     a = b;
   }
+  // element-boundary points without an id: singleton groups of the PCG form
+  for (int64_t i = 0; i < n; ++i)
+    if (glo_num[i] == 0 && !interior(i)) {
+      bst.push_back((int)bix.size());
+      bix.push_back((int)i);
+    }
   st.push_back((int)ix.size());
   bst.push_back((int)bix.size());
   gs.nseg = (int)st.size() - 1;
@@ -236,6 +254,14 @@ int gs_setup(GsMaps& gs, const int64_t* glo_num, int64_t n, std::string& err) {
     gs_free(gs);
     return -4;
   }
+  if (!skip.empty()) {
+    if (cudaMalloc(&gs.skip, (size_t)n) != cudaSuccess ||
+        cudaMemcpy(gs.skip, skip.data(), (size_t)n, cudaMemcpyHostToDevice) != cudaSuccess) {
+      err = "gs_setup: device allocation failed";
+      gs_free(gs);
+      return -4;
+    }
+  }
   return 0;
 }
 
@@ -244,6 +270,8 @@ void gs_free(GsMaps& gs) {
   cudaFree(gs.idx);
   cudaFree(gs.bstart);
   cudaFree(gs.bidx);
+  cudaFree(gs.skip);
+  gs.skip = nullptr;
   gs.start = gs.idx = gs.bstart = gs.bidx = nullptr;
   gs.nseg = gs.nidx = gs.nbseg = gs.nbidx = 0;
   gs.h_start.clear();

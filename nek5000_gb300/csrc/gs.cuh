@@ -41,12 +41,17 @@ struct GsMaps {
   int* bstart = nullptr;
   int* bidx = nullptr;
   GsClasses cls{};
+  // 1 for element-interior points that the caller's numbering shares (id != 0):
+  // the fused operator must leave them to the boundary-group kernel.
+  // nullptr when there are none (the reference's numbering).
+  unsigned char* skip = nullptr;
   std::vector<int64_t> h_start, h_idx;  // host copy of the shared maps (export)
 };
 
-// Host: build maps from glo_num (sort by (id, local index)).  Returns 0 or an
-// error code; fills err.
-int gs_setup(GsMaps& gs, const int64_t* glo_num, int64_t n, std::string& err);
+// Host: build maps from glo_num (sort by (id, local index)).  nx1 classifies
+// element-interior points: element-boundary points with id 0 join the PCG-form
+// maps as singletons (so that masks reach them).  Returns 0 or an error code.
+int gs_setup(GsMaps& gs, const int64_t* glo_num, int64_t n, int nx1, std::string& err);
 void gs_free(GsMaps& gs);
 
 // u <- gs_op(u, op): op 0 '+', 1 '*', 2 max, 3 min

@@ -280,6 +280,21 @@ __global__ void __launch_bounds__(kVecThreads)
   }
 }
 
+// Element-interior points handled by the fused operator must carry mask 1 and
+// multiplicity 1 (the reference's masks live on faces; interiors are unshared).
+template <typename T>
+__global__ void interior_check_kernel(const T* __restrict__ mask, const T* __restrict__ mult,
+                                      const unsigned char* __restrict__ skip, int nx1, int64_t n,
+                                      int* bad) {
+  const int P = nx1 * nx1 * nx1;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int p = (int)(i % P), x = p % nx1, y = (p / nx1) % nx1, z = p / (nx1 * nx1);
+    const bool in = x > 0 && x < nx1 - 1 && y > 0 && y < nx1 - 1 && z > 0 && z < nx1 - 1;
+    if (in && !(skip && skip[i]) && (mask[i] != T(1) || mult[i] != T(1))) atomicOr(bad, 1);
+  }
+}
+
 template <typename T>
 __global__ void zero_kernel(T* __restrict__ a, int64_t n) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
@@ -496,10 +511,13 @@ PcgResult pcg_solve(Handle& h, const OpData<T>& op, PcgWork<T>& wk, T* x, const 
     return res;
   }
   // boundary-group mask / multiplicity weights
-  cudaMemsetAsync(h.flag, 0, sizeof(int), s);
+  cudaMemsetAsync(h.flag, 0, 2 * sizeof(int), s);
   gs_cg_weights<T>(m.gs, mask, mult, wk.segmask.ptr, wk.segmsum.ptr, h.flag, s);
-  int nonuni = 0;
-  cudaMemcpyAsync(&nonuni, h.flag, sizeof(int), cudaMemcpyDeviceToHost, s);
+  count_launch();
+  interior_check_kernel<T><<<vec_blocks(n), kVecThreads, 0, s>>>(mask, mult, m.gs.skip, m.nx1, n,
+                                                                 h.flag + 1);
+  int flags[2] = {0, 0};
+  cudaMemcpyAsync(flags, h.flag, 2 * sizeof(int), cudaMemcpyDeviceToHost, s);
   // r = f, p = 0
   cudaMemcpyAsync(wk.r.ptr, f, n * sizeof(T), cudaMemcpyDeviceToDevice, s);
   count_launch();
@@ -522,9 +540,14 @@ PcgResult pcg_solve(Handle& h, const OpData<T>& op, PcgWork<T>& wk, T* x, const 
     set_error(h, std::string("pcg: ") + cudaGetErrorString(cudaGetLastError()));
     return res;
   }
-  if (nonuni) {
+  if (flags[0]) {
     res.status = -1;
     set_error(h, "pcg: mask differs between copies of a shared node (apply dsop '*' first)");
+    return res;
+  }
+  if (flags[1]) {
+    res.status = -1;
+    set_error(h, "pcg: an element-interior point has mask or multiplicity other than 1");
     return res;
   }
   // iteration 1 check (z, s1, s2) -- no update
