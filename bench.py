@@ -53,7 +53,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-iters", type=int, default=0, help="oracle PCG iterations per sample")
-    ap.add_argument("--inner-tol", type=float, default=1e-5, help="mixed: inner FP32 tolerance")
+    ap.add_argument("--inner-tol", type=float, default=1e-4, help="mixed: inner FP32 tolerance")
     ap.add_argument("--only-mixed", action="store_true", help="skip the plain FP64 solve")
     return ap.parse_args()
 

@@ -2,7 +2,8 @@
  * nekref.c -- CPU oracle for the Nek5000 Helmholtz/Poisson solve path.
  *
  * TEST INFRASTRUCTURE ONLY: the checker the parity tests compare the CUDA
- * library against, and the CPU baseline that bench.py times.  It is never
+ * library against, and the CPU baseline that bench.py times.  Parity
+ * unpinned: no reference output exists to pin it (see nekref.h).  It is never
  * linked into, loaded by, or called from the product library.
  *
  * Each function restates one reference routine (file:line in the Nek5000

@@ -7,6 +7,12 @@
  * baseline.  The product library (nek5000_gb300/csrc) never links, loads or
  * calls it.
  *
+ * Parity unpinned: the reference Fortran cannot be compiled or run here and
+ * ships no function-level golden vectors, so this restatement is pinned by
+ * known-answer tests (quadrature and differentiation exactness, operator
+ * symmetry and null space, spectral convergence) rather than by reference
+ * outputs.
+ *
  * Array conventions follow the Fortran: every field is (lx1,ly1,lz1,nel)
  * column-major (x fastest, element slowest), 0-based here.  D(i,j) is stored
  * d[i + j*nx].  All arithmetic is FP64, compiled with -ffp-contract=off so no
