@@ -54,6 +54,8 @@ extern "C" {
                                 (core/hmholtz.f:778)                              */
 #define NEKGPU_OPT_TMA 5     /* 1 (default): stage element blocks with bulk async
                                 copies where lx1 is even; 0: plain loads         */
+#define NEKGPU_OPT_GRAPH 6   /* 1 (default): replay each chunk of PCG iterations
+                                as one captured CUDA graph; 0: direct launches   */
 
 /* ---- life cycle ---------------------------------------------------------- */
 /* Create a handle on CUDA device *device.  Replaces the per-rank setup the

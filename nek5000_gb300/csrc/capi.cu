@@ -229,6 +229,7 @@ int nekgpu_finalize(int64_t* handle) {
   H->mesh.f32.release();
   cudaFree(H->mesh.dev_err);
   for (cudaEvent_t e : H->ax_ev) cudaEventDestroy(e);
+  if (H->gexec) cudaGraphExecDestroy(H->gexec);
   cudaFree(H->cg);
   cudaFreeHost(H->cg_host);
   cudaFree(H->flag);
@@ -265,6 +266,7 @@ int nekgpu_set_option(const int64_t* handle, const int* key, const int* value) {
       break;
     case NEKGPU_OPT_ISTEP: H->istep = *value; break;
     case NEKGPU_OPT_TMA: H->mesh.use_tma = (*value != 0); break;
+    case NEKGPU_OPT_GRAPH: H->use_graph = (*value != 0); break;
     default: return fail(H, NEKGPU_EINVAL, "unknown option");
   }
   return NEKGPU_OK;

@@ -22,7 +22,15 @@ inline std::atomic<long long>& launch_counter() {
   static std::atomic<long long> c{0};
   return c;
 }
-inline void count_launch() { launch_counter().fetch_add(1, std::memory_order_relaxed); }
+// Launches recorded into a CUDA graph are counted when the graph runs, not
+// while it is captured.
+inline bool& capturing() {
+  static thread_local bool c = false;
+  return c;
+}
+inline void count_launch(long long k = 1) {
+  if (!capturing()) launch_counter().fetch_add(k, std::memory_order_relaxed);
+}
 
 // ---- reductions: deterministic (fixed tree, no floating-point atomics) ----
 template <typename T>

@@ -25,13 +25,12 @@ __global__ void gs_op_kernel(T* __restrict__ u, const int* __restrict__ start,
   for (int c = a; c < b; ++c) u[idx[c]] = t;
 }
 
-// One group of C copies (C in 1, 2, 4, 8): indices in one vector load, all
-// gathers issued together, sum in ascending local-index order.
-template <typename T, int C>
-__device__ __forceinline__ void gs_group(const int* __restrict__ cidx, int s, T* __restrict__ w,
-                                         const T* __restrict__ p, T mask, T msum,
-                                         CompAcc<T>& acc) {
-  int id[C];
+// Groups of C copies (C in 1, 2, 4, 8): each thread takes G groups of its
+// class (block-strided, so index loads stay coalesced), loads every group's
+// indices with one vector access, issues all gathers before any use, sums each
+// group in ascending local-index order, scatters, and accumulates rho.
+template <int C>
+__device__ __forceinline__ void load_ids(const int* __restrict__ cidx, int s, int (&id)[C]) {
   if constexpr (C == 1) {
     id[0] = cidx[s];
   } else if constexpr (C == 2) {
@@ -48,22 +47,48 @@ __device__ __forceinline__ void gs_group(const int* __restrict__ cidx, int s, T*
       id[4 * h + 3] = v.w;
     }
   }
-  T v[C];
-#pragma unroll
-  for (int q = 0; q < C; ++q) v[q] = w[id[q]];
-  const T p0 = p[id[0]];
-  T t = v[0];
-#pragma unroll
-  for (int q = 1; q < C; ++q) t = t + v[q];
-  t = t * mask;
-#pragma unroll
-  for (int q = 0; q < C; ++q) w[id[q]] = t;
-  acc.add(t * p0 * msum);
 }
 
-// One thread per boundary group; the blocks of each size class are
-// contiguous in the grid, so a block runs one class.  Every block also folds
-// a strided slice of the operator's interior partials into its partial.
+template <typename T, int C, int G>
+__device__ __forceinline__ void gs_groups(const int* __restrict__ cidx, int s0, int step, int cnt,
+                                          int goff, T* __restrict__ w, const T* __restrict__ p,
+                                          const T* __restrict__ segmask,
+                                          const T* __restrict__ segmsum, CompAcc<T>& acc) {
+  int id[G][C];
+  bool on[G];
+#pragma unroll
+  for (int q = 0; q < G; ++q) {
+    const int s = s0 + q * step;
+    on[q] = s < cnt;
+    if (on[q]) load_ids<C>(cidx, s, id[q]);
+  }
+  T v[G][C], p0[G], mk[G], ms[G];
+#pragma unroll
+  for (int q = 0; q < G; ++q) {
+    if (!on[q]) continue;
+    const int s = s0 + q * step;
+#pragma unroll
+    for (int c = 0; c < C; ++c) v[q][c] = w[id[q][c]];
+    p0[q] = p[id[q][0]];
+    mk[q] = segmask[goff + s];
+    ms[q] = segmsum[goff + s];
+  }
+#pragma unroll
+  for (int q = 0; q < G; ++q) {
+    if (!on[q]) continue;
+    T t = v[q][0];
+#pragma unroll
+    for (int c = 1; c < C; ++c) t = t + v[q][c];
+    t = t * mk[q];
+#pragma unroll
+    for (int c = 0; c < C; ++c) w[id[q][c]] = t;
+    acc.add(t * p0[q] * ms[q]);
+  }
+}
+
+// Blocks of each size class are contiguous in the grid (a block runs one
+// class, kGsGroups groups per thread).  Warp 0 also folds a strided slice of
+// the operator's interior partials into the block's partial.
 template <typename T>
 __global__ void __launch_bounds__(kGsThreads)
     gs_cg_kernel(T* __restrict__ w, const T* __restrict__ p, const int* __restrict__ start,
@@ -75,37 +100,41 @@ __global__ void __launch_bounds__(kGsThreads)
   if (cg->done) return;
   int k = 0;
   while (k < kGsClasses - 1 && (int)blockIdx.x >= cls.boff[k + 1]) ++k;
-  const int sl = ((int)blockIdx.x - cls.boff[k]) * blockDim.x + threadIdx.x;  // group in class
+  const int G = gs_groups_per_thread(k);
+  const int s0 = ((int)blockIdx.x - cls.boff[k]) * blockDim.x * G + threadIdx.x;
+  const int* ci = idx + cls.ioff[k];
+  const int goff = cls.soff[k], cnt = cls.cnt[k];
   CompAcc<T> acc;
-  if (sl < cls.cnt[k]) {
-    const int g = cls.soff[k] + sl;
-    const T mk = segmask[g], ms = segmsum[g];
-    const int* ci = idx + cls.ioff[k];
-    switch (k) {
-      case 0: gs_group<T, 1>(ci, sl, w, p, mk, ms, acc); break;
-      case 1: gs_group<T, 2>(ci, sl, w, p, mk, ms, acc); break;
-      case 2: gs_group<T, 4>(ci, sl, w, p, mk, ms, acc); break;
-      case 3: gs_group<T, 8>(ci, sl, w, p, mk, ms, acc); break;
-      default: {
+  switch (k) {
+    case 0: gs_groups<T, 1, 4>(ci, s0, blockDim.x, cnt, goff, w, p, segmask, segmsum, acc); break;
+    case 1: gs_groups<T, 2, 4>(ci, s0, blockDim.x, cnt, goff, w, p, segmask, segmsum, acc); break;
+    case 2: gs_groups<T, 4, 2>(ci, s0, blockDim.x, cnt, goff, w, p, segmask, segmsum, acc); break;
+    case 3: gs_groups<T, 8, 1>(ci, s0, blockDim.x, cnt, goff, w, p, segmask, segmsum, acc); break;
+    default:
+      for (int q = 0; q < G; ++q) {
+        const int sl = s0 + q * blockDim.x;
+        if (sl >= cnt) break;
+        const int g = goff + sl;
         const int a = start[g], b = start[g + 1];
         T t = w[idx[a]];
         for (int c = a + 1; c < b; ++c) t = t + w[idx[c]];
-        t = t * mk;
+        t = t * segmask[g];
         for (int c = a; c < b; ++c) w[idx[c]] = t;
-        acc.add(t * p[idx[a]] * ms);
+        acc.add(t * p[idx[a]] * segmsum[g]);
       }
-    }
   }
   double dot = block_sum_comp(acc, red);  // thread 0
-  double pa = 0.0;
-  for (int q = blockIdx.x + gridDim.x * threadIdx.x; q < nA; q += gridDim.x * blockDim.x)
-    pa += __ldcg(partialA + q);
-  pa = block_sum(pa, red);
-  if (threadIdx.x == 0) {
-    partialB[blockIdx.x] = dot + pa;
-    __threadfence();
-    const unsigned int ticket = atomicAdd(&cg->counter[0], 1u);
-    am_last = (ticket == gridDim.x - 1);
+  if (threadIdx.x < 32) {
+    double pa = 0.0;
+    for (int q = blockIdx.x + gridDim.x * threadIdx.x; q < nA; q += gridDim.x * 32)
+      pa += __ldcg(partialA + q);
+    pa = warp_sum(pa);
+    if (threadIdx.x == 0) {
+      partialB[blockIdx.x] = dot + pa;
+      __threadfence();
+      const unsigned int ticket = atomicAdd(&cg->counter[0], 1u);
+      am_last = (ticket == gridDim.x - 1);
+    }
   }
   __syncthreads();
   if (!am_last) return;
@@ -235,7 +264,8 @@ int gs_setup(GsMaps& gs, const int64_t* glo_num, int64_t n, int nx1, std::string
     nst.push_back((int)nix.size());
     C.boff[0] = 0;
     for (int k = 0; k < kGsClasses; ++k)
-      C.boff[k + 1] = C.boff[k] + (C.cnt[k] + kGsThreads - 1) / kGsThreads;
+      C.boff[k + 1] = C.boff[k] + (C.cnt[k] + kGsThreads * gs_groups_per_thread(k) - 1) /
+                                      (kGsThreads * gs_groups_per_thread(k));
     bst.swap(nst);
     bix.swap(nix);
   }

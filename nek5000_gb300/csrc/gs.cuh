@@ -73,8 +73,13 @@ template <typename T>
 void gs_cg_weights(const GsMaps& gs, const T* mask, const T* mult, T* segmask, T* segmsum,
                    int* nonuniform, cudaStream_t s);
 
-constexpr int kGsThreads = 512;
-// Blocks of the PCG-form kernel: one thread per group, classes block-aligned.
+constexpr int kGsThreads = 256;
+// Groups per thread in the PCG-form kernel, by class (1, 2, 4, 8 copies,
+// other): about 8 gathers in flight per thread.
+__host__ __device__ constexpr int gs_groups_per_thread(int cls) {
+  return cls <= 1 ? 4 : cls == 2 ? 2 : 1;
+}
+// Blocks of the PCG-form kernel: kGsGroups groups per thread, classes block-aligned.
 inline int gs_cg_blocks(const GsMaps& gs) { return gs.cls.boff[kGsClasses] > 0 ? gs.cls.boff[kGsClasses] : 1; }
 
 }  // namespace nekgpu

@@ -95,22 +95,23 @@ struct Handle {
   std::vector<cudaEvent_t> ax_ev;  // per-launch operator timing pool
   double ms_total = 0.0, ms_axhelm = 0.0;
   int n_axhelm = 0;
-  // graph cache for the PCG iteration chunk
+  // graph cache for the PCG iteration chunk: the captured launches depend on
+  // every pointer and coefficient below, so any change recaptures.
   struct GraphKey {
-    const void* x = nullptr;
-    int prec = -1;
-    int h1mode = -1, h2mode = -1;
-    double h1s = 0, h2s = 0;
-    const void* h1 = nullptr;
-    const void* h2 = nullptr;
-    const void* f = nullptr;
+    const void* ptr[12] = {};
+    int ints[6] = {-1, -1, -1, -1, -1, -1};
+    double dbl[2] = {0, 0};
     bool operator==(const GraphKey& o) const {
-      return x == o.x && prec == o.prec && h1mode == o.h1mode && h2mode == o.h2mode &&
-             h1s == o.h1s && h2s == o.h2s && h1 == o.h1 && h2 == o.h2 && f == o.f;
+      for (int i = 0; i < 12; ++i)
+        if (ptr[i] != o.ptr[i]) return false;
+      for (int i = 0; i < 6; ++i)
+        if (ints[i] != o.ints[i]) return false;
+      return dbl[0] == o.dbl[0] && dbl[1] == o.dbl[1];
     }
   };
   GraphKey gkey;
   cudaGraphExec_t gexec = nullptr;
+  int gchunk = 0;  // iterations captured in gexec
   int graph_chunk = 16;
   bool use_graph = true;
 };

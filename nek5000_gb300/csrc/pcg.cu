@@ -26,7 +26,7 @@ constexpr int NEKGPU_ENOMEM_ = -4;
 
 inline int vec_blocks(int64_t n) {
   int64_t b = (n + kVecThreads - 1) / kVecThreads;
-  return (int)std::min<int64_t>(std::max<int64_t>(b, 1), 152 * 4);
+  return (int)std::min<int64_t>(std::max<int64_t>(b, 1), 152 * 6);
 }
 
 // ---- min/max of h1 and h2 (uniformity detection) ---------------------------
@@ -204,7 +204,8 @@ __global__ void __launch_bounds__(kVecThreads)
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   constexpr int W = 16 / sizeof(T);
   const int64_t nv = VEC ? n / W : 0;
-  for (int64_t iv = gtid; iv < nv; iv += stride) {
+  int64_t iv = gtid;
+  for (; iv < nv; iv += stride) {
     T xx[W], rr[W], pp[W], ww[W], dd[W], mm[W], bb[W];
     ld16(rr, r, iv);
     ld16(dd, d, iv);
@@ -563,6 +564,57 @@ PcgResult pcg_solve(Handle& h, const OpData<T>& op, PcgWork<T>& wk, T* x, const 
     h.ax_ev.assign(2 * (size_t)chunk, nullptr);
     for (auto& e : h.ax_ev) cudaEventCreate(&e);
   }
+  // One chunk = `chunk` iterations of the three kernels.  With graphs on, the
+  // chunk is captured once per argument set and replayed.
+  auto enqueue_chunk = [&](int k) -> cudaError_t {
+    for (int q = 0; q < k; ++q) {
+      int nAb = 0;
+      if (h.timing) cudaEventRecord(h.ax_ev[2 * q], s);
+      cudaError_t e = launch_A<T>(h, op, wk, c, exact, &nAb);
+      if (h.timing) cudaEventRecord(h.ax_ev[2 * q + 1], s);
+      if (e != cudaSuccess) return e;
+      gs_cg<T>(m.gs, wk.w.ptr, wk.p.ptr, wk.segmask.ptr, wk.segmsum.ptr, h.cg, h.partialA.ptr,
+               nAb, h.partialB.ptr, s);
+      launch_C<T>(h, wk, x, mult, binv, exact, false);
+    }
+    return cudaGetLastError();
+  };
+  bool graph = h.use_graph;
+  if (graph) {
+    Handle::GraphKey key;
+    const void* ptrs[12] = {x,        f,         mask,      mult,         binv,        wk.r.ptr,
+                            wk.w.ptr, wk.p.ptr,  wk.d.ptr,  wk.segmask.ptr, c.h1,      c.h2};
+    for (int i = 0; i < 12; ++i) key.ptr[i] = ptrs[i];
+    key.ints[0] = (int)sizeof(T);
+    key.ints[1] = c.h1mode;
+    key.ints[2] = c.h2mode;
+    key.ints[3] = (int)exact + 2 * (int)h.timing + 4 * (int)m.use_tma;
+    key.ints[4] = chunk;
+    key.ints[5] = m.nel;
+    key.dbl[0] = (double)c.h1s;
+    key.dbl[1] = (double)c.h2s;
+    if (!h.gexec || !(key == h.gkey)) {
+      if (h.gexec) cudaGraphExecDestroy(h.gexec);
+      h.gexec = nullptr;
+      cudaGraph_t g = nullptr;
+      cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed);
+      capturing() = true;
+      if (e == cudaSuccess) e = enqueue_chunk(chunk);
+      capturing() = false;
+      cudaError_t e2 = cudaStreamEndCapture(s, &g);
+      if (e == cudaSuccess) e = e2;
+      if (e == cudaSuccess) e = cudaGraphInstantiate(&h.gexec, g, 0);
+      if (g) cudaGraphDestroy(g);
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        h.gexec = nullptr;
+        graph = false;  // fall back to direct launches (same kernels)
+      } else {
+        h.gkey = key;
+        h.gchunk = chunk;
+      }
+    }
+  }
   int launched = 0, iter_before = 0;
   for (;;) {
     cudaMemcpyAsync(h.cg_host, h.cg, sizeof(CgScalars), cudaMemcpyDeviceToHost, s);
@@ -582,21 +634,21 @@ PcgResult pcg_solve(Handle& h, const OpData<T>& op, PcgWork<T>& wk, T* x, const 
     }
     if (h.cg_host->done) break;
     iter_before = h.cg_host->iter;
-    const int left = h.cg_host->maxiter - h.cg_host->iter + 1;
-    const int k = std::min(chunk, std::max(left, 1));
-    for (int q = 0; q < k; ++q) {
-      int nAb = 0;
-      if (h.timing) cudaEventRecord(h.ax_ev[2 * q], s);
-      cudaError_t e = launch_A<T>(h, op, wk, c, exact, &nAb);
-      if (h.timing) cudaEventRecord(h.ax_ev[2 * q + 1], s);
-      if (e != cudaSuccess) {
-        res.status = -3;
-        set_error(h, std::string("pcg axhelm: ") + cudaGetErrorString(e));
-        return res;
-      }
-      gs_cg<T>(m.gs, wk.w.ptr, wk.p.ptr, wk.segmask.ptr, wk.segmsum.ptr, h.cg, h.partialA.ptr, nAb,
-               h.partialB.ptr, s);
-      launch_C<T>(h, wk, x, mult, binv, exact, false);
+    cudaError_t e;
+    int k;
+    if (graph) {
+      k = chunk;
+      count_launch(3LL * chunk);
+      e = cudaGraphLaunch(h.gexec, s);
+    } else {
+      const int left = h.cg_host->maxiter - h.cg_host->iter + 1;
+      k = std::min(chunk, std::max(left, 1));
+      e = enqueue_chunk(k);
+    }
+    if (e != cudaSuccess) {
+      res.status = -3;
+      set_error(h, std::string("pcg iteration launch: ") + cudaGetErrorString(e));
+      return res;
     }
     launched = k;
   }

@@ -144,11 +144,12 @@ def _rhs(P, seed, dist="uniform"):
     return P["bm1"] * f
 
 
-@pytest.mark.parametrize("exact", [True, False])
-def test_hmholtz_poisson_config1(gpu_lib, oracle, cfg1, exact):
+@pytest.mark.parametrize("exact,graph", [(True, 1), (False, 1), (False, 0)])
+def test_hmholtz_poisson_config1(gpu_lib, oracle, cfg1, exact, graph):
     P = cfg1
     lib = _setup(gpu_lib, P)
     lib.set_exact(exact)
+    lib.set_option(6, graph)
     n = P["n"]
     h1, h2 = np.ones(n), np.zeros(n)
     rhs = _rhs(P, 0)
