@@ -139,9 +139,11 @@ int chktcg1_dev(Handle* H, double* tol, const double* res, const Coef<double>& c
 int cggo_dev(Handle* H, double* x, const double* f, const double* h1, const double* h2,
              const double* mask, const double* mult, double tin, int maxit, int maxcg,
              const double* binv, int* niter, double* rbn0, double* rbn2) {
+  H->err.clear();
   Coef<double> c;
   int rc = make_coef(H, h1, h2, c);
   if (rc) return rc;
+  if (cuda_pending(*H, "cggo: coefficient scan")) return NEKGPU_ECUDA;
   // non-trivial null space (no Dirichlet point, h2 == 0) needs the mean
   // correction of hmholtz.f:705-750, which this solver does not provide
   int st = 0;
@@ -328,6 +330,7 @@ int nekgpu_setup(const int64_t* handle, const int* lx1, const int* nel, const do
   std::string err;
   int rc = gs_setup(m.gs, glo_num, n, m.nx1, err);
   if (rc) return fail(H, rc == -4 ? NEKGPU_ENOMEM : NEKGPU_EINVAL, err);
+  if (cuda_pending(*H, "setup")) return NEKGPU_ECUDA;
   H->has_mesh = true;
   return NEKGPU_OK;
 }
@@ -465,7 +468,9 @@ int nekgpu_cggo_dev(const int64_t* handle, double* x, const double* f, const dou
     return fail(H, NEKGPU_EINVAL, "null argument");
   H->ms_axhelm = 0.0;
   H->n_axhelm = 0;
+  if (cuda_pending(*H, "cggo: on entry")) return NEKGPU_ECUDA;
   if (H->timing) cudaEventRecord(H->evt0, H->stream);
+  if (cuda_pending(*H, "cggo: timing event")) return NEKGPU_ECUDA;
   int rc = cggo_dev(H, x, f, h1, h2, mask, mult, *tin, *maxit, maxcg ? *maxcg : 900, binv, niter,
                     rbn0, rbn2);
   if (H->timing) {

@@ -165,4 +165,12 @@ MixedResult mixed_solve(Handle& h, double* x, const double* f, const double* h1,
 
 void set_error(Handle& h, const std::string& msg);
 
+// Returns true (and records `where`) when a CUDA error is pending.
+inline bool cuda_pending(Handle& h, const char* where) {
+  const cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) return false;
+  h.err = std::string(where) + ": " + cudaGetErrorString(e);
+  return true;
+}
+
 }  // namespace nekgpu

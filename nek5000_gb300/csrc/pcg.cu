@@ -384,6 +384,12 @@ static void launch_setprec_nx(Handle& h, double* d, const Coef<double>& c) {
 
 // d = 1/dssum(diag)  (setprec, hmholtz.f:380-524), FP64
 int setprec_f64(Handle& h, double* d, const Coef<double>& c) {
+  cudaError_t pre = cudaGetLastError();
+  if (pre != cudaSuccess) {
+    set_error(h, std::string("setprec: error pending from an earlier call: ") +
+                     cudaGetErrorString(pre));
+    return -3;
+  }
   switch (h.mesh.nx1) {
     case 2: launch_setprec_nx<2>(h, d, c); break;
     case 3: launch_setprec_nx<3>(h, d, c); break;
@@ -398,10 +404,23 @@ int setprec_f64(Handle& h, double* d, const Coef<double>& c) {
     case 12: launch_setprec_nx<12>(h, d, c); break;
     default: return -1;
   }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_error(h, std::string("setprec kernel: ") + cudaGetErrorString(e));
+    return -3;
+  }
   gs_op<double>(h.mesh.gs, d, 0, h.stream);
+  if ((e = cudaGetLastError()) != cudaSuccess) {
+    set_error(h, std::string("setprec dssum: ") + cudaGetErrorString(e));
+    return -3;
+  }
   count_launch();
   invert_kernel<<<vec_blocks(h.mesh.n), kVecThreads, 0, h.stream>>>(d, h.mesh.n);
-  return cudaGetLastError() == cudaSuccess ? 0 : -3;
+  if ((e = cudaGetLastError()) != cudaSuccess) {
+    set_error(h, std::string("setprec invert: ") + cudaGetErrorString(e));
+    return -3;
+  }
+  return 0;
 }
 
 // ---- PCG driver ------------------------------------------------------------
@@ -485,8 +504,16 @@ PcgResult pcg_solve(Handle& h, const OpData<T>& op, PcgWork<T>& wk, T* x, const 
     return res;
   }
   // fmax = glamax(f): an all-zero rhs returns x = 0 at once (hmholtz.f:699-701)
+  if (cuda_pending(h, "pcg: before the solve")) {
+    res.status = -3;
+    return res;
+  }
   int st = 0;
   const double fmax = device_absmax<T>(h, f, n, &st);
+  if (cuda_pending(h, "pcg: max|f|")) {
+    res.status = -3;
+    return res;
+  }
   if (st) {
     res.status = st;
     set_error(h, "pcg: reduction failed");
@@ -494,6 +521,10 @@ PcgResult pcg_solve(Handle& h, const OpData<T>& op, PcgWork<T>& wk, T* x, const 
   }
   count_launch();
   zero_kernel<T><<<vec_blocks(n), kVecThreads, 0, s>>>(x, n);
+  if (cuda_pending(h, "pcg: zero x")) {
+    res.status = -3;
+    return res;
+  }
   if (fmax == 0.0) return res;
 
   // Jacobi diagonal: given by the caller (FP32 inner solves get the FP64
@@ -508,7 +539,7 @@ PcgResult pcg_solve(Handle& h, const OpData<T>& op, PcgWork<T>& wk, T* x, const 
   }
   if (st) {
     res.status = st;
-    set_error(h, "pcg: setprec failed");
+    if (h.err.empty()) set_error(h, "pcg: setprec failed");
     return res;
   }
   // boundary-group mask / multiplicity weights
@@ -579,7 +610,9 @@ PcgResult pcg_solve(Handle& h, const OpData<T>& op, PcgWork<T>& wk, T* x, const 
     }
     return cudaGetLastError();
   };
-  bool graph = h.use_graph;
+  // Events recorded by a graph's nodes cannot be paired for elapsed time, so
+  // per-kernel timing runs the same kernels as direct launches.
+  bool graph = h.use_graph && !h.timing;
   if (graph) {
     Handle::GraphKey key;
     const void* ptrs[12] = {x,        f,         mask,      mult,         binv,        wk.r.ptr,
@@ -588,7 +621,7 @@ PcgResult pcg_solve(Handle& h, const OpData<T>& op, PcgWork<T>& wk, T* x, const 
     key.ints[0] = (int)sizeof(T);
     key.ints[1] = c.h1mode;
     key.ints[2] = c.h2mode;
-    key.ints[3] = (int)exact + 2 * (int)h.timing + 4 * (int)m.use_tma;
+    key.ints[3] = (int)exact + 4 * (int)m.use_tma;
     key.ints[4] = chunk;
     key.ints[5] = m.nel;
     key.dbl[0] = (double)c.h1s;
@@ -627,7 +660,10 @@ PcgResult pcg_solve(Handle& h, const OpData<T>& op, PcgWork<T>& wk, T* x, const 
       const int live = std::min(launched, h.cg_host->iter - iter_before);
       for (int q = 0; q < live; ++q) {
         float ms = 0.f;
-        cudaEventElapsedTime(&ms, h.ax_ev[2 * q], h.ax_ev[2 * q + 1]);
+        if (cudaEventElapsedTime(&ms, h.ax_ev[2 * q], h.ax_ev[2 * q + 1]) != cudaSuccess) {
+          cudaGetLastError();
+          ms = 0.f;
+        }
         h.ms_axhelm += ms;
       }
       h.n_axhelm += live;
