@@ -162,6 +162,37 @@ int nekgpu_hmholtz_mixed(const int64_t *handle, double *u, double *rhs, const do
                          const double *binv, const double *inner_tol, int *niter_outer,
                          int *niter_inner, double *rbn0, double *rbn2);
 
+/* ---- batched solves ---------------------------------------------------- */
+/* Many independent problems (each its own mesh, order and size) solved
+ * together: every PCG phase is one launch over all problems, iterations are
+ * replayed as captured CUDA graphs, and every problem stops at its own
+ * convergence test.  No reference counterpart: the reference solves one
+ * field per hmholtz call (velocity components one after another,
+ * core/induct.f:1064-1071); this runs such solves, and unrelated problems,
+ * side by side on one GPU. */
+int nekgpu_batch_create(const int *device, int64_t *batch);
+/* Add one problem's mesh (arguments as nekgpu_setup); *index receives its slot. */
+int nekgpu_batch_add(const int64_t *batch, const int *lx1, const int *nel, const double *dxm1,
+                     const double *g1, const double *g2, const double *g3, const double *g4,
+                     const double *g5, const double *g6, const double *bm1,
+                     const int64_t *glo_num, int *index);
+/* Solve all problems (device arrays, one pointer per problem, in slot order).
+ * Per problem: the same inputs and stopping rule as nekgpu_cggo_dev (tin < 0
+ * relative; no 900 cap: *maxit iterations at most).  *mixed != 0 selects the
+ * FP32-inner / FP64-defect-correction form (inner tolerance *inner_tol).
+ * Outputs per problem: niter (PCG iterations; total inner iterations when
+ * mixed), nouter (outer steps, mixed only; may be NULL), rbn0, rbn2 and a
+ * status code (0, NEKGPU_ENOTCONV, NEKGPU_ENAN, ...). */
+int nekgpu_batch_solve_dev(const int64_t *batch, const int *nprob, double *const *x,
+                           const double *const *f, const double *const *h1,
+                           const double *const *h2, const double *const *mask,
+                           const double *const *mult, const double *const *binv,
+                           const double *tin, const int *maxit, const int *mixed,
+                           const double *inner_tol, int *niter, int *nouter, double *rbn0,
+                           double *rbn2, int *status);
+int nekgpu_batch_last_error(const int64_t *batch, char *buf, const int *buflen);
+int nekgpu_batch_destroy(int64_t *batch);
+
 /* ---- timing of the last solve (device time, CUDA events) ----------------- */
 /* ms_total: whole call on the device; ms_axhelm: summed axhelm-kernel time of
  * the last cggo when the handle's kernel timing is on (nekgpu_set_timing). */

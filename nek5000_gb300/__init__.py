@@ -5,6 +5,6 @@ ABI of include/nekgpu.h).  This package holds its sources (csrc/), the build
 recipe (build.py), a ctypes binding (_capi.py), a front end with the
 reference's routine names (solver.py) and a synthetic box mesher (mesh.py).
 """
-from .solver import NekGpu  # noqa: F401
+from .solver import NekGpu, NekGpuBatch  # noqa: F401
 
-__all__ = ["NekGpu"]
+__all__ = ["NekGpu", "NekGpuBatch"]

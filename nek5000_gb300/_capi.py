@@ -56,6 +56,12 @@ SIGNATURES = {
                               _DP, _DP],
     "nekgpu_hmholtz_mixed": [_I64P, _P, _P, _P, _P, _P, _P, _IP, _DP, _IP, _IP, _P, _DP, _IP, _IP,
                              _DP, _DP],
+    "nekgpu_batch_create": [_IP, _I64P],
+    "nekgpu_batch_add": [_I64P, _IP, _IP, _P, _P, _P, _P, _P, _P, _P, _P, _P, _IP],
+    "nekgpu_batch_solve_dev": [_I64P, _IP, _P, _P, _P, _P, _P, _P, _P, _DP, _IP, _IP, _DP, _P, _P,
+                               _P, _P, _P],
+    "nekgpu_batch_last_error": [_I64P, C.c_char_p, _IP],
+    "nekgpu_batch_destroy": [_I64P],
 }
 
 _lib = None

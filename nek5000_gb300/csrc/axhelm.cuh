@@ -61,32 +61,33 @@ __host__ __device__ constexpr size_t axhelm_smem_bytes(int epb) {
   return (size_t)(2 * NX * (NX + 1) + epb * 3 * AxShape<NX>::LP) * sizeof(T);
 }
 
+// Block body: `blk` is the element-block index, thread (tx = i + NX*j, ty)
+// works on element blk*epb + ty; threads with ty >= epb take part in the
+// barriers only.  `smem_raw` holds axhelm_smem_bytes<NX,T>(epb) bytes.
 template <int NX, typename T, bool EXACT, bool FUSED>
-__global__ void __launch_bounds__(256) axhelm_kernel(const AxArgs<T> a) {
+__device__ __forceinline__ void axhelm_body(const AxArgs<T>& a, int blk, int tx, int ty, int epb,
+                                            unsigned char* smem_raw, double* red) {
   constexpr int R = AxShape<NX>::R, LP = AxShape<NX>::LP, P = AxShape<NX>::P;
   constexpr int NXY = NX * NX;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ double red[32];
   T* sD = reinterpret_cast<T*>(smem_raw);  // sD[i*R+l]  = D[i][l]
   T* sDT = sD + NX * R;                    // sDT[i*R+l] = D[l][i]
-  T* su = sDT + NX * R + threadIdx.y * 3 * LP;
+  const int tyc = ty < epb ? ty : 0;
+  T* su = sDT + NX * R + tyc * 3 * LP;
   T* st1 = su + LP;
   T* st2 = st1 + LP;
 
-  if constexpr (FUSED) {
-    if (a.cg->done) return;  // uniform over the grid: nothing to do after convergence
-  }
-  const int tid = threadIdx.x;
+  const int tid = tx;
   const int i = tid % NX, j = tid / NX;
-  const int ft = tid + NXY * threadIdx.y, nthr = NXY * blockDim.y;
-  for (int q = ft; q < NXY; q += nthr) {
-    const int r = q / NX, c = q % NX;
-    const T v = a.D[q];
-    sD[r * R + c] = v;
-    sDT[c * R + r] = v;
-  }
-  const int e = blockIdx.x * blockDim.y + threadIdx.y;
-  const bool act = e < a.nel;
+  const int ft = tx + NXY * ty, nthr = NXY * epb;
+  if (ty < epb)
+    for (int q = ft; q < NXY; q += nthr) {
+      const int r = q / NX, c = q % NX;
+      const T v = a.D[q];
+      sD[r * R + c] = v;
+      sDT[c * R + r] = v;
+    }
+  const int e = blk * epb + ty;
+  const bool act = ty < epb && e < a.nel;
   const size_t eo = (size_t)(act ? e : 0) * P;
 
   T beta = T(0);
@@ -107,7 +108,7 @@ __global__ void __launch_bounds__(256) axhelm_kernel(const AxArgs<T> a) {
       }
     }
     ru[k] = v;
-    su[k * NX * R + j * R + i] = v;
+    if (ty < epb) su[k * NX * R + j * R + i] = v;
   }
   __syncthreads();
 
@@ -162,8 +163,10 @@ __global__ void __launch_bounds__(256) axhelm_kernel(const AxArgs<T> a) {
       t2 *= h;
       t3 *= h;
     }
-    st1[k * NX * R + j * R + i] = t1;
-    st2[k * NX * R + j * R + i] = t2;
+    if (ty < epb) {
+      st1[k * NX * R + j * R + i] = t1;
+      st2[k * NX * R + j * R + i] = t2;
+    }
     // tm3(ij,m) = sum_k tmp3(ij,k) D(k,m)      (mxm(tmp3,nxy,dzm1,lz1,tm3,lz1))
 #pragma unroll
     for (int m = 0; m < NX; ++m) {
@@ -205,8 +208,19 @@ __global__ void __launch_bounds__(256) axhelm_kernel(const AxArgs<T> a) {
   }
   if constexpr (FUSED) {
     const double bsum = block_sum((double)dot, red);
-    if (threadIdx.x == 0 && threadIdx.y == 0) a.partial[blockIdx.x] = bsum;
+    if (tx == 0 && ty == 0) a.partial[blk] = bsum;
   }
+}
+
+template <int NX, typename T, bool EXACT, bool FUSED>
+__global__ void __launch_bounds__(256) axhelm_kernel(const AxArgs<T> a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ double red[32];
+  if constexpr (FUSED) {
+    if (a.cg->done) return;  // uniform over the grid: nothing to do after convergence
+  }
+  axhelm_body<NX, T, EXACT, FUSED>(a, blockIdx.x, threadIdx.x, threadIdx.y, blockDim.y, smem_raw,
+                                   red);
 }
 
 // Elements per block for a given lx1 (about 256 threads, at least one element).

@@ -1,0 +1,685 @@
+// batch.cu -- many independent Helmholtz solves of uneven size and order,
+// advanced together.
+//
+// Every problem keeps its own mesh, work vectors, PCG scalars and partial
+// sums (one Handle each, all on the batch's stream).  One PCG iteration of
+// the whole batch is three launches -- the fused operator, the boundary-group
+// gather-scatter and the update -- each covering every problem: a per-block
+// table maps a block to its problem, and the block runs that problem's body
+// (the operator dispatches on the problem's lx1).  A problem that has
+// converged makes its blocks return at once, so each one stops at its own
+// iteration count, exactly as if it were solved alone.  Chunks of iterations
+// are captured once as a CUDA graph and replayed.
+//
+// The mixed form runs FP64 defect correction per problem around the batched
+// FP32 PCG: every outer step solves all problems not yet converged together.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <mutex>
+
+#include "cg_kernels.cuh"
+#include "gs_kernels.cuh"
+#include "impl.cuh"
+#include "nekgpu.h"
+
+namespace nekgpu {
+
+template <typename T>
+struct BDesc {
+  AxArgs<T> ax;  // fused operator: au = w, u = p (old), p, r, d, cg, partial = rho partials
+  int nx1, epb, nblkA;
+  const int* bstart;
+  const int* bidx;
+  GsClasses cls;
+  const T* segmask;
+  const T* segmsum;
+  double* partialB;
+  int nblkB;
+  T* x;
+  const T* mult;
+  const T* binv;
+  int64_t n;
+  double* partialC;
+  int nblkC, vec;
+  CgScalars* cg;
+};
+
+namespace {
+
+constexpr int kBatchThreads = 256;
+
+template <typename T, int NX>
+__device__ __forceinline__ void batch_ax_nx(const AxArgs<T>& a, int blk, int epb,
+                                            unsigned char* smem, double* red) {
+  constexpr int NXY = NX * NX;
+  axhelm_body<NX, T, false, true>(a, blk, threadIdx.x % NXY, threadIdx.x / NXY, epb, smem, red);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kBatchThreads)
+    batch_axhelm_kernel(const BDesc<T>* __restrict__ D, const int* __restrict__ map,
+                        const int* __restrict__ base) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ double red[32];
+  const int pi = map[blockIdx.x];
+  const BDesc<T>* d = D + pi;
+  if (d->cg->done) return;
+  const AxArgs<T> a = d->ax;
+  const int blk = blockIdx.x - base[pi], epb = d->epb;
+  switch (d->nx1) {
+    case 2: batch_ax_nx<T, 2>(a, blk, epb, smem, red); break;
+    case 3: batch_ax_nx<T, 3>(a, blk, epb, smem, red); break;
+    case 4: batch_ax_nx<T, 4>(a, blk, epb, smem, red); break;
+    case 5: batch_ax_nx<T, 5>(a, blk, epb, smem, red); break;
+    case 6: batch_ax_nx<T, 6>(a, blk, epb, smem, red); break;
+    case 7: batch_ax_nx<T, 7>(a, blk, epb, smem, red); break;
+    case 8: batch_ax_nx<T, 8>(a, blk, epb, smem, red); break;
+    case 9: batch_ax_nx<T, 9>(a, blk, epb, smem, red); break;
+    case 10: batch_ax_nx<T, 10>(a, blk, epb, smem, red); break;
+    case 11: batch_ax_nx<T, 11>(a, blk, epb, smem, red); break;
+    default: batch_ax_nx<T, 12>(a, blk, epb, smem, red); break;
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kGsThreads)
+    batch_gs_kernel(const BDesc<T>* __restrict__ D, const int* __restrict__ map,
+                    const int* __restrict__ base) {
+  __shared__ double red[32];
+  __shared__ int am_last;
+  const int pi = map[blockIdx.x];
+  const BDesc<T>* d = D + pi;
+  if (d->cg->done) return;
+  gs_cg_body<T>(d->ax.au, d->ax.p, d->bstart, d->bidx, d->cls, d->segmask, d->segmsum, d->cg,
+                d->ax.partial, d->nblkA, d->partialB, blockIdx.x - base[pi], d->nblkB, red,
+                &am_last);
+}
+
+template <typename T, bool FIRST>
+__global__ void __launch_bounds__(kBatchThreads)
+    batch_update_kernel(const BDesc<T>* __restrict__ D, const int* __restrict__ map,
+                        const int* __restrict__ base) {
+  __shared__ double red[32];
+  __shared__ int am_last;
+  const int pi = map[blockIdx.x];
+  const BDesc<T>* d = D + pi;
+  if (d->cg->done) return;
+  const int blk = blockIdx.x - base[pi];
+  if (d->vec)
+    cg_update_body<T, false, FIRST, true>(d->x, const_cast<T*>(d->ax.r), d->ax.p, d->ax.au,
+                                          d->ax.d, d->mult, d->binv, d->n, d->cg, d->partialC, blk,
+                                          d->nblkC, red, &am_last);
+  else
+    cg_update_body<T, false, FIRST, false>(d->x, const_cast<T*>(d->ax.r), d->ax.p, d->ax.au,
+                                           d->ax.d, d->mult, d->binv, d->n, d->cg, d->partialC,
+                                           blk, d->nblkC, red, &am_last);
+}
+
+template <int NX, typename T>
+constexpr size_t ax_smem() {
+  return axhelm_smem_bytes<NX, T>(axhelm_epb(NX));
+}
+
+template <typename T>
+size_t batch_smem(int nx) {
+  switch (nx) {
+    case 2: return ax_smem<2, T>();
+    case 3: return ax_smem<3, T>();
+    case 4: return ax_smem<4, T>();
+    case 5: return ax_smem<5, T>();
+    case 6: return ax_smem<6, T>();
+    case 7: return ax_smem<7, T>();
+    case 8: return ax_smem<8, T>();
+    case 9: return ax_smem<9, T>();
+    case 10: return ax_smem<10, T>();
+    case 11: return ax_smem<11, T>();
+    default: return ax_smem<12, T>();
+  }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+struct Batch {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<std::unique_ptr<Handle>> probs;
+  std::string err;
+  CgScalars* cg_host_all = nullptr;  // pinned, one per problem
+  size_t cg_host_cap = 0;
+  DevBuf<unsigned char> desc;
+  DevBuf<int> map, base;
+  cudaGraphExec_t gexec = nullptr;
+  std::vector<int64_t> gkey;
+  int chunk = 16;
+  bool use_graph = true;
+};
+
+namespace {
+
+struct BatchLaunch {
+  int gridA = 0, gridB = 0, gridC = 0;
+  size_t smem = 0;
+  const void* desc = nullptr;
+  const int *mapA, *mapB, *mapC, *baseA, *baseB, *baseC;
+};
+
+// Builds descriptors and block maps for the listed problems, uploads them.
+template <typename T>
+int batch_tables(Batch& B, const std::vector<int>& ids, const std::vector<Coef<T>>& coef,
+                 const std::vector<T*>& xs, const std::vector<const T*>& mults,
+                 const std::vector<const T*>& binvs, BatchLaunch& L) {
+  const int np = (int)ids.size();
+  std::vector<BDesc<T>> hd(np);
+  std::vector<int> mapA, mapB, mapC, baseA(np), baseB(np), baseC(np);
+  size_t smem = 0;
+  for (int q = 0; q < np; ++q) {
+    Handle& h = *B.probs[ids[q]];
+    Mesh& m = h.mesh;
+    PcgWork<T>& wk = [&]() -> PcgWork<T>& {
+      if constexpr (std::is_same<T, double>::value) return h.w64;
+      else return h.w32;
+    }();
+    const OpData<T>& op = [&]() -> const OpData<T>& {
+      if constexpr (std::is_same<T, double>::value) return m.f64;
+      else return m.f32;
+    }();
+    BDesc<T>& d = hd[q];
+    memset(&d, 0, sizeof(d));
+    AxArgs<T>& a = d.ax;
+    a.au = wk.w.ptr;
+    a.u = wk.p.ptr;
+    a.G = op.G;
+    a.bm1 = op.bm1;
+    a.h1 = coef[q].h1;
+    a.h2 = coef[q].h2;
+    a.h1s = coef[q].h1s;
+    a.h2s = coef[q].h2s;
+    a.h1mode = coef[q].h1mode;
+    a.h2mode = coef[q].h2mode;
+    a.D = op.D;
+    a.nel = m.nel;
+    a.p = wk.p.ptr;
+    a.r = wk.r.ptr;
+    a.d = wk.d.ptr;
+    a.cg = h.cg;
+    a.partial = h.partialA.ptr;
+    a.err = m.dev_err;
+    a.skip = m.gs.skip;
+    d.nx1 = m.nx1;
+    d.epb = axhelm_epb(m.nx1);
+    d.nblkA = (m.nel + d.epb - 1) / d.epb;
+    d.bstart = m.gs.bstart;
+    d.bidx = m.gs.bidx;
+    d.cls = m.gs.cls;
+    d.segmask = wk.segmask.ptr;
+    d.segmsum = wk.segmsum.ptr;
+    d.partialB = h.partialB.ptr;
+    d.nblkB = gs_cg_blocks(m.gs);
+    d.x = xs[q];
+    d.mult = mults[q];
+    d.binv = binvs[q];
+    d.n = m.n;
+    d.partialC = h.partialC.ptr;
+    d.nblkC = pcg_vec_blocks(m.n);
+    auto al = [](const void* p) { return ((uintptr_t)p & 15u) == 0; };
+    d.vec = al(d.x) && al(wk.r.ptr) && al(wk.p.ptr) && al(wk.w.ptr) && al(wk.d.ptr) &&
+            al(d.mult) && al(d.binv);
+    d.cg = h.cg;
+    smem = std::max(smem, batch_smem<T>(m.nx1));
+    baseA[q] = (int)mapA.size();
+    mapA.insert(mapA.end(), d.nblkA, q);
+    baseB[q] = (int)mapB.size();
+    mapB.insert(mapB.end(), d.nblkB, q);
+    baseC[q] = (int)mapC.size();
+    mapC.insert(mapC.end(), d.nblkC, q);
+  }
+  const size_t dbytes = sizeof(BDesc<T>) * np;
+  const size_t nmap = mapA.size() + mapB.size() + mapC.size();
+  if (B.desc.ensure(dbytes) || B.map.ensure(nmap) || B.base.ensure(3 * (size_t)np)) return -4;
+  std::vector<int> maps;
+  maps.reserve(nmap);
+  maps.insert(maps.end(), mapA.begin(), mapA.end());
+  maps.insert(maps.end(), mapB.begin(), mapB.end());
+  maps.insert(maps.end(), mapC.begin(), mapC.end());
+  std::vector<int> bases;
+  bases.insert(bases.end(), baseA.begin(), baseA.end());
+  bases.insert(bases.end(), baseB.begin(), baseB.end());
+  bases.insert(bases.end(), baseC.begin(), baseC.end());
+  cudaMemcpyAsync(B.desc.ptr, hd.data(), dbytes, cudaMemcpyHostToDevice, B.stream);
+  cudaMemcpyAsync(B.map.ptr, maps.data(), nmap * sizeof(int), cudaMemcpyHostToDevice, B.stream);
+  cudaMemcpyAsync(B.base.ptr, bases.data(), bases.size() * sizeof(int), cudaMemcpyHostToDevice,
+                  B.stream);
+  if (cudaStreamSynchronize(B.stream) != cudaSuccess) return -3;
+  L.gridA = (int)mapA.size();
+  L.gridB = (int)mapB.size();
+  L.gridC = (int)mapC.size();
+  L.smem = smem;
+  L.desc = B.desc.ptr;
+  L.mapA = B.map.ptr;
+  L.mapB = B.map.ptr + mapA.size();
+  L.mapC = B.map.ptr + mapA.size() + mapB.size();
+  L.baseA = B.base.ptr;
+  L.baseB = B.base.ptr + np;
+  L.baseC = B.base.ptr + 2 * np;
+  return 0;
+}
+
+template <typename T>
+cudaError_t batch_enqueue(Batch& B, const BatchLaunch& L, int k) {
+  static bool configured = false;
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(batch_axhelm_kernel<T>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)batch_smem<T>(11) + 4096);
+    if (e != cudaSuccess) return e;
+    configured = true;
+  }
+  const BDesc<T>* D = reinterpret_cast<const BDesc<T>*>(L.desc);
+  for (int q = 0; q < k; ++q) {
+    count_launch(3);
+    batch_axhelm_kernel<T><<<L.gridA, kBatchThreads, L.smem, B.stream>>>(D, L.mapA, L.baseA);
+    batch_gs_kernel<T><<<L.gridB, kGsThreads, 0, B.stream>>>(D, L.mapB, L.baseB);
+    batch_update_kernel<T, false><<<L.gridC, kBatchThreads, 0, B.stream>>>(D, L.mapC, L.baseC);
+  }
+  return cudaGetLastError();
+}
+
+// Runs the batched PCG for the listed problems until each has stopped.
+template <typename T>
+int batch_iterate(Batch& B, const std::vector<int>& ids, const BatchLaunch& L) {
+  const int np = (int)ids.size();
+  const BDesc<T>* D = reinterpret_cast<const BDesc<T>*>(L.desc);
+  count_launch();
+  batch_update_kernel<T, true><<<L.gridC, kBatchThreads, 0, B.stream>>>(D, L.mapC, L.baseC);
+  bool graph = B.use_graph;
+  std::vector<int64_t> key = {(int64_t)sizeof(T), L.gridA, L.gridB, L.gridC, (int64_t)L.smem,
+                              (int64_t)(uintptr_t)L.desc, (int64_t)(uintptr_t)L.mapA, B.chunk};
+  if (graph && (!B.gexec || key != B.gkey)) {
+    if (B.gexec) cudaGraphExecDestroy(B.gexec);
+    B.gexec = nullptr;
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(B.stream, cudaStreamCaptureModeRelaxed);
+    capturing() = true;
+    if (e == cudaSuccess) e = batch_enqueue<T>(B, L, B.chunk);
+    capturing() = false;
+    cudaError_t e2 = cudaStreamEndCapture(B.stream, &g);
+    if (e == cudaSuccess) e = e2;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&B.gexec, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      B.gexec = nullptr;
+      graph = false;
+    } else {
+      B.gkey = key;
+    }
+  }
+  if (B.cg_host_cap < (size_t)np) {
+    cudaFreeHost(B.cg_host_all);
+    if (cudaMallocHost(&B.cg_host_all, sizeof(CgScalars) * np) != cudaSuccess) return -4;
+    B.cg_host_cap = np;
+  }
+  for (;;) {
+    for (int q = 0; q < np; ++q)
+      cudaMemcpyAsync(&B.cg_host_all[q], B.probs[ids[q]]->cg, sizeof(CgScalars),
+                      cudaMemcpyDeviceToHost, B.stream);
+    if (cudaStreamSynchronize(B.stream) != cudaSuccess) {
+      B.err = std::string("batch: ") + cudaGetErrorString(cudaGetLastError());
+      return -3;
+    }
+    bool all = true;
+    for (int q = 0; q < np; ++q) all = all && B.cg_host_all[q].done;
+    if (all) break;
+    cudaError_t e;
+    if (graph) {
+      count_launch(3LL * B.chunk);
+      e = cudaGraphLaunch(B.gexec, B.stream);
+    } else {
+      e = batch_enqueue<T>(B, L, B.chunk);
+    }
+    if (e != cudaSuccess) {
+      B.err = std::string("batch launch: ") + cudaGetErrorString(e);
+      return -3;
+    }
+  }
+  for (int q = 0; q < np; ++q) *B.probs[ids[q]]->cg_host = B.cg_host_all[q];
+  return 0;
+}
+
+// Marks a problem finished (trivial right-hand side) on the device.
+void mark_done(Handle& h) {
+  CgScalars& c = *h.cg_host;
+  memset(&c, 0, sizeof(c));
+  c.done = 1;
+  cudaMemcpyAsync(h.cg, &c, sizeof(CgScalars), cudaMemcpyHostToDevice, h.stream);
+}
+
+}  // namespace
+
+// FP64 batched cggo.  Outputs per problem: niter, rbn0, rbn2, status.
+int batch_solve_fp64(Batch& B, int np, double* const* x, const double* const* f,
+                     const double* const* h1, const double* const* h2,
+                     const double* const* mask, const double* const* mult,
+                     const double* const* binv, double tin, int maxiter, int* niter,
+                     double* rbn0, double* rbn2, int* status) {
+  std::vector<int> ids;
+  std::vector<Coef<double>> coef;
+  std::vector<double*> xs;
+  std::vector<const double*> ms, bs;
+  for (int p = 0; p < np; ++p) {
+    Handle& h = *B.probs[p];
+    h.err.clear();
+    Coef<double> c;
+    if (detect_coef<double>(h, h1[p], h2[p], h.mesh.n, c)) {
+      status[p] = NEKGPU_ECUDA;
+      continue;
+    }
+    bool trivial = false;
+    PcgResult r = pcg_prepare<double>(h, h.w64, x[p], f[p], c, mask[p], mult[p], tin, maxiter, 0,
+                                      nullptr, &trivial);
+    status[p] = r.status ? (r.status == -4 ? NEKGPU_ENOMEM : r.status == -1 ? NEKGPU_EINVAL
+                                                                             : NEKGPU_ECUDA)
+                         : 0;
+    niter[p] = 0;
+    rbn0[p] = rbn2[p] = 0.0;
+    if (r.status) continue;
+    if (trivial) {
+      mark_done(h);
+      continue;
+    }
+    ids.push_back(p);
+    coef.push_back(c);
+    xs.push_back(x[p]);
+    ms.push_back(mult[p]);
+    bs.push_back(binv[p]);
+  }
+  if (ids.empty()) return 0;
+  BatchLaunch L;
+  int rc = batch_tables<double>(B, ids, coef, xs, ms, bs, L);
+  if (rc) return rc;
+  rc = batch_iterate<double>(B, ids, L);
+  if (rc) return rc;
+  for (int p : ids) {
+    const CgScalars& c = *B.probs[p]->cg_host;
+    niter[p] = c.niter;
+    rbn0[p] = c.rbn0;
+    rbn2[p] = c.rbn2;
+    status[p] = c.nonfinite ? NEKGPU_ENAN
+                            : (!(c.rbn2 <= c.tol) && c.iter > c.maxiter) ? NEKGPU_ENOTCONV : 0;
+  }
+  return 0;
+}
+
+// Mixed batched solve: per-problem FP64 defect correction, the FP32 inner
+// PCG of all active problems batched.  niter = total inner iterations,
+// nouter = outer steps.
+int batch_solve_mixed(Batch& B, int np, double* const* x, const double* const* f,
+                      const double* const* h1, const double* const* h2,
+                      const double* const* mask, const double* const* mult,
+                      const double* const* binv, double tin, int maxiter, double inner_tol,
+                      int* niter, int* nouter, double* rbn0, double* rbn2, int* status) {
+  constexpr int kMaxOuter = 30;
+  std::vector<Coef<double>> c64(np);
+  std::vector<Coef<float>> c32(np);
+  std::vector<double> rbn(np, 0.0), tol(np, 0.0), scale(np, 1.0);
+  std::vector<char> active(np, 0);
+  for (int p = 0; p < np; ++p) {
+    Handle& h = *B.probs[p];
+    Mesh& m = h.mesh;
+    const int64_t n = m.n;
+    h.err.clear();
+    niter[p] = nouter[p] = 0;
+    rbn0[p] = rbn2[p] = 0.0;
+    status[p] = 0;
+    PcgWork<float>& wk = h.w32;
+    PcgWork<double>& w64 = h.w64;
+    if (ensure_f32(h) || wk.mask.ensure(n) || wk.mult.ensure(n) || wk.binv.ensure(n) ||
+        wk.x.ensure(n) || wk.f.ensure(n) || wk.d.ensure(n) || wk.h1.ensure(n) ||
+        wk.h2.ensure(n) || w64.r.ensure(n) || w64.w.ensure(n) || w64.d.ensure(n)) {
+      status[p] = NEKGPU_ENOMEM;
+      continue;
+    }
+    if (detect_coef<double>(h, h1[p], h2[p], n, c64[p])) {
+      status[p] = NEKGPU_ECUDA;
+      continue;
+    }
+    Coef<float>& c = c32[p];
+    c.h1mode = c64[p].h1mode;
+    c.h2mode = c64[p].h2mode;
+    c.h1s = (float)c64[p].h1s;
+    c.h2s = (float)c64[p].h2s;
+    if (c.h1mode) {
+      cast_to_f32(h, wk.h1.ptr, h1[p], 1.0, n);
+      c.h1 = wk.h1.ptr;
+    }
+    if (c.h2mode == 2) {
+      cast_to_f32(h, wk.h2.ptr, h2[p], 1.0, n);
+      c.h2 = wk.h2.ptr;
+    }
+    cast_to_f32(h, wk.mask.ptr, mask[p], 1.0, n);
+    cast_to_f32(h, wk.mult.ptr, mult[p], 1.0, n);
+    cast_to_f32(h, wk.binv.ptr, binv[p], 1.0, n);
+    if (setprec_f64(h, w64.d.ptr, c64[p])) {
+      status[p] = NEKGPU_ECUDA;
+      continue;
+    }
+    cast_to_f32(h, wk.d.ptr, w64.d.ptr, 1.0, n);
+    cudaMemsetAsync(x[p], 0, n * sizeof(double), h.stream);
+    cudaMemcpyAsync(w64.r.ptr, f[p], n * sizeof(double), cudaMemcpyDeviceToDevice, h.stream);
+    const double r0 = norm64(h, w64.r.ptr, mult[p], binv[p]);
+    if (!(r0 >= 0.0) || !std::isfinite(r0)) {
+      status[p] = NEKGPU_ENAN;
+      continue;
+    }
+    rbn0[p] = rbn2[p] = rbn[p] = r0;
+    tol[p] = tin < 0 ? std::fabs(tin) * r0 : std::fabs(tin);
+    active[p] = r0 > 0.0;
+  }
+  for (int outer = 1; outer <= kMaxOuter; ++outer) {
+    std::vector<int> ids;
+    std::vector<Coef<float>> coefs;
+    std::vector<float*> xs;
+    std::vector<const float*> ms, bs;
+    for (int p = 0; p < np; ++p) {
+      if (!active[p] || status[p]) continue;
+      if (rbn[p] <= tol[p]) {
+        active[p] = 0;
+        continue;
+      }
+      Handle& h = *B.probs[p];
+      const int64_t n = h.mesh.n;
+      int st = 0;
+      const double amax = device_absmax<double>(h, h.w64.r.ptr, n, &st);
+      if (st || amax == 0.0) {
+        active[p] = 0;
+        continue;
+      }
+      scale[p] = std::ldexp(1.0, std::ilogb(amax));
+      cast_to_f32(h, h.w32.f.ptr, h.w64.r.ptr, 1.0 / scale[p], n);
+      bool trivial = false;
+      PcgResult r = pcg_prepare<float>(h, h.w32, h.w32.x.ptr, h.w32.f.ptr, c32[p],
+                                       h.w32.mask.ptr, h.w32.mult.ptr, -inner_tol, maxiter, 0,
+                                       h.w32.d.ptr, &trivial);
+      if (r.status) {
+        status[p] = r.status == -1 ? NEKGPU_EINVAL : NEKGPU_ECUDA;
+        continue;
+      }
+      if (trivial) {
+        active[p] = 0;
+        continue;
+      }
+      ids.push_back(p);
+      coefs.push_back(c32[p]);
+      xs.push_back(h.w32.x.ptr);
+      ms.push_back(h.w32.mult.ptr);
+      bs.push_back(h.w32.binv.ptr);
+    }
+    if (ids.empty()) break;
+    BatchLaunch L;
+    int rc = batch_tables<float>(B, ids, coefs, xs, ms, bs, L);
+    if (rc) return rc;
+    rc = batch_iterate<float>(B, ids, L);
+    if (rc) return rc;
+    for (int p : ids) {
+      Handle& h = *B.probs[p];
+      const int64_t n = h.mesh.n;
+      niter[p] += h.cg_host->niter;
+      nouter[p] = outer;
+      axpy_f32(h, x[p], h.w32.x.ptr, scale[p], n);
+      const double rnew = outer_residual(h, h.w64.r.ptr, f[p], x[p], c64[p], mask[p], mult[p],
+                                         binv[p], h.w64.w.ptr);
+      if (!(rnew >= 0.0) || !std::isfinite(rnew)) {
+        status[p] = NEKGPU_ENAN;
+        continue;
+      }
+      if (rnew >= rbn[p]) active[p] = 0;  // no progress
+      rbn[p] = rbn2[p] = rnew;
+    }
+  }
+  for (int p = 0; p < np; ++p)
+    if (!status[p] && rbn0[p] > 0.0 && !(rbn[p] <= tol[p])) status[p] = NEKGPU_ENOTCONV;
+  return 0;
+}
+
+}  // namespace nekgpu
+
+// ---------------------------------------------------------------------------
+// C ABI
+using nekgpu::Batch;
+
+namespace {
+std::mutex g_bmu;
+std::map<int64_t, std::unique_ptr<Batch>> g_batches;
+int64_t g_bnext = 1;
+thread_local std::string g_berr;
+
+Batch* bget(const int64_t* b) {
+  if (!b) return nullptr;
+  std::lock_guard<std::mutex> lk(g_bmu);
+  auto it = g_batches.find(*b);
+  return it == g_batches.end() ? nullptr : it->second.get();
+}
+int bfail(Batch* B, int code, const std::string& msg) {
+  if (B) B->err = msg;
+  else g_berr = msg;
+  return code;
+}
+}  // namespace
+
+extern "C" {
+
+int nekgpu_batch_create(const int* device, int64_t* batch) {
+  if (!device || !batch) return bfail(nullptr, NEKGPU_EINVAL, "null argument");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+    return bfail(nullptr, NEKGPU_ECUDA, "no CUDA device");
+  if (*device < 0 || *device >= ndev) return bfail(nullptr, NEKGPU_EINVAL, "device out of range");
+  auto B = std::make_unique<Batch>();
+  B->device = *device;
+  cudaSetDevice(B->device);
+  if (cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking) != cudaSuccess)
+    return bfail(nullptr, NEKGPU_ECUDA, "stream creation failed");
+  std::lock_guard<std::mutex> lk(g_bmu);
+  *batch = g_bnext++;
+  g_batches[*batch] = std::move(B);
+  return NEKGPU_OK;
+}
+
+int nekgpu_batch_add(const int64_t* batch, const int* lx1, const int* nel, const double* dxm1,
+                     const double* g1, const double* g2, const double* g3, const double* g4,
+                     const double* g5, const double* g6, const double* bm1,
+                     const int64_t* glo_num, int* index) {
+  Batch* B = bget(batch);
+  if (!B) return bfail(nullptr, NEKGPU_EHANDLE, "unknown batch");
+  if (!lx1 || !nel || !dxm1 || !g1 || !g2 || !g3 || !g4 || !g5 || !g6 || !bm1 || !glo_num)
+    return bfail(B, NEKGPU_EINVAL, "null argument");
+  cudaSetDevice(B->device);
+  auto H = std::make_unique<nekgpu::Handle>();
+  std::string err;
+  if (nekgpu::handle_open(*H, B->device, B->stream, err)) return bfail(B, NEKGPU_ECUDA, err);
+  const double* g[6] = {g1, g2, g3, g4, g5, g6};
+  const int rc = nekgpu::handle_setup(*H, *lx1, *nel, dxm1, g, bm1, glo_num, err);
+  if (rc) {
+    nekgpu::handle_close(*H);
+    return bfail(B, rc, err);
+  }
+  B->probs.push_back(std::move(H));
+  if (index) *index = (int)B->probs.size() - 1;
+  return NEKGPU_OK;
+}
+
+int nekgpu_batch_solve_dev(const int64_t* batch, const int* nprob, double* const* x,
+                           const double* const* f, const double* const* h1,
+                           const double* const* h2, const double* const* mask,
+                           const double* const* mult, const double* const* binv,
+                           const double* tin, const int* maxit, const int* mixed,
+                           const double* inner_tol, int* niter, int* nouter, double* rbn0,
+                           double* rbn2, int* status) {
+  Batch* B = bget(batch);
+  if (!B) return bfail(nullptr, NEKGPU_EHANDLE, "unknown batch");
+  if (!nprob || !x || !f || !h1 || !h2 || !mask || !mult || !binv || !tin || !maxit || !niter ||
+      !rbn0 || !rbn2 || !status)
+    return bfail(B, NEKGPU_EINVAL, "null argument");
+  const int np = *nprob;
+  if (np != (int)B->probs.size())
+    return bfail(B, NEKGPU_EINVAL, "nprob differs from the number of problems added");
+  for (int p = 0; p < np; ++p)
+    if (!x[p] || !f[p] || !h1[p] || !h2[p] || !mask[p] || !mult[p] || !binv[p])
+      return bfail(B, NEKGPU_EINVAL, "null array for problem " + std::to_string(p));
+  cudaSetDevice(B->device);
+  B->err.clear();
+  int rc;
+  if (mixed && *mixed) {
+    std::vector<int> no(np, 0);
+    rc = nekgpu::batch_solve_mixed(*B, np, x, f, h1, h2, mask, mult, binv, *tin, *maxit,
+                                   inner_tol ? *inner_tol : 1e-5, niter, no.data(), rbn0, rbn2,
+                                   status);
+    if (nouter)
+      for (int p = 0; p < np; ++p) nouter[p] = no[p];
+  } else {
+    rc = nekgpu::batch_solve_fp64(*B, np, x, f, h1, h2, mask, mult, binv, *tin, *maxit, niter,
+                                  rbn0, rbn2, status);
+    if (nouter)
+      for (int p = 0; p < np; ++p) nouter[p] = 0;
+  }
+  if (rc) return bfail(B, rc == -4 ? NEKGPU_ENOMEM : NEKGPU_ECUDA,
+                       B->err.empty() ? "batch solve failed" : B->err);
+  for (int p = 0; p < np; ++p)
+    if (status[p] && status[p] != NEKGPU_ENOTCONV && B->err.empty())
+      B->err = "problem " + std::to_string(p) + ": " + B->probs[p]->err;
+  return NEKGPU_OK;
+}
+
+int nekgpu_batch_last_error(const int64_t* batch, char* buf, const int* buflen) {
+  if (!buf || !buflen || *buflen <= 0) return NEKGPU_EINVAL;
+  Batch* B = bget(batch);
+  const std::string& m = B ? B->err : g_berr;
+  const size_t k = std::min<size_t>(m.size(), (size_t)*buflen - 1);
+  std::memcpy(buf, m.data(), k);
+  buf[k] = '\0';
+  return NEKGPU_OK;
+}
+
+int nekgpu_batch_destroy(int64_t* batch) {
+  Batch* B = bget(batch);
+  if (!B) return bfail(nullptr, NEKGPU_EHANDLE, "unknown batch");
+  cudaSetDevice(B->device);
+  cudaStreamSynchronize(B->stream);
+  for (auto& h : B->probs) nekgpu::handle_close(*h);
+  B->probs.clear();
+  if (B->gexec) cudaGraphExecDestroy(B->gexec);
+  cudaFreeHost(B->cg_host_all);
+  B->desc.release();
+  B->map.release();
+  B->base.release();
+  cudaStreamDestroy(B->stream);
+  std::lock_guard<std::mutex> lk(g_bmu);
+  g_batches.erase(*batch);
+  *batch = 0;
+  return NEKGPU_OK;
+}
+
+}  // extern "C"

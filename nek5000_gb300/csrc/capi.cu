@@ -190,8 +190,144 @@ int check_n(Handle* H, const void* p) {
 }  // namespace
 
 namespace nekgpu {
-// extra reductions used above (kinds 4, 5, 6), defined in pcg.cu's sum kernel
+
+int handle_open(Handle& H, int device, cudaStream_t shared, std::string& err) {
+  cudaError_t e;
+  H.device = device;
+  if ((e = cudaSetDevice(device)) != cudaSuccess) {
+    err = std::string("cudaSetDevice: ") + cudaGetErrorString(e);
+    return -3;
+  }
+  if (shared) {
+    H.stream = shared;
+    H.own_stream = false;
+  } else if ((e = cudaStreamCreateWithFlags(&H.stream, cudaStreamNonBlocking)) != cudaSuccess) {
+    err = std::string("stream: ") + cudaGetErrorString(e);
+    return -3;
+  }
+  if (cudaMalloc(&H.cg, sizeof(CgScalars)) != cudaSuccess ||
+      cudaMallocHost(&H.cg_host, sizeof(CgScalars)) != cudaSuccess ||
+      cudaMalloc(&H.flag, sizeof(int) * 4) != cudaSuccess) {
+    err = "handle allocation failed";
+    return -4;
+  }
+  cudaMemset(H.cg, 0, sizeof(CgScalars));
+  cudaEventCreate(&H.ev0);
+  cudaEventCreate(&H.ev1);
+  cudaEventCreate(&H.evt0);
+  cudaEventCreate(&H.evt1);
+  return 0;
 }
+
+void handle_close(Handle& H) {
+  cudaSetDevice(H.device);
+  if (H.stream) cudaStreamSynchronize(H.stream);
+  gs_free(H.mesh.gs);
+  H.mesh.f64.release();
+  H.mesh.f32.release();
+  cudaFree(H.mesh.dev_err);
+  H.mesh.dev_err = nullptr;
+  for (cudaEvent_t e : H.ax_ev) cudaEventDestroy(e);
+  H.ax_ev.clear();
+  if (H.gexec) cudaGraphExecDestroy(H.gexec);
+  H.gexec = nullptr;
+  cudaFree(H.cg);
+  cudaFreeHost(H.cg_host);
+  cudaFree(H.flag);
+  H.cg = nullptr;
+  H.cg_host = nullptr;
+  H.flag = nullptr;
+  cudaEventDestroy(H.ev0);
+  cudaEventDestroy(H.ev1);
+  cudaEventDestroy(H.evt0);
+  cudaEventDestroy(H.evt1);
+  if (H.own_stream && H.stream) cudaStreamDestroy(H.stream);
+  H.stream = nullptr;
+}
+
+int handle_setup(Handle& H, int lx1, int nel, const double* dxm1, const double* const* g6,
+                 const double* bm1, const int64_t* glo_num, std::string& err) {
+  if (lx1 < 2 || lx1 > NEKGPU_MAX_LX1) {
+    err = "lx1 out of range [2, " + std::to_string(NEKGPU_MAX_LX1) + "]";
+    return NEKGPU_EINVAL;
+  }
+  if (nel < 1) {
+    err = "nel must be positive";
+    return NEKGPU_EINVAL;
+  }
+  cudaStreamSynchronize(H.stream);
+  Mesh& m = H.mesh;
+  gs_free(m.gs);
+  m.f64.release();
+  m.f32.release();
+  m.has_f32 = false;
+  H.has_mesh = false;
+  if (H.gexec) cudaGraphExecDestroy(H.gexec);
+  H.gexec = nullptr;
+  m.nx1 = lx1;
+  m.nel = nel;
+  const int P = m.nx1 * m.nx1 * m.nx1;
+  m.n = (int64_t)P * m.nel;
+  const int64_t n = m.n;
+  cudaError_t e;
+  if (cudaMalloc(&m.f64.G, 6 * n * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&m.f64.bm1, n * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&m.f64.D, m.nx1 * m.nx1 * sizeof(double)) != cudaSuccess) {
+    m.f64.release();
+    err = "mesh allocation failed";
+    return NEKGPU_ENOMEM;
+  }
+  // D row-major from the Fortran-ordered dxm1(i,j) = dxm1[i + j*lx1]
+  m.h_D.assign((size_t)m.nx1 * m.nx1, 0.0);
+  for (int i = 0; i < m.nx1; ++i)
+    for (int j = 0; j < m.nx1; ++j) m.h_D[i * m.nx1 + j] = dxm1[i + j * m.nx1];
+  cudaMemcpy(m.f64.D, m.h_D.data(), m.h_D.size() * sizeof(double), cudaMemcpyHostToDevice);
+  DevBuf<double> stage;
+  if (stage.ensure(n)) {
+    err = "staging allocation failed";
+    return NEKGPU_ENOMEM;
+  }
+  for (int q = 0; q < 6; ++q) {
+    if ((e = cudaMemcpy(stage.ptr, g6[q], n * sizeof(double), cudaMemcpyHostToDevice)) !=
+        cudaSuccess) {
+      err = std::string("geometry upload: ") + cudaGetErrorString(e);
+      return NEKGPU_ECUDA;
+    }
+    count_launch();
+    pack_g_kernel<<<nblk(n), 256, 0, H.stream>>>(m.f64.G, stage.ptr, q, P, n);
+    if ((e = cudaStreamSynchronize(H.stream)) != cudaSuccess) {
+      err = std::string("geometry pack: ") + cudaGetErrorString(e);
+      return NEKGPU_ECUDA;
+    }
+  }
+  if ((e = cudaMemcpy(m.f64.bm1, bm1, n * sizeof(double), cudaMemcpyHostToDevice)) != cudaSuccess) {
+    err = std::string("mass upload: ") + cudaGetErrorString(e);
+    return NEKGPU_ECUDA;
+  }
+  // volvm1 = glsum(bm1): serial left-to-right, as one rank of the reference
+  double vol = 0.0;
+  for (int64_t i = 0; i < n; ++i) vol = vol + bm1[i];
+  m.vol = vol;
+  if (!m.dev_err && cudaMalloc(&m.dev_err, sizeof(int)) != cudaSuccess) {
+    err = "flag allocation failed";
+    return NEKGPU_ENOMEM;
+  }
+  cudaMemset(m.dev_err, 0, sizeof(int));
+  const int rc = gs_setup(m.gs, glo_num, n, m.nx1, err);
+  if (rc) return rc == -4 ? NEKGPU_ENOMEM : NEKGPU_EINVAL;
+  e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    err = std::string("setup: ") + cudaGetErrorString(e);
+    return NEKGPU_ECUDA;
+  }
+  H.has_mesh = true;
+  return 0;
+}
+
+}  // namespace nekgpu
+
+namespace {
+}  // namespace
 
 extern "C" {
 
@@ -202,19 +338,8 @@ int nekgpu_init(const int* device, int64_t* handle) {
   if (e != cudaSuccess || ndev == 0) return fail(nullptr, NEKGPU_ECUDA, "no CUDA device");
   if (*device < 0 || *device >= ndev) return fail(nullptr, NEKGPU_EINVAL, "device out of range");
   auto H = std::make_unique<Handle>();
-  H->device = *device;
-  if ((e = cudaSetDevice(H->device)) != cudaSuccess) return cuda_fail(nullptr, e, "cudaSetDevice");
-  if ((e = cudaStreamCreateWithFlags(&H->stream, cudaStreamNonBlocking)) != cudaSuccess)
-    return cuda_fail(nullptr, e, "stream");
-  if ((e = cudaMalloc(&H->cg, sizeof(CgScalars))) != cudaSuccess) return cuda_fail(nullptr, e, "alloc");
-  if ((e = cudaMallocHost(&H->cg_host, sizeof(CgScalars))) != cudaSuccess)
-    return cuda_fail(nullptr, e, "alloc");
-  if ((e = cudaMalloc(&H->flag, sizeof(int) * 4)) != cudaSuccess) return cuda_fail(nullptr, e, "alloc");
-  cudaMemset(H->cg, 0, sizeof(CgScalars));
-  cudaEventCreate(&H->ev0);
-  cudaEventCreate(&H->ev1);
-  cudaEventCreate(&H->evt0);
-  cudaEventCreate(&H->evt1);
+  std::string err;
+  if (handle_open(*H, *device, nullptr, err)) return fail(nullptr, NEKGPU_ECUDA, err);
   std::lock_guard<std::mutex> lk(g_mu);
   *handle = g_next++;
   g_handles[*handle] = std::move(H);
@@ -224,22 +349,7 @@ int nekgpu_init(const int* device, int64_t* handle) {
 int nekgpu_finalize(int64_t* handle) {
   Handle* H = get(handle);
   if (!H) return fail(nullptr, NEKGPU_EHANDLE, "unknown handle");
-  cudaSetDevice(H->device);
-  cudaStreamSynchronize(H->stream);
-  gs_free(H->mesh.gs);
-  H->mesh.f64.release();
-  H->mesh.f32.release();
-  cudaFree(H->mesh.dev_err);
-  for (cudaEvent_t e : H->ax_ev) cudaEventDestroy(e);
-  if (H->gexec) cudaGraphExecDestroy(H->gexec);
-  cudaFree(H->cg);
-  cudaFreeHost(H->cg_host);
-  cudaFree(H->flag);
-  cudaEventDestroy(H->ev0);
-  cudaEventDestroy(H->ev1);
-  cudaEventDestroy(H->evt0);
-  cudaEventDestroy(H->evt1);
-  cudaStreamDestroy(H->stream);
+  handle_close(*H);
   std::lock_guard<std::mutex> lk(g_mu);
   g_handles.erase(*handle);
   *handle = 0;
@@ -280,58 +390,10 @@ int nekgpu_setup(const int64_t* handle, const int* lx1, const int* nel, const do
   GET_HANDLE(handle);
   if (!lx1 || !nel || !dxm1 || !g1 || !g2 || !g3 || !g4 || !g5 || !g6 || !bm1 || !glo_num)
     return fail(H, NEKGPU_EINVAL, "null argument");
-  if (*lx1 < 2 || *lx1 > NEKGPU_MAX_LX1)
-    return fail(H, NEKGPU_EINVAL, "lx1 out of range [2, " + std::to_string(NEKGPU_MAX_LX1) + "]");
-  if (*nel < 1) return fail(H, NEKGPU_EINVAL, "nel must be positive");
-  cudaStreamSynchronize(H->stream);
-  Mesh& m = H->mesh;
-  gs_free(m.gs);
-  m.f64.release();
-  m.f32.release();
-  m.has_f32 = false;
-  H->has_mesh = false;
-  m.nx1 = *lx1;
-  m.nel = *nel;
-  const int P = m.nx1 * m.nx1 * m.nx1;
-  m.n = (int64_t)P * m.nel;
-  const int64_t n = m.n;
-  cudaError_t e;
-  if ((e = cudaMalloc(&m.f64.G, 6 * n * sizeof(double))) != cudaSuccess ||
-      (e = cudaMalloc(&m.f64.bm1, n * sizeof(double))) != cudaSuccess ||
-      (e = cudaMalloc(&m.f64.D, m.nx1 * m.nx1 * sizeof(double))) != cudaSuccess) {
-    m.f64.release();
-    return fail(H, NEKGPU_ENOMEM, "mesh allocation failed");
-  }
-  // D row-major from the Fortran-ordered dxm1(i,j) = dxm1[i + j*lx1]
-  m.h_D.assign((size_t)m.nx1 * m.nx1, 0.0);
-  for (int i = 0; i < m.nx1; ++i)
-    for (int j = 0; j < m.nx1; ++j) m.h_D[i * m.nx1 + j] = dxm1[i + j * m.nx1];
-  cudaMemcpy(m.f64.D, m.h_D.data(), m.h_D.size() * sizeof(double), cudaMemcpyHostToDevice);
-  const double* gs6[6] = {g1, g2, g3, g4, g5, g6};
-  DevBuf<double> stage;
-  if (stage.ensure(n)) return fail(H, NEKGPU_ENOMEM, "staging allocation failed");
-  for (int q = 0; q < 6; ++q) {
-    if ((e = cudaMemcpy(stage.ptr, gs6[q], n * sizeof(double), cudaMemcpyHostToDevice)) !=
-        cudaSuccess)
-      return cuda_fail(H, e, "geometry upload");
-    count_launch();
-    pack_g_kernel<<<nblk(n), 256, 0, 0>>>(m.f64.G, stage.ptr, q, P, n);
-    if ((e = cudaDeviceSynchronize()) != cudaSuccess) return cuda_fail(H, e, "geometry pack");
-  }
-  if ((e = cudaMemcpy(m.f64.bm1, bm1, n * sizeof(double), cudaMemcpyHostToDevice)) != cudaSuccess)
-    return cuda_fail(H, e, "mass upload");
-  // volvm1 = glsum(bm1): serial left-to-right, as one rank of the reference
-  double vol = 0.0;
-  for (int64_t i = 0; i < n; ++i) vol = vol + bm1[i];
-  m.vol = vol;
-  if (!m.dev_err && cudaMalloc(&m.dev_err, sizeof(int)) != cudaSuccess)
-    return fail(H, NEKGPU_ENOMEM, "flag allocation failed");
-  cudaMemset(m.dev_err, 0, sizeof(int));
+  const double* g[6] = {g1, g2, g3, g4, g5, g6};
   std::string err;
-  int rc = gs_setup(m.gs, glo_num, n, m.nx1, err);
-  if (rc) return fail(H, rc == -4 ? NEKGPU_ENOMEM : NEKGPU_EINVAL, err);
-  if (cuda_pending(*H, "setup")) return NEKGPU_ECUDA;
-  H->has_mesh = true;
+  const int rc = handle_setup(*H, *lx1, *nel, dxm1, g, bm1, glo_num, err);
+  if (rc) return fail(H, rc, err);
   return NEKGPU_OK;
 }
 

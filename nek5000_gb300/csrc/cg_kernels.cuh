@@ -1,0 +1,141 @@
+// cg_kernels.cuh -- the PCG update kernel (kernel C of an iteration) as a
+// block body, shared by the single-problem and batched solvers.
+//
+//   x += alpha p ; r -= alpha w ; z = r d            (hmholtz.f:804-805, :730)
+//   s1 = sum z r mult ; s2 = sum mult binv r r       (vlsc3 :754, vlsc32 :758)
+//   last block: rtz1, rbn2 = sqrt(s2/vol), convergence (:778), beta (:794)
+#pragma once
+#include "common.cuh"
+
+namespace nekgpu {
+
+template <typename T, bool EXACT, bool FIRST>
+struct UpdatePoint {
+  // x += alpha p ; r -= alpha w ; z = r d ; s1 += z r mult ; s2 += mult binv r r
+  __device__ __forceinline__ static void run(T& x, T& r, T p, T w, T d, T m, T b, T alpha,
+                                             CompAcc<T>& a1, CompAcc<T>& a2) {
+    if (!FIRST) {
+      x = madd<EXACT>(alpha, p, x);   // add2s2(x,p,alpha)   (hmholtz.f:804)
+      r = madd<EXACT>(-alpha, w, r);  // add2s2(r,w,-alpha)  (hmholtz.f:805)
+    }
+    if (EXACT) {
+      const T z = mul_x(r, d);                         // col3 (:730)
+      a1.add(mul_x(mul_x(z, r), m));                   // vlsc3 (:754)
+      a2.add(mul_x(mul_x(mul_x(m, b), r), r));         // vlsc32 (:758, :848)
+    } else {
+      const T z = r * d;
+      a1.add(z * r * m);
+      a2.add(m * b * r * r);
+    }
+  }
+};
+
+// Block body of the update kernel: block `blk` of `nblk` (1-D blocks).
+// VEC: 16-byte vector accesses (all seven arrays 16-byte aligned).
+template <typename T, bool EXACT, bool FIRST, bool VEC>
+__device__ __forceinline__ void cg_update_body(T* __restrict__ x, T* __restrict__ r,
+                                               const T* __restrict__ p, const T* __restrict__ w,
+                                               const T* __restrict__ d,
+                                               const T* __restrict__ mult,
+                                               const T* __restrict__ binv, int64_t n,
+                                               CgScalars* cg, double* __restrict__ partial,
+                                               int blk, int nblk, double* red, int* am_last_s) {
+  int& am_last = *am_last_s;
+  const T alpha = FIRST ? T(0) : (T)cg->alpha;
+  CompAcc<T> a1, a2;
+  using P = UpdatePoint<T, EXACT, FIRST>;
+  const int64_t gtid = blk * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t stride = (int64_t)nblk * blockDim.x;
+  constexpr int W = 16 / sizeof(T);
+  const int64_t nv = VEC ? n / W : 0;
+  int64_t iv = gtid;
+  for (; iv < nv; iv += stride) {
+    T xx[W], rr[W], pp[W], ww[W], dd[W], mm[W], bb[W];
+    ld16(rr, r, iv);
+    ld16(dd, d, iv);
+    ld16(mm, mult, iv);
+    ld16(bb, binv, iv);
+    if (!FIRST) {
+      ld16(xx, x, iv);
+      ld16(pp, p, iv);
+      ld16(ww, w, iv);
+    }
+#pragma unroll
+    for (int q = 0; q < W; ++q) P::run(xx[q], rr[q], pp[q], ww[q], dd[q], mm[q], bb[q], alpha, a1, a2);
+    if (!FIRST) {
+      st16(x, xx, iv);
+      st16(r, rr, iv);
+    }
+  }
+  for (int64_t i = nv * W + gtid; i < n; i += stride) {
+    T xi = FIRST ? T(0) : x[i], ri = r[i];
+    P::run(xi, ri, FIRST ? T(0) : p[i], FIRST ? T(0) : w[i], d[i], mult[i], binv[i], alpha, a1, a2);
+    if (!FIRST) {
+      x[i] = xi;
+      r[i] = ri;
+    }
+  }
+  const double b1 = block_sum_comp(a1, red);
+  const double b2 = block_sum_comp(a2, red);
+  if (threadIdx.x == 0) {
+    partial[blk] = b1;
+    partial[nblk + blk] = b2;
+    __threadfence();
+    const unsigned int ticket = atomicAdd(&cg->counter[1], 1u);
+    am_last = (ticket == (unsigned int)nblk - 1);
+  }
+  __syncthreads();
+  if (!am_last) return;
+  double t1 = 0.0, t2 = 0.0;
+#pragma unroll 4
+  for (int q = threadIdx.x; q < nblk; q += blockDim.x) {
+    t1 += __ldcg(partial + q);
+    t2 += __ldcg(partial + nblk + q);
+  }
+  const double s1 = block_sum(t1, red);
+  const double s2 = block_sum(t2, red);
+  if (threadIdx.x == 0) {
+    cg->counter[1] = 0u;
+    const int iter = cg->iter + 1;
+    cg->iter = iter;
+    if (iter > cg->maxiter) {
+      // the reference's loop has ended (do iter=1,niter): no further check,
+      // rbn2 stays the norm of the last checked iterate
+      cg->niter = cg->maxiter;
+      cg->done = 1;
+      return;
+    }
+    cg->s1 = s1;
+    cg->s2 = s2;
+    cg->rtz2 = cg->rtz1;
+    cg->rtz1 = s1;
+    const double rbn2 = sqrt(s2 / cg->vol);
+    cg->rbn2 = rbn2;
+    if (iter == 1) cg->rbn0 = rbn2;
+    if (cg->tin < 0) cg->tol = fabs(cg->tin) * cg->rbn0;
+    if (!isfinite(rbn2) || !isfinite(s1)) {
+      cg->nonfinite = 1;
+      cg->niter = iter - 1;
+      cg->done = 1;
+    } else if (rbn2 <= cg->tol && (iter > 1 || cg->istep <= 5)) {
+      cg->niter = iter - 1;
+      cg->done = 1;
+    }
+    cg->beta = (iter == 1) ? 0.0 : s1 / cg->rtz2;
+  }
+}
+
+template <typename T, bool EXACT, bool FIRST, bool VEC>
+__global__ void __launch_bounds__(256)
+    cg_update_kernel(T* __restrict__ x, T* __restrict__ r, const T* __restrict__ p,
+                     const T* __restrict__ w, const T* __restrict__ d,
+                     const T* __restrict__ mult, const T* __restrict__ binv, int64_t n,
+                     CgScalars* cg, double* __restrict__ partial) {
+  __shared__ double red[32];
+  __shared__ int am_last;
+  if (cg->done) return;
+  cg_update_body<T, EXACT, FIRST, VEC>(x, r, p, w, d, mult, binv, n, cg, partial, blockIdx.x,
+                                       gridDim.x, red, &am_last);
+}
+
+}  // namespace nekgpu

@@ -2,7 +2,7 @@
 #include <algorithm>
 #include <numeric>
 
-#include "gs.cuh"
+#include "gs_kernels.cuh"
 
 namespace nekgpu {
 
@@ -23,130 +23,6 @@ __global__ void gs_op_kernel(T* __restrict__ u, const int* __restrict__ start,
     else t = (v < t) ? v : t;
   }
   for (int c = a; c < b; ++c) u[idx[c]] = t;
-}
-
-// Groups of C copies (C in 1, 2, 4, 8): each thread takes G groups of its
-// class (block-strided, so index loads stay coalesced), loads every group's
-// indices with one vector access, issues all gathers before any use, sums each
-// group in ascending local-index order, scatters, and accumulates rho.
-template <int C>
-__device__ __forceinline__ void load_ids(const int* __restrict__ cidx, int s, int (&id)[C]) {
-  if constexpr (C == 1) {
-    id[0] = cidx[s];
-  } else if constexpr (C == 2) {
-    const int2 v = reinterpret_cast<const int2*>(cidx)[s];
-    id[0] = v.x;
-    id[1] = v.y;
-  } else {
-#pragma unroll
-    for (int h = 0; h < C / 4; ++h) {
-      const int4 v = reinterpret_cast<const int4*>(cidx)[(C / 4) * s + h];
-      id[4 * h] = v.x;
-      id[4 * h + 1] = v.y;
-      id[4 * h + 2] = v.z;
-      id[4 * h + 3] = v.w;
-    }
-  }
-}
-
-template <typename T, int C, int G>
-__device__ __forceinline__ void gs_groups(const int* __restrict__ cidx, int s0, int step, int cnt,
-                                          int goff, T* __restrict__ w, const T* __restrict__ p,
-                                          const T* __restrict__ segmask,
-                                          const T* __restrict__ segmsum, CompAcc<T>& acc) {
-  int id[G][C];
-  bool on[G];
-#pragma unroll
-  for (int q = 0; q < G; ++q) {
-    const int s = s0 + q * step;
-    on[q] = s < cnt;
-    if (on[q]) load_ids<C>(cidx, s, id[q]);
-  }
-  T v[G][C], p0[G], mk[G], ms[G];
-#pragma unroll
-  for (int q = 0; q < G; ++q) {
-    if (!on[q]) continue;
-    const int s = s0 + q * step;
-#pragma unroll
-    for (int c = 0; c < C; ++c) v[q][c] = w[id[q][c]];
-    p0[q] = p[id[q][0]];
-    mk[q] = segmask[goff + s];
-    ms[q] = segmsum[goff + s];
-  }
-#pragma unroll
-  for (int q = 0; q < G; ++q) {
-    if (!on[q]) continue;
-    T t = v[q][0];
-#pragma unroll
-    for (int c = 1; c < C; ++c) t = t + v[q][c];
-    t = t * mk[q];
-#pragma unroll
-    for (int c = 0; c < C; ++c) w[id[q][c]] = t;
-    acc.add(t * p0[q] * ms[q]);
-  }
-}
-
-// Blocks of each size class are contiguous in the grid (a block runs one
-// class, kGsGroups groups per thread).  Warp 0 also folds a strided slice of
-// the operator's interior partials into the block's partial.
-template <typename T>
-__global__ void __launch_bounds__(kGsThreads)
-    gs_cg_kernel(T* __restrict__ w, const T* __restrict__ p, const int* __restrict__ start,
-                 const int* __restrict__ idx, const GsClasses cls,
-                 const T* __restrict__ segmask, const T* __restrict__ segmsum, CgScalars* cg,
-                 const double* __restrict__ partialA, int nA, double* __restrict__ partialB) {
-  __shared__ double red[32];
-  __shared__ int am_last;
-  if (cg->done) return;
-  int k = 0;
-  while (k < kGsClasses - 1 && (int)blockIdx.x >= cls.boff[k + 1]) ++k;
-  const int G = gs_groups_per_thread(k);
-  const int s0 = ((int)blockIdx.x - cls.boff[k]) * blockDim.x * G + threadIdx.x;
-  const int* ci = idx + cls.ioff[k];
-  const int goff = cls.soff[k], cnt = cls.cnt[k];
-  CompAcc<T> acc;
-  switch (k) {
-    case 0: gs_groups<T, 1, 4>(ci, s0, blockDim.x, cnt, goff, w, p, segmask, segmsum, acc); break;
-    case 1: gs_groups<T, 2, 4>(ci, s0, blockDim.x, cnt, goff, w, p, segmask, segmsum, acc); break;
-    case 2: gs_groups<T, 4, 2>(ci, s0, blockDim.x, cnt, goff, w, p, segmask, segmsum, acc); break;
-    case 3: gs_groups<T, 8, 1>(ci, s0, blockDim.x, cnt, goff, w, p, segmask, segmsum, acc); break;
-    default:
-      for (int q = 0; q < G; ++q) {
-        const int sl = s0 + q * blockDim.x;
-        if (sl >= cnt) break;
-        const int g = goff + sl;
-        const int a = start[g], b = start[g + 1];
-        T t = w[idx[a]];
-        for (int c = a + 1; c < b; ++c) t = t + w[idx[c]];
-        t = t * segmask[g];
-        for (int c = a; c < b; ++c) w[idx[c]] = t;
-        acc.add(t * p[idx[a]] * segmsum[g]);
-      }
-  }
-  double dot = block_sum_comp(acc, red);  // thread 0
-  if (threadIdx.x < 32) {
-    double pa = 0.0;
-    for (int q = blockIdx.x + gridDim.x * threadIdx.x; q < nA; q += gridDim.x * 32)
-      pa += __ldcg(partialA + q);
-    pa = warp_sum(pa);
-    if (threadIdx.x == 0) {
-      partialB[blockIdx.x] = dot + pa;
-      __threadfence();
-      const unsigned int ticket = atomicAdd(&cg->counter[0], 1u);
-      am_last = (ticket == gridDim.x - 1);
-    }
-  }
-  __syncthreads();
-  if (!am_last) return;
-  double pb = 0.0;
-#pragma unroll 8
-  for (int q = threadIdx.x; q < (int)gridDim.x; q += blockDim.x) pb += __ldcg(partialB + q);
-  const double rho = block_sum(pb, red);
-  if (threadIdx.x == 0) {
-    cg->rho = rho;
-    cg->alpha = cg->rtz1 / rho;
-    cg->counter[0] = 0u;
-  }
 }
 
 template <typename T>

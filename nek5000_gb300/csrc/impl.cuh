@@ -113,6 +113,7 @@ struct Handle {
   cudaGraphExec_t gexec = nullptr;
   int gchunk = 0;  // iterations captured in gexec
   int graph_chunk = 16;
+  bool own_stream = true;
   bool use_graph = true;
 };
 
@@ -152,6 +153,21 @@ PcgResult pcg_solve(Handle& h, const OpData<T>& op, PcgWork<T>& wk, T* x, const 
                     int maxiter, int istep, bool exact, const T* dpre = nullptr);
 template <typename T>
 double device_absmax(Handle& h, const T* a, int64_t n, int* status);
+template <typename T>
+PcgResult pcg_prepare(Handle& h, PcgWork<T>& wk, T* x, const T* f, const Coef<T>& c,
+                      const T* mask, const T* mult, double tin, int maxiter, int istep,
+                      const T* dpre, bool* trivial);
+int pcg_vec_blocks(int64_t n);
+
+// Mixed-precision helpers (mixed.cu), used by the batched solver too.
+int ensure_f32(Handle& h);
+void cast_to_f32(Handle& h, float* o, const double* a, double scale, int64_t n);
+void axpy_f32(Handle& h, double* x, const float* e, double scale, int64_t n);
+// r = f - mask * dssum(A x) (FP64); returns cggo's norm of r, or -1 on error.
+double outer_residual(Handle& h, double* r, const double* f, const double* x,
+                      const Coef<double>& c, const double* mask, const double* mult,
+                      const double* binv, double* w);
+double norm64(Handle& h, const double* r, const double* mult, const double* binv);
 
 // Mixed precision (mixed.cu): FP32 inner PCG in an FP64 defect-correction loop.
 struct MixedResult {
@@ -164,6 +180,13 @@ MixedResult mixed_solve(Handle& h, double* x, const double* f, const double* h1,
                         const double* binv, double tin, int maxit, double inner_tol);
 
 void set_error(Handle& h, const std::string& msg);
+
+// Handle life cycle and mesh upload (capi.cu); `shared` != nullptr makes the
+// handle use that stream instead of creating one.
+int handle_open(Handle& h, int device, cudaStream_t shared, std::string& err);
+void handle_close(Handle& h);
+int handle_setup(Handle& h, int lx1, int nel, const double* dxm1, const double* const* g6,
+                 const double* bm1, const int64_t* glo_num, std::string& err);
 
 // Returns true (and records `where`) when a CUDA error is pending.
 inline bool cuda_pending(Handle& h, const char* where) {

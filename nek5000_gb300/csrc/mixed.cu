@@ -89,6 +89,8 @@ double host_sum(Handle& h, int nb, int* st) {
   return s;
 }
 
+}  // namespace
+
 int ensure_f32(Handle& h) {
   Mesh& m = h.mesh;
   if (m.has_f32) return 0;
@@ -113,7 +115,47 @@ int ensure_f32(Handle& h) {
   return 0;
 }
 
-}  // namespace
+
+void cast_to_f32(Handle& h, float* o, const double* a, double scale, int64_t n) {
+  count_launch();
+  cast_scale_kernel<float, double><<<blocks(n), kThreads, 0, h.stream>>>(o, a, scale, n);
+}
+
+void axpy_f32(Handle& h, double* x, const float* e, double scale, int64_t n) {
+  count_launch();
+  axpy_kernel<<<blocks(n), kThreads, 0, h.stream>>>(x, e, scale, n);
+}
+
+double norm64(Handle& h, const double* r, const double* mult, const double* binv) {
+  const int64_t n = h.mesh.n;
+  const int nb = blocks(n);
+  if (h.red.ensure(nb)) return -1.0;
+  count_launch();
+  norm_kernel<<<nb, kThreads, 0, h.stream>>>(r, mult, binv, n, h.red.ptr);
+  int st = 0;
+  const double s2 = host_sum(h, nb, &st);
+  return st ? -1.0 : std::sqrt(s2 / h.mesh.vol);
+}
+
+double outer_residual(Handle& h, double* r, const double* f, const double* x,
+                      const Coef<double>& c, const double* mask, const double* mult,
+                      const double* binv, double* w) {
+  Mesh& m = h.mesh;
+  const int64_t n = m.n;
+  const int nb = blocks(n);
+  if (h.red.ensure(nb)) return -1.0;
+  cudaError_t e = launch_axhelm<double, false>(m, m.f64, w, x, c, h.stream);
+  if (e != cudaSuccess) {
+    set_error(h, std::string("outer residual: axhelm ") + cudaGetErrorString(e));
+    return -1.0;
+  }
+  gs_op<double>(m.gs, w, 0, h.stream);
+  count_launch();
+  residual_kernel<<<nb, kThreads, 0, h.stream>>>(r, f, w, mask, mult, binv, n, h.red.ptr);
+  int st = 0;
+  const double s2 = host_sum(h, nb, &st);
+  return st ? -1.0 : std::sqrt(s2 / m.vol);
+}
 
 MixedResult mixed_solve(Handle& h, double* x, const double* f, const double* h1,
                         const double* h2, const double* mask, const double* mult,

@@ -13,6 +13,7 @@
 #include <algorithm>
 #include <cmath>
 
+#include "cg_kernels.cuh"
 #include "impl.cuh"
 
 namespace nekgpu {
@@ -166,121 +167,6 @@ __global__ void sum_kernel(int kind, const double* __restrict__ a, const double*
 }
 
 // ---- PCG update / convergence kernel ---------------------------------------
-template <typename T, bool EXACT, bool FIRST>
-struct UpdatePoint {
-  // x += alpha p ; r -= alpha w ; z = r d ; s1 += z r mult ; s2 += mult binv r r
-  __device__ __forceinline__ static void run(T& x, T& r, T p, T w, T d, T m, T b, T alpha,
-                                             CompAcc<T>& a1, CompAcc<T>& a2) {
-    if (!FIRST) {
-      x = madd<EXACT>(alpha, p, x);   // add2s2(x,p,alpha)   (hmholtz.f:804)
-      r = madd<EXACT>(-alpha, w, r);  // add2s2(r,w,-alpha)  (hmholtz.f:805)
-    }
-    if (EXACT) {
-      const T z = mul_x(r, d);                         // col3 (:730)
-      a1.add(mul_x(mul_x(z, r), m));                   // vlsc3 (:754)
-      a2.add(mul_x(mul_x(mul_x(m, b), r), r));         // vlsc32 (:758, :848)
-    } else {
-      const T z = r * d;
-      a1.add(z * r * m);
-      a2.add(m * b * r * r);
-    }
-  }
-};
-
-// VEC: 16-byte vector accesses (all seven arrays 16-byte aligned).
-template <typename T, bool EXACT, bool FIRST, bool VEC>
-__global__ void __launch_bounds__(kVecThreads)
-    cg_update_kernel(T* __restrict__ x, T* __restrict__ r, const T* __restrict__ p,
-                     const T* __restrict__ w, const T* __restrict__ d,
-                     const T* __restrict__ mult, const T* __restrict__ binv, int64_t n,
-                     CgScalars* cg, double* __restrict__ partial) {
-  __shared__ double red[32];
-  __shared__ int am_last;
-  if (cg->done) return;
-  const T alpha = FIRST ? T(0) : (T)cg->alpha;
-  CompAcc<T> a1, a2;
-  using P = UpdatePoint<T, EXACT, FIRST>;
-  const int64_t gtid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  constexpr int W = 16 / sizeof(T);
-  const int64_t nv = VEC ? n / W : 0;
-  int64_t iv = gtid;
-  for (; iv < nv; iv += stride) {
-    T xx[W], rr[W], pp[W], ww[W], dd[W], mm[W], bb[W];
-    ld16(rr, r, iv);
-    ld16(dd, d, iv);
-    ld16(mm, mult, iv);
-    ld16(bb, binv, iv);
-    if (!FIRST) {
-      ld16(xx, x, iv);
-      ld16(pp, p, iv);
-      ld16(ww, w, iv);
-    }
-#pragma unroll
-    for (int q = 0; q < W; ++q) P::run(xx[q], rr[q], pp[q], ww[q], dd[q], mm[q], bb[q], alpha, a1, a2);
-    if (!FIRST) {
-      st16(x, xx, iv);
-      st16(r, rr, iv);
-    }
-  }
-  for (int64_t i = nv * W + gtid; i < n; i += stride) {
-    T xi = FIRST ? T(0) : x[i], ri = r[i];
-    P::run(xi, ri, FIRST ? T(0) : p[i], FIRST ? T(0) : w[i], d[i], mult[i], binv[i], alpha, a1, a2);
-    if (!FIRST) {
-      x[i] = xi;
-      r[i] = ri;
-    }
-  }
-  const double b1 = block_sum_comp(a1, red);
-  const double b2 = block_sum_comp(a2, red);
-  if (threadIdx.x == 0) {
-    partial[blockIdx.x] = b1;
-    partial[gridDim.x + blockIdx.x] = b2;
-    __threadfence();
-    const unsigned int ticket = atomicAdd(&cg->counter[1], 1u);
-    am_last = (ticket == gridDim.x - 1);
-  }
-  __syncthreads();
-  if (!am_last) return;
-  double t1 = 0.0, t2 = 0.0;
-#pragma unroll 4
-  for (int q = threadIdx.x; q < (int)gridDim.x; q += blockDim.x) {
-    t1 += __ldcg(partial + q);
-    t2 += __ldcg(partial + gridDim.x + q);
-  }
-  const double s1 = block_sum(t1, red);
-  const double s2 = block_sum(t2, red);
-  if (threadIdx.x == 0) {
-    cg->counter[1] = 0u;
-    const int iter = cg->iter + 1;
-    cg->iter = iter;
-    if (iter > cg->maxiter) {
-      // the reference's loop has ended (do iter=1,niter): no further check,
-      // rbn2 stays the norm of the last checked iterate
-      cg->niter = cg->maxiter;
-      cg->done = 1;
-      return;
-    }
-    cg->s1 = s1;
-    cg->s2 = s2;
-    cg->rtz2 = cg->rtz1;
-    cg->rtz1 = s1;
-    const double rbn2 = sqrt(s2 / cg->vol);
-    cg->rbn2 = rbn2;
-    if (iter == 1) cg->rbn0 = rbn2;
-    if (cg->tin < 0) cg->tol = fabs(cg->tin) * cg->rbn0;
-    if (!isfinite(rbn2) || !isfinite(s1)) {
-      cg->nonfinite = 1;
-      cg->niter = iter - 1;
-      cg->done = 1;
-    } else if (rbn2 <= cg->tol && (iter > 1 || cg->istep <= 5)) {
-      cg->niter = iter - 1;
-      cg->done = 1;
-    }
-    cg->beta = (iter == 1) ? 0.0 : s1 / cg->rtz2;
-  }
-}
-
 // Element-interior points handled by the fused operator must carry mask 1 and
 // multiplicity 1 (the reference's masks live on faces; interiors are unshared).
 template <typename T>
@@ -306,6 +192,8 @@ __global__ void zero_kernel(T* __restrict__ a, int64_t n) {
 }  // namespace
 
 // ---- host helpers ------------------------------------------------------------
+int pcg_vec_blocks(int64_t n) { return vec_blocks(n); }
+
 template <typename T>
 int detect_coef(Handle& h, const T* h1, const T* h2, int64_t n, Coef<T>& c) {
   const int nb = vec_blocks(n);
@@ -485,11 +373,17 @@ double device_absmax(Handle& h, const T* a, int64_t n, int* status) {
 template double device_absmax<double>(Handle&, const double*, int64_t, int*);
 template double device_absmax<float>(Handle&, const float*, int64_t, int*);
 
+// Everything of one solve before its first iteration (hmholtz.f:683-701 and
+// the iteration-1 state): buffers, max|f| (an all-zero rhs returns x = 0,
+// res.niter = 0 and *trivial = true), Jacobi diagonal, boundary-group
+// weights and checks, r = f, p = 0, scalars.  The iteration-1 check kernel
+// is not launched.
 template <typename T>
-PcgResult pcg_solve(Handle& h, const OpData<T>& op, PcgWork<T>& wk, T* x, const T* f,
-                    const Coef<T>& c, const T* mask, const T* mult, const T* binv, double tin,
-                    int maxiter, int istep, bool exact, const T* dpre) {
+PcgResult pcg_prepare(Handle& h, PcgWork<T>& wk, T* x, const T* f, const Coef<T>& c,
+                      const T* mask, const T* mult, double tin, int maxiter, int istep,
+                      const T* dpre, bool* trivial) {
   PcgResult res;
+  *trivial = false;
   Mesh& m = h.mesh;
   const int64_t n = m.n;
   cudaStream_t s = h.stream;
@@ -525,7 +419,10 @@ PcgResult pcg_solve(Handle& h, const OpData<T>& op, PcgWork<T>& wk, T* x, const 
     res.status = -3;
     return res;
   }
-  if (fmax == 0.0) return res;
+  if (fmax == 0.0) {
+    *trivial = true;
+    return res;
+  }
 
   // Jacobi diagonal: given by the caller (FP32 inner solves get the FP64
   // diagonal cast once), or setprec in FP64 here.
@@ -582,6 +479,24 @@ PcgResult pcg_solve(Handle& h, const OpData<T>& op, PcgWork<T>& wk, T* x, const 
     set_error(h, "pcg: an element-interior point has mask or multiplicity other than 1");
     return res;
   }
+  return res;
+}
+template PcgResult pcg_prepare<double>(Handle&, PcgWork<double>&, double*, const double*,
+                                       const Coef<double>&, const double*, const double*, double,
+                                       int, int, const double*, bool*);
+template PcgResult pcg_prepare<float>(Handle&, PcgWork<float>&, float*, const float*,
+                                      const Coef<float>&, const float*, const float*, double, int,
+                                      int, const float*, bool*);
+
+template <typename T>
+PcgResult pcg_solve(Handle& h, const OpData<T>& op, PcgWork<T>& wk, T* x, const T* f,
+                    const Coef<T>& c, const T* mask, const T* mult, const T* binv, double tin,
+                    int maxiter, int istep, bool exact, const T* dpre) {
+  Mesh& m = h.mesh;
+  cudaStream_t s = h.stream;
+  bool trivial = false;
+  PcgResult res = pcg_prepare<T>(h, wk, x, f, c, mask, mult, tin, maxiter, istep, dpre, &trivial);
+  if (res.status || trivial) return res;
   // iteration 1 check (z, s1, s2) -- no update
   launch_C<T>(h, wk, x, mult, binv, exact, true);
   // main loop: chunks of iterations, one host check per chunk.  With kernel

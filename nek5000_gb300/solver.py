@@ -191,3 +191,75 @@ class NekGpu:
         del name
         return self._solve_mixed(self._L.nekgpu_hmholtz_mixed, u, rhs, h1, h2, mask, mult, imsh,
                                  tli, maxit, isd, binv, inner_tol)
+
+
+class NekGpuBatch:
+    """Many independent problems solved together (nekgpu_batch_*).
+
+    add() takes one problem's mesh like NekGpu.setup(); solve() takes lists of
+    torch float64 CUDA tensors, one per problem in the order added."""
+
+    def __init__(self, device: int = 0):
+        self._L = _capi.load()
+        self._b = C.c_int64(0)
+        rc = self._L.nekgpu_batch_create(C.byref(_cint(device)), C.byref(self._b))
+        if rc:
+            raise _capi.NekGpuError(rc, self.last_error())
+        self.sizes = []
+        self._keep = []
+
+    def last_error(self) -> str:
+        buf = C.create_string_buffer(1024)
+        self._L.nekgpu_batch_last_error(C.byref(self._b), buf, C.byref(_cint(1024)))
+        return buf.value.decode(errors="replace")
+
+    def add(self, lx1, nel, D, g, bm1, glo_num) -> int:
+        n = lx1 ** 3 * nel
+        dxm1 = np.ascontiguousarray(np.asarray(D, dtype=np.float64).T)
+        g = np.ascontiguousarray(np.asarray(g, dtype=np.float64).reshape(6, n))
+        bm1 = np.ascontiguousarray(bm1, dtype=np.float64)
+        glo = np.ascontiguousarray(glo_num, dtype=np.int64)
+        idx = _cint(0)
+        gp = [g[q].ctypes.data_as(C.c_void_p) for q in range(6)]
+        rc = self._L.nekgpu_batch_add(C.byref(self._b), C.byref(_cint(lx1)), C.byref(_cint(nel)),
+                                      dxm1.ctypes.data_as(C.c_void_p), *gp,
+                                      bm1.ctypes.data_as(C.c_void_p),
+                                      glo.ctypes.data_as(C.c_void_p), C.byref(idx))
+        if rc:
+            raise _capi.NekGpuError(rc, self.last_error())
+        self.sizes.append(n)
+        return idx.value
+
+    def solve(self, x, f, h1, h2, mask, mult, binv, tin=-1e-10, maxit=10 ** 6, mixed=False,
+              inner_tol=1e-5):
+        """Returns a dict of per-problem lists: niter, nouter, rbn0, rbn2, status."""
+        np_ = len(self.sizes)
+        arr = lambda ts: (C.c_void_p * np_)(*[t.data_ptr() for t in ts])
+        for ts in (x, f, h1, h2, mask, mult, binv):
+            if len(ts) != np_:
+                raise ValueError("one array per problem is required")
+            for t in ts:
+                _ptr(t)  # type / device checks
+        niter = (C.c_int * np_)()
+        nouter = (C.c_int * np_)()
+        r0 = (C.c_double * np_)()
+        r2 = (C.c_double * np_)()
+        st = (C.c_int * np_)()
+        rc = self._L.nekgpu_batch_solve_dev(
+            C.byref(self._b), C.byref(_cint(np_)), arr(x), arr(f), arr(h1), arr(h2), arr(mask),
+            arr(mult), arr(binv), C.byref(_cdouble(tin)), C.byref(_cint(int(maxit))),
+            C.byref(_cint(int(mixed))), C.byref(_cdouble(inner_tol)), niter, nouter, r0, r2, st)
+        if rc:
+            raise _capi.NekGpuError(rc, self.last_error())
+        return dict(niter=list(niter), nouter=list(nouter), rbn0=list(r0), rbn2=list(r2),
+                    status=list(st))
+
+    def close(self):
+        if getattr(self, "_b", None) is not None and self._b.value:
+            self._L.nekgpu_batch_destroy(C.byref(self._b))
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,96 @@
+"""Batched solves: problems of uneven order and size advanced together.
+
+Each problem of the batch must stop at its own iteration count and return
+exactly what a solve of that problem alone returns (the batched launches run
+the same per-problem arithmetic), and agree with the oracle like a single
+solve does.  The mixed form must meet the FP64 tolerance per problem."""
+import numpy as np
+import pytest
+
+from conftest import rng_unit_vector
+
+pytestmark = pytest.mark.gpu
+
+CASES = [  # (lx1, kx, ky, kz, periodic, h2)
+    (6, 2, 3, 2, (False, False, False), 0.0),
+    (8, 3, 2, 2, (False, True, True), 10.0),
+    (10, 2, 2, 2, (False, False, False), 1500.0),
+    (7, 2, 2, 3, (False, False, False), 0.0),
+    (9, 2, 2, 2, (False, False, False), 1.0),
+    (8, 2, 2, 2, (False, False, False), 0.0),  # zero right-hand side
+]
+
+
+@pytest.fixture(scope="module")
+def problems(oracle):
+    out = []
+    for q, (nx1, kx, ky, kz, per, h2) in enumerate(CASES):
+        P = oracle.box_problem(nx1, kx, ky, kz, periodic=per, v=rng_unit_vector(30 + q))
+        n = P["n"]
+        rng = np.random.default_rng(30 + q)
+        f = P["ops"].dssum(P["bm1"] * (P["ops"].dssum(rng.standard_normal(n)) * P["mult"]))
+        f = f * P["mask"]
+        if q == len(CASES) - 1:
+            f[:] = 0.0
+        P["f"] = f
+        P["h1v"] = np.ones(n)
+        P["h2v"] = np.full(n, h2)
+        out.append(P)
+    return out
+
+
+def _dev(torch, a):
+    return torch.tensor(a, device="cuda")
+
+
+def test_batch_fp64_equals_single_solves(gpu_lib, oracle, problems):
+    torch = pytest.importorskip("torch")
+    from nek5000_gb300 import NekGpuBatch
+    B = NekGpuBatch(0)
+    for P in problems:
+        B.add(P["nx1"], P["nel"], P["D"], P["g"], P["bm1"], P["glo_num"])
+    xs = [torch.zeros(P["n"], dtype=torch.float64, device="cuda") for P in problems]
+    col = lambda k: [_dev(torch, P[k]) for P in problems]
+    res = B.solve(xs, col("f"), col("h1v"), col("h2v"), col("mask"), col("mult"), col("binv"),
+                  tin=-1e-10)
+    assert res["status"] == [0] * len(problems)
+    for q, P in enumerate(problems):
+        lib = gpu_lib(0)
+        lib.setup(P["nx1"], P["nel"], P["D"], P["g"], P["bm1"], P["glo_num"])
+        x1 = torch.zeros(P["n"], dtype=torch.float64, device="cuda")
+        it, r0, r2, rc = lib.cggo(x1, _dev(torch, P["f"]), _dev(torch, P["h1v"]),
+                                  _dev(torch, P["h2v"]), _dev(torch, P["mask"]),
+                                  _dev(torch, P["mult"]), 1, -1e-10, 10 ** 6, 1,
+                                  _dev(torch, P["binv"]), maxcg=10 ** 6)
+        assert res["niter"][q] == it
+        assert torch.equal(xs[q], x1), q
+        if it:
+            x_ref, it_ref, _, _ = P["ops"].cggo(P["f"], P["h1v"], P["h2v"], P["mask"], P["mult"],
+                                               P["binv"], -1e-10, maxcg=10 ** 6)
+            assert abs(it - it_ref) <= 1
+            err = np.linalg.norm(x1.cpu().numpy() - x_ref) / np.linalg.norm(x_ref)
+            assert err < 2e-11, (q, err)
+    assert res["niter"][-1] == 0 and float(xs[-1].abs().max()) == 0.0
+    # uneven orders really stop at different counts
+    assert len(set(res["niter"][:-1])) > 1
+
+
+def test_batch_mixed_meets_fp64_tolerance(gpu_lib, oracle, problems):
+    torch = pytest.importorskip("torch")
+    from nek5000_gb300 import NekGpuBatch
+    B = NekGpuBatch(0)
+    for P in problems:
+        B.add(P["nx1"], P["nel"], P["D"], P["g"], P["bm1"], P["glo_num"])
+    xs = [torch.zeros(P["n"], dtype=torch.float64, device="cuda") for P in problems]
+    col = lambda k: [_dev(torch, P[k]) for P in problems]
+    res = B.solve(xs, col("f"), col("h1v"), col("h2v"), col("mask"), col("mult"), col("binv"),
+                  tin=-1e-10, mixed=True, inner_tol=1e-5)
+    assert res["status"] == [0] * len(problems)
+    for q, P in enumerate(problems[:-1]):
+        x = xs[q].cpu().numpy()
+        ops = P["ops"]
+        w = ops.dssum(ops.axhelm(x, P["h1v"], P["h2v"])) * P["mask"]
+        r = P["f"] - w
+        rn = np.sqrt(np.sum(P["mult"] * P["binv"] * r * r) / np.sum(P["bm1"]))
+        assert rn <= 1.05e-10 * res["rbn0"][q], (q, rn / res["rbn0"][q])
+        assert 2 <= res["nouter"][q] <= 8
