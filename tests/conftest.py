@@ -36,3 +36,14 @@ def gpu_lib():
     build.build()
     from nek5000_gb300 import NekGpu
     return NekGpu
+
+
+def rank_spread(oracle, P, solve):
+    """Largest relative change of the oracle's solution when its dot products
+    are summed as P = 2, 3, 4, 7, 8 ranks would; returns (1-rank solution, spread)."""
+    base = solve(P["ops"])
+    worst = 0.0
+    for nt in (2, 3, 4, 7, 8):
+        ops = oracle.Ops(P["nx1"], P["nel"], P["D"], P["g"], P["bm1"], P["glo_num"], nt)
+        worst = max(worst, np.linalg.norm(solve(ops) - base) / np.linalg.norm(base))
+    return base, worst

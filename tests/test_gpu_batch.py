@@ -7,7 +7,7 @@ solve does.  The mixed form must meet the FP64 tolerance per problem."""
 import numpy as np
 import pytest
 
-from conftest import rng_unit_vector
+from conftest import rank_spread, rng_unit_vector
 
 pytestmark = pytest.mark.gpu
 
@@ -68,8 +68,11 @@ def test_batch_fp64_equals_single_solves(gpu_lib, oracle, problems):
             x_ref, it_ref, _, _ = P["ops"].cggo(P["f"], P["h1v"], P["h2v"], P["mask"], P["mult"],
                                                P["binv"], -1e-10, maxcg=10 ** 6)
             assert abs(it - it_ref) <= 1
+            _, spread = rank_spread(oracle, P, lambda ops: ops.cggo(
+                P["f"], P["h1v"], P["h2v"], P["mask"], P["mult"], P["binv"], -1e-10,
+                maxcg=10 ** 6)[0])
             err = np.linalg.norm(x1.cpu().numpy() - x_ref) / np.linalg.norm(x_ref)
-            assert err < 2e-11, (q, err)
+            assert err <= max(1e-12, 2 * spread), (q, err, spread)
     assert res["niter"][-1] == 0 and float(xs[-1].abs().max()) == 0.0
     # uneven orders really stop at different counts
     assert len(set(res["niter"][:-1])) > 1

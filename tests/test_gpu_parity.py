@@ -16,7 +16,7 @@ Tolerances:
 import numpy as np
 import pytest
 
-from conftest import rng_unit_vector
+from conftest import rank_spread, rng_unit_vector
 
 pytestmark = pytest.mark.gpu
 
@@ -37,16 +37,6 @@ def cfg1(oracle):
 def cfgp(oracle):
     """Config-2 shape at small size: Dirichlet x, periodic y/z, N=5."""
     return oracle.box_problem(6, 3, 4, 3, periodic=(False, True, True), v=rng_unit_vector(1))
-
-
-def rank_spread(oracle, P, solve):
-    """Largest relative change of the oracle's solution over P-rank sum orders."""
-    base = solve(P["ops"])
-    worst = 0.0
-    for nt in (2, 3, 4, 7, 8):
-        ops = oracle.Ops(P["nx1"], P["nel"], P["D"], P["g"], P["bm1"], P["glo_num"], nt)
-        worst = max(worst, np.linalg.norm(solve(ops) - base) / np.linalg.norm(base))
-    return base, worst
 
 
 def rel(a, b):
