@@ -55,6 +55,9 @@ def parse():
     ap.add_argument("--cpu-iters", type=int, default=0, help="oracle PCG iterations per sample")
     ap.add_argument("--inner-tol", type=float, default=1e-4, help="mixed: inner FP32 tolerance")
     ap.add_argument("--only-mixed", action="store_true", help="skip the plain FP64 solve")
+    ap.add_argument("--workload", default="helmholtz", choices=["helmholtz", "batch"],
+                    help="batch: 3 velocity solves + 61 uneven Poisson problems in one batch")
+    ap.add_argument("--batch-problems", type=int, default=61)
     return ap.parse_args()
 
 
@@ -368,10 +371,106 @@ def run_gpu(args):
     lib.close()
 
 
+def batch_workload(nprob, seed=4):
+    """Three velocity-component Helmholtz problems (E=16^3, N=7, h1=1,
+    h2=1.5/dt with dt=1e-3) plus nprob Poisson problems with E log-uniform in
+    [64, 8192] (near-cubic kx*ky*kz) and N uniform in 5..9; every problem a
+    seeded deformed box with a standard-normal right-hand side."""
+    from nek5000_gb300 import mesh
+    rng = np.random.default_rng(seed)
+    specs = [(7, (16, 16, 16), 1500.0, 100 + c) for c in range(3)]
+    for q in range(nprob):
+        E = int(round(np.exp(rng.uniform(np.log(64), np.log(8192)))))
+        kx = max(2, int(round(E ** (1 / 3))))
+        ky = max(2, int(round((E / kx) ** 0.5)))
+        kz = max(2, int(round(E / (kx * ky))))
+        specs.append((int(rng.integers(5, 10)), (kx, ky, kz), 0.0, 200 + q))
+    probs = []
+    for N, (kx, ky, kz), h2, sd in specs:
+        M = mesh.box_mesh(N, kx, ky, kz, seed=sd)
+        r = np.random.default_rng(sd)
+        nglob = int(M["lattice"].max()) + 1
+        fg = r.standard_normal(nglob)[M["lattice"]]
+        M["f"] = mesh.dssum_host(M["lattice"], M["bm1"] * fg, nglob) * M["mask"]
+        M["h1"] = np.ones(M["n"])
+        M["h2"] = np.full(M["n"], h2)
+        M["spec"] = (N, kx, ky, kz, h2)
+        for k in ("x", "y", "z"):
+            M.pop(k, None)
+        probs.append(M)
+    return probs
+
+
+def run_batch(args):
+    import torch
+    ws, rank, local, pg = dist_setup(args.gpus)
+    torch.cuda.set_device(local)
+    from nek5000_gb300 import NekGpuBatch
+    from nek5000_gb300 import build as nb
+    nb.build()
+    probs = batch_workload(args.batch_problems)
+    B = NekGpuBatch(local)
+    for M in probs:
+        B.add(M["lx1"], M["nel"], M["D"], M["g"], M["bm1"], M["glo_num"])
+        M.pop("g")
+    dev = lambda a: torch.tensor(a, device=f"cuda:{local}")
+    cols = {k: [dev(M[k]) for M in probs] for k in ("f", "h1", "h2", "mask", "mult", "binv")}
+    xs = [torch.zeros(M["n"], dtype=torch.float64, device=f"cuda:{local}") for M in probs]
+    ns = np.array([M["n"] for M in probs], dtype=np.float64)
+
+    def solve(mixed):
+        return B.solve(xs, cols["f"], cols["h1"], cols["h2"], cols["mask"], cols["mult"],
+                       cols["binv"], tin=-args.tol, mixed=mixed, inner_tol=args.inner_tol)
+
+    out = {}
+    for mixed in (False, True):
+        for _ in range(args.warmup):
+            solve(mixed)
+        barrier(pg)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        with Clocks(local) as ck:
+            for _ in range(args.steps):
+                res = solve(mixed)
+            torch.cuda.synchronize()
+        T = allmax(pg, time.perf_counter() - t0)
+        if any(s != 0 for s in res["status"]):
+            raise RuntimeError(f"batch: status {res['status']}: {B.last_error()}")
+        out[mixed] = dict(res=res, T=T, clocks=ck.summary())
+    it64 = np.array(out[False]["res"]["niter"], dtype=np.float64)
+    v64 = allsum(pg, float((ns * it64).sum()) * args.steps) / out[False]["T"]
+    vmx = allsum(pg, float((ns * it64).sum()) * args.steps) / out[True]["T"]
+    line = {"metric": METRIC + " (batched workload)", "value": vmx, "unit": "DOF-iters/s",
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * out[True]["T"] / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 inner / f64 outer",
+            "data": "synthetic",
+            "config": {"workload": f"batch: 3 x helmholtz E=16^3 N=7 h2=1500 + "
+                                   f"{args.batch_problems} poisson E in [64,8192] log-uniform, "
+                                   "N in 5..9", "problems": len(probs),
+                       "n_points_total": int(ns.sum()),
+                       "value_definition": "sum_p n_p * (FP64 iterations of p) / batch solve time",
+                       "orders": [M["spec"][0] for M in probs],
+                       "elements": [M["nel"] for M in probs],
+                       "fp64_iterations": out[False]["res"]["niter"],
+                       "mixed_inner_iterations": out[True]["res"]["niter"],
+                       "mixed_outer_steps": out[True]["res"]["nouter"],
+                       "parallelism": f"replicas{ws}"},
+            "fp64": {"value": v64, "unit": "DOF-iters/s",
+                     "ms_per_step": 1e3 * out[False]["T"] / args.steps},
+            "speedup_mixed_vs_fp64": vmx / v64,
+            "clocks": out[True]["clocks"]}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    B.close()
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batch":
+        run_batch(args)
     else:
         run_gpu(args)
 
