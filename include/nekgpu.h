@@ -162,6 +162,26 @@ int nekgpu_hmholtz_mixed(const int64_t *handle, double *u, double *rhs, const do
                          const double *binv, const double *inner_tol, int *niter_outer,
                          int *niter_inner, double *rbn0, double *rbn2);
 
+/* ---- adjoint with respect to the viscosity h1 -------------------------- */
+/* gh1[p] = d(lam^T A(h1) u)/d h1[p] = (grad lam)_p . (G_p grad u)_p for every
+ * local point p (A is linear in h1; grad is the reference-element gradient
+ * and G_p the geometric factors of core/coef.f:633-784).  For J(u) with
+ * A(h1) u = f and adjoint A lam = dJ/du, dJ/dh1 = -gh1.  No reference
+ * counterpart (the reference's adjoint, core/perturb.f, is the adjoint
+ * Navier-Stokes equation, not a derivative of axhelm). */
+int nekgpu_axhelm_adjoint_h1(const int64_t *handle, double *gh1, const double *lam,
+                             const double *u);
+int nekgpu_axhelm_adjoint_h1_dev(const int64_t *handle, double *gh1, const double *lam,
+                                 const double *u);
+/* Adjoint solve A lam = g: the operator is symmetric, so this is cggo
+ * (core/hmholtz.f:611) with the same arguments; provided as its own entry
+ * point so adjoint code reads as such. */
+int nekgpu_cggo_adjoint_dev(const int64_t *handle, double *lam, const double *g,
+                            const double *h1, const double *h2, const double *mask,
+                            const double *mult, const int *imsh, const double *tin,
+                            const int *maxit, const int *isd, const double *binv,
+                            const int *maxcg, int *niter, double *rbn0, double *rbn2);
+
 /* ---- batched solves ---------------------------------------------------- */
 /* Many independent problems (each its own mesh, order and size) solved
  * together: every PCG phase is one launch over all problems, iterations are

@@ -56,6 +56,10 @@ SIGNATURES = {
                               _DP, _DP],
     "nekgpu_hmholtz_mixed": [_I64P, _P, _P, _P, _P, _P, _P, _IP, _DP, _IP, _IP, _P, _DP, _IP, _IP,
                              _DP, _DP],
+    "nekgpu_axhelm_adjoint_h1": [_I64P, _P, _P, _P],
+    "nekgpu_axhelm_adjoint_h1_dev": [_I64P, _P, _P, _P],
+    "nekgpu_cggo_adjoint_dev": [_I64P, _P, _P, _P, _P, _P, _P, _IP, _DP, _IP, _IP, _P, _IP, _IP, _DP,
+                                _DP],
     "nekgpu_batch_create": [_IP, _I64P],
     "nekgpu_batch_add": [_I64P, _IP, _IP, _P, _P, _P, _P, _P, _P, _P, _P, _P, _IP],
     "nekgpu_batch_solve_dev": [_I64P, _IP, _P, _P, _P, _P, _P, _P, _P, _DP, _IP, _IP, _DP, _P, _P,

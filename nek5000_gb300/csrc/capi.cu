@@ -691,6 +691,41 @@ int nekgpu_hmholtz_mixed(const int64_t* handle, double* u, double* rhs, const do
   return rc2 ? rc2 : rc;
 }
 
+int nekgpu_axhelm_adjoint_h1_dev(const int64_t* handle, double* gh1, const double* lam,
+                                 const double* u) {
+  GET_HANDLE(handle);
+  NEED_MESH();
+  if (check_n(H, gh1) || check_n(H, lam) || check_n(H, u)) return NEKGPU_EINVAL;
+  cudaError_t e = axhelm_adjoint_h1(H->mesh, gh1, lam, u, H->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(H->stream);
+  if (e != cudaSuccess) return cuda_fail(H, e, "axhelm_adjoint_h1");
+  return NEKGPU_OK;
+}
+
+int nekgpu_axhelm_adjoint_h1(const int64_t* handle, double* gh1, const double* lam,
+                             const double* u) {
+  GET_HANDLE(handle);
+  NEED_MESH();
+  if (check_n(H, gh1) || check_n(H, lam) || check_n(H, u)) return NEKGPU_EINVAL;
+  const int64_t n = H->mesh.n;
+  int rc;
+  if ((rc = h2d(H, H->io0, lam, n)) || (rc = h2d(H, H->io1, u, n))) return rc;
+  if (H->io3.ensure(n)) return fail(H, NEKGPU_ENOMEM, "staging allocation failed");
+  rc = nekgpu_axhelm_adjoint_h1_dev(handle, H->io3.ptr, H->io0.ptr, H->io1.ptr);
+  if (rc) return rc;
+  return d2h(H, gh1, H->io3.ptr, n);
+}
+
+int nekgpu_cggo_adjoint_dev(const int64_t* handle, double* lam, const double* g,
+                            const double* h1, const double* h2, const double* mask,
+                            const double* mult, const int* imsh, const double* tin,
+                            const int* maxit, const int* isd, const double* binv,
+                            const int* maxcg, int* niter, double* rbn0, double* rbn2) {
+  // The Helmholtz operator is symmetric, so the adjoint solve is cggo itself.
+  return nekgpu_cggo_dev(handle, lam, g, h1, h2, mask, mult, imsh, tin, maxit, isd, binv, maxcg,
+                         niter, rbn0, rbn2);
+}
+
 int nekgpu_launch_count(int64_t* count) {
   if (!count) return NEKGPU_EINVAL;
   *count = (int64_t)launch_counter().load();

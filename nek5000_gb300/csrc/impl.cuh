@@ -128,6 +128,9 @@ cudaError_t launch_axhelm_cg(const Mesh& m, const OpData<T>& op, T* w, T* p, con
                              const T* d, const Coef<T>& c, const CgScalars* cg, double* partial,
                              int* nblocks, cudaStream_t s);
 int axhelm_blocks(int nx1, int nel);
+// gh1_p = d(lam^T A(h1) u)/d h1_p for every local point (adjoint.cu).
+cudaError_t axhelm_adjoint_h1(const Mesh& m, double* gh1, const double* lam, const double* u,
+                              cudaStream_t s);
 
 // ---- solver / vector kernels (pcg.cu) ---------------------------------------
 template <typename T>

@@ -168,6 +168,17 @@ class NekGpu:
         fn = self._L.nekgpu_hmholtz_dev if _is_dev(u) else self._L.nekgpu_hmholtz
         return self._solve(fn, u, rhs, h1, h2, mask, mult, imsh, tli, maxit, isd, binv, maxcg)
 
+    def axhelm_adjoint_h1(self, gh1, lam, u):
+        """gh1 = d(lam^T A(h1) u)/dh1 per local point (dJ/dh1 = -gh1 for the adjoint lam)."""
+        fn = self._L.nekgpu_axhelm_adjoint_h1_dev if _is_dev(u) else self._L.nekgpu_axhelm_adjoint_h1
+        self._check(fn(C.byref(self._h), _ptr(gh1), _ptr(lam), _ptr(u)))
+        return gh1
+
+    def cggo_adjoint(self, lam, g, h1, h2, mask, mult, imsh, tin, maxit, isd, binv, maxcg=900):
+        """Adjoint solve A lam = g (device arrays; the operator is symmetric)."""
+        return self._solve(self._L.nekgpu_cggo_adjoint_dev, lam, g, h1, h2, mask, mult, imsh, tin,
+                           maxit, isd, binv, maxcg)
+
     def _solve_mixed(self, fn, a, b, h1, h2, mask, mult, imsh, tol, maxit, isd, binv, inner_tol):
         no, ni, r0, r2 = _cint(0), _cint(0), _cdouble(0), _cdouble(0)
         rc = fn(C.byref(self._h), _ptr(a), _ptr(b), _ptr(h1), _ptr(h2), _ptr(mask), _ptr(mult),
