@@ -140,6 +140,25 @@ int nekgpu_hmholtz_dev(const int64_t *handle, double *u, double *rhs, const doub
                        const double *binv, const int *maxcg, int *niter, double *rbn0,
                        double *rbn2);
 
+/* Allocation-free operator.  No counterpart in the reference: it exists for
+ * callers that cannot let a library allocate device memory -- a code that
+ * has given all device memory to its own pool allocator, one that runs under
+ * a hard memory budget, or a time-step loop that must not pay for the
+ * device-wide synchronisation cudaMalloc brings.  Same arguments and result
+ * as nekgpu_axhelm_dev (device arrays); it keeps the partial results of its
+ * h1/h2 scan in one fixed array of NEKGPU_NOALLOC_MAX_POINTS / 2048 * 4
+ * doubles (64 KiB) that every GPU loading this library holds until the
+ * process exits, and makes no device allocation itself.  Meshes of more than
+ * NEKGPU_NOALLOC_MAX_POINTS local points are rejected with NEKGPU_EINVAL.
+ * The first call on a device looks up that array's device address, so make
+ * it before any stream capture.  Calls share the array: calls that overlap on
+ * the GPU (from several threads or handles at once) race on it; each call
+ * writes every slot it reads, so nothing needs clearing between calls. */
+#define NEKGPU_NOALLOC_MAX_POINTS 4194304
+int nekgpu_axhelm_dev_noalloc(const int64_t *handle, double *au, const double *u,
+                              const double *h1, const double *h2, const int *imesh,
+                              const int *isd);
+
 /* ---- mixed precision --------------------------------------------------- */
 /* Same system and FP64 stopping rule as cggo, solved by FP64 defect
  * correction around an FP32 Jacobi-PCG: each outer step solves A e = r in

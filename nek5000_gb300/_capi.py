@@ -17,6 +17,7 @@ OK = 0
 EINVAL, EHANDLE, ECUDA, ENOMEM, ENOTCONV, ENOSETUP, ENAN = -1, -2, -3, -4, -5, -6, -7
 OPT_EXACT, OPT_TIMING, OPT_CHUNK, OPT_ISTEP, OPT_TMA, OPT_GRAPH = 1, 2, 3, 4, 5, 6
 MAX_LX1 = 12
+NOALLOC_MAX_POINTS = 4194304
 
 STATUS_NAMES = {
     0: "NEKGPU_OK", -1: "NEKGPU_EINVAL", -2: "NEKGPU_EHANDLE", -3: "NEKGPU_ECUDA",
@@ -39,6 +40,7 @@ SIGNATURES = {
     "nekgpu_gs_maps": [_I64P, _I64P, _I64P, _P, _P],
     "nekgpu_axhelm": [_I64P, _P, _P, _P, _P, _IP, _IP],
     "nekgpu_axhelm_dev": [_I64P, _P, _P, _P, _P, _IP, _IP],
+    "nekgpu_axhelm_dev_noalloc": [_I64P, _P, _P, _P, _P, _IP, _IP],
     "nekgpu_dssum": [_I64P, _P],
     "nekgpu_dssum_dev": [_I64P, _P],
     "nekgpu_dsop_dev": [_I64P, _P, C.c_char_p],

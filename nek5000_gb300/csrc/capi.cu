@@ -324,10 +324,10 @@ int handle_setup(Handle& H, int lx1, int nel, const double* dxm1, const double* 
   return 0;
 }
 
-}  // namespace nekgpu
+Handle* handle_lookup(const int64_t* h) { return get(h); }
+int handle_fail(Handle* H, int code, const std::string& msg) { return fail(H, code, msg); }
 
-namespace {
-}  // namespace
+}  // namespace nekgpu
 
 extern "C" {
 
