@@ -53,12 +53,19 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-iters", type=int, default=0, help="oracle PCG iterations per sample")
-    ap.add_argument("--inner-tol", type=float, default=1e-4, help="mixed: inner FP32 tolerance")
+    ap.add_argument("--inner-tol", type=float, default=None,
+                    help="mixed: inner FP32 tolerance (default: the library's for the mode)")
     ap.add_argument("--only-mixed", action="store_true", help="skip the plain FP64 solve")
+    ap.add_argument("--mixed-mode", type=int, default=1, choices=[0, 1],
+                    help="mixed: 1 residual replacement keeping the search direction, "
+                         "0 restarted FP32 PCG per outer step")
     ap.add_argument("--workload", default="helmholtz", choices=["helmholtz", "batch"],
                     help="batch: 3 velocity solves + 61 uneven Poisson problems in one batch")
     ap.add_argument("--batch-problems", type=int, default=61)
-    return ap.parse_args()
+    args = ap.parse_args()
+    if args.inner_tol is None:  # the library's defaults; the batch solve restarts per outer step
+        args.inner_tol = 1e-2 if (args.mixed_mode == 1 and args.workload == "helmholtz") else 1e-4
+    return args
 
 
 def workload(k, N):
@@ -246,6 +253,7 @@ def run_gpu(args):
     x = torch.zeros(n, dtype=torch.float64, device=f"cuda:{local}")
     big = 10 ** 6
     lib.set_option(2, 1)  # timing: solve-total and per-launch operator events
+    lib.set_option(7, args.mixed_mode)
 
     def fp64():
         it, r0, r2, rc = lib.cggo(x, f, h1, h2, mask, mult, 1, -args.tol, big, 1, binv, maxcg=big)
@@ -312,7 +320,9 @@ def run_gpu(args):
             "config": {"workload": f"helmholtz E={args.k}^3 N={args.N} h1=1 h2=10 "
                                    "dirichlet-x periodic-yz", "n_points": n,
                        "solver": "mixed: fp32 jacobi-pcg (inner tol "
-                                 f"{args.inner_tol:g}) in fp64 defect correction",
+                                 f"{args.inner_tol:g}) in fp64 defect correction, " +
+                                 ("fp64 residual replacement, search direction kept"
+                                  if args.mixed_mode == 1 else "restarted per outer step"),
                        "value_definition": "n * (FP64 PCG iteration count) / mixed solve time",
                        "tol": args.tol, "outer_steps": outer, "inner_iterations": inner,
                        "inner_rate_dof_iters_per_s": allsum(pg, n * sum(inner)) / rmx["T"],

@@ -56,6 +56,10 @@ extern "C" {
                                 copies where lx1 is even; 0: plain loads         */
 #define NEKGPU_OPT_GRAPH 6   /* 1 (default): replay each chunk of PCG iterations
                                 as one captured CUDA graph; 0: direct launches   */
+#define NEKGPU_OPT_MIXED_MODE 7  /* mixed solve: 1 (default) one FP32 PCG whose
+                                residual is replaced by the FP64 one each time
+                                it drops by inner_tol, search direction kept;
+                                0 a fresh FP32 PCG per outer step               */
 
 /* ---- life cycle ---------------------------------------------------------- */
 /* Create a handle on CUDA device *device.  Replaces the per-rank setup the
@@ -161,13 +165,17 @@ int nekgpu_axhelm_dev_noalloc(const int64_t *handle, double *au, const double *u
 
 /* ---- mixed precision --------------------------------------------------- */
 /* Same system and FP64 stopping rule as cggo, solved by FP64 defect
- * correction around an FP32 Jacobi-PCG: each outer step solves A e = r in
- * FP32 (G, D, fields, diagonal stored FP32) to *inner_tol relative (default
- * 1e-5 when NULL), adds e to x in FP64 and recomputes r = f - A x with the
- * FP64 operator.  Stops when the FP64 norm sqrt(sum r^2 mult binv / vol)
- * reaches |tin| (tin >= 0) or |tin| * its initial value (tin < 0).  *maxit
- * caps each inner solve.  Outputs: outer steps, total inner iterations, first
- * and last FP64 norms.  No reference counterpart: it replaces cggo
+ * correction around an FP32 Jacobi-PCG (G, D, fields, diagonal stored FP32).
+ * Each time the FP32 residual has dropped by *inner_tol, the FP32 correction
+ * is added to x in FP64 and r = f - A x is recomputed with the FP64 operator.
+ * NEKGPU_OPT_MIXED_MODE 1 (default) puts that r back into the running FP32
+ * PCG and keeps its search direction (default *inner_tol 1e-2 when NULL);
+ * mode 0 starts a fresh FP32 PCG on it (default *inner_tol 1e-5).  Stops when
+ * the FP64 norm sqrt(sum r^2 mult binv / vol) reaches |tin| (tin >= 0) or
+ * |tin| * its initial value (tin < 0).  *maxit caps the FP32 iterations (of
+ * the whole solve in mode 1, of each inner solve in mode 0).  Outputs: outer
+ * steps (FP64 residual evaluations), total inner iterations, first and last
+ * FP64 norms.  No reference counterpart: it replaces cggo
  * (core/hmholtz.f:611) for callers that accept FP32 inner arithmetic. */
 int nekgpu_cggo_mixed_dev(const int64_t *handle, double *x, const double *f, const double *h1,
                           const double *h2, const double *mask, const double *mult,

@@ -15,7 +15,8 @@ LIB_PATH = os.path.join(HERE, "libnekgpu.so")
 
 OK = 0
 EINVAL, EHANDLE, ECUDA, ENOMEM, ENOTCONV, ENOSETUP, ENAN = -1, -2, -3, -4, -5, -6, -7
-OPT_EXACT, OPT_TIMING, OPT_CHUNK, OPT_ISTEP, OPT_TMA, OPT_GRAPH = 1, 2, 3, 4, 5, 6
+OPT_EXACT, OPT_TIMING, OPT_CHUNK, OPT_ISTEP, OPT_TMA, OPT_GRAPH, OPT_MIXED_MODE = (
+    1, 2, 3, 4, 5, 6, 7)
 MAX_LX1 = 12
 NOALLOC_MAX_POINTS = 4194304
 

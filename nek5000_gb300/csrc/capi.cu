@@ -379,6 +379,10 @@ int nekgpu_set_option(const int64_t* handle, const int* key, const int* value) {
     case NEKGPU_OPT_ISTEP: H->istep = *value; break;
     case NEKGPU_OPT_TMA: H->mesh.use_tma = (*value != 0); break;
     case NEKGPU_OPT_GRAPH: H->use_graph = (*value != 0); break;
+    case NEKGPU_OPT_MIXED_MODE:
+      if (*value != 0 && *value != 1) return fail(H, NEKGPU_EINVAL, "mixed mode must be 0 or 1");
+      H->mixed_mode = *value;
+      break;
     default: return fail(H, NEKGPU_EINVAL, "unknown option");
   }
   return NEKGPU_OK;
@@ -631,12 +635,13 @@ int nekgpu_cggo_mixed_dev(const int64_t* handle, double* x, const double* f, con
   if (check_n(H, x) || check_n(H, f) || check_n(H, h1) || check_n(H, h2) || check_n(H, mask) ||
       check_n(H, mult) || check_n(H, binv) || !tin || !maxit)
     return fail(H, NEKGPU_EINVAL, "null argument");
-  const double itol = inner_tol ? *inner_tol : 1e-5;
+  const double itol = inner_tol ? *inner_tol : (H->mixed_mode == 1 ? 1e-2 : 1e-5);
   if (!(itol > 0.0 && itol < 1.0)) return fail(H, NEKGPU_EINVAL, "inner_tol must be in (0, 1)");
   H->ms_axhelm = 0.0;
   H->n_axhelm = 0;
   if (H->timing) cudaEventRecord(H->evt0, H->stream);
-  MixedResult r = mixed_solve(*H, x, f, h1, h2, mask, mult, binv, *tin, *maxit, itol);
+  MixedResult r = mixed_solve(*H, x, f, h1, h2, mask, mult, binv, *tin, *maxit, itol,
+                              H->mixed_mode);
   if (H->timing) {
     cudaEventRecord(H->evt1, H->stream);
     cudaEventSynchronize(H->evt1);

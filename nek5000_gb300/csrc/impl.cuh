@@ -115,6 +115,7 @@ struct Handle {
   int graph_chunk = 16;
   bool own_stream = true;
   bool use_graph = true;
+  int mixed_mode = 1;  // see mixed_solve
 };
 
 // ---- operator entry points (axhelm_*.cu) ---------------------------------
@@ -161,6 +162,12 @@ PcgResult pcg_prepare(Handle& h, PcgWork<T>& wk, T* x, const T* f, const Coef<T>
                       const T* mask, const T* mult, double tin, int maxiter, int istep,
                       const T* dpre, bool* trivial);
 int pcg_vec_blocks(int64_t n);
+// Iteration-1 check of a prepared solve (no update), then the iterations.
+template <typename T>
+void pcg_first_check(Handle& h, PcgWork<T>& wk, T* x, const T* mult, const T* binv, bool exact);
+template <typename T>
+PcgResult pcg_iterate(Handle& h, const OpData<T>& op, PcgWork<T>& wk, T* x, const Coef<T>& c,
+                      const T* mult, const T* binv, bool exact);
 
 // Mixed-precision helpers (mixed.cu), used by the batched solver too.
 int ensure_f32(Handle& h);
@@ -175,12 +182,17 @@ double norm64(Handle& h, const double* r, const double* mult, const double* binv
 // Mixed precision (mixed.cu): FP32 inner PCG in an FP64 defect-correction loop.
 struct MixedResult {
   int outer = 0, inner = 0;
+  int restarts = 0;  // mode 1: replacements that also restarted the direction
   double rbn0 = 0, rbn2 = 0;
   int status = 0;
 };
+// mode 0: each outer step is a fresh FP32 PCG to inner_tol (restarted);
+// mode 1: one FP32 PCG whose residual is replaced by the FP64 one whenever it
+// has dropped by inner_tol, keeping the search direction (reliable updates).
 MixedResult mixed_solve(Handle& h, double* x, const double* f, const double* h1,
                         const double* h2, const double* mask, const double* mult,
-                        const double* binv, double tin, int maxit, double inner_tol);
+                        const double* binv, double tin, int maxit, double inner_tol,
+                        int mode = 0);
 
 void set_error(Handle& h, const std::string& msg);
 

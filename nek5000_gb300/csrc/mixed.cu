@@ -76,6 +76,32 @@ __global__ void norm_kernel(const double* __restrict__ r, const double* __restri
   if (threadIdx.x == 0) partial[blockIdx.x] = acc;
 }
 
+__global__ void scale_kernel(float* __restrict__ a, float f, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    a[i] *= f;
+}
+
+// partial[b] = sum (r d) r mult, partial[nb + b] = sum mult binv r r (FP32 data)
+__global__ void rz_kernel(const float* __restrict__ r, const float* __restrict__ d,
+                          const float* __restrict__ mult, const float* __restrict__ binv,
+                          int64_t n, double* __restrict__ partial) {
+  __shared__ double red[32];
+  CompAcc<float> a1, a2;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const float ri = r[i], m = mult[i];
+    a1.add(ri * d[i] * ri * m);
+    a2.add(m * binv[i] * ri * ri);
+  }
+  const double b1 = block_sum_comp(a1, red);
+  const double b2 = block_sum_comp(a2, red);
+  if (threadIdx.x == 0) {
+    partial[blockIdx.x] = b1;
+    partial[gridDim.x + blockIdx.x] = b2;
+  }
+}
+
 double host_sum(Handle& h, int nb, int* st) {
   std::vector<double> hp((size_t)nb);
   if (cudaMemcpyAsync(hp.data(), h.red.ptr, nb * sizeof(double), cudaMemcpyDeviceToHost,
@@ -159,7 +185,7 @@ double outer_residual(Handle& h, double* r, const double* f, const double* x,
 
 MixedResult mixed_solve(Handle& h, double* x, const double* f, const double* h1,
                         const double* h2, const double* mask, const double* mult,
-                        const double* binv, double tin, int maxit, double inner_tol) {
+                        const double* binv, double tin, int maxit, double inner_tol, int mode) {
   MixedResult res;
   Mesh& m = h.mesh;
   const int64_t n = m.n;
@@ -233,6 +259,96 @@ MixedResult mixed_solve(Handle& h, double* x, const double* f, const double* h1,
   const double tol = tin < 0 ? std::fabs(tin) * rbn0 : std::fabs(tin);
   double rbn = rbn0;
   const bool exact = false;
+  if (mode == 1) {
+    // One FP32 PCG; whenever its residual has dropped by inner_tol the
+    // correction joins x in FP64, r = f - A x is recomputed in FP64 and put
+    // back (rescaled) as the FP32 residual, and the search direction p and
+    // beta are kept (rescaled), so the Krylov space built so far is not lost.
+    int st2 = 0;
+    double amax = device_absmax<double>(h, w64.r.ptr, n, &st2);
+    if (st2 || amax == 0.0) {
+      res.status = st2 ? -3 : 0;
+      return res;
+    }
+    double scale = std::ldexp(1.0, std::ilogb(amax));
+    cast(wk.f.ptr, w64.r.ptr, 1.0 / scale);
+    bool trivial = false;
+    PcgResult pr = pcg_prepare<float>(h, wk, wk.x.ptr, wk.f.ptr, c32, wk.mask.ptr, wk.mult.ptr,
+                                      -inner_tol, maxit, 0, wk.d.ptr, &trivial);
+    if (pr.status) {
+      res.status = pr.status;
+      return res;
+    }
+    pcg_first_check<float>(h, wk, wk.x.ptr, wk.mult.ptr, wk.binv.ptr, false);
+    for (int upd = 1; upd <= 100000; ++upd) {
+      pr = pcg_iterate<float>(h, m.f32, wk, wk.x.ptr, c32, wk.mult.ptr, wk.binv.ptr, false);
+      if (pr.status && pr.status != -5) {
+        res.status = pr.status;
+        return res;
+      }
+      res.outer = upd;
+      res.inner = h.cg_host->niter;
+      const bool capped = h.cg_host->iter > h.cg_host->maxiter;
+      count_launch();
+      axpy_kernel<<<nb, kThreads, 0, s>>>(x, wk.x.ptr, scale, n);
+      const double rnew = outer_residual(h, w64.r.ptr, f, x, c64, mask, mult, binv, w64.w.ptr);
+      if (!(rnew >= 0.0) || !std::isfinite(rnew)) {
+        res.status = -7;
+        set_error(h, "mixed: non-finite outer residual");
+        return res;
+      }
+      const bool progress = rnew < rbn;
+      rbn = rnew;
+      if (rbn <= tol || capped || !progress) break;
+      // residual replacement, rescaled to a power of two near max |r|
+      amax = device_absmax<double>(h, w64.r.ptr, n, &st2);
+      if (st2 || amax == 0.0) break;
+      const double s_new = std::ldexp(1.0, std::ilogb(amax));
+      const double ratio = scale / s_new;  // exact: both powers of two
+      cast(wk.r.ptr, w64.r.ptr, 1.0 / s_new);
+      count_launch();
+      scale_kernel<<<nb, kThreads, 0, s>>>(wk.p.ptr, (float)ratio, n);
+      cudaMemsetAsync(wk.x.ptr, 0, n * sizeof(float), s);
+      count_launch();
+      rz_kernel<<<nb, kThreads, 0, s>>>(wk.r.ptr, wk.d.ptr, wk.mult.ptr, wk.binv.ptr, n,
+                                        h.red.ptr);
+      std::vector<double> hp(2 * (size_t)nb);
+      cudaMemcpyAsync(hp.data(), h.red.ptr, hp.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                      s);
+      if (cudaStreamSynchronize(s) != cudaSuccess) {
+        res.status = -3;
+        return res;
+      }
+      double s1 = 0.0, s2 = 0.0;
+      for (int b = 0; b < nb; ++b) {
+        s1 += hp[b];
+        s2 += hp[nb + b];
+      }
+      CgScalars& c = *h.cg_host;  // state after the last (iterated) check
+      const double rec = c.rbn2 * ratio;  // FP32 recurrence norm, new scaling
+      c.rtz2 = c.rtz2 * ratio * ratio;
+      c.rtz1 = s1;
+      c.rbn0 = std::sqrt(s2 / m.vol);
+      // Keep the search direction while the true residual is still close to
+      // the recurrence one; once FP32 drift dominates (true norm more than
+      // twice the recurrence norm) p no longer fits r and the direction is
+      // restarted (beta = 0: p = z).
+      c.beta = (c.rbn0 <= 2.0 * rec) ? s1 / c.rtz2 : 0.0;
+      if (c.beta == 0.0) ++res.restarts;
+      c.rbn2 = c.rbn0;
+      c.tol = inner_tol * c.rbn0;
+      c.done = 0;
+      c.counter[0] = c.counter[1] = c.counter[2] = c.counter[3] = 0u;
+      cudaMemcpyAsync(h.cg, &c, sizeof(CgScalars), cudaMemcpyHostToDevice, s);
+      scale = s_new;
+    }
+    res.rbn2 = rbn;
+    if (!(rbn <= tol)) {
+      res.status = -5;
+      set_error(h, "mixed: defect correction did not reach the tolerance");
+    }
+    return res;
+  }
   for (int outer = 1; outer <= kMaxOuter; ++outer) {
     if (rbn <= tol) break;
     const double amax = device_absmax<double>(h, w64.r.ptr, n, &st);

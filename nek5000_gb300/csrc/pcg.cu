@@ -489,6 +489,19 @@ template PcgResult pcg_prepare<float>(Handle&, PcgWork<float>&, float*, const fl
                                       int, const float*, bool*);
 
 template <typename T>
+PcgResult pcg_iterate(Handle& h, const OpData<T>& op, PcgWork<T>& wk, T* x, const Coef<T>& c,
+                      const T* mult, const T* binv, bool exact);
+
+template <typename T>
+void pcg_first_check(Handle& h, PcgWork<T>& wk, T* x, const T* mult, const T* binv, bool exact) {
+  launch_C<T>(h, wk, x, mult, binv, exact, true);
+}
+template void pcg_first_check<double>(Handle&, PcgWork<double>&, double*, const double*,
+                                      const double*, bool);
+template void pcg_first_check<float>(Handle&, PcgWork<float>&, float*, const float*, const float*,
+                                     bool);
+
+template <typename T>
 PcgResult pcg_solve(Handle& h, const OpData<T>& op, PcgWork<T>& wk, T* x, const T* f,
                     const Coef<T>& c, const T* mask, const T* mult, const T* binv, double tin,
                     int maxiter, int istep, bool exact, const T* dpre) {
@@ -499,6 +512,19 @@ PcgResult pcg_solve(Handle& h, const OpData<T>& op, PcgWork<T>& wk, T* x, const 
   if (res.status || trivial) return res;
   // iteration 1 check (z, s1, s2) -- no update
   launch_C<T>(h, wk, x, mult, binv, exact, true);
+  return pcg_iterate<T>(h, op, wk, x, c, mult, binv, exact);
+}
+
+// Iterations of a prepared solve (after its iteration-1 check) until the
+// device flags it done; then the reference's outputs.
+template <typename T>
+PcgResult pcg_iterate(Handle& h, const OpData<T>& op, PcgWork<T>& wk, T* x, const Coef<T>& c,
+                      const T* mult, const T* binv, bool exact) {
+  PcgResult res;
+  Mesh& m = h.mesh;
+  cudaStream_t s = h.stream;
+  const T* f = wk.r.ptr;  // graph key only
+  const T* mask = wk.segmask.ptr;
   // main loop: chunks of iterations, one host check per chunk.  With kernel
   // timing on, every fused-axhelm launch is bracketed by events; after the
   // chunk's check, the first (iterations completed in the chunk) of them are
@@ -617,6 +643,11 @@ PcgResult pcg_solve(Handle& h, const OpData<T>& op, PcgWork<T>& wk, T* x, const 
   return res;
 }
 
+template PcgResult pcg_iterate<double>(Handle&, const OpData<double>&, PcgWork<double>&,
+                                       double*, const Coef<double>&, const double*, const double*,
+                                       bool);
+template PcgResult pcg_iterate<float>(Handle&, const OpData<float>&, PcgWork<float>&, float*,
+                                      const Coef<float>&, const float*, const float*, bool);
 template PcgResult pcg_solve<double>(Handle&, const OpData<double>&, PcgWork<double>&, double*,
                                      const double*, const Coef<double>&, const double*,
                                      const double*, const double*, double, int, int, bool,

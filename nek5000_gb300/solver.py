@@ -183,21 +183,22 @@ class NekGpu:
         no, ni, r0, r2 = _cint(0), _cint(0), _cdouble(0), _cdouble(0)
         rc = fn(C.byref(self._h), _ptr(a), _ptr(b), _ptr(h1), _ptr(h2), _ptr(mask), _ptr(mult),
                 C.byref(_cint(imsh)), C.byref(_cdouble(tol)), C.byref(_cint(int(maxit))),
-                C.byref(_cint(isd)), _ptr(binv), C.byref(_cdouble(inner_tol)), C.byref(no),
+                C.byref(_cint(isd)), _ptr(binv),
+                None if inner_tol is None else C.byref(_cdouble(inner_tol)), C.byref(no),
                 C.byref(ni), C.byref(r0), C.byref(r2))
         self._check(rc, allow=(_capi.ENOTCONV,))
         return no.value, ni.value, r0.value, r2.value, rc
 
-    def cggo_mixed(self, x, f, h1, h2, mask, mult, imsh, tin, maxit, isd, binv, inner_tol=1e-5):
+    def cggo_mixed(self, x, f, h1, h2, mask, mult, imsh, tin, maxit, isd, binv, inner_tol=None):
         """FP32-inner / FP64-defect-correction form of cggo (device arrays).
-        Returns (outer steps, inner iterations, rbn0, rbn2, status)."""
+        inner_tol None takes the library's default for the mixed mode.  Returns (outer steps, inner iterations, rbn0, rbn2, status)."""
         if not _is_dev(x):
             raise TypeError("cggo_mixed takes device arrays")
         return self._solve_mixed(self._L.nekgpu_cggo_mixed_dev, x, f, h1, h2, mask, mult, imsh,
                                  tin, maxit, isd, binv, inner_tol)
 
     def hmholtz_mixed(self, name, u, rhs, h1, h2, mask, mult, imsh, tli, maxit, isd, binv,
-                      inner_tol=1e-5):
+                      inner_tol=None):
         """hmholtz with the mixed-precision solve (host arrays)."""
         del name
         return self._solve_mixed(self._L.nekgpu_hmholtz_mixed, u, rhs, h1, h2, mask, mult, imsh,

@@ -1,6 +1,13 @@
 """Mixed precision: FP32 inner PCG inside FP64 defect correction, against the
 FP64 oracle on the same seeded mesh and right-hand side.
 
+Both forms of the defect correction are run: mode 1 (default) keeps one FP32
+PCG and replaces its residual by the FP64 one each time it has dropped by
+inner_tol; mode 0 starts a fresh FP32 PCG at every outer step.
+
+Each mode runs with its default inner tolerance (1e-2 for mode 1, 1e-5 for
+mode 0).
+
 Pass criteria (per solve):
   * the FP64 residual of the returned x, recomputed by the oracle's operator
     (r = f - mask*dssum(A x), cggo's norm), is <= 1.05 * 1e-10 * rbn0;
@@ -23,13 +30,15 @@ def fp64_residual_norm(P, x, f, h1, h2):
     return np.sqrt(np.sum(P["mult"] * P["binv"] * r * r) / np.sum(P["bm1"]))
 
 
+@pytest.mark.parametrize("mode", [1, 0])
 @pytest.mark.parametrize("case", [
     dict(nx1=10, k=(3, 3, 3), periodic=(False, False, False), h2=0.0, seed=2),   # N=9 Poisson
     dict(nx1=8, k=(3, 4, 3), periodic=(False, True, True), h2=10.0, seed=1),     # Helmholtz, periodic
     dict(nx1=6, k=(2, 2, 2), periodic=(False, False, False), h2=1500.0, seed=3), # velocity-like h2
 ])
-def test_mixed_meets_fp64_tolerance(gpu_lib, oracle, case):
+def test_mixed_meets_fp64_tolerance(gpu_lib, oracle, case, mode):
     torch = pytest.importorskip("torch")
+    from nek5000_gb300 import _capi
     kx, ky, kz = case["k"]
     P = oracle.box_problem(case["nx1"], kx, ky, kz, periodic=case["periodic"],
                            v=rng_unit_vector(case["seed"]))
@@ -41,20 +50,23 @@ def test_mixed_meets_fp64_tolerance(gpu_lib, oracle, case):
                                                   maxcg=10 ** 6)
     lib = gpu_lib(0)
     lib.setup(P["nx1"], P["nel"], P["D"], P["g"], P["bm1"], P["glo_num"])
+    lib.set_option(_capi.OPT_MIXED_MODE, mode)
     dev = lambda a: torch.tensor(a, device="cuda")
     x = torch.zeros(n, dtype=torch.float64, device="cuda")
     outer, inner, r0, r2, rc = lib.cggo_mixed(x, dev(f), dev(h1), dev(h2), dev(P["mask"]),
                                               dev(P["mult"]), 1, -1e-10, 10 ** 6, 1, dev(P["binv"]),
-                                              inner_tol=1e-5)
+                                              inner_tol=None)
     assert rc == 0, lib.last_error()
     xs = x.cpu().numpy()
     assert abs(r0 - r0_ref) <= 1e-12 * r0_ref
     rn = fp64_residual_norm(P, xs, f, h1, h2)
     assert rn <= 1.05e-10 * r0_ref, (rn / r0_ref, outer, inner)
     err = np.linalg.norm(xs - x_ref) / np.linalg.norm(x_ref)
-    print(f"mixed: outer {outer} inner {inner} (FP64 cggo {it_ref}), rel. error vs FP64 oracle {err:.2e}")
+    print(f"mixed mode {mode}: outer {outer} inner {inner} (FP64 cggo {it_ref}), rel. error vs FP64 oracle {err:.2e}")
     assert err <= 1e-8
-    assert 2 <= outer <= 6
+    assert 2 <= outer <= (12 if mode == 1 else 6)
+    if mode == 1:  # the kept search direction: no more FP32 iterations than FP64 ones, +10%
+        assert inner <= 1.1 * it_ref + 5, (inner, it_ref)
 
 
 def test_mixed_host_entry_point(gpu_lib, oracle):
