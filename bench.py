@@ -59,28 +59,57 @@ def parse():
     ap.add_argument("--mixed-mode", type=int, default=1, choices=[0, 1],
                     help="mixed: 1 residual replacement keeping the search direction, "
                          "0 restarted FP32 PCG per outer step")
-    ap.add_argument("--workload", default="helmholtz", choices=["helmholtz", "batch"],
-                    help="batch: 3 velocity solves + 61 uneven Poisson problems in one batch")
+    ap.add_argument("--workload", default="helmholtz",
+                    choices=["helmholtz", "poisson-n9", "batch", "axhelm-sweep"],
+                    help="helmholtz: E=32^3 N=7 (default); poisson-n9: E=24^3 N=9 Poisson; "
+                         "batch: 3 velocity solves + 61 uneven Poisson problems in one batch; "
+                         "axhelm-sweep: in-solve operator bandwidth at N=5,7,9, E=32^3")
     ap.add_argument("--batch-problems", type=int, default=61)
     args = ap.parse_args()
+    if args.workload == "poisson-n9":
+        if args.k == 32:
+            args.k = 24
+        if args.N == 7:
+            args.N = 9
     if args.inner_tol is None:  # the library's defaults; the batch solve restarts per outer step
-        args.inner_tol = 1e-2 if (args.mixed_mode == 1 and args.workload == "helmholtz") else 1e-4
+        args.inner_tol = 1e-2 if (args.mixed_mode == 1 and args.workload != "batch") else 1e-4
     return args
 
 
-def workload(k, N):
+def workload(k, N, kind="helmholtz"):
+    """helmholtz: deformed box (seed 1), Dirichlet on the x-faces, periodic in
+    y and z, h1 = 1, h2 = 10, standard-normal right-hand side per global node.
+    poisson: deformed box (seed 0), Dirichlet on every face, h1 = 1, h2 = 0,
+    uniform [-1, 1] right-hand side per global node (seed 0).  Both
+    mass-weighted: rhs = bm1 * f."""
     from nek5000_gb300 import mesh
-    M = mesh.box_mesh(N, k, k, k, periodic=(False, True, True),
-                      dirichlet=(True, True, False, False, False, False), seed=1)
-    rng = np.random.default_rng(1)
-    nglob = int(M["lattice"].max()) + 1
-    f = rng.standard_normal(nglob)[M["lattice"]]
+    if kind == "poisson":
+        M = mesh.box_mesh(N, k, k, k, seed=0)
+        rng = np.random.default_rng(0)
+        nglob = int(M["lattice"].max()) + 1
+        f = rng.uniform(-1.0, 1.0, nglob)[M["lattice"]]
+        h2 = 0.0
+    else:
+        M = mesh.box_mesh(N, k, k, k, periodic=(False, True, True),
+                          dirichlet=(True, True, False, False, False, False), seed=1)
+        rng = np.random.default_rng(1)
+        nglob = int(M["lattice"].max()) + 1
+        f = rng.standard_normal(nglob)[M["lattice"]]
+        h2 = 10.0
     M["rhs"] = M["bm1"] * f
     # assembled, masked right-hand side (what hmholtz hands to cggo)
     M["f"] = mesh.dssum_host(M["lattice"], M["rhs"], nglob) * M["mask"]
     M["h1"] = np.ones(M["n"])
-    M["h2"] = np.full(M["n"], 10.0)
+    M["h2"] = np.full(M["n"], h2)
+    for c in ("x", "y", "z"):
+        M.pop(c, None)
     return M
+
+
+def workload_name(args):
+    if args.workload == "poisson-n9":
+        return f"poisson E={args.k}^3 N={args.N} h1=1 h2=0 dirichlet-all"
+    return f"helmholtz E={args.k}^3 N={args.N} h1=1 h2=10 dirichlet-x periodic-yz"
 
 
 def peaks():
@@ -210,7 +239,7 @@ def run_reference(args):
     ws, rank, local, pg = dist_setup(args.gpus)
     if rank != 0:
         return
-    M = workload(args.k, args.N)
+    M = workload(args.k, args.N, "poisson" if args.workload == "poisson-n9" else "helmholtz")
     nth = os.cpu_count() or 1
     iters = args.cpu_iters or 100
     for _ in range(args.warmup):
@@ -227,8 +256,7 @@ def run_reference(args):
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"helmholtz E={args.k}^3 N={args.N} h1=1 h2=10 "
-                                   "dirichlet-x periodic-yz", "n_points": M["n"]},
+            "config": {"workload": workload_name(args), "n_points": M["n"]},
             "cpu_baseline": {"value": value, "unit": "DOF-iters/s", "cores": nth, "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": "DOF-iters/s", "h2d_bytes_per_step": 0,
@@ -243,7 +271,7 @@ def run_gpu(args):
     from nek5000_gb300 import NekGpu
     from nek5000_gb300 import build as nb
     nb.build()
-    M = workload(args.k, args.N)
+    M = workload(args.k, args.N, "poisson" if args.workload == "poisson-n9" else "helmholtz")
     n = M["n"]
     lib = NekGpu(local)
     lib.setup(M["lx1"], M["nel"], M["D"], M["g"], M["bm1"], M["glo_num"])
@@ -299,12 +327,16 @@ def run_gpu(args):
     fp64_block = {
         "value": v64, "unit": "DOF-iters/s", "iterations": r64["iters"],
         "ms_per_solve": 1e3 * r64["T"] / args.steps,
-        "axhelm": {"kernel": "axhelm_kernel<8,double,fused>", "avg_launch_ms": r64["ms_ax"],
+        "axhelm": {"kernel": f"axhelm_kernel<{M['lx1']},double,fused>",
+                   "avg_launch_ms": r64["ms_ax"],
                    "GB/s": b64 * n / (r64["ms_ax"] * 1e-3) / 1e9, "bytes_per_point": b64,
                    "fp64_tflops": flops_pt * n / (r64["ms_ax"] * 1e-3) / 1e12,
                    "ncu_fp64_pipe_active_pct": (ns64 or {}).get("fp64_pipe_active_pct")},
         "gpu_launches": r64["launches"], "clocks": r64["clocks"]}
+    x64 = x.clone() if not args.only_mixed else None
     rmx = timed(mixed)
+    err64 = (float(torch.linalg.norm(x - x64) / torch.linalg.norm(x64))
+             if x64 is not None else None)
     outer = [o for o, i in rmx["iters"]]
     inner = [i for o, i in rmx["iters"]]
     # time to solution, counted with the FP64 solve's iteration count
@@ -317,8 +349,7 @@ def run_gpu(args):
             "ms_per_step": 1e3 * rmx["T"] / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 inner / f64 outer",
             "data": "synthetic",
-            "config": {"workload": f"helmholtz E={args.k}^3 N={args.N} h1=1 h2=10 "
-                                   "dirichlet-x periodic-yz", "n_points": n,
+            "config": {"workload": workload_name(args), "n_points": n,
                        "solver": "mixed: fp32 jacobi-pcg (inner tol "
                                  f"{args.inner_tol:g}) in fp64 defect correction, " +
                                  ("fp64 residual replacement, search direction kept"
@@ -326,10 +357,15 @@ def run_gpu(args):
                        "value_definition": "n * (FP64 PCG iteration count) / mixed solve time",
                        "tol": args.tol, "outer_steps": outer, "inner_iterations": inner,
                        "inner_rate_dof_iters_per_s": allsum(pg, n * sum(inner)) / rmx["T"],
+                       "rel_error_vs_fp64_solution": err64,
+                       "operator_shape": {"fp64": lib.ax_shape(0)[:2], "fp32": lib.ax_shape(1)[:2],
+                                          "note": "(kind 0 plain / 1 TMA, elements per block), "
+                                                  "autotuned on the first solve"},
                        "l2": "inputs larger than L2", "parallelism": f"replicas{ws}"},
             "fp64": fp64_block,
             "speedup_mixed_vs_fp64": vmx / v64 if v64 > 0 else None,
-            "roofline": {"kernel": "axhelm_kernel<8,float,fused> (inner solve)", "bound": "hbm",
+            "roofline": {"kernel": f"fused fp32 operator lx1={M['lx1']} (inner solve)",
+                         "bound": "hbm",
                          "achieved": ax_gbs, "peak": peak, "unit": "GB/s", "frac": ax_gbs / peak,
                          "peak_source": peak_src, "bytes_per_point": b32,
                          "avg_launch_ms": rmx["ms_ax"], "launches_timed": rmx["n_ax"],
@@ -475,12 +511,64 @@ def run_batch(args):
     B.close()
 
 
+def run_sweep(args):
+    """In-solve fused operator at N = 5, 7, 9 on the E=32^3 Helmholtz box:
+    60 PCG iterations per precision, every operator launch timed with CUDA
+    events; bytes per point are the fused operator's algorithmic 12 words."""
+    import torch
+    ws, rank, local, pg = dist_setup(args.gpus)
+    torch.cuda.set_device(local)
+    from nek5000_gb300 import NekGpu
+    from nek5000_gb300 import build as nb
+    nb.build()
+    peak, peak_src = peaks()
+    rows = []
+    l0 = None
+    for N in (5, 7, 9):
+        M = workload(args.k, N)
+        n = M["n"]
+        lib = NekGpu(local)
+        lib.setup(M["lx1"], M["nel"], M["D"], M["g"], M["bm1"], M["glo_num"])
+        lib.set_option(2, 1)
+        dev = lambda a: torch.tensor(a, device=f"cuda:{local}")
+        a = [dev(M[c]) for c in ("f", "h1", "h2", "mask", "mult")]
+        binv = dev(M["binv"])
+        x = torch.zeros(n, dtype=torch.float64, device=f"cuda:{local}")
+        row = {"N": N, "n_points": n}
+        if l0 is None:
+            l0 = lib.launch_count()
+        for prec, w in ((0, 8), (1, 4)):
+            for rep in range(2):  # the first call also tunes the launch shape
+                if prec == 0:
+                    lib.cggo(x, *a, 1, -1e-30, 60, 1, binv, maxcg=60)
+                else:
+                    lib.cggo_mixed(x, *a, 1, -1e-30, 60, 1, binv)
+            t_tot, t_ax, k_ax = lib.last_timing()
+            ms = t_ax / max(k_ax, 1)
+            gbs = 12 * w * n / (ms * 1e-3) / 1e9
+            row["fp64" if prec == 0 else "fp32"] = {
+                "avg_launch_ms": ms, "launches": k_ax, "GB/s": gbs, "frac": gbs / peak,
+                "shape": lib.ax_shape(prec)[:2]}
+        rows.append(row)
+        lib.close()
+        del a, binv, x, M
+        torch.cuda.empty_cache()
+    if rank == 0:
+        print(json.dumps({"metric": "fused operator HBM GB/s in the PCG, N=5,7,9",
+                          "unit": "GB/s", "peak": peak, "peak_source": peak_src,
+                          "workload": f"helmholtz E={args.k}^3 h1=1 h2=10, 60 iterations",
+                          "bytes_per_point": {"fp64": 96, "fp32": 48},
+                          "sweep": rows}), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "batch":
         run_batch(args)
+    elif args.workload == "axhelm-sweep":
+        run_sweep(args)
     else:
         run_gpu(args)
 

@@ -56,6 +56,10 @@ extern "C" {
                                 copies where lx1 is even; 0: plain loads         */
 #define NEKGPU_OPT_GRAPH 6   /* 1 (default): replay each chunk of PCG iterations
                                 as one captured CUDA graph; 0: direct launches   */
+#define NEKGPU_OPT_AUTOTUNE 8  /* 1 (default): on the first solve of a mesh in
+                                a precision, time the operator's launch shapes
+                                and keep the fastest (nekgpu_autotune); 0: the
+                                built-in shapes.  Setting it forgets the picks. */
 #define NEKGPU_OPT_MIXED_MODE 7  /* mixed solve: 1 (default) one FP32 PCG whose
                                 residual is replaced by the FP64 one each time
                                 it drops by inner_tol, search direction kept;
@@ -239,6 +243,33 @@ int nekgpu_batch_solve_dev(const int64_t *batch, const int *nprob, double *const
                            double *rbn2, int *status);
 int nekgpu_batch_last_error(const int64_t *batch, char *buf, const int *buflen);
 int nekgpu_batch_destroy(int64_t *batch);
+
+/* ---- operator launch shapes (autotuner) ---------------------------------- */
+/* No counterpart in the reference.  The operator's launch shape is the kernel
+ * kind (0: plain-load kernel, 1: TMA-staged FP32 kernel) and the number of
+ * elements each thread block owns.  Every shape gives identical results (the
+ * per-point arithmetic does not depend on the block, and the PCG's partial
+ * sums are per element); only the speed differs.  precision: 0 FP64, 1 FP32
+ * (the mixed solve's inner PCG).
+ * nekgpu_autotune: times every candidate shape of the fused PCG operator on
+ *   this mesh now, for coefficient modes h1mode (0 uniform, 1 per point) and
+ *   h2mode (0 none, 1 uniform, 2 per point), and keeps the fastest; a mesh
+ *   already tuned in this precision, or one of the same kind tuned earlier in
+ *   the process (device, lx1, nel, modes), keeps that pick without timing.
+ *   Call it before a stream capture that contains a solve.
+ * nekgpu_ax_shape: the shape in use (the built-in one while untuned; *ms = 0).
+ * nekgpu_set_ax_shape: pins a shape from nekgpu_ax_candidates (kind -1: back
+ *   to built-in / tuning), e.g. to replay a recorded pick.
+ * nekgpu_ax_candidates: on entry *count = room in kinds/epbs; on return the
+ *   number of candidates. */
+int nekgpu_autotune(const int64_t *handle, const int *precision, const int *h1mode,
+                    const int *h2mode, int *kind, int *epb, double *ms);
+int nekgpu_ax_shape(const int64_t *handle, const int *precision, int *kind, int *epb,
+                    double *ms);
+int nekgpu_set_ax_shape(const int64_t *handle, const int *precision, const int *kind,
+                        const int *epb);
+int nekgpu_ax_candidates(const int64_t *handle, const int *precision, int *kinds, int *epbs,
+                         int *count);
 
 /* ---- timing of the last solve (device time, CUDA events) ----------------- */
 /* ms_total: whole call on the device; ms_axhelm: summed axhelm-kernel time of

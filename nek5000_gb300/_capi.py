@@ -17,6 +17,7 @@ OK = 0
 EINVAL, EHANDLE, ECUDA, ENOMEM, ENOTCONV, ENOSETUP, ENAN = -1, -2, -3, -4, -5, -6, -7
 OPT_EXACT, OPT_TIMING, OPT_CHUNK, OPT_ISTEP, OPT_TMA, OPT_GRAPH, OPT_MIXED_MODE = (
     1, 2, 3, 4, 5, 6, 7)
+OPT_AUTOTUNE = 8
 MAX_LX1 = 12
 NOALLOC_MAX_POINTS = 4194304
 
@@ -55,6 +56,10 @@ SIGNATURES = {
     "nekgpu_set_timing": [_I64P, _IP],
     "nekgpu_last_timing": [_I64P, _DP, _DP, _IP],
     "nekgpu_launch_count": [_I64P],
+    "nekgpu_autotune": [_I64P, _IP, _IP, _IP, _IP, _IP, _DP],
+    "nekgpu_ax_shape": [_I64P, _IP, _IP, _IP, _DP],
+    "nekgpu_set_ax_shape": [_I64P, _IP, _IP, _IP],
+    "nekgpu_ax_candidates": [_I64P, _IP, _P, _P, _IP],
     "nekgpu_cggo_mixed_dev": [_I64P, _P, _P, _P, _P, _P, _P, _IP, _DP, _IP, _IP, _P, _DP, _IP, _IP,
                               _DP, _DP],
     "nekgpu_hmholtz_mixed": [_I64P, _P, _P, _P, _P, _P, _P, _IP, _DP, _IP, _IP, _P, _DP, _IP, _IP,

@@ -21,7 +21,9 @@
 // stage forms p <- r*d + beta*p (col3 + add2s1, :730, :795) and stores it,
 // the operator is applied to the new p, and the element-interior part of
 // rho = sum w*p*mult (glsc3 :801; interior points have mult = 1 and are not
-// touched by dssum/mask) is reduced into one FP64 partial per block.
+// touched by dssum/mask) is reduced into one FP64 partial per element, in an
+// order fixed by the element's own point indices, so that the number of
+// elements a block holds changes the speed and never the result.
 #pragma once
 #include "common.cuh"
 
@@ -44,7 +46,7 @@ struct AxArgs {
   const T* r;
   const T* d;
   const CgScalars* cg;
-  double* partial; // one per block
+  double* partial; // one per element
   int* err;        // device flag: set if a bounded wait expired
   const unsigned char* skip;  // interior points owned by the boundary-group kernel
 };
@@ -55,6 +57,32 @@ struct AxShape {
   static constexpr int LP = NX * NX * R;     // padded element slab
   static constexpr int P = NX * NX * NX;
 };
+
+// Sum of one value per thread (i,j) of an element's slab in a fixed order:
+// each row j summed over i left to right, then the row sums over j.  `buf`
+// holds NX*NX + NX doubles owned by this element; threads with own = false
+// (no element in this block slot) take part in the barriers only.  The sum is
+// stored to *out by thread 0 of the element when out is not null.
+template <int NX>
+__device__ __forceinline__ void element_sum(double v, double* buf, int tx, bool own,
+                                            double* out) {
+  constexpr int NXY = NX * NX;
+  if (own) buf[tx] = v;
+  __syncthreads();
+  if (own && tx < NX) {
+    double s = buf[tx * NX];
+#pragma unroll
+    for (int c = 1; c < NX; ++c) s += buf[tx * NX + c];
+    buf[NXY + tx] = s;
+  }
+  __syncthreads();
+  if (own && tx == 0 && out) {
+    double s = buf[NXY];
+#pragma unroll
+    for (int r = 1; r < NX; ++r) s += buf[NXY + r];
+    *out = s;
+  }
+}
 
 template <int NX, typename T>
 __host__ __device__ constexpr size_t axhelm_smem_bytes(int epb) {
@@ -207,8 +235,11 @@ __device__ __forceinline__ void axhelm_body(const AxArgs<T>& a, int blk, int tx,
     }
   }
   if constexpr (FUSED) {
-    const double bsum = block_sum((double)dot, red);
-    if (tx == 0 && ty == 0) a.partial[blk] = bsum;
+    // The element's u slab (read only before the first barrier) holds the
+    // NX*NX + NX doubles of the sum: NX^2 (NX+1) sizeof(T) >= 8 NX (NX+1).
+    (void)red;
+    element_sum<NX>((double)dot, reinterpret_cast<double*>(su), tid, ty < epb,
+                    act ? a.partial + e : nullptr);
   }
 }
 

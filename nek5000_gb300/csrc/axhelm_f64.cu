@@ -3,21 +3,11 @@
 
 namespace nekgpu {
 
-// Upper bound on the blocks of any operator launch (sizes the rho partials).
+// Number of rho partials of a fused operator launch (one per element, for
+// every launch shape).
 int axhelm_blocks(int nx1, int nel) {
-  int epb = axhelm_epb(nx1);
-  int b = (nel + epb - 1) / epb;
-  int t = 1;
-  switch (nx1) {
-    case 2: t = tma_epb<2>(); break;
-    case 4: t = tma_epb<4>(); break;
-    case 6: t = tma_epb<6>(); break;
-    case 8: t = tma_epb<8>(); break;
-    case 10: t = tma_epb<10>(); break;
-    case 12: t = tma_epb<12>(); break;
-    default: t = epb;
-  }
-  return std::max(b, (nel + t - 1) / t);
+  (void)nx1;
+  return nel;
 }
 
 template cudaError_t launch_axhelm<double, true>(const Mesh&, const OpData<double>&, double*,

@@ -1,51 +1,37 @@
-// axhelm_launch.cuh -- runtime dispatch of axhelm_kernel over lx1.
-// Included by one translation unit per precision so the instantiations
-// compile in parallel.
+// axhelm_launch.cuh -- runtime dispatch of the operator over lx1 and the
+// launch shape (kernel kind, elements per block).  Included by one
+// translation unit per precision so the instantiations compile in parallel;
+// the TMA-staged FP32 kernels live in axhelm_tma.cu.
 #pragma once
-#include "axhelm_tma.cuh"
+#include "axhelm.cuh"
 #include "impl.cuh"
 
 namespace nekgpu {
 
+// TMA-staged FP32 operator (axhelm_tma.cu): lx1 even, 16-byte aligned arrays;
+// epb one of tma_epb_cand<lx1> (0: the built-in count).  Writes one rho
+// partial per element when fused.
+cudaError_t launch_tma_f32(const Mesh& m, const AxArgs<float>& a, bool fused, int epb,
+                           int* nparts, cudaStream_t s);
+
 template <int NX, typename T, bool EXACT, bool FUSED>
-static cudaError_t launch_ax_nx(const Mesh& m, const AxArgs<T>& a, int* nblocks, cudaStream_t s) {
-  const int epb = axhelm_epb(NX);
+static cudaError_t launch_ax_nx(const Mesh& m, const AxArgs<T>& a, int epb, int* nparts,
+                                cudaStream_t s) {
+  if (epb < 1 || epb * NX * NX > 256) epb = axhelm_epb(NX);
   const size_t smem = axhelm_smem_bytes<NX, T>(epb);
-  static bool configured = false;  // per instantiation
+  static bool configured = false;  // per instantiation: room for the largest shape
   if (!configured) {
     cudaError_t e = cudaFuncSetAttribute(axhelm_kernel<NX, T, EXACT, FUSED>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)axhelm_smem_bytes<NX, T>(axhelm_epb(NX)));
     if (e != cudaSuccess) return e;
     configured = true;
   }
   const int nb = (m.nel + epb - 1) / epb;
-  if (nblocks) *nblocks = nb;
+  if (nparts) *nparts = m.nel;
   dim3 block(NX * NX, epb);
   count_launch();
   axhelm_kernel<NX, T, EXACT, FUSED><<<nb, block, smem, s>>>(a);
-  return cudaGetLastError();
-}
-
-// TMA-staged form: even lx1 (so one element's slice is a multiple of 16
-// bytes) and 16-byte aligned arrays.
-template <int NX, typename T, bool FUSED>
-static cudaError_t launch_tma_nx(const Mesh& m, const AxArgs<T>& a, int* nblocks, cudaStream_t s) {
-  constexpr int EPB = tma_epb<NX>();
-  const size_t smem = tma_smem_bytes<NX, T>(FUSED, a.h1mode, a.h2mode);
-  static bool configured = false;
-  if (!configured) {
-    const int maxb = (int)tma_smem_bytes<NX, T>(true, 1, 2);
-    cudaError_t e = cudaFuncSetAttribute(axhelm_tma_kernel<NX, T, FUSED>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, maxb);
-    if (e != cudaSuccess) return e;
-    cudaFuncSetAttribute(axhelm_tma_kernel<NX, T, FUSED>,
-                         cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-    configured = true;
-  }
-  const int nb = (m.nel + EPB - 1) / EPB;
-  if (nblocks) *nblocks = nb;
-  count_launch();
-  axhelm_tma_kernel<NX, T, FUSED><<<nb, dim3(NX * NX, EPB), smem, s>>>(a);
   return cudaGetLastError();
 }
 
@@ -61,33 +47,40 @@ static bool tma_ok(const AxArgs<T>& a) {
   return ok;
 }
 
+// The launch shape in use for precision T: the autotuner's pick once it has
+// run for this mesh, else the built-in one (TMA for FP32 where it applies).
+template <typename T>
+inline AxShapeSel ax_shape(const Mesh& m) {
+  const AxShapeSel& sel = m.ax_sel[sizeof(T) == 4 ? 1 : 0];
+  if (sel.kind >= 0) return sel;
+  AxShapeSel d;
+  d.kind = (sizeof(T) == 4 && m.use_tma && m.nx1 % 2 == 0) ? 1 : 0;
+  d.epb = d.kind ? 0 : axhelm_epb(m.nx1);  // 0: the TMA kernel's built-in count
+  return d;
+}
+
 template <typename T, bool EXACT, bool FUSED>
-static cudaError_t launch_ax(const Mesh& m, const AxArgs<T>& a, int* nblocks, cudaStream_t s) {
-  // FP64 is bound by the FP64 pipe, where the plain-load kernel (D in shared
-  // memory, higher occupancy) is faster; the TMA form serves FP32.
-  if (!EXACT && sizeof(T) == 4 && m.use_tma && tma_ok<T, FUSED>(a)) {
-    switch (m.nx1) {
-      case 2: return launch_tma_nx<2, T, FUSED>(m, a, nblocks, s);
-      case 4: return launch_tma_nx<4, T, FUSED>(m, a, nblocks, s);
-      case 6: return launch_tma_nx<6, T, FUSED>(m, a, nblocks, s);
-      case 8: return launch_tma_nx<8, T, FUSED>(m, a, nblocks, s);
-      case 10: return launch_tma_nx<10, T, FUSED>(m, a, nblocks, s);
-      case 12: return launch_tma_nx<12, T, FUSED>(m, a, nblocks, s);
-      default: break;
-    }
+static cudaError_t launch_ax(const Mesh& m, const AxArgs<T>& a, int* nparts, cudaStream_t s) {
+  const AxShapeSel sh = ax_shape<T>(m);
+  if constexpr (!EXACT && sizeof(T) == 4) {
+    // FP64 is bound by the FP64 pipe, where the plain-load kernel (D in
+    // shared memory, higher occupancy) is faster; the TMA form serves FP32.
+    if (sh.kind == 1 && m.use_tma && m.nx1 % 2 == 0 && tma_ok<T, FUSED>(a))
+      return launch_tma_f32(m, a, FUSED, sh.epb, nparts, s);
   }
+  const int epb = sh.kind == 0 ? sh.epb : axhelm_epb(m.nx1);
   switch (m.nx1) {
-    case 2: return launch_ax_nx<2, T, EXACT, FUSED>(m, a, nblocks, s);
-    case 3: return launch_ax_nx<3, T, EXACT, FUSED>(m, a, nblocks, s);
-    case 4: return launch_ax_nx<4, T, EXACT, FUSED>(m, a, nblocks, s);
-    case 5: return launch_ax_nx<5, T, EXACT, FUSED>(m, a, nblocks, s);
-    case 6: return launch_ax_nx<6, T, EXACT, FUSED>(m, a, nblocks, s);
-    case 7: return launch_ax_nx<7, T, EXACT, FUSED>(m, a, nblocks, s);
-    case 8: return launch_ax_nx<8, T, EXACT, FUSED>(m, a, nblocks, s);
-    case 9: return launch_ax_nx<9, T, EXACT, FUSED>(m, a, nblocks, s);
-    case 10: return launch_ax_nx<10, T, EXACT, FUSED>(m, a, nblocks, s);
-    case 11: return launch_ax_nx<11, T, EXACT, FUSED>(m, a, nblocks, s);
-    case 12: return launch_ax_nx<12, T, EXACT, FUSED>(m, a, nblocks, s);
+    case 2: return launch_ax_nx<2, T, EXACT, FUSED>(m, a, epb, nparts, s);
+    case 3: return launch_ax_nx<3, T, EXACT, FUSED>(m, a, epb, nparts, s);
+    case 4: return launch_ax_nx<4, T, EXACT, FUSED>(m, a, epb, nparts, s);
+    case 5: return launch_ax_nx<5, T, EXACT, FUSED>(m, a, epb, nparts, s);
+    case 6: return launch_ax_nx<6, T, EXACT, FUSED>(m, a, epb, nparts, s);
+    case 7: return launch_ax_nx<7, T, EXACT, FUSED>(m, a, epb, nparts, s);
+    case 8: return launch_ax_nx<8, T, EXACT, FUSED>(m, a, epb, nparts, s);
+    case 9: return launch_ax_nx<9, T, EXACT, FUSED>(m, a, epb, nparts, s);
+    case 10: return launch_ax_nx<10, T, EXACT, FUSED>(m, a, epb, nparts, s);
+    case 11: return launch_ax_nx<11, T, EXACT, FUSED>(m, a, epb, nparts, s);
+    case 12: return launch_ax_nx<12, T, EXACT, FUSED>(m, a, epb, nparts, s);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -123,14 +116,14 @@ cudaError_t launch_axhelm(const Mesh& m, const OpData<T>& op, T* au, const T* u,
 template <typename T, bool EXACT>
 cudaError_t launch_axhelm_cg(const Mesh& m, const OpData<T>& op, T* w, T* p, const T* r,
                              const T* d, const Coef<T>& c, const CgScalars* cg, double* partial,
-                             int* nblocks, cudaStream_t s) {
+                             int* nparts, cudaStream_t s) {
   AxArgs<T> a = make_args(m, op, w, p, c);
   a.p = p;
   a.r = r;
   a.d = d;
   a.cg = cg;
   a.partial = partial;
-  return launch_ax<T, EXACT, true>(m, a, nblocks, s);
+  return launch_ax<T, EXACT, true>(m, a, nparts, s);
 }
 
 }  // namespace nekgpu

@@ -3,7 +3,8 @@
 // Same mathematics and contraction order as axhelm.cuh (core/hmholtz.f:72-259,
 // 3-D deformed path), organised for HBM bandwidth:
 //
-//  * one block owns EPB consecutive elements; since every array is
+//  * one block owns EPB consecutive elements (a compile-time shape the
+//    autotuner picks from tma_epb_cand); since every array is
 //    element-major, their u (or p, r, d), G, bm1 and coefficient slices are
 //    each one contiguous range, staged into shared memory by a handful of
 //    1-D bulk asynchronous copies (cp.async.bulk) completing on one mbarrier
@@ -21,9 +22,17 @@
 
 namespace nekgpu {
 
+// Built-in elements per block: about 128 threads, at least one element.
 template <int NX>
 __host__ __device__ constexpr int tma_epb() {
   return (128 / (NX * NX)) > 0 ? (128 / (NX * NX)) : 1;
+}
+
+// Shapes the autotuner may pick: half, once and twice the built-in count.
+template <int NX>
+__host__ __device__ constexpr int tma_epb_cand(int q) {
+  return q == 0 ? (tma_epb<NX>() / 2 > 0 ? tma_epb<NX>() / 2 : 1)
+                : (q == 1 ? tma_epb<NX>() : 2 * tma_epb<NX>());
 }
 
 // Number of staged field slices (of EPB*P values) besides G and the work slabs.
@@ -33,11 +42,11 @@ __host__ __device__ constexpr int tma_nslices(bool fused, int h1mode, int h2mode
 
 // The fused form reuses the r and d slices (consumed by the p update) as the
 // two work slabs; the plain form needs two more.
-template <int NX, typename T>
+template <int NX, typename T, int EPB>
 __host__ __device__ constexpr size_t tma_smem_bytes(bool fused, int h1mode, int h2mode) {
   constexpr int P = NX * NX * NX;
   return 64 /* mbarrier + pad */ + (size_t)NX * NX * sizeof(T) /* D */ +
-         (size_t)tma_epb<NX>() * P * sizeof(T) *
+         (size_t)EPB * P * sizeof(T) *
              (tma_nslices(fused, h1mode, h2mode) + 6 + (fused ? 0 : 2));
 }
 
@@ -74,26 +83,10 @@ __device__ __forceinline__ void load_row(const T* __restrict__ p, T (&v)[NX]) {
   }
 }
 
-// Block sum of a per-thread value: warp sums in T, one FP64 value per warp.
-template <typename T>
-__device__ __forceinline__ double block_sum_warps(T v, double* scratch) {
-  v = warp_sum(v);
-  const int tid = threadIdx.x + blockDim.x * threadIdx.y;
-  const int nw = (blockDim.x * blockDim.y + 31) >> 5;
-  if ((tid & 31) == 0) scratch[tid >> 5] = (double)v;
-  __syncthreads();
-  double s = 0.0;
-  if (tid == 0)
-    for (int q = 0; q < nw; ++q) s += scratch[q];
-  return s;  // valid in thread 0
-}
-
-template <int NX, typename T, bool FUSED>
-__global__ void __launch_bounds__(NX* NX* tma_epb<NX>())
-    axhelm_tma_kernel(const AxArgs<T> a) {
-  constexpr int P = NX * NX * NX, NXY = NX * NX, EPB = tma_epb<NX>();
+template <int NX, typename T, bool FUSED, int EPB>
+__global__ void __launch_bounds__(NX* NX* EPB) axhelm_tma_kernel(const AxArgs<T> a) {
+  constexpr int P = NX * NX * NX, NXY = NX * NX;
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  __shared__ double red[32];
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
   T* sD = reinterpret_cast<T*>(smem_raw + 64);  // D[i][l] row-major
   // staged slices, each EPB*P values, 16-byte aligned (P*sizeof(T) % 16 == 0)
@@ -236,8 +229,11 @@ __global__ void __launch_bounds__(NX* NX* tma_epb<NX>())
     }
   }
   if constexpr (FUSED) {
-    const double bsum = block_sum_warps(dot, red);
-    if (tid == 0) a.partial[blockIdx.x] = bsum;
+    // one partial per element, summed as axhelm.cuh's kernel does; the
+    // element's staged G (read only before the second barrier) holds the
+    // NX*NX + NX doubles: 6 NX^3 sizeof(T) >= 8 NX (NX+1)
+    element_sum<NX>((double)dot, reinterpret_cast<double*>(sG + 6 * lo), threadIdx.x, true,
+                    el < ne ? a.partial + e0 + el : nullptr);
   }
   if (tid == 0 && ok) mbar_inval(bar);
 }

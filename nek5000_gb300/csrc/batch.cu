@@ -29,7 +29,7 @@ namespace nekgpu {
 template <typename T>
 struct BDesc {
   AxArgs<T> ax;  // fused operator: au = w, u = p (old), p, r, d, cg, partial = rho partials
-  int nx1, epb, nblkA;
+  int nx1, epb, nblkA;  // operator blocks; the rho partials are one per element (ax.nel)
   const int* bstart;
   const int* bidx;
   GsClasses cls;
@@ -93,7 +93,7 @@ __global__ void __launch_bounds__(kGsThreads)
   const BDesc<T>* d = D + pi;
   if (d->cg->done) return;
   gs_cg_body<T>(d->ax.au, d->ax.p, d->bstart, d->bidx, d->cls, d->segmask, d->segmsum, d->cg,
-                d->ax.partial, d->nblkA, d->partialB, blockIdx.x - base[pi], d->nblkB, red,
+                d->ax.partial, d->ax.nel, d->partialB, blockIdx.x - base[pi], d->nblkB, red,
                 &am_last);
 }
 
@@ -598,6 +598,7 @@ int nekgpu_batch_add(const int64_t* batch, const int* lx1, const int* nel, const
     return bfail(B, NEKGPU_EINVAL, "null argument");
   cudaSetDevice(B->device);
   auto H = std::make_unique<nekgpu::Handle>();
+  H->autotune = false;  // the batched operator launches its own shape
   std::string err;
   if (nekgpu::handle_open(*H, B->device, B->stream, err)) return bfail(B, NEKGPU_ECUDA, err);
   const double* g[6] = {g1, g2, g3, g4, g5, g6};

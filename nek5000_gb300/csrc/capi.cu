@@ -261,6 +261,7 @@ int handle_setup(Handle& H, int lx1, int nel, const double* dxm1, const double* 
   m.f64.release();
   m.f32.release();
   m.has_f32 = false;
+  m.ax_sel[0] = m.ax_sel[1] = AxShapeSel();
   H.has_mesh = false;
   if (H.gexec) cudaGraphExecDestroy(H.gexec);
   H.gexec = nullptr;
@@ -377,7 +378,14 @@ int nekgpu_set_option(const int64_t* handle, const int* key, const int* value) {
       H->graph_chunk = *value;
       break;
     case NEKGPU_OPT_ISTEP: H->istep = *value; break;
-    case NEKGPU_OPT_TMA: H->mesh.use_tma = (*value != 0); break;
+    case NEKGPU_OPT_TMA:
+      H->mesh.use_tma = (*value != 0);
+      H->mesh.ax_sel[1] = AxShapeSel();  // FP32 shape: tuned again (or built-in)
+      break;
+    case NEKGPU_OPT_AUTOTUNE:
+      H->autotune = (*value != 0);
+      H->mesh.ax_sel[0] = H->mesh.ax_sel[1] = AxShapeSel();
+      break;
     case NEKGPU_OPT_GRAPH: H->use_graph = (*value != 0); break;
     case NEKGPU_OPT_MIXED_MODE:
       if (*value != 0 && *value != 1) return fail(H, NEKGPU_EINVAL, "mixed mode must be 0 or 1");
@@ -729,6 +737,107 @@ int nekgpu_cggo_adjoint_dev(const int64_t* handle, double* lam, const double* g,
   // The Helmholtz operator is symmetric, so the adjoint solve is cggo itself.
   return nekgpu_cggo_dev(handle, lam, g, h1, h2, mask, mult, imsh, tin, maxit, isd, binv, maxcg,
                          niter, rbn0, rbn2);
+}
+
+// ---- operator launch shapes (autotuner) -------------------------------------
+int nekgpu_autotune(const int64_t* handle, const int* precision, const int* h1mode,
+                    const int* h2mode, int* kind, int* epb, double* ms) {
+  GET_HANDLE(handle);
+  NEED_MESH();
+  if (!precision || !h1mode || !h2mode) return fail(H, NEKGPU_EINVAL, "null argument");
+  const int prec = *precision;
+  if (prec != 0 && prec != 1) return fail(H, NEKGPU_EINVAL, "precision must be 0 or 1");
+  if (*h1mode < 0 || *h1mode > 1 || *h2mode < 0 || *h2mode > 2)
+    return fail(H, NEKGPU_EINVAL, "h1mode must be 0..1 and h2mode 0..2");
+  const int64_t n = H->mesh.n;
+  const bool was = H->autotune;
+  H->autotune = true;
+  int rc = 0;
+  if (prec == 0) {
+    PcgWork<double>& wk = H->w64;
+    if (wk.h1.ensure(n) || wk.h2.ensure(n)) rc = NEKGPU_ENOMEM;
+    if (!rc) {
+      Coef<double> c;
+      c.h1mode = *h1mode;
+      c.h2mode = *h2mode;
+      c.h2s = *h2mode == 1 ? 1.0 : 0.0;
+      c.h1 = wk.h1.ptr;
+      c.h2 = wk.h2.ptr;
+      cudaMemsetAsync(wk.h1.ptr, 0, n * sizeof(double), H->stream);
+      cudaMemsetAsync(wk.h2.ptr, 0, n * sizeof(double), H->stream);
+      rc = tune_operator<double>(*H, H->mesh.f64, wk, c);
+    }
+  } else {
+    PcgWork<float>& wk = H->w32;
+    rc = ensure_f32(*H);
+    if (!rc && (wk.h1.ensure(n) || wk.h2.ensure(n))) rc = NEKGPU_ENOMEM;
+    if (!rc) {
+      Coef<float> c;
+      c.h1mode = *h1mode;
+      c.h2mode = *h2mode;
+      c.h2s = *h2mode == 1 ? 1.f : 0.f;
+      c.h1 = wk.h1.ptr;
+      c.h2 = wk.h2.ptr;
+      cudaMemsetAsync(wk.h1.ptr, 0, n * sizeof(float), H->stream);
+      cudaMemsetAsync(wk.h2.ptr, 0, n * sizeof(float), H->stream);
+      rc = tune_operator<float>(*H, H->mesh.f32, wk, c);
+    }
+  }
+  H->autotune = was;
+  if (rc) return fail(H, rc, H->err.empty() ? "autotune failed" : H->err);
+  const AxShapeSel sh = ax_shape_in_use(H->mesh, prec);
+  if (kind) *kind = sh.kind;
+  if (epb) *epb = sh.epb;
+  if (ms) *ms = sh.ms;
+  return NEKGPU_OK;
+}
+
+int nekgpu_ax_shape(const int64_t* handle, const int* precision, int* kind, int* epb,
+                    double* ms) {
+  GET_HANDLE(handle);
+  NEED_MESH();
+  if (!precision || (*precision != 0 && *precision != 1))
+    return fail(H, NEKGPU_EINVAL, "precision must be 0 or 1");
+  const AxShapeSel sh = ax_shape_in_use(H->mesh, *precision);
+  if (kind) *kind = sh.kind;
+  if (epb) *epb = sh.epb;
+  if (ms) *ms = H->mesh.ax_sel[*precision].kind >= 0 ? sh.ms : 0.0;
+  return NEKGPU_OK;
+}
+
+int nekgpu_set_ax_shape(const int64_t* handle, const int* precision, const int* kind,
+                        const int* epb) {
+  GET_HANDLE(handle);
+  NEED_MESH();
+  if (!precision || !kind || !epb) return fail(H, NEKGPU_EINVAL, "null argument");
+  const int prec = *precision;
+  if (prec != 0 && prec != 1) return fail(H, NEKGPU_EINVAL, "precision must be 0 or 1");
+  if (*kind == -1) {  // back to the built-in shape / tuning
+    H->mesh.ax_sel[prec] = AxShapeSel();
+    return NEKGPU_OK;
+  }
+  for (const AxShapeSel& c : ax_candidates(H->mesh.nx1, prec, H->mesh.use_tma))
+    if (c.kind == *kind && c.epb == *epb) {
+      H->mesh.ax_sel[prec] = c;
+      return NEKGPU_OK;
+    }
+  return fail(H, NEKGPU_EINVAL, "not a launch shape of this mesh (nekgpu_ax_candidates)");
+}
+
+int nekgpu_ax_candidates(const int64_t* handle, const int* precision, int* kinds, int* epbs,
+                         int* count) {
+  GET_HANDLE(handle);
+  NEED_MESH();
+  if (!precision || !count || (*precision != 0 && *precision != 1))
+    return fail(H, NEKGPU_EINVAL, "bad argument");
+  const std::vector<AxShapeSel> v = ax_candidates(H->mesh.nx1, *precision, H->mesh.use_tma);
+  const int cap = *count;
+  *count = (int)v.size();
+  for (int q = 0; q < (int)v.size() && q < cap; ++q) {
+    if (kinds) kinds[q] = v[q].kind;
+    if (epbs) epbs[q] = v[q].epb;
+  }
+  return NEKGPU_OK;
 }
 
 int nekgpu_launch_count(int64_t* count) {

@@ -46,6 +46,17 @@ struct OpData {
   }
 };
 
+// Launch shape of the operator in one precision: kind 0 is axhelm_kernel
+// (axhelm.cuh) with `epb` elements per block, kind 1 the TMA-staged FP32
+// kernel (axhelm_tma.cuh) with `epb` elements per block (0: its built-in
+// count); kind -1 means "not tuned: built-in shape".  `ms` is the tuned
+// launch time.  Every shape gives the same results (per-element partials).
+struct AxShapeSel {
+  int kind = -1;
+  int epb = 0;
+  float ms = 0.f;
+};
+
 struct Mesh {
   int nx1 = 0, nel = 0;
   int64_t n = 0;
@@ -57,6 +68,7 @@ struct Mesh {
   int* dev_err = nullptr;  // device flag raised by a kernel whose bounded wait expired
   bool use_tma = true;     // TMA-staged operator where lx1 and alignment allow
   std::vector<double> h_D;  // lx1*lx1 row-major (host copy)
+  AxShapeSel ax_sel[2];     // [0] FP64, [1] FP32 (see tune.cu)
 };
 
 // Coefficient descriptor after uniformity detection.
@@ -116,6 +128,8 @@ struct Handle {
   bool own_stream = true;
   bool use_graph = true;
   int mixed_mode = 1;  // see mixed_solve
+  bool autotune = true;  // time the operator's launch shapes on first solve (tune.cu)
+  DevBuf<CgScalars> cg_tune;  // scalars of the tuning launches (beta = 0, not done)
 };
 
 // ---- operator entry points (axhelm_*.cu) ---------------------------------
@@ -129,6 +143,18 @@ cudaError_t launch_axhelm_cg(const Mesh& m, const OpData<T>& op, T* w, T* p, con
                              const T* d, const Coef<T>& c, const CgScalars* cg, double* partial,
                              int* nblocks, cudaStream_t s);
 int axhelm_blocks(int nx1, int nel);
+// Autotuner (tune.cu): times the fused operator's candidate launch shapes on
+// this mesh (work vectors r, p, w of `wk` as scratch, zeroed) and keeps the
+// fastest in mesh.ax_sel; a process-wide cache keyed by device, lx1, nel and
+// coefficient modes makes later meshes of the same kind reuse the pick.
+// Returns 0 or a negative status.  Must not run inside a stream capture.
+template <typename T>
+int tune_operator(Handle& h, const OpData<T>& op, PcgWork<T>& wk, const Coef<T>& c);
+// Candidate shapes for lx1 = nx and precision prec (0 FP64, 1 FP32).
+std::vector<AxShapeSel> ax_candidates(int nx, int prec, bool tma);
+// The shape a launch in precision prec uses now (the built-in one, with its
+// elements per block filled in, while the mesh is untuned).
+AxShapeSel ax_shape_in_use(const Mesh& m, int prec);
 // gh1_p = d(lam^T A(h1) u)/d h1_p for every local point (adjoint.cu).
 cudaError_t axhelm_adjoint_h1(const Mesh& m, double* gh1, const double* lam, const double* u,
                               cudaStream_t s);

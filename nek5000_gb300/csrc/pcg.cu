@@ -397,6 +397,18 @@ PcgResult pcg_prepare(Handle& h, PcgWork<T>& wk, T* x, const T* f, const Coef<T>
     set_error(h, "pcg: device allocation failed");
     return res;
   }
+  // launch shape of the fused operator (first solve of this mesh; r, p, w are
+  // scratch until they are set below)
+  {
+    const OpData<T>* op;
+    if constexpr (std::is_same<T, double>::value) op = &m.f64;
+    else op = &m.f32;
+    const int st = tune_operator<T>(h, *op, wk, c);
+    if (st) {
+      res.status = st;
+      return res;
+    }
+  }
   // fmax = glamax(f): an all-zero rhs returns x = 0 at once (hmholtz.f:699-701)
   if (cuda_pending(h, "pcg: before the solve")) {
     res.status = -3;
@@ -562,7 +574,8 @@ PcgResult pcg_iterate(Handle& h, const OpData<T>& op, PcgWork<T>& wk, T* x, cons
     key.ints[0] = (int)sizeof(T);
     key.ints[1] = c.h1mode;
     key.ints[2] = c.h2mode;
-    key.ints[3] = (int)exact + 4 * (int)m.use_tma;
+    const AxShapeSel& sh = m.ax_sel[sizeof(T) == 4 ? 1 : 0];
+    key.ints[3] = (int)exact + 4 * (int)m.use_tma + 8 * (sh.kind + 1) + 32 * sh.epb;
     key.ints[4] = chunk;
     key.ints[5] = m.nel;
     key.dbl[0] = (double)c.h1s;

@@ -93,6 +93,35 @@ class NekGpu:
         self._L.nekgpu_launch_count(C.byref(c))
         return c.value
 
+    # ---- operator launch shapes ---------------------------------------------
+    def autotune(self, precision: int = 0, h1mode: int = 0, h2mode: int = 1):
+        """Time the operator's launch shapes now; returns (kind, epb, ms)."""
+        k, e, ms = _cint(0), _cint(0), _cdouble(0)
+        self._check(self._L.nekgpu_autotune(C.byref(self._h), C.byref(_cint(precision)),
+                                            C.byref(_cint(h1mode)), C.byref(_cint(h2mode)),
+                                            C.byref(k), C.byref(e), C.byref(ms)))
+        return k.value, e.value, ms.value
+
+    def ax_shape(self, precision: int = 0):
+        """Launch shape in use: (kind, elements per block, tuned ms or 0)."""
+        k, e, ms = _cint(0), _cint(0), _cdouble(0)
+        self._check(self._L.nekgpu_ax_shape(C.byref(self._h), C.byref(_cint(precision)),
+                                            C.byref(k), C.byref(e), C.byref(ms)))
+        return k.value, e.value, ms.value
+
+    def set_ax_shape(self, precision: int, kind: int, epb: int = 0):
+        self._check(self._L.nekgpu_set_ax_shape(C.byref(self._h), C.byref(_cint(precision)),
+                                                C.byref(_cint(kind)), C.byref(_cint(epb))))
+
+    def ax_candidates(self, precision: int = 0):
+        """Candidate launch shapes [(kind, epb), ...] of this mesh."""
+        cnt = _cint(64)
+        kinds = (C.c_int * 64)()
+        epbs = (C.c_int * 64)()
+        self._check(self._L.nekgpu_ax_candidates(C.byref(self._h), C.byref(_cint(precision)),
+                                                 kinds, epbs, C.byref(cnt)))
+        return [(kinds[q], epbs[q]) for q in range(min(cnt.value, 64))]
+
     # ---- mesh -------------------------------------------------------------
     def setup(self, lx1: int, nel: int, D, g, bm1, glo_num):
         """D: (lx1,lx1) numpy with D[i,j] = dl_j/dr(z_i) (the reference's dxm1);
