@@ -71,8 +71,8 @@ def parse():
             args.k = 24
         if args.N == 7:
             args.N = 9
-    if args.inner_tol is None:  # the library's defaults; the batch solve restarts per outer step
-        args.inner_tol = 1e-2 if (args.mixed_mode == 1 and args.workload != "batch") else 1e-4
+    if args.inner_tol is None:  # the library's defaults for the mode
+        args.inner_tol = 1e-2 if args.mixed_mode == 1 else 1e-5
     return args
 
 
@@ -466,7 +466,9 @@ def run_batch(args):
 
     def solve(mixed):
         return B.solve(xs, cols["f"], cols["h1"], cols["h2"], cols["mask"], cols["mult"],
-                       cols["binv"], tin=-args.tol, mixed=mixed, inner_tol=args.inner_tol)
+                       cols["binv"], tin=-args.tol,
+                       mixed=(1 if args.mixed_mode == 1 else 2) if mixed else 0,
+                       inner_tol=args.inner_tol)
 
     out = {}
     for mixed in (False, True):
@@ -501,6 +503,12 @@ def run_batch(args):
                        "fp64_iterations": out[False]["res"]["niter"],
                        "mixed_inner_iterations": out[True]["res"]["niter"],
                        "mixed_outer_steps": out[True]["res"]["nouter"],
+                       "solver": "mixed: fp32 jacobi-pcg (inner tol "
+                                 f"{args.inner_tol:g}) in fp64 defect correction, " +
+                                 ("fp64 residual replacement, search direction kept"
+                                  if args.mixed_mode == 1 else "restarted per outer step"),
+                       "operator_block_threads": {"fp64": B.shape(0)[0], "fp32": B.shape(1)[0],
+                                                  "note": "autotuned on the first solve"},
                        "parallelism": f"replicas{ws}"},
             "fp64": {"value": v64, "unit": "DOF-iters/s",
                      "ms_per_step": 1e3 * out[False]["T"] / args.steps},

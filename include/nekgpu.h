@@ -229,8 +229,10 @@ int nekgpu_batch_add(const int64_t *batch, const int *lx1, const int *nel, const
                      const int64_t *glo_num, int *index);
 /* Solve all problems (device arrays, one pointer per problem, in slot order).
  * Per problem: the same inputs and stopping rule as nekgpu_cggo_dev (tin < 0
- * relative; no 900 cap: *maxit iterations at most).  *mixed != 0 selects the
- * FP32-inner / FP64-defect-correction form (inner tolerance *inner_tol).
+ * relative; no 900 cap: *maxit iterations at most).  *mixed selects the
+ * FP32-inner / FP64-defect-correction form: 1 with residual replacement into
+ * each problem's running FP32 PCG (default *inner_tol 1e-2 when NULL), 2
+ * restarted per outer step (default *inner_tol 1e-5); 0 is plain FP64.
  * Outputs per problem: niter (PCG iterations; total inner iterations when
  * mixed), nouter (outer steps, mixed only; may be NULL), rbn0, rbn2 and a
  * status code (0, NEKGPU_ENOTCONV, NEKGPU_ENAN, ...). */
@@ -241,6 +243,15 @@ int nekgpu_batch_solve_dev(const int64_t *batch, const int *nprob, double *const
                            const double *tin, const int *maxit, const int *mixed,
                            const double *inner_tol, int *niter, int *nouter, double *rbn0,
                            double *rbn2, int *status);
+/* Operator block size of the batched solve in precision 0 (FP64) or 1 (FP32):
+ * picked by timing 128- and 256-thread blocks on the first solve of a problem
+ * set (every size gives identical results), or pinned with
+ * nekgpu_batch_set_shape (*threads 128 or 256; 0 returns to tuning).
+ * *threads = 0 before the first solve; *ms is the tuned launch time.  No
+ * reference counterpart.  A 128-thread block is a candidate only when every
+ * problem's lx1^2 <= 128. */
+int nekgpu_batch_shape(const int64_t *batch, const int *precision, int *threads, double *ms);
+int nekgpu_batch_set_shape(const int64_t *batch, const int *precision, const int *threads);
 int nekgpu_batch_last_error(const int64_t *batch, char *buf, const int *buflen);
 int nekgpu_batch_destroy(int64_t *batch);
 

@@ -57,6 +57,8 @@ SIGNATURES = {
     "nekgpu_last_timing": [_I64P, _DP, _DP, _IP],
     "nekgpu_launch_count": [_I64P],
     "nekgpu_autotune": [_I64P, _IP, _IP, _IP, _IP, _IP, _DP],
+    "nekgpu_batch_shape": [_I64P, _IP, _IP, _DP],
+    "nekgpu_batch_set_shape": [_I64P, _IP, _IP],
     "nekgpu_ax_shape": [_I64P, _IP, _IP, _IP, _DP],
     "nekgpu_set_ax_shape": [_I64P, _IP, _IP, _IP],
     "nekgpu_ax_candidates": [_I64P, _IP, _P, _P, _IP],

@@ -117,26 +117,34 @@ __global__ void __launch_bounds__(kBatchThreads)
                                            blk, d->nblkC, red, &am_last);
 }
 
-template <int NX, typename T>
-constexpr size_t ax_smem() {
-  return axhelm_smem_bytes<NX, T>(axhelm_epb(NX));
+// Shared memory of one operator block: epb elements of lx1 = nx.
+template <typename T>
+size_t batch_smem(int nx, int epb) {
+  switch (nx) {
+    case 2: return axhelm_smem_bytes<2, T>(epb);
+    case 3: return axhelm_smem_bytes<3, T>(epb);
+    case 4: return axhelm_smem_bytes<4, T>(epb);
+    case 5: return axhelm_smem_bytes<5, T>(epb);
+    case 6: return axhelm_smem_bytes<6, T>(epb);
+    case 7: return axhelm_smem_bytes<7, T>(epb);
+    case 8: return axhelm_smem_bytes<8, T>(epb);
+    case 9: return axhelm_smem_bytes<9, T>(epb);
+    case 10: return axhelm_smem_bytes<10, T>(epb);
+    case 11: return axhelm_smem_bytes<11, T>(epb);
+    default: return axhelm_smem_bytes<12, T>(epb);
+  }
 }
 
+// Elements per operator block of lx1 = nx in a block of `threads` threads.
+inline int batch_epb(int nx, int threads) { return std::max(1, threads / (nx * nx)); }
+
+// Largest operator-block shared memory over every lx1 at up to kBatchThreads.
 template <typename T>
-size_t batch_smem(int nx) {
-  switch (nx) {
-    case 2: return ax_smem<2, T>();
-    case 3: return ax_smem<3, T>();
-    case 4: return ax_smem<4, T>();
-    case 5: return ax_smem<5, T>();
-    case 6: return ax_smem<6, T>();
-    case 7: return ax_smem<7, T>();
-    case 8: return ax_smem<8, T>();
-    case 9: return ax_smem<9, T>();
-    case 10: return ax_smem<10, T>();
-    case 11: return ax_smem<11, T>();
-    default: return ax_smem<12, T>();
-  }
+size_t batch_smem_max() {
+  size_t b = 0;
+  for (int nx = 2; nx <= NEKGPU_MAX_LX1; ++nx)
+    b = std::max(b, batch_smem<T>(nx, batch_epb(nx, kBatchThreads)));
+  return b;
 }
 
 }  // namespace
@@ -155,12 +163,19 @@ struct Batch {
   std::vector<int64_t> gkey;
   int chunk = 16;
   bool use_graph = true;
+  // operator block size per precision ([0] FP64, [1] FP32): picked by
+  // batch_tune for the problem set in tkey, or pinned (pinned[prec] != 0)
+  int threads[2] = {0, 0};
+  int pinned[2] = {0, 0};
+  std::vector<int64_t> tkey[2];
+  float tune_ms[2] = {0.f, 0.f};
 };
 
 namespace {
 
 struct BatchLaunch {
   int gridA = 0, gridB = 0, gridC = 0;
+  int threadsA = kBatchThreads;  // operator block size
   size_t smem = 0;
   const void* desc = nullptr;
   const int *mapA, *mapB, *mapC, *baseA, *baseB, *baseC;
@@ -170,7 +185,9 @@ struct BatchLaunch {
 template <typename T>
 int batch_tables(Batch& B, const std::vector<int>& ids, const std::vector<Coef<T>>& coef,
                  const std::vector<T*>& xs, const std::vector<const T*>& mults,
-                 const std::vector<const T*>& binvs, BatchLaunch& L) {
+                 const std::vector<const T*>& binvs, BatchLaunch& L, int threads = 0) {
+  if (threads <= 0) threads = B.threads[sizeof(T) == 4 ? 1 : 0];
+  if (threads <= 0) threads = kBatchThreads;
   const int np = (int)ids.size();
   std::vector<BDesc<T>> hd(np);
   std::vector<int> mapA, mapB, mapC, baseA(np), baseB(np), baseC(np);
@@ -209,7 +226,7 @@ int batch_tables(Batch& B, const std::vector<int>& ids, const std::vector<Coef<T
     a.err = m.dev_err;
     a.skip = m.gs.skip;
     d.nx1 = m.nx1;
-    d.epb = axhelm_epb(m.nx1);
+    d.epb = batch_epb(m.nx1, threads);
     d.nblkA = (m.nel + d.epb - 1) / d.epb;
     d.bstart = m.gs.bstart;
     d.bidx = m.gs.bidx;
@@ -228,7 +245,7 @@ int batch_tables(Batch& B, const std::vector<int>& ids, const std::vector<Coef<T
     d.vec = al(d.x) && al(wk.r.ptr) && al(wk.p.ptr) && al(wk.w.ptr) && al(wk.d.ptr) &&
             al(d.mult) && al(d.binv);
     d.cg = h.cg;
-    smem = std::max(smem, batch_smem<T>(m.nx1));
+    smem = std::max(smem, batch_smem<T>(m.nx1, d.epb));
     baseA[q] = (int)mapA.size();
     mapA.insert(mapA.end(), d.nblkA, q);
     baseB[q] = (int)mapB.size();
@@ -257,6 +274,7 @@ int batch_tables(Batch& B, const std::vector<int>& ids, const std::vector<Coef<T
   L.gridB = (int)mapB.size();
   L.gridC = (int)mapC.size();
   L.smem = smem;
+  L.threadsA = threads;
   L.desc = B.desc.ptr;
   L.mapA = B.map.ptr;
   L.mapB = B.map.ptr + mapA.size();
@@ -273,14 +291,14 @@ cudaError_t batch_enqueue(Batch& B, const BatchLaunch& L, int k) {
   if (!configured) {
     cudaError_t e = cudaFuncSetAttribute(batch_axhelm_kernel<T>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)batch_smem<T>(11) + 4096);
+                                         (int)batch_smem_max<T>());
     if (e != cudaSuccess) return e;
     configured = true;
   }
   const BDesc<T>* D = reinterpret_cast<const BDesc<T>*>(L.desc);
   for (int q = 0; q < k; ++q) {
     count_launch(3);
-    batch_axhelm_kernel<T><<<L.gridA, kBatchThreads, L.smem, B.stream>>>(D, L.mapA, L.baseA);
+    batch_axhelm_kernel<T><<<L.gridA, L.threadsA, L.smem, B.stream>>>(D, L.mapA, L.baseA);
     batch_gs_kernel<T><<<L.gridB, kGsThreads, 0, B.stream>>>(D, L.mapB, L.baseB);
     batch_update_kernel<T, false><<<L.gridC, kBatchThreads, 0, B.stream>>>(D, L.mapC, L.baseC);
   }
@@ -288,14 +306,96 @@ cudaError_t batch_enqueue(Batch& B, const BatchLaunch& L, int k) {
 }
 
 // Runs the batched PCG for the listed problems until each has stopped.
+// Picks the operator block size for a problem set: times a batched operator
+// launch for every candidate (128 or 256 threads; 128 only when every
+// element slab fits) and keeps the fastest, once per problem set and
+// precision.  Runs on freshly prepared problems only (beta = 0, p = 0), where
+// the launches it times change nothing the first iteration reads.  Every
+// size gives the same results (per-element rho partials).
 template <typename T>
-int batch_iterate(Batch& B, const std::vector<int>& ids, const BatchLaunch& L) {
+int batch_tune(Batch& B, const std::vector<int>& ids, const std::vector<Coef<T>>& coef,
+               const std::vector<T*>& xs, const std::vector<const T*>& mults,
+               const std::vector<const T*>& binvs) {
+  const int prec = sizeof(T) == 4 ? 1 : 0;
+  if (B.pinned[prec]) {
+    B.threads[prec] = B.pinned[prec];
+    return 0;
+  }
+  std::vector<int64_t> key;
+  int maxnxy = 0;
+  for (size_t q = 0; q < ids.size(); ++q) {
+    const Mesh& m = B.probs[ids[q]]->mesh;
+    key.push_back(m.nx1);
+    key.push_back(m.nel);
+    key.push_back(coef[q].h1mode * 4 + coef[q].h2mode);
+    maxnxy = std::max(maxnxy, m.nx1 * m.nx1);
+  }
+  if (B.threads[prec] && key == B.tkey[prec]) return 0;
+  std::vector<int> cand;
+  for (int t : {128, 256})
+    if (t >= maxnxy) cand.push_back(t);
+  int best = kBatchThreads;
+  float best_ms = 0.f;
+  if (cand.size() > 1) {
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return -3;
+    best_ms = 1e30f;
+    for (int t : cand) {
+      BatchLaunch L;
+      int rc = batch_tables<T>(B, ids, coef, xs, mults, binvs, L, t);
+      if (rc) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        return rc;
+      }
+      const BDesc<T>* D = reinterpret_cast<const BDesc<T>*>(L.desc);
+      cudaError_t e = batch_enqueue<T>(B, L, 0);  // sets the kernel's shared-memory limit
+      count_launch(4);
+      batch_axhelm_kernel<T><<<L.gridA, L.threadsA, L.smem, B.stream>>>(D, L.mapA, L.baseA);
+      cudaEventRecord(e0, B.stream);
+      for (int q = 0; q < 3; ++q)
+        batch_axhelm_kernel<T><<<L.gridA, L.threadsA, L.smem, B.stream>>>(D, L.mapA, L.baseA);
+      cudaEventRecord(e1, B.stream);
+      if (e == cudaSuccess) e = cudaGetLastError();
+      float ms = 0.f;
+      if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+      if (e != cudaSuccess) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        B.err = std::string("batch autotune: ") + cudaGetErrorString(e);
+        return -3;
+      }
+      if (ms < best_ms) {
+        best_ms = ms;
+        best = t;
+      }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    best_ms /= 3.f;
+  } else if (!cand.empty()) {
+    best = cand[0];
+  }
+  B.threads[prec] = best;
+  B.tune_ms[prec] = best_ms;
+  B.tkey[prec] = key;
+  return 0;
+}
+
+// first: run the iteration-1 check of freshly prepared problems first (not
+// after a residual replacement, which sets the scalars itself).
+template <typename T>
+int batch_iterate(Batch& B, const std::vector<int>& ids, const BatchLaunch& L, bool first = true) {
   const int np = (int)ids.size();
   const BDesc<T>* D = reinterpret_cast<const BDesc<T>*>(L.desc);
-  count_launch();
-  batch_update_kernel<T, true><<<L.gridC, kBatchThreads, 0, B.stream>>>(D, L.mapC, L.baseC);
+  if (first) {
+    count_launch();
+    batch_update_kernel<T, true><<<L.gridC, kBatchThreads, 0, B.stream>>>(D, L.mapC, L.baseC);
+  }
   bool graph = B.use_graph;
   std::vector<int64_t> key = {(int64_t)sizeof(T), L.gridA, L.gridB, L.gridC, (int64_t)L.smem,
+                              L.threadsA,
                               (int64_t)(uintptr_t)L.desc, (int64_t)(uintptr_t)L.mapA, B.chunk};
   if (graph && (!B.gexec || key != B.gkey)) {
     if (B.gexec) cudaGraphExecDestroy(B.gexec);
@@ -397,8 +497,10 @@ int batch_solve_fp64(Batch& B, int np, double* const* x, const double* const* f,
     bs.push_back(binv[p]);
   }
   if (ids.empty()) return 0;
+  int rc = batch_tune<double>(B, ids, coef, xs, ms, bs);
+  if (rc) return rc;
   BatchLaunch L;
-  int rc = batch_tables<double>(B, ids, coef, xs, ms, bs, L);
+  rc = batch_tables<double>(B, ids, coef, xs, ms, bs, L);
   if (rc) return rc;
   rc = batch_iterate<double>(B, ids, L);
   if (rc) return rc;
@@ -414,13 +516,16 @@ int batch_solve_fp64(Batch& B, int np, double* const* x, const double* const* f,
 }
 
 // Mixed batched solve: per-problem FP64 defect correction, the FP32 inner
-// PCG of all active problems batched.  niter = total inner iterations,
-// nouter = outer steps.
+// PCG of all active problems batched.  mode 1: one FP32 PCG per problem with
+// residual replacement (mixed_replace) each time its residual has dropped by
+// inner_tol; mode 0: a fresh FP32 PCG per outer step.  niter = total inner
+// iterations, nouter = outer steps (FP64 residual evaluations).
 int batch_solve_mixed(Batch& B, int np, double* const* x, const double* const* f,
                       const double* const* h1, const double* const* h2,
                       const double* const* mask, const double* const* mult,
                       const double* const* binv, double tin, int maxiter, double inner_tol,
-                      int* niter, int* nouter, double* rbn0, double* rbn2, int* status) {
+                      int mode, int* niter, int* nouter, double* rbn0, double* rbn2,
+                      int* status) {
   constexpr int kMaxOuter = 30;
   std::vector<Coef<double>> c64(np);
   std::vector<Coef<float>> c32(np);
@@ -478,7 +583,99 @@ int batch_solve_mixed(Batch& B, int np, double* const* x, const double* const* f
     tol[p] = tin < 0 ? std::fabs(tin) * r0 : std::fabs(tin);
     active[p] = r0 > 0.0;
   }
-  for (int outer = 1; outer <= kMaxOuter; ++outer) {
+  if (mode == 1) {
+    // all problems: one FP32 PCG each, prepared once
+    std::vector<int> ids;
+    std::vector<Coef<float>> coefs;
+    std::vector<float*> xs;
+    std::vector<const float*> ms, bs;
+    for (int p = 0; p < np; ++p) {
+      if (!active[p] || status[p]) continue;
+      if (rbn[p] <= tol[p]) {
+        active[p] = 0;
+        continue;
+      }
+      Handle& h = *B.probs[p];
+      const int64_t n = h.mesh.n;
+      int st = 0;
+      const double amax = device_absmax<double>(h, h.w64.r.ptr, n, &st);
+      if (st || amax == 0.0) {
+        active[p] = 0;
+        continue;
+      }
+      scale[p] = std::ldexp(1.0, std::ilogb(amax));
+      cast_to_f32(h, h.w32.f.ptr, h.w64.r.ptr, 1.0 / scale[p], n);
+      bool trivial = false;
+      PcgResult r = pcg_prepare<float>(h, h.w32, h.w32.x.ptr, h.w32.f.ptr, c32[p],
+                                       h.w32.mask.ptr, h.w32.mult.ptr, -inner_tol, maxiter, 0,
+                                       h.w32.d.ptr, &trivial);
+      if (r.status) {
+        status[p] = r.status == -1 ? NEKGPU_EINVAL : NEKGPU_ECUDA;
+        continue;
+      }
+      if (trivial) {
+        active[p] = 0;
+        continue;
+      }
+      ids.push_back(p);
+      coefs.push_back(c32[p]);
+      xs.push_back(h.w32.x.ptr);
+      ms.push_back(h.w32.mult.ptr);
+      bs.push_back(h.w32.binv.ptr);
+    }
+    if (!ids.empty()) {
+      const int rc = batch_tune<float>(B, ids, coefs, xs, ms, bs);
+      if (rc) return rc;
+    }
+    bool first = true;
+    for (int upd = 1; !ids.empty() && upd <= 100000; ++upd) {
+      BatchLaunch L;
+      int rc = batch_tables<float>(B, ids, coefs, xs, ms, bs, L);
+      if (rc) return rc;
+      rc = batch_iterate<float>(B, ids, L, first);
+      if (rc) return rc;
+      first = false;
+      std::vector<int> keep;
+      std::vector<Coef<float>> kc;
+      std::vector<float*> kx;
+      std::vector<const float*> km, kb;
+      for (size_t q = 0; q < ids.size(); ++q) {
+        const int p = ids[q];
+        Handle& h = *B.probs[p];
+        const int64_t n = h.mesh.n;
+        const bool capped = h.cg_host->iter > h.cg_host->maxiter;
+        niter[p] = h.cg_host->niter;
+        nouter[p] = upd;
+        axpy_f32(h, x[p], h.w32.x.ptr, scale[p], n);
+        const double rnew = outer_residual(h, h.w64.r.ptr, f[p], x[p], c64[p], mask[p], mult[p],
+                                           binv[p], h.w64.w.ptr);
+        if (!(rnew >= 0.0) || !std::isfinite(rnew)) {
+          status[p] = NEKGPU_ENAN;
+          continue;
+        }
+        const bool progress = rnew < rbn[p];
+        rbn[p] = rbn2[p] = rnew;
+        if (rnew <= tol[p] || capped || !progress) continue;
+        const int rr = mixed_replace(h, scale[p], inner_tol, nullptr);
+        if (rr < 0) {
+          status[p] = NEKGPU_ECUDA;
+          continue;
+        }
+        if (rr == 1) continue;
+        keep.push_back(p);
+        kc.push_back(coefs[q]);
+        kx.push_back(xs[q]);
+        km.push_back(ms[q]);
+        kb.push_back(bs[q]);
+      }
+      ids.swap(keep);
+      coefs.swap(kc);
+      xs.swap(kx);
+      ms.swap(km);
+      bs.swap(kb);
+    }
+  }
+  for (int outer = 1; mode != 1 && outer <= kMaxOuter; ++outer) {
     std::vector<int> ids;
     std::vector<Coef<float>> coefs;
     std::vector<float*> xs;
@@ -518,6 +715,10 @@ int batch_solve_mixed(Batch& B, int np, double* const* x, const double* const* f
       bs.push_back(h.w32.binv.ptr);
     }
     if (ids.empty()) break;
+    if (outer == 1) {
+      const int rc = batch_tune<float>(B, ids, coefs, xs, ms, bs);
+      if (rc) return rc;
+    }
     BatchLaunch L;
     int rc = batch_tables<float>(B, ids, coefs, xs, ms, bs, L);
     if (rc) return rc;
@@ -634,10 +835,13 @@ int nekgpu_batch_solve_dev(const int64_t* batch, const int* nprob, double* const
   B->err.clear();
   int rc;
   if (mixed && *mixed) {
+    if (*mixed != 1 && *mixed != 2) return bfail(B, NEKGPU_EINVAL, "mixed must be 0, 1 or 2");
+    const int mode = *mixed == 1 ? 1 : 0;
+    const double itol = inner_tol ? *inner_tol : (mode == 1 ? 1e-2 : 1e-5);
+    if (!(itol > 0.0 && itol < 1.0)) return bfail(B, NEKGPU_EINVAL, "inner_tol must be in (0, 1)");
     std::vector<int> no(np, 0);
-    rc = nekgpu::batch_solve_mixed(*B, np, x, f, h1, h2, mask, mult, binv, *tin, *maxit,
-                                   inner_tol ? *inner_tol : 1e-5, niter, no.data(), rbn0, rbn2,
-                                   status);
+    rc = nekgpu::batch_solve_mixed(*B, np, x, f, h1, h2, mask, mult, binv, *tin, *maxit, itol,
+                                   mode, niter, no.data(), rbn0, rbn2, status);
     if (nouter)
       for (int p = 0; p < np; ++p) nouter[p] = no[p];
   } else {
@@ -651,6 +855,29 @@ int nekgpu_batch_solve_dev(const int64_t* batch, const int* nprob, double* const
   for (int p = 0; p < np; ++p)
     if (status[p] && status[p] != NEKGPU_ENOTCONV && B->err.empty())
       B->err = "problem " + std::to_string(p) + ": " + B->probs[p]->err;
+  return NEKGPU_OK;
+}
+
+int nekgpu_batch_shape(const int64_t* batch, const int* precision, int* threads, double* ms) {
+  Batch* B = bget(batch);
+  if (!B) return bfail(nullptr, NEKGPU_EHANDLE, "unknown batch");
+  if (!precision || (*precision != 0 && *precision != 1))
+    return bfail(B, NEKGPU_EINVAL, "precision must be 0 or 1");
+  if (threads) *threads = B->threads[*precision];
+  if (ms) *ms = B->tune_ms[*precision];
+  return NEKGPU_OK;
+}
+
+int nekgpu_batch_set_shape(const int64_t* batch, const int* precision, const int* threads) {
+  Batch* B = bget(batch);
+  if (!B) return bfail(nullptr, NEKGPU_EHANDLE, "unknown batch");
+  if (!precision || !threads || (*precision != 0 && *precision != 1))
+    return bfail(B, NEKGPU_EINVAL, "bad argument");
+  if (*threads != 0 && *threads != 128 && *threads != 256)
+    return bfail(B, NEKGPU_EINVAL, "threads must be 0 (autotune), 128 or 256");
+  B->pinned[*precision] = *threads;
+  B->threads[*precision] = 0;
+  B->tkey[*precision].clear();
   return NEKGPU_OK;
 }
 

@@ -212,6 +212,8 @@ struct MixedResult {
   double rbn0 = 0, rbn2 = 0;
   int status = 0;
 };
+// Residual replacement into the running FP32 PCG (see mixed.cu).
+int mixed_replace(Handle& h, double& scale, double inner_tol, int* restarts);
 // mode 0: each outer step is a fresh FP32 PCG to inner_tol (restarted);
 // mode 1: one FP32 PCG whose residual is replaced by the FP64 one whenever it
 // has dropped by inner_tol, keeping the search direction (reliable updates).

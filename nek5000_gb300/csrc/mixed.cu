@@ -183,6 +183,61 @@ double outer_residual(Handle& h, double* r, const double* f, const double* x,
   return st ? -1.0 : std::sqrt(s2 / m.vol);
 }
 
+// Residual replacement: h.w64.r holds r = f - A x (FP64).  It becomes the
+// residual of the running FP32 PCG of h.w32, rescaled by a power of two near
+// max |r| (*scale: old in, new out; the ratio of two powers of two is exact,
+// so p is rescaled exactly), x32 is zeroed (its old content is already in x),
+// and the scalars after the last check (h.cg_host) are updated for the new r:
+// r.z, norm and tolerance recomputed, rtz of the previous iterate rescaled,
+// beta = (r.z)_new / (r.z)_old.  The direction restarts (beta = 0, p = z,
+// counted in *restarts) when the true norm exceeds twice the recurrence norm,
+// i.e. FP32 drift dominates and p no longer fits r.  Returns 0, 1 when r is
+// zero (nothing to iterate on), or a negative status.
+int mixed_replace(Handle& h, double& scale, double inner_tol, int* restarts) {
+  PcgWork<float>& wk = h.w32;
+  PcgWork<double>& w64 = h.w64;
+  const Mesh& m = h.mesh;
+  const int64_t n = m.n;
+  cudaStream_t s = h.stream;
+  const int nb = blocks(n);
+  int st = 0;
+  const double amax = device_absmax<double>(h, w64.r.ptr, n, &st);
+  if (st) return -3;
+  if (amax == 0.0) return 1;
+  const double s_new = std::ldexp(1.0, std::ilogb(amax));
+  const double ratio = scale / s_new;
+  count_launch(3);
+  cast_scale_kernel<float, double><<<nb, kThreads, 0, s>>>(wk.r.ptr, w64.r.ptr, 1.0 / s_new, n);
+  scale_kernel<<<nb, kThreads, 0, s>>>(wk.p.ptr, (float)ratio, n);
+  cudaMemsetAsync(wk.x.ptr, 0, n * sizeof(float), s);
+  rz_kernel<<<nb, kThreads, 0, s>>>(wk.r.ptr, wk.d.ptr, wk.mult.ptr, wk.binv.ptr, n, h.red.ptr);
+  std::vector<double> hp(2 * (size_t)nb);
+  cudaMemcpyAsync(hp.data(), h.red.ptr, hp.size() * sizeof(double), cudaMemcpyDeviceToHost, s);
+  if (cudaStreamSynchronize(s) != cudaSuccess) {
+    set_error(h, std::string("mixed: ") + cudaGetErrorString(cudaGetLastError()));
+    return -3;
+  }
+  double s1 = 0.0, s2 = 0.0;
+  for (int b = 0; b < nb; ++b) {
+    s1 += hp[b];
+    s2 += hp[nb + b];
+  }
+  CgScalars& c = *h.cg_host;  // state after the last (iterated) check
+  const double rec = c.rbn2 * ratio;  // FP32 recurrence norm, new scaling
+  c.rtz2 = c.rtz2 * ratio * ratio;
+  c.rtz1 = s1;
+  c.rbn0 = std::sqrt(s2 / m.vol);
+  c.beta = (c.rbn0 <= 2.0 * rec) ? s1 / c.rtz2 : 0.0;
+  if (c.beta == 0.0 && restarts) ++*restarts;
+  c.rbn2 = c.rbn0;
+  c.tol = inner_tol * c.rbn0;
+  c.done = 0;
+  c.counter[0] = c.counter[1] = c.counter[2] = c.counter[3] = 0u;
+  cudaMemcpyAsync(h.cg, &c, sizeof(CgScalars), cudaMemcpyHostToDevice, s);
+  scale = s_new;
+  return 0;
+}
+
 MixedResult mixed_solve(Handle& h, double* x, const double* f, const double* h1,
                         const double* h2, const double* mask, const double* mult,
                         const double* binv, double tin, int maxit, double inner_tol, int mode) {
@@ -300,47 +355,12 @@ MixedResult mixed_solve(Handle& h, double* x, const double* f, const double* h1,
       const bool progress = rnew < rbn;
       rbn = rnew;
       if (rbn <= tol || capped || !progress) break;
-      // residual replacement, rescaled to a power of two near max |r|
-      amax = device_absmax<double>(h, w64.r.ptr, n, &st2);
-      if (st2 || amax == 0.0) break;
-      const double s_new = std::ldexp(1.0, std::ilogb(amax));
-      const double ratio = scale / s_new;  // exact: both powers of two
-      cast(wk.r.ptr, w64.r.ptr, 1.0 / s_new);
-      count_launch();
-      scale_kernel<<<nb, kThreads, 0, s>>>(wk.p.ptr, (float)ratio, n);
-      cudaMemsetAsync(wk.x.ptr, 0, n * sizeof(float), s);
-      count_launch();
-      rz_kernel<<<nb, kThreads, 0, s>>>(wk.r.ptr, wk.d.ptr, wk.mult.ptr, wk.binv.ptr, n,
-                                        h.red.ptr);
-      std::vector<double> hp(2 * (size_t)nb);
-      cudaMemcpyAsync(hp.data(), h.red.ptr, hp.size() * sizeof(double), cudaMemcpyDeviceToHost,
-                      s);
-      if (cudaStreamSynchronize(s) != cudaSuccess) {
-        res.status = -3;
+      const int rr = mixed_replace(h, scale, inner_tol, &res.restarts);
+      if (rr < 0) {
+        res.status = rr;
         return res;
       }
-      double s1 = 0.0, s2 = 0.0;
-      for (int b = 0; b < nb; ++b) {
-        s1 += hp[b];
-        s2 += hp[nb + b];
-      }
-      CgScalars& c = *h.cg_host;  // state after the last (iterated) check
-      const double rec = c.rbn2 * ratio;  // FP32 recurrence norm, new scaling
-      c.rtz2 = c.rtz2 * ratio * ratio;
-      c.rtz1 = s1;
-      c.rbn0 = std::sqrt(s2 / m.vol);
-      // Keep the search direction while the true residual is still close to
-      // the recurrence one; once FP32 drift dominates (true norm more than
-      // twice the recurrence norm) p no longer fits r and the direction is
-      // restarted (beta = 0: p = z).
-      c.beta = (c.rbn0 <= 2.0 * rec) ? s1 / c.rtz2 : 0.0;
-      if (c.beta == 0.0) ++res.restarts;
-      c.rbn2 = c.rbn0;
-      c.tol = inner_tol * c.rbn0;
-      c.done = 0;
-      c.counter[0] = c.counter[1] = c.counter[2] = c.counter[3] = 0u;
-      cudaMemcpyAsync(h.cg, &c, sizeof(CgScalars), cudaMemcpyHostToDevice, s);
-      scale = s_new;
+      if (rr == 1) break;
     }
     res.rbn2 = rbn;
     if (!(rbn <= tol)) {

@@ -272,8 +272,10 @@ class NekGpuBatch:
         return idx.value
 
     def solve(self, x, f, h1, h2, mask, mult, binv, tin=-1e-10, maxit=10 ** 6, mixed=False,
-              inner_tol=1e-5):
-        """Returns a dict of per-problem lists: niter, nouter, rbn0, rbn2, status."""
+              inner_tol=None):
+        """mixed: False/0 FP64; True/1 FP32 inner PCG with residual replacement;
+        2 restarted FP32 inner PCG.  inner_tol None takes the library default.
+        Returns a dict of per-problem lists: niter, nouter, rbn0, rbn2, status."""
         np_ = len(self.sizes)
         arr = lambda ts: (C.c_void_p * np_)(*[t.data_ptr() for t in ts])
         for ts in (x, f, h1, h2, mask, mult, binv):
@@ -289,11 +291,28 @@ class NekGpuBatch:
         rc = self._L.nekgpu_batch_solve_dev(
             C.byref(self._b), C.byref(_cint(np_)), arr(x), arr(f), arr(h1), arr(h2), arr(mask),
             arr(mult), arr(binv), C.byref(_cdouble(tin)), C.byref(_cint(int(maxit))),
-            C.byref(_cint(int(mixed))), C.byref(_cdouble(inner_tol)), niter, nouter, r0, r2, st)
+            C.byref(_cint(int(mixed))),
+            None if inner_tol is None else C.byref(_cdouble(inner_tol)), niter, nouter, r0, r2, st)
         if rc:
             raise _capi.NekGpuError(rc, self.last_error())
         return dict(niter=list(niter), nouter=list(nouter), rbn0=list(r0), rbn2=list(r2),
                     status=list(st))
+
+    def shape(self, precision: int = 0):
+        """Operator block size in use for the batch: (threads, tuned ms)."""
+        t, ms = _cint(0), _cdouble(0)
+        rc = self._L.nekgpu_batch_shape(C.byref(self._b), C.byref(_cint(precision)), C.byref(t),
+                                        C.byref(ms))
+        if rc:
+            raise _capi.NekGpuError(rc, self.last_error())
+        return t.value, ms.value
+
+    def set_shape(self, precision: int, threads: int):
+        """Pin the operator block size (128 or 256; 0 returns to tuning)."""
+        rc = self._L.nekgpu_batch_set_shape(C.byref(self._b), C.byref(_cint(precision)),
+                                            C.byref(_cint(threads)))
+        if rc:
+            raise _capi.NekGpuError(rc, self.last_error())
 
     def close(self):
         if getattr(self, "_b", None) is not None and self._b.value:
