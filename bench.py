@@ -65,6 +65,9 @@ def parse():
                          "batch: 3 velocity solves + 61 uneven Poisson problems in one batch; "
                          "axhelm-sweep: in-solve operator bandwidth at N=5,7,9, E=32^3")
     ap.add_argument("--batch-problems", type=int, default=61)
+    ap.add_argument("--fp32-shape", default=None,
+                    help="pin the FP32 operator launch shape 'kind,epb' instead of autotuning "
+                         "(kind 0 plain, 1 TMA; see nekgpu_ax_candidates)")
     args = ap.parse_args()
     if args.workload == "poisson-n9":
         if args.k == 32:
@@ -282,6 +285,9 @@ def run_gpu(args):
     big = 10 ** 6
     lib.set_option(2, 1)  # timing: solve-total and per-launch operator events
     lib.set_option(7, args.mixed_mode)
+    if args.fp32_shape:
+        kind, epb = (int(v) for v in args.fp32_shape.split(","))
+        lib.set_ax_shape(1, kind, epb)
 
     def fp64():
         it, r0, r2, rc = lib.cggo(x, f, h1, h2, mask, mult, 1, -args.tol, big, 1, binv, maxcg=big)
