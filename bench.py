@@ -304,20 +304,26 @@ def run_gpu(args):
         barrier(pg)
         torch.cuda.synchronize()
         l0 = lib.launch_count()
-        its, ms_tot, ms_ax, n_ax = [], 0.0, 0.0, 0
+        its, ms_tot, ms_ax, n_ax, ms_gs, ms_up = [], 0.0, 0.0, 0, 0.0, 0.0
         with Clocks(local) as ck:
             for _ in range(args.steps):
                 it, rc = solve()
                 if rc != 0:
                     raise RuntimeError(f"solve did not converge: {lib.last_error()}")
                 t_tot, t_ax, k_ax = lib.last_timing()
+                _, t_gs, t_up, _ = lib.last_kernel_times()
                 its.append(it)
                 ms_tot += t_tot
                 ms_ax += t_ax
                 n_ax += k_ax
+                ms_gs += t_gs
+                ms_up += t_up
         torch.cuda.synchronize()
         barrier(pg)
-        return dict(iters=its, T=allmax(pg, ms_tot / 1e3), ms_ax=ms_ax / max(n_ax, 1), n_ax=n_ax,
+        k = max(n_ax, 1)
+        return dict(iters=its, T=allmax(pg, ms_tot / 1e3), ms_ax=ms_ax / k, n_ax=n_ax,
+                    per_iter_ms={"operator": ms_ax / k, "boundary_groups": ms_gs / k,
+                                 "update": ms_up / k},
                     launches=lib.launch_count() - l0, clocks=ck.summary())
 
     peak, peak_src = peaks()
@@ -338,6 +344,7 @@ def run_gpu(args):
                    "GB/s": b64 * n / (r64["ms_ax"] * 1e-3) / 1e9, "bytes_per_point": b64,
                    "fp64_tflops": flops_pt * n / (r64["ms_ax"] * 1e-3) / 1e12,
                    "ncu_fp64_pipe_active_pct": (ns64 or {}).get("fp64_pipe_active_pct")},
+        "per_iteration_ms": r64.get("per_iter_ms"),
         "gpu_launches": r64["launches"], "clocks": r64["clocks"]}
     x64 = x.clone() if not args.only_mixed else None
     rmx = timed(mixed)
@@ -375,6 +382,7 @@ def run_gpu(args):
                          "achieved": ax_gbs, "peak": peak, "unit": "GB/s", "frac": ax_gbs / peak,
                          "peak_source": peak_src, "bytes_per_point": b32,
                          "avg_launch_ms": rmx["ms_ax"], "launches_timed": rmx["n_ax"],
+                         "inner_iteration_ms": rmx["per_iter_ms"],
                          "traffic": ns32["dram_bytes_per_point"] * n if ns32 else None},
             "gpu_launches": rmx["launches"],
             "clocks": rmx["clocks"]}

@@ -288,6 +288,11 @@ int nekgpu_ax_candidates(const int64_t *handle, const int *precision, int *kinds
 int nekgpu_set_timing(const int64_t *handle, const int *on);
 int nekgpu_last_timing(const int64_t *handle, double *ms_total, double *ms_axhelm,
                        int *n_axhelm);
+/* The same per-launch timing split over the three kernels of a PCG
+ * iteration (operator; boundary-group sum, mask and rho; update), summed over
+ * the timed iterations of the last solve. */
+int nekgpu_last_kernel_times(const int64_t *handle, double *ms_axhelm, double *ms_gs,
+                             double *ms_update, int *iterations);
 /* Kernels this library has launched in the process so far (all handles). */
 int nekgpu_launch_count(int64_t *count);
 

@@ -58,6 +58,7 @@ SIGNATURES = {
     "nekgpu_launch_count": [_I64P],
     "nekgpu_autotune": [_I64P, _IP, _IP, _IP, _IP, _IP, _DP],
     "nekgpu_batch_shape": [_I64P, _IP, _IP, _DP],
+    "nekgpu_last_kernel_times": [_I64P, _DP, _DP, _DP, _IP],
     "nekgpu_batch_set_shape": [_I64P, _IP, _IP],
     "nekgpu_ax_shape": [_I64P, _IP, _IP, _IP, _DP],
     "nekgpu_set_ax_shape": [_I64P, _IP, _IP, _IP],

@@ -49,6 +49,13 @@ struct AxArgs {
   double* partial; // one per element
   int* err;        // device flag: set if a bounded wait expired
   const unsigned char* skip;  // interior points owned by the boundary-group kernel
+  // Fused form: 0 = rho partial over element-interior points (the
+  // reference's glsc3 of the assembled w, its boundary part added by the
+  // boundary-group kernel); 1 = over every local point of the unassembled w,
+  // which equals the same rho because p is continuous and zero where masked
+  // (sum_g w_g p_g = sum_i w_local_i p_i), and spares the boundary-group
+  // kernel its p reads.  The FP32 inner solve uses 1.
+  int allrho;
 };
 
 template <int NX>
@@ -226,10 +233,11 @@ __device__ __forceinline__ void axhelm_body(const AxArgs<T>& a, int blk, int tx,
         const T bm = __ldg(a.bm1 + eo + pt);
         s = EXACT ? add_x(s, mul_x(mul_x(hh, bm), ru[k])) : fma(hh * bm, ru[k], s);
       }
-      a.au[eo + pt] = s;
+      if constexpr (FUSED && sizeof(T) == 4) st_hint(a.au + eo + pt, s, l2_policy_evict_last());
+      else a.au[eo + pt] = s;
       if constexpr (FUSED) {
-        if (i > 0 && i < NX - 1 && j > 0 && j < NX - 1 && k > 0 && k < NX - 1 &&
-            (!a.skip || !a.skip[eo + pt]))
+        if (a.allrho || (i > 0 && i < NX - 1 && j > 0 && j < NX - 1 && k > 0 && k < NX - 1 &&
+                         (!a.skip || !a.skip[eo + pt])))
           dot = fma(s, ru[k], dot);
       }
     }

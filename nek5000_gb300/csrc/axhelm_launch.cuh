@@ -123,6 +123,7 @@ cudaError_t launch_axhelm_cg(const Mesh& m, const OpData<T>& op, T* w, T* p, con
   a.d = d;
   a.cg = cg;
   a.partial = partial;
+  a.allrho = sizeof(T) == 4 ? 1 : 0;  // FP32: rho over every point (see AxArgs)
   return launch_ax<T, EXACT, true>(m, a, nparts, s);
 }
 

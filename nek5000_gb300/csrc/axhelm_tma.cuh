@@ -119,15 +119,17 @@ __global__ void __launch_bounds__(NX* NX* EPB) axhelm_tma_kernel(const AxArgs<T>
     const size_t off = (size_t)e0 * P;
     const uint32_t total = fb * (1 + (FUSED ? 2 : 0) + hb + hh1 + hh2 + 6);
     mbar_expect_tx(bar, total);
-    bulk_g2s(sU, a.u + off, fb, bar);
+    // every input is read once per apply: evict first, so that L2 keeps w
+    const uint64_t pol = l2_policy_evict_first();
+    bulk_g2s_hint(sU, a.u + off, fb, bar, pol);
     if constexpr (FUSED) {
-      bulk_g2s(sR, a.r + off, fb, bar);
-      bulk_g2s(sDg, a.d + off, fb, bar);
+      bulk_g2s_hint(sR, a.r + off, fb, bar, pol);
+      bulk_g2s_hint(sDg, a.d + off, fb, bar, pol);
     }
-    if (hb) bulk_g2s(sB, a.bm1 + off, fb, bar);
-    if (hh1) bulk_g2s(sH1, a.h1 + off, fb, bar);
-    if (hh2) bulk_g2s(sH2, a.h2 + off, fb, bar);
-    bulk_g2s(sG, a.G + 6 * off, 6 * fb, bar);
+    if (hb) bulk_g2s_hint(sB, a.bm1 + off, fb, bar, pol);
+    if (hh1) bulk_g2s_hint(sH1, a.h1 + off, fb, bar, pol);
+    if (hh2) bulk_g2s_hint(sH2, a.h2 + off, fb, bar, pol);
+    bulk_g2s_hint(sG, a.G + 6 * off, 6 * fb, bar, pol);
   }
   // D rows / columns of this thread while the copies fly
   const int i = threadIdx.x % NX, j = threadIdx.x / NX, el = threadIdx.y;
@@ -201,6 +203,7 @@ __global__ void __launch_bounds__(NX* NX* EPB) axhelm_tma_kernel(const AxArgs<T>
   __syncthreads();
 
   T dot = T(0);
+  const uint64_t keep = l2_policy_evict_last();
 #pragma unroll
   for (int k = 0; k < NX; ++k) {
     const T* s1 = st1 + lo + k * NXY;
@@ -220,10 +223,11 @@ __global__ void __launch_bounds__(NX* NX* EPB) axhelm_tma_kernel(const AxArgs<T>
         const T hv = hh2 ? sH2[lo + pt] : a.h2s;
         s = fma(hv * sB[lo + pt], ru[k], s);
       }
-      a.au[eo + pt] = s;
+      if constexpr (FUSED && sizeof(T) == 4) st_hint(a.au + eo + pt, s, keep);
+      else a.au[eo + pt] = s;
       if constexpr (FUSED) {
-        if (i > 0 && i < NX - 1 && j > 0 && j < NX - 1 && k > 0 && k < NX - 1 &&
-            (!a.skip || !a.skip[eo + pt]))
+        if (a.allrho || (i > 0 && i < NX - 1 && j > 0 && j < NX - 1 && k > 0 && k < NX - 1 &&
+                         (!a.skip || !a.skip[eo + pt])))
           dot = fma(s, ru[k], dot);
       }
     }

@@ -540,7 +540,7 @@ int nekgpu_cggo_dev(const int64_t* handle, double* x, const double* f, const dou
   if (check_n(H, x) || check_n(H, f) || check_n(H, mask) || check_n(H, mult) ||
       check_n(H, binv) || !tin || !maxit)
     return fail(H, NEKGPU_EINVAL, "null argument");
-  H->ms_axhelm = 0.0;
+  H->ms_axhelm = H->ms_gs = H->ms_update = 0.0;
   H->n_axhelm = 0;
   if (cuda_pending(*H, "cggo: on entry")) return NEKGPU_ECUDA;
   if (H->timing) cudaEventRecord(H->evt0, H->stream);
@@ -592,7 +592,7 @@ int nekgpu_hmholtz_dev(const int64_t* handle, double* u, double* rhs, const doub
   if (check_n(H, u) || check_n(H, rhs) || check_n(H, mask) || check_n(H, mult) ||
       check_n(H, binv) || !tli || !maxit)
     return fail(H, NEKGPU_EINVAL, "null argument");
-  H->ms_axhelm = 0.0;
+  H->ms_axhelm = H->ms_gs = H->ms_update = 0.0;
   H->n_axhelm = 0;
   if (H->timing) cudaEventRecord(H->evt0, H->stream);
   int rc = hmholtz_dev(H, u, rhs, h1, h2, mask, mult, *tli, *maxit, maxcg ? *maxcg : 900, binv,
@@ -645,7 +645,7 @@ int nekgpu_cggo_mixed_dev(const int64_t* handle, double* x, const double* f, con
     return fail(H, NEKGPU_EINVAL, "null argument");
   const double itol = inner_tol ? *inner_tol : (H->mixed_mode == 1 ? 1e-2 : 1e-5);
   if (!(itol > 0.0 && itol < 1.0)) return fail(H, NEKGPU_EINVAL, "inner_tol must be in (0, 1)");
-  H->ms_axhelm = 0.0;
+  H->ms_axhelm = H->ms_gs = H->ms_update = 0.0;
   H->n_axhelm = 0;
   if (H->timing) cudaEventRecord(H->evt0, H->stream);
   MixedResult r = mixed_solve(*H, x, f, h1, h2, mask, mult, binv, *tin, *maxit, itol,
@@ -850,6 +850,16 @@ int nekgpu_set_timing(const int64_t* handle, const int* on) {
   GET_HANDLE(handle);
   if (!on) return fail(H, NEKGPU_EINVAL, "null argument");
   H->timing = (*on != 0);
+  return NEKGPU_OK;
+}
+
+int nekgpu_last_kernel_times(const int64_t* handle, double* ms_axhelm, double* ms_gs,
+                             double* ms_update, int* iterations) {
+  GET_HANDLE(handle);
+  if (ms_axhelm) *ms_axhelm = H->ms_axhelm;
+  if (ms_gs) *ms_gs = H->ms_gs;
+  if (ms_update) *ms_update = H->ms_update;
+  if (iterations) *iterations = H->n_axhelm;
   return NEKGPU_OK;
 }
 

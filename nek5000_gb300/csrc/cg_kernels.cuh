@@ -48,6 +48,7 @@ __device__ __forceinline__ void cg_update_body(T* __restrict__ x, T* __restrict_
   const int64_t stride = (int64_t)nblk * blockDim.x;
   constexpr int W = 16 / sizeof(T);
   const int64_t nv = VEC ? n / W : 0;
+  const uint64_t wpol = sizeof(T) == 4 ? l2_policy_evict_first() : 0;
   int64_t iv = gtid;
   for (; iv < nv; iv += stride) {
     T xx[W], rr[W], pp[W], ww[W], dd[W], mm[W], bb[W];
@@ -58,7 +59,10 @@ __device__ __forceinline__ void cg_update_body(T* __restrict__ x, T* __restrict_
     if (!FIRST) {
       ld16(xx, x, iv);
       ld16(pp, p, iv);
-      ld16(ww, w, iv);
+      if constexpr (sizeof(T) == 4)  // last use of the L2-resident w
+        *reinterpret_cast<float4*>(ww) = ld_hint4(reinterpret_cast<const float*>(w) + 4 * iv, wpol);
+      else
+        ld16(ww, w, iv);
     }
 #pragma unroll
     for (int q = 0; q < W; ++q) P::run(xx[q], rr[q], pp[q], ww[q], dd[q], mm[q], bb[q], alpha, a1, a2);

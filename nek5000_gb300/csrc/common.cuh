@@ -132,6 +132,38 @@ __device__ __forceinline__ void st16(T* base, const T* v, int64_t iv) {
   reinterpret_cast<V*>(base)[iv] = *reinterpret_cast<const V*>(v);
 }
 
+// L2 eviction priorities for one access (createpolicy + .L2::cache_hint,
+// sm_80 and later).  The FP32 PCG keeps its 4-byte-per-point operator output
+// w resident in L2 from the operator kernel through the boundary-group and
+// update kernels: the operator streams its inputs with evict_first and
+// stores w with evict_last, the boundary-group kernel touches w with
+// evict_last, and the update kernel's last read of w uses evict_first.
+__device__ __forceinline__ uint64_t l2_policy_evict_first() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ uint64_t l2_policy_evict_last() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ float ld_hint(const float* a, uint64_t pol) {
+  float v;
+  asm volatile("ld.global.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(a), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ float4 ld_hint4(const float* a, uint64_t pol) {
+  float4 v;
+  asm volatile("ld.global.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
+               : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+               : "l"(a), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ void st_hint(float* a, float v, uint64_t pol) {
+  asm volatile("st.global.L2::cache_hint.f32 [%0], %1, %2;" ::"l"(a), "f"(v), "l"(pol) : "memory");
+}
+
 // Scalars of one PCG solve, resident on the device (no host round trip per
 // iteration).  All FP64, whatever the field precision.
 struct CgScalars {

@@ -194,11 +194,11 @@ void gs_op(const GsMaps& gs, T* u, int op, cudaStream_t s) {
 
 template <typename T>
 void gs_cg(const GsMaps& gs, T* w, const T* p, const T* segmask, const T* segmsum,
-           CgScalars* cg, double* partialA, int nA, double* partialB, cudaStream_t s) {
+           CgScalars* cg, double* partialA, int nA, double* partialB, cudaStream_t s, bool rho) {
   const int nb = gs_cg_blocks(gs);
   count_launch();
   gs_cg_kernel<T><<<nb, kGsThreads, 0, s>>>(w, p, gs.bstart, gs.bidx, gs.cls, segmask, segmsum,
-                                            cg, partialA, nA, partialB);
+                                            cg, partialA, nA, partialB, rho ? 1 : 0);
 }
 
 template <typename T>
@@ -213,9 +213,9 @@ void gs_cg_weights(const GsMaps& gs, const T* mask, const T* mult, T* segmask, T
 template void gs_op<double>(const GsMaps&, double*, int, cudaStream_t);
 template void gs_op<float>(const GsMaps&, float*, int, cudaStream_t);
 template void gs_cg<double>(const GsMaps&, double*, const double*, const double*, const double*,
-                            CgScalars*, double*, int, double*, cudaStream_t);
+                            CgScalars*, double*, int, double*, cudaStream_t, bool);
 template void gs_cg<float>(const GsMaps&, float*, const float*, const float*, const float*,
-                           CgScalars*, double*, int, double*, cudaStream_t);
+                           CgScalars*, double*, int, double*, cudaStream_t, bool);
 template void gs_cg_weights<double>(const GsMaps&, const double*, const double*, double*, double*,
                                     int*, cudaStream_t);
 template void gs_cg_weights<float>(const GsMaps&, const float*, const float*, float*, float*,

@@ -59,12 +59,14 @@ template <typename T>
 void gs_op(const GsMaps& gs, T* u, int op, cudaStream_t s);
 
 // PCG form: for every boundary group g, s = mask_g * sum w; w <- s on all
-// copies; rho partial += s * p_g * msum_g.  The last block adds these
-// partials to the interior partials left by the fused axhelm (nA of them)
-// and sets rho, alpha = rtz1/rho.
+// copies; rho partial += s * p_g * msum_g (rho = true).  The last block adds
+// these partials to the per-element partials left by the fused axhelm (nA of
+// them) and sets rho, alpha = rtz1/rho.  rho = false: the operator's
+// partials already hold all of rho (AxArgs::allrho).
 template <typename T>
 void gs_cg(const GsMaps& gs, T* w, const T* p, const T* segmask, const T* segmsum,
-           CgScalars* cg, double* partialA, int nA, double* partialB, cudaStream_t s);
+           CgScalars* cg, double* partialA, int nA, double* partialB, cudaStream_t s,
+           bool rho = true);
 
 // Per-segment mask value (mask at the first copy) and sum of mult over the
 // copies, for the bound maps.  Returns via `nonuniform` (device int) whether

@@ -1,7 +1,8 @@
 // gs_kernels.cuh -- the PCG form of the gather-scatter (kernel B of an
 // iteration) as a block body, shared by the single-problem and batched
 // solvers: w = mask * dssum(w) on every element-boundary group, boundary part
-// of rho = sum w p mult (core/hmholtz.f:797-801), then alpha = rtz1 / rho.
+// of rho = sum w p mult (core/hmholtz.f:797-801; skipped when the operator
+// reduced rho over every point), then alpha = rtz1 / rho.
 #pragma once
 #include "gs.cuh"
 
@@ -31,7 +32,21 @@ __device__ __forceinline__ void load_ids(const int* __restrict__ cidx, int s, in
   }
 }
 
-template <typename T, int C, int G>
+// FP32 w is touched with an evict-last L2 policy (it stays resident for the
+// update kernel).  RHO = false skips the rho accumulation (the operator then
+// reduced rho over every local point, see AxArgs::allrho).
+template <typename T>
+__device__ __forceinline__ T w_load(const T* w, int i, uint64_t pol) {
+  if constexpr (sizeof(T) == 4) return ld_hint(w + i, pol);
+  else return w[i];
+}
+template <typename T>
+__device__ __forceinline__ void w_store(T* w, int i, T v, uint64_t pol) {
+  if constexpr (sizeof(T) == 4) st_hint(w + i, v, pol);
+  else w[i] = v;
+}
+
+template <typename T, int C, int G, bool RHO>
 __device__ __forceinline__ void gs_groups(const int* __restrict__ cidx, int s0, int step, int cnt,
                                           int goff, T* __restrict__ w, const T* __restrict__ p,
                                           const T* __restrict__ segmask,
@@ -44,16 +59,19 @@ __device__ __forceinline__ void gs_groups(const int* __restrict__ cidx, int s0, 
     on[q] = s < cnt;
     if (on[q]) load_ids<C>(cidx, s, id[q]);
   }
+  const uint64_t keep = sizeof(T) == 4 ? l2_policy_evict_last() : 0;
   T v[G][C], p0[G], mk[G], ms[G];
 #pragma unroll
   for (int q = 0; q < G; ++q) {
     if (!on[q]) continue;
     const int s = s0 + q * step;
 #pragma unroll
-    for (int c = 0; c < C; ++c) v[q][c] = w[id[q][c]];
-    p0[q] = p[id[q][0]];
+    for (int c = 0; c < C; ++c) v[q][c] = w_load(w, id[q][c], keep);
+    if constexpr (RHO) {
+      p0[q] = p[id[q][0]];
+      ms[q] = segmsum[goff + s];
+    }
     mk[q] = segmask[goff + s];
-    ms[q] = segmsum[goff + s];
   }
 #pragma unroll
   for (int q = 0; q < G; ++q) {
@@ -63,8 +81,8 @@ __device__ __forceinline__ void gs_groups(const int* __restrict__ cidx, int s0, 
     for (int c = 1; c < C; ++c) t = t + v[q][c];
     t = t * mk[q];
 #pragma unroll
-    for (int c = 0; c < C; ++c) w[id[q][c]] = t;
-    acc.add(t * p0[q] * ms[q]);
+    for (int c = 0; c < C; ++c) w_store(w, id[q][c], t, keep);
+    if constexpr (RHO) acc.add(t * p0[q] * ms[q]);
   }
 }
 
@@ -80,7 +98,7 @@ __device__ __forceinline__ void gs_cg_body(T* __restrict__ w, const T* __restric
                                            const T* __restrict__ segmsum, CgScalars* cg,
                                            const double* __restrict__ partialA, int nA,
                                            double* __restrict__ partialB, int blk, int nblk,
-                                           double* red, int* am_last_s) {
+                                           double* red, int* am_last_s, bool rho = true) {
   int& am_last = *am_last_s;
   int k = 0;
   while (k < kGsClasses - 1 && blk >= cls.boff[k + 1]) ++k;
@@ -89,11 +107,15 @@ __device__ __forceinline__ void gs_cg_body(T* __restrict__ w, const T* __restric
   const int* ci = idx + cls.ioff[k];
   const int goff = cls.soff[k], cnt = cls.cnt[k];
   CompAcc<T> acc;
+#define NEKGPU_GS_CLASS(C, GG)                                                              \
+  if (rho) gs_groups<T, C, GG, true>(ci, s0, blockDim.x, cnt, goff, w, p, segmask, segmsum, acc); \
+  else gs_groups<T, C, GG, false>(ci, s0, blockDim.x, cnt, goff, w, p, segmask, segmsum, acc);
   switch (k) {
-    case 0: gs_groups<T, 1, 4>(ci, s0, blockDim.x, cnt, goff, w, p, segmask, segmsum, acc); break;
-    case 1: gs_groups<T, 2, 4>(ci, s0, blockDim.x, cnt, goff, w, p, segmask, segmsum, acc); break;
-    case 2: gs_groups<T, 4, 2>(ci, s0, blockDim.x, cnt, goff, w, p, segmask, segmsum, acc); break;
-    case 3: gs_groups<T, 8, 1>(ci, s0, blockDim.x, cnt, goff, w, p, segmask, segmsum, acc); break;
+    case 0: NEKGPU_GS_CLASS(1, 4) break;
+    case 1: NEKGPU_GS_CLASS(2, 4) break;
+    case 2: NEKGPU_GS_CLASS(4, 2) break;
+    case 3: NEKGPU_GS_CLASS(8, 1) break;
+#undef NEKGPU_GS_CLASS
     default:
       for (int q = 0; q < G; ++q) {
         const int sl = s0 + q * blockDim.x;
@@ -104,7 +126,7 @@ __device__ __forceinline__ void gs_cg_body(T* __restrict__ w, const T* __restric
         for (int c = a + 1; c < b; ++c) t = t + w[idx[c]];
         t = t * segmask[g];
         for (int c = a; c < b; ++c) w[idx[c]] = t;
-        acc.add(t * p[idx[a]] * segmsum[g]);
+        if (rho) acc.add(t * p[idx[a]] * segmsum[g]);
       }
   }
   double dot = block_sum_comp(acc, red);  // thread 0
@@ -124,10 +146,10 @@ __device__ __forceinline__ void gs_cg_body(T* __restrict__ w, const T* __restric
   double pb = 0.0;
 #pragma unroll 8
   for (int q = threadIdx.x; q < nblk; q += blockDim.x) pb += __ldcg(partialB + q);
-  const double rho = block_sum(pb, red);
+  const double rho_all = block_sum(pb, red);
   if (threadIdx.x == 0) {
-    cg->rho = rho;
-    cg->alpha = cg->rtz1 / rho;
+    cg->rho = rho_all;
+    cg->alpha = cg->rtz1 / rho_all;
     cg->counter[0] = 0u;
   }
 }
@@ -137,12 +159,13 @@ __global__ void __launch_bounds__(kGsThreads)
     gs_cg_kernel(T* __restrict__ w, const T* __restrict__ p, const int* __restrict__ start,
                  const int* __restrict__ idx, const GsClasses cls,
                  const T* __restrict__ segmask, const T* __restrict__ segmsum, CgScalars* cg,
-                 const double* __restrict__ partialA, int nA, double* __restrict__ partialB) {
+                 const double* __restrict__ partialA, int nA, double* __restrict__ partialB,
+                 int rho) {
   __shared__ double red[32];
   __shared__ int am_last;
   if (cg->done) return;
   gs_cg_body<T>(w, p, start, idx, cls, segmask, segmsum, cg, partialA, nA, partialB, blockIdx.x,
-                gridDim.x, red, &am_last);
+                gridDim.x, red, &am_last, rho != 0);
 }
 
 }  // namespace nekgpu

@@ -105,7 +105,7 @@ struct Handle {
   bool timing = false;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, evt0 = nullptr, evt1 = nullptr;
   std::vector<cudaEvent_t> ax_ev;  // per-launch operator timing pool
-  double ms_total = 0.0, ms_axhelm = 0.0;
+  double ms_total = 0.0, ms_axhelm = 0.0, ms_gs = 0.0, ms_update = 0.0;
   int n_axhelm = 0;
   // graph cache for the PCG iteration chunk: the captured launches depend on
   // every pointer and coefficient below, so any change recaptures.

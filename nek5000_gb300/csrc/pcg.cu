@@ -543,9 +543,11 @@ PcgResult pcg_iterate(Handle& h, const OpData<T>& op, PcgWork<T>& wk, T* x, cons
   // the live launches and are summed (later ones found the solve converged
   // and returned at once).
   const int chunk = std::max(1, h.graph_chunk);
-  if (h.timing && h.ax_ev.size() < 2 * (size_t)chunk) {
+  // four events per iteration: before the operator, after it, after the
+  // boundary-group kernel, after the update
+  if (h.timing && h.ax_ev.size() < 4 * (size_t)chunk) {
     for (cudaEvent_t e : h.ax_ev) cudaEventDestroy(e);
-    h.ax_ev.assign(2 * (size_t)chunk, nullptr);
+    h.ax_ev.assign(4 * (size_t)chunk, nullptr);
     for (auto& e : h.ax_ev) cudaEventCreate(&e);
   }
   // One chunk = `chunk` iterations of the three kernels.  With graphs on, the
@@ -553,13 +555,16 @@ PcgResult pcg_iterate(Handle& h, const OpData<T>& op, PcgWork<T>& wk, T* x, cons
   auto enqueue_chunk = [&](int k) -> cudaError_t {
     for (int q = 0; q < k; ++q) {
       int nAb = 0;
-      if (h.timing) cudaEventRecord(h.ax_ev[2 * q], s);
+      if (h.timing) cudaEventRecord(h.ax_ev[4 * q], s);
       cudaError_t e = launch_A<T>(h, op, wk, c, exact, &nAb);
-      if (h.timing) cudaEventRecord(h.ax_ev[2 * q + 1], s);
+      if (h.timing) cudaEventRecord(h.ax_ev[4 * q + 1], s);
       if (e != cudaSuccess) return e;
+      // FP32: rho came whole from the operator (AxArgs::allrho)
       gs_cg<T>(m.gs, wk.w.ptr, wk.p.ptr, wk.segmask.ptr, wk.segmsum.ptr, h.cg, h.partialA.ptr,
-               nAb, h.partialB.ptr, s);
+               nAb, h.partialB.ptr, s, sizeof(T) != 4);
+      if (h.timing) cudaEventRecord(h.ax_ev[4 * q + 2], s);
       launch_C<T>(h, wk, x, mult, binv, exact, false);
+      if (h.timing) cudaEventRecord(h.ax_ev[4 * q + 3], s);
     }
     return cudaGetLastError();
   };
@@ -612,13 +617,18 @@ PcgResult pcg_iterate(Handle& h, const OpData<T>& op, PcgWork<T>& wk, T* x, cons
     }
     if (h.timing && launched) {
       const int live = std::min(launched, h.cg_host->iter - iter_before);
-      for (int q = 0; q < live; ++q) {
+      auto span = [&](int a, int b) {
         float ms = 0.f;
-        if (cudaEventElapsedTime(&ms, h.ax_ev[2 * q], h.ax_ev[2 * q + 1]) != cudaSuccess) {
+        if (cudaEventElapsedTime(&ms, h.ax_ev[a], h.ax_ev[b]) != cudaSuccess) {
           cudaGetLastError();
           ms = 0.f;
         }
-        h.ms_axhelm += ms;
+        return (double)ms;
+      };
+      for (int q = 0; q < live; ++q) {
+        h.ms_axhelm += span(4 * q, 4 * q + 1);
+        h.ms_gs += span(4 * q + 1, 4 * q + 2);
+        h.ms_update += span(4 * q + 2, 4 * q + 3);
       }
       h.n_axhelm += live;
     }

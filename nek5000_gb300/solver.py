@@ -88,6 +88,14 @@ class NekGpu:
                                                C.byref(k)))
         return t.value, a.value, k.value
 
+    def last_kernel_times(self):
+        """(ms operator, ms boundary groups, ms update, iterations) of the last
+        solve with kernel timing on, summed over its iterations."""
+        a, g, u, k = _cdouble(0), _cdouble(0), _cdouble(0), _cint(0)
+        self._check(self._L.nekgpu_last_kernel_times(C.byref(self._h), C.byref(a), C.byref(g),
+                                                     C.byref(u), C.byref(k)))
+        return a.value, g.value, u.value, k.value
+
     def launch_count(self) -> int:
         c = C.c_int64(0)
         self._L.nekgpu_launch_count(C.byref(c))
