@@ -255,6 +255,39 @@ int nekgpu_batch_set_shape(const int64_t *batch, const int *precision, const int
 int nekgpu_batch_last_error(const int64_t *batch, char *buf, const int *buflen);
 int nekgpu_batch_destroy(int64_t *batch);
 
+/* ---- projection onto previous solutions (core/navier4.f:562-1188) --------- */
+/* hsolve with projection (navier4.f:562, the ifstdh = .false. branch): the
+ * right-hand side r is masked by vmk and dssum'ed in place, its part in the
+ * span of the space's stored B = A X is removed (project1, :636), the rest is
+ * solved as hmhzpf does (:513: chktcg1 on tli, then cggo with that tolerance;
+ * param(22) is the caller's business), and the solution u gets the matching
+ * part of span(X) back and joins the space (project2, :1129; proj_ortho,
+ * :852).  A change of h1 or h2 since the space was built triggers B = A X
+ * and a full re-orthonormalisation (iproj_chk :788, proj_ortho_full_cgs2
+ * :1060).  The space lives on the device inside the handle, selected by
+ * *space (0 <= *space < NEKGPU_PROJ_SPACES; the reference's per-field approx
+ * / napprox arrays); it holds at most mmx vectors (default
+ * NEKGPU_PROJ_DEFAULT = (mxprev - 4) / 2 with the reference's mxprev = 20).
+ * Outputs as nekgpu_cggo_dev plus *m (vectors in the space afterwards). */
+#define NEKGPU_PROJ_SPACES 16
+#define NEKGPU_PROJ_MAX 16
+#define NEKGPU_PROJ_DEFAULT 8
+int nekgpu_hsolve_dev(const int64_t *handle, const int *space, double *u, double *r,
+                      const double *h1, const double *h2, const double *vmk, const double *vml,
+                      const int *imsh, const double *tli, const int *maxit, const int *isd,
+                      const double *bi, const int *maxcg, int *niter, double *rbn0,
+                      double *rbn2, int *m);
+/* The same with host arrays (u out, r in/out). */
+int nekgpu_hsolve(const int64_t *handle, const int *space, double *u, double *r,
+                  const double *h1, const double *h2, const double *vmk, const double *vml,
+                  const int *imsh, const double *tli, const int *maxit, const int *isd,
+                  const double *bi, const int *maxcg, int *niter, double *rbn0, double *rbn2,
+                  int *m);
+/* Empty space *space and set its capacity to *mmx vectors (1..NEKGPU_PROJ_MAX). */
+int nekgpu_proj_setup(const int64_t *handle, const int *space, const int *mmx);
+/* Number of vectors in space *space. */
+int nekgpu_proj_count(const int64_t *handle, const int *space, int *m);
+
 /* ---- operator launch shapes (autotuner) ---------------------------------- */
 /* No counterpart in the reference.  The operator's launch shape is the kernel
  * kind (0: plain-load kernel, 1: TMA-staged FP32 kernel) and the number of

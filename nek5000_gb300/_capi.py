@@ -20,6 +20,7 @@ OPT_EXACT, OPT_TIMING, OPT_CHUNK, OPT_ISTEP, OPT_TMA, OPT_GRAPH, OPT_MIXED_MODE 
 OPT_AUTOTUNE = 8
 MAX_LX1 = 12
 NOALLOC_MAX_POINTS = 4194304
+PROJ_SPACES, PROJ_MAX, PROJ_DEFAULT = 16, 16, 8
 
 STATUS_NAMES = {
     0: "NEKGPU_OK", -1: "NEKGPU_EINVAL", -2: "NEKGPU_EHANDLE", -3: "NEKGPU_ECUDA",
@@ -59,6 +60,12 @@ SIGNATURES = {
     "nekgpu_autotune": [_I64P, _IP, _IP, _IP, _IP, _IP, _DP],
     "nekgpu_batch_shape": [_I64P, _IP, _IP, _DP],
     "nekgpu_last_kernel_times": [_I64P, _DP, _DP, _DP, _IP],
+    "nekgpu_hsolve_dev": [_I64P, _IP, _P, _P, _P, _P, _P, _P, _IP, _DP, _IP, _IP, _P, _IP, _IP,
+                          _DP, _DP, _IP],
+    "nekgpu_hsolve": [_I64P, _IP, _P, _P, _P, _P, _P, _P, _IP, _DP, _IP, _IP, _P, _IP, _IP, _DP,
+                      _DP, _IP],
+    "nekgpu_proj_setup": [_I64P, _IP, _IP],
+    "nekgpu_proj_count": [_I64P, _IP, _IP],
     "nekgpu_batch_set_shape": [_I64P, _IP, _IP],
     "nekgpu_ax_shape": [_I64P, _IP, _IP, _IP, _DP],
     "nekgpu_set_ax_shape": [_I64P, _IP, _IP, _IP],

@@ -262,6 +262,7 @@ int handle_setup(Handle& H, int lx1, int nel, const double* dxm1, const double* 
   m.f32.release();
   m.has_f32 = false;
   m.ax_sel[0] = m.ax_sel[1] = AxShapeSel();
+  H.proj.clear();  // projection spaces belong to the old mesh
   H.has_mesh = false;
   if (H.gexec) cudaGraphExecDestroy(H.gexec);
   H.gexec = nullptr;
@@ -737,6 +738,93 @@ int nekgpu_cggo_adjoint_dev(const int64_t* handle, double* lam, const double* g,
   // The Helmholtz operator is symmetric, so the adjoint solve is cggo itself.
   return nekgpu_cggo_dev(handle, lam, g, h1, h2, mask, mult, imsh, tin, maxit, isd, binv, maxcg,
                          niter, rbn0, rbn2);
+}
+
+// ---- projection onto previous solutions (proj.cu) ----------------------------
+int nekgpu_hsolve_dev(const int64_t* handle, const int* space, double* u, double* r,
+                      const double* h1, const double* h2, const double* vmk, const double* vml,
+                      const int* imsh, const double* tli, const int* maxit, const int* isd,
+                      const double* bi, const int* maxcg, int* niter, double* rbn0,
+                      double* rbn2, int* m) {
+  GET_HANDLE(handle);
+  NEED_MESH();
+  (void)imsh;
+  (void)isd;
+  if (!space || !tli || !maxit || check_n(H, u) || check_n(H, r) || check_n(H, h1) ||
+      check_n(H, h2) || check_n(H, vmk) || check_n(H, vml) || check_n(H, bi))
+    return fail(H, NEKGPU_EINVAL, "null argument");
+  H->err.clear();
+  ProjSpace* P = nullptr;
+  if (proj_space(*H, *space, &P)) return fail(H, NEKGPU_EINVAL, H->err);
+  if (proj_alloc(*H, *P)) return fail(H, NEKGPU_ENOMEM, H->err);
+  const int64_t n = H->mesh.n;
+  count_launch();
+  mul_kernel<<<nblk(n), 256, 0, H->stream>>>(r, vmk, n);  // col2(r, vmk)
+  gs_op<double>(H->mesh.gs, r, 0, H->stream);               // dssum(r)
+  Coef<double> c;
+  int rc = make_coef(H, h1, h2, c);
+  if (rc) return rc;
+  if ((rc = proj_project1(*H, *P, r, c, h1, h2, vmk, vml)))
+    return fail(H, rc == -4 ? NEKGPU_ENOMEM : NEKGPU_ECUDA, H->err);
+  double tol = *tli;  // hmhzpf: tol = tli, then chktcg1
+  if ((rc = chktcg1_dev(H, &tol, r, c, vmk, vml, bi))) return rc;
+  const int cap = maxcg ? *maxcg : 900;
+  rc = cggo_dev(H, u, r, h1, h2, vmk, vml, tol, *maxit, cap, bi, niter, rbn0, rbn2);
+  if (rc && rc != NEKGPU_ENOTCONV) return rc;
+  const int rc2 = proj_project2(*H, *P, u, c, vmk, vml);
+  if (rc2) return fail(H, rc2 == -4 ? NEKGPU_ENOMEM : NEKGPU_ECUDA, H->err);
+  if (m) *m = P->m;
+  return rc;
+}
+
+int nekgpu_hsolve(const int64_t* handle, const int* space, double* u, double* r,
+                  const double* h1, const double* h2, const double* vmk, const double* vml,
+                  const int* imsh, const double* tli, const int* maxit, const int* isd,
+                  const double* bi, const int* maxcg, int* niter, double* rbn0, double* rbn2,
+                  int* m) {
+  GET_HANDLE(handle);
+  NEED_MESH();
+  if (check_n(H, u) || check_n(H, r) || check_n(H, h1) || check_n(H, h2) || check_n(H, vmk) ||
+      check_n(H, vml) || check_n(H, bi))
+    return NEKGPU_EINVAL;
+  const int64_t n = H->mesh.n;
+  int rc;
+  if ((rc = h2d(H, H->io0, r, n)) || (rc = h2d(H, H->io1, h1, n)) ||
+      (rc = h2d(H, H->io2, h2, n)) || (rc = h2d(H, H->io4, vmk, n)) ||
+      (rc = h2d(H, H->io7, vml, n)) || (rc = h2d(H, H->io8, bi, n)))
+    return rc;
+  if (H->io3.ensure(n)) return fail(H, NEKGPU_ENOMEM, "staging allocation failed");
+  rc = nekgpu_hsolve_dev(handle, space, H->io3.ptr, H->io0.ptr, H->io1.ptr, H->io2.ptr,
+                         H->io4.ptr, H->io7.ptr, imsh, tli, maxit, isd, H->io8.ptr, maxcg, niter,
+                         rbn0, rbn2, m);
+  if (rc && rc != NEKGPU_ENOTCONV) return rc;
+  int rc2 = d2h(H, u, H->io3.ptr, n);
+  if (!rc2) rc2 = d2h(H, r, H->io0.ptr, n);
+  return rc2 ? rc2 : rc;
+}
+
+int nekgpu_proj_setup(const int64_t* handle, const int* space, const int* mmx) {
+  GET_HANDLE(handle);
+  if (!space || !mmx) return fail(H, NEKGPU_EINVAL, "null argument");
+  if (*mmx < 1 || *mmx > NEKGPU_PROJ_MAX)
+    return fail(H, NEKGPU_EINVAL, "mmx must be in [1, NEKGPU_PROJ_MAX]");
+  ProjSpace* P = nullptr;
+  if (proj_space(*H, *space, &P)) return fail(H, NEKGPU_EINVAL, H->err);
+  P->xx.release();
+  P->bb.release();
+  P->h1old.release();
+  P->mmx = *mmx;
+  P->m = 0;
+  return NEKGPU_OK;
+}
+
+int nekgpu_proj_count(const int64_t* handle, const int* space, int* m) {
+  GET_HANDLE(handle);
+  if (!space || !m) return fail(H, NEKGPU_EINVAL, "null argument");
+  ProjSpace* P = nullptr;
+  if (proj_space(*H, *space, &P)) return fail(H, NEKGPU_EINVAL, H->err);
+  *m = P->m;
+  return NEKGPU_OK;
 }
 
 // ---- operator launch shapes (autotuner) -------------------------------------

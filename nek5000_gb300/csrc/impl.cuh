@@ -7,6 +7,7 @@
 #include "axhelm.cuh"
 #include "common.cuh"
 #include "gs.cuh"
+#include "nekgpu.h"
 
 namespace nekgpu {
 
@@ -86,6 +87,14 @@ struct PcgWork {
   DevBuf<T> r, w, p, d, mult, binv, mask, segmask, segmsum, x, f, h1, h2;
 };
 
+// One projection space of previous solutions (proj.cu): X and B = A X, each
+// mmx vectors of n back to back, xbar / bbar, and the h1 / h2 the space was
+// built with.
+struct ProjSpace {
+  int mmx = 0, m = 0;
+  DevBuf<double> xx, bb, xbar, bbar, h1old, h2old;
+};
+
 struct Handle {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -129,6 +138,7 @@ struct Handle {
   bool use_graph = true;
   int mixed_mode = 1;  // see mixed_solve
   bool autotune = true;  // time the operator's launch shapes on first solve (tune.cu)
+  std::vector<std::unique_ptr<ProjSpace>> proj;  // projection spaces by index (proj.cu)
   DevBuf<CgScalars> cg_tune;  // scalars of the tuning launches (beta = 0, not done)
 };
 
@@ -212,6 +222,13 @@ struct MixedResult {
   double rbn0 = 0, rbn2 = 0;
   int status = 0;
 };
+// Projection onto previous solutions (proj.cu).
+int proj_space(Handle& h, int space, ProjSpace** out);
+int proj_alloc(Handle& h, ProjSpace& P);
+int proj_project1(Handle& h, ProjSpace& P, double* b, const Coef<double>& c, const double* h1,
+                  const double* h2, const double* msk, const double* w);
+int proj_project2(Handle& h, ProjSpace& P, double* x, const Coef<double>& c, const double* msk,
+                  const double* w);
 // Residual replacement into the running FP32 PCG (see mixed.cu).
 int mixed_replace(Handle& h, double& scale, double inner_tol, int* restarts);
 // mode 0: each outer step is a fresh FP32 PCG to inner_tol (restarted);

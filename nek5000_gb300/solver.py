@@ -198,6 +198,32 @@ class NekGpu:
         fn = self._L.nekgpu_cggo_dev if _is_dev(x) else self._L.nekgpu_cggo
         return self._solve(fn, x, f, h1, h2, mask, mult, imsh, tin, maxit, isd, binv, maxcg)
 
+    def hsolve(self, name, u, r, h1, h2, vmk, vml, imsh, tol, maxit, isd, bi, space=0,
+               maxcg=900):
+        """hsolve with projection onto previous solutions of projection space
+        `space` (navier4.f:562).  u: out; r: in/out (masked, dssum'ed and
+        projected in place).  Returns (niter, rbn0, rbn2, m, status)."""
+        del name
+        fn = self._L.nekgpu_hsolve_dev if _is_dev(u) else self._L.nekgpu_hsolve
+        niter, r0, r2, m = _cint(0), _cdouble(0), _cdouble(0), _cint(0)
+        mc = C.byref(_cint(int(maxcg))) if maxcg is not None else None
+        rc = fn(C.byref(self._h), C.byref(_cint(space)), _ptr(u), _ptr(r), _ptr(h1), _ptr(h2),
+                _ptr(vmk), _ptr(vml), C.byref(_cint(imsh)), C.byref(_cdouble(tol)),
+                C.byref(_cint(int(maxit))), C.byref(_cint(isd)), _ptr(bi), mc, C.byref(niter),
+                C.byref(r0), C.byref(r2), C.byref(m))
+        self._check(rc, allow=(_capi.ENOTCONV,))
+        return niter.value, r0.value, r2.value, m.value, rc
+
+    def proj_setup(self, space: int, mmx: int = 8):
+        """Empty projection space `space` and give it room for mmx vectors."""
+        self._check(self._L.nekgpu_proj_setup(C.byref(self._h), C.byref(_cint(space)),
+                                              C.byref(_cint(mmx))))
+
+    def proj_count(self, space: int) -> int:
+        m = _cint(0)
+        self._check(self._L.nekgpu_proj_count(C.byref(self._h), C.byref(_cint(space)), C.byref(m)))
+        return m.value
+
     def hmholtz(self, name, u, rhs, h1, h2, mask, mult, imsh, tli, maxit, isd, binv, maxcg=900):
         """name is accepted for signature parity (the reference uses it only for
         the pressure branch and log lines).  rhs is dssum'd and masked in place."""

@@ -1157,3 +1157,288 @@ void ref_local_grad3_t(double *u, const double *ur, const double *us, const doub
   ref_mxm(ut, m2, d, m1, w, m1);
   for (int i = 0; i < m3; ++i) u[i] = u[i] + w[i];
 }
+
+/* ======================================================================== */
+/* Residual projection onto previous solutions (navier4.f:562-1188).        */
+/* ======================================================================== */
+struct ref_proj {
+  int mmx, m;
+  int64_t n;
+  double *xx, *bb;           /* X(n,mmx), B(n,mmx) = A*X                      */
+  double *xbar, *bbar;       /* best fit in X and A*xbar                      */
+  double *h1old, *h2old;     /* h1 / h2 the basis was built with (zero-filled) */
+};
+
+ref_proj *ref_proj_create(const ref_ops *ops, int mmx) {
+  ref_proj *p = (ref_proj *)calloc(1, sizeof(ref_proj));
+  const int64_t n = ops->n;
+  p->mmx = mmx;
+  p->n = n;
+  p->xx = (double *)calloc((size_t)n * mmx, sizeof(double));
+  p->bb = (double *)calloc((size_t)n * mmx, sizeof(double));
+  p->xbar = (double *)calloc(n, sizeof(double));
+  p->bbar = (double *)calloc(n, sizeof(double));
+  p->h1old = (double *)calloc(n, sizeof(double));
+  p->h2old = (double *)calloc(n, sizeof(double));
+  return p;
+}
+
+void ref_proj_free(ref_proj *p) {
+  if (!p) return;
+  free(p->xx); free(p->bb); free(p->xbar); free(p->bbar); free(p->h1old); free(p->h2old);
+  free(p);
+}
+
+int ref_proj_m(const ref_proj *p) { return p->m; }
+const double *ref_proj_x(const ref_proj *p, int k) { return p->xx + (size_t)k * p->n; }
+const double *ref_proj_b(const ref_proj *p, int k) { return p->bb + (size_t)k * p->n; }
+
+/* proj_matvec (navier4.f:827): b = mask * dssum(A x), imsh = 1, isd = 1 */
+static void proj_matvec(const ref_ops *ops, double *b, const double *x, const double *h1,
+                        const double *h2, const double *msk) {
+  const int64_t n = ops->n;
+  ref_axhelm(ops, b, x, h1, h2);
+  ref_dssum(ops, b);
+  PFOR
+  for (int64_t i = 0; i < n; ++i) b[i] = b[i] * msk[i];
+}
+
+/* vlsc3 summed over ranks (gop): sum x*w*y */
+static double gdot3(const ref_ops *ops, const double *x, const double *w, const double *y) {
+  double s;
+  GLOBAL_SUM(ops, s, x[i] * w[i] * y[i]);
+  return s;
+}
+
+/* 0.5*(vlsc3(a,w,b) + vlsc3(c,w,d)) per rank, then gop over ranks
+ * (proj_ortho :865-876, proj_ortho_full_cgs2 :1078-1086) */
+static double gdot3_sym(const ref_ops *ops, const double *a, const double *w, const double *b,
+                        const double *c, const double *d) {
+  int P_ = ops->nthreads < 1 ? 1 : ops->nthreads;
+  if (P_ > 256) P_ = 256;
+  double part_[256];
+  const int64_t nxyz_ = (int64_t)ops->nx1 * ops->nx1 * ops->nx1;
+  _Pragma("omp parallel for num_threads(P_) schedule(static,1)")
+  for (int r_ = 0; r_ < P_; ++r_) {
+    int64_t e0_ = (int64_t)ops->nel * r_ / P_, e1_ = (int64_t)ops->nel * (r_ + 1) / P_;
+    double s1 = 0.0, s2 = 0.0;
+    for (int64_t i = e0_ * nxyz_; i < e1_ * nxyz_; ++i) s1 = s1 + a[i] * w[i] * b[i];
+    for (int64_t i = e0_ * nxyz_; i < e1_ * nxyz_; ++i) s2 = s2 + c[i] * w[i] * d[i];
+    part_[r_] = 0.5 * (s1 + s2);
+  }
+  double tot_ = part_[0];
+  for (int r_ = 1; r_ < P_; ++r_) tot_ = tot_ + part_[r_];
+  return tot_;
+}
+
+/* add2s2 (math.f:689): a = a + c1*b */
+static void add2s2(const ref_ops *ops, double *a, const double *b, double c1) {
+  const int64_t n = ops->n;
+  PFOR
+  for (int64_t i = 0; i < n; ++i) a[i] = a[i] + c1 * b[i];
+}
+
+static void cmult(const ref_ops *ops, double *a, double c) {
+  const int64_t n = ops->n;
+  PFOR
+  for (int64_t i = 0; i < n; ++i) a[i] = a[i] * c;
+}
+
+/* hypot (navier4.f:1330-1342, Nek's own, not libm's) */
+static double nek_hypot(double a, double b) {
+  double c = fabs(a), d = fabs(b);
+  double x = c > d ? c : d;
+  double ix = 1.0 / x;
+  double t = c < d ? c : d;
+  t = ix * t;
+  return x * sqrt(1.0 + t * t);
+}
+
+/* givens_rotation (navier4.f:1308) */
+static void givens_rotation(double a, double b, double *c, double *s, double *r) {
+  if (b != 0.0) {
+    double h = nek_hypot(a, b);
+    double d = 1.0 / h;
+    *c = fabs(a) * d;
+    *s = copysign(d, a) * b;
+    *r = copysign(1.0, a) * h;
+  } else {
+    *c = 1.0;
+    *s = 0.0;
+    *r = a;
+  }
+}
+
+/* proj_ortho_full_cgs2 (navier4.f:1060-1127) */
+static void proj_ortho_full_cgs2(const ref_ops *ops, ref_proj *p, const double *w) {
+  const int64_t n = ops->n;
+  int m = p->m;
+  if (m <= 0) return;
+  double tol = 1.0e-7;
+  double alpha[64];
+  int flag[64];
+  for (int it = 0; it < 2; ++it) {
+    for (int k = m; k >= 1; --k) {
+      double *xk = p->xx + (size_t)(k - 1) * n, *bk = p->bb + (size_t)(k - 1) * n;
+      for (int j = m; j >= k; --j) {
+        const double *xj = p->xx + (size_t)(j - 1) * n, *bj = p->bb + (size_t)(j - 1) * n;
+        alpha[j - 1] = gdot3_sym(ops, xj, w, bk, bj, xk);
+      }
+      for (int j = m; j >= k + 1; --j) {
+        add2s2(ops, xk, p->xx + (size_t)(j - 1) * n, -alpha[j - 1]);
+        add2s2(ops, bk, p->bb + (size_t)(j - 1) * n, -alpha[j - 1]);
+      }
+      double normp = sqrt(alpha[k - 1]);
+      double normk = sqrt(gdot3(ops, xk, w, bk));
+      if (normk > tol * normp) {
+        double scl1 = 1.0 / normk;
+        cmult(ops, xk, scl1);
+        cmult(ops, bk, scl1);
+        flag[k - 1] = 1;
+      } else {
+        flag[k - 1] = 0;
+      }
+    }
+  }
+  int k = 0;
+  for (int j = 1; j <= m; ++j) {
+    if (flag[j - 1] == 1) {
+      k = k + 1;
+      if (k < j) {
+        memcpy(p->xx + (size_t)(k - 1) * n, p->xx + (size_t)(j - 1) * n, sizeof(double) * n);
+        memcpy(p->bb + (size_t)(k - 1) * n, p->bb + (size_t)(j - 1) * n, sizeof(double) * n);
+      }
+    }
+  }
+  p->m = k;
+}
+
+/* project1 (navier4.f:636-733) + project1_a (:735-825); b <- b - B*alpha */
+static void project1(const ref_ops *ops, ref_proj *p, double *b, const double *h1,
+                     const double *h2, const double *msk, const double *w) {
+  const int64_t n = ops->n;
+  int m = p->m;
+  if (m <= 0) return;
+  /* iproj_chk (:788-820): matrix changed if h1/h2 differ from the old ones */
+  double dh1 = 0.0, dh2 = 0.0;
+  for (int64_t i = 0; i < n; ++i) {
+    double a1 = fabs(h1[i] - p->h1old[i]), a2 = fabs(h2[i] - p->h2old[i]);
+    dh1 = dh1 > a1 ? dh1 : a1;
+    dh2 = dh2 > a2 ? dh2 : a2;
+  }
+  double dh = dh1 > dh2 ? dh1 : dh2;
+  if (dh > 0.0) {
+    memcpy(p->h1old, h1, sizeof(double) * n);
+    memcpy(p->h2old, h2, sizeof(double) * n);
+    for (int j = 0; j < m; ++j)
+      proj_matvec(ops, p->bb + (size_t)j * n, p->xx + (size_t)j * n, h1, h2, msk);
+    proj_ortho_full_cgs2(ops, p, w);
+    m = p->m;
+  }
+  double alpha[64];
+  /* first round of CGS */
+  for (int k = 0; k < m; ++k) alpha[k] = gdot3(ops, p->xx + (size_t)k * n, w, b);
+  PFOR
+  for (int64_t i = 0; i < n; ++i) p->xbar[i] = alpha[0] * p->xx[i]; /* cmult2 */
+  PFOR
+  for (int64_t i = 0; i < n; ++i) p->bbar[i] = alpha[0] * p->bb[i];
+  add2s2(ops, b, p->bb, -alpha[0]);
+  for (int k = 1; k < m; ++k) {
+    add2s2(ops, p->xbar, p->xx + (size_t)k * n, alpha[k]);
+    add2s2(ops, p->bbar, p->bb + (size_t)k * n, alpha[k]);
+    add2s2(ops, b, p->bb + (size_t)k * n, -alpha[k]);
+  }
+  /* second round */
+  for (int k = 0; k < m; ++k) alpha[k] = gdot3(ops, p->xx + (size_t)k * n, w, b);
+  for (int k = 0; k < m; ++k) {
+    add2s2(ops, p->xbar, p->xx + (size_t)k * n, alpha[k]);
+    add2s2(ops, p->bbar, p->bb + (size_t)k * n, alpha[k]);
+    add2s2(ops, b, p->bb + (size_t)k * n, -alpha[k]);
+  }
+}
+
+/* proj_ortho (navier4.f:852-957): O(nm) update after appending x_m, b_m */
+static void proj_ortho(const ref_ops *ops, ref_proj *p, const double *w) {
+  const int64_t n = ops->n;
+  int m = p->m;
+  if (m <= 0) return;
+  double alpha[64], beta[64];
+  double *xm = p->xx + (size_t)(m - 1) * n, *bm = p->bb + (size_t)(m - 1) * n;
+  for (int k = 0; k < m; ++k) {
+    const double *xk = p->xx + (size_t)k * n, *bk = p->bb + (size_t)k * n;
+    alpha[k] = gdot3_sym(ops, xk, w, bm, bk, xm);
+  }
+  double nrm = sqrt(alpha[m - 1]);
+  for (int k = 0; k < m - 1; ++k) {
+    add2s2(ops, xm, p->xx + (size_t)k * n, -alpha[k]);
+    add2s2(ops, bm, p->bb + (size_t)k * n, -alpha[k]);
+  }
+  for (int k = 0; k < m - 1; ++k) {
+    const double *xk = p->xx + (size_t)k * n, *bk = p->bb + (size_t)k * n;
+    beta[k] = gdot3_sym(ops, xk, w, bm, bk, xm);
+  }
+  for (int k = 0; k < m - 1; ++k) {
+    add2s2(ops, xm, p->xx + (size_t)k * n, -beta[k]);
+    add2s2(ops, bm, p->bb + (size_t)k * n, -beta[k]);
+    alpha[k] = alpha[k] + beta[k];
+  }
+  alpha[m - 1] = sqrt(gdot3(ops, xm, w, bm));
+  double tol = 1.0e-7;
+  if (alpha[m - 1] > tol * nrm) {
+    double scl1 = 1.0 / alpha[m - 1];
+    cmult(ops, xm, scl1);
+    cmult(ops, bm, scl1);
+    for (int k = m; k >= 2; --k) {
+      int h = k - 1;
+      double c, s;
+      givens_rotation(alpha[h - 1], alpha[k - 1], &c, &s, &nrm);
+      alpha[h - 1] = nrm;
+      double *xh = p->xx + (size_t)(h - 1) * n, *xk = p->xx + (size_t)(k - 1) * n;
+      double *bh = p->bb + (size_t)(h - 1) * n, *bk = p->bb + (size_t)(k - 1) * n;
+      PFOR
+      for (int64_t i = 0; i < n; ++i) {
+        double scl1_ = c * xh[i] + s * xk[i];
+        xk[i] = -s * xh[i] + c * xk[i];
+        xh[i] = scl1_;
+        double scl2_ = c * bh[i] + s * bk[i];
+        bk[i] = -s * bh[i] + c * bk[i];
+        bh[i] = scl2_;
+      }
+    }
+  } else {
+    p->m = m - 1;
+  }
+}
+
+/* project2 (navier4.f:1129-1154) + project2_a (:1156-1187) */
+static void project2(const ref_ops *ops, ref_proj *p, double *x, const double *h1,
+                     const double *h2, const double *msk, const double *w) {
+  const int64_t n = ops->n;
+  if (p->m > 0) {
+    PFOR
+    for (int64_t i = 0; i < n; ++i) x[i] = x[i] + p->xbar[i]; /* add2 */
+  }
+  p->m = p->m + 1 < p->mmx ? p->m + 1 : p->mmx;
+  double *xm = p->xx + (size_t)(p->m - 1) * n, *bm = p->bb + (size_t)(p->m - 1) * n;
+  memcpy(xm, x, sizeof(double) * n);
+  proj_matvec(ops, bm, xm, h1, h2, msk);
+  proj_ortho(ops, p, w);
+}
+
+/* hsolve with projection (navier4.f:562-634, the ifstdh = .false. branch) and
+ * hmhzpf (:513-560, param(22) = 0, not 'PRES'): r <- dssum(r*vmk), project,
+ * chktcg1 + cggo, un-project and update the space. */
+int ref_hsolve(const ref_ops *ops, ref_proj *p, double *u, double *r, const double *h1,
+               const double *h2, const double *vmk, const double *vml, double tli, int maxit,
+               int maxcg, int istep, const double *binv, double *rbn0, double *rbn2) {
+  const int64_t n = ops->n;
+  PFOR
+  for (int64_t i = 0; i < n; ++i) r[i] = r[i] * vmk[i]; /* col2 */
+  ref_dssum(ops, r);
+  project1(ops, p, r, h1, h2, vmk, vml);
+  double tol = tli;
+  ref_chktcg1(ops, &tol, r, h1, h2, vmk, vml, binv);
+  int niter = ref_cggo(ops, u, r, h1, h2, vmk, vml, tol, maxit, maxcg, istep, binv, rbn0, rbn2);
+  project2(ops, p, u, h1, h2, vmk, vml);
+  return niter;
+}

@@ -88,6 +88,24 @@ int ref_hmholtz(const ref_ops *ops, double *u, double *rhs, const double *h1,
                 int maxit, int maxcg, int istep, const double *binv, double *rbn0,
                 double *rbn2);
 
+/* ---- residual projection onto previous solutions (navier4.f:562-1188) --- */
+/* One projection space (X, B = A X, xbar, bbar, h1old, h2old; the
+ * reference's approx / napprox arrays) of at most mmx vectors
+ * ((mxprev-4)/2 = 8 in the reference's default SIZE). */
+typedef struct ref_proj ref_proj;
+ref_proj *ref_proj_create(const ref_ops *ops, int mmx);
+void ref_proj_free(ref_proj *p);
+int ref_proj_m(const ref_proj *p);
+const double *ref_proj_x(const ref_proj *p, int k);
+const double *ref_proj_b(const ref_proj *p, int k);
+/* hsolve with projection (navier4.f:562, ifstdh = .false.): r is masked and
+ * dssum'ed in place, projected (project1), solved by hmhzpf (chktcg1 +
+ * cggo, tolerance tli as chktcg1 leaves it), u un-projected and appended to
+ * the space (project2).  Returns cggo's niter. */
+int ref_hsolve(const ref_ops *ops, ref_proj *p, double *u, double *r, const double *h1,
+               const double *h2, const double *vmk, const double *vml, double tli, int maxit,
+               int maxcg, int istep, const double *binv, double *rbn0, double *rbn2);
+
 /* local_grad3 (navier5.f:428) / local_grad3_t (navier1.f:4669), one element */
 void ref_local_grad3(double *ur, double *us, double *ut, const double *u, int N,
                      const double *d, const double *dt);

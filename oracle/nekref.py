@@ -76,6 +76,19 @@ def lib():
                                       C.c_int, C.c_int, _dp, C.POINTER(C.c_double),
                                       C.POINTER(C.c_double)]
             L.ref_hmholtz.restype = C.c_int
+            L.ref_proj_create.argtypes = [_vp, C.c_int]
+            L.ref_proj_create.restype = _vp
+            L.ref_proj_free.argtypes = [_vp]
+            L.ref_proj_m.argtypes = [_vp]
+            L.ref_proj_m.restype = C.c_int
+            L.ref_proj_x.argtypes = [_vp, C.c_int]
+            L.ref_proj_x.restype = C.POINTER(C.c_double)
+            L.ref_proj_b.argtypes = [_vp, C.c_int]
+            L.ref_proj_b.restype = C.POINTER(C.c_double)
+            L.ref_hsolve.argtypes = [_vp, _vp, _dp, _dp, _dp, _dp, _dp, _dp, C.c_double, C.c_int,
+                                     C.c_int, C.c_int, _dp, C.POINTER(C.c_double),
+                                     C.POINTER(C.c_double)]
+            L.ref_hsolve.restype = C.c_int
             L.ref_local_grad3.argtypes = [_dp, _dp, _dp, _dp, C.c_int, _dp, _dp]
             L.ref_local_grad3_t.argtypes = [_dp, _dp, _dp, _dp, C.c_int, _dp, _dp, _dp]
             L.ref_mxm.argtypes = [_dp, C.c_int, _dp, C.c_int, _dp, C.c_int]
@@ -237,6 +250,43 @@ class Ops:
                                int(min(maxit, 2 ** 31 - 1)), int(min(maxcg, 2 ** 31 - 1)),
                                int(istep), _c(binv), C.byref(r0), C.byref(r2))
         return u, rhs, it, r0.value, r2.value
+
+
+class Projection:
+    """One projection space of previous solutions (navier4.f:562-1188) on an
+    Ops mesh; hsolve() is the reference's hsolve with projection on."""
+
+    def __init__(self, ops, mmx=8):
+        self.ops = ops
+        self.h = lib().ref_proj_create(ops.h, int(mmx))
+
+    def __del__(self):
+        try:
+            lib().ref_proj_free(self.h)
+        except Exception:
+            pass
+
+    @property
+    def m(self):
+        return lib().ref_proj_m(self.h)
+
+    def basis(self):
+        """(X, B) as (m, n) arrays (copies)."""
+        n, m = self.ops.n, self.m
+        X = np.array([np.ctypeslib.as_array(lib().ref_proj_x(self.h, k), (n,)) for k in range(m)])
+        B = np.array([np.ctypeslib.as_array(lib().ref_proj_b(self.h, k), (n,)) for k in range(m)])
+        return X.reshape(m, n), B.reshape(m, n)
+
+    def hsolve(self, r, h1, h2, vmk, vml, binv, tli, maxit=10 ** 9, maxcg=900, istep=0):
+        """Returns (u, r_after, niter, rbn0, rbn2)."""
+        o = self.ops
+        u = np.zeros(o.n)
+        r = np.array(r, dtype=np.float64, copy=True)
+        r0, r2 = C.c_double(0), C.c_double(0)
+        it = lib().ref_hsolve(o.h, self.h, u, r, _c(h1), _c(h2), _c(vmk), _c(vml), float(tli),
+                              int(min(maxit, 2 ** 31 - 1)), int(min(maxcg, 2 ** 31 - 1)),
+                              int(istep), _c(binv), C.byref(r0), C.byref(r2))
+        return u, r, it, r0.value, r2.value
 
 
 def local_grad3(u, D):

@@ -192,3 +192,32 @@ def test_threaded_oracle_matches_serial(oracle):
     a1 = P1["ops"].axhelm(u, np.ones(n), np.zeros(n))
     a4 = P4["ops"].axhelm(u, np.ones(n), np.zeros(n))
     assert np.array_equal(a1, a4)  # per-element work is order-independent
+
+
+def test_projection_restatement_properties(oracle):
+    """project1/project2 (navier4.f:636-1187): after a sequence of hsolve calls
+    the space is B-orthonormal in (x, y)_mult, the projected right-hand side
+    is orthogonal to it, and every returned u solves the masked system."""
+    from conftest import rng_unit_vector
+    P = oracle.box_problem(5, 2, 2, 3, v=rng_unit_vector(13))
+    ops, n = P["ops"], P["n"]
+    proj = oracle.Projection(ops, 4)
+    rng = np.random.default_rng(13)
+    f0, f1 = rng.standard_normal(n), rng.standard_normal(n)
+    h1, h2 = np.ones(n), np.full(n, 50.0)
+    its = []
+    for t in range(7):
+        f = f0 + np.cos(0.5 * t) * f1 + 1e-2 * np.random.default_rng(t).standard_normal(n)
+        rhs = P["bm1"] * ops.dssum(f * P["mult"])
+        u, r, it, r0, r2 = proj.hsolve(rhs, h1, h2, P["mask"], P["mult"], P["binv"], 1e-11)
+        its.append(it)
+        w = P["mult"]
+        if proj.m > 1 and t < 6:
+            X, B = proj.basis()
+            G = (X * w) @ B.T
+            assert np.abs(G - np.eye(len(G))).max() < 1e-12
+        # u solves mask * dssum(A u) = mask * dssum(rhs*mask) (hsolve's rhs)
+        b = ops.dssum(rhs * P["mask"])
+        res = ops.dssum(ops.axhelm(u, h1, h2)) * P["mask"] - b
+        assert np.sqrt(np.sum(P["mult"] * P["binv"] * res ** 2) / P["bm1"].sum()) < 1e-9
+    assert proj.m == 4 and its[-1] < its[0]
