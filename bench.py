@@ -371,6 +371,7 @@ def run_gpu(args):
                        "tol": args.tol, "outer_steps": outer, "inner_iterations": inner,
                        "inner_rate_dof_iters_per_s": allsum(pg, n * sum(inner)) / rmx["T"],
                        "rel_error_vs_fp64_solution": err64,
+                       "gs_shape_fp32": lib.gs_shape(1)[:2],
                        "operator_shape": {"fp64": lib.ax_shape(0)[:2], "fp32": lib.ax_shape(1)[:2],
                                           "note": "(kind 0 plain / 1 TMA, elements per block), "
                                                   "autotuned on the first solve"},

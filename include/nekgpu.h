@@ -310,6 +310,17 @@ int nekgpu_autotune(const int64_t *handle, const int *precision, const int *h1mo
                     const int *h2mode, int *kind, int *epb, double *ms);
 int nekgpu_ax_shape(const int64_t *handle, const int *precision, int *kind, int *epb,
                     double *ms);
+/* Boundary-group (dssum) kernel of the PCG iteration: threads per block and
+ * the shift applied to the default groups per thread (2^gshift).  The FP32
+ * inner solve's shape is tuned with the operator's (its rho does not depend
+ * on it); the FP64 solve keeps the default (its boundary rho partials are
+ * per block). */
+int nekgpu_gs_shape(const int64_t *handle, const int *precision, int *threads, int *gshift,
+                    double *ms);
+/* Pins the FP32 boundary-group kernel shape (threads 128, 256 or 512; gshift
+ * -1, 0 or 1); *threads = 0 returns to the default / tuning.  A pinned
+ * operator shape (nekgpu_set_ax_shape) skips the tuning of both. */
+int nekgpu_set_gs_shape(const int64_t *handle, const int *threads, const int *gshift);
 int nekgpu_set_ax_shape(const int64_t *handle, const int *precision, const int *kind,
                         const int *epb);
 int nekgpu_ax_candidates(const int64_t *handle, const int *precision, int *kinds, int *epbs,

@@ -68,6 +68,8 @@ SIGNATURES = {
     "nekgpu_proj_count": [_I64P, _IP, _IP],
     "nekgpu_batch_set_shape": [_I64P, _IP, _IP],
     "nekgpu_ax_shape": [_I64P, _IP, _IP, _IP, _DP],
+    "nekgpu_gs_shape": [_I64P, _IP, _IP, _IP, _DP],
+    "nekgpu_set_gs_shape": [_I64P, _IP, _IP],
     "nekgpu_set_ax_shape": [_I64P, _IP, _IP, _IP],
     "nekgpu_ax_candidates": [_I64P, _IP, _P, _P, _IP],
     "nekgpu_cggo_mixed_dev": [_I64P, _P, _P, _P, _P, _P, _P, _IP, _DP, _IP, _IP, _P, _DP, _IP, _IP,

@@ -386,6 +386,9 @@ int nekgpu_set_option(const int64_t* handle, const int* key, const int* value) {
     case NEKGPU_OPT_AUTOTUNE:
       H->autotune = (*value != 0);
       H->mesh.ax_sel[0] = H->mesh.ax_sel[1] = AxShapeSel();
+      H->mesh.gs.cls_tuned[0] = H->mesh.gs.cls_tuned[1] = GsClasses{};
+      H->mesh.gs_gshift[0] = H->mesh.gs_gshift[1] = 0;
+      H->mesh.gs_ms[0] = H->mesh.gs_ms[1] = 0.f;
       break;
     case NEKGPU_OPT_GRAPH: H->use_graph = (*value != 0); break;
     case NEKGPU_OPT_MIXED_MODE:
@@ -877,6 +880,38 @@ int nekgpu_autotune(const int64_t* handle, const int* precision, const int* h1mo
   if (kind) *kind = sh.kind;
   if (epb) *epb = sh.epb;
   if (ms) *ms = sh.ms;
+  return NEKGPU_OK;
+}
+
+int nekgpu_gs_shape(const int64_t* handle, const int* precision, int* threads, int* gshift,
+                    double* ms) {
+  GET_HANDLE(handle);
+  NEED_MESH();
+  if (!precision || (*precision != 0 && *precision != 1))
+    return fail(H, NEKGPU_EINVAL, "precision must be 0 or 1");
+  const GsClasses& c = H->mesh.gs.cls_tuned[*precision];
+  const bool tuned = c.threads > 0;
+  if (threads) *threads = tuned ? c.threads : H->mesh.gs.cls.threads;
+  if (gshift) *gshift = tuned ? H->mesh.gs_gshift[*precision] : 0;
+  if (ms) *ms = tuned ? H->mesh.gs_ms[*precision] : 0.0;
+  return NEKGPU_OK;
+}
+
+int nekgpu_set_gs_shape(const int64_t* handle, const int* threads, const int* gshift) {
+  GET_HANDLE(handle);
+  NEED_MESH();
+  if (!threads || !gshift) return fail(H, NEKGPU_EINVAL, "null argument");
+  if (*threads == 0) {  // back to the default / tuning
+    H->mesh.gs.cls_tuned[1] = GsClasses{};
+    H->mesh.gs_gshift[1] = 0;
+    H->mesh.gs_ms[1] = 0.f;
+    return NEKGPU_OK;
+  }
+  if ((*threads != 128 && *threads != 256 && *threads != 512) || *gshift < -1 || *gshift > 1)
+    return fail(H, NEKGPU_EINVAL, "threads must be 128, 256 or 512 and gshift -1, 0 or 1");
+  H->mesh.gs.cls_tuned[1] = gs_shape(H->mesh.gs.cls, *threads, *gshift);
+  H->mesh.gs_gshift[1] = *gshift;
+  H->mesh.gs_ms[1] = 0.f;
   return NEKGPU_OK;
 }
 

@@ -138,10 +138,7 @@ int gs_setup(GsMaps& gs, const int64_t* glo_num, int64_t n, int nx1, std::string
       C.ioff[cur] = (int)nix.size();
     }
     nst.push_back((int)nix.size());
-    C.boff[0] = 0;
-    for (int k = 0; k < kGsClasses; ++k)
-      C.boff[k + 1] = C.boff[k] + (C.cnt[k] + kGsThreads * gs_groups_per_thread(k) - 1) /
-                                      (kGsThreads * gs_groups_per_thread(k));
+    C = gs_shape(C, kGsThreads, 0);
     bst.swap(nst);
     bix.swap(nix);
   }
@@ -180,6 +177,8 @@ void gs_free(GsMaps& gs) {
   gs.skip = nullptr;
   gs.start = gs.idx = gs.bstart = gs.bidx = nullptr;
   gs.nseg = gs.nidx = gs.nbseg = gs.nbidx = 0;
+  gs.cls = GsClasses{};
+  gs.cls_tuned[0] = gs.cls_tuned[1] = GsClasses{};  // tuned shapes belong to the old maps
   gs.h_start.clear();
   gs.h_idx.clear();
 }
@@ -192,13 +191,32 @@ void gs_op(const GsMaps& gs, T* u, int op, cudaStream_t s) {
       u, gs.start, gs.idx, gs.nseg, op);
 }
 
+GsClasses gs_shape(const GsClasses& cls, int threads, int gshift) {
+  GsClasses C = cls;
+  C.threads = threads;
+  C.boff[0] = 0;
+  for (int k = 0; k < kGsClasses; ++k) {
+    C.g[k] = gs_groups_shifted(k, gshift);
+    C.boff[k + 1] = C.boff[k] + (C.cnt[k] + threads * C.g[k] - 1) / (threads * C.g[k]);
+  }
+  return C;
+}
+
 template <typename T>
 void gs_cg(const GsMaps& gs, T* w, const T* p, const T* segmask, const T* segmsum,
-           CgScalars* cg, double* partialA, int nA, double* partialB, cudaStream_t s, bool rho) {
-  const int nb = gs_cg_blocks(gs);
+           CgScalars* cg, double* partialA, int nA, double* partialB, cudaStream_t s, bool rho,
+           const GsClasses* shape) {
+  const GsClasses& C = (shape && shape->threads > 0) ? *shape : gs.cls;
+  const int nb = gs_cg_blocks(C);
+  // the shape's groups-per-thread shift, recovered from class 0 (4 by default)
+  const int g0 = C.g[0];
+  auto kern = rho ? (g0 <= 2 ? gs_cg_kernel<T, -1, true>
+                             : g0 >= 8 ? gs_cg_kernel<T, 1, true> : gs_cg_kernel<T, 0, true>)
+                  : (g0 <= 2 ? gs_cg_kernel<T, -1, false>
+                             : g0 >= 8 ? gs_cg_kernel<T, 1, false> : gs_cg_kernel<T, 0, false>);
   count_launch();
-  gs_cg_kernel<T><<<nb, kGsThreads, 0, s>>>(w, p, gs.bstart, gs.bidx, gs.cls, segmask, segmsum,
-                                            cg, partialA, nA, partialB, rho ? 1 : 0);
+  kern<<<nb, C.threads, 0, s>>>(w, p, gs.bstart, gs.bidx, C, segmask, segmsum, cg, partialA, nA,
+                                partialB);
 }
 
 template <typename T>
@@ -213,9 +231,11 @@ void gs_cg_weights(const GsMaps& gs, const T* mask, const T* mult, T* segmask, T
 template void gs_op<double>(const GsMaps&, double*, int, cudaStream_t);
 template void gs_op<float>(const GsMaps&, float*, int, cudaStream_t);
 template void gs_cg<double>(const GsMaps&, double*, const double*, const double*, const double*,
-                            CgScalars*, double*, int, double*, cudaStream_t, bool);
+                            CgScalars*, double*, int, double*, cudaStream_t, bool,
+                            const GsClasses*);
 template void gs_cg<float>(const GsMaps&, float*, const float*, const float*, const float*,
-                           CgScalars*, double*, int, double*, cudaStream_t, bool);
+                           CgScalars*, double*, int, double*, cudaStream_t, bool,
+                           const GsClasses*);
 template void gs_cg_weights<double>(const GsMaps&, const double*, const double*, double*, double*,
                                     int*, cudaStream_t);
 template void gs_cg_weights<float>(const GsMaps&, const float*, const float*, float*, float*,

@@ -30,6 +30,8 @@ struct GsClasses {
   int soff[kGsClasses];     // first group index of the class
   int ioff[kGsClasses];     // first idx entry of the class (multiple of 4)
   int boff[kGsClasses + 1]; // first block of the class in the launch
+  int g[kGsClasses];        // groups per thread of the class (1, 2, 4 or 8)
+  int threads;              // threads per block
 };
 
 struct GsMaps {
@@ -40,7 +42,8 @@ struct GsMaps {
   int nbseg = 0, nbidx = 0;  // all boundary groups
   int* bstart = nullptr;
   int* bidx = nullptr;
-  GsClasses cls{};
+  GsClasses cls{};          // launch shape of the batched solver and the default
+  GsClasses cls_tuned[2]{};  // [0] FP64, [1] FP32 single-problem PCG (threads 0: = cls)
   // 1 for element-interior points that the caller's numbering shares (id != 0):
   // the fused operator must leave them to the boundary-group kernel.
   // nullptr when there are none (the reference's numbering).
@@ -66,7 +69,7 @@ void gs_op(const GsMaps& gs, T* u, int op, cudaStream_t s);
 template <typename T>
 void gs_cg(const GsMaps& gs, T* w, const T* p, const T* segmask, const T* segmsum,
            CgScalars* cg, double* partialA, int nA, double* partialB, cudaStream_t s,
-           bool rho = true);
+           bool rho = true, const GsClasses* shape = nullptr);
 
 // Per-segment mask value (mask at the first copy) and sum of mult over the
 // copies, for the bound maps.  Returns via `nonuniform` (device int) whether
@@ -75,13 +78,20 @@ template <typename T>
 void gs_cg_weights(const GsMaps& gs, const T* mask, const T* mult, T* segmask, T* segmsum,
                    int* nonuniform, cudaStream_t s);
 
-constexpr int kGsThreads = 256;
-// Groups per thread in the PCG-form kernel, by class (1, 2, 4, 8 copies,
-// other): about 8 gathers in flight per thread.
+constexpr int kGsThreads = 256;     // default block of the PCG-form kernel
+constexpr int kGsMaxThreads = 512;  // largest block the autotuner tries
+// Default groups per thread in the PCG-form kernel, by class (1, 2, 4, 8
+// copies, other): about 8 gathers in flight per thread.
 __host__ __device__ constexpr int gs_groups_per_thread(int cls) {
   return cls <= 1 ? 4 : cls == 2 ? 2 : 1;
 }
-// Blocks of the PCG-form kernel: kGsGroups groups per thread, classes block-aligned.
-inline int gs_cg_blocks(const GsMaps& gs) { return gs.cls.boff[kGsClasses] > 0 ? gs.cls.boff[kGsClasses] : 1; }
+// Launch shape of the PCG-form kernel: `threads` per block and the default
+// groups per thread scaled by 2^gshift (clamped to 1..8; the "other" class
+// keeps 1), classes block-aligned.  Returns the shape; cls's counts and
+// offsets are kept.
+GsClasses gs_shape(const GsClasses& cls, int threads, int gshift);
+// Blocks of the PCG-form kernel for a shape.
+inline int gs_cg_blocks(const GsClasses& c) { return c.boff[kGsClasses] > 0 ? c.boff[kGsClasses] : 1; }
+inline int gs_cg_blocks(const GsMaps& gs) { return gs_cg_blocks(gs.cls); }
 
 }  // namespace nekgpu

@@ -90,7 +90,15 @@ __device__ __forceinline__ void gs_groups(const int* __restrict__ cidx, int s0, 
 // contiguous (a block runs one class).  Warp 0 also folds a strided slice of
 // the operator's interior partials into the block's partial; the last block
 // sets rho and alpha = rtz1 / rho.
-template <typename T>
+// Groups per thread of class k under a groups-per-thread shift (the host's
+// gs_shape computes the same numbers for the block offsets).
+__host__ __device__ constexpr int gs_groups_shifted(int k, int gshift) {
+  return k >= kGsClasses - 1 ? 1
+         : gshift >= 0       ? ((gs_groups_per_thread(k) << gshift) > 8 ? 8 : (gs_groups_per_thread(k) << gshift))
+                             : ((gs_groups_per_thread(k) >> (-gshift)) < 1 ? 1 : (gs_groups_per_thread(k) >> (-gshift)));
+}
+
+template <typename T, int GSH = 0, bool RHO = true>
 __device__ __forceinline__ void gs_cg_body(T* __restrict__ w, const T* __restrict__ p,
                                            const int* __restrict__ start,
                                            const int* __restrict__ idx, const GsClasses& cls,
@@ -98,24 +106,24 @@ __device__ __forceinline__ void gs_cg_body(T* __restrict__ w, const T* __restric
                                            const T* __restrict__ segmsum, CgScalars* cg,
                                            const double* __restrict__ partialA, int nA,
                                            double* __restrict__ partialB, int blk, int nblk,
-                                           double* red, int* am_last_s, bool rho = true) {
+                                           double* red, int* am_last_s) {
+  constexpr bool rho = RHO;
   int& am_last = *am_last_s;
   int k = 0;
   while (k < kGsClasses - 1 && blk >= cls.boff[k + 1]) ++k;
-  const int G = gs_groups_per_thread(k);
+  const int G = cls.g[k];  // = gs_groups_shifted(k, GSH)
   const int s0 = (blk - cls.boff[k]) * blockDim.x * G + threadIdx.x;
   const int* ci = idx + cls.ioff[k];
   const int goff = cls.soff[k], cnt = cls.cnt[k];
   CompAcc<T> acc;
-#define NEKGPU_GS_CLASS(C, GG)                                                              \
-  if (rho) gs_groups<T, C, GG, true>(ci, s0, blockDim.x, cnt, goff, w, p, segmask, segmsum, acc); \
-  else gs_groups<T, C, GG, false>(ci, s0, blockDim.x, cnt, goff, w, p, segmask, segmsum, acc);
+#define NEKGPU_GS_CG(C, GG) \
+  gs_groups<T, C, GG, RHO>(ci, s0, blockDim.x, cnt, goff, w, p, segmask, segmsum, acc);
   switch (k) {
-    case 0: NEKGPU_GS_CLASS(1, 4) break;
-    case 1: NEKGPU_GS_CLASS(2, 4) break;
-    case 2: NEKGPU_GS_CLASS(4, 2) break;
-    case 3: NEKGPU_GS_CLASS(8, 1) break;
-#undef NEKGPU_GS_CLASS
+    case 0: NEKGPU_GS_CG(1, gs_groups_shifted(0, GSH)) break;
+    case 1: NEKGPU_GS_CG(2, gs_groups_shifted(1, GSH)) break;
+    case 2: NEKGPU_GS_CG(4, gs_groups_shifted(2, GSH)) break;
+    case 3: NEKGPU_GS_CG(8, gs_groups_shifted(3, GSH)) break;
+#undef NEKGPU_GS_CG
     default:
       for (int q = 0; q < G; ++q) {
         const int sl = s0 + q * blockDim.x;
@@ -126,8 +134,43 @@ __device__ __forceinline__ void gs_cg_body(T* __restrict__ w, const T* __restric
         for (int c = a + 1; c < b; ++c) t = t + w[idx[c]];
         t = t * segmask[g];
         for (int c = a; c < b; ++c) w[idx[c]] = t;
-        if (rho) acc.add(t * p[idx[a]] * segmsum[g]);
+        if constexpr (RHO) acc.add(t * p[idx[a]] * segmsum[g]);
       }
+  }
+  if constexpr (!rho) {
+    // The operator's per-element partials hold all of rho.  Warp 0 folds a
+    // strided slice of them and the last block's warp 0 sums the block
+    // partials in lane order; no block-wide barrier, so the other warps leave
+    // as soon as their groups are done.
+    // Warp 0 of block b folds the fixed chunks b, b + nblk, ... of
+    // kFoldChunk partials (lane l takes every 32nd one), so that the sum does
+    // not depend on the block count whenever nblk covers every chunk.
+    if (threadIdx.x >= 32) return;
+    constexpr int kFoldChunk = 1024;
+    double pa = 0.0;
+    for (int c0 = blk * kFoldChunk; c0 < nA; c0 += nblk * kFoldChunk)
+      for (int q = c0 + threadIdx.x; q < min(c0 + kFoldChunk, nA); q += 32)
+        pa += __ldcg(partialA + q);
+    pa = warp_sum(pa);
+    unsigned int last = 0;
+    if (threadIdx.x == 0) {
+      partialB[blk] = pa;
+      __threadfence();
+      const unsigned int ticket = atomicAdd(&cg->counter[0], 1u);
+      last = (ticket == (unsigned int)nblk - 1) ? 1u : 0u;
+    }
+    last = __shfl_sync(0xffffffffu, last, 0);
+    if (!last) return;
+    __threadfence();
+    double pb = 0.0;
+    for (int q = threadIdx.x; q < nblk; q += 32) pb += __ldcg(partialB + q);
+    pb = warp_sum(pb);
+    if (threadIdx.x == 0) {
+      cg->rho = pb;
+      cg->alpha = cg->rtz1 / pb;
+      cg->counter[0] = 0u;
+    }
+    return;
   }
   double dot = block_sum_comp(acc, red);  // thread 0
   if (threadIdx.x < 32) {
@@ -154,18 +197,17 @@ __device__ __forceinline__ void gs_cg_body(T* __restrict__ w, const T* __restric
   }
 }
 
-template <typename T>
-__global__ void __launch_bounds__(kGsThreads)
+template <typename T, int GSH, bool RHO>
+__global__ void __launch_bounds__(kGsMaxThreads)
     gs_cg_kernel(T* __restrict__ w, const T* __restrict__ p, const int* __restrict__ start,
                  const int* __restrict__ idx, const GsClasses cls,
                  const T* __restrict__ segmask, const T* __restrict__ segmsum, CgScalars* cg,
-                 const double* __restrict__ partialA, int nA, double* __restrict__ partialB,
-                 int rho) {
+                 const double* __restrict__ partialA, int nA, double* __restrict__ partialB) {
   __shared__ double red[32];
   __shared__ int am_last;
   if (cg->done) return;
-  gs_cg_body<T>(w, p, start, idx, cls, segmask, segmsum, cg, partialA, nA, partialB, blockIdx.x,
-                gridDim.x, red, &am_last, rho != 0);
+  gs_cg_body<T, GSH, RHO>(w, p, start, idx, cls, segmask, segmsum, cg, partialA, nA, partialB,
+                          blockIdx.x, gridDim.x, red, &am_last);
 }
 
 }  // namespace nekgpu

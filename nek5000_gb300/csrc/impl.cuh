@@ -70,6 +70,10 @@ struct Mesh {
   bool use_tma = true;     // TMA-staged operator where lx1 and alignment allow
   std::vector<double> h_D;  // lx1*lx1 row-major (host copy)
   AxShapeSel ax_sel[2];     // [0] FP64, [1] FP32 (see tune.cu)
+  // boundary-group kernel shape tuned per precision (gs.cls_tuned), as
+  // (threads, groups-per-thread shift) and its launch time
+  int gs_gshift[2] = {0, 0};
+  float gs_ms[2] = {0.f, 0.f};
 };
 
 // Coefficient descriptor after uniformity detection.

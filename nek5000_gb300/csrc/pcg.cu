@@ -388,7 +388,8 @@ PcgResult pcg_prepare(Handle& h, PcgWork<T>& wk, T* x, const T* f, const Coef<T>
   const int64_t n = m.n;
   cudaStream_t s = h.stream;
   const int nA = axhelm_blocks(m.nx1, m.nel);
-  const int nB = std::max(gs_cg_blocks(m.gs), 1);
+  const int nB = std::max(
+      std::max(gs_cg_blocks(m.gs), gs_cg_blocks(m.gs.cls_tuned[sizeof(T) == 4 ? 1 : 0])), 1);
   const int nC = vec_blocks(n);
   if (wk.r.ensure(n) || wk.w.ensure(n) || wk.p.ensure(n) || wk.d.ensure(n) ||
       wk.segmask.ensure(m.gs.nbseg) || wk.segmsum.ensure(m.gs.nbseg) ||
@@ -561,7 +562,7 @@ PcgResult pcg_iterate(Handle& h, const OpData<T>& op, PcgWork<T>& wk, T* x, cons
       if (e != cudaSuccess) return e;
       // FP32: rho came whole from the operator (AxArgs::allrho)
       gs_cg<T>(m.gs, wk.w.ptr, wk.p.ptr, wk.segmask.ptr, wk.segmsum.ptr, h.cg, h.partialA.ptr,
-               nAb, h.partialB.ptr, s, sizeof(T) != 4);
+               nAb, h.partialB.ptr, s, sizeof(T) != 4, &m.gs.cls_tuned[sizeof(T) == 4 ? 1 : 0]);
       if (h.timing) cudaEventRecord(h.ax_ev[4 * q + 2], s);
       launch_C<T>(h, wk, x, mult, binv, exact, false);
       if (h.timing) cudaEventRecord(h.ax_ev[4 * q + 3], s);
@@ -580,7 +581,9 @@ PcgResult pcg_iterate(Handle& h, const OpData<T>& op, PcgWork<T>& wk, T* x, cons
     key.ints[1] = c.h1mode;
     key.ints[2] = c.h2mode;
     const AxShapeSel& sh = m.ax_sel[sizeof(T) == 4 ? 1 : 0];
-    key.ints[3] = (int)exact + 4 * (int)m.use_tma + 8 * (sh.kind + 1) + 32 * sh.epb;
+    const GsClasses& gc = m.gs.cls_tuned[sizeof(T) == 4 ? 1 : 0];
+    key.ints[3] = (int)exact + 4 * (int)m.use_tma + 8 * (sh.kind + 1) + 32 * sh.epb +
+                  4096 * (gc.threads / 32) + 65536 * (m.gs_gshift[sizeof(T) == 4 ? 1 : 0] + 4);
     key.ints[4] = chunk;
     key.ints[5] = m.nel;
     key.dbl[0] = (double)c.h1s;

@@ -61,10 +61,14 @@ namespace {
 using Key = std::tuple<int, int, int, int, int, int, int>;  // dev, nx, nel, prec, h1m, h2m, tma
 std::mutex g_mu;
 std::map<Key, AxShapeSel> g_cache;
+std::map<Key, std::pair<int, int>> g_gs_cache;  // boundary-group kernel (threads, gshift)
 
 constexpr int kWarm = 2, kReps = 5;
 
 }  // namespace
+
+template <typename T>
+int tune_gs(Handle& h, PcgWork<T>& wk);
 
 template <typename T>
 int tune_operator(Handle& h, const OpData<T>& op, PcgWork<T>& wk, const Coef<T>& c) {
@@ -77,6 +81,11 @@ int tune_operator(Handle& h, const OpData<T>& op, PcgWork<T>& wk, const Coef<T>&
     auto it = g_cache.find(key);
     if (it != g_cache.end()) {
       m.ax_sel[prec] = it->second;
+      auto gt = g_gs_cache.find(key);
+      if (gt != g_gs_cache.end()) {
+        m.gs.cls_tuned[prec] = gs_shape(m.gs.cls, gt->second.first, gt->second.second);
+        m.gs_gshift[prec] = gt->second.second;
+      }
       return 0;
     }
   }
@@ -141,8 +150,89 @@ int tune_operator(Handle& h, const OpData<T>& op, PcgWork<T>& wk, const Coef<T>&
     return -3;
   }
   m.ax_sel[prec] = best;
+  const int gst = tune_gs<T>(h, wk);
+  if (gst) return gst;
   std::lock_guard<std::mutex> lk(g_mu);
   g_cache[key] = best;
+  if (prec == 1) g_gs_cache[key] = {m.gs.cls_tuned[prec].threads, m.gs_gshift[prec]};
+  return 0;
+}
+
+// The boundary-group kernel's shape: threads per block and groups per thread
+// (times 2^gshift of the defaults), timed like the operator's on zeroed data.
+// Every shape computes the same sums in the same order per group; the rho
+// partials it adds are per block, so the FP64 rho (boundary part) can change
+// in its last bits with the shape -- the FP64 shape is therefore left at the
+// default, and only the FP32 inner solve (whose rho comes from the operator)
+// is tuned.
+template <typename T>
+int tune_gs(Handle& h, PcgWork<T>& wk) {
+  Mesh& m = h.mesh;
+  const int prec = sizeof(T) == 4 ? 1 : 0;
+  if (prec == 0) return 0;
+  const int64_t n = m.n;
+  cudaStream_t s = h.stream;
+  if (wk.w.ensure(n) || wk.p.ensure(n) || wk.segmask.ensure(m.gs.nbseg) ||
+      wk.segmsum.ensure(m.gs.nbseg) || h.partialA.ensure(m.nel) || h.cg_tune.ensure(1)) {
+    set_error(h, "autotune: device allocation failed");
+    return -4;
+  }
+  cudaMemsetAsync(wk.w.ptr, 0, n * sizeof(T), s);
+  cudaMemsetAsync(wk.p.ptr, 0, n * sizeof(T), s);
+  if (m.gs.nbseg) {
+    cudaMemsetAsync(wk.segmask.ptr, 0, m.gs.nbseg * sizeof(T), s);
+    cudaMemsetAsync(wk.segmsum.ptr, 0, m.gs.nbseg * sizeof(T), s);
+  }
+  cudaMemsetAsync(h.partialA.ptr, 0, m.nel * sizeof(double), s);
+  CgScalars z;
+  memset(&z, 0, sizeof(z));
+  cudaMemcpyAsync(h.cg_tune.ptr, &z, sizeof(z), cudaMemcpyHostToDevice, s);
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+    set_error(h, "autotune: cudaEventCreate failed");
+    return -3;
+  }
+  float best = 1e30f;
+  GsClasses bestc = m.gs.cls;
+  int bestg = 0;
+  for (int threads : {128, 256, 512})
+    for (int gshift : {-1, 0, 1}) {
+      const GsClasses c = gs_shape(m.gs.cls, threads, gshift);
+      if (h.partialB.ensure(gs_cg_blocks(c))) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        set_error(h, "autotune: device allocation failed");
+        return -4;
+      }
+      auto launch = [&]() {
+        gs_cg<T>(m.gs, wk.w.ptr, wk.p.ptr, wk.segmask.ptr, wk.segmsum.ptr, h.cg_tune.ptr,
+                 h.partialA.ptr, m.nel, h.partialB.ptr, s, false, &c);
+      };
+      for (int q = 0; q < kWarm; ++q) launch();
+      cudaEventRecord(e0, s);
+      for (int q = 0; q < kReps; ++q) launch();
+      cudaEventRecord(e1, s);
+      float ms = 0.f;
+      cudaError_t e = cudaEventSynchronize(e1);
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+      if (e != cudaSuccess) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        set_error(h, std::string("autotune: ") + cudaGetErrorString(e));
+        return -3;
+      }
+      ms /= kReps;
+      if (ms < best) {
+        best = ms;
+        bestc = c;
+        bestg = gshift;
+      }
+    }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  m.gs.cls_tuned[prec] = bestc;
+  m.gs_gshift[prec] = bestg;
+  m.gs_ms[prec] = best;
   return 0;
 }
 

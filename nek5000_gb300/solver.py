@@ -117,6 +117,18 @@ class NekGpu:
                                             C.byref(k), C.byref(e), C.byref(ms)))
         return k.value, e.value, ms.value
 
+    def gs_shape(self, precision: int = 1):
+        """Boundary-group kernel shape: (threads, gshift, tuned ms or 0)."""
+        t, g, ms = _cint(0), _cint(0), _cdouble(0)
+        self._check(self._L.nekgpu_gs_shape(C.byref(self._h), C.byref(_cint(precision)),
+                                            C.byref(t), C.byref(g), C.byref(ms)))
+        return t.value, g.value, ms.value
+
+    def set_gs_shape(self, threads: int, gshift: int = 0):
+        """Pin the FP32 boundary-group kernel shape (threads 0: default / tuning)."""
+        self._check(self._L.nekgpu_set_gs_shape(C.byref(self._h), C.byref(_cint(threads)),
+                                                C.byref(_cint(gshift))))
+
     def set_ax_shape(self, precision: int, kind: int, epb: int = 0):
         self._check(self._L.nekgpu_set_ax_shape(C.byref(self._h), C.byref(_cint(precision)),
                                                 C.byref(_cint(kind)), C.byref(_cint(epb))))

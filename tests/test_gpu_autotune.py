@@ -96,3 +96,29 @@ def test_autotune_picks_a_candidate(gpu_lib, oracle):
     assert lib.ax_shape(0)[2] == 0.0
     with pytest.raises(_capi.NekGpuError):
         lib.set_ax_shape(0, 1, 2)  # no TMA kernel in FP64
+
+
+@pytest.mark.parametrize("nx1", [8, 5])
+def test_fp32_boundary_group_shapes_give_identical_solves(gpu_lib, oracle, nx1):
+    """The FP32 boundary-group kernel's shape (threads per block, groups per
+    thread) changes speed only: group sums run in the same order, and the
+    operator's rho partials are folded in fixed chunks."""
+    torch = pytest.importorskip("torch")
+    P, f, h1, h2 = _problem(oracle, nx1, (4, 3, 3), 10.0, 24)
+    lib = gpu_lib(0)
+    lib.setup(P["nx1"], P["nel"], P["D"], P["g"], P["bm1"], P["glo_num"])
+    lib.set_ax_shape(1, *lib.ax_candidates(1)[0])  # operator shape pinned: no tuning
+    dev = lambda a: torch.tensor(a, device="cuda")
+    args = [dev(a) for a in (f, h1, h2, P["mask"], P["mult"])]
+    runs = []
+    for threads in (128, 256, 512):
+        for gshift in (-1, 0, 1):
+            lib.set_gs_shape(threads, gshift)
+            assert lib.gs_shape(1)[:2] == (threads, gshift)
+            x = torch.zeros(P["n"], dtype=torch.float64, device="cuda")
+            no, ni, r0, r2, rc = lib.cggo_mixed(x, *args, 1, -1e-10, 10 ** 6, 1, dev(P["binv"]))
+            assert rc == 0
+            runs.append((ni, r2, x.cpu().numpy()))
+    for ni, r2, x in runs[1:]:
+        assert ni == runs[0][0] and r2 == runs[0][1]
+        assert np.array_equal(x, runs[0][2])
