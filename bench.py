@@ -60,11 +60,14 @@ def parse():
                     help="mixed: 1 residual replacement keeping the search direction, "
                          "0 restarted FP32 PCG per outer step")
     ap.add_argument("--workload", default="helmholtz",
-                    choices=["helmholtz", "poisson-n9", "batch", "axhelm-sweep"],
+                    choices=["helmholtz", "poisson-n9", "batch", "axhelm-sweep", "hsolve"],
                     help="helmholtz: E=32^3 N=7 (default); poisson-n9: E=24^3 N=9 Poisson; "
                          "batch: 3 velocity solves + 61 uneven Poisson problems in one batch; "
-                         "axhelm-sweep: in-solve operator bandwidth at N=5,7,9, E=32^3")
+                         "axhelm-sweep: in-solve operator bandwidth at N=5,7,9, E=32^3; "
+                         "hsolve: a sequence of solves with projection onto previous solutions")
     ap.add_argument("--batch-problems", type=int, default=61)
+    ap.add_argument("--fp64-shape", default=None,
+                    help="pin the FP64 operator launch shape 'kind,epb' instead of autotuning")
     ap.add_argument("--fp32-shape", default=None,
                     help="pin the FP32 operator launch shape 'kind,epb' instead of autotuning "
                          "(kind 0 plain, 1 TMA; see nekgpu_ax_candidates)")
@@ -285,9 +288,10 @@ def run_gpu(args):
     big = 10 ** 6
     lib.set_option(2, 1)  # timing: solve-total and per-launch operator events
     lib.set_option(7, args.mixed_mode)
-    if args.fp32_shape:
-        kind, epb = (int(v) for v in args.fp32_shape.split(","))
-        lib.set_ax_shape(1, kind, epb)
+    for prec, spec in ((0, args.fp64_shape), (1, args.fp32_shape)):
+        if spec:
+            kind, epb = (int(v) for v in spec.split(","))
+            lib.set_ax_shape(prec, kind, epb)
 
     def fp64():
         it, r0, r2, rc = lib.cggo(x, f, h1, h2, mask, mult, 1, -args.tol, big, 1, binv, maxcg=big)
@@ -584,6 +588,79 @@ def run_sweep(args):
                           "sweep": rows}), flush=True)
 
 
+def run_hsolve(args):
+    """Time stepping with projection (hsolve, navier4.f:562): a sequence of
+    FP64 Helmholtz solves (E=k^3, N, h1 = 1, h2 = 1500 as for a velocity step
+    with dt = 1e-3) whose right-hand sides vary smoothly, each to the absolute
+    tolerance tol * rinit of the first, once through nekgpu_hsolve_dev
+    (projection space of 8) and once through plain cggo."""
+    import torch
+    ws, rank, local, pg = dist_setup(args.gpus)
+    torch.cuda.set_device(local)
+    from nek5000_gb300 import NekGpu, mesh
+    from nek5000_gb300 import build as nb
+    nb.build()
+    M = mesh.box_mesh(args.N, args.k, args.k, args.k, seed=3)
+    n = M["n"]
+    nglob = int(M["lattice"].max()) + 1
+    lib = NekGpu(local)
+    lib.setup(M["lx1"], M["nel"], M["D"], M["g"], M["bm1"], M["glo_num"])
+    dev = lambda a: torch.tensor(a, device=f"cuda:{local}")
+    h1, h2 = dev(np.ones(n)), dev(np.full(n, 1500.0))
+    mask, mult, binv = dev(M["mask"]), dev(M["mult"]), dev(M["binv"])
+    rng = np.random.default_rng(3)
+    fs = [rng.standard_normal(nglob)[M["lattice"]] for _ in range(3)]
+    bm1 = dev(M["bm1"])
+    steps = max(args.steps, 1) * 10
+
+    def rhs(t):  # local (unassembled) right-hand side, as hsolve takes it
+        f = fs[0] + np.sin(0.05 * t) * fs[1] + 1e-3 * t * fs[2]
+        return dev(M["bm1"] * f)
+
+    rinit = None
+    out = {}
+    for mode in ("projection", "plain"):
+        lib.proj_setup(0, 8)
+        its, ms = [], []
+        for t in range(steps + args.warmup):
+            r = rhs(t)
+            if rinit is None:
+                ra = lib.dssum(r.clone()) * mask
+                rinit = float(torch.sqrt(torch.sum(mult * binv * ra * ra) / torch.sum(bm1)))
+            tol = args.tol * rinit
+            u = torch.zeros(n, dtype=torch.float64, device=f"cuda:{local}")
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            if mode == "projection":
+                it, r0, r2, m, rc = lib.hsolve("VELX", u, r, h1, h2, mask, mult, 1, tol, 10 ** 6,
+                                               1, binv, space=0, maxcg=10 ** 6)
+            else:  # hmholtz's right-hand side: dssum, then mask
+                r = lib.dssum(r) * mask
+                it, r0, r2, rc = lib.cggo(u, r, h1, h2, mask, mult, 1, tol, 10 ** 6, 1, binv,
+                                          maxcg=10 ** 6)
+            torch.cuda.synchronize()
+            if t >= args.warmup:
+                its.append(it)
+                ms.append(1e3 * (time.perf_counter() - t0))
+        out[mode] = {"iterations": its, "ms_per_solve": sum(ms) / len(ms),
+                     "total_s": sum(ms) / 1e3}
+    if rank == 0:
+        sp = out["plain"]["total_s"] / out["projection"]["total_s"]
+        print(json.dumps({"metric": "time-stepping Helmholtz solves with projection onto "
+                                    "previous solutions (hsolve)",
+                          "value": out["projection"]["ms_per_solve"], "unit": "ms/solve",
+                          "higher_is_better": False, "steps": steps, "warmup": args.warmup,
+                          "n_gpus": ws, "dtype": "f64", "data": "synthetic",
+                          "config": {"workload": f"helmholtz E={args.k}^3 N={args.N} h1=1 "
+                                                 "h2=1500 dirichlet-all, rhs f0 + sin(0.05t) f1 "
+                                                 "+ 1e-3 t f2", "n_points": n,
+                                     "tol": f"{args.tol:g} * rinit (absolute)",
+                                     "projection_space": 8},
+                          "projection": out["projection"], "plain_cggo": out["plain"],
+                          "speedup_projection_vs_plain": sp}), flush=True)
+    lib.close()
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -592,6 +669,8 @@ def main():
         run_batch(args)
     elif args.workload == "axhelm-sweep":
         run_sweep(args)
+    elif args.workload == "hsolve":
+        run_hsolve(args)
     else:
         run_gpu(args)
 
