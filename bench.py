@@ -68,6 +68,8 @@ def parse():
     ap.add_argument("--batch-problems", type=int, default=61)
     ap.add_argument("--fp64-shape", default=None,
                     help="pin the FP64 operator launch shape 'kind,epb' instead of autotuning")
+    ap.add_argument("--gs-shape", default=None,
+                    help="pin the FP32 boundary-group kernel shape 'threads,gshift'")
     ap.add_argument("--fp32-shape", default=None,
                     help="pin the FP32 operator launch shape 'kind,epb' instead of autotuning "
                          "(kind 0 plain, 1 TMA; see nekgpu_ax_candidates)")
@@ -292,6 +294,9 @@ def run_gpu(args):
         if spec:
             kind, epb = (int(v) for v in spec.split(","))
             lib.set_ax_shape(prec, kind, epb)
+    if args.gs_shape:
+        threads, gshift = (int(v) for v in args.gs_shape.split(","))
+        lib.set_gs_shape(threads, gshift)
 
     def fp64():
         it, r0, r2, rc = lib.cggo(x, f, h1, h2, mask, mult, 1, -args.tol, big, 1, binv, maxcg=big)

@@ -66,27 +66,34 @@ struct AxShape {
 };
 
 // Sum of one value per thread (i,j) of an element's slab in a fixed order:
-// each row j summed over i left to right, then the row sums over j.  `buf`
-// holds NX*NX + NX doubles owned by this element; threads with own = false
-// (no element in this block slot) take part in the barriers only.  The sum is
+// each row j summed over i left to right in the field precision V, then the
+// row sums over j in FP64 (so an FP32 kernel spends only 2 NX FP64
+// operations per element).  `buf` holds element_sum_bytes<NX, V>() bytes
+// owned by this element, 8-byte aligned; threads with own = false (no
+// element in this block slot) take part in the barriers only.  The sum is
 // stored to *out by thread 0 of the element when out is not null.
-template <int NX>
-__device__ __forceinline__ void element_sum(double v, double* buf, int tx, bool own,
-                                            double* out) {
-  constexpr int NXY = NX * NX;
-  if (own) buf[tx] = v;
+template <int NX, typename V>
+__host__ __device__ constexpr int element_sum_rows_offset() {
+  return ((NX * NX * (int)sizeof(V) + 7) / 8) * 8;  // bytes to the row sums
+}
+template <int NX, typename V>
+__device__ __forceinline__ void element_sum(V v, void* buf, int tx, bool own, double* out) {
+  V* vals = reinterpret_cast<V*>(buf);
+  double* rows = reinterpret_cast<double*>(reinterpret_cast<unsigned char*>(buf) +
+                                           element_sum_rows_offset<NX, V>());
+  if (own) vals[tx] = v;
   __syncthreads();
   if (own && tx < NX) {
-    double s = buf[tx * NX];
+    V s = vals[tx * NX];
 #pragma unroll
-    for (int c = 1; c < NX; ++c) s += buf[tx * NX + c];
-    buf[NXY + tx] = s;
+    for (int c = 1; c < NX; ++c) s += vals[tx * NX + c];
+    rows[tx] = (double)s;
   }
   __syncthreads();
   if (own && tx == 0 && out) {
-    double s = buf[NXY];
+    double s = rows[0];
 #pragma unroll
-    for (int r = 1; r < NX; ++r) s += buf[NXY + r];
+    for (int r = 1; r < NX; ++r) s += rows[r];
     *out = s;
   }
 }
@@ -244,10 +251,9 @@ __device__ __forceinline__ void axhelm_body(const AxArgs<T>& a, int blk, int tx,
   }
   if constexpr (FUSED) {
     // The element's u slab (read only before the first barrier) holds the
-    // NX*NX + NX doubles of the sum: NX^2 (NX+1) sizeof(T) >= 8 NX (NX+1).
+    // sum's NX^2 values and NX doubles: NX^2 (NX+1) sizeof(T) is enough.
     (void)red;
-    element_sum<NX>((double)dot, reinterpret_cast<double*>(su), tid, ty < epb,
-                    act ? a.partial + e : nullptr);
+    element_sum<NX, T>(dot, su, tid, ty < epb, act ? a.partial + e : nullptr);
   }
 }
 

@@ -235,9 +235,8 @@ __global__ void __launch_bounds__(NX* NX* EPB) axhelm_tma_kernel(const AxArgs<T>
   if constexpr (FUSED) {
     // one partial per element, summed as axhelm.cuh's kernel does; the
     // element's staged G (read only before the second barrier) holds the
-    // NX*NX + NX doubles: 6 NX^3 sizeof(T) >= 8 NX (NX+1)
-    element_sum<NX>((double)dot, reinterpret_cast<double*>(sG + 6 * lo), threadIdx.x, true,
-                    el < ne ? a.partial + e0 + el : nullptr);
+    // sum's NX^2 values and NX doubles: 6 NX^3 sizeof(T) is enough
+    element_sum<NX, T>(dot, sG + 6 * lo, threadIdx.x, true, el < ne ? a.partial + e0 + el : nullptr);
   }
   if (tid == 0 && ok) mbar_inval(bar);
 }
