@@ -39,6 +39,7 @@ struct AxArgs {
   const T* h2;     // h2 array (h2mode 2)
   T h1s, h2s;      // uniform h1 (h1mode 0) / h2 (h2mode 1)
   int h1mode, h2mode;
+  const T* hbm;    // h2 * bm1 per point, formed once per solve (h2mode != 0), or null
   const T* D;      // lx1*lx1 row-major, D[i][j]
   int nel;
   // fused PCG operands
@@ -134,6 +135,7 @@ __device__ __forceinline__ void axhelm_body(const AxArgs<T>& a, int blk, int tx,
 
   T beta = T(0);
   if constexpr (FUSED) beta = (T)a.cg->beta;
+  const bool unit_h1 = a.h1mode == 0 && a.h1s == T(1);
 
   T ru[NX];
 #pragma unroll
@@ -196,14 +198,16 @@ __device__ __forceinline__ void axhelm_body(const AxArgs<T>& a, int blk, int tx,
     t2 = madd<EXACT>(ut, g6, t2);
     t3 = madd<EXACT>(ur, g5, t3);
     t3 = madd<EXACT>(us, g6, t3);
-    if (EXACT) {
-      t1 = mul_x(t1, h);
-      t2 = mul_x(t2, h);
-      t3 = mul_x(t3, h);
-    } else {
-      t1 *= h;
-      t2 *= h;
-      t3 *= h;
+    if (!unit_h1) {  // h1 = 1: the products are exact, skip them
+      if (EXACT) {
+        t1 = mul_x(t1, h);
+        t2 = mul_x(t2, h);
+        t3 = mul_x(t3, h);
+      } else {
+        t1 *= h;
+        t2 *= h;
+        t3 *= h;
+      }
     }
     if (ty < epb) {
       st1[k * NX * R + j * R + i] = t1;
@@ -236,9 +240,15 @@ __device__ __forceinline__ void axhelm_body(const AxArgs<T>& a, int blk, int tx,
     const int pt = k * NXY + j * NX + i;
     if (act) {
       if (a.h2mode) {  // addcol4(au,helm2,bm1,u): au + helm2*bm1*u  (:225)
-        const T hh = (a.h2mode == 1) ? a.h2s : __ldg(a.h2 + eo + pt);
-        const T bm = __ldg(a.bm1 + eo + pt);
-        s = EXACT ? add_x(s, mul_x(mul_x(hh, bm), ru[k])) : fma(hh * bm, ru[k], s);
+        T hb;
+        if (a.hbm) {
+          hb = __ldg(a.hbm + eo + pt);  // = helm2*bm1, rounded as below
+        } else {
+          const T hh = (a.h2mode == 1) ? a.h2s : __ldg(a.h2 + eo + pt);
+          const T bm = __ldg(a.bm1 + eo + pt);
+          hb = EXACT ? mul_x(hh, bm) : hh * bm;
+        }
+        s = EXACT ? add_x(s, mul_x(hb, ru[k])) : fma(hb, ru[k], s);
       }
       if constexpr (FUSED && sizeof(T) == 4) st_hint(a.au + eo + pt, s, l2_policy_evict_last());
       else a.au[eo + pt] = s;

@@ -99,6 +99,7 @@ static AxArgs<T> make_args(const Mesh& m, const OpData<T>& op, T* au, const T* u
   a.h2s = c.h2s;
   a.h1mode = c.h1mode;
   a.h2mode = c.h2mode;
+  a.hbm = c.h2mode ? c.hbm : nullptr;
   a.D = op.D;
   a.nel = m.nel;
   a.err = m.dev_err;

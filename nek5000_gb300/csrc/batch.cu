@@ -40,6 +40,8 @@ struct BDesc {
   T* x;
   const T* mult;
   const T* binv;
+  const T* md;  // folded update weights mult*d, mult*binv (pcg_solve_extras)
+  const T* mb;
   int64_t n;
   double* partialC;
   int nblkC, vec;
@@ -107,14 +109,15 @@ __global__ void __launch_bounds__(kBatchThreads)
   const BDesc<T>* d = D + pi;
   if (d->cg->done) return;
   const int blk = blockIdx.x - base[pi];
+  // the single-problem solve's fused multiply-add form: folded weights
   if (d->vec)
-    cg_update_body<T, false, FIRST, true>(d->x, const_cast<T*>(d->ax.r), d->ax.p, d->ax.au,
-                                          d->ax.d, d->mult, d->binv, d->n, d->cg, d->partialC, blk,
-                                          d->nblkC, red, &am_last);
+    cg_update_body<T, false, FIRST, true, true>(d->x, const_cast<T*>(d->ax.r), d->ax.p, d->ax.au,
+                                                d->md, d->mult, d->mb, d->n, d->cg, d->partialC,
+                                                blk, d->nblkC, red, &am_last);
   else
-    cg_update_body<T, false, FIRST, false>(d->x, const_cast<T*>(d->ax.r), d->ax.p, d->ax.au,
-                                           d->ax.d, d->mult, d->binv, d->n, d->cg, d->partialC,
-                                           blk, d->nblkC, red, &am_last);
+    cg_update_body<T, false, FIRST, false, true>(d->x, const_cast<T*>(d->ax.r), d->ax.p,
+                                                 d->ax.au, d->md, d->mult, d->mb, d->n, d->cg,
+                                                 d->partialC, blk, d->nblkC, red, &am_last);
 }
 
 // Shared memory of one operator block: epb elements of lx1 = nx.
@@ -235,15 +238,18 @@ int batch_tables(Batch& B, const std::vector<int>& ids, const std::vector<Coef<T
     d.segmsum = wk.segmsum.ptr;
     d.partialB = h.partialB.ptr;
     d.nblkB = gs_cg_blocks(m.gs);
+    a.hbm = coef[q].h2mode ? coef[q].hbm : nullptr;
     d.x = xs[q];
     d.mult = mults[q];
     d.binv = binvs[q];
+    d.md = wk.md.ptr;
+    d.mb = wk.mb.ptr;
     d.n = m.n;
     d.partialC = h.partialC.ptr;
     d.nblkC = pcg_vec_blocks(m.n);
     auto al = [](const void* p) { return ((uintptr_t)p & 15u) == 0; };
-    d.vec = al(d.x) && al(wk.r.ptr) && al(wk.p.ptr) && al(wk.w.ptr) && al(wk.d.ptr) &&
-            al(d.mult) && al(d.binv);
+    d.vec = al(d.x) && al(wk.r.ptr) && al(wk.p.ptr) && al(wk.w.ptr) && al(d.md) &&
+            al(d.mult) && al(d.mb);
     d.cg = h.cg;
     smem = std::max(smem, batch_smem<T>(m.nx1, d.epb));
     baseA[q] = (int)mapA.size();
@@ -490,6 +496,10 @@ int batch_solve_fp64(Batch& B, int np, double* const* x, const double* const* f,
       mark_done(h);
       continue;
     }
+    if (pcg_solve_extras<double>(h, h.mesh.f64, h.w64, mult[p], binv[p], c, false)) {
+      status[p] = NEKGPU_ENOMEM;
+      continue;
+    }
     ids.push_back(p);
     coef.push_back(c);
     xs.push_back(x[p]);
@@ -617,6 +627,11 @@ int batch_solve_mixed(Batch& B, int np, double* const* x, const double* const* f
         active[p] = 0;
         continue;
       }
+      if (pcg_solve_extras<float>(h, h.mesh.f32, h.w32, h.w32.mult.ptr, h.w32.binv.ptr, c32[p],
+                                  false)) {
+        status[p] = NEKGPU_ENOMEM;
+        continue;
+      }
       ids.push_back(p);
       coefs.push_back(c32[p]);
       xs.push_back(h.w32.x.ptr);
@@ -706,6 +721,11 @@ int batch_solve_mixed(Batch& B, int np, double* const* x, const double* const* f
       }
       if (trivial) {
         active[p] = 0;
+        continue;
+      }
+      if (pcg_solve_extras<float>(h, h.mesh.f32, h.w32, h.w32.mult.ptr, h.w32.binv.ptr, c32[p],
+                                  false)) {
+        status[p] = NEKGPU_ENOMEM;
         continue;
       }
       ids.push_back(p);

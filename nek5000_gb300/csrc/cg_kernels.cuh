@@ -3,13 +3,19 @@
 //
 //   x += alpha p ; r -= alpha w ; z = r d            (hmholtz.f:804-805, :730)
 //   s1 = sum z r mult ; s2 = sum mult binv r r       (vlsc3 :754, vlsc32 :758)
+//   (fused multiply-add form: s1 = sum (r r) md, s2 = sum (r r) mb with the
+//   per-solve weights md = mult d, mb = mult binv)
 //   last block: rtz1, rbn2 = sqrt(s2/vol), convergence (:778), beta (:794)
 #pragma once
 #include "common.cuh"
 
 namespace nekgpu {
 
-template <typename T, bool EXACT, bool FIRST>
+// FOLD (fused multiply-add form only): d and b arrive as the folded weights
+// md = mult d and mb = mult binv, and z r mult = (r r) md, mult binv r r =
+// (r r) mb -- the same sums with one array and three operations fewer per
+// point (z is not stored: the operator recomputes it).
+template <typename T, bool EXACT, bool FIRST, bool FOLD = false>
 struct UpdatePoint {
   // x += alpha p ; r -= alpha w ; z = r d ; s1 += z r mult ; s2 += mult binv r r
   __device__ __forceinline__ static void run(T& x, T& r, T p, T w, T d, T m, T b, T alpha,
@@ -18,7 +24,11 @@ struct UpdatePoint {
       x = madd<EXACT>(alpha, p, x);   // add2s2(x,p,alpha)   (hmholtz.f:804)
       r = madd<EXACT>(-alpha, w, r);  // add2s2(r,w,-alpha)  (hmholtz.f:805)
     }
-    if (EXACT) {
+    if (FOLD) {
+      const T rr = r * r;
+      a1.add(rr * d);  // d = mult * d
+      a2.add(rr * b);  // b = mult * binv
+    } else if (EXACT) {
       const T z = mul_x(r, d);                         // col3 (:730)
       a1.add(mul_x(mul_x(z, r), m));                   // vlsc3 (:754)
       a2.add(mul_x(mul_x(mul_x(m, b), r), r));         // vlsc32 (:758, :848)
@@ -32,7 +42,7 @@ struct UpdatePoint {
 
 // Block body of the update kernel: block `blk` of `nblk` (1-D blocks).
 // VEC: 16-byte vector accesses (all seven arrays 16-byte aligned).
-template <typename T, bool EXACT, bool FIRST, bool VEC>
+template <typename T, bool EXACT, bool FIRST, bool VEC, bool FOLD = false>
 __device__ __forceinline__ void cg_update_body(T* __restrict__ x, T* __restrict__ r,
                                                const T* __restrict__ p, const T* __restrict__ w,
                                                const T* __restrict__ d,
@@ -43,7 +53,7 @@ __device__ __forceinline__ void cg_update_body(T* __restrict__ x, T* __restrict_
   int& am_last = *am_last_s;
   const T alpha = FIRST ? T(0) : (T)cg->alpha;
   CompAcc<T> a1, a2;
-  using P = UpdatePoint<T, EXACT, FIRST>;
+  using P = UpdatePoint<T, EXACT, FIRST, FOLD>;
   const int64_t gtid = blk * (int64_t)blockDim.x + threadIdx.x;
   const int64_t stride = (int64_t)nblk * blockDim.x;
   constexpr int W = 16 / sizeof(T);
@@ -54,7 +64,7 @@ __device__ __forceinline__ void cg_update_body(T* __restrict__ x, T* __restrict_
     T xx[W], rr[W], pp[W], ww[W], dd[W], mm[W], bb[W];
     ld16(rr, r, iv);
     ld16(dd, d, iv);
-    ld16(mm, mult, iv);
+    if (!FOLD) ld16(mm, mult, iv);
     ld16(bb, binv, iv);
     if (!FIRST) {
       ld16(xx, x, iv);
@@ -73,7 +83,8 @@ __device__ __forceinline__ void cg_update_body(T* __restrict__ x, T* __restrict_
   }
   for (int64_t i = nv * W + gtid; i < n; i += stride) {
     T xi = FIRST ? T(0) : x[i], ri = r[i];
-    P::run(xi, ri, FIRST ? T(0) : p[i], FIRST ? T(0) : w[i], d[i], mult[i], binv[i], alpha, a1, a2);
+    P::run(xi, ri, FIRST ? T(0) : p[i], FIRST ? T(0) : w[i], d[i], FOLD ? T(0) : mult[i],
+           binv[i], alpha, a1, a2);
     if (!FIRST) {
       x[i] = xi;
       r[i] = ri;
@@ -129,7 +140,7 @@ __device__ __forceinline__ void cg_update_body(T* __restrict__ x, T* __restrict_
   }
 }
 
-template <typename T, bool EXACT, bool FIRST, bool VEC>
+template <typename T, bool EXACT, bool FIRST, bool VEC, bool FOLD>
 __global__ void __launch_bounds__(256)
     cg_update_kernel(T* __restrict__ x, T* __restrict__ r, const T* __restrict__ p,
                      const T* __restrict__ w, const T* __restrict__ d,
@@ -138,8 +149,8 @@ __global__ void __launch_bounds__(256)
   __shared__ double red[32];
   __shared__ int am_last;
   if (cg->done) return;
-  cg_update_body<T, EXACT, FIRST, VEC>(x, r, p, w, d, mult, binv, n, cg, partial, blockIdx.x,
-                                       gridDim.x, red, &am_last);
+  cg_update_body<T, EXACT, FIRST, VEC, FOLD>(x, r, p, w, d, mult, binv, n, cg, partial,
+                                             blockIdx.x, gridDim.x, red, &am_last);
 }
 
 }  // namespace nekgpu

@@ -83,12 +83,15 @@ struct Coef {
   T h1s = T(1), h2s = T(0);
   const T* h1 = nullptr;
   const T* h2 = nullptr;
+  const T* hbm = nullptr;  // h2 * bm1 per point when a solve has formed it (AxArgs::hbm)
 };
 
 // Work space of one PCG precision.
 template <typename T>
 struct PcgWork {
   DevBuf<T> r, w, p, d, mult, binv, mask, segmask, segmsum, x, f, h1, h2;
+  DevBuf<T> md, mb;  // folded update weights mult*d, mult*binv (fused multiply-add form)
+  DevBuf<T> hbm;     // h2 * bm1 of the current solve
 };
 
 // One projection space of previous solutions (proj.cu): X and B = A X, each
@@ -123,11 +126,11 @@ struct Handle {
   // graph cache for the PCG iteration chunk: the captured launches depend on
   // every pointer and coefficient below, so any change recaptures.
   struct GraphKey {
-    const void* ptr[12] = {};
+    const void* ptr[15] = {};
     int ints[6] = {-1, -1, -1, -1, -1, -1};
     double dbl[2] = {0, 0};
     bool operator==(const GraphKey& o) const {
-      for (int i = 0; i < 12; ++i)
+      for (int i = 0; i < 15; ++i)
         if (ptr[i] != o.ptr[i]) return false;
       for (int i = 0; i < 6; ++i)
         if (ints[i] != o.ints[i]) return false;
@@ -202,9 +205,14 @@ PcgResult pcg_prepare(Handle& h, PcgWork<T>& wk, T* x, const T* f, const Coef<T>
                       const T* mask, const T* mult, double tin, int maxiter, int istep,
                       const T* dpre, bool* trivial);
 int pcg_vec_blocks(int64_t n);
+// Per-solve data of a prepared solve: the update kernel's folded weights
+// (fused multiply-add form) and, for FP64, h2*bm1 (sets c.hbm).
+template <typename T>
+int pcg_solve_extras(Handle& h, const OpData<T>& op, PcgWork<T>& wk, const T* mult, const T* binv,
+                     Coef<T>& c, bool exact);
 // Iteration-1 check of a prepared solve (no update), then the iterations.
 template <typename T>
-void pcg_first_check(Handle& h, PcgWork<T>& wk, T* x, const T* mult, const T* binv, bool exact);
+int pcg_first_check(Handle& h, PcgWork<T>& wk, T* x, const T* mult, const T* binv, bool exact);
 template <typename T>
 PcgResult pcg_iterate(Handle& h, const OpData<T>& op, PcgWork<T>& wk, T* x, const Coef<T>& c,
                       const T* mult, const T* binv, bool exact);

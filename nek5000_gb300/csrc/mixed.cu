@@ -334,7 +334,10 @@ MixedResult mixed_solve(Handle& h, double* x, const double* f, const double* h1,
       res.status = pr.status;
       return res;
     }
-    pcg_first_check<float>(h, wk, wk.x.ptr, wk.mult.ptr, wk.binv.ptr, false);
+    if (pcg_first_check<float>(h, wk, wk.x.ptr, wk.mult.ptr, wk.binv.ptr, false)) {
+      res.status = -4;
+      return res;
+    }
     for (int upd = 1; upd <= 100000; ++upd) {
       pr = pcg_iterate<float>(h, m.f32, wk, wk.x.ptr, c32, wk.mult.ptr, wk.binv.ptr, false);
       if (pr.status && pr.status != -5) {

@@ -328,25 +328,50 @@ static cudaError_t launch_A(Handle& h, const OpData<T>& op, PcgWork<T>& wk, cons
   }
 }
 
+// The fused multiply-add form reads the folded weights wk.md = mult d and
+// wk.mb = mult binv (pcg_prepare); the exact form the reference's arrays.
 template <typename T>
 static void launch_C(Handle& h, PcgWork<T>& wk, T* x, const T* mult, const T* binv, bool exact,
                      bool first) {
   const int64_t n = h.mesh.n;
   const int nb = vec_blocks(n);
   auto al = [](const void* q) { return ((uintptr_t)q & 15u) == 0; };
-  const bool vec = al(x) && al(wk.r.ptr) && al(wk.p.ptr) && al(wk.w.ptr) && al(wk.d.ptr) &&
-                   al(mult) && al(binv);
-  auto kern = vec ? (exact ? (first ? cg_update_kernel<T, true, true, true>
-                                    : cg_update_kernel<T, true, false, true>)
-                           : (first ? cg_update_kernel<T, false, true, true>
-                                    : cg_update_kernel<T, false, false, true>))
-                  : (exact ? (first ? cg_update_kernel<T, true, true, false>
-                                    : cg_update_kernel<T, true, false, false>)
-                           : (first ? cg_update_kernel<T, false, true, false>
-                                    : cg_update_kernel<T, false, false, false>));
+  const T* dd = exact ? wk.d.ptr : wk.md.ptr;
+  const T* bb = exact ? binv : wk.mb.ptr;
+  const bool vec = al(x) && al(wk.r.ptr) && al(wk.p.ptr) && al(wk.w.ptr) && al(dd) &&
+                   al(mult) && al(bb);
+  auto kern = vec ? (exact ? (first ? cg_update_kernel<T, true, true, true, false>
+                                    : cg_update_kernel<T, true, false, true, false>)
+                           : (first ? cg_update_kernel<T, false, true, true, true>
+                                    : cg_update_kernel<T, false, false, true, true>))
+                  : (exact ? (first ? cg_update_kernel<T, true, true, false, false>
+                                    : cg_update_kernel<T, true, false, false, false>)
+                           : (first ? cg_update_kernel<T, false, true, false, true>
+                                    : cg_update_kernel<T, false, false, false, true>));
   count_launch();
-  kern<<<nb, kVecThreads, 0, h.stream>>>(x, wk.r.ptr, wk.p.ptr, wk.w.ptr, wk.d.ptr, mult, binv, n,
-                                         h.cg, h.partialC.ptr);
+  kern<<<nb, kVecThreads, 0, h.stream>>>(x, wk.r.ptr, wk.p.ptr, wk.w.ptr, dd, mult, bb, n, h.cg,
+                                         h.partialC.ptr);
+}
+
+template <typename T, bool EXACT>
+__global__ void hbm_kernel(T* __restrict__ hbm, const T* __restrict__ h2, T h2s, int h2mode,
+                           const T* __restrict__ bm1, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const T hh = h2mode == 1 ? h2s : h2[i];
+    hbm[i] = EXACT ? mul_x(hh, bm1[i]) : hh * bm1[i];
+  }
+}
+
+template <typename T>
+__global__ void fold_weights_kernel(T* __restrict__ md, T* __restrict__ mb,
+                                    const T* __restrict__ d, const T* __restrict__ mult,
+                                    const T* __restrict__ binv, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    md[i] = mult[i] * d[i];
+    mb[i] = mult[i] * binv[i];
+  }
 }
 
 template <typename T>
@@ -505,13 +530,62 @@ template <typename T>
 PcgResult pcg_iterate(Handle& h, const OpData<T>& op, PcgWork<T>& wk, T* x, const Coef<T>& c,
                       const T* mult, const T* binv, bool exact);
 
+// Folded update weights of a prepared solve (fused multiply-add form).
 template <typename T>
-void pcg_first_check(Handle& h, PcgWork<T>& wk, T* x, const T* mult, const T* binv, bool exact) {
-  launch_C<T>(h, wk, x, mult, binv, exact, true);
+static int prepare_weights(Handle& h, PcgWork<T>& wk, const T* mult, const T* binv, bool exact) {
+  if (exact) return 0;
+  const int64_t n = h.mesh.n;
+  if (wk.md.ensure(n) || wk.mb.ensure(n)) {
+    set_error(h, "pcg: device allocation failed");
+    return -4;
+  }
+  count_launch();
+  fold_weights_kernel<T><<<vec_blocks(n), kVecThreads, 0, h.stream>>>(wk.md.ptr, wk.mb.ptr,
+                                                                      wk.d.ptr, mult, binv, n);
+  return 0;
 }
-template void pcg_first_check<double>(Handle&, PcgWork<double>&, double*, const double*,
+
+template <typename T>
+int pcg_solve_extras(Handle& h, const OpData<T>& op, PcgWork<T>& wk, const T* mult, const T* binv,
+                     Coef<T>& c, bool exact) {
+  int st = prepare_weights<T>(h, wk, mult, binv, exact);
+  if (st) return st;
+  // FP64: h2 * bm1 once per solve, for the operator's mass term (the same
+  // rounded product the operator would form per point and iteration)
+  if constexpr (std::is_same<T, double>::value) {
+    if (c.h2mode) {
+      const int64_t n = h.mesh.n;
+      if (wk.hbm.ensure(n)) {
+        set_error(h, "pcg: device allocation failed");
+        return -4;
+      }
+      count_launch();
+      if (exact)
+        hbm_kernel<T, true><<<vec_blocks(n), kVecThreads, 0, h.stream>>>(
+            wk.hbm.ptr, c.h2, c.h2s, c.h2mode, op.bm1, n);
+      else
+        hbm_kernel<T, false><<<vec_blocks(n), kVecThreads, 0, h.stream>>>(
+            wk.hbm.ptr, c.h2, c.h2s, c.h2mode, op.bm1, n);
+      c.hbm = wk.hbm.ptr;
+    }
+  }
+  return 0;
+}
+template int pcg_solve_extras<double>(Handle&, const OpData<double>&, PcgWork<double>&,
+                                      const double*, const double*, Coef<double>&, bool);
+template int pcg_solve_extras<float>(Handle&, const OpData<float>&, PcgWork<float>&,
+                                     const float*, const float*, Coef<float>&, bool);
+
+template <typename T>
+int pcg_first_check(Handle& h, PcgWork<T>& wk, T* x, const T* mult, const T* binv, bool exact) {
+  const int st = prepare_weights<T>(h, wk, mult, binv, exact);
+  if (st) return st;
+  launch_C<T>(h, wk, x, mult, binv, exact, true);
+  return 0;
+}
+template int pcg_first_check<double>(Handle&, PcgWork<double>&, double*, const double*,
                                       const double*, bool);
-template void pcg_first_check<float>(Handle&, PcgWork<float>&, float*, const float*, const float*,
+template int pcg_first_check<float>(Handle&, PcgWork<float>&, float*, const float*, const float*,
                                      bool);
 
 template <typename T>
@@ -523,9 +597,11 @@ PcgResult pcg_solve(Handle& h, const OpData<T>& op, PcgWork<T>& wk, T* x, const 
   bool trivial = false;
   PcgResult res = pcg_prepare<T>(h, wk, x, f, c, mask, mult, tin, maxiter, istep, dpre, &trivial);
   if (res.status || trivial) return res;
+  Coef<T> cc = c;
+  if ((res.status = pcg_solve_extras<T>(h, op, wk, mult, binv, cc, exact))) return res;
   // iteration 1 check (z, s1, s2) -- no update
   launch_C<T>(h, wk, x, mult, binv, exact, true);
-  return pcg_iterate<T>(h, op, wk, x, c, mult, binv, exact);
+  return pcg_iterate<T>(h, op, wk, x, cc, mult, binv, exact);
 }
 
 // Iterations of a prepared solve (after its iteration-1 check) until the
@@ -574,9 +650,10 @@ PcgResult pcg_iterate(Handle& h, const OpData<T>& op, PcgWork<T>& wk, T* x, cons
   bool graph = h.use_graph && !h.timing;
   if (graph) {
     Handle::GraphKey key;
-    const void* ptrs[12] = {x,        f,         mask,      mult,         binv,        wk.r.ptr,
-                            wk.w.ptr, wk.p.ptr,  wk.d.ptr,  wk.segmask.ptr, c.h1,      c.h2};
-    for (int i = 0; i < 12; ++i) key.ptr[i] = ptrs[i];
+    const void* ptrs[15] = {x,        f,        mask,      mult,           binv, wk.r.ptr,
+                            wk.w.ptr, wk.p.ptr, wk.d.ptr,  wk.md.ptr,      c.h1, c.h2,
+                            wk.mb.ptr, c.hbm,   wk.segmask.ptr};
+    for (int i = 0; i < 15; ++i) key.ptr[i] = ptrs[i];
     key.ints[0] = (int)sizeof(T);
     key.ints[1] = c.h1mode;
     key.ints[2] = c.h2mode;
