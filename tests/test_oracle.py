@@ -221,3 +221,34 @@ def test_projection_restatement_properties(oracle):
         res = ops.dssum(ops.axhelm(u, h1, h2)) * P["mask"] - b
         assert np.sqrt(np.sum(P["mult"] * P["binv"] * res ** 2) / P["bm1"].sum()) < 1e-9
     assert proj.m == 4 and its[-1] < its[0]
+
+
+def test_oracle_matches_committed_golden_fixtures(oracle):
+    """tests/golden/oracle_golden.npz (made by tests/golden/make_golden.py)
+    pins the restatement against itself: integer outputs and iteration counts
+    exactly, floating-point outputs to 1e-12 relative (exact on the machine
+    that made them; libm and numpy's vector math may round differently on
+    another architecture)."""
+    import importlib.util
+    import os
+    here = os.path.dirname(os.path.abspath(__file__))
+    spec = importlib.util.spec_from_file_location("make_golden",
+                                                  os.path.join(here, "golden", "make_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    ref = np.load(os.path.join(here, "golden", "oracle_golden.npz"))
+    got = mg.compute()
+    assert set(ref.files) == set(got)
+    for k in ref.files:
+        a, b = ref[k], np.asarray(got[k])
+        assert a.shape == b.shape, k
+        if a.dtype.kind in "iu":
+            assert np.array_equal(a, b), k
+        elif k.endswith("_stats"):
+            cnt = a[..., 0] if k != "proj_stats" else a[:, :2]
+            cnt_b = b[..., 0] if k != "proj_stats" else b[:, :2]
+            assert np.array_equal(cnt, cnt_b), k  # iteration counts (and space sizes)
+            assert np.allclose(a, b, rtol=1e-10, atol=0), k
+        else:
+            scale = np.max(np.abs(a)) if a.size else 1.0
+            assert np.max(np.abs(a - b)) <= 1e-12 * max(scale, 1e-300), k
