@@ -133,8 +133,13 @@ __device__ __forceinline__ void axhelm_body(const AxArgs<T>& a, int blk, int tx,
   const bool act = ty < epb && e < a.nel;
   const size_t eo = (size_t)(act ? e : 0) * P;
 
-  T beta = T(0);
-  if constexpr (FUSED) beta = (T)a.cg->beta;
+  T beta = T(0), zmean = T(0);
+  bool mcor = false;
+  if constexpr (FUSED) {
+    beta = (T)a.cg->beta;
+    mcor = a.cg->mcor != 0;
+    if (mcor) zmean = (T)a.cg->zmean;
+  }
   const bool unit_h1 = a.h1mode == 0 && a.h1s == T(1);
 
   T ru[NX];
@@ -144,7 +149,8 @@ __device__ __forceinline__ void axhelm_body(const AxArgs<T>& a, int blk, int tx,
     T v = T(0);
     if (act) {
       if constexpr (FUSED) {
-        const T z = EXACT ? mul_x(a.r[eo + pt], a.d[eo + pt]) : a.r[eo + pt] * a.d[eo + pt];
+        T z = EXACT ? mul_x(a.r[eo + pt], a.d[eo + pt]) : a.r[eo + pt] * a.d[eo + pt];
+        if (mcor) z = EXACT ? add_x(z, zmean) : z + zmean;  // cadd(z,rmean) (hmholtz.f:749)
         v = madd<EXACT>(beta, a.u[eo + pt], z);  // add2s1: p = beta*p + z
         a.p[eo + pt] = v;
       } else {

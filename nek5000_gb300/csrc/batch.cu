@@ -496,6 +496,13 @@ int batch_solve_fp64(Batch& B, int np, double* const* x, const double* const* f,
       mark_done(h);
       continue;
     }
+    if (h.mcor) {
+      status[p] = NEKGPU_EINVAL;
+      set_error(h, "batch: singular operator (no Dirichlet point and h2 = 0): solve it with "
+                   "nekgpu_cggo_dev, which applies cggo's null-space correction");
+      mark_done(h);
+      continue;
+    }
     if (pcg_solve_extras<double>(h, h.mesh.f64, h.w64, mult[p], binv[p], c, false)) {
       status[p] = NEKGPU_ENOMEM;
       continue;
@@ -560,6 +567,15 @@ int batch_solve_mixed(Batch& B, int np, double* const* x, const double* const* f
     if (detect_coef<double>(h, h1[p], h2[p], n, c64[p])) {
       status[p] = NEKGPU_ECUDA;
       continue;
+    }
+    if (c64[p].h2mode == 0) {  // no Dirichlet point and h2 = 0: a null space
+      int st0 = 0;
+      const double skmin = device_sum(h, 6, mask[p], nullptr, nullptr, n, &st0);
+      if (!st0 && skmin > 0.0) {
+        status[p] = NEKGPU_EINVAL;
+        set_error(h, "batch: singular operator (no Dirichlet point and h2 = 0)");
+        continue;
+      }
     }
     Coef<float>& c = c32[p];
     c.h1mode = c64[p].h1mode;

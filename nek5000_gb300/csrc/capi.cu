@@ -144,15 +144,8 @@ int cggo_dev(Handle* H, double* x, const double* f, const double* h1, const doub
   int rc = make_coef(H, h1, h2, c);
   if (rc) return rc;
   if (cuda_pending(*H, "cggo: coefficient scan")) return NEKGPU_ECUDA;
-  // non-trivial null space (no Dirichlet point, h2 == 0) needs the mean
-  // correction of hmholtz.f:705-750, which this solver does not provide
-  int st = 0;
-  if (c.h2mode == 0) {
-    const double skmin = device_sum(*H, 6, mask, nullptr, nullptr, H->mesh.n, &st);  // glmin(mask)
-    if (!st && skmin > 0.0)
-      return fail(H, NEKGPU_EINVAL,
-                  "cggo: singular operator (no Dirichlet point and h2 = 0) is not supported");
-  }
+  // a non-trivial null space (no Dirichlet point, h2 == 0) gets cggo's mean
+  // correction (hmholtz.f:705-750) inside the FP64 solve
   const int maxiter = std::min(maxit, maxcg);
   PcgResult r = pcg_solve<double>(*H, H->mesh.f64, H->w64, x, f, c, mask, mult, binv, tin,
                                   maxiter, H->istep, H->exact);

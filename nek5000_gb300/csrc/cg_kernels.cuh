@@ -40,6 +40,8 @@ struct UpdatePoint {
   }
 };
 
+__device__ __forceinline__ void cg_finalize(CgScalars* cg, double s1, double s2);
+
 // Block body of the update kernel: block `blk` of `nblk` (1-D blocks).
 // VEC: 16-byte vector accesses (all seven arrays 16-byte aligned).
 template <typename T, bool EXACT, bool FIRST, bool VEC, bool FOLD = false>
@@ -109,7 +111,14 @@ __device__ __forceinline__ void cg_update_body(T* __restrict__ x, T* __restrict_
   }
   const double s1 = block_sum(t1, red);
   const double s2 = block_sum(t2, red);
-  if (threadIdx.x == 0) {
+  if (threadIdx.x == 0) cg_finalize(cg, s1, s2);
+}
+
+// The last block's step of the update kernel: counts the iteration, stores
+// rtz1 = s1 and rbn2 = sqrt(s2/vol), tests convergence (hmholtz.f:778) and
+// forms beta (:794).
+__device__ __forceinline__ void cg_finalize(CgScalars* cg, double s1, double s2) {
+  {
     cg->counter[1] = 0u;
     const int iter = cg->iter + 1;
     cg->iter = iter;
@@ -151,6 +160,65 @@ __global__ void __launch_bounds__(256)
   if (cg->done) return;
   cg_update_body<T, EXACT, FIRST, VEC, FOLD>(x, r, p, w, d, mult, binv, n, cg, partial,
                                              blockIdx.x, gridDim.x, red, &am_last);
+}
+
+// The update kernel with cggo's null-space correction (no Dirichlet point
+// and h2 = 0, hmholtz.f:705-720, :747-750): z = r d, then z += rmean with
+// rmean = smean * sum z bm1 (smean = -1 / sum bm1), and s1 = sum z r mult
+// over the corrected z, formed as sum (r d) r mult + rmean sum r mult.  The
+// kernel publishes rmean (cg->zmean) for the next operator launch, which
+// forms p = (r d + rmean) + beta p.
+template <typename T, bool EXACT, bool FIRST>
+__global__ void __launch_bounds__(256)
+    cg_update_mcor_kernel(T* __restrict__ x, T* __restrict__ r, const T* __restrict__ p,
+                          const T* __restrict__ w, const T* __restrict__ d,
+                          const T* __restrict__ mult, const T* __restrict__ binv,
+                          const T* __restrict__ bm1, int64_t n, CgScalars* cg,
+                          double* __restrict__ partial) {
+  __shared__ double red[32];
+  __shared__ int am_last;
+  if (cg->done) return;
+  const T alpha = FIRST ? T(0) : (T)cg->alpha;
+  double a1 = 0.0, a2 = 0.0, a3 = 0.0, a4 = 0.0;
+  const int nblk = gridDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)nblk * blockDim.x) {
+    T ri = r[i];
+    if (!FIRST) {
+      x[i] = madd<EXACT>(alpha, p[i], x[i]);
+      ri = madd<EXACT>(-alpha, w[i], ri);
+      r[i] = ri;
+    }
+    const T m = mult[i];
+    const T z = EXACT ? mul_x(ri, d[i]) : ri * d[i];
+    a1 += (double)(EXACT ? mul_x(mul_x(z, ri), m) : z * ri * m);
+    a2 += (double)(EXACT ? mul_x(mul_x(mul_x(m, binv[i]), ri), ri) : m * binv[i] * ri * ri);
+    a3 += (double)(EXACT ? mul_x(z, bm1[i]) : z * bm1[i]);
+    a4 += (double)(EXACT ? mul_x(ri, m) : ri * m);
+  }
+  const double b1 = block_sum(a1, red), b2 = block_sum(a2, red);
+  const double b3 = block_sum(a3, red), b4 = block_sum(a4, red);
+  if (threadIdx.x == 0) {
+    partial[blockIdx.x] = b1;
+    partial[nblk + blockIdx.x] = b2;
+    partial[2 * nblk + blockIdx.x] = b3;
+    partial[3 * nblk + blockIdx.x] = b4;
+    __threadfence();
+    const unsigned int ticket = atomicAdd(&cg->counter[1], 1u);
+    am_last = (ticket == (unsigned int)nblk - 1);
+  }
+  __syncthreads();
+  if (!am_last) return;
+  double t[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int q = threadIdx.x; q < nblk; q += blockDim.x)
+    for (int k = 0; k < 4; ++k) t[k] += __ldcg(partial + k * nblk + q);
+  double s[4];
+  for (int k = 0; k < 4; ++k) s[k] = block_sum(t[k], red);
+  if (threadIdx.x == 0) {
+    const double zmean = cg->smean * s[2];
+    cg->zmean = zmean;
+    cg_finalize(cg, s[0] + zmean * s[3], s[1]);
+  }
 }
 
 }  // namespace nekgpu

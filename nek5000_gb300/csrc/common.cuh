@@ -177,6 +177,10 @@ struct CgScalars {
   int istep;      // reference istep (for the "at least one iteration" rule)
   int nonfinite;  // set when a non-finite norm is met
   unsigned int counter[4];  // last-block tickets, one per reduction site
+  // null-space correction (no Dirichlet point and h2 = 0, hmholtz.f:705-750)
+  int mcor;       // 1: active
+  double smean;   // -1 / sum bm1
+  double zmean;   // rmean of the last check: z = r d + zmean
 };
 
 // Exact-order helpers: products and sums are rounded separately (no fused

@@ -27,12 +27,18 @@ __global__ void gs_op_kernel(T* __restrict__ u, const int* __restrict__ start,
 
 template <typename T>
 __global__ void gs_cg_weights_kernel(const int* __restrict__ start, const int* __restrict__ idx,
-                                     int nseg, const T* __restrict__ mask,
+                                     int nseg, const GsClasses cls, const T* __restrict__ mask,
                                      const T* __restrict__ mult, T* __restrict__ segmask,
                                      T* __restrict__ segmsum, int* nonuniform) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nseg) return;
-  const int a = start[s], b = start[s + 1];
+  // A group of the 1-, 2-, 4- or 8-copy classes has exactly that many copies:
+  // the idx entries after the last group of a class up to the next 16-byte
+  // boundary are padding and belong to no group.
+  int k = 0;
+  while (k < kGsClasses - 1 && s >= cls.soff[k] + cls.cnt[k]) ++k;
+  const int a = start[s];
+  const int b = k < kGsClasses - 1 ? a + (1 << k) : start[s + 1];
   const T m0 = mask[idx[a]];
   double ms = 0.0;
   for (int c = a; c < b; ++c) {
@@ -225,7 +231,7 @@ void gs_cg_weights(const GsMaps& gs, const T* mask, const T* mult, T* segmask, T
   if (gs.nbseg == 0) return;
   count_launch();
   gs_cg_weights_kernel<T><<<(gs.nbseg + kGsThreads - 1) / kGsThreads, kGsThreads, 0, s>>>(
-      gs.bstart, gs.bidx, gs.nbseg, mask, mult, segmask, segmsum, nonuniform);
+      gs.bstart, gs.bidx, gs.nbseg, gs.cls, mask, mult, segmask, segmsum, nonuniform);
 }
 
 template void gs_op<double>(const GsMaps&, double*, int, cudaStream_t);

@@ -144,6 +144,7 @@ struct Handle {
   bool own_stream = true;
   bool use_graph = true;
   int mixed_mode = 1;  // see mixed_solve
+  bool mcor = false;   // current FP64 solve has cggo's null-space correction
   bool autotune = true;  // time the operator's launch shapes on first solve (tune.cu)
   std::vector<std::unique_ptr<ProjSpace>> proj;  // projection spaces by index (proj.cu)
   DevBuf<CgScalars> cg_tune;  // scalars of the tuning launches (beta = 0, not done)

@@ -265,6 +265,16 @@ MixedResult mixed_solve(Handle& h, double* x, const double* f, const double* h1,
     set_error(h, "mixed: coefficient scan failed");
     return res;
   }
+  if (c64.h2mode == 0) {  // no Dirichlet point and h2 = 0: a null space
+    int st0 = 0;
+    const double skmin = device_sum(h, 6, mask, nullptr, nullptr, n, &st0);
+    if (!st0 && skmin > 0.0) {
+      res.status = -1;
+      set_error(h, "mixed: singular operator (no Dirichlet point and h2 = 0): use the FP64 "
+                   "solve, which applies cggo's null-space correction");
+      return res;
+    }
+  }
   Coef<float> c32;
   c32.h1mode = c64.h1mode;
   c32.h2mode = c64.h2mode;

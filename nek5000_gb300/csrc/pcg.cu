@@ -182,6 +182,14 @@ __global__ void interior_check_kernel(const T* __restrict__ mask, const T* __res
   }
 }
 
+// add2s2 (math.f:689): a = a + c b, rounded as the reference
+__global__ void axpy_exact_kernel(double* __restrict__ a, const double* __restrict__ b, double c,
+                                  int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    a[i] = __dadd_rn(a[i], __dmul_rn(c, b[i]));
+}
+
 template <typename T>
 __global__ void zero_kernel(T* __restrict__ a, int64_t n) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
@@ -335,6 +343,18 @@ static void launch_C(Handle& h, PcgWork<T>& wk, T* x, const T* mult, const T* bi
                      bool first) {
   const int64_t n = h.mesh.n;
   const int nb = vec_blocks(n);
+  if constexpr (std::is_same<T, double>::value) {
+    if (h.mcor) {  // null-space correction: the reference's z, unfolded
+      auto k = exact ? (first ? cg_update_mcor_kernel<double, true, true>
+                              : cg_update_mcor_kernel<double, true, false>)
+                     : (first ? cg_update_mcor_kernel<double, false, true>
+                              : cg_update_mcor_kernel<double, false, false>);
+      count_launch();
+      k<<<nb, kVecThreads, 0, h.stream>>>(x, wk.r.ptr, wk.p.ptr, wk.w.ptr, wk.d.ptr, mult, binv,
+                                          h.mesh.f64.bm1, n, h.cg, h.partialC.ptr);
+      return;
+    }
+  }
   auto al = [](const void* q) { return ((uintptr_t)q & 15u) == 0; };
   const T* dd = exact ? wk.d.ptr : wk.md.ptr;
   const T* bb = exact ? binv : wk.mb.ptr;
@@ -418,7 +438,7 @@ PcgResult pcg_prepare(Handle& h, PcgWork<T>& wk, T* x, const T* f, const Coef<T>
   const int nC = vec_blocks(n);
   if (wk.r.ensure(n) || wk.w.ensure(n) || wk.p.ensure(n) || wk.d.ensure(n) ||
       wk.segmask.ensure(m.gs.nbseg) || wk.segmsum.ensure(m.gs.nbseg) ||
-      h.partialA.ensure(nA) || h.partialB.ensure(nB) || h.partialC.ensure(2 * (size_t)nC)) {
+      h.partialA.ensure(nA) || h.partialB.ensure(nB) || h.partialC.ensure(4 * (size_t)nC)) {
     res.status = -4;
     set_error(h, "pcg: device allocation failed");
     return res;
@@ -489,8 +509,33 @@ PcgResult pcg_prepare(Handle& h, PcgWork<T>& wk, T* x, const T* f, const Coef<T>
   cudaMemcpyAsync(wk.r.ptr, f, n * sizeof(T), cudaMemcpyDeviceToDevice, s);
   count_launch();
   zero_kernel<T><<<vec_blocks(n), kVecThreads, 0, s>>>(wk.p.ptr, n);
+  // non-trivial null space (no Dirichlet point, h2 = 0; hmholtz.f:703-720):
+  // r += rmean dssum(bm1), rmean = smean sum r mult, smean = -1 / sum bm1
+  h.mcor = false;
+  double smean = 0.0;
+  if constexpr (std::is_same<T, double>::value) {
+    if (c.h2mode == 0) {
+      const double skmin = device_sum(h, 6, mask, nullptr, nullptr, n, &st);  // glmin(mask)
+      if (!st && skmin > 0.0) {
+        h.mcor = true;
+        smean = -1.0 / device_sum(h, 0, m.f64.bm1, nullptr, nullptr, n, &st);
+        const double rmean = smean * device_sum(h, 5, wk.r.ptr, mult, nullptr, n, &st);
+        cudaMemcpyAsync(wk.w.ptr, m.f64.bm1, n * sizeof(double), cudaMemcpyDeviceToDevice, s);
+        gs_op<double>(m.gs, wk.w.ptr, 0, s);
+        count_launch();
+        axpy_exact_kernel<<<vec_blocks(n), kVecThreads, 0, s>>>(wk.r.ptr, wk.w.ptr, rmean, n);
+      }
+      if (st) {
+        res.status = st;
+        set_error(h, "pcg: reduction failed");
+        return res;
+      }
+    }
+  }
   CgScalars& hc = *h.cg_host;
   memset(&hc, 0, sizeof(CgScalars));
+  hc.mcor = h.mcor ? 1 : 0;
+  hc.smean = smean;
   hc.rtz1 = 1.0;
   hc.tin = tin;
   hc.tol = std::fabs(tin);
@@ -656,7 +701,7 @@ PcgResult pcg_iterate(Handle& h, const OpData<T>& op, PcgWork<T>& wk, T* x, cons
     for (int i = 0; i < 15; ++i) key.ptr[i] = ptrs[i];
     key.ints[0] = (int)sizeof(T);
     key.ints[1] = c.h1mode;
-    key.ints[2] = c.h2mode;
+    key.ints[2] = c.h2mode + 8 * (int)h.mcor;
     const AxShapeSel& sh = m.ax_sel[sizeof(T) == 4 ? 1 : 0];
     const GsClasses& gc = m.gs.cls_tuned[sizeof(T) == 4 ? 1 : 0];
     key.ints[3] = (int)exact + 4 * (int)m.use_tma + 8 * (sh.kind + 1) + 32 * sh.epb +

@@ -260,3 +260,83 @@ def test_cggo_irregular_group_sizes(gpu_lib, oracle):
                               10 ** 6, 1, dev(binv), maxcg=10 ** 6)
     assert rc == 0 and abs(it - it_ref) <= 1
     assert np.linalg.norm(x.cpu().numpy() - x_ref) <= 1e-11 * np.linalg.norm(x_ref)
+
+
+@pytest.mark.parametrize("exact", [False, True])
+def test_cggo_null_space_correction(gpu_lib, oracle, exact):
+    """No Dirichlet point and h2 = 0 (Neumann in x, periodic in y and z): cggo
+    applies its mean correction (hmholtz.f:705-750) -- r += rmean dssum(bm1)
+    before the loop, z += smean sum(z bm1) in every iteration.  The GPU must
+    follow the oracle's iterations and solution; the mixed and batched solves
+    refuse the singular system."""
+    torch = pytest.importorskip("torch")
+    from nek5000_gb300 import _capi, NekGpuBatch
+    P = oracle.box_problem(7, 3, 3, 3, periodic=(False, True, True),
+                           dirichlet=(False,) * 6, v=rng_unit_vector(31))
+    n = P["n"]
+    assert P["mask"].min() == 1.0
+    rng = np.random.default_rng(31)
+    f = P["ops"].dssum(P["bm1"] * (P["ops"].dssum(rng.standard_normal(n)) * P["mult"]))
+    h1, h2 = np.ones(n), np.zeros(n)
+    x_ref, it_ref, r0_ref, r2_ref = P["ops"].cggo(f, h1, h2, P["mask"], P["mult"], P["binv"],
+                                                  -1e-10, maxcg=10 ** 6)
+    _, spread = rank_spread(oracle, P, lambda ops: ops.cggo(
+        f, h1, h2, P["mask"], P["mult"], P["binv"], -1e-10, maxcg=10 ** 6)[0])
+    lib = gpu_lib(0)
+    lib.setup(P["nx1"], P["nel"], P["D"], P["g"], P["bm1"], P["glo_num"])
+    lib.set_exact(exact)
+    dev = lambda a: torch.tensor(a, device="cuda")
+    x = torch.zeros(n, dtype=torch.float64, device="cuda")
+    it, r0, r2, rc = lib.cggo(x, dev(f), dev(h1), dev(h2), dev(P["mask"]), dev(P["mult"]), 1,
+                              -1e-10, 10 ** 6, 1, dev(P["binv"]), maxcg=10 ** 6)
+    assert rc == 0
+    assert abs(it - it_ref) <= 1, (it, it_ref)
+    assert abs(r0 - r0_ref) <= 1e-12 * r0_ref
+    err = np.linalg.norm(x.cpu().numpy() - x_ref) / np.linalg.norm(x_ref)
+    print(f"null-space correction: {it} iterations (oracle {it_ref}), rel. error {err:.2e}, "
+          f"oracle spread {spread:.2e}")
+    assert err <= max(1e-12, 2 * spread)
+    # mixed and batched solves refuse it
+    xm = torch.zeros(n, dtype=torch.float64, device="cuda")
+    with pytest.raises(_capi.NekGpuError) as e:
+        lib.cggo_mixed(xm, dev(f), dev(h1), dev(h2), dev(P["mask"]), dev(P["mult"]), 1, -1e-10,
+                       10 ** 6, 1, dev(P["binv"]))
+    assert e.value.code == _capi.EINVAL
+    B = NekGpuBatch(0)
+    B.add(P["nx1"], P["nel"], P["D"], P["g"], P["bm1"], P["glo_num"])
+    res = B.solve([xm], [dev(f)], [dev(h1)], [dev(h2)], [dev(P["mask"])], [dev(P["mult"])],
+                  [dev(P["binv"])], tin=-1e-10)
+    assert res["status"] == [_capi.EINVAL]
+
+
+@pytest.mark.parametrize("case", [((7, 3, 3, 3), (False,) * 6),
+                                  ((7, 3, 3, 3), (False, True, False, False, False, False)),
+                                  ((6, 4, 3, 2), (False,) * 6)])
+def test_cggo_neumann_faces(gpu_lib, oracle, case):
+    """Unmasked element faces on the domain boundary (Neumann) make singleton
+    boundary groups live.  When a size class does not fill its last 16-byte
+    run, the entries up to the boundary are padding and belong to no group;
+    the mask and multiplicity weights of the class's last group must ignore
+    them.  Iteration counts and solutions follow the oracle."""
+    torch = pytest.importorskip("torch")
+    (nx1, kx, ky, kz), dirichlet = case
+    P = oracle.box_problem(nx1, kx, ky, kz, periodic=(False, True, True), dirichlet=dirichlet,
+                           v=rng_unit_vector(33))
+    n = P["n"]
+    rng = np.random.default_rng(33)
+    f = P["ops"].dssum(P["bm1"] * (P["ops"].dssum(rng.standard_normal(n)) * P["mult"]))
+    f = f * P["mask"]
+    h1, h2 = np.ones(n), np.ones(n)
+    x_ref, it_ref, r0_ref, r2_ref = P["ops"].cggo(f, h1, h2, P["mask"], P["mult"], P["binv"],
+                                                  -1e-10, maxcg=10 ** 6)
+    _, spread = rank_spread(oracle, P, lambda ops: ops.cggo(
+        f, h1, h2, P["mask"], P["mult"], P["binv"], -1e-10, maxcg=10 ** 6)[0])
+    lib = gpu_lib(0)
+    lib.setup(P["nx1"], P["nel"], P["D"], P["g"], P["bm1"], P["glo_num"])
+    dev = lambda a: torch.tensor(a, device="cuda")
+    x = torch.zeros(n, dtype=torch.float64, device="cuda")
+    it, r0, r2, rc = lib.cggo(x, dev(f), dev(h1), dev(h2), dev(P["mask"]), dev(P["mult"]), 1,
+                              -1e-10, 10 ** 6, 1, dev(P["binv"]), maxcg=10 ** 6)
+    assert rc == 0 and abs(it - it_ref) <= 1, (it, it_ref)
+    err = np.linalg.norm(x.cpu().numpy() - x_ref) / np.linalg.norm(x_ref)
+    assert err <= max(1e-12, 2 * spread), (err, spread)
