@@ -60,11 +60,13 @@ def parse():
                     help="mixed: 1 residual replacement keeping the search direction, "
                          "0 restarted FP32 PCG per outer step")
     ap.add_argument("--workload", default="helmholtz",
-                    choices=["helmholtz", "poisson-n9", "batch", "axhelm-sweep", "hsolve"],
+                    choices=["helmholtz", "poisson-n9", "batch", "axhelm-sweep", "hsolve",
+                             "adjoint"],
                     help="helmholtz: E=32^3 N=7 (default); poisson-n9: E=24^3 N=9 Poisson; "
                          "batch: 3 velocity solves + 61 uneven Poisson problems in one batch; "
                          "axhelm-sweep: in-solve operator bandwidth at N=5,7,9, E=32^3; "
-                         "hsolve: a sequence of solves with projection onto previous solutions")
+                         "hsolve: a sequence of solves with projection onto previous solutions; "
+                         "adjoint: dJ/dh1 through the adjoint solve, E=16^3 N=7")
     ap.add_argument("--batch-problems", type=int, default=61)
     ap.add_argument("--fp64-shape", default=None,
                     help="pin the FP64 operator launch shape 'kind,epb' instead of autotuning")
@@ -666,6 +668,76 @@ def run_hsolve(args):
     lib.close()
 
 
+def run_adjoint(args):
+    """Gradient of J = 0.5 |u - u*|_B^2 with respect to the per-point viscosity
+    h1 on E=16^3, N=7 (h1 = exp(0.3 g), g a seeded smooth random field of
+    correlation length 0.2; h2 = 0; all-Dirichlet box): forward FP64 solve,
+    adjoint solve (the operator is symmetric) and the axhelm adjoint kernel,
+    every step on the device."""
+    import torch
+    ws, rank, local, pg = dist_setup(args.gpus)
+    torch.cuda.set_device(local)
+    from nek5000_gb300 import NekGpu, mesh
+    from nek5000_gb300 import build as nb
+    nb.build()
+    k = 16 if args.k == 32 else args.k
+    M = mesh.box_mesh(args.N, k, k, k, seed=5)
+    n = M["n"]
+    x, y, z = M["x"], M["y"], M["z"]
+    r = np.random.default_rng(5)
+    kv = r.standard_normal((64, 3)) / 0.2
+    ph = r.uniform(0, 2 * np.pi, 64)
+    am = r.standard_normal(64) * np.sqrt(2.0 / 64)
+    g = np.zeros(n)
+    for q in range(64):  # the Gaussian random field, mode by mode
+        g += am[q] * np.cos(x * kv[q, 0] + y * kv[q, 1] + z * kv[q, 2] + ph[q])
+    h1v = np.exp(0.3 * g)
+    lib = NekGpu(local)
+    lib.setup(M["lx1"], M["nel"], M["D"], M["g"], M["bm1"], M["glo_num"])
+    dev = lambda a: torch.tensor(a, device=f"cuda:{local}")
+    h1, h2 = dev(h1v), torch.zeros(n, dtype=torch.float64, device=f"cuda:{local}")
+    mask, mult, binv, bm1 = dev(M["mask"]), dev(M["mult"]), dev(M["binv"]), dev(M["bm1"])
+    nglob = int(M["lattice"].max()) + 1
+    f = dev(M["bm1"] * np.random.default_rng(6).standard_normal(nglob)[M["lattice"]])
+    lib.dssum(f)
+    f = f * mask
+    ustar = torch.zeros(n, dtype=torch.float64, device=f"cuda:{local}")
+    lib.cggo(ustar, f, dev(h1v * 1.1), h2, mask, mult, 1, -1e-10, 10 ** 6, 1, binv, maxcg=10 ** 6)
+
+    def gradient():
+        u = torch.zeros_like(ustar)
+        it1, _, _, _ = lib.cggo(u, f, h1, h2, mask, mult, 1, -1e-10, 10 ** 6, 1, binv,
+                                maxcg=10 ** 6)
+        gsrc = bm1 * (u - ustar)
+        lib.dssum(gsrc)
+        gsrc = gsrc * mask
+        lam = torch.zeros_like(u)
+        it2, _, _, _ = lib.cggo_adjoint(lam, gsrc, h1, h2, mask, mult, 1, -1e-10, 10 ** 6, 1,
+                                        binv, maxcg=10 ** 6)
+        gh1 = torch.zeros_like(u)
+        lib.axhelm_adjoint_h1(gh1, lam, u)
+        return it1, it2, -gh1
+
+    for _ in range(args.warmup):
+        gradient()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        it1, it2, grad = gradient()
+    torch.cuda.synchronize()
+    T = (time.perf_counter() - t0) / args.steps
+    if rank == 0:
+        print(json.dumps({"metric": "adjoint gradient dJ/dh1 (forward solve + adjoint solve + "
+                                    "axhelm adjoint)", "value": 1e3 * T, "unit": "ms/gradient",
+                          "higher_is_better": False, "steps": args.steps, "warmup": args.warmup,
+                          "n_gpus": ws, "dtype": "f64", "data": "synthetic",
+                          "config": {"workload": f"E={k}^3 N={args.N} h1=exp(0.3 g) h2=0 "
+                                                 "dirichlet-all", "n_points": n,
+                                     "forward_iterations": it1, "adjoint_iterations": it2,
+                                     "grad_norm": float(torch.linalg.norm(grad))}}), flush=True)
+    lib.close()
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -676,6 +748,8 @@ def main():
         run_sweep(args)
     elif args.workload == "hsolve":
         run_hsolve(args)
+    elif args.workload == "adjoint":
+        run_adjoint(args)
     else:
         run_gpu(args)
 
