@@ -61,12 +61,13 @@ def parse():
                          "0 restarted FP32 PCG per outer step")
     ap.add_argument("--workload", default="helmholtz",
                     choices=["helmholtz", "poisson-n9", "batch", "axhelm-sweep", "hsolve",
-                             "adjoint"],
+                             "adjoint", "velocity3"],
                     help="helmholtz: E=32^3 N=7 (default); poisson-n9: E=24^3 N=9 Poisson; "
                          "batch: 3 velocity solves + 61 uneven Poisson problems in one batch; "
                          "axhelm-sweep: in-solve operator bandwidth at N=5,7,9, E=32^3; "
                          "hsolve: a sequence of solves with projection onto previous solutions; "
-                         "adjoint: dJ/dh1 through the adjoint solve, E=16^3 N=7")
+                         "adjoint: dJ/dh1 through the adjoint solve, E=16^3 N=7; "
+                         "velocity3: 3 velocity components in one fused mixed solve")
     ap.add_argument("--batch-problems", type=int, default=61)
     ap.add_argument("--fp64-shape", default=None,
                     help="pin the FP64 operator launch shape 'kind,epb' instead of autotuning")
@@ -738,6 +739,153 @@ def run_adjoint(args):
     lib.close()
 
 
+VELOCITY_FACES = ((True, True, True, True, True, True),      # u: every wall
+                  (True, True, False, False, False, False),  # v: x walls only
+                  (True, True, True, True, True, False))     # w: outflow at z+
+
+
+def run_velocity3(args):
+    """The three velocity components of one time step (ophinv,
+    core/induct.f:1064-1071): one deformed box E=k^3, N (seed 4), h1 = 1,
+    h2 = 1500 (1.5/dt, dt = 1e-3), a mask per component (every wall; the x
+    walls only; every wall but the z+ outflow), standard-normal right-hand
+    sides per global node (seeds 40, 41, 42), each solved to tol * its rbn0.
+    Timed three ways: the fused multi-field mixed solve
+    (nekgpu_cggo_mixed_multi_dev), three single-field mixed solves, three FP64
+    solves."""
+    import torch
+    ws, rank, local, pg = dist_setup(args.gpus)
+    torch.cuda.set_device(local)
+    from nek5000_gb300 import NekGpu, mesh
+    from nek5000_gb300 import build as nb
+    nb.build()
+    M = mesh.box_mesh(args.N, args.k, args.k, args.k, seed=4)
+    n = M["n"]
+    nglob = int(M["lattice"].max()) + 1
+    dev = lambda a: torch.tensor(a, device=f"cuda:{local}")
+    masks, fs = [], []
+    for c, faces in enumerate(VELOCITY_FACES):
+        mk = mesh.face_mask(M, faces)
+        g = np.random.default_rng(40 + c).standard_normal(nglob)[M["lattice"]]
+        masks.append(dev(mk))
+        fs.append(dev(mesh.dssum_host(M["lattice"], M["bm1"] * g, nglob) * mk))
+    lib = NekGpu(local)
+    lib.setup(M["lx1"], M["nel"], M["D"], M["g"], M["bm1"], M["glo_num"])
+    h1, h2 = dev(np.ones(n)), dev(np.full(n, 1500.0))
+    mult, binv = dev(M["mult"]), dev(M["binv"])
+    del M
+    xs = [torch.zeros(n, dtype=torch.float64, device=f"cuda:{local}") for _ in range(3)]
+    big = 10 ** 6
+    lib.set_option(2, 1)  # timing: solve-total and per-kernel events
+    kt = [0.0, 0.0, 0.0, 0]  # operator, boundary groups, update ms; iterations
+
+    def kernel_times():
+        t_ax, t_gs, t_up, it = lib.last_kernel_times()
+        for q, v in enumerate((t_ax, t_gs, t_up, it)):
+            kt[q] += v
+
+    def multi():
+        r = lib.cggo_mixed_multi(xs, fs, h1, h2, masks, mult, 1, -args.tol, big, 1, binv,
+                                 inner_tol=args.inner_tol)
+        if any(r["status"]):
+            raise RuntimeError(f"multi-field solve: {r} {lib.last_error()}")
+        kernel_times()
+        return r["ninner"]
+
+    def mixed():
+        its = []
+        for c in range(3):
+            no, ni, r0, r2, rc = lib.cggo_mixed(xs[c], fs[c], h1, h2, masks[c], mult, 1,
+                                                -args.tol, big, 1, binv, inner_tol=args.inner_tol)
+            if rc:
+                raise RuntimeError(lib.last_error())
+            kernel_times()
+            its.append(ni)
+        return its
+
+    def fp64():
+        its = []
+        for c in range(3):
+            it, r0, r2, rc = lib.cggo(xs[c], fs[c], h1, h2, masks[c], mult, 1, -args.tol, big, 1,
+                                      binv, maxcg=big)
+            if rc:
+                raise RuntimeError(lib.last_error())
+            its.append(it)
+        return its
+
+    def timed(solve):
+        for _ in range(args.warmup):
+            solve()
+        barrier(pg)
+        torch.cuda.synchronize()
+        l0 = lib.launch_count()
+        t = 0.0
+        kt[:] = [0.0, 0.0, 0.0, 0]
+        with Clocks(local) as ck:
+            for _ in range(args.steps):
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                its = solve()
+                torch.cuda.synchronize()
+                t += time.perf_counter() - t0
+        barrier(pg)
+        k = max(kt[3], 1)
+        return dict(its=its, T=allmax(pg, t), launches=lib.launch_count() - l0,
+                    clocks=ck.summary(),
+                    per_iter_ms={"operator": kt[0] / k, "boundary_groups": kt[1] / k,
+                                 "update": kt[2] / k, "iterations_timed": kt[3]})
+
+    out = {}
+    if not args.only_mixed:
+        out["fp64"] = timed(fp64)
+        ref = [x.clone() for x in xs]
+        out["mixed_single"] = timed(mixed)
+    out["mixed_multi"] = timed(multi)
+    err = (max(float(torch.linalg.norm(xs[c] - ref[c]) / torch.linalg.norm(ref[c]))
+               for c in range(3)) if not args.only_mixed else None)
+    it64 = out["fp64"]["its"] if "fp64" in out else out["mixed_multi"]["its"]
+    rate = {k: allsum(pg, n * sum(it64) * args.steps) / v["T"] for k, v in out.items()}
+    # the fused operator's algorithmic bytes: G (6), d, bm1 once; p, r in and
+    # p, w out per field (FP32 words)
+    b_op = 4 * (8 + 4 * 3)
+    op_ms = out["mixed_multi"]["per_iter_ms"]["operator"]
+    gbs = b_op * n / (op_ms * 1e-3) / 1e9 if op_ms > 0 else None
+    peak, peak_src = peaks()
+    if rank == 0:
+        ms = {k: 1e3 * v["T"] / args.steps for k, v in out.items()}
+        single = out.get("mixed_single")
+        print(json.dumps({
+            "metric": "DOF-iters/s, 3 velocity components E=32^3 N=7 to 1e-10 (fused "
+                      "multi-field mixed solve)",
+            "value": rate["mixed_multi"], "unit": "DOF-iters/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms["mixed_multi"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 inner / f64 outer", "data": "synthetic",
+            "config": {"workload": f"velocity E={args.k}^3 N={args.N} h1=1 h2=1500, 3 fields "
+                                   "(masks: all walls / x walls / all but z+)",
+                       "n_points": n, "tol": args.tol, "inner_tol": args.inner_tol,
+                       "value_definition": "n * (sum of the 3 FP64 PCG iteration counts) / time "
+                                           "of the 3-field solve",
+                       "fp64_iterations": it64 if "fp64" in out else None,
+                       "inner_iterations_single": single["its"] if single else None,
+                       "inner_iterations_multi": out["mixed_multi"]["its"],
+                       "rel_error_vs_fp64_solution": err,
+                       "l2": "inputs larger than L2", "parallelism": f"replicas{ws}"},
+            "ms_per_3_field_solve": ms, "dof_iters_per_s": rate,
+            "inner_iteration_ms": {k: v["per_iter_ms"] for k, v in out.items()},
+            "speedup_multi_vs_single_mixed": (single["T"] / out["mixed_multi"]["T"]
+                                              if single else None),
+            "speedup_multi_vs_fp64": (out["fp64"]["T"] / out["mixed_multi"]["T"]
+                                      if "fp64" in out else None),
+            "roofline": {"kernel": f"fused 3-field fp32 operator lx1={args.N + 1}",
+                         "bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s",
+                         "frac": gbs / peak if gbs else None, "peak_source": peak_src,
+                         "bytes_per_point": b_op, "avg_launch_ms": op_ms, "traffic": None},
+            "gpu_launches": out["mixed_multi"]["launches"],
+            "clocks": out["mixed_multi"]["clocks"]}), flush=True)
+    lib.close()
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -750,6 +898,8 @@ def main():
         run_hsolve(args)
     elif args.workload == "adjoint":
         run_adjoint(args)
+    elif args.workload == "velocity3":
+        run_velocity3(args)
     else:
         run_gpu(args)
 

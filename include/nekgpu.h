@@ -186,6 +186,24 @@ int nekgpu_cggo_mixed_dev(const int64_t *handle, double *x, const double *f, con
                           const int *imsh, const double *tin, const int *maxit, const int *isd,
                           const double *binv, const double *inner_tol, int *niter_outer,
                           int *niter_inner, double *rbn0, double *rbn2);
+/* Several fields of one mesh that share h1, h2, mult and binv -- the velocity
+ * components of a time step, which the reference solves one after another
+ * (ophinv, core/induct.f:1064-1071) -- solved together by the mixed solve
+ * (residual replacement): per field x, f (device arrays, as
+ * nekgpu_cggo_mixed_dev) and mask; *nfield <= NEKGPU_MULTI_MAX.  Every FP32
+ * iteration of all fields is one operator launch that reads the geometric
+ * factors once, one boundary-group launch and one update launch; each field
+ * keeps its own scalars and stopping test.  Outputs per field: outer steps,
+ * inner iterations, first and last FP64 norms and a status code (0,
+ * NEKGPU_ENOTCONV, NEKGPU_ENAN, NEKGPU_EINVAL for a singular system).  Odd
+ * lx1 solves the fields one after another.  No reference counterpart. */
+#define NEKGPU_MULTI_MAX 3
+int nekgpu_cggo_mixed_multi_dev(const int64_t *handle, const int *nfield, double *const *x,
+                                const double *const *f, const double *h1, const double *h2,
+                                const double *const *mask, const double *mult, const int *imsh,
+                                const double *tin, const int *maxit, const int *isd,
+                                const double *binv, const double *inner_tol, int *niter_outer,
+                                int *niter_inner, double *rbn0, double *rbn2, int *status);
 /* hmholtz (core/hmholtz.f:2-69) with the mixed-precision solve, host arrays. */
 int nekgpu_hmholtz_mixed(const int64_t *handle, double *u, double *rhs, const double *h1,
                          const double *h2, const double *mask, const double *mult,

@@ -21,6 +21,7 @@ OPT_AUTOTUNE = 8
 MAX_LX1 = 12
 NOALLOC_MAX_POINTS = 4194304
 PROJ_SPACES, PROJ_MAX, PROJ_DEFAULT = 16, 16, 8
+MULTI_MAX = 3
 
 STATUS_NAMES = {
     0: "NEKGPU_OK", -1: "NEKGPU_EINVAL", -2: "NEKGPU_EHANDLE", -3: "NEKGPU_ECUDA",
@@ -65,6 +66,8 @@ SIGNATURES = {
     "nekgpu_hsolve": [_I64P, _IP, _P, _P, _P, _P, _P, _P, _IP, _DP, _IP, _IP, _P, _IP, _IP, _DP,
                       _DP, _IP],
     "nekgpu_proj_setup": [_I64P, _IP, _IP],
+    "nekgpu_cggo_mixed_multi_dev": [_I64P, _IP, _P, _P, _P, _P, _P, _P, _IP, _DP, _IP, _IP, _P,
+                                    _DP, _IP, _IP, _DP, _DP, _IP],
     "nekgpu_proj_count": [_I64P, _IP, _IP],
     "nekgpu_batch_set_shape": [_I64P, _IP, _IP],
     "nekgpu_ax_shape": [_I64P, _IP, _IP, _IP, _DP],

@@ -102,6 +102,16 @@ struct ProjSpace {
   DevBuf<double> xx, bb, xbar, bbar, h1old, h2old;
 };
 
+// One field of the multi-field mixed solve (multi.cu): its FP32 PCG vectors,
+// FP32 mask and boundary-group mask, FP64 residual and scalars.
+struct MultiField {
+  DevBuf<float> mask, segmask;
+  DevBuf<double> r64;
+  DevBuf<CgScalars> cg;
+  CgScalars* cg_host = nullptr;  // pinned
+  ~MultiField() { cudaFreeHost(cg_host); }
+};
+
 struct Handle {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -111,6 +121,8 @@ struct Handle {
   CgScalars* cg = nullptr;       // device
   CgScalars* cg_host = nullptr;  // pinned mirror
   DevBuf<double> partialA, partialB, partialC, red;
+  // multi-field solve: r, p, w, x of every field, field c at c * n
+  DevBuf<float> mfr, mfp, mfw, mfx;
   int* flag = nullptr;           // device int scratch
   PcgWork<double> w64;
   PcgWork<float> w32;
@@ -147,6 +159,9 @@ struct Handle {
   bool mcor = false;   // current FP64 solve has cggo's null-space correction
   bool autotune = true;  // time the operator's launch shapes on first solve (tune.cu)
   std::vector<std::unique_ptr<ProjSpace>> proj;  // projection spaces by index (proj.cu)
+  std::vector<std::unique_ptr<MultiField>> multi;  // fields of the multi-field solve
+  DevBuf<double> mpartialA, mpartialB, mpartialC;
+  DevBuf<unsigned int> mcounter;
   DevBuf<CgScalars> cg_tune;  // scalars of the tuning launches (beta = 0, not done)
 };
 
@@ -206,6 +221,9 @@ PcgResult pcg_prepare(Handle& h, PcgWork<T>& wk, T* x, const T* f, const Coef<T>
                       const T* mask, const T* mult, double tin, int maxiter, int istep,
                       const T* dpre, bool* trivial);
 int pcg_vec_blocks(int64_t n);
+// Sets *bad when an element-interior point (not in a boundary group) has mask
+// or multiplicity other than 1 (FP32 arrays; the fused operator assumes 1).
+void launch_interior_check(Handle& h, const float* mask, const float* mult, int* bad);
 // Per-solve data of a prepared solve: the update kernel's folded weights
 // (fused multiply-add form) and, for FP64, h2*bm1 (sets c.hbm).
 template <typename T>
@@ -244,6 +262,20 @@ int proj_project2(Handle& h, ProjSpace& P, double* x, const Coef<double>& c, con
                   const double* w);
 // Residual replacement into the running FP32 PCG (see mixed.cu).
 int mixed_replace(Handle& h, double& scale, double inner_tol, int* restarts);
+// The same for any FP32 PCG: its vectors, the FP64 residual, its scalars.
+struct ReplaceTarget {
+  float* r32;
+  float* p32;
+  float* x32;
+  const float* d32;
+  const float* mult32;
+  const float* binv32;
+  const double* r64;
+  CgScalars* cg_dev;
+  CgScalars* cg_host;
+};
+int mixed_replace_into(Handle& h, const ReplaceTarget& t, double& scale, double inner_tol,
+                       int* restarts);
 // mode 0: each outer step is a fresh FP32 PCG to inner_tol (restarted);
 // mode 1: one FP32 PCG whose residual is replaced by the FP64 one whenever it
 // has dropped by inner_tol, keeping the search direction (reliable updates).

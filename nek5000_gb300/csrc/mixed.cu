@@ -183,8 +183,9 @@ double outer_residual(Handle& h, double* r, const double* f, const double* x,
   return st ? -1.0 : std::sqrt(s2 / m.vol);
 }
 
-// Residual replacement: h.w64.r holds r = f - A x (FP64).  It becomes the
-// residual of the running FP32 PCG of h.w32, rescaled by a power of two near
+// Residual replacement: t.r64 (h.w64.r for mixed_replace) holds r = f - A x
+// (FP64).  It becomes the residual of the running FP32 PCG (t's vectors and
+// scalars; h.w32 and h.cg for mixed_replace), rescaled by a power of two near
 // max |r| (*scale: old in, new out; the ratio of two powers of two is exact,
 // so p is rescaled exactly), x32 is zeroed (its old content is already in x),
 // and the scalars after the last check (h.cg_host) are updated for the new r:
@@ -195,22 +196,28 @@ double outer_residual(Handle& h, double* r, const double* f, const double* x,
 // zero (nothing to iterate on), or a negative status.
 int mixed_replace(Handle& h, double& scale, double inner_tol, int* restarts) {
   PcgWork<float>& wk = h.w32;
-  PcgWork<double>& w64 = h.w64;
+  ReplaceTarget t{wk.r.ptr, wk.p.ptr, wk.x.ptr, wk.d.ptr, wk.mult.ptr, wk.binv.ptr,
+                  h.w64.r.ptr, h.cg, h.cg_host};
+  return mixed_replace_into(h, t, scale, inner_tol, restarts);
+}
+
+int mixed_replace_into(Handle& h, const ReplaceTarget& t, double& scale, double inner_tol,
+                       int* restarts) {
   const Mesh& m = h.mesh;
   const int64_t n = m.n;
   cudaStream_t s = h.stream;
   const int nb = blocks(n);
   int st = 0;
-  const double amax = device_absmax<double>(h, w64.r.ptr, n, &st);
+  const double amax = device_absmax<double>(h, t.r64, n, &st);
   if (st) return -3;
   if (amax == 0.0) return 1;
   const double s_new = std::ldexp(1.0, std::ilogb(amax));
   const double ratio = scale / s_new;
   count_launch(3);
-  cast_scale_kernel<float, double><<<nb, kThreads, 0, s>>>(wk.r.ptr, w64.r.ptr, 1.0 / s_new, n);
-  scale_kernel<<<nb, kThreads, 0, s>>>(wk.p.ptr, (float)ratio, n);
-  cudaMemsetAsync(wk.x.ptr, 0, n * sizeof(float), s);
-  rz_kernel<<<nb, kThreads, 0, s>>>(wk.r.ptr, wk.d.ptr, wk.mult.ptr, wk.binv.ptr, n, h.red.ptr);
+  cast_scale_kernel<float, double><<<nb, kThreads, 0, s>>>(t.r32, t.r64, 1.0 / s_new, n);
+  scale_kernel<<<nb, kThreads, 0, s>>>(t.p32, (float)ratio, n);
+  cudaMemsetAsync(t.x32, 0, n * sizeof(float), s);
+  rz_kernel<<<nb, kThreads, 0, s>>>(t.r32, t.d32, t.mult32, t.binv32, n, h.red.ptr);
   std::vector<double> hp(2 * (size_t)nb);
   cudaMemcpyAsync(hp.data(), h.red.ptr, hp.size() * sizeof(double), cudaMemcpyDeviceToHost, s);
   if (cudaStreamSynchronize(s) != cudaSuccess) {
@@ -222,7 +229,7 @@ int mixed_replace(Handle& h, double& scale, double inner_tol, int* restarts) {
     s1 += hp[b];
     s2 += hp[nb + b];
   }
-  CgScalars& c = *h.cg_host;  // state after the last (iterated) check
+  CgScalars& c = *t.cg_host;  // state after the last (iterated) check
   const double rec = c.rbn2 * ratio;  // FP32 recurrence norm, new scaling
   c.rtz2 = c.rtz2 * ratio * ratio;
   c.rtz1 = s1;
@@ -233,7 +240,7 @@ int mixed_replace(Handle& h, double& scale, double inner_tol, int* restarts) {
   c.tol = inner_tol * c.rbn0;
   c.done = 0;
   c.counter[0] = c.counter[1] = c.counter[2] = c.counter[3] = 0u;
-  cudaMemcpyAsync(h.cg, &c, sizeof(CgScalars), cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(t.cg_dev, &c, sizeof(CgScalars), cudaMemcpyHostToDevice, s);
   scale = s_new;
   return 0;
 }

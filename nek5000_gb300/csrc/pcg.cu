@@ -202,6 +202,12 @@ __global__ void zero_kernel(T* __restrict__ a, int64_t n) {
 // ---- host helpers ------------------------------------------------------------
 int pcg_vec_blocks(int64_t n) { return vec_blocks(n); }
 
+void launch_interior_check(Handle& h, const float* mask, const float* mult, int* bad) {
+  count_launch();
+  interior_check_kernel<float><<<vec_blocks(h.mesh.n), kVecThreads, 0, h.stream>>>(
+      mask, mult, h.mesh.gs.skip, h.mesh.nx1, h.mesh.n, bad);
+}
+
 template <typename T>
 int detect_coef(Handle& h, const T* h1, const T* h2, int64_t n, Coef<T>& c) {
   const int nb = vec_blocks(n);

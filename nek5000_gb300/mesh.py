@@ -197,7 +197,28 @@ def box_mesh(N: int, kx: int, ky: int, kz: int, periodic=(False, False, False),
     return dict(lx1=nx, nel=nel, n=n, kx=kx, ky=ky, kz=kz, D=D, zgll=z, wgll=w,
                 g=g.reshape(6, n), bm1=bm1, glo_num=glo, mask=mask, mult=mult, binv=binv,
                 vol=float(bm1.sum()), x=x.reshape(-1), y=y.reshape(-1), z=zc.reshape(-1),
-                lattice=lat)
+                lattice=lat, periodic=tuple(periodic))
+
+
+def face_mask(M, dirichlet):
+    """The mask of box_mesh's mesh M for another set of Dirichlet faces
+    (x-, x+, y-, y+, z-, z+), e.g. per velocity component."""
+    N = M["lx1"] - 1
+    per = M.get("periodic", (False, False, False))
+    ngx = M["kx"] * N + 1
+    ngy = M["ky"] * N + (0 if per[1] else 1)
+    ngz = M["kz"] * N + (0 if per[2] else 1)
+    lat = M["lattice"]
+    I, J, K = lat % ngx, (lat // ngx) % ngy, lat // (ngx * ngy)
+    mask = np.ones(M["n"])
+    for flag, on, sel in ((dirichlet[0], True, I == 0), (dirichlet[1], True, I == ngx - 1),
+                          (dirichlet[2], not per[1], J == 0),
+                          (dirichlet[3], not per[1], J == ngy - 1),
+                          (dirichlet[4], not per[2], K == 0),
+                          (dirichlet[5], not per[2], K == ngz - 1)):
+        if flag and on:
+            mask[sel] = 0.0
+    return mask
 
 
 def dssum_host(lattice, u, nglob=None):

@@ -272,6 +272,29 @@ class NekGpu:
         return self._solve_mixed(self._L.nekgpu_cggo_mixed_dev, x, f, h1, h2, mask, mult, imsh,
                                  tin, maxit, isd, binv, inner_tol)
 
+    def cggo_mixed_multi(self, xs, fs, h1, h2, masks, mult, imsh, tin, maxit, isd, binv,
+                         inner_tol=None):
+        """Several fields sharing h1, h2, mult, binv (device arrays; one x, f
+        and mask per field) in one fused mixed solve.  Returns a dict of
+        per-field lists: nouter, ninner, rbn0, rbn2, status."""
+        nf = len(xs)
+        if not (len(fs) == len(masks) == nf) or not 1 <= nf <= _capi.MULTI_MAX:
+            raise ValueError("one x, f and mask per field, at most MULTI_MAX fields")
+        for t in list(xs) + list(fs) + list(masks):
+            if not _is_dev(t):
+                raise TypeError("cggo_mixed_multi takes device arrays")
+        arr = lambda ts: (C.c_void_p * nf)(*[t.data_ptr() for t in ts])
+        no, ni = (C.c_int * nf)(), (C.c_int * nf)()
+        r0, r2, st = (C.c_double * nf)(), (C.c_double * nf)(), (C.c_int * nf)()
+        rc = self._L.nekgpu_cggo_mixed_multi_dev(
+            C.byref(self._h), C.byref(_cint(nf)), arr(xs), arr(fs), _ptr(h1), _ptr(h2),
+            arr(masks), _ptr(mult), C.byref(_cint(imsh)), C.byref(_cdouble(tin)),
+            C.byref(_cint(int(maxit))), C.byref(_cint(isd)), _ptr(binv),
+            None if inner_tol is None else C.byref(_cdouble(inner_tol)), no, ni, r0, r2, st)
+        self._check(rc)
+        return dict(nouter=list(no), ninner=list(ni), rbn0=list(r0), rbn2=list(r2),
+                    status=list(st))
+
     def hmholtz_mixed(self, name, u, rhs, h1, h2, mask, mult, imsh, tli, maxit, isd, binv,
                       inner_tol=None):
         """hmholtz with the mixed-precision solve (host arrays)."""
