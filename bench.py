@@ -61,13 +61,14 @@ def parse():
                          "0 restarted FP32 PCG per outer step")
     ap.add_argument("--workload", default="helmholtz",
                     choices=["helmholtz", "poisson-n9", "batch", "axhelm-sweep", "hsolve",
-                             "adjoint", "velocity3"],
+                             "adjoint", "velocity3", "ingest"],
                     help="helmholtz: E=32^3 N=7 (default); poisson-n9: E=24^3 N=9 Poisson; "
                          "batch: 3 velocity solves + 61 uneven Poisson problems in one batch; "
                          "axhelm-sweep: in-solve operator bandwidth at N=5,7,9, E=32^3; "
                          "hsolve: a sequence of solves with projection onto previous solutions; "
                          "adjoint: dJ/dh1 through the adjoint solve, E=16^3 N=7; "
-                         "velocity3: 3 velocity components in one fused mixed solve")
+                         "velocity3: 3 velocity components in one fused mixed solve; "
+                         "ingest: .re2 mesh ingestion on the host")
     ap.add_argument("--batch-problems", type=int, default=61)
     ap.add_argument("--fp64-shape", default=None,
                     help="pin the FP64 operator launch shape 'kind,epb' instead of autotuning")
@@ -886,6 +887,117 @@ def run_velocity3(args):
     lib.close()
 
 
+def write_box_re2(path, k, jitter=0.2, seed=6):
+    """A #v002 .re2 file of a k^3 box of straight-sided hexahedra on the unit
+    cube (interior vertices moved by up to jitter * h, elements in a seeded
+    random order), walls on every outside face."""
+    rng = np.random.default_rng(seed)
+    nv = k + 1
+    g = np.stack(np.meshgrid(*(np.arange(nv) / k,) * 3, indexing="ij"), -1)
+    inner = np.zeros((nv,) * 3, dtype=bool)
+    inner[1:-1, 1:-1, 1:-1] = True
+    g[inner] += jitter / k * rng.uniform(-1, 1, (int(inner.sum()), 3))
+    nel = k ** 3
+    order = rng.permutation(nel)
+    ex, ey, ez = order % k, (order // k) % k, order // (k * k)
+    pre = [(0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0), (0, 0, 1), (1, 0, 1), (1, 1, 1), (0, 1, 1)]
+    rec = np.zeros((nel, 25))
+    for c, (i, j, l) in enumerate(pre):
+        for d in range(3):
+            rec[:, 1 + 8 * d + c] = g[ex + i, ey + j, ez + l, d]
+    faces = []  # preprocessor faces: 1 y-, 2 x+, 3 y+, 4 x-, 5 z-, 6 z+
+    for f, on in ((1, ey == 0), (2, ex == k - 1), (3, ey == k - 1), (4, ex == 0),
+                  (5, ez == 0), (6, ez == k - 1)):
+        q = np.nonzero(on)[0]
+        b = np.zeros((len(q), 8))
+        b[:, 0], b[:, 1] = q + 1, f
+        faces.append(b)
+    bcr = np.concatenate(faces)
+    bcbytes = bcr.astype("<f8").tobytes()
+    # the type occupies the 8th word of each record
+    raw = bytearray(bcbytes)
+    for r in range(len(bcr)):
+        raw[64 * r + 56:64 * r + 64] = b"W       "
+    with open(path, "wb") as fh:
+        fh.write(f"#v002{nel:9d}{3:3d}{nel:9d} hdr".ljust(80).encode())
+        fh.write(np.float32(6.54321).tobytes())
+        fh.write(rec.astype("<f8").tobytes())
+        fh.write(np.float64(0).tobytes())          # no curved sides
+        fh.write(np.float64(len(bcr)).tobytes())   # one boundary section
+        fh.write(bytes(raw))
+    return nel
+
+
+def run_ingest(args):
+    """Mesh ingestion on the host: a k^3 box of perturbed straight-sided
+    hexahedra in a .re2 file read, its vertex connectivity computed from the
+    corners (the reference's gencon algorithm), its GLL points numbered
+    (set_vert) and placed (xyzlin) at order N, geometric factors formed and
+    the mesh handed to the GPU (nekgpu_setup)."""
+    import tempfile
+    import torch
+    from nek5000_gb300 import NekGpu, meshio
+    from nek5000_gb300 import build as nb
+    from nek5000_gb300.mesh import deriv_matrix, geometry, gll
+    nb.build()
+    k, nx = args.k, args.N + 1
+    tmp = tempfile.mkdtemp()
+    path = os.path.join(tmp, "box.re2")
+    nel = write_box_re2(path, k)
+    D = None
+    T = {"read_re2": 0.0, "connect": 0.0, "setvert3d": 0.0, "xyzlin": 0.0, "geometry": 0.0,
+         "gpu_setup": 0.0}
+    steps = max(args.steps, 1)
+    for it in range(args.warmup + steps):
+        t = [time.perf_counter()]
+        R = meshio.read_re2(path)
+        t.append(time.perf_counter())
+        vertex, nvert = meshio.connect(R["xc"], R["yc"], R["zc"], *R["bcs"][0])
+        t.append(time.perf_counter())
+        glo, ngv = meshio.setvert3d(nx, vertex)
+        t.append(time.perf_counter())
+        zg, wg = gll(nx)
+        x, y, z = meshio.xyzlin(nx, zg, R["xc"], R["yc"], R["zc"])
+        t.append(time.perf_counter())
+        shp = (nel, nx, nx, nx)
+        D = deriv_matrix(zg)
+        g, bm1, _ = geometry(x.reshape(shp), y.reshape(shp), z.reshape(shp), D, wg)
+        t.append(time.perf_counter())
+        lib = NekGpu(0)
+        lib.setup(nx, nel, D, g, bm1, glo)
+        torch.cuda.synchronize()
+        t.append(time.perf_counter())
+        lib.close()
+        del g, x, y, z
+        if it >= args.warmup:
+            for key, a, b in zip(T, t[:-1], t[1:]):
+                T[key] += (b - a) / steps
+    native = T["read_re2"] + T["connect"] + T["setvert3d"] + T["xyzlin"]
+    line = {"metric": f"mesh ingestion elements/s (.re2 read, connectivity, set_vert, xyzlin; "
+                      f"E={k}^3 N={args.N})",
+            "value": nel / native, "unit": "elements/s", "n_gpus": 1, "steps": steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * native, "higher_is_better": True,
+            "scaling": "none", "vs_baseline": None, "dtype": "f64 / int64", "data": "synthetic",
+            "config": {"workload": f"perturbed box E={k}^3 (seeded element order), N={args.N}",
+                       "elements": nel, "vertices": int(nvert), "glo_ids": int(ngv),
+                       "file_bytes": os.path.getsize(path)},
+            "ms": {kk: 1e3 * v for kk, v in T.items()},
+            "end_to_end_ms_incl_geometry_and_gpu_setup": 1e3 * sum(T.values())}
+    if not args.no_cpu:
+        from oracle import nekref
+        t0 = time.perf_counter()
+        glo_ref, ngv_ref = nekref.setvert3d(nx, nel, vertex.reshape(-1))
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": nel / dt, "unit": "elements/s (set_vert only)",
+                                "cores": 1, "kind": "port",
+                                "sample": "the oracle's restatement of set_vert on the same "
+                                          "vertex ids (gencon is Fortran: no compiler here)",
+                                "identical_glo_num": bool(np.array_equal(glo, glo_ref))}
+    print(json.dumps(line), flush=True)
+    os.remove(path)
+    os.rmdir(tmp)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -900,6 +1012,8 @@ def main():
         run_adjoint(args)
     elif args.workload == "velocity3":
         run_velocity3(args)
+    elif args.workload == "ingest":
+        run_ingest(args)
     else:
         run_gpu(args)
 

@@ -1,0 +1,102 @@
+/*
+ * nekmesh.h -- host-side mesh ingestion for the solve path: the reference's
+ * mesh (.re2) and connectivity (.co2) files, vertex connectivity computed
+ * from element corners, the global numbering of GLL points and the GLL
+ * coordinates of straight-sided elements.  These produce the arrays
+ * nekgpu_setup takes (glo_num, and the coordinates the geometric factors are
+ * computed from) for meshes that are not boxes.
+ *
+ * Host code only: no GPU is touched.  Arrays are the reference's layouts:
+ * element corners (2^ndim per element) in the file's (preprocessor) corner
+ * order unless a name says "tensor" order (corner i + 2 j + 4 k); faces in
+ * the preprocessor face order the reference keeps cbc/bc in.  Element and
+ * vertex numbers are 1-based, as in the reference.
+ *
+ * Status: 0 or a negative NEKGPU_E* code (nekgpu.h); NEKGPU_EIO for a file
+ * that cannot be read or does not follow the format.  nekmesh_last_error()
+ * gives the message of the calling thread's last failure.
+ */
+#ifndef NEKMESH_H
+#define NEKMESH_H
+#include <stdint.h>
+
+#include "nekgpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NEKGPU_EIO (-8) /* file missing, short or not in the expected format */
+
+int nekmesh_last_error(char *buf, const int *buflen);
+
+/* ---- .re2 (core/reader_re2.f) -------------------------------------------- */
+/* Reads a whole .re2 file: the 80-byte header (read_re2_hdr :543-620,
+ * versions #v001 with 4-byte words, #v002/#v003/#v004 with 8-byte words),
+ * the byte-order test value 6.54321, the element records (group and corner
+ * coordinates, readp_re2_mesh :68-157, buf_to_xyz :430-471), the curved-side
+ * records (readp_re2_curve :159-286, buf_to_curve :473-501) and every
+ * boundary-condition section present (readp_re2_bc :288-428, buf_to_bc
+ * :503-541).  Files of either byte order are read. */
+int nekmesh_re2_open(const char *path, int64_t *mesh);
+/* nelgt, ndim, nelgv from the header; wdsize 4 or 8; the number of
+ * curved-side records; the number of boundary-condition sections. */
+int nekmesh_re2_header(const int64_t *mesh, int *nelgt, int *ndim, int *nelgv, int *wdsize,
+                       int64_t *ncurve, int *nbcfield);
+/* Corner coordinates xc, yc, zc (2^ndim per element, file order; zc may be
+ * null for ndim = 2) and the element groups (may be null). */
+int nekmesh_re2_xyz(const int64_t *mesh, double *xc, double *yc, double *zc, int *group);
+/* The curved-side records: element (1-based), side, the 5 curve values and
+ * the curve type character; any output may be null. */
+int nekmesh_re2_curves(const int64_t *mesh, int *elem, int *side, double *curve, char *ccurve);
+/* Boundary-condition section *field (0-based, in file order) as the
+ * reference's dense arrays: cbc[(e*2ndim + f)*3 .. +3] the 3-character type
+ * ("E  " where the file has no record), bc[(e*2ndim + f)*5 .. +5] its values
+ * (0 where no record). */
+int nekmesh_re2_bc(const int64_t *mesh, const int *field, char *cbc, double *bc);
+int nekmesh_re2_close(int64_t *mesh);
+
+/* ---- .co2 (core/map2.f read_con :327-471) --------------------------------- */
+/* Reads the header (132 bytes: #v001 fixed format a5,3i12 or #v002 free
+ * format: nelgt nelgv nv), the byte-order test value and the records (element
+ * id and nv vertex ids, 4-byte integers).  vertex (nv * nelgt, element-major,
+ * placed by element id) may be null to query the sizes. */
+int nekmesh_co2_read(const char *path, int *nelgt, int *nelgv, int *nv, int64_t *vertex);
+/* Writes a #v001 .co2 file, as tools/gencon dmpfile does. */
+int nekmesh_co2_write(const char *path, const int *nelgt, const int *nelgv, const int *nv,
+                      const int64_t *vertex);
+
+/* ---- connectivity from coordinates (tools/gencon/gencon.f) ----------------- */
+/* Global vertex ids (tensor corner order, 1-based, ranked) of nel elements in
+ * ndim = 3 from their corners (file order): corners closer than tol times
+ * the smaller of their elements' shortest corner-to-neighbour distance are one
+ * vertex (unique_vertex2 :1708-1812, set_d2 :308-343; tol 0.2 is gencon's
+ * default); faces sharing three vertices with a neighbour get the fourth
+ * (face_chk :1827-1925); faces of type "P  " in cbc/bc (the first
+ * boundary-condition section, preprocessor face order; may be null) are
+ * joined with the face their bc values name (periodic_vtx :1296-1411,
+ * find_connctd_pairs :1413-1540).  Fails with NEKGPU_EINVAL when an element
+ * ends up with a repeated vertex (self_chk) or a periodic face pair does not
+ * match. */
+int nekmesh_connect(const int *nel, const int *ndim, const double *xc, const double *yc,
+                    const double *zc, const char *cbc, const double *bc, const double *tol,
+                    int64_t *vertex, int64_t *nvert);
+
+/* ---- global numbering (core/navier8.f setvert3d :2004-2183) ---------------- */
+/* glo_num (nx^3 per element) of nel elements from their vertex ids (tensor
+ * corner order): vertices keep their ids, edge and face interiors are
+ * numbered by the ranked edges and faces in the reference's orientation,
+ * element interiors get 0; *ngv = the number of ids used. */
+int nekmesh_setvert3d(const int *nx, const int *nel, const int64_t *vertex, int64_t *glo_num,
+                      int64_t *ngv);
+
+/* ---- GLL coordinates of straight-sided elements (core/genxyz.f xyzlin) ---- */
+/* x, y, z (nx^3 per element) by the trilinear map of the corners xc, yc, zc
+ * (file order) at the GLL nodes zgll[0..nx-1] (xyzlin :1269-1320). */
+int nekmesh_xyzlin(const int *nx, const int *nel, const double *zgll, const double *xc,
+                   const double *yc, const double *zc, double *x, double *y, double *z);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libnekgpu.so")
 
 OK = 0
-EINVAL, EHANDLE, ECUDA, ENOMEM, ENOTCONV, ENOSETUP, ENAN = -1, -2, -3, -4, -5, -6, -7
+EINVAL, EHANDLE, ECUDA, ENOMEM, ENOTCONV, ENOSETUP, ENAN, EIO = -1, -2, -3, -4, -5, -6, -7, -8
 OPT_EXACT, OPT_TIMING, OPT_CHUNK, OPT_ISTEP, OPT_TMA, OPT_GRAPH, OPT_MIXED_MODE = (
     1, 2, 3, 4, 5, 6, 7)
 OPT_AUTOTUNE = 8
@@ -26,6 +26,7 @@ MULTI_MAX = 3
 STATUS_NAMES = {
     0: "NEKGPU_OK", -1: "NEKGPU_EINVAL", -2: "NEKGPU_EHANDLE", -3: "NEKGPU_ECUDA",
     -4: "NEKGPU_ENOMEM", -5: "NEKGPU_ENOTCONV", -6: "NEKGPU_ENOSETUP", -7: "NEKGPU_ENAN",
+    -8: "NEKGPU_EIO",
 }
 
 # Every exported entry point and its argument types.  Pointer arguments are
@@ -36,6 +37,20 @@ _I64P = C.POINTER(C.c_int64)
 _IP = C.POINTER(C.c_int)
 _DP = C.POINTER(C.c_double)
 SIGNATURES = {
+    # mesh ingestion (include/nekmesh.h): host code
+    "nekmesh_last_error": [C.c_char_p, _IP],
+    "nekmesh_re2_open": [C.c_char_p, _I64P],
+    "nekmesh_re2_header": [_I64P, _IP, _IP, _IP, _IP, _I64P, _IP],
+    "nekmesh_re2_xyz": [_I64P, _P, _P, _P, _P],
+    "nekmesh_re2_curves": [_I64P, _P, _P, _P, _P],
+    "nekmesh_re2_bc": [_I64P, _IP, _P, _P],
+    "nekmesh_re2_close": [_I64P],
+    "nekmesh_co2_read": [C.c_char_p, _IP, _IP, _IP, _P],
+    "nekmesh_co2_write": [C.c_char_p, _IP, _IP, _IP, _P],
+    "nekmesh_connect": [_IP, _IP, _P, _P, _P, _P, _P, _DP, _P, _I64P],
+    "nekmesh_setvert3d": [_IP, _IP, _P, _P, _I64P],
+    "nekmesh_xyzlin": [_IP, _IP, _P, _P, _P, _P, _P, _P, _P],
+    # solve path (include/nekgpu.h)
     "nekgpu_init": [_IP, _I64P],
     "nekgpu_finalize": [_I64P],
     "nekgpu_last_error": [_I64P, C.c_char_p, _IP],

@@ -13,10 +13,18 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libnekgpu.so")
-SOURCES = ["axhelm_f64.cu", "axhelm_f32.cu", "axhelm_tma.cu", "tune.cu", "gs.cu", "pcg.cu", "mixed.cu", "batch.cu", "adjoint.cu", "proj.cu", "multi.cu", "noalloc.cu", "capi.cu"]
+SOURCES = ["axhelm_f64.cu", "axhelm_f32.cu", "axhelm_tma.cu", "tune.cu", "gs.cu", "pcg.cu", "mixed.cu", "batch.cu", "adjoint.cu", "proj.cu", "multi.cu", "noalloc.cu", "capi.cu",
+           "meshio.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
          "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
+# host-only sources: no contraction into fused multiply-adds, so that x86 and
+# aarch64 hosts round the same way
+HOST_FLAGS = ["-Xcompiler", "-ffp-contract=off"]
+
+
+def _obj(src: str) -> str:
+    return os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
 
 
 def nvcc() -> str:
@@ -36,14 +44,15 @@ def _stale(obj: str, deps) -> bool:
 def build(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
-    headers.append(os.path.join(ROOT, "include", "nekgpu.h"))
+    headers += [os.path.join(ROOT, "include", h) for h in ("nekgpu.h", "nekmesh.h")]
     nv = nvcc()
     jobs = []
     for src in SOURCES:
         s = os.path.join(CSRC, src)
-        o = os.path.join(BUILD, src.replace(".cu", ".o"))
+        o = _obj(src)
         if force or _stale(o, [s] + headers):
-            jobs.append([nv, *ARCH, *FLAGS, "-c", s, "-o", o])
+            extra = HOST_FLAGS if src.endswith(".cpp") else []
+            jobs.append([nv, *ARCH, *FLAGS, *extra, "-c", s, "-o", o])
     if jobs:
         with cf.ThreadPoolExecutor(max_workers=len(jobs)) as ex:
             futs = [ex.submit(subprocess.run, j, capture_output=True, text=True) for j in jobs]
@@ -53,7 +62,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
                     print(r.stdout)
                 if r.returncode != 0:
                     raise RuntimeError(f"nvcc failed: {' '.join(j)}\n{r.stdout}\n{r.stderr}")
-    objs = [os.path.join(BUILD, s.replace(".cu", ".o")) for s in SOURCES]
+    objs = [_obj(s) for s in SOURCES]
     if force or jobs or _stale(LIB, objs):
         r = subprocess.run([nv, *ARCH, "-shared", "-o", LIB, *objs], capture_output=True, text=True)
         if r.returncode != 0:

@@ -1,0 +1,839 @@
+// meshio.cpp -- mesh ingestion on the host: the reference's .re2 mesh and
+// .co2 connectivity files, vertex connectivity from element corners (the
+// reference's gencon tool), the global numbering of GLL points (set_vert)
+// and the GLL coordinates of straight-sided elements (xyzlin).  Host code
+// only; the arrays produced are what nekgpu_setup consumes.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <numeric>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "nekmesh.h"
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+// ---- raw file access ---------------------------------------------------------
+bool slurp(const char* path, std::vector<unsigned char>& buf) {
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return false;
+  std::fseek(f, 0, SEEK_END);
+  const long sz = std::ftell(f);
+  std::fseek(f, 0, SEEK_SET);
+  if (sz < 0) {
+    std::fclose(f);
+    return false;
+  }
+  buf.resize((size_t)sz);
+  const size_t got = sz ? std::fread(buf.data(), 1, (size_t)sz, f) : 0;
+  std::fclose(f);
+  return got == (size_t)sz;
+}
+
+// Words of a binary mesh file: 4 or 8 bytes, either byte order.  Integers in
+// 8-byte files are stored as reals (the reference converts them by
+// truncation, copyi4 in core/math.f:269).
+struct Words {
+  const unsigned char* p = nullptr;
+  size_t size = 0;
+  bool swap = false;
+  int wd = 8;
+
+  bool has(size_t off, size_t n) const { return off <= size && n <= size - off; }
+  uint32_t u32(size_t off) const {
+    unsigned char b[4];
+    std::memcpy(b, p + off, 4);
+    if (swap) std::reverse(b, b + 4);
+    uint32_t v;
+    std::memcpy(&v, b, 4);
+    return v;
+  }
+  uint64_t u64(size_t off) const {
+    unsigned char b[8];
+    std::memcpy(b, p + off, 8);
+    if (swap) std::reverse(b, b + 8);
+    uint64_t v;
+    std::memcpy(&v, b, 8);
+    return v;
+  }
+  double real(size_t off) const {
+    if (wd == 8) {
+      const uint64_t u = u64(off);
+      double d;
+      std::memcpy(&d, &u, 8);
+      return d;
+    }
+    const uint32_t u = u32(off);
+    float f;
+    std::memcpy(&f, &u, 4);
+    return (double)f;
+  }
+  int64_t integer(size_t off) const {
+    if (wd == 8) return (int64_t)real(off);  // truncation, as copyi4
+    return (int64_t)(int32_t)u32(off);
+  }
+};
+
+// The byte-order test value every binary file carries after its header.
+bool byte_order(const unsigned char* p, bool* swap) {
+  for (int s = 0; s < 2; ++s) {
+    unsigned char b[4];
+    std::memcpy(b, p, 4);
+    if (s) std::reverse(b, b + 4);
+    float f;
+    std::memcpy(&f, b, 4);
+    if (std::fabs(f - 6.54321f) < 1e-5f) {
+      *swap = s != 0;
+      return true;
+    }
+  }
+  return false;
+}
+
+// Integer field [a, b) of a fixed-format header (blanks allowed).
+bool field_int(const std::string& h, size_t a, size_t b, int64_t* v) {
+  if (a >= h.size()) return false;
+  std::string s = h.substr(a, b - a);
+  char* end = nullptr;
+  const long long x = std::strtoll(s.c_str(), &end, 10);
+  if (end == s.c_str()) return false;
+  *v = x;
+  return true;
+}
+
+// ---- .re2 --------------------------------------------------------------------
+struct Curve {
+  int64_t e;
+  int side;
+  double v[5];
+  char type;
+};
+struct Bc {
+  int64_t e;
+  int face;
+  double v[5];
+  char type[3];
+};
+struct Re2 {
+  std::string version;
+  int wd = 8, ndim = 3;
+  int64_t nelgt = 0, nelgv = 0;
+  std::vector<int> group;
+  std::vector<double> xc, yc, zc;  // 2^ndim per element, file order
+  std::vector<Curve> curves;
+  std::vector<std::vector<Bc>> bcs;
+};
+
+std::mutex g_mu;
+std::unordered_map<int64_t, std::unique_ptr<Re2>> g_meshes;
+int64_t g_next = 1;
+
+Re2* lookup(const int64_t* h) {
+  if (!h) return nullptr;
+  std::lock_guard<std::mutex> lk(g_mu);
+  auto it = g_meshes.find(*h);
+  return it == g_meshes.end() ? nullptr : it->second.get();
+}
+
+int read_re2(const char* path, Re2& m) {
+  std::vector<unsigned char> buf;
+  if (!path || !slurp(path, buf)) return fail(NEKGPU_EIO, std::string("cannot read ") + (path ? path : "(null)"));
+  if (buf.size() < 84) return fail(NEKGPU_EIO, "re2: file shorter than its header");
+  const std::string hdr(reinterpret_cast<const char*>(buf.data()), 80);
+  m.version = hdr.substr(0, 5);
+  if (m.version.size() != 5 || m.version[0] != '#' || m.version[1] != 'v')
+    return fail(NEKGPU_EIO, "re2: no #vNNN version in the header");
+  int64_t ndim = 0;
+  if (m.version == "#v004") {  // free format: version nelgt ndim nelgv nbc
+    char v[8];
+    long long a = 0, c = 0, nb = 0;
+    int d = 0;
+    if (std::sscanf(hdr.c_str(), "%5s %lld %d %lld %lld", v, &a, &d, &c, &nb) < 4)
+      return fail(NEKGPU_EIO, "re2: unreadable #v004 header");
+    m.nelgt = a;
+    ndim = d;
+    m.nelgv = c;
+  } else if (!field_int(hdr, 5, 14, &m.nelgt) || !field_int(hdr, 14, 17, &ndim) ||
+             !field_int(hdr, 17, 26, &m.nelgv)) {
+    return fail(NEKGPU_EIO, "re2: unreadable header (format a5,i9,i3,i9)");
+  }
+  m.wd = (m.version == "#v002" || m.version == "#v003" || m.version == "#v004") ? 8 : 4;
+  m.ndim = (int)ndim;
+  if (m.ndim != 2 && m.ndim != 3) return fail(NEKGPU_EIO, "re2: ndim must be 2 or 3");
+  if (m.nelgt <= 0 || m.nelgv <= 0 || m.nelgv > m.nelgt)
+    return fail(NEKGPU_EIO, "re2: invalid element counts in the header");
+  Words w;
+  w.p = buf.data();
+  w.size = buf.size();
+  w.wd = m.wd;
+  if (!byte_order(buf.data() + 80, &w.swap)) return fail(NEKGPU_EIO, "re2: byte-order test value not found");
+  const int nv = 1 << m.ndim;
+  const size_t rec = (size_t)(1 + m.ndim * nv) * m.wd;  // group, x(nv), y(nv)[, z(nv)]
+  size_t off = 84;
+  if (!w.has(off, rec * (size_t)m.nelgt)) return fail(NEKGPU_EIO, "re2: file ends inside the element records");
+  const size_t ne = (size_t)m.nelgt;
+  m.group.resize(ne);
+  m.xc.resize(ne * nv);
+  m.yc.resize(ne * nv);
+  m.zc.assign(m.ndim == 3 ? ne * nv : 0, 0.0);
+  for (size_t e = 0; e < ne; ++e, off += rec) {
+    m.group[e] = (int)w.integer(off);
+    for (int c = 0; c < nv; ++c) {
+      m.xc[e * nv + c] = w.real(off + (size_t)(1 + c) * m.wd);
+      m.yc[e * nv + c] = w.real(off + (size_t)(1 + nv + c) * m.wd);
+      if (m.ndim == 3) m.zc[e * nv + c] = w.real(off + (size_t)(1 + 2 * nv + c) * m.wd);
+    }
+  }
+  // curved sides: a count word, then records eg, side, curve(5), type
+  const size_t r8 = (size_t)8 * m.wd;
+  if (!w.has(off, m.wd)) return fail(NEKGPU_EIO, "re2: file ends before the curved-side count");
+  const int64_t ncurve = w.integer(off);
+  off += m.wd;
+  if (ncurve < 0 || !w.has(off, r8 * (size_t)ncurve))
+    return fail(NEKGPU_EIO, "re2: file ends inside the curved-side records");
+  m.curves.resize((size_t)ncurve);
+  for (int64_t q = 0; q < ncurve; ++q, off += r8) {
+    Curve& c = m.curves[(size_t)q];
+    c.e = w.integer(off);
+    c.side = (int)w.integer(off + m.wd);
+    for (int k = 0; k < 5; ++k) c.v[k] = w.real(off + (size_t)(2 + k) * m.wd);
+    c.type = (char)buf[off + 7 * (size_t)m.wd];  // characters are not byte-swapped
+    if (c.e < 1 || c.e > m.nelgt) return fail(NEKGPU_EIO, "re2: curved-side record names no element");
+  }
+  // boundary-condition sections until the end of the file
+  while (off < buf.size()) {
+    if (!w.has(off, m.wd)) return fail(NEKGPU_EIO, "re2: truncated boundary-condition count");
+    const int64_t nbc = w.integer(off);
+    off += m.wd;
+    if (nbc < 0 || !w.has(off, r8 * (size_t)nbc))
+      return fail(NEKGPU_EIO, "re2: file ends inside the boundary-condition records");
+    std::vector<Bc> sec((size_t)nbc);
+    for (int64_t q = 0; q < nbc; ++q, off += r8) {
+      Bc& b = sec[(size_t)q];
+      b.e = w.integer(off);
+      b.face = (int)w.integer(off + m.wd);
+      for (int k = 0; k < 5; ++k) b.v[k] = w.real(off + (size_t)(2 + k) * m.wd);
+      std::memcpy(b.type, &buf[off + 7 * (size_t)m.wd], 3);
+      if (b.e < 1 || b.e > m.nelgt || b.face < 1 || b.face > 2 * m.ndim)
+        return fail(NEKGPU_EIO, "re2: boundary-condition record names no element face");
+    }
+    m.bcs.push_back(std::move(sec));
+  }
+  return NEKGPU_OK;
+}
+
+// ---- connectivity (the algorithm of the reference's gencon tool) -------------
+// Corner order conversions: the file (preprocessor) order lists the bottom
+// face counter-clockwise, then the top; tensor order is i + 2 j + 4 k.
+constexpr int kPreOfTensor[8] = {0, 1, 3, 2, 4, 5, 7, 6};
+// Preprocessor face of each tensor face (r-, r+, s-, s+, t-, t+), and back.
+constexpr int kPreFace[6] = {4, 2, 1, 3, 5, 6};
+constexpr int kTensorFace[6] = {3, 2, 4, 1, 5, 6};
+// Corners of each tensor face in circulant order (counter-clockwise seen
+// from outside), used to match periodic face pairs.
+constexpr int kFaceCycle[6][4] = {{0, 4, 6, 2}, {1, 3, 7, 5}, {0, 1, 5, 4},
+                                  {2, 6, 7, 3}, {0, 2, 3, 1}, {4, 5, 7, 6}};
+// Corners of each tensor face (face_chk order).
+constexpr int kFaceCorners[6][4] = {{0, 2, 4, 6}, {1, 3, 5, 7}, {0, 1, 4, 5},
+                                    {2, 3, 6, 7}, {0, 1, 2, 3}, {4, 5, 6, 7}};
+// The three edge neighbours of each tensor corner.
+constexpr int kNeighbour[8][3] = {{1, 2, 4}, {0, 3, 5}, {0, 3, 6}, {1, 2, 7},
+                                  {0, 5, 6}, {1, 4, 7}, {2, 4, 7}, {3, 5, 6}};
+
+struct Dsu {
+  std::vector<int64_t> parent;
+  explicit Dsu(int64_t n) : parent((size_t)n) { std::iota(parent.begin(), parent.end(), 0); }
+  int64_t find(int64_t a) {
+    while (parent[(size_t)a] != a) {
+      parent[(size_t)a] = parent[(size_t)parent[(size_t)a]];
+      a = parent[(size_t)a];
+    }
+    return a;
+  }
+  // the representative of a set is its smallest member
+  void join(int64_t a, int64_t b) {
+    a = find(a);
+    b = find(b);
+    if (a == b) return;
+    if (b < a) std::swap(a, b);
+    parent[(size_t)b] = a;
+  }
+};
+
+// Rank the values of ids (1-based, ascending order of value).
+int64_t rank_ids(std::vector<int64_t>& ids) {
+  std::vector<int64_t> u(ids);
+  std::sort(u.begin(), u.end());
+  u.erase(std::unique(u.begin(), u.end()), u.end());
+  for (auto& v : ids) v = (int64_t)(std::lower_bound(u.begin(), u.end(), v) - u.begin()) + 1;
+  return (int64_t)u.size();
+}
+
+// Lexicographic segmentation of all element corners (unique_vertex2): within
+// each segment, sort by one coordinate and cut where neighbours differ by
+// more than tol times the smaller of their characteristic lengths; ndim
+// passes over the ndim coordinates.  Corners left in one segment are one
+// vertex; vertex ids are the segments' ranks in the final order.
+std::vector<int64_t> unique_vertices(const std::vector<double>& X, const std::vector<double>& L2,
+                                     int64_t n, double tol) {
+  const double qq = tol * tol;
+  std::vector<int64_t> order((size_t)n);
+  std::iota(order.begin(), order.end(), 0);
+  std::vector<char> cut((size_t)n, 0);
+  if (n) cut[0] = 1;
+  for (int pass = 0; pass < 3; ++pass)
+    for (int j = 0; j < 3; ++j) {
+      int64_t a = 0;
+      while (a < n) {
+        int64_t b = a + 1;
+        while (b < n && !cut[(size_t)b]) ++b;
+        std::stable_sort(order.begin() + a, order.begin() + b, [&](int64_t p, int64_t q) {
+          return X[(size_t)(3 * p + j)] < X[(size_t)(3 * q + j)];
+        });
+        a = b;
+      }
+      for (int64_t i = 1; i < n; ++i) {
+        const int64_t p = order[(size_t)i], q = order[(size_t)(i - 1)];
+        const double d = X[(size_t)(3 * p + j)] - X[(size_t)(3 * q + j)];
+        if (d * d > qq * std::min(L2[(size_t)p], L2[(size_t)q])) cut[(size_t)i] = 1;
+      }
+    }
+  std::vector<int64_t> id((size_t)n);
+  int64_t g = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    if (cut[(size_t)i]) ++g;
+    id[(size_t)order[(size_t)i]] = g;
+  }
+  return id;
+}
+
+// face_chk: a face of element e whose corners are shared, three of four, with
+// element f gets the fourth joined to the corner of f's matching face that
+// e does not share.  Returns whether a join was made.
+bool repair_faces(std::vector<int64_t>& cell, int64_t nel) {
+  // vertex -> elements
+  int64_t nvid = 0;
+  for (auto v : cell) nvid = std::max(nvid, v);
+  std::vector<int64_t> start((size_t)nvid + 2, 0);
+  for (auto v : cell) ++start[(size_t)v + 1];
+  for (size_t i = 1; i < start.size(); ++i) start[i] += start[i - 1];
+  std::vector<int64_t> elems(cell.size());
+  {
+    std::vector<int64_t> fill(start.begin(), start.end() - 1);
+    for (int64_t e = 0; e < nel; ++e)
+      for (int c = 0; c < 8; ++c) elems[(size_t)fill[(size_t)cell[(size_t)(8 * e + c)]]++] = e;
+  }
+  auto touches = [&](int64_t v, int64_t e) {
+    for (int64_t k = start[(size_t)v]; k < start[(size_t)v + 1]; ++k)
+      if (elems[(size_t)k] == e) return true;
+    return false;
+  };
+  std::vector<int64_t> share;
+  for (int64_t e = 0; e < nel; ++e)
+    for (int f = 0; f < 6; ++f) {
+      share.clear();
+      for (int c = 0; c < 4; ++c) {
+        const int64_t v = cell[(size_t)(8 * e + kFaceCorners[f][c])];
+        for (int64_t k = start[(size_t)v]; k < start[(size_t)v + 1]; ++k)
+          if (elems[(size_t)k] != e) share.push_back(elems[(size_t)k]);
+      }
+      std::sort(share.begin(), share.end());
+      for (size_t a = 0; a < share.size();) {
+        size_t b = a;
+        while (b < share.size() && share[b] == share[a]) ++b;
+        if (b - a == 3) {  // three corners shared with element o: find the fourth
+          const int64_t o = share[a];
+          int miss = -1;
+          for (int c = 0; c < 4; ++c)
+            if (!touches(cell[(size_t)(8 * e + kFaceCorners[f][c])], o)) miss = kFaceCorners[f][c];
+          // o's face with three corners on e, and its corner not on e
+          int other = -1;
+          for (int g = 0; g < 6 && other < 0; ++g) {
+            int cnt = 0, lone = -1;
+            for (int c = 0; c < 4; ++c) {
+              if (touches(cell[(size_t)(8 * o + kFaceCorners[g][c])], e)) ++cnt;
+              else lone = kFaceCorners[g][c];
+            }
+            if (cnt == 3) other = lone;
+          }
+          if (miss < 0 || other < 0) return false;
+          const int64_t v1 = cell[(size_t)(8 * e + miss)], v2 = cell[(size_t)(8 * o + other)];
+          const int64_t keep = std::min(v1, v2), drop = std::max(v1, v2);
+          for (auto& v : cell)
+            if (v == drop) v = keep;
+          return true;
+        }
+        a = b;
+      }
+    }
+  return false;
+}
+
+}  // namespace
+
+// =============================================================================
+// C ABI
+extern "C" {
+
+int nekmesh_last_error(char* buf, const int* buflen) {
+  if (!buf || !buflen || *buflen <= 0) return NEKGPU_EINVAL;
+  std::snprintf(buf, (size_t)*buflen, "%s", g_err.c_str());
+  return NEKGPU_OK;
+}
+
+int nekmesh_re2_open(const char* path, int64_t* mesh) {
+  if (!mesh) return fail(NEKGPU_EINVAL, "null mesh handle");
+  auto m = std::make_unique<Re2>();
+  const int rc = read_re2(path, *m);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lk(g_mu);
+  *mesh = g_next++;
+  g_meshes[*mesh] = std::move(m);
+  return NEKGPU_OK;
+}
+
+int nekmesh_re2_header(const int64_t* mesh, int* nelgt, int* ndim, int* nelgv, int* wdsize,
+                       int64_t* ncurve, int* nbcfield) {
+  Re2* m = lookup(mesh);
+  if (!m) return fail(NEKGPU_EHANDLE, "unknown mesh handle");
+  if (nelgt) *nelgt = (int)m->nelgt;
+  if (ndim) *ndim = m->ndim;
+  if (nelgv) *nelgv = (int)m->nelgv;
+  if (wdsize) *wdsize = m->wd;
+  if (ncurve) *ncurve = (int64_t)m->curves.size();
+  if (nbcfield) *nbcfield = (int)m->bcs.size();
+  return NEKGPU_OK;
+}
+
+int nekmesh_re2_xyz(const int64_t* mesh, double* xc, double* yc, double* zc, int* group) {
+  Re2* m = lookup(mesh);
+  if (!m) return fail(NEKGPU_EHANDLE, "unknown mesh handle");
+  if (xc) std::copy(m->xc.begin(), m->xc.end(), xc);
+  if (yc) std::copy(m->yc.begin(), m->yc.end(), yc);
+  if (zc && m->ndim == 3) std::copy(m->zc.begin(), m->zc.end(), zc);
+  if (group) std::copy(m->group.begin(), m->group.end(), group);
+  return NEKGPU_OK;
+}
+
+int nekmesh_re2_curves(const int64_t* mesh, int* elem, int* side, double* curve, char* ccurve) {
+  Re2* m = lookup(mesh);
+  if (!m) return fail(NEKGPU_EHANDLE, "unknown mesh handle");
+  for (size_t q = 0; q < m->curves.size(); ++q) {
+    const Curve& c = m->curves[q];
+    if (elem) elem[q] = (int)c.e;
+    if (side) side[q] = c.side;
+    if (curve) std::copy(c.v, c.v + 5, curve + 5 * q);
+    if (ccurve) ccurve[q] = c.type;
+  }
+  return NEKGPU_OK;
+}
+
+int nekmesh_re2_bc(const int64_t* mesh, const int* field, char* cbc, double* bc) {
+  Re2* m = lookup(mesh);
+  if (!m) return fail(NEKGPU_EHANDLE, "unknown mesh handle");
+  if (!field || *field < 0 || *field >= (int)m->bcs.size())
+    return fail(NEKGPU_EINVAL, "no such boundary-condition section");
+  const int nf = 2 * m->ndim;
+  const size_t nfe = (size_t)m->nelgt * nf;
+  if (cbc)
+    for (size_t q = 0; q < nfe; ++q) std::memcpy(cbc + 3 * q, "E  ", 3);
+  if (bc) std::fill(bc, bc + 5 * nfe, 0.0);
+  for (const Bc& b : m->bcs[(size_t)*field]) {
+    const size_t q = (size_t)(b.e - 1) * nf + (size_t)(b.face - 1);
+    if (cbc) std::memcpy(cbc + 3 * q, b.type, 3);
+    if (bc) std::copy(b.v, b.v + 5, bc + 5 * q);
+  }
+  return NEKGPU_OK;
+}
+
+int nekmesh_re2_close(int64_t* mesh) {
+  if (!mesh) return fail(NEKGPU_EINVAL, "null mesh handle");
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!g_meshes.erase(*mesh)) return fail(NEKGPU_EHANDLE, "unknown mesh handle");
+  *mesh = 0;
+  return NEKGPU_OK;
+}
+
+int nekmesh_co2_read(const char* path, int* nelgt, int* nelgv, int* nv, int64_t* vertex) {
+  std::vector<unsigned char> buf;
+  if (!path || !slurp(path, buf)) return fail(NEKGPU_EIO, std::string("cannot read ") + (path ? path : "(null)"));
+  if (buf.size() < 136) return fail(NEKGPU_EIO, "co2: file shorter than its header");
+  const std::string hdr(reinterpret_cast<const char*>(buf.data()), 132);
+  const std::string version = hdr.substr(0, 5);
+  int64_t a = 0, b = 0, c = 0;
+  if (version == "#v002") {
+    char v[8];
+    long long x = 0, y = 0, z = 0;
+    if (std::sscanf(hdr.c_str(), "%5s %lld %lld %lld", v, &x, &y, &z) != 4)
+      return fail(NEKGPU_EIO, "co2: unreadable #v002 header");
+    a = x;
+    b = y;
+    c = z;
+  } else if (!field_int(hdr, 5, 17, &a) || !field_int(hdr, 17, 29, &b) || !field_int(hdr, 29, 41, &c)) {
+    return fail(NEKGPU_EIO, "co2: unreadable header (format a5,3i12)");
+  }
+  if (a <= 0 || b <= 0 || b > a || (c != 4 && c != 8)) return fail(NEKGPU_EIO, "co2: invalid sizes in the header");
+  Words w;
+  w.p = buf.data();
+  w.size = buf.size();
+  w.wd = 4;
+  if (!byte_order(buf.data() + 132, &w.swap)) return fail(NEKGPU_EIO, "co2: byte-order test value not found");
+  if (nelgt) *nelgt = (int)a;
+  if (nelgv) *nelgv = (int)b;
+  if (nv) *nv = (int)c;
+  if (!vertex) return NEKGPU_OK;
+  const size_t rec = (size_t)(c + 1) * 4;
+  if (!w.has(136, rec * (size_t)a)) return fail(NEKGPU_EIO, "co2: file ends inside the records");
+  std::vector<char> seen((size_t)a, 0);
+  for (int64_t r = 0; r < a; ++r) {
+    const size_t off = 136 + rec * (size_t)r;
+    const int64_t eid = (int64_t)(int32_t)w.u32(off);
+    if (eid < 1 || eid > a || seen[(size_t)(eid - 1)])
+      return fail(NEKGPU_EIO, "co2: element ids are not a permutation of 1..nelgt");
+    seen[(size_t)(eid - 1)] = 1;
+    for (int64_t k = 0; k < c; ++k)
+      vertex[(size_t)((eid - 1) * c + k)] = (int64_t)(int32_t)w.u32(off + 4 * (size_t)(k + 1));
+  }
+  return NEKGPU_OK;
+}
+
+int nekmesh_co2_write(const char* path, const int* nelgt, const int* nelgv, const int* nv,
+                      const int64_t* vertex) {
+  if (!path || !nelgt || !nelgv || !nv || !vertex || *nelgt <= 0 || *nelgv <= 0 ||
+      *nelgv > *nelgt || (*nv != 4 && *nv != 8))
+    return fail(NEKGPU_EINVAL, "co2 write: bad arguments");
+  FILE* f = std::fopen(path, "wb");
+  if (!f) return fail(NEKGPU_EIO, std::string("cannot write ") + path);
+  char hdr[133];
+  std::memset(hdr, ' ', 132);
+  char tmp[64];
+  const int len = std::snprintf(tmp, sizeof tmp, "#v001%12d%12d%12d", *nelgt, *nelgv, *nv);
+  std::memcpy(hdr, tmp, (size_t)len);
+  const float test = 6.54321f;
+  bool ok = std::fwrite(hdr, 1, 132, f) == 132 && std::fwrite(&test, 4, 1, f) == 1;
+  std::vector<int32_t> rec((size_t)*nv + 1);
+  for (int e = 0; ok && e < *nelgt; ++e) {
+    rec[0] = e + 1;
+    for (int k = 0; k < *nv; ++k) {
+      const int64_t v = vertex[(size_t)e * *nv + k];
+      if (v < 1 || v > INT32_MAX) ok = false;
+      rec[(size_t)k + 1] = (int32_t)v;
+    }
+    ok = ok && std::fwrite(rec.data(), 4, rec.size(), f) == rec.size();
+  }
+  ok = (std::fclose(f) == 0) && ok;
+  return ok ? NEKGPU_OK : fail(NEKGPU_EIO, std::string("co2 write failed: ") + path);
+}
+
+int nekmesh_connect(const int* nel_, const int* ndim_, const double* xc, const double* yc,
+                    const double* zc, const char* cbc, const double* bc, const double* tol_,
+                    int64_t* vertex, int64_t* nvert) {
+  if (!nel_ || !ndim_ || !xc || !yc || !zc || !vertex || *nel_ <= 0)
+    return fail(NEKGPU_EINVAL, "connect: bad arguments");
+  if (*ndim_ != 3) return fail(NEKGPU_EINVAL, "connect: only ndim = 3 is served");
+  const int64_t nel = *nel_, n = 8 * nel;
+  const double tol = tol_ ? *tol_ : 0.2;
+  if (!(tol > 0.0)) return fail(NEKGPU_EINVAL, "connect: tolerance must be positive");
+  // corners in tensor order; squared shortest edge at each corner (set_d2)
+  std::vector<double> X((size_t)(3 * n)), L2((size_t)n);
+  for (int64_t e = 0; e < nel; ++e)
+    for (int c = 0; c < 8; ++c) {
+      const size_t src = (size_t)(8 * e + kPreOfTensor[c]), dst = (size_t)(8 * e + c);
+      X[3 * dst] = xc[src];
+      X[3 * dst + 1] = yc[src];
+      X[3 * dst + 2] = zc[src];
+    }
+  for (int64_t e = 0; e < nel; ++e)
+    for (int c = 0; c < 8; ++c) {
+      double m = 1e300;
+      const size_t p = (size_t)(8 * e + c);
+      for (int k = 0; k < 3; ++k) {
+        const size_t q = (size_t)(8 * e + kNeighbour[c][k]);
+        double d2 = 0.0;
+        for (int j = 0; j < 3; ++j) d2 += (X[3 * q + j] - X[3 * p + j]) * (X[3 * q + j] - X[3 * p + j]);
+        m = std::min(m, d2);
+      }
+      L2[p] = m;
+    }
+  std::vector<int64_t> cell = unique_vertices(X, L2, n, tol);
+  rank_ids(cell);
+  // repair faces that share three of four corners (at most five rounds)
+  for (int round = 0; round < 5; ++round)
+    if (!repair_faces(cell, nel)) break;
+  rank_ids(cell);
+  // periodic face pairs
+  if (cbc && bc) {
+    Dsu dsu(n + 1);
+    bool any = false;
+    for (int64_t e = 0; e < nel; ++e)
+      for (int tf = 0; tf < 6; ++tf) {
+        const size_t q = (size_t)(6 * e + kPreFace[tf] - 1);
+        if (std::memcmp(cbc + 3 * q, "P  ", 3) != 0) continue;
+        any = true;
+        const int64_t je = (int64_t)std::fabs(bc[5 * q]) - 1;
+        const int jpf = (int)bc[5 * q + 1];
+        if (je < 0 || je >= nel || jpf < 1 || jpf > 6)
+          return fail(NEKGPU_EINVAL, "connect: periodic face names no element face");
+        const int jf = kTensorFace[jpf - 1] - 1;
+        const size_t qj = (size_t)(6 * je + jpf - 1);
+        if (std::memcmp(cbc + 3 * qj, "P  ", 3) != 0 || (int64_t)std::fabs(bc[5 * qj]) - 1 != e ||
+            kTensorFace[(int)bc[5 * qj + 1] - 1] - 1 != tf)
+          return fail(NEKGPU_EINVAL, "connect: periodic faces do not point at each other");
+        // both faces' corners about their means; the cyclic shift (walking the
+        // partner face backwards) that brings them closest
+        double a[4][3], b[4][3], mean_a[3] = {0, 0, 0}, mean_b[3] = {0, 0, 0}, x0m = 0.0;
+        for (int i = 0; i < 4; ++i)
+          for (int k = 0; k < 3; ++k) {
+            a[i][k] = X[(size_t)(3 * (8 * e + kFaceCycle[tf][i]) + k)];
+            b[i][k] = X[(size_t)(3 * (8 * je + kFaceCycle[jf][i]) + k)];
+            mean_a[k] += a[i][k];
+            mean_b[k] += b[i][k];
+            x0m = std::max(x0m, std::max(std::fabs(a[i][k]), std::fabs(b[i][k])));
+          }
+        for (int i = 0; i < 4; ++i)
+          for (int k = 0; k < 3; ++k) {
+            a[i][k] -= mean_a[k] / 4;
+            b[i][k] -= mean_b[k] / 4;
+          }
+        int best = 0;
+        double dmin = 1e300;
+        for (int s = 0; s < 4; ++s) {
+          double d2 = 0.0;
+          for (int i = 0; i < 4; ++i) {
+            const int j = 3 - (i + s) % 4;
+            for (int k = 0; k < 3; ++k) d2 += (a[i][k] - b[j][k]) * (a[i][k] - b[j][k]);
+          }
+          if (d2 < dmin) {
+            dmin = d2;
+            best = s;
+          }
+        }
+        if (std::sqrt(dmin) > 1e-3 * x0m)
+          return fail(NEKGPU_EINVAL, "connect: periodic face pair " + std::to_string(e + 1) + "/" +
+                                         std::to_string(tf + 1) + " does not match its partner");
+        for (int i = 0; i < 4; ++i) {
+          const int j = 3 - (i + best) % 4;
+          dsu.join(cell[(size_t)(8 * e + kFaceCycle[tf][i])], cell[(size_t)(8 * je + kFaceCycle[jf][j])]);
+        }
+      }
+    if (any) {
+      for (auto& v : cell) v = dsu.find(v);
+      rank_ids(cell);
+    }
+  }
+  // no element may meet itself (self_chk)
+  for (int64_t e = 0; e < nel; ++e)
+    for (int i = 0; i < 8; ++i)
+      for (int j = i + 1; j < 8; ++j)
+        if (cell[(size_t)(8 * e + i)] == cell[(size_t)(8 * e + j)])
+          return fail(NEKGPU_EINVAL, "connect: element " + std::to_string(e + 1) +
+                                         " has two corners on one vertex (tighten the tolerance)");
+  int64_t nv = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    vertex[i] = cell[(size_t)i];
+    nv = std::max(nv, cell[(size_t)i]);
+  }
+  if (nvert) *nvert = nv;
+  return NEKGPU_OK;
+}
+
+int nekmesh_setvert3d(const int* nx_, const int* nel_, const int64_t* vertex, int64_t* glo_num,
+                      int64_t* ngv_out) {
+  if (!nx_ || !nel_ || !vertex || !glo_num || *nx_ < 2 || *nel_ <= 0)
+    return fail(NEKGPU_EINVAL, "setvert3d: bad arguments");
+  const int64_t nx = *nx_, nel = *nel_, nxyz = nx * nx * nx, nxx = nx * nx;
+  auto G = [&](int64_t e, int64_t i, int64_t j, int64_t k) -> int64_t& {  // 0-based i, j, k
+    return glo_num[(size_t)(nxyz * e + i + nx * (j + nx * k))];
+  };
+  std::fill(glo_num, glo_num + nxyz * nel, (int64_t)0);
+  int64_t ngv = 0;
+  for (int64_t q = 0; q < 8 * nel; ++q) ngv = std::max(ngv, vertex[q]);
+  for (int64_t e = 0; e < nel; ++e)
+    for (int c = 0; c < 8; ++c)
+      G(e, (c & 1) * (nx - 1), ((c >> 1) & 1) * (nx - 1), (c >> 2) * (nx - 1)) = vertex[8 * e + c];
+  if (nx == 2) {
+    if (ngv_out) *ngv_out = ngv;
+    return NEKGPU_OK;
+  }
+  // ---- edges: ranked by their (smaller, larger) end ids.  Edge slot s of an
+  // element: r-edges s = j + 2k, s-edges 4 + i + 2k, t-edges 8 + i + 2j.
+  struct Key {
+    int64_t a, b, c;
+    int64_t pos;
+  };
+  auto rank_keys = [](std::vector<Key>& t, std::vector<int64_t>& rank) {
+    std::sort(t.begin(), t.end(), [](const Key& x, const Key& y) {
+      if (x.a != y.a) return x.a < y.a;
+      if (x.b != y.b) return x.b < y.b;
+      if (x.c != y.c) return x.c < y.c;
+      return x.pos < y.pos;
+    });
+    int64_t r = 0;
+    for (size_t i = 0; i < t.size(); ++i) {
+      if (i == 0 || t[i].a != t[i - 1].a || t[i].b != t[i - 1].b || t[i].c != t[i - 1].c) ++r;
+      rank[(size_t)t[i].pos] = r;
+    }
+    return r;
+  };
+  std::vector<Key> keys((size_t)(12 * nel));
+  std::vector<int64_t> enm((size_t)(12 * nel));
+  for (int64_t e = 0; e < nel; ++e) {
+    const int64_t* v = vertex + 8 * e;
+    for (int s = 0; s < 12; ++s) {
+      int c0, c1;
+      const int b0 = s & 1, b1 = (s >> 1) & 1;
+      if (s < 4) {  // r-edge (j, k) = (b0, b1)
+        c0 = 2 * b0 + 4 * b1;
+        c1 = c0 + 1;
+      } else if (s < 8) {  // s-edge (i, k)
+        c0 = b0 + 4 * b1;
+        c1 = c0 + 2;
+      } else {  // t-edge (i, j)
+        c0 = b0 + 2 * b1;
+        c1 = c0 + 4;
+      }
+      keys[(size_t)(12 * e + s)] = {std::min(v[c0], v[c1]), std::max(v[c0], v[c1]), 0, 12 * e + s};
+    }
+  }
+  const int64_t nedge = rank_keys(keys, enm);
+  const int64_t ne = nx - 2;
+  for (int64_t e = 0; e < nel; ++e)
+    for (int s = 0; s < 12; ++s) {
+      const int64_t igv = ngv + ne * (enm[(size_t)(12 * e + s)] - 1);
+      const int b0 = s & 1, b1 = (s >> 1) & 1;
+      // the edge's first corner, its step through the element, its last corner
+      int64_t i0 = 0, j0 = 0, k0 = 0, di = 0, dj = 0, dk = 0;
+      if (s < 4) {
+        j0 = b0 * (nx - 1);
+        k0 = b1 * (nx - 1);
+        di = 1;
+      } else if (s < 8) {
+        i0 = b0 * (nx - 1);
+        k0 = b1 * (nx - 1);
+        dj = 1;
+      } else {
+        i0 = b0 * (nx - 1);
+        j0 = b1 * (nx - 1);
+        dk = 1;
+      }
+      const bool forward =
+          G(e, i0, j0, k0) < G(e, i0 + di * (nx - 1), j0 + dj * (nx - 1), k0 + dk * (nx - 1));
+      for (int64_t t = 1; t <= nx - 2; ++t)
+        G(e, i0 + di * t, j0 + dj * t, k0 + dk * t) = forward ? igv + t : igv + 1 + ne - t;
+    }
+  ngv += nedge * ne;
+  // ---- faces: ranked by their three smallest corner ids
+  static const int fc[6][4] = {{0, 2, 4, 6}, {1, 3, 5, 7}, {0, 1, 4, 5},
+                               {2, 3, 6, 7}, {0, 1, 2, 3}, {4, 5, 6, 7}};
+  keys.assign((size_t)(6 * nel), Key{});
+  std::vector<int64_t> fnm((size_t)(6 * nel));
+  for (int64_t e = 0; e < nel; ++e)
+    for (int f = 0; f < 6; ++f) {
+      int64_t c[4];
+      for (int q = 0; q < 4; ++q) c[q] = vertex[8 * e + fc[f][q]];
+      std::sort(c, c + 4);
+      keys[(size_t)(6 * e + f)] = {c[0], c[1], c[2], 6 * e + f};
+    }
+  const int64_t nface = rank_keys(keys, fnm);
+  // A face's points as (i index, j index) over the 1-based linear point
+  // numbering of the element: face f runs i from i0 to i1 by is and j from j0
+  // to j1 by js, point = i + nx (j - 1) (the reference's skpdat, dsset).
+  const int64_t sk[6][6] = {{1, nx * (nx - 1) + 1, nx, 1, nx * (nx - 1) + 1, nx},
+                            {nx, nx * (nx - 1) + nx, nx, 1, nx * (nx - 1) + 1, nx},
+                            {1, nx, 1, 1, nx * (nx - 1) + 1, nx},
+                            {1 + nx * (nx - 1), nx * nx, 1, 1, nx * (nx - 1) + 1, nx},
+                            {1, nx, 1, 1, nx, 1},
+                            {1 + nxx * (nx - 1), nx + nxx * (nx - 1), 1, 1, nx, 1}};
+  const int64_t nif = (nx - 2) * (nx - 2);
+  for (int64_t e = 0; e < nel; ++e) {
+    int64_t* ge = glo_num + nxyz * e - 1;  // 1-based point index
+    for (int f = 0; f < 6; ++f) {
+      int64_t i0 = sk[f][0], i1 = sk[f][1], is = sk[f][2], j0 = sk[f][3], j1 = sk[f][4], js = sk[f][5];
+      const int64_t g[4] = {ge[i0 + nx * (j0 - 1)], ge[i1 + nx * (j0 - 1)], ge[i0 + nx * (j1 - 1)],
+                            ge[i1 + nx * (j1 - 1)]};
+      const int lo = (int)(std::min_element(g, g + 4) - g);
+      // count from the smallest corner towards its smaller neighbour
+      bool ij = false;
+      int idir = 1, jdir = 1;
+      switch (lo) {
+        case 0: ij = g[1] < g[2]; break;
+        case 1: idir = -1; ij = g[0] < g[3]; break;
+        case 2: jdir = -1; ij = g[3] < g[0]; break;
+        default: idir = jdir = -1; ij = g[2] < g[1]; break;
+      }
+      if (idir < 0) {
+        std::swap(i0, i1);
+        is = -is;
+      }
+      if (jdir < 0) {
+        std::swap(j0, j1);
+        js = -js;
+      }
+      const int64_t ig0 = ngv + nif * (fnm[(size_t)(6 * e + f)] - 1);
+      const int64_t ni = (i1 - i0) / is + 1, nj = (j1 - j0) / js + 1;
+      int64_t k = 0, l = 0;
+      for (int64_t outer = 0; outer < (ij ? nj : ni); ++outer)
+        for (int64_t inner = 0; inner < (ij ? ni : nj); ++inner) {
+          const int64_t i = i0 + (ij ? inner : outer) * is, j = j0 + (ij ? outer : inner) * js;
+          ++k;
+          if (k > nx && k < nxx - nx && k % nx != 1 && k % nx != 0) ge[i + nx * (j - 1)] = ++l + ig0;
+        }
+    }
+  }
+  ngv += nface * nif;
+  if (ngv_out) *ngv_out = ngv;
+  return NEKGPU_OK;
+}
+
+int nekmesh_xyzlin(const int* nx_, const int* nel_, const double* zg, const double* xc,
+                   const double* yc, const double* zc, double* x, double* y, double* z) {
+  if (!nx_ || !nel_ || !zg || !xc || !yc || !zc || !x || !y || !z || *nx_ < 2 || *nel_ <= 0)
+    return fail(NEKGPU_EINVAL, "xyzlin: bad arguments");
+  const int nx = *nx_;
+  const int64_t nel = *nel_, nxyz = (int64_t)nx * nx * nx;
+  // linear interpolation weights at the nodes: (1 - z)/2 and (1 + z)/2
+  std::vector<double> h0((size_t)nx), h1((size_t)nx);
+  for (int i = 0; i < nx; ++i) {
+    h0[(size_t)i] = (1.0 - zg[i]) / 2.0;
+    h1[(size_t)i] = (1.0 + zg[i]) / 2.0;
+  }
+  const double* src[3] = {xc, yc, zc};
+  double* dst[3] = {x, y, z};
+  std::vector<double> t1((size_t)nx * 4), t2((size_t)nx * nx * 2);
+  for (int64_t e = 0; e < nel; ++e)
+    for (int d = 0; d < 3; ++d) {
+      double u[8];  // tensor order
+      for (int c = 0; c < 8; ++c) u[c] = src[d][8 * e + kPreOfTensor[c]];
+      // r, then s, then t (each a two-term sum)
+      for (int bc = 0; bc < 4; ++bc)
+        for (int i = 0; i < nx; ++i)
+          t1[(size_t)(i + nx * bc)] = h0[(size_t)i] * u[2 * bc] + h1[(size_t)i] * u[2 * bc + 1];
+      for (int c = 0; c < 2; ++c)
+        for (int j = 0; j < nx; ++j)
+          for (int i = 0; i < nx; ++i)
+            t2[(size_t)(i + nx * (j + nx * c))] =
+                t1[(size_t)(i + nx * (2 * c))] * h0[(size_t)j] + t1[(size_t)(i + nx * (2 * c + 1))] * h1[(size_t)j];
+      double* out = dst[d] + nxyz * e;
+      for (int k = 0; k < nx; ++k)
+        for (int j = 0; j < nx; ++j)
+          for (int i = 0; i < nx; ++i)
+            out[i + nx * (j + nx * k)] = t2[(size_t)(i + nx * j)] * h0[(size_t)k] +
+                                         t2[(size_t)(i + nx * (j + nx))] * h1[(size_t)k];
+    }
+  return NEKGPU_OK;
+}
+
+}  // extern "C"

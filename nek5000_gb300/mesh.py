@@ -86,6 +86,47 @@ def unit_vector(seed: int):
     return v / np.linalg.norm(v)
 
 
+def geometry(x, y, z, D, w):
+    """Geometric factors of elements given their GLL coordinates x, y, z
+    (each (nel, lx1, lx1, lx1), x index fastest): G1..G6 as (6, n), the mass
+    bm1 and the Jacobian (core/coef.f glmapm1 / geodat1)."""
+    nel, nx = x.shape[0], x.shape[-1]
+    zc = z
+    # reference-element derivatives: r along ix (last axis), s along iy, t along iz
+    def dr(f):
+        return np.einsum("il,ekjl->ekji", D, f, optimize=True)
+
+    def ds(f):
+        return np.einsum("jl,ekli->ekji", D, f, optimize=True)
+
+    def dt(f):
+        return np.einsum("kl,elji->ekji", D, f, optimize=True)
+
+    xr, yr, zr = dr(x), dr(y), dr(zc)
+    xs, ys, zs = ds(x), ds(y), ds(zc)
+    xt, yt, zt = dt(x), dt(y), dt(zc)
+    jac = (xr * (ys * zt - yt * zs) - xs * (yr * zt - yt * zr) + xt * (yr * zs - ys * zr))
+    # cofactors (rows of J * grad r, grad s, grad t)
+    rx, ry, rz = ys * zt - yt * zs, xt * zs - xs * zt, xs * yt - xt * ys
+    sx, sy, sz = yt * zr - yr * zt, xr * zt - xt * zr, xt * yr - xr * yt
+    tx, ty, tz = yr * zs - ys * zr, xs * zr - xr * zs, xr * ys - xs * yr
+    del xr, yr, zr, xs, ys, zs, xt, yt, zt
+    w3 = (w[None, None, :] * w[None, :, None] * w[:, None, None])[None]
+    wj = w3 / jac
+    g = np.empty((6, nel, nx, nx, nx))
+    g[0] = (rx * rx + ry * ry + rz * rz) * wj
+    g[1] = (sx * sx + sy * sy + sz * sz) * wj
+    g[2] = (tx * tx + ty * ty + tz * tz) * wj
+    g[3] = (rx * sx + ry * sy + rz * sz) * wj
+    g[4] = (rx * tx + ry * ty + rz * tz) * wj
+    g[5] = (sx * tx + sy * ty + sz * tz) * wj
+    del rx, ry, rz, sx, sy, sz, tx, ty, tz
+    bm1 = (jac * w3).reshape(-1)
+    if np.any(jac <= 0):
+        raise ValueError("non-positive Jacobian: the element map is tangled")
+    return g.reshape(6, -1), bm1, jac.reshape(-1)
+
+
 def box_mesh(N: int, kx: int, ky: int, kz: int, periodic=(False, False, False),
              dirichlet=None, amp: float = 0.05, v=None, seed: int = 0):
     """Build the operator data for a deformed box.
@@ -120,38 +161,7 @@ def box_mesh(N: int, kx: int, ky: int, kz: int, periodic=(False, False, False),
     y = Y + s * v[1]
     zc = Z + s * v[2]
     del X, Y, Z, s
-    # reference-element derivatives: r along ix (last axis), s along iy, t along iz
-    def dr(f):
-        return np.einsum("il,ekjl->ekji", D, f, optimize=True)
-
-    def ds(f):
-        return np.einsum("jl,ekli->ekji", D, f, optimize=True)
-
-    def dt(f):
-        return np.einsum("kl,elji->ekji", D, f, optimize=True)
-
-    xr, yr, zr = dr(x), dr(y), dr(zc)
-    xs, ys, zs = ds(x), ds(y), ds(zc)
-    xt, yt, zt = dt(x), dt(y), dt(zc)
-    jac = (xr * (ys * zt - yt * zs) - xs * (yr * zt - yt * zr) + xt * (yr * zs - ys * zr))
-    # cofactors (rows of J * grad r, grad s, grad t)
-    rx, ry, rz = ys * zt - yt * zs, xt * zs - xs * zt, xs * yt - xt * ys
-    sx, sy, sz = yt * zr - yr * zt, xr * zt - xt * zr, xt * yr - xr * yt
-    tx, ty, tz = yr * zs - ys * zr, xs * zr - xr * zs, xr * ys - xs * yr
-    del xr, yr, zr, xs, ys, zs, xt, yt, zt
-    w3 = (w[None, None, :] * w[None, :, None] * w[:, None, None])[None]
-    wj = w3 / jac
-    g = np.empty((6, nel, nx, nx, nx))
-    g[0] = (rx * rx + ry * ry + rz * rz) * wj
-    g[1] = (sx * sx + sy * sy + sz * sz) * wj
-    g[2] = (tx * tx + ty * ty + tz * tz) * wj
-    g[3] = (rx * sx + ry * sy + rz * sz) * wj
-    g[4] = (rx * tx + ry * ty + rz * tz) * wj
-    g[5] = (sx * tx + sy * ty + sz * tz) * wj
-    del rx, ry, rz, sx, sy, sz, tx, ty, tz
-    bm1 = (jac * w3).reshape(-1)
-    if np.any(jac <= 0):
-        raise ValueError("deformation tangles the mesh (non-positive Jacobian)")
+    g, bm1, jac = geometry(x, y, zc, D, w)
     # global lattice ids
     ngx = kx * N + 1
     ngy = ky * N + (0 if periodic[1] else 1)

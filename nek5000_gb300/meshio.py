@@ -1,0 +1,203 @@
+"""Mesh ingestion: the reference's .re2 / .co2 files to the arrays the solve
+path takes (python side of include/nekmesh.h; the work is done by the
+library's host code).
+
+    M = load_mesh("case.re2", N=7)             # connectivity from coordinates
+    M = load_mesh("case.re2", N=7, co2="case.co2")
+    h = NekGpu(0); h.setup(M["lx1"], M["nel"], M["D"], M["g"], M["bm1"], M["glo_num"])
+
+load_mesh returns the same keys as mesh.box_mesh (lx1, nel, n, D, g, bm1,
+glo_num, mask, mult, binv, vol, x, y, z, zgll, wgll) plus the file's
+boundary conditions.  Elements are straight-sided (the trilinear map of their
+corners, core/genxyz.f xyzlin); a mesh with curved sides is refused.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _capi
+from .mesh import deriv_matrix, geometry, gll
+
+DIRICHLET_VELOCITY = ("W  ", "V  ", "v  ")  # wall and prescribed velocity
+
+
+def _lib():
+    return _capi.load()
+
+
+def _check(rc):
+    if rc != 0:
+        buf = C.create_string_buffer(512)
+        _lib().nekmesh_last_error(buf, C.byref(C.c_int(512)))
+        raise _capi.NekGpuError(rc, buf.value.decode(errors="replace"))
+
+
+def _p(a):
+    return C.c_void_p(a.ctypes.data) if a is not None else None
+
+
+def read_re2(path: str) -> dict:
+    """Everything a .re2 file holds (core/reader_re2.f): header fields, element
+    groups, corners (nel, 2^ndim) in file order, curved sides and every
+    boundary-condition section as the reference's dense (cbc, bc) arrays."""
+    L = _lib()
+    h = C.c_int64(0)
+    _check(L.nekmesh_re2_open(str(path).encode(), C.byref(h)))
+    try:
+        nelgt, ndim, nelgv, wd, nbf = (C.c_int() for _ in range(5))
+        ncurve = C.c_int64()
+        _check(L.nekmesh_re2_header(C.byref(h), C.byref(nelgt), C.byref(ndim), C.byref(nelgv),
+                                    C.byref(wd), C.byref(ncurve), C.byref(nbf)))
+        ne, nd, nv = nelgt.value, ndim.value, 1 << ndim.value
+        xc, yc = np.zeros((ne, nv)), np.zeros((ne, nv))
+        zc = np.zeros((ne, nv)) if nd == 3 else None
+        group = np.zeros(ne, dtype=np.int32)
+        _check(L.nekmesh_re2_xyz(C.byref(h), _p(xc), _p(yc), _p(zc), _p(group)))
+        nc = ncurve.value
+        elem, side = np.zeros(nc, dtype=np.int32), np.zeros(nc, dtype=np.int32)
+        curve, ctype = np.zeros((nc, 5)), C.create_string_buffer(max(nc, 1))
+        _check(L.nekmesh_re2_curves(C.byref(h), _p(elem), _p(side), _p(curve), ctype))
+        bcs = []
+        nf = 2 * nd
+        for f in range(nbf.value):
+            cbc = C.create_string_buffer(3 * nf * ne)
+            bc = np.zeros((ne, nf, 5))
+            _check(L.nekmesh_re2_bc(C.byref(h), C.byref(C.c_int(f)), cbc, _p(bc)))
+            raw = cbc.raw.decode("latin-1")
+            types = np.array([raw[3 * q:3 * q + 3] for q in range(nf * ne)]).reshape(ne, nf)
+            bcs.append((types, bc))
+        return dict(nelgt=ne, ndim=nd, nelgv=nelgv.value, wdsize=wd.value, group=group, xc=xc,
+                    yc=yc, zc=zc,
+                    curves=dict(elem=elem, side=side, curve=curve,
+                                ccurve=ctype.raw[:nc].decode("latin-1")),
+                    bcs=bcs)
+    finally:
+        L.nekmesh_re2_close(C.byref(h))
+
+
+def read_co2(path: str) -> dict:
+    """A .co2 connectivity file (core/map2.f read_con): vertex ids (nel, nv)
+    in tensor corner order, placed by element id."""
+    L = _lib()
+    ne, nev, nv = C.c_int(), C.c_int(), C.c_int()
+    _check(L.nekmesh_co2_read(str(path).encode(), C.byref(ne), C.byref(nev), C.byref(nv), None))
+    vertex = np.zeros((ne.value, nv.value), dtype=np.int64)
+    _check(L.nekmesh_co2_read(str(path).encode(), C.byref(ne), C.byref(nev), C.byref(nv),
+                              _p(vertex)))
+    return dict(nelgt=ne.value, nelgv=nev.value, nv=nv.value, vertex=vertex)
+
+
+def write_co2(path: str, vertex, nelgv: int | None = None) -> None:
+    vertex = np.ascontiguousarray(vertex, dtype=np.int64)
+    ne, nv = vertex.shape
+    _check(_lib().nekmesh_co2_write(str(path).encode(), C.byref(C.c_int(ne)),
+                                    C.byref(C.c_int(nelgv or ne)), C.byref(C.c_int(nv)),
+                                    _p(vertex)))
+
+
+def connect(xc, yc, zc, cbc=None, bc=None, tol: float = 0.2):
+    """Vertex ids (nel, 8), tensor corner order, from the corners (file
+    order) and the periodic faces of the first boundary section (the
+    reference's gencon algorithm).  Returns (vertex, number of vertices)."""
+    xc, yc, zc = (np.ascontiguousarray(a, dtype=np.float64) for a in (xc, yc, zc))
+    ne = xc.shape[0]
+    vertex = np.zeros((ne, 8), dtype=np.int64)
+    nvert = C.c_int64()
+    cbuf = None
+    if cbc is not None:
+        cbuf = C.create_string_buffer("".join(np.asarray(cbc).reshape(-1)).encode("latin-1"))
+        bc = np.ascontiguousarray(bc, dtype=np.float64)
+    _check(_lib().nekmesh_connect(C.byref(C.c_int(ne)), C.byref(C.c_int(3)), _p(xc), _p(yc),
+                                  _p(zc), cbuf, _p(bc) if cbc is not None else None,
+                                  C.byref(C.c_double(tol)), _p(vertex), C.byref(nvert)))
+    return vertex, nvert.value
+
+
+def setvert3d(nx: int, vertex):
+    """glo_num of every GLL point (core/navier8.f setvert3d); returns
+    (glo_num, number of ids)."""
+    vertex = np.ascontiguousarray(vertex, dtype=np.int64)
+    ne = vertex.shape[0]
+    glo = np.zeros(ne * nx ** 3, dtype=np.int64)
+    ngv = C.c_int64()
+    _check(_lib().nekmesh_setvert3d(C.byref(C.c_int(nx)), C.byref(C.c_int(ne)), _p(vertex),
+                                    _p(glo), C.byref(ngv)))
+    return glo, ngv.value
+
+
+def xyzlin(nx: int, zgll, xc, yc, zc):
+    """GLL coordinates (nel*nx^3 each) of straight-sided elements."""
+    xc, yc, zc = (np.ascontiguousarray(a, dtype=np.float64) for a in (xc, yc, zc))
+    zgll = np.ascontiguousarray(zgll, dtype=np.float64)
+    ne = xc.shape[0]
+    out = [np.zeros(ne * nx ** 3) for _ in range(3)]
+    _check(_lib().nekmesh_xyzlin(C.byref(C.c_int(nx)), C.byref(C.c_int(ne)), _p(zgll), _p(xc),
+                                 _p(yc), _p(zc), *(_p(o) for o in out)))
+    return out
+
+
+# Points of each preprocessor face (1-based face number) of an element, as
+# (ix, iy, iz) selections on the (iz, iy, ix) element array.
+def _face_points(face: int, nx: int):
+    s = slice(None)
+    return {1: (s, 0, s), 2: (s, s, nx - 1), 3: (s, nx - 1, s), 4: (s, s, 0),
+            5: (0, s, s), 6: (nx - 1, s, s)}[face]
+
+
+def _dsop(glo, u, op):
+    """Host direct-stiffness sum ('+') or product ('*') over shared points."""
+    out = u.copy()
+    shared = glo > 0
+    ids = glo[shared]
+    uniq, inv = np.unique(ids, return_inverse=True)
+    if op == "+":
+        acc = np.bincount(inv, weights=u[shared], minlength=len(uniq))
+    else:
+        acc = np.ones(len(uniq))
+        np.multiply.at(acc, inv, u[shared])
+    out[shared] = acc[inv]
+    return out
+
+
+def load_mesh(re2: str, N: int, co2: str | None = None, field: int = 0,
+              dirichlet=DIRICHLET_VELOCITY, tol: float = 0.2) -> dict:
+    """The operator data of a .re2 mesh at polynomial order N (lx1 = N+1):
+    GLL coordinates (xyzlin), geometric factors and mass, global numbering
+    (the .co2 file when given, else connectivity from the corners), the mask
+    of boundary-condition section `field` (zero on faces whose type is in
+    `dirichlet`, then multiplied across shared points as dsop '*'),
+    multiplicity and inverse mass."""
+    R = read_re2(re2)
+    if R["ndim"] != 3:
+        raise ValueError("only 3-D meshes are served")
+    if len(R["curves"]["elem"]):
+        raise ValueError("curved sides are not served (straight-sided elements only)")
+    nx = N + 1
+    ne = R["nelgt"]
+    zg, wg = gll(nx)
+    D = deriv_matrix(zg)
+    x, y, z = xyzlin(nx, zg, R["xc"], R["yc"], R["zc"])
+    shape = (ne, nx, nx, nx)
+    g, bm1, jac = geometry(x.reshape(shape), y.reshape(shape), z.reshape(shape), D, wg)
+    cbc, bc = R["bcs"][field] if R["bcs"] else (None, None)
+    if co2 is not None:
+        C2 = read_co2(co2)
+        if C2["nelgt"] != ne or C2["nv"] != 8:
+            raise ValueError("the .co2 file does not match the mesh")
+        vertex = C2["vertex"]
+    else:
+        vertex, _ = connect(R["xc"], R["yc"], R["zc"], cbc, bc, tol)
+    glo, ngv = setvert3d(nx, vertex)
+    n = ne * nx ** 3
+    mask = np.ones(shape)
+    if cbc is not None:
+        for e, f in zip(*np.nonzero(np.isin(cbc, list(dirichlet)))):
+            mask[(e,) + _face_points(int(f) + 1, nx)] = 0.0
+    mask = _dsop(glo, mask.reshape(-1), "*")
+    mult = 1.0 / _dsop(glo, np.ones(n), "+")
+    binv = 1.0 / _dsop(glo, bm1, "+")
+    return dict(lx1=nx, nel=ne, n=n, D=D, zgll=zg, wgll=wg, g=g, bm1=bm1, jac=jac,
+                glo_num=glo, ngv=ngv, vertex=vertex, mask=mask, mult=mult, binv=binv,
+                vol=float(bm1.sum()), x=x, y=y, z=z, cbc=cbc, bc=bc, group=R["group"])

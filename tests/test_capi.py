@@ -10,9 +10,13 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def declared_symbols():
-    src = open(os.path.join(ROOT, "include", "nekgpu.h")).read()
-    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    return sorted(set(re.findall(r"\bint\s+(nekgpu_\w+)\s*\(", src)))
+    syms = set()
+    for h in sorted(os.listdir(os.path.join(ROOT, "include"))):
+        if h.endswith(".h"):
+            src = open(os.path.join(ROOT, "include", h)).read()
+            src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+            syms |= set(re.findall(r"\bint\s+(nek(?:gpu|mesh)_\w+)\s*\(", src))
+    return sorted(syms)
 
 
 @pytest.fixture(scope="module")
@@ -25,7 +29,8 @@ def lib():
 def test_header_declares_the_reference_boundary():
     syms = declared_symbols()
     for must in ("nekgpu_axhelm", "nekgpu_dssum", "nekgpu_setprec", "nekgpu_cggo", "nekgpu_hmholtz",
-                 "nekgpu_setup", "nekgpu_init", "nekgpu_finalize"):
+                 "nekgpu_setup", "nekgpu_init", "nekgpu_finalize", "nekmesh_re2_open",
+                 "nekmesh_co2_read", "nekmesh_connect", "nekmesh_setvert3d"):
         assert must in syms
 
 

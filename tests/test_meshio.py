@@ -1,0 +1,209 @@
+"""Mesh ingestion (include/nekmesh.h): .re2 / .co2 readers, connectivity from
+element corners, set_vert numbering and the trilinear GLL coordinates, on
+the host (no GPU).
+
+The .re2 layout is pinned on the reference's own genbox output
+(short_tests/lpm_one/uniform.re2, written from uniform.box: a 5x5x5 box on
+the unit cube with walls on every side) when the reference tree is present;
+tests/golden/re2_reference.json holds what was read from it.  set_vert is
+compared with the oracle's restatement bit for bit."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from re2_util import box_elements, rotate_elements, same_partition, write_re2
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLDEN = os.path.join(ROOT, "tests", "golden", "re2_reference.json")
+REF_RE2 = "/root/reference/short_tests/lpm_one/uniform.re2"
+
+
+@pytest.fixture(scope="module")
+def mio():
+    from nek5000_gb300 import build
+    build.build()
+    from nek5000_gb300 import meshio
+    return meshio
+
+
+@pytest.mark.parametrize("version,big", [("#v002", False), ("#v002", True), ("#v001", False)])
+def test_re2_round_trip(mio, tmp_path, version, big):
+    xc, yc, zc, _, bcs = box_elements(3, 2, 2, jitter=0.2, seed=3)
+    curves = [(2, 5, (0.1, 0.2, 0.3, 0.4, 0.5), "m"), (7, 11, (1.0, 0, 0, 0, 0), "C")]
+    thermal = [(1, 4, (3.5, 0, 0, 0, 0), "t  ")]
+    p = tmp_path / "box.re2"
+    write_re2(p, xc, yc, zc, bcs, version=version, big_endian=big, curves=curves,
+              groups=np.arange(12) % 3, extra_bc_sections=(thermal,))
+    R = mio.read_re2(p)
+    assert (R["nelgt"], R["ndim"], R["nelgv"]) == (12, 3, 12)
+    assert R["wdsize"] == (4 if version == "#v001" else 8)
+    rtol = 1e-7 if version == "#v001" else 0.0
+    for a, b in ((R["xc"], xc), (R["yc"], yc), (R["zc"], zc)):
+        np.testing.assert_allclose(a, b, rtol=rtol, atol=rtol)
+    assert list(R["group"]) == list(np.arange(12) % 3)
+    assert list(R["curves"]["elem"]) == [2, 7] and list(R["curves"]["side"]) == [5, 11]
+    assert R["curves"]["ccurve"] == "mC"
+    np.testing.assert_allclose(R["curves"]["curve"][0], [0.1, 0.2, 0.3, 0.4, 0.5], rtol=rtol)
+    assert len(R["bcs"]) == 2
+    cbc, bc = R["bcs"][0]
+    for (el, f, vals, t) in bcs:
+        assert cbc[el - 1, f - 1] == t
+    assert (cbc == "W  ").sum() == len(bcs) and (cbc == "E  ").sum() == 12 * 6 - len(bcs)
+    cbc2, bc2 = R["bcs"][1]
+    assert cbc2[0, 3] == "t  " and bc2[0, 3, 0] == pytest.approx(3.5)
+
+
+def test_re2_errors(mio, tmp_path):
+    from nek5000_gb300 import _capi
+    with pytest.raises(_capi.NekGpuError) as ei:
+        mio.read_re2(tmp_path / "missing.re2")
+    assert ei.value.code == _capi.EIO
+    xc, yc, zc, _, bcs = box_elements(2, 2, 2)
+    p = tmp_path / "t.re2"
+    write_re2(p, xc, yc, zc, bcs)
+    data = open(p, "rb").read()
+    for bad in (data[:500], b"#x002" + data[5:], data[:80] + b"\0\0\0\0" + data[84:]):
+        open(p, "wb").write(bad)
+        with pytest.raises(_capi.NekGpuError) as ei:
+            mio.read_re2(p)
+        assert ei.value.code == _capi.EIO
+
+
+def test_reference_genbox_file(mio):
+    """The reference's uniform.re2 holds the box uniform.box describes: 5^3
+    elements of 0.2, x fastest, corners in preprocessor order, W on every
+    outside face (150 records) and E inside."""
+    ref = json.load(open(GOLDEN))["uniform.re2"]
+    if not os.path.exists(REF_RE2):
+        pytest.skip("reference tree not present (golden digest checked by its generator)")
+    R = mio.read_re2(REF_RE2)
+    assert (R["nelgt"], R["ndim"], R["nelgv"], R["wdsize"]) == tuple(ref["header"])
+    xc, yc, zc, _, bcs = box_elements(5, 5, 5)
+    np.testing.assert_allclose(R["xc"], xc, atol=1e-15)
+    np.testing.assert_allclose(R["yc"], yc, atol=1e-15)
+    np.testing.assert_allclose(R["zc"], zc, atol=1e-15)
+    cbc, bc = R["bcs"][0]
+    assert (cbc == "W  ").sum() == ref["n_wall_faces"] == len(bcs)
+    for (el, f, vals, t) in bcs:
+        assert cbc[el - 1, f - 1] == "W  "
+    assert float(np.sum(R["xc"] + 2 * R["yc"] + 3 * R["zc"])) == pytest.approx(ref["corner_sum"])
+
+
+@pytest.mark.parametrize("periodic_y", [False, True])
+def test_connectivity_matches_the_lattice(mio, periodic_y):
+    perm = np.random.default_rng(5).permutation(4 * 3 * 3)
+    xc, yc, zc, lattice, bcs = box_elements(4, 3, 3, periodic_y=periodic_y, jitter=0.25, seed=5,
+                                            perm=perm)
+    nel = xc.shape[0]
+    cbc = np.full((nel, 6), "E  ")
+    bc = np.zeros((nel, 6, 5))
+    for (el, f, vals, t) in bcs:
+        cbc[el - 1, f - 1] = t
+        bc[el - 1, f - 1] = vals
+    vertex, nv = mio.connect(xc, yc, zc, cbc, bc)
+    assert same_partition(vertex, lattice)
+    assert nv == len(np.unique(lattice))
+    assert vertex.min() == 1 and vertex.max() == nv
+
+
+def test_connectivity_errors(mio):
+    from nek5000_gb300 import _capi
+    xc, yc, zc, _, bcs = box_elements(2, 2, 2, periodic_y=True)
+    nel = 8
+    cbc = np.full((nel, 6), "E  ")
+    bc = np.zeros((nel, 6, 5))
+    for (el, f, vals, t) in bcs:
+        cbc[el - 1, f - 1] = t
+        bc[el - 1, f - 1] = vals
+    with pytest.raises(_capi.NekGpuError):  # a tolerance that merges whole elements
+        mio.connect(xc, yc, zc, cbc, bc, tol=3.0)
+    bad = bc.copy()
+    q = np.argwhere(cbc == "P  ")[0]
+    bad[q[0], q[1], 0] = (q[0] + 1) % nel + 1  # partner that does not point back
+    with pytest.raises(_capi.NekGpuError):
+        mio.connect(xc, yc, zc, cbc, bad)
+
+
+@pytest.mark.parametrize("nx", [2, 3, 5, 8])
+def test_setvert3d_matches_the_oracle(mio, oracle, nx):
+    xc, yc, zc, lattice, _ = box_elements(3, 2, 2, periodic_y=True, seed=1,
+                                          perm=np.random.default_rng(1).permutation(12))
+    # relabel the vertices at random: the numbering must follow them
+    relabel = np.random.default_rng(2).permutation(lattice.max()) + 1
+    vertex = relabel[lattice - 1]
+    glo, ngv = mio.setvert3d(nx, vertex)
+    glo_ref, ngv_ref = oracle.setvert3d(nx, 12, vertex.reshape(-1))
+    assert ngv == ngv_ref
+    assert np.array_equal(glo, glo_ref)
+
+
+def test_xyzlin_is_the_trilinear_map(mio):
+    from nek5000_gb300.mesh import gll
+    xc, yc, zc, _, _ = box_elements(2, 2, 1, jitter=0.3, seed=4)
+    nx = 6
+    zg, _ = gll(nx)
+    x, y, z = mio.xyzlin(nx, zg, xc, yc, zc)
+    h = np.stack([(1 - zg) / 2, (1 + zg) / 2])  # (2, nx)
+    pre = [0, 1, 3, 2, 4, 5, 7, 6]  # tensor corner -> preprocessor corner
+    for arr, c in ((x, xc), (y, yc), (z, zc)):
+        u = c[:, pre].reshape(-1, 2, 2, 2)  # (e, k, j, i)
+        want = np.einsum("ekji,kz,jy,ix->ezyx", u, h, h, h).reshape(-1)
+        np.testing.assert_allclose(arr, want, rtol=0, atol=1e-15)
+
+
+def test_co2_round_trip_and_load_mesh(mio, tmp_path):
+    from nek5000_gb300 import mesh
+    xc, yc, zc, lattice, bcs = box_elements(3, 3, 2)
+    p = tmp_path / "box.re2"
+    write_re2(p, xc, yc, zc, bcs)
+    M = mio.load_mesh(p, N=5)
+    c2 = tmp_path / "box.co2"
+    mio.write_co2(c2, M["vertex"])
+    C2 = mio.read_co2(c2)
+    assert np.array_equal(C2["vertex"], M["vertex"]) and C2["nv"] == 8
+    M2 = mio.load_mesh(p, N=5, co2=c2)
+    assert np.array_equal(M2["glo_num"], M["glo_num"])
+    # the same box from the box mesher (undeformed, walls everywhere)
+    B = mesh.box_mesh(5, 3, 3, 2, amp=0.0)
+    np.testing.assert_allclose(M["g"], B["g"], rtol=1e-12, atol=1e-13)
+    np.testing.assert_allclose(M["bm1"], B["bm1"], rtol=1e-13)
+    assert same_partition(M["glo_num"] + (M["glo_num"] == 0) * (10 ** 9 + np.arange(M["n"])),
+                          B["glo_num"] + (B["glo_num"] == 0) * (10 ** 9 + np.arange(B["n"])))
+    np.testing.assert_array_equal(M["mask"], B["mask"])
+    np.testing.assert_allclose(M["mult"], B["mult"], rtol=1e-15)
+    np.testing.assert_allclose(M["binv"], B["binv"], rtol=1e-13)
+
+
+def test_rotated_elements_give_a_continuous_numbering(mio, tmp_path):
+    """Elements whose corner lists start at different corners (mixed local
+    frames): the numbering must still join exactly the coincident points, so
+    the average over copies of a smooth field is the field itself and every
+    point's copy count is its geometric multiplicity."""
+    xc, yc, zc, _, _ = box_elements(3, 3, 3, jitter=0.2, seed=9,
+                                    perm=np.random.default_rng(9).permutation(27))
+    xc, yc, zc = rotate_elements(xc, yc, zc, seed=9)
+    p = tmp_path / "rot.re2"
+    write_re2(p, xc, yc, zc, [])
+    M = mio.load_mesh(p, N=4)
+    assert np.all(M["jac"] > 0)
+    f = np.sin(2 * M["x"]) * np.cos(3 * M["y"]) + M["z"] ** 2
+    avg = mio._dsop(M["glo_num"], f, "+") * M["mult"]
+    np.testing.assert_allclose(avg, f, rtol=0, atol=1e-13)
+    # copy counts: 8 at interior lattice vertices, 4 on interior edges, 2 on faces
+    cnt = np.rint(1 / M["mult"]).astype(int)
+    key = np.round(np.stack([M["x"], M["y"], M["z"]], 1), 9)
+    _, inv, counts = np.unique(key, axis=0, return_inverse=True, return_counts=True)
+    assert np.array_equal(cnt, counts[inv.reshape(-1)])
+
+
+def test_face_repair_joins_a_displaced_corner(mio):
+    """One element's copy of an interior vertex moved by 0.3 h (beyond the
+    0.2 tolerance): its faces share three of four corners with their
+    neighbours, and the repair step (gencon face_chk) joins the fourth."""
+    xc, yc, zc, lattice, _ = box_elements(3, 3, 3)
+    e = 0  # element (0,0,0): its preprocessor corner 7 (index 6) is lattice vertex (1,1,1)
+    xc[e, 6] += 0.3 / 3
+    vertex, nv = mio.connect(xc, yc, zc)
+    assert same_partition(vertex, lattice) and nv == lattice.max()
