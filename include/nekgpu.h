@@ -90,6 +90,27 @@ int nekgpu_setup(const int64_t *handle, const int *lx1, const int *nel, const do
                  const double *g1, const double *g2, const double *g3, const double *g4,
                  const double *g5, const double *g6, const double *bm1, const int64_t *glo_num);
 
+/* As nekgpu_setup, with the geometric factors and the mass computed on the
+ * device from the GLL coordinates xm1, ym1, zm1 (host arrays, lx1^3 nel
+ * each) and the GLL weights wxm1 (lx1): xyzrst (core/coef.f:879-926), glmapm1
+ * (:555-631) and geodat1 (:633-784), with W3M1 = w(i) w(j) w(k); products,
+ * sums and 1/J rounded one by one in the reference's order, so G1..G6 and
+ * bm1 are the reference's bit for bit.  NEKGPU_EINVAL when a Jacobian is not
+ * positive. */
+int nekgpu_setup_xyz(const int64_t *handle, const int *lx1, const int *nel, const double *dxm1,
+                     const double *wxm1, const double *xm1, const double *ym1, const double *zm1,
+                     const int64_t *glo_num);
+/* A moved mesh (same numbering): G1..G6, bm1 and volvm1 recomputed from new
+ * device coordinates, as the reference's geom_reset does each step of a
+ * moving-boundary run (geom_reset, core/ic.f:1824, -> geom1, core/coef.f:360).
+ * On NEKGPU_EINVAL (a Jacobian not positive) the refused geometry is left in
+ * place: pass valid coordinates before the next solve. */
+int nekgpu_geom_update_dev(const int64_t *handle, const double *wxm1, const double *xm1,
+                           const double *ym1, const double *zm1);
+/* The geometry in use, copied to host arrays (lx1^3 nel each; any may be
+ * null). */
+int nekgpu_geometry(const int64_t *handle, double *g1, double *g2, double *g3, double *g4,
+                    double *g5, double *g6, double *bm1);
 /* Number of shared groups and of local copies in them (gs_setup's maps);
  * with non-null outputs, copies the CSR maps: seg_start[nseg+1], idx[nidx]
  * (0-based local indices, ascending inside a group, groups by ascending id). */

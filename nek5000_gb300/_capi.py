@@ -56,6 +56,9 @@ SIGNATURES = {
     "nekgpu_last_error": [_I64P, C.c_char_p, _IP],
     "nekgpu_set_option": [_I64P, _IP, _IP],
     "nekgpu_setup": [_I64P, _IP, _IP, _P, _P, _P, _P, _P, _P, _P, _P, _P],
+    "nekgpu_setup_xyz": [_I64P, _IP, _IP, _P, _P, _P, _P, _P, _P],
+    "nekgpu_geom_update_dev": [_I64P, _P, _P, _P, _P],
+    "nekgpu_geometry": [_I64P, _P, _P, _P, _P, _P, _P, _P],
     "nekgpu_gs_maps": [_I64P, _I64P, _I64P, _P, _P],
     "nekgpu_axhelm": [_I64P, _P, _P, _P, _P, _IP, _IP],
     "nekgpu_axhelm_dev": [_I64P, _P, _P, _P, _P, _IP, _IP],

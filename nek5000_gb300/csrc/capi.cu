@@ -238,8 +238,8 @@ void handle_close(Handle& H) {
   H.stream = nullptr;
 }
 
-int handle_setup(Handle& H, int lx1, int nel, const double* dxm1, const double* const* g6,
-                 const double* bm1, const int64_t* glo_num, std::string& err) {
+// Mesh sizes, D, and the device arrays of the geometry (old mesh dropped).
+static int mesh_prepare(Handle& H, int lx1, int nel, const double* dxm1, std::string& err) {
   if (lx1 < 2 || lx1 > NEKGPU_MAX_LX1) {
     err = "lx1 out of range [2, " + std::to_string(NEKGPU_MAX_LX1) + "]";
     return NEKGPU_EINVAL;
@@ -264,7 +264,6 @@ int handle_setup(Handle& H, int lx1, int nel, const double* dxm1, const double* 
   const int P = m.nx1 * m.nx1 * m.nx1;
   m.n = (int64_t)P * m.nel;
   const int64_t n = m.n;
-  cudaError_t e;
   if (cudaMalloc(&m.f64.G, 6 * n * sizeof(double)) != cudaSuccess ||
       cudaMalloc(&m.f64.bm1, n * sizeof(double)) != cudaSuccess ||
       cudaMalloc(&m.f64.D, m.nx1 * m.nx1 * sizeof(double)) != cudaSuccess) {
@@ -277,6 +276,38 @@ int handle_setup(Handle& H, int lx1, int nel, const double* dxm1, const double* 
   for (int i = 0; i < m.nx1; ++i)
     for (int j = 0; j < m.nx1; ++j) m.h_D[i * m.nx1 + j] = dxm1[i + j * m.nx1];
   cudaMemcpy(m.f64.D, m.h_D.data(), m.h_D.size() * sizeof(double), cudaMemcpyHostToDevice);
+  return 0;
+}
+
+// Numbering-side setup once the geometry is in place.
+static int mesh_finish(Handle& H, const int64_t* glo_num, std::string& err) {
+  Mesh& m = H.mesh;
+  const int64_t n = m.n;
+  cudaError_t e;
+  if (!m.dev_err && cudaMalloc(&m.dev_err, sizeof(int)) != cudaSuccess) {
+    err = "flag allocation failed";
+    return NEKGPU_ENOMEM;
+  }
+  cudaMemset(m.dev_err, 0, sizeof(int));
+  const int rc = gs_setup(m.gs, glo_num, n, m.nx1, err);
+  if (rc) return rc == -4 ? NEKGPU_ENOMEM : NEKGPU_EINVAL;
+  e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    err = std::string("setup: ") + cudaGetErrorString(e);
+    return NEKGPU_ECUDA;
+  }
+  H.has_mesh = true;
+  return 0;
+}
+
+int handle_setup(Handle& H, int lx1, int nel, const double* dxm1, const double* const* g6,
+                 const double* bm1, const int64_t* glo_num, std::string& err) {
+  int rc0 = mesh_prepare(H, lx1, nel, dxm1, err);
+  if (rc0) return rc0;
+  Mesh& m = H.mesh;
+  const int64_t n = m.n;
+  const int P = m.nx1 * m.nx1 * m.nx1;
+  cudaError_t e;
   DevBuf<double> stage;
   if (stage.ensure(n)) {
     err = "staging allocation failed";
@@ -303,20 +334,36 @@ int handle_setup(Handle& H, int lx1, int nel, const double* dxm1, const double* 
   double vol = 0.0;
   for (int64_t i = 0; i < n; ++i) vol = vol + bm1[i];
   m.vol = vol;
-  if (!m.dev_err && cudaMalloc(&m.dev_err, sizeof(int)) != cudaSuccess) {
-    err = "flag allocation failed";
+  return mesh_finish(H, glo_num, err);
+}
+
+int geom_from_xyz(Handle& H, const double* x, const double* y, const double* z, const double* w,
+                  std::string& err);
+
+// As handle_setup, with G and bm1 computed on the device from the GLL
+// coordinates (host arrays) and weights.
+int handle_setup_xyz(Handle& H, int lx1, int nel, const double* dxm1, const double* wxm1,
+                     const double* xm1, const double* ym1, const double* zm1,
+                     const int64_t* glo_num, std::string& err) {
+  int rc0 = mesh_prepare(H, lx1, nel, dxm1, err);
+  if (rc0) return rc0;
+  const int64_t n = H.mesh.n;
+  if (H.io0.ensure(n) || H.io1.ensure(n) || H.io2.ensure(n)) {
+    err = "staging allocation failed";
     return NEKGPU_ENOMEM;
   }
-  cudaMemset(m.dev_err, 0, sizeof(int));
-  const int rc = gs_setup(m.gs, glo_num, n, m.nx1, err);
-  if (rc) return rc == -4 ? NEKGPU_ENOMEM : NEKGPU_EINVAL;
-  e = cudaGetLastError();
-  if (e != cudaSuccess) {
-    err = std::string("setup: ") + cudaGetErrorString(e);
-    return NEKGPU_ECUDA;
+  const double* src[3] = {xm1, ym1, zm1};
+  double* dst[3] = {H.io0.ptr, H.io1.ptr, H.io2.ptr};
+  for (int q = 0; q < 3; ++q) {
+    cudaError_t e = cudaMemcpy(dst[q], src[q], n * sizeof(double), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      err = std::string("coordinate upload: ") + cudaGetErrorString(e);
+      return NEKGPU_ECUDA;
+    }
   }
-  H.has_mesh = true;
-  return 0;
+  rc0 = geom_from_xyz(H, H.io0.ptr, H.io1.ptr, H.io2.ptr, wxm1, err);
+  if (rc0) return rc0;
+  return mesh_finish(H, glo_num, err);
 }
 
 Handle* handle_lookup(const int64_t* h) { return get(h); }
@@ -403,6 +450,49 @@ int nekgpu_setup(const int64_t* handle, const int* lx1, const int* nel, const do
   std::string err;
   const int rc = handle_setup(*H, *lx1, *nel, dxm1, g, bm1, glo_num, err);
   if (rc) return fail(H, rc, err);
+  return NEKGPU_OK;
+}
+
+int nekgpu_setup_xyz(const int64_t* handle, const int* lx1, const int* nel, const double* dxm1,
+                     const double* wxm1, const double* xm1, const double* ym1, const double* zm1,
+                     const int64_t* glo_num) {
+  GET_HANDLE(handle);
+  if (!lx1 || !nel || !dxm1 || !wxm1 || !xm1 || !ym1 || !zm1 || !glo_num)
+    return fail(H, NEKGPU_EINVAL, "null argument");
+  std::string err;
+  const int rc = handle_setup_xyz(*H, *lx1, *nel, dxm1, wxm1, xm1, ym1, zm1, glo_num, err);
+  if (rc) return fail(H, rc, err);
+  return NEKGPU_OK;
+}
+
+int nekgpu_geom_update_dev(const int64_t* handle, const double* wxm1, const double* xm1,
+                           const double* ym1, const double* zm1) {
+  GET_HANDLE(handle);
+  NEED_MESH();
+  if (!wxm1 || !xm1 || !ym1 || !zm1) return fail(H, NEKGPU_EINVAL, "null argument");
+  std::string err;
+  const int rc = geom_from_xyz(*H, xm1, ym1, zm1, wxm1, err);
+  if (rc) return fail(H, rc, err);
+  return NEKGPU_OK;
+}
+
+int nekgpu_geometry(const int64_t* handle, double* g1, double* g2, double* g3, double* g4,
+                    double* g5, double* g6, double* bm1) {
+  GET_HANDLE(handle);
+  NEED_MESH();
+  const Mesh& m = H->mesh;
+  const int64_t n = m.n;
+  const int P = m.nx1 * m.nx1 * m.nx1;
+  std::vector<double> packed((size_t)(6 * n));
+  if (cudaMemcpy(packed.data(), m.f64.G, 6 * n * sizeof(double), cudaMemcpyDeviceToHost) !=
+          cudaSuccess ||
+      (bm1 && cudaMemcpy(bm1, m.f64.bm1, n * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess))
+    return fail(H, NEKGPU_ECUDA, "geometry download failed");
+  double* out[6] = {g1, g2, g3, g4, g5, g6};
+  for (int q = 0; q < 6; ++q)
+    if (out[q])
+      for (int64_t e = 0; e < m.nel; ++e)
+        std::memcpy(out[q] + e * P, packed.data() + (e * 6 + q) * P, P * sizeof(double));
   return NEKGPU_OK;
 }
 

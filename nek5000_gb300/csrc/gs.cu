@@ -1,5 +1,6 @@
 // gs.cu -- gather-scatter maps and kernels (see gs.cuh).
 #include <algorithm>
+#include <cstdint>
 #include <numeric>
 
 #include "gs_kernels.cuh"
@@ -58,11 +59,32 @@ int gs_setup(GsMaps& gs, const int64_t* glo_num, int64_t n, int nx1, std::string
     return -1;
   }
   gs.n = n;
+  // (id, local index) pairs of the numbered points in (id, index) order: a
+  // counting sort by id when the ids are dense (set_vert's are), else a sort
   std::vector<std::pair<int64_t, int>> pr;
-  pr.reserve((size_t)(n / 2));
-  for (int64_t i = 0; i < n; ++i)
-    if (glo_num[i] != 0) pr.emplace_back(glo_num[i], (int)i);
-  std::sort(pr.begin(), pr.end());
+  {
+    int64_t cnt_n = 0, gmin = INT64_MAX, gmax = INT64_MIN;
+    for (int64_t i = 0; i < n; ++i)
+      if (glo_num[i] != 0) {
+        ++cnt_n;
+        gmin = std::min(gmin, glo_num[i]);
+        gmax = std::max(gmax, glo_num[i]);
+      }
+    pr.resize((size_t)cnt_n);
+    if (cnt_n && gmax - gmin < 4 * n) {
+      std::vector<int> bucket((size_t)(gmax - gmin + 2), 0);
+      for (int64_t i = 0; i < n; ++i)
+        if (glo_num[i] != 0) ++bucket[(size_t)(glo_num[i] - gmin + 1)];
+      for (size_t b = 1; b < bucket.size(); ++b) bucket[b] += bucket[b - 1];
+      for (int64_t i = 0; i < n; ++i)  // ascending i: indices ascend within an id
+        if (glo_num[i] != 0) pr[(size_t)bucket[(size_t)(glo_num[i] - gmin)]++] = {glo_num[i], (int)i};
+    } else {
+      size_t q = 0;
+      for (int64_t i = 0; i < n; ++i)
+        if (glo_num[i] != 0) pr[q++] = {glo_num[i], (int)i};
+      std::sort(pr.begin(), pr.end());
+    }
+  }
   std::vector<int> st, ix, bst, bix;
   st.reserve(pr.size() / 2 + 1);
   ix.reserve(pr.size());
@@ -111,13 +133,18 @@ int gs_setup(GsMaps& gs, const int64_t* glo_num, int64_t n, int nx1, std::string
       const int sz = bst[g + 1] - bst[g];
       return sz == 1 ? 0 : sz == 2 ? 1 : sz == 4 ? 2 : sz == 8 ? 3 : 4;
     };
-    std::vector<int> ord(ns);
-    std::iota(ord.begin(), ord.end(), 0);
-    std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) {
-      const int ca = cls_of(a), cb = cls_of(b);
-      if (ca != cb) return ca < cb;
-      return bix[bst[a]] < bix[bst[b]];
-    });
+    // groups by class, then by first index (first indices are distinct):
+    // one pass over the local points per class
+    std::vector<int> group_at((size_t)n, -1);
+    for (size_t g = 0; g < ns; ++g) group_at[(size_t)bix[bst[g]]] = (int)g;
+    std::vector<int> by_cls[kGsClasses];
+    for (int64_t i = 0; i < n; ++i) {
+      const int g = group_at[(size_t)i];
+      if (g >= 0) by_cls[cls_of(g)].push_back(g);
+    }
+    std::vector<int> ord;
+    ord.reserve(ns);
+    for (int k = 0; k < kGsClasses; ++k) ord.insert(ord.end(), by_cls[k].begin(), by_cls[k].end());
     std::vector<int> nst, nix;
     nst.reserve(bst.size());
     nix.reserve(bix.size() + 16);

@@ -161,6 +161,39 @@ class NekGpu:
                                          glo.ctypes.data_as(C.c_void_p)))
         self.n, self.lx1, self.nel = n, lx1, nel
 
+    def setup_xyz(self, lx1: int, nel: int, D, w, x, y, z, glo_num):
+        """setup with G1..G6 and bm1 computed on the GPU from the GLL
+        coordinates x, y, z ((n,) numpy each) and the GLL weights w (lx1)."""
+        n = lx1 ** 3 * nel
+        dxm1 = np.ascontiguousarray(np.asarray(D, dtype=np.float64).T)
+        w = np.ascontiguousarray(w, dtype=np.float64)
+        xyz = [np.ascontiguousarray(a, dtype=np.float64).reshape(-1) for a in (x, y, z)]
+        glo = np.ascontiguousarray(glo_num, dtype=np.int64)
+        if any(a.size != n for a in xyz) or glo.size != n or w.size != lx1:
+            raise ValueError("x, y, z, glo_num must have lx1^3*nel entries, w lx1")
+        self._check(self._L.nekgpu_setup_xyz(C.byref(self._h), C.byref(_cint(lx1)),
+                                             C.byref(_cint(nel)), _ptr(dxm1), _ptr(w),
+                                             *(_ptr(a) for a in xyz),
+                                             glo.ctypes.data_as(C.c_void_p)))
+        self.n, self.lx1, self.nel = n, lx1, nel
+
+    def geom_update(self, w, x, y, z):
+        """New coordinates (torch float64 CUDA tensors) of the same mesh."""
+        w = np.ascontiguousarray(w, dtype=np.float64)
+        for t in (x, y, z):
+            if not _is_dev(t):
+                raise TypeError("geom_update takes device arrays")
+        self._check(self._L.nekgpu_geom_update_dev(C.byref(self._h), _ptr(w), _ptr(x), _ptr(y),
+                                                   _ptr(z)))
+
+    def geometry(self):
+        """(g (6, n), bm1 (n,)) in use, as numpy."""
+        g = np.zeros((6, self.n))
+        bm1 = np.zeros(self.n)
+        self._check(self._L.nekgpu_geometry(C.byref(self._h), *(_ptr(g[q]) for q in range(6)),
+                                            _ptr(bm1)))
+        return g, bm1
+
     def gs_maps(self):
         ns, ni = C.c_int64(0), C.c_int64(0)
         self._check(self._L.nekgpu_gs_maps(C.byref(self._h), C.byref(ns), C.byref(ni), None, None))

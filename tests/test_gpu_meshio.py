@@ -68,3 +68,51 @@ def test_re2_mesh_solves_match_the_oracle(gpu_lib, oracle, tmp_path, case):
     assert rn <= 1.05e-10 * r0m
     assert np.linalg.norm(xmh - x_ref) <= 1e-8 * np.linalg.norm(x_ref)
     print(case, "fp64 iterations", it, "mixed", no, ni)
+
+
+@pytest.mark.parametrize("nx1", [2, 3, 5, 8, 10, 12])
+def test_device_geometry_is_the_reference_bit_for_bit(gpu_lib, oracle, nx1):
+    """nekgpu_setup_xyz: G1..G6 and bm1 formed on the GPU from xm1, ym1, zm1
+    equal the oracle's xyzrst / glmapm1 / geodat1 restatement exactly."""
+    from conftest import rng_unit_vector
+    P = oracle.box_problem(nx1, 3, 2, 2, v=rng_unit_vector(nx1 + 40), amp=0.08)
+    lib = gpu_lib(0)
+    lib.setup_xyz(P["nx1"], P["nel"], P["D"], P["wgll"], P["x"], P["y"], P["z"], P["glo_num"])
+    g, bm1 = lib.geometry()
+    assert np.array_equal(g, P["g"].reshape(6, -1))
+    assert np.array_equal(bm1, P["bm1"])
+
+
+def test_moving_mesh_geometry_update(gpu_lib, oracle):
+    """nekgpu_geom_update_dev: new coordinates of the same mesh give the
+    oracle's geometry of the moved mesh, and the solve sees it (volume and
+    operator both updated)."""
+    torch = pytest.importorskip("torch")
+    from conftest import rng_unit_vector
+    P = oracle.box_problem(8, 3, 3, 2, v=rng_unit_vector(50), amp=0.05)
+    Q = oracle.box_problem(8, 3, 3, 2, v=rng_unit_vector(51), amp=0.09)  # the moved mesh
+    lib = gpu_lib(0)
+    lib.setup_xyz(P["nx1"], P["nel"], P["D"], P["wgll"], P["x"], P["y"], P["z"], P["glo_num"])
+    dev = lambda a: torch.tensor(a, device="cuda")
+    lib.geom_update(P["wgll"], dev(Q["x"]), dev(Q["y"]), dev(Q["z"]))
+    g, bm1 = lib.geometry()
+    assert np.array_equal(g, Q["g"].reshape(6, -1)) and np.array_equal(bm1, Q["bm1"])
+    n = Q["n"]
+    h1, h2 = np.ones(n), np.full(n, 10.0)
+    f = Q["ops"].dssum(Q["bm1"] * np.random.default_rng(52).standard_normal(n)) * Q["mask"]
+    x_ref, it_ref, r0_ref, _ = Q["ops"].cggo(f, h1, h2, Q["mask"], Q["mult"], Q["binv"], -1e-10,
+                                             maxcg=10 ** 6)
+    x = torch.zeros(n, dtype=torch.float64, device="cuda")
+    it, r0, r2, rc = lib.cggo(x, dev(f), dev(h1), dev(h2), dev(Q["mask"]), dev(Q["mult"]), 1,
+                              -1e-10, 10 ** 6, 1, dev(Q["binv"]), maxcg=10 ** 6)
+    assert rc == 0 and abs(it - it_ref) <= 1
+    assert abs(r0 - r0_ref) <= 1e-13 * r0_ref  # the volume was updated too
+    assert np.linalg.norm(x.cpu().numpy() - x_ref) <= 1e-10 * np.linalg.norm(x_ref)
+    # a tangled element map is refused, not computed
+    bad = Q["x"].copy()
+    P3 = Q["nx1"] ** 3
+    bad[:P3] = bad[:P3][::-1].copy()  # mirror element 0
+    from nek5000_gb300 import _capi
+    with pytest.raises(_capi.NekGpuError) as ei:
+        lib.geom_update(P["wgll"], dev(bad), dev(Q["y"]), dev(Q["z"]))
+    assert ei.value.code == _capi.EINVAL
