@@ -50,6 +50,7 @@ SIGNATURES = {
     "nekmesh_connect": [_IP, _IP, _P, _P, _P, _P, _P, _DP, _P, _I64P],
     "nekmesh_setvert3d": [_IP, _IP, _P, _P, _I64P],
     "nekmesh_xyzlin": [_IP, _IP, _P, _P, _P, _P, _P, _P, _P],
+    "nekmesh_genxyz": [_IP, _IP, _P, _P, _P, _P, _I64P, _P, _P, _P, C.c_char_p, _P, _P, _P],
     # solve path (include/nekgpu.h)
     "nekgpu_init": [_IP, _I64P],
     "nekgpu_finalize": [_I64P],

@@ -57,6 +57,10 @@ struct AxArgs {
   // (sum_g w_g p_g = sum_i w_local_i p_i), and spares the boundary-group
   // kernel its p reads.  The FP32 inner solve uses 1.
   int allrho;
+  // 1: G, d, bm1, h1, h2 are read by several launches of one iteration (the
+  // fields of a multi-field solve): staged with the default L2 policy so that
+  // the later reads hit L2; 0: every input is read once (evict first).
+  int shared_in;
 };
 
 template <int NX>

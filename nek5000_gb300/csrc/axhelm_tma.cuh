@@ -83,10 +83,12 @@ __device__ __forceinline__ void load_row(const T* __restrict__ p, T (&v)[NX]) {
   }
 }
 
+// Body of the kernel for element block `blk` (elements blk*EPB ...); the
+// block's threads are (NX*NX, EPB); smem_raw is its dynamic shared memory.
 template <int NX, typename T, bool FUSED, int EPB>
-__global__ void __launch_bounds__(NX* NX* EPB) axhelm_tma_kernel(const AxArgs<T> a) {
+__device__ __forceinline__ void axhelm_tma_body(const AxArgs<T>& a, int blk,
+                                                unsigned char* smem_raw) {
   constexpr int P = NX * NX * NX, NXY = NX * NX;
-  extern __shared__ __align__(128) unsigned char smem_raw[];
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
   T* sD = reinterpret_cast<T*>(smem_raw + 64);  // D[i][l] row-major
   // staged slices, each EPB*P values, 16-byte aligned (P*sizeof(T) % 16 == 0)
@@ -106,7 +108,7 @@ __global__ void __launch_bounds__(NX* NX* EPB) axhelm_tma_kernel(const AxArgs<T>
     if (a.cg->done) return;
   }
   const int tid = threadIdx.x + NXY * threadIdx.y;
-  const int e0 = blockIdx.x * EPB;
+  const int e0 = blk * EPB;
   const int ne = min(EPB, a.nel - e0);  // elements of this block
   if (tid == 0) {
     mbar_init(bar, 1);
@@ -120,16 +122,18 @@ __global__ void __launch_bounds__(NX* NX* EPB) axhelm_tma_kernel(const AxArgs<T>
     const uint32_t total = fb * (1 + (FUSED ? 2 : 0) + hb + hh1 + hh2 + 6);
     mbar_expect_tx(bar, total);
     // every input is read once per apply: evict first, so that L2 keeps w
+    // (operands shared by the fields of a multi-field solve: default policy)
     const uint64_t pol = l2_policy_evict_first();
+    const uint64_t spol = a.shared_in ? l2_policy_evict_normal() : pol;
     bulk_g2s_hint(sU, a.u + off, fb, bar, pol);
     if constexpr (FUSED) {
       bulk_g2s_hint(sR, a.r + off, fb, bar, pol);
-      bulk_g2s_hint(sDg, a.d + off, fb, bar, pol);
+      bulk_g2s_hint(sDg, a.d + off, fb, bar, spol);
     }
-    if (hb) bulk_g2s_hint(sB, a.bm1 + off, fb, bar, pol);
-    if (hh1) bulk_g2s_hint(sH1, a.h1 + off, fb, bar, pol);
-    if (hh2) bulk_g2s_hint(sH2, a.h2 + off, fb, bar, pol);
-    bulk_g2s_hint(sG, a.G + 6 * off, 6 * fb, bar, pol);
+    if (hb) bulk_g2s_hint(sB, a.bm1 + off, fb, bar, spol);
+    if (hh1) bulk_g2s_hint(sH1, a.h1 + off, fb, bar, spol);
+    if (hh2) bulk_g2s_hint(sH2, a.h2 + off, fb, bar, spol);
+    bulk_g2s_hint(sG, a.G + 6 * off, 6 * fb, bar, spol);
   }
   // D rows / columns of this thread while the copies fly
   const int i = threadIdx.x % NX, j = threadIdx.x / NX, el = threadIdx.y;
@@ -239,6 +243,12 @@ __global__ void __launch_bounds__(NX* NX* EPB) axhelm_tma_kernel(const AxArgs<T>
     element_sum<NX, T>(dot, sG + 6 * lo, threadIdx.x, true, el < ne ? a.partial + e0 + el : nullptr);
   }
   if (tid == 0 && ok) mbar_inval(bar);
+}
+
+template <int NX, typename T, bool FUSED, int EPB>
+__global__ void __launch_bounds__(NX* NX* EPB) axhelm_tma_kernel(const AxArgs<T> a) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  axhelm_tma_body<NX, T, FUSED, EPB>(a, blockIdx.x, smem_raw);
 }
 
 }  // namespace nekgpu

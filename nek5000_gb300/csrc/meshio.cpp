@@ -4,6 +4,7 @@
 // and the GLL coordinates of straight-sided elements (xyzlin).  Host code
 // only; the arrays produced are what nekgpu_setup consumes.
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -795,6 +796,162 @@ int nekmesh_setvert3d(const int* nx_, const int* nel_, const int64_t* vertex, in
   }
   ngv += nface * nif;
   if (ngv_out) *ngv_out = ngv;
+  return NEKGPU_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// Interpolation weights at xx from the nodes x[0..n] (order 0 of Fornberg's
+// recursion, as fd_weights_full, core/fast3d.f:1294, evaluates them).
+void fd_weights0(double xx, const double* x, int n, double* c) {
+  double c1 = 1.0, c4 = x[0] - xx;
+  for (int j = 0; j <= n; ++j) c[j] = 0.0;
+  c[0] = 1.0;
+  for (int i = 1; i <= n; ++i) {
+    double c2 = 1.0;
+    const double c5 = c4;
+    c4 = x[i] - xx;
+    for (int j = 0; j < i; ++j) {
+      const double c3 = x[i] - x[j];
+      c2 = c2 * c3;
+      c[i] = -(((c1 * c5) * c[i - 1]) / c2);
+      c[j] = (c4 * c[j]) / c3;
+    }
+    c1 = c2;
+  }
+}
+
+// v (nv^3) = (C x B x A) u (nu^3) with A[i][a] = wt[i*nu + a] for all three
+// directions, as tensr3 (core/fasts.f:125): r, then s, then t, each an
+// nu-term sum in order.
+void tensor3(double* v, int nv, const double* u, int nu, const double* wt) {
+  std::vector<double> t1((size_t)nv * nu * nu), t2((size_t)nv * nv * nu);
+  for (int bc = 0; bc < nu * nu; ++bc)
+    for (int i = 0; i < nv; ++i) {
+      double s = wt[i * nu] * u[nu * bc];
+      for (int a = 1; a < nu; ++a) s = s + wt[i * nu + a] * u[a + nu * bc];
+      t1[(size_t)(i + nv * bc)] = s;
+    }
+  for (int c = 0; c < nu; ++c)
+    for (int j = 0; j < nv; ++j)
+      for (int i = 0; i < nv; ++i) {
+        double s = t1[(size_t)(i + nv * (nu * c))] * wt[j * nu];
+        for (int b = 1; b < nu; ++b) s = s + t1[(size_t)(i + nv * (b + nu * c))] * wt[j * nu + b];
+        t2[(size_t)(i + nv * (j + nv * c))] = s;
+      }
+  for (int k = 0; k < nv; ++k)
+    for (int j = 0; j < nv; ++j)
+      for (int i = 0; i < nv; ++i) {
+        double s = t2[(size_t)(i + nv * j)] * wt[k * nu];
+        for (int c = 1; c < nu; ++c) s = s + t2[(size_t)(i + nv * (j + nv * c))] * wt[k * nu + c];
+        v[i + nv * (j + nv * k)] = s;
+      }
+}
+
+// Gordon-Hall extension of a 3x3x3 array from its vertices and edges
+// (gh_face_extend_3d, core/navier5.f:2502, gh_type 2) at nodes -1, 0, 1.
+void gordon_hall_edges3(double* x) {
+  constexpr int n = 3;
+  const double zg[3] = {-1.0, 0.0, 1.0};
+  auto at = [](int i, int j, int k) { return i + n * (j + n * k); };
+  auto lin = [&](int end, int i) {  // 0.5 ((n-end)(1-z) + (end-1)(1+z)) / (n-1), end 1 or n
+    return 0.5 * ((double)(n - end) * (1.0 - zg[i]) + (double)(end - 1) * (1.0 + zg[i])) / (double)(n - 1);
+  };
+  double v[27] = {0}, e[27] = {0};
+  for (int kk = 1; kk <= n; kk += n - 1)
+    for (int jj = 1; jj <= n; jj += n - 1)
+      for (int ii = 1; ii <= n; ii += n - 1)
+        for (int k = 0; k < n; ++k)
+          for (int j = 0; j < n; ++j)
+            for (int i = 0; i < n; ++i)
+              v[at(i, j, k)] = v[at(i, j, k)] +
+                               lin(ii, i) * lin(jj, j) * lin(kk, k) * x[at(ii - 1, jj - 1, kk - 1)];
+  for (int kk = 1; kk <= n; kk += n - 1)  // x-edges
+    for (int jj = 1; jj <= n; jj += n - 1)
+      for (int k = 0; k < n; ++k)
+        for (int j = 0; j < n; ++j)
+          for (int i = 0; i < n; ++i)
+            e[at(i, j, k)] = e[at(i, j, k)] + lin(jj, j) * lin(kk, k) *
+                                                  (x[at(i, jj - 1, kk - 1)] - v[at(i, jj - 1, kk - 1)]);
+  for (int kk = 1; kk <= n; kk += n - 1)  // y-edges
+    for (int ii = 1; ii <= n; ii += n - 1)
+      for (int k = 0; k < n; ++k)
+        for (int j = 0; j < n; ++j)
+          for (int i = 0; i < n; ++i)
+            e[at(i, j, k)] = e[at(i, j, k)] + lin(ii, i) * lin(kk, k) *
+                                                  (x[at(ii - 1, j, kk - 1)] - v[at(ii - 1, j, kk - 1)]);
+  for (int jj = 1; jj <= n; jj += n - 1)  // z-edges
+    for (int ii = 1; ii <= n; ii += n - 1)
+      for (int k = 0; k < n; ++k)
+        for (int j = 0; j < n; ++j)
+          for (int i = 0; i < n; ++i)
+            e[at(i, j, k)] = e[at(i, j, k)] + lin(ii, i) * lin(jj, j) *
+                                                  (x[at(ii - 1, jj - 1, k)] - v[at(ii - 1, jj - 1, k)]);
+  for (int q = 0; q < 27; ++q) x[q] = e[q] + v[q];
+}
+
+// Midside node of each preprocessor edge (1..12) in the 3x3x3 array.
+constexpr int kEdgeMid[12] = {1, 5, 7, 3, 19, 23, 25, 21, 9, 11, 17, 15};
+
+}  // namespace
+
+extern "C" {
+
+int nekmesh_genxyz(const int* nx_, const int* nel_, const double* zg, const double* xc,
+                   const double* yc, const double* zc, const int64_t* ncurve, const int* elem,
+                   const int* side, const double* curve, const char* ccurve, double* x, double* y,
+                   double* z) {
+  if (!nx_ || !nel_ || !zg || !xc || !yc || !zc || !x || !y || !z || *nx_ < 2 || *nel_ <= 0 ||
+      (ncurve && *ncurve > 0 && (!elem || !side || !curve || !ccurve)))
+    return fail(NEKGPU_EINVAL, "genxyz: bad arguments");
+  const int nx = *nx_;
+  const int64_t nel = *nel_, nxyz = (int64_t)nx * nx * nx, nc = ncurve ? *ncurve : 0;
+  // midside nodes per element (edges 1..12); any other curve type is refused
+  std::vector<int64_t> first((size_t)nel, -1);
+  std::vector<std::array<int, 12>> mid;
+  for (int64_t q = 0; q < nc; ++q) {
+    const int64_t e = elem[q] - 1;
+    if (e < 0 || e >= nel) return fail(NEKGPU_EINVAL, "genxyz: curve record names no element");
+    if (ccurve[q] == ' ' || ccurve[q] == '\0') continue;
+    if (ccurve[q] != 'm')
+      return fail(NEKGPU_EINVAL, std::string("genxyz: curved side type '") + ccurve[q] +
+                                     "' not served (only 'm' midside nodes)");
+    if (side[q] < 1 || side[q] > 12) return fail(NEKGPU_EINVAL, "genxyz: midside node on no edge");
+    if (first[(size_t)e] < 0) {
+      first[(size_t)e] = (int64_t)mid.size();
+      std::array<int, 12> none;
+      none.fill(-1);
+      mid.push_back(none);
+    }
+    mid[(size_t)first[(size_t)e]][side[q] - 1] = (int)q;
+  }
+  // straight-sided elements (and every element when nx = 2, as linquad)
+  int rc = nekmesh_xyzlin(nx_, nel_, zg, xc, yc, zc, x, y, z);
+  if (rc || nx == 2) return rc;
+  // quadratic elements (xyzquad, core/genxyz.f:1334): the trilinear 3x3x3
+  // map, the file's midside nodes on their edges, edges extended inward by
+  // Gordon-Hall, then the quadratic interpolant at the GLL nodes
+  const double zq[3] = {-1.0, 0.0, 1.0};
+  std::vector<double> wq((size_t)nx * 3);
+  for (int i = 0; i < nx; ++i) fd_weights0(zg[i], zq, 2, &wq[(size_t)i * 3]);
+  const double* src[3] = {xc, yc, zc};
+  double* dst[3] = {x, y, z};
+  const double wl[6] = {1.0, 0.0, 0.5, 0.5, 0.0, 1.0};  // (1-z)/2, (1+z)/2 at -1, 0, 1
+  for (int64_t e = 0; e < nel; ++e) {
+    if (first[(size_t)e] < 0) continue;
+    const auto& m = mid[(size_t)first[(size_t)e]];
+    for (int d = 0; d < 3; ++d) {
+      double u[8], q3[27];
+      for (int c = 0; c < 8; ++c) u[c] = src[d][8 * e + kPreOfTensor[c]];
+      tensor3(q3, 3, u, 2, wl);
+      for (int k = 0; k < 12; ++k)
+        if (m[k] >= 0) q3[kEdgeMid[k]] = curve[5 * (size_t)m[k] + d];
+      gordon_hall_edges3(q3);
+      tensor3(dst[d] + nxyz * e, nx, q3, 3, wq.data());
+    }
+  }
   return NEKGPU_OK;
 }
 

@@ -7,10 +7,11 @@
 // convergence test, residual replacements, mask), but one iteration of all of
 // them is three kernels:
 //
-//  * the fused operator stages an element's geometric factors, Jacobi
-//    diagonal and mass once and applies the operator to every live field's
-//    search direction (p = r d + beta p first), so G -- half of an FP32
-//    operator's traffic -- is read once for all fields;
+//  * one operator launch for every live field: block b runs the single-field
+//    TMA kernel body on field b % nc of element b / nc, so the blocks of an
+//    element's fields run side by side and its geometric factors, Jacobi
+//    diagonal and mass -- more than half of an FP32 operator's traffic --
+//    come from DRAM once and from L2 for the other fields;
 //  * the boundary-group kernel loads each group's indices once and gathers,
 //    masks and scatters every live field's w;
 //  * the update kernel reads the folded weights once for all fields.
@@ -34,24 +35,6 @@ namespace nekgpu {
 
 constexpr int kMaxFields = NEKGPU_MULTI_MAX;
 
-struct MultiOpArgs {
-  const float* G;
-  const float* bm1;
-  const float* h1;
-  const float* h2;
-  float h1s, h2s;
-  int h1mode, h2mode;
-  const float* D;
-  const float* d;  // Jacobi diagonal (shared)
-  int nel, nc;
-  float* p[kMaxFields];        // in: old p; out: new p
-  const float* r[kMaxFields];
-  float* w[kMaxFields];
-  const CgScalars* cg[kMaxFields];
-  double* partial[kMaxFields];  // per element rho partials
-  int* err;
-};
-
 namespace {
 
 constexpr int kThreads = 256;
@@ -61,220 +44,37 @@ inline int vblocks(int64_t n) {
   return (int)std::min<int64_t>(std::max<int64_t>((n + kThreads - 1) / kThreads, 1), kBlocks);
 }
 
-// Threads of one field's group: lx1^2 rounded up to whole warps, so that
-// the groups of the three fields never share a warp.
-template <int NX>
-__host__ __device__ constexpr int multi_group() {
-  return ((NX * NX + 31) / 32) * 32;
-}
-
-// Slices staged per element (each lx1^3 floats): G (6), the Jacobi diagonal
-// d, bm1 (h2 != 0), h1 and h2 (per point), then the old p and the r of every
-// field and two work slabs.  After the p updates the r slab of field c is its
-// first work slab, the d slab the second one of field 0 and the two extra
-// slabs those of fields 1 and 2; in the last phase the p slab of field c holds
-// its element sum.
-inline int multi_slices(int h1mode, int h2mode) {
-  return 6 + 1 + (h2mode ? 1 : 0) + (h1mode == 1 ? 1 : 0) + (h2mode == 2 ? 1 : 0) +
-         2 * kMaxFields + (kMaxFields - 1);
-}
-
-// Row stride of the staged D: whole 16-byte vectors (rows are read as
-// vectors), not a multiple of 8 floats.
-template <int NX>
-__host__ __device__ constexpr int multi_ldp() {
-  return ((NX + 3) / 4) * 4 + ((((NX + 3) / 4) * 4) % 8 == 0 ? 4 : 0);
-}
+// The operator of every live field, one launch: block b applies the
+// single-field TMA kernel body (axhelm_tma.cuh, one element per block) to
+// field b % nc of element b / nc.  The blocks of one element's fields run
+// side by side, so the element's G, d, bm1 (and per-point h1, h2), staged
+// with the default L2 policy, come from DRAM once and from L2 for the other
+// fields; each field's arithmetic is exactly the single-field solve's.
+struct MultiTmaArgs {
+  AxArgs<float> base;  // shared operands and modes; per-field pointers below
+  float* p[kMaxFields];
+  const float* r[kMaxFields];
+  float* w[kMaxFields];
+  const CgScalars* cg[kMaxFields];
+  double* partial[kMaxFields];
+  int nc;
+};
 
 template <int NX>
-size_t multi_smem_bytes(int h1mode, int h2mode) {
-  return 64 + (size_t)NX * multi_ldp<NX>() * sizeof(float) +
-         (size_t)multi_slices(h1mode, h2mode) * NX * NX * NX * sizeof(float);
-}
-
-// One element per block and one group of threads per field (thread (i,j) of
-// group c walks the z-column of field c); every group runs the same phases
-// between the same block barriers, so a field that has converged only idles.
-// Blocks per SM the register budget is held to (lx1 = 8: 5 blocks of 192
-// threads, 64 registers each, at 33 KB of shared memory per block; lx1 = 10
-// and 12 keep their registers).  Measured at lx1 = 8, E = 32^3, three live
-// fields: 0.32 ms per launch at 5 blocks (D in registers, D^T from shared
-// memory), 0.36 ms at 4 blocks with D^T in registers as well, 0.38 ms at 6
-// blocks with both from shared memory: the kernel is bound by shared-memory
-// wavefronts and occupancy, not by DRAM.
-template <int NX>
-__host__ __device__ constexpr int multi_min_blocks() {
-  return NX <= 4 ? 10 : NX <= 8 ? 5 : 1;
-}
-
-template <int NX>
-__global__ void __launch_bounds__(kMaxFields* multi_group<NX>(), multi_min_blocks<NX>())
-    multi_op_kernel(const MultiOpArgs a) {
-  constexpr int P = NX * NX * NX, NXY = NX * NX, GS = multi_group<NX>(), LDP = multi_ldp<NX>();
+__global__ void __launch_bounds__(NX* NX) multi_op_kernel(const MultiTmaArgs m) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  bool live[kMaxFields];
-  bool any = false;
-#pragma unroll
-  for (int c = 0; c < kMaxFields; ++c) {
-    live[c] = c < a.nc && !a.cg[c]->done;
-    any = any || live[c];
-  }
-  if (!any) return;  // uniform over the grid
-  uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
-  float* sD = reinterpret_cast<float*>(smem_raw + 64);  // D[r][l] at r LDP + l
-  float* base = sD + NX * LDP;
-  const int hb = a.h2mode ? 1 : 0, hh1 = a.h1mode == 1 ? 1 : 0, hh2 = a.h2mode == 2 ? 1 : 0;
-  float* sG = base;
-  float* sDg = sG + 6 * P;
-  float* sB = sDg + P;
-  float* sH1 = sB + hb * P;
-  float* sH2 = sH1 + hh1 * P;
-  float* sU0 = sH2 + hh2 * P;          // old p of field c: sU0 + c P
-  float* sR0 = sU0 + kMaxFields * P;   // r of field c: sR0 + c P
-  float* sX0 = sR0 + kMaxFields * P;   // work slabs of fields 1, 2
-  const int tid = threadIdx.x;
-  const int fc = tid / GS, lt = tid % GS;  // this thread's field and place in it
-  const int e = blockIdx.x;
-  if (tid == 0) {
-    mbar_init(bar, 1);
-    mbar_fence_init();
-  }
-  for (int q = tid; q < NXY; q += blockDim.x) {
-    sD[(q / NX) * LDP + q % NX] = a.D[q];
-  }
-  __syncthreads();
-  if (tid == 0) {
-    const uint32_t fb = (uint32_t)(P * sizeof(float));
-    const size_t off = (size_t)e * P;
-    int nlive = 0;
-#pragma unroll
-    for (int c = 0; c < kMaxFields; ++c) nlive += live[c] ? 1 : 0;
-    mbar_expect_tx(bar, fb * (6 + 1 + hb + hh1 + hh2 + 2 * nlive));
-    const uint64_t pol = l2_policy_evict_first();
-    bulk_g2s_hint(sG, a.G + 6 * off, 6 * fb, bar, pol);
-    bulk_g2s_hint(sDg, a.d + off, fb, bar, pol);
-    if (hb) bulk_g2s_hint(sB, a.bm1 + off, fb, bar, pol);
-    if (hh1) bulk_g2s_hint(sH1, a.h1 + off, fb, bar, pol);
-    if (hh2) bulk_g2s_hint(sH2, a.h2 + off, fb, bar, pol);
-#pragma unroll
-    for (int c = 0; c < kMaxFields; ++c)
-      if (live[c]) {
-        bulk_g2s_hint(sU0 + c * P, a.p[c] + off, fb, bar, pol);
-        bulk_g2s_hint(sR0 + c * P, a.r[c] + off, fb, bar, pol);
-      }
-  }
-  // this thread's field, its slabs and its point column
-  bool mine = false;
-  float* sU = sU0;
-  float* st1 = sR0;
-  float* st2 = sDg;
-  float* wc = a.w[0];
-  float* pc = a.p[0];
-  double* partc = a.partial[0];
-  float beta = 0.f;
+  const int f = blockIdx.x % m.nc, e = blockIdx.x / m.nc;
+  AxArgs<float> a = m.base;
 #pragma unroll
   for (int c = 0; c < kMaxFields; ++c)
-    if (fc == c) {
-      mine = live[c] && lt < NXY;
-      sU = sU0 + c * P;
-      st1 = sR0 + c * P;
-      st2 = c == 0 ? sDg : sX0 + (c - 1) * P;
-      wc = a.w[c];
-      pc = a.p[c];
-      partc = a.partial[c] + e;
+    if (f == c) {
+      a.u = a.p = m.p[c];
+      a.au = m.w[c];
+      a.r = m.r[c];
+      a.cg = m.cg[c];
+      a.partial = m.partial[c];
     }
-  const int i = lt % NX, j = (lt / NX) % NX;
-  float Di[NX], Dj[NX];
-#pragma unroll
-  for (int l = 0; l < NX; ++l) {
-    Di[l] = a.D[i * NX + l];
-    Dj[l] = a.D[j * NX + l];
-  }
-  const bool ok = mbar_wait_bounded(bar, 0, a.err);
-  const bool act = ok && mine;
-  if (act) beta = (float)a.cg[fc]->beta;
-  const size_t eo = (size_t)e * P;
-  // p = beta p + r d (add2s1)
-  float ru[NX];
-#pragma unroll
-  for (int k = 0; k < NX; ++k) {
-    const int pt = k * NXY + j * NX + i;
-    float v = 0.f;
-    if (act) {
-      v = fma(beta, sU[pt], st1[pt] * sDg[pt]);
-      sU[pt] = v;
-      pc[eo + pt] = v;
-    }
-    ru[k] = v;
-  }
-  __syncthreads();  // every field's p is in place; the r and d slabs are free
-  float rau[NX];
-#pragma unroll
-  for (int m = 0; m < NX; ++m) rau[m] = 0.f;
-  if (act) {
-#pragma unroll
-    for (int k = 0; k < NX; ++k) {
-      const float* slab = sU + k * NXY;
-      float row[NX], dk[NX];
-      load_row<NX, float>(slab + j * NX, row);
-      load_row<NX, float>(sD + k * LDP, dk);
-      float ur = Di[0] * row[0];
-#pragma unroll
-      for (int l = 1; l < NX; ++l) ur = fma(Di[l], row[l], ur);
-      float us = slab[i] * Dj[0];
-#pragma unroll
-      for (int l = 1; l < NX; ++l) us = fma(slab[l * NX + i], Dj[l], us);
-      float ut = ru[0] * dk[0];
-#pragma unroll
-      for (int l = 1; l < NX; ++l) ut = fma(ru[l], dk[l], ut);
-      const int pt = k * NXY + j * NX + i;
-      const float g1 = sG[pt], g2 = sG[P + pt], g3 = sG[2 * P + pt], g4 = sG[3 * P + pt],
-                  g5 = sG[4 * P + pt], g6 = sG[5 * P + pt];
-      const float h = hh1 ? sH1[pt] : a.h1s;
-      float t1 = ur * g1, t2 = us * g2, t3 = ut * g3;
-      t1 = fma(us, g4, t1);
-      t1 = fma(ut, g5, t1);
-      t2 = fma(ur, g4, t2);
-      t2 = fma(ut, g6, t2);
-      t3 = fma(ur, g5, t3);
-      t3 = fma(us, g6, t3);
-      st1[pt] = t1 * h;
-      st2[pt] = t2 * h;
-      t3 *= h;
-#pragma unroll
-      for (int m = 0; m < NX; ++m) rau[m] = (k == 0) ? t3 * dk[m] : fma(t3, dk[m], rau[m]);
-    }
-  }
-  __syncthreads();
-  float dot = 0.f;
-  if (act) {
-    const uint64_t keep = l2_policy_evict_last();
-#pragma unroll
-    for (int k = 0; k < NX; ++k) {
-      const float* s1 = st1 + k * NXY;
-      const float* s2 = st2 + k * NXY;
-      float row[NX];
-      load_row<NX, float>(s1 + j * NX, row);
-      // D^T from the staged D (registers go to occupancy)
-      float tm1 = sD[i] * row[0];
-#pragma unroll
-      for (int l = 1; l < NX; ++l) tm1 = fma(sD[l * LDP + i], row[l], tm1);
-      float tm2 = s2[i] * sD[j];
-#pragma unroll
-      for (int l = 1; l < NX; ++l) tm2 = fma(s2[l * NX + i], sD[l * LDP + j], tm2);
-      float sv = (tm1 + tm2) + rau[k];
-      const int pt = k * NXY + j * NX + i;
-      if (hb) {
-        const float hv = hh2 ? sH2[pt] : a.h2s;
-        sv = fma(hv * sB[pt], ru[k], sv);
-      }
-      st_hint(wc + eo + pt, sv, keep);
-      dot = fma(sv, ru[k], dot);  // rho over every point (AxArgs::allrho)
-    }
-  }
-  // the field's p slab (read only before the second barrier) holds its sum
-  element_sum<NX, float>(dot, sU, lt, mine, act ? partc : nullptr);
-  if (tid == 0 && ok) mbar_inval(bar);
+  axhelm_tma_body<NX, float, true, 1>(a, e, smem_raw);
 }
 
 // Boundary groups of C copies, G per thread: indices loaded once, every live
@@ -528,31 +328,31 @@ __global__ void fold_kernel(float* __restrict__ md, float* __restrict__ mb,
 }
 
 template <int NX>
-cudaError_t launch_op_nx(const MultiOpArgs& a, cudaStream_t s) {
-  const size_t smem = multi_smem_bytes<NX>(a.h1mode, a.h2mode);
-  static size_t configured = 0;
-  if (smem > configured) {
+cudaError_t launch_op_nx(const MultiTmaArgs& m, cudaStream_t s) {
+  const size_t smem = tma_smem_bytes<NX, float, 1>(true, m.base.h1mode, m.base.h2mode);
+  static bool configured = false;
+  if (!configured) {
+    const int maxb = (int)tma_smem_bytes<NX, float, 1>(true, 1, 2);
     cudaError_t e = cudaFuncSetAttribute(multi_op_kernel<NX>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, maxb);
     if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(multi_op_kernel<NX>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                             (int)cudaSharedmemCarveoutMaxShared);
-    if (e != cudaSuccess) return e;
-    configured = smem;
+    cudaFuncSetAttribute(multi_op_kernel<NX>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                         100);
+    configured = true;
   }
   count_launch();
-  multi_op_kernel<NX><<<a.nel, kMaxFields * multi_group<NX>(), smem, s>>>(a);
+  multi_op_kernel<NX><<<m.base.nel * m.nc, NX * NX, smem, s>>>(m);
   return cudaGetLastError();
 }
 
-cudaError_t launch_op(int nx, const MultiOpArgs& a, cudaStream_t s) {
+cudaError_t launch_op(int nx, const MultiTmaArgs& m, cudaStream_t s) {
   switch (nx) {
-    case 2: return launch_op_nx<2>(a, s);
-    case 4: return launch_op_nx<4>(a, s);
-    case 6: return launch_op_nx<6>(a, s);
-    case 8: return launch_op_nx<8>(a, s);
-    case 10: return launch_op_nx<10>(a, s);
-    case 12: return launch_op_nx<12>(a, s);
+    case 2: return launch_op_nx<2>(m, s);
+    case 4: return launch_op_nx<4>(m, s);
+    case 6: return launch_op_nx<6>(m, s);
+    case 8: return launch_op_nx<8>(m, s);
+    case 10: return launch_op_nx<10>(m, s);
+    case 12: return launch_op_nx<12>(m, s);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -724,20 +524,23 @@ int mixed_multi_solve(Handle& h, int nc, double* const* x, const double* const* 
     return -3;
   }
   // kernel arguments (fixed for the whole solve)
-  MultiOpArgs oa{};
-  oa.G = m.f32.G;
-  oa.bm1 = m.f32.bm1;
-  oa.h1 = c32.h1mode ? w32.h1.ptr : nullptr;
-  oa.h2 = c32.h2mode == 2 ? w32.h2.ptr : nullptr;
-  oa.h1s = c32.h1s;
-  oa.h2s = c32.h2s;
-  oa.h1mode = c32.h1mode;
-  oa.h2mode = c32.h2mode;
-  oa.D = m.f32.D;
-  oa.d = w32.d.ptr;
-  oa.nel = m.nel;
+  MultiTmaArgs oa{};
+  oa.base.G = m.f32.G;
+  oa.base.bm1 = m.f32.bm1;
+  oa.base.h1 = c32.h1mode ? w32.h1.ptr : nullptr;
+  oa.base.h2 = c32.h2mode == 2 ? w32.h2.ptr : nullptr;
+  oa.base.h1s = c32.h1s;
+  oa.base.h2s = c32.h2s;
+  oa.base.h1mode = c32.h1mode;
+  oa.base.h2mode = c32.h2mode;
+  oa.base.D = m.f32.D;
+  oa.base.d = w32.d.ptr;
+  oa.base.nel = m.nel;
+  oa.base.err = m.dev_err;
+  oa.base.skip = m.gs.skip;
+  oa.base.allrho = 1;
+  oa.base.shared_in = 1;
   oa.nc = nc;
-  oa.err = m.dev_err;
   MultiGsArgs ga{};
   ga.partialB = h.mpartialB.ptr;
   ga.counter = h.mcounter.ptr;
@@ -757,8 +560,9 @@ int mixed_multi_solve(Handle& h, int nc, double* const* x, const double* const* 
   ua.counter = h.mcounter.ptr + 1;
   ua.n = n;
   ua.nc = nc;
-  bool aligned = al16(oa.G) && al16(oa.bm1) && al16(oa.d) && al16(oa.D) &&
-                 (!oa.h1 || al16(oa.h1)) && (!oa.h2 || al16(oa.h2)) && al16(ua.md) && al16(ua.mb);
+  bool aligned = al16(oa.base.G) && al16(oa.base.bm1) && al16(oa.base.d) &&
+                 (!oa.base.h1 || al16(oa.base.h1)) && (!oa.base.h2 || al16(oa.base.h2)) &&
+                 al16(ua.md) && al16(ua.mb);
   for (int c = 0; c < nc; ++c) {
     MultiField& F = *h.multi[c];
     oa.p[c] = fp(c);

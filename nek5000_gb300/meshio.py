@@ -8,8 +8,9 @@ library's host code).
 
 load_mesh returns the same keys as mesh.box_mesh (lx1, nel, n, D, g, bm1,
 glo_num, mask, mult, binv, vol, x, y, z, zgll, wgll) plus the file's
-boundary conditions.  Elements are straight-sided (the trilinear map of their
-corners, core/genxyz.f xyzlin); a mesh with curved sides is refused.
+boundary conditions.  Elements are mapped from their corners (core/genxyz.f
+xyzlin) or, with 'm' midside nodes, quadratically (xyzquad); other curved
+side types (arcs, spheres) are refused.
 """
 from __future__ import annotations
 
@@ -138,6 +139,29 @@ def xyzlin(nx: int, zgll, xc, yc, zc):
     return out
 
 
+def genxyz(nx: int, zgll, xc, yc, zc, curves=None):
+    """GLL coordinates (nel*nx^3 each): straight-sided elements by the
+    trilinear map, elements with 'm' midside nodes by the reference's
+    quadratic map (xyzquad); curves as read_re2 returns them."""
+    xc, yc, zc = (np.ascontiguousarray(a, dtype=np.float64) for a in (xc, yc, zc))
+    zgll = np.ascontiguousarray(zgll, dtype=np.float64)
+    ne = xc.shape[0]
+    out = [np.zeros(ne * nx ** 3) for _ in range(3)]
+    nc = 0 if curves is None else len(curves["elem"])
+    if nc:
+        elem = np.ascontiguousarray(curves["elem"], dtype=np.int32)
+        side = np.ascontiguousarray(curves["side"], dtype=np.int32)
+        cv = np.ascontiguousarray(curves["curve"], dtype=np.float64)
+        ctype = curves["ccurve"].encode("latin-1")
+    else:
+        elem = side = cv = None
+        ctype = None
+    _check(_lib().nekmesh_genxyz(C.byref(C.c_int(nx)), C.byref(C.c_int(ne)), _p(zgll), _p(xc),
+                                 _p(yc), _p(zc), C.byref(C.c_int64(nc)), _p(elem), _p(side),
+                                 _p(cv), ctype, *(_p(o) for o in out)))
+    return out
+
+
 # Points of each preprocessor face (1-based face number) of an element, as
 # (ix, iy, iz) selections on the (iz, iy, ix) element array.
 def _face_points(face: int, nx: int):
@@ -164,7 +188,7 @@ def _dsop(glo, u, op):
 def load_mesh(re2: str, N: int, co2: str | None = None, field: int = 0,
               dirichlet=DIRICHLET_VELOCITY, tol: float = 0.2) -> dict:
     """The operator data of a .re2 mesh at polynomial order N (lx1 = N+1):
-    GLL coordinates (xyzlin), geometric factors and mass, global numbering
+    GLL coordinates (genxyz), geometric factors and mass, global numbering
     (the .co2 file when given, else connectivity from the corners), the mask
     of boundary-condition section `field` (zero on faces whose type is in
     `dirichlet`, then multiplied across shared points as dsop '*'),
@@ -172,13 +196,11 @@ def load_mesh(re2: str, N: int, co2: str | None = None, field: int = 0,
     R = read_re2(re2)
     if R["ndim"] != 3:
         raise ValueError("only 3-D meshes are served")
-    if len(R["curves"]["elem"]):
-        raise ValueError("curved sides are not served (straight-sided elements only)")
     nx = N + 1
     ne = R["nelgt"]
     zg, wg = gll(nx)
     D = deriv_matrix(zg)
-    x, y, z = xyzlin(nx, zg, R["xc"], R["yc"], R["zc"])
+    x, y, z = genxyz(nx, zg, R["xc"], R["yc"], R["zc"], R["curves"])
     shape = (ne, nx, nx, nx)
     g, bm1, jac = geometry(x.reshape(shape), y.reshape(shape), z.reshape(shape), D, wg)
     cbc, bc = R["bcs"][field] if R["bcs"] else (None, None)

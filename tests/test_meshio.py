@@ -207,3 +207,74 @@ def test_face_repair_joins_a_displaced_corner(mio):
     xc[e, 6] += 0.3 / 3
     vertex, nv = mio.connect(xc, yc, zc)
     assert same_partition(vertex, lattice) and nv == lattice.max()
+
+
+# edges of an element (preprocessor numbering 1..12) as pairs of preprocessor corners
+PRE_EDGES = [(0, 1), (1, 2), (2, 3), (3, 0), (4, 5), (5, 6), (6, 7), (7, 4), (0, 4), (1, 5),
+             (2, 6), (3, 7)]
+
+
+def _quad_map(p):
+    """A map whose every component is linear plus univariate quadratics:
+    reproduced exactly by vertex + edge Gordon-Hall blending."""
+    x, y, z = p[..., 0], p[..., 1], p[..., 2]
+    return np.stack([x + 0.3 * y * y, y + 0.2 * z * z - 0.1 * x * x, z + 0.25 * x * x], -1)
+
+
+def _midside_mesh(kx, ky, kz, mapf, straight=False):
+    xc, yc, zc, lattice, bcs = box_elements(kx, ky, kz)
+    P = np.stack([xc, yc, zc], -1)  # (nel, 8, 3) box corners
+    curves = []
+    for e in range(P.shape[0]):
+        for k, (a, b) in enumerate(PRE_EDGES):
+            m = 0.5 * (P[e, a] + P[e, b])
+            node = m if straight else mapf(m)
+            curves.append((e + 1, k + 1, (node[0], node[1], node[2], 0.0, 0.0), "m"))
+    Q = P if straight else mapf(P)
+    return Q[..., 0], Q[..., 1], Q[..., 2], curves, bcs
+
+
+def _curves_dict(curves):
+    return dict(elem=np.array([c[0] for c in curves]), side=np.array([c[1] for c in curves]),
+                curve=np.array([c[2] for c in curves]), ccurve="".join(c[3] for c in curves))
+
+
+def test_midside_nodes_reproduce_quadratic_maps(mio):
+    """xyzquad + Gordon-Hall: on an element whose map is the composition of a
+    map with univariate-quadratic components with the trilinear box map, the
+    GLL points are that map's values; with midpoints of straight edges the
+    result is the trilinear map."""
+    from nek5000_gb300.mesh import gll
+    nx = 7
+    zg, _ = gll(nx)
+    xc, yc, zc, curves, _ = _midside_mesh(2, 2, 1, _quad_map)
+    x, y, z = mio.genxyz(nx, zg, xc, yc, zc, _curves_dict(curves))
+    # the box points at the GLL nodes (trilinear map of the box corners), mapped
+    bx, by, bz, _, _ = box_elements(2, 2, 1)
+    px, py, pz = mio.xyzlin(nx, zg, bx, by, bz)
+    want = _quad_map(np.stack([px, py, pz], -1))
+    got = np.stack([x, y, z], -1)
+    np.testing.assert_allclose(got, want, rtol=0, atol=4e-15)
+    # straight midpoints: the trilinear map
+    xc, yc, zc, curves, _ = _midside_mesh(2, 2, 1, None, straight=True)
+    got = np.stack(mio.genxyz(nx, zg, xc, yc, zc, _curves_dict(curves)), -1)
+    np.testing.assert_allclose(got, np.stack([px, py, pz], -1), rtol=0, atol=4e-16)
+
+
+def test_midside_mesh_loads_continuous(mio, tmp_path):
+    """A .re2 mesh with 'm' records on every edge: load_mesh gives positive
+    Jacobians and a numbering under which a smooth field is continuous."""
+    xc, yc, zc, curves, bcs = _midside_mesh(3, 2, 2, _quad_map)
+    p = tmp_path / "quad.re2"
+    write_re2(p, xc, yc, zc, bcs, curves=curves)
+    M = mio.load_mesh(p, N=6)
+    assert np.all(M["jac"] > 0)
+    f = np.cos(M["x"]) * np.sin(2 * M["y"]) + M["z"]
+    avg = mio._dsop(M["glo_num"], f, "+") * M["mult"]
+    np.testing.assert_allclose(avg, f, rtol=0, atol=1e-13)
+    # other curve types are refused
+    write_re2(p, xc, yc, zc, bcs, curves=[(1, 1, (0.5, 0, 0, 0, 0), "C")])
+    from nek5000_gb300 import _capi
+    with pytest.raises(_capi.NekGpuError) as ei:
+        mio.load_mesh(p, N=6)
+    assert ei.value.code == _capi.EINVAL
