@@ -96,16 +96,21 @@ int nekmesh_setvert3d(const int *nx, const int *nel, const int64_t *vertex, int6
 int nekmesh_xyzlin(const int *nx, const int *nel, const double *zgll, const double *xc,
                    const double *yc, const double *zc, double *x, double *y, double *z);
 
-/* ---- GLL coordinates with midside nodes (core/genxyz.f linquad :1235) ---- */
+/* ---- GLL coordinates of curved elements (core/genxyz.f genxyz :558) ----- */
 /* As nekmesh_xyzlin for elements without curved sides; an element with a
  * midside-node record (type 'm' on edge 1..12, the 3 node coordinates in
  * curve[5q .. 5q+2]) gets xyzquad's map (:1334-1380): its trilinear 3x3x3
  * nodes, the given midside nodes on their edges, the edges extended inward
  * by Gordon-Hall (gh_face_extend_3d, core/navier5.f:2502, vertices and
  * edges), then the quadratic interpolant at the GLL nodes (Fornberg weights,
- * fd_weights_full, core/fast3d.f:1294; tensr3, core/fasts.f:125).  Records of
- * any other curve type (arcs, spheres, ...) give NEKGPU_EINVAL; records
- * with a blank type are ignored.  nx = 2 ignores midside nodes, as linquad. */
+ * fd_weights_full, core/fast3d.f:1294; tensr3, core/fasts.f:125).  Then
+ * every circular-arc record (type 'C' on edge 1..8, signed radius in
+ * curve[5q]; positive with the centre on the element's side) bends its edge
+ * as arcsrf does (core/genxyz.f:2-101), the bend blended linearly across the
+ * element.  Records of any other curve type (spheres, ...) give
+ * NEKGPU_EINVAL, as does an arc shorter in radius than half its chord;
+ * records with a blank type are ignored.  nx = 2 ignores midside nodes, as
+ * linquad. */
 int nekmesh_genxyz(const int *nx, const int *nel, const double *zgll, const double *xc,
                    const double *yc, const double *zc, const int64_t *ncurve, const int *elem,
                    const int *side, const double *curve, const char *ccurve, double *x, double *y,

@@ -895,6 +895,62 @@ void gordon_hall_edges3(double* x) {
 // Midside node of each preprocessor edge (1..12) in the 3x3x3 array.
 constexpr int kEdgeMid[12] = {1, 5, 7, 3, 19, 23, 25, 21, 9, 11, 17, 15};
 
+// arcsrf (core/genxyz.f:2-101): edge isid (1..8, in a face of constant t)
+// of an element bent into a circular arc of the given radius in the x-y
+// plane (positive: centre on the element's side), the bend blended linearly
+// across the element.  xc, yc: the element's 8 corners (file order); x, y its
+// GLL coordinates (nx^3).  Returns false when the radius is shorter than half
+// the chord.
+bool arc_edge(int nx, const double* zg, const double* xc, const double* yc, int isid,
+              double radius, double* x, double* y) {
+  const int c1 = isid - 1, c2 = isid == 4 ? 0 : isid == 8 ? 4 : isid;
+  const double p1x = xc[c1], p1y = yc[c1], p2x = xc[c2], p2y = yc[c2];
+  const double gap = std::sqrt((p1x - p2x) * (p1x - p2x) + (p1y - p2y) * (p1y - p2y));
+  if (std::fabs(2.0 * radius) <= gap * 1.00001) return false;
+  const double xs = p2y - p1y, ys = p1x - p2x;
+  const double xys = std::sqrt(xs * xs + ys * ys);
+  const double dtheta = std::fabs(std::asin(0.5 * gap / radius));
+  const double p12x = (p1x + p2x) / 2.0, p12y = (p1y + p2y) / 2.0;
+  const double xcen = p12x - xs / xys * radius * std::cos(dtheta);
+  const double ycen = p12y - ys / xys * radius * std::cos(dtheta);
+  const double theta0 = std::atan2(p12y - ycen, p12x - xcen);
+  // the bend along the edge, in the edge's r (or s) order
+  const int side = (isid - 1) % 4 + 1;  // mod1(isid, 4)
+  std::vector<double> bx((size_t)nx), by((size_t)nx), h0((size_t)nx), h1((size_t)nx);
+  for (int i = 0; i < nx; ++i) {
+    h0[(size_t)i] = (1.0 - zg[i]) * 0.5;
+    h1[(size_t)i] = (1.0 + zg[i]) * 0.5;
+  }
+  for (int ix = 0; ix < nx; ++ix) {
+    const int it = side > 2 ? nx - 1 - ix : ix;
+    const double r = radius < 0.0 ? -zg[ix] : zg[ix];
+    bx[(size_t)it] = xcen + std::fabs(radius) * std::cos(theta0 + r * dtheta) -
+                     (h0[(size_t)ix] * p1x + h1[(size_t)ix] * p2x);
+    by[(size_t)it] = ycen + std::fabs(radius) * std::sin(theta0 + r * dtheta) -
+                     (h0[(size_t)ix] * p1y + h1[(size_t)ix] * p2y);
+  }
+  // tensor face of the edge (eface1: 3, 2, 4, 1): r- / r+ faces carry a bend
+  // along s, s- / s+ faces a bend along r; blended in t by the edge's level
+  const int tf = kTensorFace[side - 1];  // 1..4
+  const std::vector<double>& hz = (isid - 1) / 4 == 0 ? h0 : h1;
+  for (int k = 0; k < nx; ++k)
+    for (int j = 0; j < nx; ++j)
+      for (int i = 0; i < nx; ++i) {
+        const size_t q = (size_t)(i + nx * (j + nx * k));
+        if (tf <= 2) {  // addtnsr(x, H(:,1,tf), bend, H(:,3,izt))
+          const double hh = bx[(size_t)j] * hz[(size_t)k], hy = by[(size_t)j] * hz[(size_t)k];
+          const double hr = tf == 1 ? h0[(size_t)i] : h1[(size_t)i];
+          x[q] = x[q] + hh * hr;
+          y[q] = y[q] + hy * hr;
+        } else {  // addtnsr(x, bend, H(:,2,tf-2), H(:,3,izt))
+          const double hh = (tf == 3 ? h0[(size_t)j] : h1[(size_t)j]) * hz[(size_t)k];
+          x[q] = x[q] + hh * bx[(size_t)i];
+          y[q] = y[q] + hh * by[(size_t)i];
+        }
+      }
+  return true;
+}
+
 }  // namespace
 
 extern "C" {
@@ -911,13 +967,19 @@ int nekmesh_genxyz(const int* nx_, const int* nel_, const double* zg, const doub
   // midside nodes per element (edges 1..12); any other curve type is refused
   std::vector<int64_t> first((size_t)nel, -1);
   std::vector<std::array<int, 12>> mid;
+  std::vector<int64_t> arcs;  // records of circular-arc edges
   for (int64_t q = 0; q < nc; ++q) {
     const int64_t e = elem[q] - 1;
     if (e < 0 || e >= nel) return fail(NEKGPU_EINVAL, "genxyz: curve record names no element");
     if (ccurve[q] == ' ' || ccurve[q] == '\0') continue;
+    if (ccurve[q] == 'C') {
+      if (side[q] < 1 || side[q] > 12) return fail(NEKGPU_EINVAL, "genxyz: arc on no edge");
+      if (side[q] <= 8) arcs.push_back(q);  // the reference bends edges 1..8 only
+      continue;
+    }
     if (ccurve[q] != 'm')
       return fail(NEKGPU_EINVAL, std::string("genxyz: curved side type '") + ccurve[q] +
-                                     "' not served (only 'm' midside nodes)");
+                                     "' not served (midside nodes 'm' and arcs 'C' are)");
     if (side[q] < 1 || side[q] > 12) return fail(NEKGPU_EINVAL, "genxyz: midside node on no edge");
     if (first[(size_t)e] < 0) {
       first[(size_t)e] = (int64_t)mid.size();
@@ -929,7 +991,8 @@ int nekmesh_genxyz(const int* nx_, const int* nel_, const double* zg, const doub
   }
   // straight-sided elements (and every element when nx = 2, as linquad)
   int rc = nekmesh_xyzlin(nx_, nel_, zg, xc, yc, zc, x, y, z);
-  if (rc || nx == 2) return rc;
+  if (rc) return rc;
+  if (nx == 2 && arcs.empty()) return NEKGPU_OK;
   // quadratic elements (xyzquad, core/genxyz.f:1334): the trilinear 3x3x3
   // map, the file's midside nodes on their edges, edges extended inward by
   // Gordon-Hall, then the quadratic interpolant at the GLL nodes
@@ -939,7 +1002,7 @@ int nekmesh_genxyz(const int* nx_, const int* nel_, const double* zg, const doub
   const double* src[3] = {xc, yc, zc};
   double* dst[3] = {x, y, z};
   const double wl[6] = {1.0, 0.0, 0.5, 0.5, 0.0, 1.0};  // (1-z)/2, (1+z)/2 at -1, 0, 1
-  for (int64_t e = 0; e < nel; ++e) {
+  for (int64_t e = 0; e < nel && nx > 2; ++e) {
     if (first[(size_t)e] < 0) continue;
     const auto& m = mid[(size_t)first[(size_t)e]];
     for (int d = 0; d < 3; ++d) {
@@ -951,6 +1014,18 @@ int nekmesh_genxyz(const int* nx_, const int* nel_, const double* zg, const doub
       gordon_hall_edges3(q3);
       tensor3(dst[d] + nxyz * e, nx, q3, 3, wq.data());
     }
+  }
+  // circular-arc edges, added after the linear / quadratic map, element by
+  // element and edge by edge (genxyz's order)
+  std::stable_sort(arcs.begin(), arcs.end(), [&](int64_t a, int64_t b) {
+    return elem[a] != elem[b] ? elem[a] < elem[b] : side[a] < side[b];
+  });
+  for (const int64_t q : arcs) {
+    const int64_t e = elem[q] - 1;
+    if (!arc_edge(nx, zg, xc + 8 * e, yc + 8 * e, side[q], curve[5 * (size_t)q], x + nxyz * e,
+                  y + nxyz * e))
+      return fail(NEKGPU_EINVAL, "genxyz: arc radius shorter than half its chord (element " +
+                                     std::to_string(e + 1) + ", edge " + std::to_string(side[q]) + ")");
   }
   return NEKGPU_OK;
 }

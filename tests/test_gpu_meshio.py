@@ -21,15 +21,21 @@ def _mesh(tmp_path, case):
                                         perm=np.random.default_rng(21).permutation(36))
         xc, yc, zc = rotate_elements(xc, yc, zc, seed=21)
         bcs = []
-    else:  # periodic in y, walls on the x and z faces
+    elif case == "periodic":  # periodic in y, walls on the x and z faces
         xc, yc, zc, _, bcs = box_elements(4, 3, 3, periodic_y=True, jitter=0.2, seed=22,
                                           perm=np.random.default_rng(22).permutation(36))
+    else:  # an annular ring with circular-arc edges, walls inside and outside
+        from test_meshio import _annulus
+        xc, yc, zc, curves, bcs = _annulus(nt=12, nr=3, nz=2)
+        p = tmp_path / "annulus.re2"
+        write_re2(p, xc, yc, zc, bcs, curves=curves)
+        return meshio.load_mesh(p, N=7)
     p = tmp_path / f"{case}.re2"
     write_re2(p, xc, yc, zc, bcs)
     return meshio.load_mesh(p, N=7)
 
 
-@pytest.mark.parametrize("case", ["rotated", "periodic"])
+@pytest.mark.parametrize("case", ["rotated", "periodic", "annulus"])
 def test_re2_mesh_solves_match_the_oracle(gpu_lib, oracle, tmp_path, case):
     torch = pytest.importorskip("torch")
     M = _mesh(tmp_path, case)

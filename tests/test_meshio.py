@@ -273,8 +273,66 @@ def test_midside_mesh_loads_continuous(mio, tmp_path):
     avg = mio._dsop(M["glo_num"], f, "+") * M["mult"]
     np.testing.assert_allclose(avg, f, rtol=0, atol=1e-13)
     # other curve types are refused
-    write_re2(p, xc, yc, zc, bcs, curves=[(1, 1, (0.5, 0, 0, 0, 0), "C")])
+    write_re2(p, xc, yc, zc, bcs, curves=[(1, 1, (0.5, 0, 0, 0, 0), "s")])
     from nek5000_gb300 import _capi
     with pytest.raises(_capi.NekGpuError) as ei:
         mio.load_mesh(p, N=6)
     assert ei.value.code == _capi.EINVAL
+
+
+def _annulus(nt=8, nr=2, nz=1, ri=0.5, ro=1.0, h=0.5, arcs=True):
+    """Elements of an annular ring (nt around, nr across, nz high): corners in
+    file order (bottom counter-clockwise seen from +z, then top), the
+    circular-arc records of their inner and outer edges (positive radius where
+    the centre is on the element's side), walls on every outside face."""
+    xc, yc, zc, curves, bcs = [], [], [], [], []
+    e = 0
+    for kz in range(nz):
+        for jt in range(nt):
+            t0, t1 = 2 * np.pi * jt / nt, 2 * np.pi * (jt + 1) / nt
+            for ir in range(nr):
+                r0, r1 = ri + (ro - ri) * ir / nr, ri + (ro - ri) * (ir + 1) / nr
+                quad = [(r0, t0), (r1, t0), (r1, t1), (r0, t1)]
+                xs = [r * np.cos(t) for r, t in quad]
+                ys = [r * np.sin(t) for r, t in quad]
+                xc.append(xs + xs)
+                yc.append(ys + ys)
+                zc.append([h * kz / nz] * 4 + [h * (kz + 1) / nz] * 4)
+                e += 1
+                if arcs:
+                    for edge, rad in ((2, r1), (4, -r0), (6, r1), (8, -r0)):
+                        curves.append((e, edge, (rad, 0.0, 0.0, 0.0, 0.0), "C"))
+                if ir == 0:
+                    bcs.append((e, 4, (0.0,) * 5, "W  "))
+                if ir == nr - 1:
+                    bcs.append((e, 2, (0.0,) * 5, "W  "))
+                if kz == 0:
+                    bcs.append((e, 5, (0.0,) * 5, "W  "))
+                if kz == nz - 1:
+                    bcs.append((e, 6, (0.0,) * 5, "W  "))
+    return np.array(xc), np.array(yc), np.array(zc), curves, bcs
+
+
+def test_arc_edges_make_an_exact_annulus(mio, tmp_path):
+    """Circular-arc edges (arcsrf): the GLL points of the bent edges lie on
+    their circles, the numbering is continuous around the ring, and the mesh
+    volume converges to the annulus' (a polygonal ring misses it by 2.6%)."""
+    ri, ro, h = 0.5, 1.0, 0.5
+    exact = np.pi * (ro * ro - ri * ri) * h
+    vols = {}
+    for arcs in (True, False):
+        xc, yc, zc, curves, bcs = _annulus(ri=ri, ro=ro, h=h, arcs=arcs)
+        p = tmp_path / f"ring{arcs}.re2"
+        write_re2(p, xc, yc, zc, bcs, curves=curves)
+        M = mio.load_mesh(p, N=7)
+        assert np.all(M["jac"] > 0)
+        vols[arcs] = M["vol"]
+        f = M["x"] * M["y"] + np.cos(M["z"])
+        avg = mio._dsop(M["glo_num"], f, "+") * M["mult"]
+        np.testing.assert_allclose(avg, f, rtol=0, atol=1e-13)
+        if arcs:
+            rad = np.hypot(M["x"], M["y"]).reshape(M["nel"], 8, 8, 8)
+            np.testing.assert_allclose(rad[1::2, :, :, -1], ro, rtol=0, atol=1e-14)  # outer edges
+            np.testing.assert_allclose(rad[0::2, :, :, 0], ri, rtol=0, atol=1e-14)   # inner edges
+    assert abs(vols[True] - exact) <= 1e-8 * exact, (vols[True], exact)
+    assert abs(vols[False] - exact) > 1e-2 * exact
