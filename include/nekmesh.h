@@ -90,6 +90,13 @@ int nekmesh_connect(const int *nel, const int *ndim, const double *xc, const dou
 int nekmesh_setvert3d(const int *nx, const int *nel, const int64_t *vertex, int64_t *glo_num,
                       int64_t *ngv);
 
+/* Single-element periodicity (check_p_bc, core/navier8.f:2571-2620): an
+ * element whose two opposite faces both have type "p  " in cbc (preprocessor
+ * face order, 6 per element) gets, point by point across the element, the
+ * smaller of the two faces' ids on both; set_vert applies it after
+ * setvert3d. */
+int nekmesh_check_p_bc(const int *nx, const int *nel, const char *cbc, int64_t *glo_num);
+
 /* ---- GLL coordinates of straight-sided elements (core/genxyz.f xyzlin) ---- */
 /* x, y, z (nx^3 per element) by the trilinear map of the corners xc, yc, zc
  * (file order) at the GLL nodes zgll[0..nx-1] (xyzlin :1269-1320). */

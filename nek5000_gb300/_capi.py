@@ -49,6 +49,7 @@ SIGNATURES = {
     "nekmesh_co2_write": [C.c_char_p, _IP, _IP, _IP, _P],
     "nekmesh_connect": [_IP, _IP, _P, _P, _P, _P, _P, _DP, _P, _I64P],
     "nekmesh_setvert3d": [_IP, _IP, _P, _P, _I64P],
+    "nekmesh_check_p_bc": [_IP, _IP, C.c_char_p, _P],
     "nekmesh_xyzlin": [_IP, _IP, _P, _P, _P, _P, _P, _P, _P],
     "nekmesh_genxyz": [_IP, _IP, _P, _P, _P, _P, _I64P, _P, _P, _P, C.c_char_p, _P, _P, _P],
     # solve path (include/nekgpu.h)

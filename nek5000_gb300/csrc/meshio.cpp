@@ -1030,6 +1030,33 @@ int nekmesh_genxyz(const int* nx_, const int* nel_, const double* zg, const doub
   return NEKGPU_OK;
 }
 
+int nekmesh_check_p_bc(const int* nx_, const int* nel_, const char* cbc, int64_t* glo_num) {
+  if (!nx_ || !nel_ || !cbc || !glo_num || *nx_ < 2 || *nel_ <= 0)
+    return fail(NEKGPU_EINVAL, "check_p_bc: bad arguments");
+  const int64_t nx = *nx_, nel = *nel_, nxyz = nx * nx * nx;
+  for (int64_t e = 0; e < nel; ++e)
+    for (int dir = 0; dir < 3; ++dir) {  // tensor faces 2 dir and 2 dir + 1
+      const char* a = cbc + 3 * (6 * e + kPreFace[2 * dir] - 1);
+      const char* b = cbc + 3 * (6 * e + kPreFace[2 * dir + 1] - 1);
+      if (std::memcmp(a, "p  ", 3) != 0 || std::memcmp(b, "p  ", 3) != 0) continue;
+      int64_t* g = glo_num + nxyz * e;
+      const int64_t st = dir == 0 ? 1 : dir == 1 ? nx : nx * nx;  // step across the element
+      for (int64_t v = 0; v < nx; ++v)
+        for (int64_t u = 0; u < nx; ++u) {
+          // the point (u, v) of the face pair: the other two indices
+          int64_t i0;
+          if (dir == 0) i0 = nx * (u + nx * v);
+          else if (dir == 1) i0 = u + nx * nx * v;
+          else i0 = u + nx * v;
+          const int64_t lo = i0, hi = i0 + (nx - 1) * st;
+          const int64_t m = std::min(g[lo], g[hi]);
+          g[lo] = m;
+          g[hi] = m;
+        }
+    }
+  return NEKGPU_OK;
+}
+
 int nekmesh_xyzlin(const int* nx_, const int* nel_, const double* zg, const double* xc,
                    const double* yc, const double* zc, double* x, double* y, double* z) {
   if (!nx_ || !nel_ || !zg || !xc || !yc || !zc || !x || !y || !z || *nx_ < 2 || *nel_ <= 0)

@@ -129,6 +129,15 @@ def setvert3d(nx: int, vertex):
     return glo, ngv.value
 
 
+def check_p_bc(nx: int, cbc, glo):
+    """Single-element periodicity ('p  ' on two opposite faces of an element:
+    core/navier8.f check_p_bc), applied to glo in place."""
+    cbuf = C.create_string_buffer("".join(np.asarray(cbc).reshape(-1)).encode("latin-1"))
+    _check(_lib().nekmesh_check_p_bc(C.byref(C.c_int(nx)), C.byref(C.c_int(len(cbc))), cbuf,
+                                     _p(glo)))
+    return glo
+
+
 def xyzlin(nx: int, zgll, xc, yc, zc):
     """GLL coordinates (nel*nx^3 each) of straight-sided elements."""
     xc, yc, zc = (np.ascontiguousarray(a, dtype=np.float64) for a in (xc, yc, zc))
@@ -214,6 +223,8 @@ def load_mesh(re2: str, N: int, co2: str | None = None, field: int = 0,
     else:
         vertex, _ = connect(R["xc"], R["yc"], R["zc"], cbc, bc, tol)
     glo, ngv = setvert3d(nx, vertex)
+    if cbc is not None:
+        check_p_bc(nx, cbc, glo)
     n = ne * nx ** 3
     mask = np.ones(shape)
     if cbc is not None:

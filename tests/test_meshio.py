@@ -336,3 +336,24 @@ def test_arc_edges_make_an_exact_annulus(mio, tmp_path):
             np.testing.assert_allclose(rad[0::2, :, :, 0], ri, rtol=0, atol=1e-14)   # inner edges
     assert abs(vols[True] - exact) <= 1e-8 * exact, (vols[True], exact)
     assert abs(vols[False] - exact) > 1e-2 * exact
+
+
+def test_single_element_periodicity(mio, tmp_path):
+    """'p  ' on both z faces of a one-element-high box (check_p_bc): the
+    points of each element's z faces share ids, so a z-periodic field stays
+    continuous and those points count twice as often."""
+    xc, yc, zc, lattice, bcs = box_elements(3, 2, 1, jitter=0.0)
+    bcs = [b for b in bcs if b[1] not in (5, 6)]
+    for e in range(6):
+        bcs += [(e + 1, 5, (0.0,) * 5, "p  "), (e + 1, 6, (0.0,) * 5, "p  ")]
+    p = tmp_path / "p.re2"
+    write_re2(p, xc, yc, zc, bcs)
+    M = mio.load_mesh(p, N=4)
+    nx = 5
+    g = M["glo_num"].reshape(6, nx, nx, nx)
+    assert np.array_equal(g[:, 0], g[:, -1])
+    f = np.cos(2 * np.pi * M["z"]) + M["x"] * M["y"]   # periodic in z with period 1
+    avg = mio._dsop(M["glo_num"], f, "+") * M["mult"]
+    np.testing.assert_allclose(avg, f, rtol=0, atol=1e-13)
+    cnt = np.rint(1 / M["mult"]).reshape(6, nx, nx, nx)
+    assert np.all(cnt[:, 0, 1:-1, 1:-1] == 2) and np.all(cnt[:, 1:-1, 1:-1, 1:-1] == 1)
