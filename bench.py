@@ -61,14 +61,15 @@ def parse():
                          "0 restarted FP32 PCG per outer step")
     ap.add_argument("--workload", default="helmholtz",
                     choices=["helmholtz", "poisson-n9", "batch", "axhelm-sweep", "hsolve",
-                             "adjoint", "velocity3", "ingest"],
+                             "adjoint", "velocity3", "ingest", "pressure"],
                     help="helmholtz: E=32^3 N=7 (default); poisson-n9: E=24^3 N=9 Poisson; "
                          "batch: 3 velocity solves + 61 uneven Poisson problems in one batch; "
                          "axhelm-sweep: in-solve operator bandwidth at N=5,7,9, E=32^3; "
                          "hsolve: a sequence of solves with projection onto previous solutions; "
                          "adjoint: dJ/dh1 through the adjoint solve, E=16^3 N=7; "
                          "velocity3: 3 velocity components in one fused mixed solve; "
-                         "ingest: .re2 mesh ingestion on the host")
+                         "ingest: .re2 mesh ingestion on the host; "
+                         "pressure: the pressure solve's GMRES")
     ap.add_argument("--batch-problems", type=int, default=61)
     ap.add_argument("--fp64-shape", default=None,
                     help="pin the FP64 operator launch shape 'kind,epb' instead of autotuning")
@@ -83,6 +84,8 @@ def parse():
             args.k = 24
         if args.N == 7:
             args.N = 9
+    if args.workload == "pressure" and args.k == 32:
+        args.k = 16  # restarted GMRES needs several times cggo's iterations
     if args.inner_tol is None:  # the library's defaults for the mode
         args.inner_tol = 1e-2 if args.mixed_mode == 1 else 1e-5
     return args
@@ -887,6 +890,74 @@ def run_velocity3(args):
     lib.close()
 
 
+def run_pressure(args):
+    """The pressure solve's Krylov method (hmh_gmres, restart 30) on the
+    E=k^3, N Poisson problem (all-Dirichlet box, h1 = 1, h2 = 0, seed 0), to
+    1e-10 of the initial residual norm, beside FP64 Jacobi-PCG (cggo) on the
+    same system; both with the Jacobi preconditioner."""
+    import torch
+    ws, rank, local, pg = dist_setup(args.gpus)
+    torch.cuda.set_device(local)
+    from nek5000_gb300 import NekGpu
+    from nek5000_gb300 import build as nb
+    nb.build()
+    M = workload(args.k, args.N, "poisson")
+    n = M["n"]
+    lib = NekGpu(local)
+    lib.setup(M["lx1"], M["nel"], M["D"], M["g"], M["bm1"], M["glo_num"])
+    dev = lambda a: torch.tensor(a, device=f"cuda:{local}")
+    f, h1, h2 = dev(M["f"]), dev(M["h1"]), dev(M["h2"])
+    mask, mult, binv = dev(M["mask"]), dev(M["mult"]), dev(M["binv"])
+
+    def gmres():
+        x = f.clone()
+        return lib.hmh_gmres(x, h1, h2, mult, mask, -args.tol, maxit=10 ** 5, kmax=30)
+
+    def cg():
+        x = torch.zeros(n, dtype=torch.float64, device=f"cuda:{local}")
+        return lib.cggo(x, f, h1, h2, mask, mult, 1, -args.tol, 10 ** 6, 1, binv, maxcg=10 ** 6)
+
+    out = {}
+    for name, fn in (("gmres", gmres), ("cggo", cg)):
+        for _ in range(args.warmup):
+            r = fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        with Clocks(local) as ck:
+            for _ in range(args.steps):
+                r = fn()
+            torch.cuda.synchronize()
+        T = (time.perf_counter() - t0) / args.steps
+        out[name] = dict(iterations=r[0], ms_per_solve=1e3 * T,
+                         dof_iters_per_s=n * r[0] / T, clocks=ck.summary())
+    line = {"metric": f"pressure-solve GMRES (hmh_gmres, restart 30, Jacobi) DOF-iters/s, "
+                      f"E={args.k}^3 N={args.N} Poisson",
+            "value": out["gmres"]["dof_iters_per_s"], "unit": "DOF-iters/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": out["gmres"]["ms_per_solve"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": workload_name(argparse.Namespace(workload="poisson-n9", k=args.k,
+                                                                    N=args.N)),
+                       "n_points": n, "tol": f"{args.tol:g} x initial rnorm"},
+            "gmres": out["gmres"], "cggo_same_system": out["cggo"],
+            "clocks": out["gmres"]["clocks"]}
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        from oracle import nekref
+        nth = os.cpu_count() or 1
+        ops = nekref.Ops(M["lx1"], M["nel"], M["D"], M["g"], M["bm1"], M["glo_num"], nth)
+        t0 = time.perf_counter()
+        _, itc, _, _ = ops.gmres(M["f"], M["h1"], M["h2"], M["mult"], M["mask"], -args.tol,
+                                 maxit=20, m=30)
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": n * itc / dt, "unit": "DOF-iters/s", "cores": nth,
+                                "kind": "port",
+                                "sample": f"{itc} GMRES iterations of the full problem ({dt:.1f} s),"
+                                          " the oracle's hmh_gmres restatement"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    lib.close()
+
+
 def write_box_re2(path, k, jitter=0.2, seed=6):
     """A #v002 .re2 file of a k^3 box of straight-sided hexahedra on the unit
     cube (interior vertices moved by up to jitter * h, elements in a seeded
@@ -1011,6 +1082,8 @@ def main():
         run_velocity3(args)
     elif args.workload == "ingest":
         run_ingest(args)
+    elif args.workload == "pressure":
+        run_pressure(args)
     else:
         run_gpu(args)
 

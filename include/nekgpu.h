@@ -90,6 +90,27 @@ int nekgpu_setup(const int64_t *handle, const int *lx1, const int *nel, const do
                  const double *g1, const double *g2, const double *g3, const double *g4,
                  const double *g5, const double *g6, const double *bm1, const int64_t *glo_num);
 
+/* The pressure solve's Krylov method: hmh_gmres (core/gmres.f:304-560),
+ * right-preconditioned restarted GMRES with restart length *kmax (the
+ * reference's lgmres, 30; at most NEKGPU_GMRES_MAX) on
+ * A x = mask * dssum(axhelm(x, h1, h2)) (gmres.f:284-302), inner products
+ * weighted by wt (vmult), classical Gram-Schmidt, Givens rotations.  res
+ * (device array): in the right-hand side, out the solution.  Stops when
+ * rnorm = |gamma| / sqrt(volvm1) < *tol (absolute; *tol < 0: relative to the
+ * initial rnorm, as param(21) < 0) or after *maxit iterations (status
+ * NEKGPU_ENOTCONV above the tolerance).  *null_space != 0 removes the mean
+ * of every preconditioned vector and of the solution (ortho,
+ * core/navier1.f:223-256), for a pure-Neumann pressure (ifvcor).  The
+ * preconditioner is the Jacobi diagonal (setprec), standing in for the
+ * reference's Schwarz-multigrid / FDM + coarse-grid one: iteration counts are
+ * this method's; the solution is the same system's to the tolerance.
+ * Outputs: iterations, initial and final rnorm. */
+#define NEKGPU_GMRES_MAX 50
+int nekgpu_hmh_gmres_dev(const int64_t *handle, double *res, const double *h1, const double *h2,
+                         const double *wt, const double *mask, const double *tol,
+                         const int *maxit, const int *kmax, const int *null_space, int *niter,
+                         double *div0, double *rnorm);
+
 /* As nekgpu_setup, with the geometric factors and the mass computed on the
  * device from the GLL coordinates xm1, ym1, zm1 (host arrays, lx1^3 nel
  * each) and the GLL weights wxm1 (lx1): xyzrst (core/coef.f:879-926), glmapm1

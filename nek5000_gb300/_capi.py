@@ -22,6 +22,7 @@ MAX_LX1 = 12
 NOALLOC_MAX_POINTS = 4194304
 PROJ_SPACES, PROJ_MAX, PROJ_DEFAULT = 16, 16, 8
 MULTI_MAX = 3
+GMRES_MAX = 50
 
 STATUS_NAMES = {
     0: "NEKGPU_OK", -1: "NEKGPU_EINVAL", -2: "NEKGPU_EHANDLE", -3: "NEKGPU_ECUDA",
@@ -58,6 +59,7 @@ SIGNATURES = {
     "nekgpu_last_error": [_I64P, C.c_char_p, _IP],
     "nekgpu_set_option": [_I64P, _IP, _IP],
     "nekgpu_setup": [_I64P, _IP, _IP, _P, _P, _P, _P, _P, _P, _P, _P, _P],
+    "nekgpu_hmh_gmres_dev": [_I64P, _P, _P, _P, _P, _P, _DP, _IP, _IP, _IP, _IP, _DP, _DP],
     "nekgpu_setup_xyz": [_I64P, _IP, _IP, _P, _P, _P, _P, _P, _P],
     "nekgpu_geom_update_dev": [_I64P, _P, _P, _P, _P],
     "nekgpu_geometry": [_I64P, _P, _P, _P, _P, _P, _P, _P],

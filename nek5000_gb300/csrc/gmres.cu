@@ -1,0 +1,381 @@
+// gmres.cu -- the pressure solve's Krylov method on the device: hmh_gmres
+// (core/gmres.f:304-560), right-preconditioned restarted GMRES on
+// ax() = mask * dssum(axhelm(x)) (gmres.f:284-302) with weights wt (vmult).
+//
+// Per inner iteration: z_j = M v_j (and the mean removed when the operator
+// has a null space, ortho, core/navier1.f:223-256), w = A z_j, the j
+// weighted dot products (w, v_i) in one pass per eight vectors, w -= sum
+// h_ij v_i point by point in i order fused with (w, w), then the Givens
+// rotation, the residual estimate and v_{j+1} = w / alpha.  Pointwise
+// arithmetic is rounded as the reference's (no fused multiply-adds); the
+// dot products are block sums added on the host in block order.
+//
+// The reference preconditions with hybrid Schwarz multigrid or FDM local
+// solves plus an XXT / AMG coarse solve (gmres.f:447-470); here M is the
+// Jacobi diagonal of setprec, the one preconditioner this library has, so
+// the iteration counts are this method's, not the reference's; the solution
+// is the same linear system's to the tolerance.
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "impl.cuh"
+
+namespace nekgpu {
+namespace {
+
+constexpr int kT = 256;
+constexpr int kDots = 8;  // weighted dot products per pass
+
+inline int nblocks(int64_t n) {
+  return (int)std::min<int64_t>(std::max<int64_t>((n + kT - 1) / kT, 1), 152 * 6);
+}
+
+__device__ __forceinline__ double block_reduce(double v, double* red) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0)
+    for (int q = 0; q < kT / 32; ++q) s += red[q];
+  return s;
+}
+
+// partial[blk] = sum a b wt over the block's points (glsc3 / vlsc3 terms)
+__global__ void __launch_bounds__(kT) wdot_kernel(const double* __restrict__ a,
+                                                  const double* __restrict__ b,
+                                                  const double* __restrict__ wt, int64_t n,
+                                                  double* __restrict__ partial) {
+  __shared__ double red[kT / 32];
+  double s = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)kT + threadIdx.x; i < n; i += (int64_t)gridDim.x * kT)
+    s += __dmul_rn(__dmul_rn(a[i], b[i]), wt[i]);
+  s = block_reduce(s, red);
+  if (threadIdx.x == 0) partial[blockIdx.x] = s;
+}
+
+// partial[blk * kDots + k] = sum w v_k wt, k < cnt, v_k = V + k n
+__global__ void __launch_bounds__(kT) mdot_kernel(const double* __restrict__ w,
+                                                  const double* __restrict__ V, int cnt,
+                                                  const double* __restrict__ wt, int64_t n,
+                                                  double* __restrict__ partial) {
+  __shared__ double red[kT / 32];
+  double acc[kDots];
+#pragma unroll
+  for (int k = 0; k < kDots; ++k) acc[k] = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)kT + threadIdx.x; i < n; i += (int64_t)gridDim.x * kT) {
+    const double ww = w[i], t = wt[i];
+#pragma unroll
+    for (int k = 0; k < kDots; ++k)
+      if (k < cnt) acc[k] += __dmul_rn(__dmul_rn(ww, V[(int64_t)k * n + i]), t);
+  }
+  for (int k = 0; k < cnt; ++k) {
+    const double s = block_reduce(acc[k], red);
+    if (threadIdx.x == 0) partial[(int64_t)blockIdx.x * kDots + k] = s;
+  }
+}
+
+// w = w + (-h_i) v_i for i < j in order (add2s2), then partial = sum w w wt
+__global__ void __launch_bounds__(kT) msub_kernel(double* __restrict__ w,
+                                                  const double* __restrict__ V, int j,
+                                                  const double* __restrict__ h,
+                                                  const double* __restrict__ wt, int64_t n,
+                                                  double* __restrict__ partial) {
+  __shared__ double red[kT / 32];
+  double s = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)kT + threadIdx.x; i < n; i += (int64_t)gridDim.x * kT) {
+    double v = w[i];
+    for (int k = 0; k < j; ++k) v = __dadd_rn(v, __dmul_rn(-h[k], V[(int64_t)k * n + i]));
+    w[i] = v;
+    s += __dmul_rn(__dmul_rn(v, v), wt[i]);
+  }
+  s = block_reduce(s, red);
+  if (threadIdx.x == 0) partial[blockIdx.x] = s;
+}
+
+// x = x + c_i z_i for i < j in order (add2s2)
+__global__ void xupd_kernel(double* __restrict__ x, const double* __restrict__ Z, int j,
+                            const double* __restrict__ c, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    double v = x[i];
+    for (int k = 0; k < j; ++k) v = __dadd_rn(v, __dmul_rn(c[k], Z[(int64_t)k * n + i]));
+    x[i] = v;
+  }
+}
+
+// z = d (1 v) (the preconditioner on mu v); partial = sum z (for ortho)
+__global__ void __launch_bounds__(kT) prec_kernel(double* __restrict__ z,
+                                                  const double* __restrict__ d,
+                                                  const double* __restrict__ v, int64_t n,
+                                                  double* __restrict__ partial) {
+  __shared__ double red[kT / 32];
+  double s = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)kT + threadIdx.x; i < n; i += (int64_t)gridDim.x * kT) {
+    const double zz = __dmul_rn(d[i], v[i]);
+    z[i] = zz;
+    s += zz;
+  }
+  s = block_reduce(s, red);
+  if (threadIdx.x == 0 && partial) partial[blockIdx.x] = s;
+}
+
+__global__ void sum_kernel(const double* __restrict__ a, int64_t n, double* __restrict__ partial) {
+  __shared__ double red[kT / 32];
+  double s = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)kT + threadIdx.x; i < n; i += (int64_t)gridDim.x * kT)
+    s += a[i];
+  s = block_reduce(s, red);
+  if (threadIdx.x == 0) partial[blockIdx.x] = s;
+}
+
+__global__ void cadd_kernel(double* __restrict__ a, double c, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    a[i] = __dadd_rn(a[i], c);
+}
+
+__global__ void scale_kernel(double* __restrict__ dst, const double* __restrict__ src, double c,
+                             int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    dst[i] = __dmul_rn(src[i], c);
+}
+
+__global__ void mask_kernel(double* __restrict__ w, const double* __restrict__ m, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    w[i] = __dmul_rn(w[i], m[i]);
+}
+
+// r = res + (-1) w (copy + add2s2)
+__global__ void resid_kernel(double* __restrict__ r, const double* __restrict__ res,
+                             const double* __restrict__ w, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    r[i] = __dadd_rn(res[i], -w[i]);
+}
+
+struct Gm {
+  Handle& h;
+  cudaStream_t s;
+  int64_t n;
+  int nb;
+  std::vector<double> host;
+
+  // the block partials (nb * per) summed in block order
+  int sums(int per, int cnt, double* out) {
+    host.resize((size_t)nb * per);
+    cudaMemcpyAsync(host.data(), h.red.ptr, host.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                    s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) {
+      set_error(h, std::string("gmres: ") + cudaGetErrorString(cudaGetLastError()));
+      return -3;
+    }
+    for (int k = 0; k < cnt; ++k) {
+      double t = 0.0;
+      for (int b = 0; b < nb; ++b) t += host[(size_t)b * per + k];
+      out[k] = t;
+    }
+    return 0;
+  }
+};
+
+}  // namespace
+
+// hmh_gmres with the Jacobi preconditioner; res: in the right-hand side, out
+// the solution.  Returns 0, -3 (CUDA), -4 (allocation), -5 (iteration cap
+// reached above the tolerance).
+int gmres_solve(Handle& h, double* res, const double* h1, const double* h2, const double* wt,
+                const double* mask, double tol, int maxit, int m, bool null_space, int* niter,
+                double* div0_out, double* rnorm_out) {
+  Mesh& msh = h.mesh;
+  const int64_t n = msh.n;
+  cudaStream_t s = h.stream;
+  Gm g{h, s, n, nblocks(n), {}};
+  const int nb = g.nb;
+  if (h.gm_V.ensure((size_t)m * n) || h.gm_Z.ensure((size_t)m * n) || h.gm_r.ensure(n) ||
+      h.gm_w.ensure(n) || h.gm_x.ensure(n) || h.gm_d.ensure(n) || h.gm_c.ensure(m + 1) ||
+      h.red.ensure((size_t)nb * kDots)) {
+    set_error(h, "gmres: device allocation failed");
+    return -4;
+  }
+  Coef<double> c;
+  if (detect_coef<double>(h, h1, h2, n, c)) {
+    set_error(h, "gmres: coefficient scan failed");
+    return -3;
+  }
+  if (setprec_f64(h, h.gm_d.ptr, c)) {
+    set_error(h, "gmres: setprec failed");
+    return -3;
+  }
+  double *V = h.gm_V.ptr, *Z = h.gm_Z.ptr, *r = h.gm_r.ptr, *w = h.gm_w.ptr, *x = h.gm_x.ptr;
+  const double* d = h.gm_d.ptr;
+  auto apply_A = [&](double* out, const double* in) -> int {
+    cudaError_t e = h.exact ? launch_axhelm<double, true>(msh, msh.f64, out, in, c, s)
+                            : launch_axhelm<double, false>(msh, msh.f64, out, in, c, s);
+    if (e != cudaSuccess) {
+      set_error(h, std::string("gmres: operator launch: ") + cudaGetErrorString(e));
+      return -3;
+    }
+    gs_op<double>(msh.gs, out, 0, s);
+    count_launch();
+    mask_kernel<<<nb, kT, 0, s>>>(out, mask, n);
+    return 0;
+  };
+  auto ortho = [&](double* z, const double* partial_done) -> int {
+    if (!null_space) return 0;
+    if (!partial_done) {
+      count_launch();
+      sum_kernel<<<nb, kT, 0, s>>>(z, n, h.red.ptr);
+    }
+    double sum = 0.0;
+    if (g.sums(1, 1, &sum)) return -3;
+    count_launch();
+    cadd_kernel<<<nb, kT, 0, s>>>(z, -(sum / (double)n), n);
+    return 0;
+  };
+  cudaMemsetAsync(x, 0, n * sizeof(double), s);
+  const double norm_fac = 1.0 / std::sqrt(msh.vol);
+  double tolpss = std::fabs(tol), div0 = 0.0, rnorm = 0.0;
+  std::vector<double> H((size_t)(m + 1) * (m + 1), 0.0), cs((size_t)m + 1), sn((size_t)m + 1),
+      gam((size_t)m + 2), hcol((size_t)m + 1);
+  auto HM = [&](int i, int j) -> double& { return H[(size_t)i + (size_t)(m + 1) * j]; };
+  int iter = 0;
+  bool conv = false;
+  while (!conv) {
+    if (iter == 0) {
+      cudaMemcpyAsync(r, res, n * sizeof(double), cudaMemcpyDeviceToDevice, s);
+    } else {
+      if (apply_A(w, x)) return -3;
+      count_launch();
+      resid_kernel<<<nb, kT, 0, s>>>(r, res, w, n);
+    }
+    count_launch();
+    wdot_kernel<<<nb, kT, 0, s>>>(r, r, wt, n, h.red.ptr);
+    double rr = 0.0;
+    if (g.sums(1, 1, &rr)) return -3;
+    gam[0] = std::sqrt(rr);
+    if (iter == 0) {
+      div0 = gam[0] * norm_fac;
+      if (tol < 0) tolpss = std::fabs(tol) * div0;
+    }
+    rnorm = 0.0;
+    if (gam[0] == 0.0) break;  // lucky convergence
+    count_launch();
+    scale_kernel<<<nb, kT, 0, s>>>(V, r, 1.0 / gam[0], n);
+    int j = 0;
+    for (j = 0; j < m; ++j) {
+      ++iter;
+      double* zj = Z + (size_t)n * j;
+      const double* vj = V + (size_t)n * j;
+      count_launch();
+      prec_kernel<<<nb, kT, 0, s>>>(zj, d, vj, n, null_space ? h.red.ptr : nullptr);
+      if (ortho(zj, null_space ? h.red.ptr : nullptr)) return -3;
+      if (apply_A(w, zj)) return -3;
+      // h_ij = (w, v_i), i <= j, eight vectors per pass
+      for (int i0 = 0; i0 <= j; i0 += kDots) {
+        const int cnt = std::min(kDots, j + 1 - i0);
+        count_launch();
+        mdot_kernel<<<nb, kT, 0, s>>>(w, V + (size_t)n * i0, cnt, wt, n, h.red.ptr);
+        if (g.sums(kDots, cnt, &hcol[(size_t)i0])) return -3;
+      }
+      for (int i = 0; i <= j; ++i) HM(i, j) = hcol[(size_t)i];
+      cudaMemcpyAsync(h.gm_c.ptr, hcol.data(), (j + 1) * sizeof(double), cudaMemcpyHostToDevice,
+                      s);
+      count_launch();
+      msub_kernel<<<nb, kT, 0, s>>>(w, V, j + 1, h.gm_c.ptr, wt, n, h.red.ptr);
+      double ww = 0.0;
+      if (g.sums(1, 1, &ww)) return -3;
+      for (int i = 0; i < j; ++i) {  // Givens rotations on the new column
+        const double t = HM(i, j);
+        HM(i, j) = cs[(size_t)i] * t + sn[(size_t)i] * HM(i + 1, j);
+        HM(i + 1, j) = -sn[(size_t)i] * t + cs[(size_t)i] * HM(i + 1, j);
+      }
+      const double alpha = std::sqrt(ww);
+      rnorm = 0.0;
+      if (alpha == 0.0) {
+        conv = true;
+        break;
+      }
+      const double l = std::sqrt(HM(j, j) * HM(j, j) + alpha * alpha);
+      const double tmp = 1.0 / l;
+      cs[(size_t)j] = HM(j, j) * tmp;
+      sn[(size_t)j] = alpha * tmp;
+      HM(j, j) = l;
+      gam[(size_t)j + 1] = -sn[(size_t)j] * gam[(size_t)j];
+      gam[(size_t)j] = cs[(size_t)j] * gam[(size_t)j];
+      rnorm = std::fabs(gam[(size_t)j + 1]) * norm_fac;
+      if (iter + 1 > maxit || rnorm < tolpss) {
+        conv = true;
+        break;
+      }
+      if (j == m - 1) break;  // restart
+      count_launch();
+      scale_kernel<<<nb, kT, 0, s>>>(V + (size_t)n * (j + 1), w, 1.0 / alpha, n);
+    }
+    // back substitution, then x += sum c_i z_i
+    const int jj = j < m ? j : m - 1;
+    for (int k = jj; k >= 0; --k) {
+      double t = gam[(size_t)k];
+      for (int i = jj; i > k; --i) t = t - HM(k, i) * cs[(size_t)i];
+      cs[(size_t)k] = t / HM(k, k);
+    }
+    cudaMemcpyAsync(h.gm_c.ptr, cs.data(), (jj + 1) * sizeof(double), cudaMemcpyHostToDevice, s);
+    count_launch();
+    xupd_kernel<<<nb, kT, 0, s>>>(x, Z, jj + 1, h.gm_c.ptr, n);
+  }
+  cudaMemcpyAsync(res, x, n * sizeof(double), cudaMemcpyDeviceToDevice, s);
+  if (ortho(res, nullptr)) return -3;
+  if (cudaStreamSynchronize(s) != cudaSuccess) {
+    set_error(h, std::string("gmres: ") + cudaGetErrorString(cudaGetLastError()));
+    return -3;
+  }
+  *niter = iter;
+  *div0_out = div0;
+  *rnorm_out = rnorm;
+  if (!(rnorm < tolpss) && rnorm != 0.0 && gam[0] != 0.0) {
+    set_error(h, "gmres: iteration cap reached above the tolerance");
+    return -5;
+  }
+  return 0;
+}
+
+}  // namespace nekgpu
+
+// ---------------------------------------------------------------------------
+// C ABI
+namespace nekgpu {
+Handle* handle_lookup(const int64_t* h);
+int handle_fail(Handle* H, int code, const std::string& msg);
+}  // namespace nekgpu
+
+using namespace nekgpu;
+
+extern "C" int nekgpu_hmh_gmres_dev(const int64_t* handle, double* res, const double* h1,
+                                    const double* h2, const double* wt, const double* mask,
+                                    const double* tol, const int* maxit, const int* kmax,
+                                    const int* null_space, int* niter, double* div0,
+                                    double* rnorm) {
+  Handle* H = handle_lookup(handle);
+  if (!H) return handle_fail(nullptr, NEKGPU_EHANDLE, "unknown handle");
+  if (cudaSetDevice(H->device) != cudaSuccess)
+    return handle_fail(H, NEKGPU_ECUDA, "cudaSetDevice failed");
+  if (!H->has_mesh) return handle_fail(H, NEKGPU_ENOSETUP, "mesh not set up (nekgpu_setup)");
+  if (!res || !h1 || !h2 || !wt || !mask || !tol || !maxit || !niter || !div0 || !rnorm)
+    return handle_fail(H, NEKGPU_EINVAL, "null argument");
+  const int m = kmax ? *kmax : 30;
+  if (m < 1 || m > NEKGPU_GMRES_MAX)
+    return handle_fail(H, NEKGPU_EINVAL, "restart length must be in [1, NEKGPU_GMRES_MAX]");
+  if (*maxit < 1) return handle_fail(H, NEKGPU_EINVAL, "maxit must be positive");
+  H->err.clear();
+  const int rc = gmres_solve(*H, res, h1, h2, wt, mask, *tol, *maxit, m,
+                             null_space && *null_space != 0, niter, div0, rnorm);
+  if (rc == -5) return handle_fail(H, NEKGPU_ENOTCONV, H->err);
+  if (rc) return handle_fail(H, rc == -4 ? NEKGPU_ENOMEM : NEKGPU_ECUDA,
+                             H->err.empty() ? "gmres failed" : H->err);
+  return NEKGPU_OK;
+}

@@ -123,6 +123,9 @@ struct Handle {
   DevBuf<double> partialA, partialB, partialC, red;
   // multi-field solve: r, p, w, x of every field, field c at c * n
   DevBuf<float> mfr, mfp, mfw, mfx;
+  // GMRES (gmres.cu): Arnoldi and preconditioned vectors, work vectors,
+  // Jacobi diagonal, coefficient staging
+  DevBuf<double> gm_V, gm_Z, gm_r, gm_w, gm_x, gm_d, gm_c;
   int* flag = nullptr;           // device int scratch
   PcgWork<double> w64;
   PcgWork<float> w32;
@@ -221,6 +224,10 @@ PcgResult pcg_prepare(Handle& h, PcgWork<T>& wk, T* x, const T* f, const Coef<T>
                       const T* mask, const T* mult, double tin, int maxiter, int istep,
                       const T* dpre, bool* trivial);
 int pcg_vec_blocks(int64_t n);
+// hmh_gmres with the Jacobi preconditioner (gmres.cu); 0, -3, -4 or -5.
+int gmres_solve(Handle& h, double* res, const double* h1, const double* h2, const double* wt,
+                const double* mask, double tol, int maxit, int m, bool null_space, int* niter,
+                double* div0, double* rnorm);
 // Sets *bad when an element-interior point (not in a boundary group) has mask
 // or multiplicity other than 1 (FP32 arrays; the fused operator assumes 1).
 void launch_interior_check(Handle& h, const float* mask, const float* mult, int* bad);

@@ -161,6 +161,20 @@ class NekGpu:
                                          glo.ctypes.data_as(C.c_void_p)))
         self.n, self.lx1, self.nel = n, lx1, nel
 
+    def hmh_gmres(self, res, h1, h2, wt, mask, tol, maxit=10 ** 6, kmax=30, null_space=False):
+        """The pressure solve's GMRES (device arrays; res: rhs in, solution
+        out).  Returns (iterations, div0, rnorm, status)."""
+        for t in (res, h1, h2, wt, mask):
+            if not _is_dev(t):
+                raise TypeError("hmh_gmres takes device arrays")
+        it, d0, rn = _cint(0), _cdouble(0), _cdouble(0)
+        rc = self._L.nekgpu_hmh_gmres_dev(
+            C.byref(self._h), _ptr(res), _ptr(h1), _ptr(h2), _ptr(wt), _ptr(mask),
+            C.byref(_cdouble(tol)), C.byref(_cint(int(maxit))), C.byref(_cint(kmax)),
+            C.byref(_cint(int(bool(null_space)))), C.byref(it), C.byref(d0), C.byref(rn))
+        self._check(rc, allow=(_capi.ENOTCONV,))
+        return it.value, d0.value, rn.value, rc
+
     def setup_xyz(self, lx1: int, nel: int, D, w, x, y, z, glo_num):
         """setup with G1..G6 and bm1 computed on the GPU from the GLL
         coordinates x, y, z ((n,) numpy each) and the GLL weights w (lx1)."""

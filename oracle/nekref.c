@@ -1442,3 +1442,138 @@ int ref_hsolve(const ref_ops *ops, ref_proj *p, double *u, double *r, const doub
   project2(ops, p, u, h1, h2, vmk, vml);
   return niter;
 }
+
+/* ========================================================================
+ * hmh_gmres -- core/gmres.f:304-560 (see nekref.h), preconditioner M = diag
+ * ====================================================================== */
+static void gm_ax(const ref_ops *ops, double *w, const double *x, const double *h1,
+                  const double *h2, const double *mask) {
+  ref_axhelm(ops, w, x, h1, h2); /* ax, gmres.f:284-302 */
+  ref_dssum(ops, w);
+  for (int64_t i = 0; i < ops->n; ++i) w[i] = w[i] * mask[i];
+}
+
+static void gm_ortho(const ref_ops *ops, double *z, int null_space) {
+  if (!null_space) return;
+  double sum; /* glsum / ntotg, cadd (navier1.f:242-245) */
+  GLOBAL_SUM(ops, sum, z[i]);
+  const double rlam = sum / (double)ops->n;
+  for (int64_t i = 0; i < ops->n; ++i) z[i] = z[i] + (-rlam);
+}
+
+int ref_gmres(const ref_ops *ops, double *res, const double *h1, const double *h2,
+              const double *wt, const double *mask, double tol, int maxit, int m, int null_space,
+              double *div0_out, double *rnorm_out) {
+  const int64_t n = ops->n;
+  if (m < 1) m = 1;
+  double *d = (double *)malloc(sizeof(double) * n);
+  double *r = (double *)malloc(sizeof(double) * n);
+  double *w = (double *)malloc(sizeof(double) * n);
+  double *x = (double *)calloc((size_t)n, sizeof(double));
+  double *V = (double *)malloc(sizeof(double) * n * m);
+  double *Z = (double *)malloc(sizeof(double) * n * m);
+  double *H = (double *)calloc((size_t)(m + 1) * (m + 1), sizeof(double)); /* H[i + (m+1) j] */
+  double *c = (double *)calloc((size_t)m + 1, sizeof(double));
+  double *sn = (double *)calloc((size_t)m + 1, sizeof(double));
+  double *gam = (double *)calloc((size_t)m + 2, sizeof(double));
+  ref_setprec(ops, d, h1, h2);
+  const double norm_fac = 1.0 / sqrt(ops->vol);
+  double tolpss = fabs(tol), div0 = 0.0, rnorm = 0.0;
+  int iter = 0, iconv = 0;
+#define HM(i, j) H[(i) + (size_t)(m + 1) * (j)]
+  while (!iconv) {
+    if (iter == 0) {
+      for (int64_t i = 0; i < n; ++i) r[i] = 1.0 * res[i]; /* col3(r, ml, res) */
+    } else {
+      gm_ax(ops, w, x, h1, h2, mask);
+      for (int64_t i = 0; i < n; ++i) r[i] = res[i] + (-1.0) * w[i]; /* add2s2(r, w, -1) */
+    }
+    gam[0] = sqrt(ref_glsc3(ops, r, r, wt));
+    if (iter == 0) {
+      div0 = gam[0] * norm_fac;
+      if (tol < 0) tolpss = fabs(tol) * div0;
+    }
+    rnorm = 0.0;
+    if (gam[0] == 0.0) break; /* lucky convergence */
+    double temp = 1.0 / gam[0];
+    for (int64_t i = 0; i < n; ++i) V[i] = r[i] * temp;
+    int j;
+    int restart = 0;
+    for (j = 0; j < m; ++j) {
+      ++iter;
+      double *zj = Z + (size_t)n * j, *vj = V + (size_t)n * j;
+      for (int64_t i = 0; i < n; ++i) zj[i] = d[i] * (1.0 * vj[i]); /* M (mu v_j) */
+      gm_ortho(ops, zj, null_space);
+      gm_ax(ops, w, zj, h1, h2, mask);
+      for (int iv = 0; iv <= j; ++iv) { /* h_ij = vlsc3(w, v_i, wt) */
+        const double *vi = V + (size_t)n * iv;
+        double hs;
+        GLOBAL_SUM(ops, hs, w[i] * vi[i] * wt[i]);
+        HM(iv, j) = hs;
+      }
+      for (int i = 0; i <= j; ++i) {
+        const double *vi = V + (size_t)n * i;
+        const double a = -HM(i, j);
+        for (int64_t q = 0; q < n; ++q) w[q] = w[q] + a * vi[q];
+      }
+      for (int i = 0; i < j; ++i) { /* Givens rotations on the new column */
+        const double t = HM(i, j);
+        HM(i, j) = c[i] * t + sn[i] * HM(i + 1, j);
+        HM(i + 1, j) = -sn[i] * t + c[i] * HM(i + 1, j);
+      }
+      const double alpha = sqrt(ref_glsc3(ops, w, w, wt));
+      rnorm = 0.0;
+      if (alpha == 0.0) {
+        iconv = 1;
+        break;
+      }
+      const double l = sqrt(HM(j, j) * HM(j, j) + alpha * alpha);
+      temp = 1.0 / l;
+      c[j] = HM(j, j) * temp;
+      sn[j] = alpha * temp;
+      HM(j, j) = l;
+      gam[j + 1] = -sn[j] * gam[j];
+      gam[j] = c[j] * gam[j];
+      rnorm = fabs(gam[j + 1]) * norm_fac;
+      if (iter + 1 > maxit || rnorm < tolpss) {
+        iconv = 1;
+        break;
+      }
+      if (j == m - 1) {
+        restart = 1;
+        break;
+      }
+      temp = 1.0 / alpha;
+      double *vn = V + (size_t)n * (j + 1);
+      for (int64_t i = 0; i < n; ++i) vn[i] = w[i] * temp;
+    }
+    (void)restart;
+    /* back substitution c = H^-1 gamma, then x += sum c_i z_i */
+    const int jj = j < m ? j : m - 1;
+    for (int k = jj; k >= 0; --k) {
+      double t = gam[k];
+      for (int i = jj; i > k; --i) t = t - HM(k, i) * c[i];
+      c[k] = t / HM(k, k);
+    }
+    for (int i = 0; i <= jj; ++i) {
+      const double *zi = Z + (size_t)n * i;
+      for (int64_t q = 0; q < n; ++q) x[q] = x[q] + c[i] * zi[q];
+    }
+  }
+#undef HM
+  for (int64_t i = 0; i < n; ++i) res[i] = x[i];
+  gm_ortho(ops, res, null_space);
+  if (div0_out) *div0_out = div0;
+  if (rnorm_out) *rnorm_out = rnorm;
+  free(d);
+  free(r);
+  free(w);
+  free(x);
+  free(V);
+  free(Z);
+  free(H);
+  free(c);
+  free(sn);
+  free(gam);
+  return iter;
+}

@@ -106,6 +106,22 @@ int ref_hsolve(const ref_ops *ops, ref_proj *p, double *u, double *r, const doub
                const double *h2, const double *vmk, const double *vml, double tli, int maxit,
                int maxcg, int istep, const double *binv, double *rbn0, double *rbn2);
 
+/* hmh_gmres (gmres.f:304-560): right-preconditioned restarted GMRES on
+ * ax() = dssum(axhelm(x)) * mask (gmres.f:284-302), weights wt (vmult),
+ * restart length m (lgmres), classical Gram-Schmidt (the 1st pass of
+ * :430-446), Givens rotations, back substitution; ml = mu = 1
+ * (uzawa_gmres_split :252-271); ortho() (navier1.f:223-256) removes the mean
+ * of z_j and of the result when null_space is set.  The preconditioner is
+ * M w = d w with d = setprec's Jacobi diagonal: a stand-in for the
+ * reference's Schwarz-multigrid / FDM + coarse-grid preconditioner, which
+ * this restatement does not have.  res: in the right-hand side, out the
+ * solution.  tol: absolute on rnorm = |gamma| / sqrt(volvm1) (tol < 0:
+ * relative to the initial one).  Returns the iteration count; *div0 and
+ * *rnorm the first and last residual norms. */
+int ref_gmres(const ref_ops *ops, double *res, const double *h1, const double *h2,
+              const double *wt, const double *mask, double tol, int maxit, int m, int null_space,
+              double *div0, double *rnorm);
+
 /* local_grad3 (navier5.f:428) / local_grad3_t (navier1.f:4669), one element */
 void ref_local_grad3(double *ur, double *us, double *ut, const double *u, int N,
                      const double *d, const double *dt);

@@ -89,6 +89,9 @@ def lib():
                                      C.c_int, C.c_int, _dp, C.POINTER(C.c_double),
                                      C.POINTER(C.c_double)]
             L.ref_hsolve.restype = C.c_int
+            L.ref_gmres.argtypes = [_vp, _dp, _dp, _dp, _dp, _dp, C.c_double, C.c_int, C.c_int,
+                                    C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+            L.ref_gmres.restype = C.c_int
             L.ref_local_grad3.argtypes = [_dp, _dp, _dp, _dp, C.c_int, _dp, _dp]
             L.ref_local_grad3_t.argtypes = [_dp, _dp, _dp, _dp, C.c_int, _dp, _dp, _dp]
             L.ref_mxm.argtypes = [_dp, C.c_int, _dp, C.c_int, _dp, C.c_int]
@@ -240,6 +243,15 @@ class Ops:
                             int(min(maxit, 2 ** 31 - 1)), int(min(maxcg, 2 ** 31 - 1)), int(istep),
                             _c(binv), C.byref(r0), C.byref(r2))
         return x, it, r0.value, r2.value
+
+    def gmres(self, rhs, h1, h2, wt, mask, tol, maxit=10 ** 6, m=30, null_space=False):
+        """hmh_gmres with the Jacobi stand-in preconditioner (nekref.h).
+        Returns (x, iterations, div0, rnorm)."""
+        x = np.array(rhs, dtype=np.float64, copy=True)
+        d0, rn = C.c_double(0), C.c_double(0)
+        it = lib().ref_gmres(self.h, x, _c(h1), _c(h2), _c(wt), _c(mask), float(tol),
+                             int(maxit), int(m), int(bool(null_space)), C.byref(d0), C.byref(rn))
+        return x, it, d0.value, rn.value
 
     def hmholtz(self, rhs, h1, h2, mask, mult, binv, tli, maxit=10 ** 9, maxcg=900, istep=0):
         """Returns (u, rhs_after_dssum_mask, niter, rbn0, rbn2)."""

@@ -252,3 +252,28 @@ def test_oracle_matches_committed_golden_fixtures(oracle):
         else:
             scale = np.max(np.abs(a)) if a.size else 1.0
             assert np.max(np.abs(a - b)) <= 1e-12 * max(scale, 1e-300), k
+
+
+def test_gmres_restatement_solves_the_system(oracle):
+    """hmh_gmres restated (Jacobi stand-in preconditioner): its residual
+    estimate equals the true weighted residual, restarts do not change the
+    solution beyond the tolerance, and the null-space case returns a
+    zero-mean solution of a consistent system."""
+    from conftest import rng_unit_vector
+    P = oracle.box_problem(5, 3, 2, 2, v=rng_unit_vector(61))
+    n, ops = P["n"], P["ops"]
+    h1, h2 = np.ones(n), np.zeros(n)
+    f = ops.dssum(P["bm1"] * np.random.default_rng(61).standard_normal(n)) * P["mask"]
+    x, it, d0, rn = ops.gmres(f, h1, h2, P["mult"], P["mask"], -1e-10, m=30)
+    r = f - ops.dssum(ops.axhelm(x, h1, h2)) * P["mask"]
+    true = np.sqrt(np.sum(r * r * P["mult"]) / np.sum(P["bm1"]))
+    assert rn < 1e-10 * d0 and abs(true - rn) <= 1e-3 * rn
+    x5, it5, _, _ = ops.gmres(f, h1, h2, P["mult"], P["mask"], -1e-10, m=5)
+    assert it5 > it and np.linalg.norm(x5 - x) <= 1e-8 * np.linalg.norm(x)
+    Q = oracle.box_problem(5, 2, 2, 2, dirichlet=(False,) * 6, v=rng_unit_vector(62))
+    nq, oq = Q["n"], Q["ops"]
+    g = oq.dssum(Q["bm1"] * np.random.default_rng(62).standard_normal(nq))
+    g = g - np.sum(g * Q["mult"]) / np.sum(Q["mult"])
+    xq, itq, d0q, rnq = oq.gmres(g, np.ones(nq), np.zeros(nq), Q["mult"], Q["mask"], -1e-10,
+                                 maxit=4000, null_space=True)
+    assert rnq < 1e-10 * d0q and abs(np.mean(xq)) < 1e-14
