@@ -27,8 +27,8 @@ namespace {
 constexpr int kT = 256;
 constexpr int kDots = 8;  // weighted dot products per pass
 
-inline int nblocks(int64_t n) {
-  return (int)std::min<int64_t>(std::max<int64_t>((n + kT - 1) / kT, 1), 152 * 6);
+inline int nblocks(int64_t n) {  // about four points per thread, at most 152 x 6 blocks
+  return (int)std::min<int64_t>(std::max<int64_t>((n + 4 * kT - 1) / (4 * kT), 1), 152 * 6);
 }
 
 __device__ __forceinline__ double block_reduce(double v, double* red) {
@@ -57,24 +57,53 @@ __global__ void __launch_bounds__(kT) wdot_kernel(const double* __restrict__ a,
   if (threadIdx.x == 0) partial[blockIdx.x] = s;
 }
 
-// partial[blk * kDots + k] = sum w v_k wt, k < cnt, v_k = V + k n
+// partial[blk * kDots + k] = sum w v_k wt, k < CNT, v_k = V + k n; the CNT
+// sums of a block reduced together (one shared-memory exchange)
+template <int CNT>
 __global__ void __launch_bounds__(kT) mdot_kernel(const double* __restrict__ w,
-                                                  const double* __restrict__ V, int cnt,
+                                                  const double* __restrict__ V,
                                                   const double* __restrict__ wt, int64_t n,
                                                   double* __restrict__ partial) {
-  __shared__ double red[kT / 32];
-  double acc[kDots];
+  __shared__ double red[kT / 32][CNT];
+  double acc[CNT];
 #pragma unroll
-  for (int k = 0; k < kDots; ++k) acc[k] = 0.0;
+  for (int k = 0; k < CNT; ++k) acc[k] = 0.0;
   for (int64_t i = blockIdx.x * (int64_t)kT + threadIdx.x; i < n; i += (int64_t)gridDim.x * kT) {
     const double ww = w[i], t = wt[i];
 #pragma unroll
-    for (int k = 0; k < kDots; ++k)
-      if (k < cnt) acc[k] += __dmul_rn(__dmul_rn(ww, V[(int64_t)k * n + i]), t);
+    for (int k = 0; k < CNT; ++k) acc[k] += __dmul_rn(__dmul_rn(ww, V[(int64_t)k * n + i]), t);
   }
-  for (int k = 0; k < cnt; ++k) {
-    const double s = block_reduce(acc[k], red);
-    if (threadIdx.x == 0) partial[(int64_t)blockIdx.x * kDots + k] = s;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < CNT; ++k) {
+    double v = acc[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) red[wid][k] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < CNT) {
+    double t = 0.0;
+    for (int q = 0; q < kT / 32; ++q) t += red[q][threadIdx.x];
+    partial[(int64_t)blockIdx.x * kDots + threadIdx.x] = t;
+  }
+}
+
+void launch_mdot(int cnt, int nb, cudaStream_t s, const double* w, const double* V,
+                 const double* wt, int64_t n, double* partial) {
+  count_launch();
+  switch (cnt) {
+#define NEKGPU_MDOT(C) \
+  case C: mdot_kernel<C><<<nb, kT, 0, s>>>(w, V, wt, n, partial); break;
+    NEKGPU_MDOT(1)
+    NEKGPU_MDOT(2)
+    NEKGPU_MDOT(3)
+    NEKGPU_MDOT(4)
+    NEKGPU_MDOT(5)
+    NEKGPU_MDOT(6)
+    NEKGPU_MDOT(7)
+    default: mdot_kernel<8><<<nb, kT, 0, s>>>(w, V, wt, n, partial); break;
+#undef NEKGPU_MDOT
   }
 }
 
@@ -279,8 +308,7 @@ int gmres_solve(Handle& h, double* res, const double* h1, const double* h2, cons
       // h_ij = (w, v_i), i <= j, eight vectors per pass
       for (int i0 = 0; i0 <= j; i0 += kDots) {
         const int cnt = std::min(kDots, j + 1 - i0);
-        count_launch();
-        mdot_kernel<<<nb, kT, 0, s>>>(w, V + (size_t)n * i0, cnt, wt, n, h.red.ptr);
+        launch_mdot(cnt, nb, s, w, V + (size_t)n * i0, wt, n, h.red.ptr);
         if (g.sums(kDots, cnt, &hcol[(size_t)i0])) return -3;
       }
       for (int i = 0; i <= j; ++i) HM(i, j) = hcol[(size_t)i];
