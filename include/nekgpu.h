@@ -110,6 +110,11 @@ int nekgpu_hmh_gmres_dev(const int64_t *handle, double *res, const double *h1, c
                          const double *wt, const double *mask, const double *tol,
                          const int *maxit, const int *kmax, const int *null_space, int *niter,
                          double *div0, double *rnorm);
+/* The same on host arrays (copied in and out inside the call). */
+int nekgpu_hmh_gmres(const int64_t *handle, double *res, const double *h1, const double *h2,
+                     const double *wt, const double *mask, const double *tol, const int *maxit,
+                     const int *kmax, const int *null_space, int *niter, double *div0,
+                     double *rnorm);
 
 /* As nekgpu_setup, with the geometric factors and the mass computed on the
  * device from the GLL coordinates xm1, ym1, zm1 (host arrays, lx1^3 nel

@@ -162,13 +162,14 @@ class NekGpu:
         self.n, self.lx1, self.nel = n, lx1, nel
 
     def hmh_gmres(self, res, h1, h2, wt, mask, tol, maxit=10 ** 6, kmax=30, null_space=False):
-        """The pressure solve's GMRES (device arrays; res: rhs in, solution
-        out).  Returns (iterations, div0, rnorm, status)."""
-        for t in (res, h1, h2, wt, mask):
-            if not _is_dev(t):
-                raise TypeError("hmh_gmres takes device arrays")
+        """The pressure solve's GMRES (res: rhs in, solution out; all device
+        arrays or all host arrays).  Returns (iterations, div0, rnorm, status)."""
+        dev = [_is_dev(t) for t in (res, h1, h2, wt, mask)]
+        if any(dev) and not all(dev):
+            raise TypeError("hmh_gmres takes all device or all host arrays")
+        fn = self._L.nekgpu_hmh_gmres_dev if dev[0] else self._L.nekgpu_hmh_gmres
         it, d0, rn = _cint(0), _cdouble(0), _cdouble(0)
-        rc = self._L.nekgpu_hmh_gmres_dev(
+        rc = fn(
             C.byref(self._h), _ptr(res), _ptr(h1), _ptr(h2), _ptr(wt), _ptr(mask),
             C.byref(_cdouble(tol)), C.byref(_cint(int(maxit))), C.byref(_cint(kmax)),
             C.byref(_cint(int(bool(null_space)))), C.byref(it), C.byref(d0), C.byref(rn))

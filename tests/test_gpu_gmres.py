@@ -65,3 +65,22 @@ def test_gmres_reports_the_iteration_cap(gpu_lib, oracle):
     it, d0, rn, rc = lib.hmh_gmres(dev(f), dev(np.ones(n)), dev(np.zeros(n)), dev(P["mult"]),
                                    dev(P["mask"]), -1e-10, maxit=5, kmax=30)
     assert rc == _capi.ENOTCONV and it == 5 and rn > 1e-10 * d0
+
+
+def test_gmres_host_entry_point(gpu_lib, oracle):
+    """nekgpu_hmh_gmres (host arrays) returns what the device entry point does."""
+    torch = pytest.importorskip("torch")
+    P = oracle.box_problem(6, 2, 3, 2, v=rng_unit_vector(77))
+    n = P["n"]
+    lib = gpu_lib(0)
+    lib.setup(P["nx1"], P["nel"], P["D"], P["g"], P["bm1"], P["glo_num"])
+    f = P["ops"].dssum(P["bm1"] * np.random.default_rng(78).standard_normal(n)) * P["mask"]
+    h1, h2 = np.ones(n), np.full(n, 3.0)
+    xh = f.copy()
+    ith, d0h, rnh, rch = lib.hmh_gmres(xh, h1, h2, P["mult"], P["mask"], -1e-10, kmax=20)
+    dev = lambda a: torch.tensor(a, device="cuda")
+    xd = dev(f)
+    itd, d0d, rnd, rcd = lib.hmh_gmres(xd, dev(h1), dev(h2), dev(P["mult"]), dev(P["mask"]),
+                                       -1e-10, kmax=20)
+    assert rch == rcd == 0 and ith == itd and d0h == d0d and rnh == rnd
+    assert np.array_equal(xh, xd.cpu().numpy())
