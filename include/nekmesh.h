@@ -110,14 +110,18 @@ int nekmesh_xyzlin(const int *nx, const int *nel, const double *zgll, const doub
  * nodes, the given midside nodes on their edges, the edges extended inward
  * by Gordon-Hall (gh_face_extend_3d, core/navier5.f:2502, vertices and
  * edges), then the quadratic interpolant at the GLL nodes (Fornberg weights,
- * fd_weights_full, core/fast3d.f:1294; tensr3, core/fasts.f:125).  Then
- * every circular-arc record (type 'C' on edge 1..8, signed radius in
- * curve[5q]; positive with the centre on the element's side) bends its edge
- * as arcsrf does (core/genxyz.f:2-101), the bend blended linearly across the
- * element.  Records of any other curve type (spheres, ...) give
- * NEKGPU_EINVAL, as does an arc shorter in radius than half its chord;
- * records with a blank type are ignored.  nx = 2 ignores midside nodes, as
- * linquad. */
+ * fd_weights_full, core/fast3d.f:1294; tensr3, core/fasts.f:125).  Then,
+ * element by element as genxyz does: every spherical-face record (type 's'
+ * on face 1..6, centre in curve[5q .. 5q+2], radius in curve[5q+3]) makes
+ * the face a sphere patch as sphsrf does (core/genxyz.f:677-842: great-circle
+ * edges, crossings of opposite-edge arcs inside, the deflection spread
+ * linearly from the opposite face), then every circular-arc record (type
+ * 'C' on edge 1..8, signed radius in curve[5q]; positive with the centre on
+ * the element's side) bends its edge as arcsrf does (:2-101), the bend
+ * blended linearly across the element.  Records of any other curve type
+ * ('e' surfaces) give NEKGPU_EINVAL, as do an arc shorter in radius than
+ * half its chord and a sphere corner off its sphere; records with a blank
+ * type are ignored.  nx = 2 ignores midside nodes, as linquad. */
 int nekmesh_genxyz(const int *nx, const int *nel, const double *zgll, const double *xc,
                    const double *yc, const double *zc, const int64_t *ncurve, const int *elem,
                    const int *side, const double *curve, const char *ccurve, double *x, double *y,

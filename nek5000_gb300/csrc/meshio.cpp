@@ -895,6 +895,128 @@ void gordon_hall_edges3(double* x) {
 // Midside node of each preprocessor edge (1..12) in the 3x3x3 array.
 constexpr int kEdgeMid[12] = {1, 5, 7, 3, 19, 23, 25, 21, 9, 11, 17, 15};
 
+// sphsrf (core/genxyz.f:677-842): face ifce (1..6, preprocessor order) of an
+// element made a patch of the sphere of the given centre and radius: the
+// face's four edges become great-circle arcs (edg3d :844), the interior
+// points the normalised crossings of the arcs through opposite edge points,
+// then the face's deflection is spread linearly from the opposite face.
+// xc, yc, zc: the element's corners (file order); x, y, z its GLL
+// coordinates.  Returns false when a corner is not on the sphere or the
+// radius is not positive (crn3d :929-1021).
+bool sphere_face(int nx, const double* zg, const double* xc, const double* yc, const double* zc,
+                 int ifce, const double* cv, double* x, double* y, double* z) {
+  const double ctr[3] = {cv[0], cv[1], cv[2]}, radius = cv[3];
+  if (!(radius > 0.0)) return false;
+  const int iface = kTensorFace[ifce - 1];  // eface1
+  // corners of the face (crn3d: indvtx, tensor numbering, to file order)
+  static const int indvtx[6][4] = {{1, 5, 3, 7}, {2, 4, 6, 8}, {1, 2, 5, 6},
+                                   {3, 7, 4, 8}, {1, 3, 2, 4}, {5, 6, 7, 8}};
+  double xcv[4][3];
+  for (int i = 0; i < 4; ++i) {
+    const int k = kPreOfTensor[indvtx[iface - 1][i] - 1];
+    xcv[i][0] = xc[k] - ctr[0];
+    xcv[i][1] = yc[k] - ctr[1];
+    xcv[i][2] = zc[k] - ctr[2];
+    const double radt = std::sqrt(xcv[i][0] * xcv[i][0] + xcv[i][1] * xcv[i][1] +
+                                  xcv[i][2] * xcv[i][2]);
+    if (std::fabs(radt - radius) / radius > 1e-4) return false;
+  }
+  auto dot = [](const double* a, const double* b) {
+    double s = 0.0;
+    for (int k = 0; k < 3; ++k) s = s + a[k] * b[k];
+    return s;
+  };
+  auto cross = [](double* v1, const double* v2, const double* v3) {
+    v1[0] = v2[1] * v3[2] - v2[2] * v3[1];
+    v1[1] = v2[2] * v3[0] - v2[0] * v3[2];
+    v1[2] = v2[0] * v3[1] - v2[1] * v3[0];
+  };
+  auto norm3 = [&](double* v) {
+    const double l = std::sqrt(dot(v, v));
+    if (l > 0) {
+      v[0] = v[0] / l;
+      v[1] = v[1] / l;
+      v[2] = v[2] / l;
+    }
+  };
+  std::vector<double> srf((size_t)3 * nx * nx);  // srf(3, nx, nx), (i, j)
+  auto S = [&](int i, int j) { return &srf[(size_t)3 * (i + nx * j)]; };
+  // edg3d: the great-circle arc from x1 to x2 at the GLL nodes
+  auto edge = [&](const double* x1, const double* x2, int i1, int i2, int j1, int j2) {
+    double u1[3] = {x1[0], x1[1], x1[2]}, u2[3] = {x2[0], x2[1], x2[2]}, vn[3], b[3];
+    norm3(u1);
+    norm3(u2);
+    cross(vn, x1, x2);
+    cross(b, vn, x1);
+    norm3(vn);
+    norm3(b);
+    const double theta = std::acos(dot(u1, u2));
+    int ij = 0;
+    for (int j = j1; j <= j2; ++j)
+      for (int i = i1; i <= i2; ++i, ++ij) {
+        const double tp = 0.5 * theta * (zg[ij] + 1.0);
+        const double ct = std::cos(tp), st = std::sin(tp);
+        for (int v = 0; v < 3; ++v) S(i, j)[v] = ct * u1[v] + st * b[v];
+      }
+  };
+  // xcv(3,2,2): corner (a, b) is xcv[a + 2 b]
+  edge(xcv[0], xcv[2], 0, 0, 0, nx - 1);
+  edge(xcv[1], xcv[3], nx - 1, nx - 1, 0, nx - 1);
+  edge(xcv[0], xcv[1], 0, nx - 1, 0, 0);
+  edge(xcv[2], xcv[3], 0, nx - 1, nx - 1, nx - 1);
+  // sign of the curvature from a face corner and the corner opposite it
+  static const int cface[6][2] = {{1, 4}, {2, 1}, {3, 2}, {4, 3}, {1, 5}, {5, 1}};
+  const int iv = cface[ifce - 1][0] - 1, io = cface[ifce - 1][1] - 1;
+  const double vout[3] = {xc[iv] - xc[io], yc[iv] - yc[io], zc[iv] - zc[io]};
+  const double vsph[3] = {xc[iv] - ctr[0], yc[iv] - ctr[1], zc[iv] - ctr[2]};
+  const bool concave = !(dot(vsph, vout) > 0);
+  for (int j = 1; j < nx - 1; ++j) {
+    double vn1[3], vn2[3];
+    cross(vn1, S(0, j), S(nx - 1, j));
+    for (int i = 1; i < nx - 1; ++i) {
+      cross(vn2, S(i, 0), S(i, nx - 1));
+      if (concave) cross(S(i, j), vn2, vn1);
+      else cross(S(i, j), vn1, vn2);
+    }
+  }
+  for (int q = 0; q < nx * nx; ++q) norm3(&srf[(size_t)3 * q]);
+  for (double& v : srf) v = v * radius;
+  for (int q = 0; q < nx * nx; ++q)
+    for (int v = 0; v < 3; ++v) srf[(size_t)3 * q + v] = srf[(size_t)3 * q + v] + ctr[v];
+  if (iface == 1 || iface == 4 || iface == 5)  // transpose
+    for (int j = 0; j < nx; ++j)
+      for (int i = j + 1; i < nx; ++i)
+        for (int v = 0; v < 3; ++v) std::swap(S(i, j)[v], S(j, i)[v]);
+  // the face's deflection, spread linearly from the opposite face
+  const int64_t NX = nx, NXX = (int64_t)nx * nx;
+  const int64_t sk[6][6] = {{1, NX * (NX - 1) + 1, NX, 1, NX * (NX - 1) + 1, NX},
+                            {NX, NX * (NX - 1) + NX, NX, 1, NX * (NX - 1) + 1, NX},
+                            {1, NX, 1, 1, NX * (NX - 1) + 1, NX},
+                            {1 + NX * (NX - 1), NXX, 1, 1, NX * (NX - 1) + 1, NX},
+                            {1, NX, 1, 1, NX, 1},
+                            {1 + NXX * (NX - 1), NX + NXX * (NX - 1), 1, 1, NX, 1}};
+  const int64_t* d = sk[iface - 1];
+  const int64_t iopp[3] = {NX - 1, NX * (NX - 1), NXX * (NX - 1)};
+  const int idir = 2 * (iface % 2) - 1, ifc2 = (iface + 1) / 2;
+  double* c3[3] = {x, y, z};
+  int q = 0;
+  for (int64_t j2 = d[3]; d[5] > 0 ? j2 <= d[4] : j2 >= d[4]; j2 += d[5])
+    for (int64_t j1 = d[0]; d[2] > 0 ? j1 <= d[1] : j1 >= d[1]; j1 += d[2], ++q) {
+      const int64_t jopp = j1 + iopp[ifc2 - 1] * idir;
+      const int64_t face_pt = j1 - 1 + NX * (j2 - 1);
+      double dx[3];
+      for (int v = 0; v < 3; ++v) dx[v] = srf[(size_t)3 * q + v] - c3[v][face_pt];
+      const int64_t joff = (j1 - jopp) / (NX - 1);
+      for (int ix = 2; ix <= nx; ++ix) {
+        const int64_t jj = jopp + joff * (ix - 1);
+        const double zeta = 0.5 * (zg[ix - 1] + 1.0);
+        const int64_t pt = jj - 1 + NX * (j2 - 1);
+        for (int v = 0; v < 3; ++v) c3[v][pt] = c3[v][pt] + dx[v] * zeta;
+      }
+    }
+  return true;
+}
+
 // arcsrf (core/genxyz.f:2-101): edge isid (1..8, in a face of constant t)
 // of an element bent into a circular arc of the given radius in the x-y
 // plane (positive: centre on the element's side), the bend blended linearly
@@ -977,9 +1099,14 @@ int nekmesh_genxyz(const int* nx_, const int* nel_, const double* zg, const doub
       if (side[q] <= 8) arcs.push_back(q);  // the reference bends edges 1..8 only
       continue;
     }
+    if (ccurve[q] == 's') {
+      if (side[q] < 1 || side[q] > 6) return fail(NEKGPU_EINVAL, "genxyz: sphere on no face");
+      arcs.push_back(q);  // applied with the arcs, faces first
+      continue;
+    }
     if (ccurve[q] != 'm')
       return fail(NEKGPU_EINVAL, std::string("genxyz: curved side type '") + ccurve[q] +
-                                     "' not served (midside nodes 'm' and arcs 'C' are)");
+                                     "' not served (midside nodes 'm', arcs 'C', spheres 's' are)");
     if (side[q] < 1 || side[q] > 12) return fail(NEKGPU_EINVAL, "genxyz: midside node on no edge");
     if (first[(size_t)e] < 0) {
       first[(size_t)e] = (int64_t)mid.size();
@@ -1015,13 +1142,22 @@ int nekmesh_genxyz(const int* nx_, const int* nel_, const double* zg, const doub
       tensor3(dst[d] + nxyz * e, nx, q3, 3, wq.data());
     }
   }
-  // circular-arc edges, added after the linear / quadratic map, element by
-  // element and edge by edge (genxyz's order)
+  // spherical faces, then circular-arc edges, after the linear / quadratic
+  // map, element by element, faces and edges in order (genxyz's order)
+  auto rank = [&](int64_t q) { return (ccurve[q] == 's' ? 0 : 100) + side[q]; };
   std::stable_sort(arcs.begin(), arcs.end(), [&](int64_t a, int64_t b) {
-    return elem[a] != elem[b] ? elem[a] < elem[b] : side[a] < side[b];
+    return elem[a] != elem[b] ? elem[a] < elem[b] : rank(a) < rank(b);
   });
   for (const int64_t q : arcs) {
     const int64_t e = elem[q] - 1;
+    if (ccurve[q] == 's') {
+      if (!sphere_face(nx, zg, xc + 8 * e, yc + 8 * e, zc + 8 * e, side[q], curve + 5 * (size_t)q,
+                       x + nxyz * e, y + nxyz * e, z + nxyz * e))
+        return fail(NEKGPU_EINVAL, "genxyz: element " + std::to_string(e + 1) + " face " +
+                                       std::to_string(side[q]) +
+                                       ": corner not on its sphere, or radius not positive");
+      continue;
+    }
     if (!arc_edge(nx, zg, xc + 8 * e, yc + 8 * e, side[q], curve[5 * (size_t)q], x + nxyz * e,
                   y + nxyz * e))
       return fail(NEKGPU_EINVAL, "genxyz: arc radius shorter than half its chord (element " +

@@ -9,9 +9,9 @@ library's host code).
 load_mesh returns the same keys as mesh.box_mesh (lx1, nel, n, D, g, bm1,
 glo_num, mask, mult, binv, vol, x, y, z, zgll, wgll) plus the file's
 boundary conditions.  Elements are mapped from their corners (core/genxyz.f
-xyzlin) or, with 'm' midside nodes, quadratically (xyzquad), and 'C' edges
-are bent into circular arcs (arcsrf); other curved side types (spheres, 'e'
-surfaces) are refused.
+xyzlin) or, with 'm' midside nodes, quadratically (xyzquad); 's' faces are
+made sphere patches (sphsrf) and 'C' edges circular arcs (arcsrf); 'e'
+surfaces are refused.
 """
 from __future__ import annotations
 
@@ -152,8 +152,8 @@ def xyzlin(nx: int, zgll, xc, yc, zc):
 def genxyz(nx: int, zgll, xc, yc, zc, curves=None):
     """GLL coordinates (nel*nx^3 each): straight-sided elements by the
     trilinear map, elements with 'm' midside nodes by the reference's
-    quadratic map (xyzquad), 'C' edges bent into arcs (arcsrf); curves as
-    read_re2 returns them."""
+    quadratic map (xyzquad), 's' faces made sphere patches (sphsrf), 'C'
+    edges bent into arcs (arcsrf); curves as read_re2 returns them."""
     xc, yc, zc = (np.ascontiguousarray(a, dtype=np.float64) for a in (xc, yc, zc))
     zgll = np.ascontiguousarray(zgll, dtype=np.float64)
     ne = xc.shape[0]

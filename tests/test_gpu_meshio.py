@@ -24,6 +24,12 @@ def _mesh(tmp_path, case):
     elif case == "periodic":  # periodic in y, walls on the x and z faces
         xc, yc, zc, _, bcs = box_elements(4, 3, 3, periodic_y=True, jitter=0.2, seed=22,
                                           perm=np.random.default_rng(22).permutation(36))
+    elif case == "shell":  # a spherical shell with spherical faces, walls inside and outside
+        from test_meshio import _cubed_shell
+        xc, yc, zc, curves, bcs = _cubed_shell()
+        p = tmp_path / "shell.re2"
+        write_re2(p, xc, yc, zc, bcs, curves=curves)
+        return meshio.load_mesh(p, N=7)
     else:  # an annular ring with circular-arc edges, walls inside and outside
         from test_meshio import _annulus
         xc, yc, zc, curves, bcs = _annulus(nt=12, nr=3, nz=2)
@@ -35,7 +41,7 @@ def _mesh(tmp_path, case):
     return meshio.load_mesh(p, N=7)
 
 
-@pytest.mark.parametrize("case", ["rotated", "periodic", "annulus"])
+@pytest.mark.parametrize("case", ["rotated", "periodic", "annulus", "shell"])
 def test_re2_mesh_solves_match_the_oracle(gpu_lib, oracle, tmp_path, case):
     torch = pytest.importorskip("torch")
     M = _mesh(tmp_path, case)

@@ -357,3 +357,59 @@ def test_single_element_periodicity(mio, tmp_path):
     np.testing.assert_allclose(avg, f, rtol=0, atol=1e-13)
     cnt = np.rint(1 / M["mult"]).reshape(6, nx, nx, nx)
     assert np.all(cnt[:, 0, 1:-1, 1:-1] == 2) and np.all(cnt[:, 1:-1, 1:-1, 1:-1] == 1)
+
+
+def _cubed_shell(ri=0.5, ro=1.0, k=2, spheres=True):
+    """A spherical shell from the six faces of a cube (k x k elements per face,
+    one across): corners on the spheres, 's' records on the inner (face 5) and
+    outer (face 6) sides, walls there."""
+    frames = [((1, 0, 0), (0, 1, 0), (0, 0, 1)), ((-1, 0, 0), (0, 0, 1), (0, 1, 0)),
+              ((0, 1, 0), (0, 0, 1), (1, 0, 0)), ((0, -1, 0), (1, 0, 0), (0, 0, 1)),
+              ((0, 0, 1), (1, 0, 0), (0, 1, 0)), ((0, 0, -1), (0, 1, 0), (1, 0, 0))]
+    us = np.linspace(-1, 1, k + 1)
+    xc, yc, zc, curves, bcs = [], [], [], [], []
+    e = 0
+    for nrm, eu, ev in frames:
+        nrm, eu, ev = (np.array(a, dtype=float) for a in (nrm, eu, ev))
+        for jv in range(k):
+            for iu in range(k):
+                pts = []
+                for r in (ri, ro):
+                    for (a, b) in ((0, 0), (1, 0), (1, 1), (0, 1)):
+                        p = nrm + us[iu + a] * eu + us[jv + b] * ev
+                        pts.append(r * p / np.linalg.norm(p))
+                pts = np.array(pts)
+                xc.append(pts[:, 0])
+                yc.append(pts[:, 1])
+                zc.append(pts[:, 2])
+                e += 1
+                if spheres:
+                    curves += [(e, 5, (0.0, 0.0, 0.0, ri, 0.0), "s"),
+                               (e, 6, (0.0, 0.0, 0.0, ro, 0.0), "s")]
+                bcs += [(e, 5, (0.0,) * 5, "W  "), (e, 6, (0.0,) * 5, "W  ")]
+    return np.array(xc), np.array(yc), np.array(zc), curves, bcs
+
+
+def test_spherical_faces_make_an_exact_shell(mio, tmp_path):
+    """Spherical faces (sphsrf): the GLL points of the inner and outer faces
+    lie on their spheres, the numbering is continuous, and the volume
+    converges to the shell's (straight-sided elements miss it by percents)."""
+    ri, ro = 0.5, 1.0
+    exact = 4.0 / 3.0 * np.pi * (ro ** 3 - ri ** 3)
+    vols = {}
+    for sph in (True, False):
+        xc, yc, zc, curves, bcs = _cubed_shell(ri, ro, spheres=sph)
+        p = tmp_path / f"shell{sph}.re2"
+        write_re2(p, xc, yc, zc, bcs, curves=curves)
+        M = mio.load_mesh(p, N=7)
+        assert np.all(M["jac"] > 0)
+        vols[sph] = M["vol"]
+        f = M["x"] * M["y"] + np.sin(M["z"])
+        avg = mio._dsop(M["glo_num"], f, "+") * M["mult"]
+        np.testing.assert_allclose(avg, f, rtol=0, atol=1e-13)
+        if sph:
+            rad = np.sqrt(M["x"] ** 2 + M["y"] ** 2 + M["z"] ** 2).reshape(M["nel"], 8, 8, 8)
+            np.testing.assert_allclose(rad[:, 0], ri, rtol=0, atol=1e-14)
+            np.testing.assert_allclose(rad[:, -1], ro, rtol=0, atol=1e-14)
+    assert abs(vols[True] - exact) <= 1e-11 * exact, (vols[True], exact)  # 1.8e-13 at N = 7
+    assert abs(vols[False] - exact) > 1e-1 * exact                          # 23 % off
