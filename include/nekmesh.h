@@ -62,6 +62,12 @@ int nekmesh_re2_close(int64_t *mesh);
  * id and nv vertex ids, 4-byte integers).  vertex (nv * nelgt, element-major,
  * placed by element id) may be null to query the sizes. */
 int nekmesh_co2_read(const char *path, int *nelgt, int *nelgv, int *nv, int64_t *vertex);
+/* .ma2 map file (core/map2.f read_map :712-940; written by tools/genmap
+ * dmp_mapfile): 132-byte header (a5,7i12: version, nel, ...), the byte-order
+ * test value, then per element its partition (0-based) and its vertex ids
+ * (4-byte integers, tensor corner order, used as read).  vertex (nv * nel)
+ * and part (nel) may be null to query the sizes; nv is 8 (or 4 in 2-D). */
+int nekmesh_ma2_read(const char *path, int *nel, int *nv, int64_t *vertex, int *part);
 /* Writes a #v001 .co2 file, as tools/gencon dmpfile does. */
 int nekmesh_co2_write(const char *path, const int *nelgt, const int *nelgv, const int *nv,
                       const int64_t *vertex);

@@ -48,6 +48,7 @@ SIGNATURES = {
     "nekmesh_re2_close": [_I64P],
     "nekmesh_co2_read": [C.c_char_p, _IP, _IP, _IP, _P],
     "nekmesh_co2_write": [C.c_char_p, _IP, _IP, _IP, _P],
+    "nekmesh_ma2_read": [C.c_char_p, _IP, _IP, _P, _P],
     "nekmesh_connect": [_IP, _IP, _P, _P, _P, _P, _P, _DP, _P, _I64P],
     "nekmesh_setvert3d": [_IP, _IP, _P, _P, _I64P],
     "nekmesh_check_p_bc": [_IP, _IP, C.c_char_p, _P],

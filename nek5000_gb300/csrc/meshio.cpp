@@ -511,6 +511,35 @@ int nekmesh_co2_read(const char* path, int* nelgt, int* nelgv, int* nv, int64_t*
   return NEKGPU_OK;
 }
 
+int nekmesh_ma2_read(const char* path, int* nel, int* nv, int64_t* vertex, int* part) {
+  std::vector<unsigned char> buf;
+  if (!path || !slurp(path, buf)) return fail(NEKGPU_EIO, std::string("cannot read ") + (path ? path : "(null)"));
+  if (buf.size() < 136) return fail(NEKGPU_EIO, "ma2: file shorter than its header");
+  const std::string hdr(reinterpret_cast<const char*>(buf.data()), 132);
+  int64_t ne = 0;
+  if (hdr.compare(0, 2, "#v") != 0 || !field_int(hdr, 5, 17, &ne) || ne <= 0)
+    return fail(NEKGPU_EIO, "ma2: unreadable header (format a5,7i12)");
+  Words w;
+  w.p = buf.data();
+  w.size = buf.size();
+  w.wd = 4;
+  if (!byte_order(buf.data() + 132, &w.swap)) return fail(NEKGPU_EIO, "ma2: byte-order test value not found");
+  const size_t body = buf.size() - 136;
+  if (body % ((size_t)ne * 4) != 0) return fail(NEKGPU_EIO, "ma2: records do not fill the file");
+  const int64_t per = (int64_t)(body / ((size_t)ne * 4));  // partition + vertices
+  if (per != 5 && per != 9) return fail(NEKGPU_EIO, "ma2: records of neither 4 nor 8 vertices");
+  if (nel) *nel = (int)ne;
+  if (nv) *nv = (int)(per - 1);
+  for (int64_t e = 0; e < ne; ++e) {
+    const size_t off = 136 + (size_t)(e * per) * 4;
+    if (part) part[e] = (int)(int32_t)w.u32(off);
+    if (vertex)
+      for (int64_t k = 0; k < per - 1; ++k)
+        vertex[(size_t)(e * (per - 1) + k)] = (int64_t)(int32_t)w.u32(off + 4 * (size_t)(k + 1));
+  }
+  return NEKGPU_OK;
+}
+
 int nekmesh_co2_write(const char* path, const int* nelgt, const int* nelgv, const int* nv,
                       const int64_t* vertex) {
   if (!path || !nelgt || !nelgv || !nv || !vertex || *nelgt <= 0 || *nelgv <= 0 ||

@@ -3,7 +3,7 @@ path takes (python side of include/nekmesh.h; the work is done by the
 library's host code).
 
     M = load_mesh("case.re2", N=7)             # connectivity from coordinates
-    M = load_mesh("case.re2", N=7, co2="case.co2")
+    M = load_mesh("case.re2", N=7, co2="case.co2")   # or ma2="case.ma2"
     h = NekGpu(0); h.setup(M["lx1"], M["nel"], M["D"], M["g"], M["bm1"], M["glo_num"])
 
 load_mesh returns the same keys as mesh.box_mesh (lx1, nel, n, D, g, bm1,
@@ -89,6 +89,19 @@ def read_co2(path: str) -> dict:
     _check(L.nekmesh_co2_read(str(path).encode(), C.byref(ne), C.byref(nev), C.byref(nv),
                               _p(vertex)))
     return dict(nelgt=ne.value, nelgv=nev.value, nv=nv.value, vertex=vertex)
+
+
+def read_ma2(path: str) -> dict:
+    """A .ma2 map file (core/map2.f read_map): vertex ids (nel, nv) and the
+    0-based partition of every element."""
+    L = _lib()
+    ne, nv = C.c_int(), C.c_int()
+    _check(L.nekmesh_ma2_read(str(path).encode(), C.byref(ne), C.byref(nv), None, None))
+    vertex = np.zeros((ne.value, nv.value), dtype=np.int64)
+    part = np.zeros(ne.value, dtype=np.int32)
+    _check(L.nekmesh_ma2_read(str(path).encode(), C.byref(ne), C.byref(nv), _p(vertex),
+                              _p(part)))
+    return dict(nel=ne.value, nv=nv.value, vertex=vertex, part=part)
 
 
 def write_co2(path: str, vertex, nelgv: int | None = None) -> None:
@@ -197,7 +210,7 @@ def _dsop(glo, u, op):
 
 
 def load_mesh(re2: str, N: int, co2: str | None = None, field: int = 0,
-              dirichlet=DIRICHLET_VELOCITY, tol: float = 0.2) -> dict:
+              dirichlet=DIRICHLET_VELOCITY, tol: float = 0.2, ma2: str | None = None) -> dict:
     """The operator data of a .re2 mesh at polynomial order N (lx1 = N+1):
     GLL coordinates (genxyz), geometric factors and mass, global numbering
     (the .co2 file when given, else connectivity from the corners), the mask
@@ -220,6 +233,11 @@ def load_mesh(re2: str, N: int, co2: str | None = None, field: int = 0,
         if C2["nelgt"] != ne or C2["nv"] != 8:
             raise ValueError("the .co2 file does not match the mesh")
         vertex = C2["vertex"]
+    elif ma2 is not None:
+        M2 = read_ma2(ma2)
+        if M2["nel"] != ne or M2["nv"] != 8:
+            raise ValueError("the .ma2 file does not match the mesh")
+        vertex = M2["vertex"]
     else:
         vertex, _ = connect(R["xc"], R["yc"], R["zc"], cbc, bc, tol)
     glo, ngv = setvert3d(nx, vertex)

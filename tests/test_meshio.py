@@ -413,3 +413,28 @@ def test_spherical_faces_make_an_exact_shell(mio, tmp_path):
             np.testing.assert_allclose(rad[:, -1], ro, rtol=0, atol=1e-14)
     assert abs(vols[True] - exact) <= 1e-11 * exact, (vols[True], exact)  # 1.8e-13 at N = 7
     assert abs(vols[False] - exact) > 1e-1 * exact                          # 23 % off
+
+
+def test_ma2_reader(mio, tmp_path):
+    """A .ma2 map file as genmap writes it (#v001 header a5,7i12, the test
+    value, then partition and eight vertex ids per element, either byte
+    order): read back, and load_mesh numbers the mesh as from the corners."""
+    import struct
+    xc, yc, zc, lattice, bcs = box_elements(3, 2, 2)
+    p = tmp_path / "box.re2"
+    write_re2(p, xc, yc, zc, bcs)
+    M = mio.load_mesh(p, N=4)
+    part = np.arange(12) % 3
+    for big in (False, True):
+        e = ">" if big else "<"
+        hdr = f"#v001{12:12d}{M['vertex'].max():12d}{1:12d}{2:12d}{0:12d}{0:12d}{0:12d}"
+        out = hdr.ljust(132).encode() + struct.pack(e + "f", 6.54321)
+        for q in range(12):
+            out += struct.pack(e + "9i", part[q], *M["vertex"][q])
+        m2 = tmp_path / f"box{big}.ma2"
+        m2.write_bytes(out)
+        R = mio.read_ma2(m2)
+        assert R["nel"] == 12 and R["nv"] == 8
+        assert np.array_equal(R["vertex"], M["vertex"]) and np.array_equal(R["part"], part)
+    M2 = mio.load_mesh(p, N=4, ma2=m2)
+    assert np.array_equal(M2["glo_num"], M["glo_num"])
