@@ -23,7 +23,7 @@ __global__ void __launch_bounds__(256)
                       const double* __restrict__ u, const double* __restrict__ G,
                       const double* __restrict__ D, int nel) {
   constexpr int P = NX * NX * NX, NXY = NX * NX, R = NX + 1;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  extern __shared__ __align__(128) unsigned char smem_raw[];
   double* sD = reinterpret_cast<double*>(smem_raw);  // D[i][l] at i*R + l
   double* su = sD + NX * R + threadIdx.y * 2 * P;
   double* sl = su + P;

@@ -343,7 +343,7 @@ __device__ __forceinline__ void axhelm_body(const AxArgs<T>& a, int blk, int tx,
 
 template <int NX, typename T, bool EXACT, bool FUSED>
 __global__ void __launch_bounds__(256) axhelm_kernel(const AxArgs<T> a) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ double red[32];
   if constexpr (FUSED) {
     if (a.cg->done) return;  // uniform over the grid: nothing to do after convergence

@@ -54,7 +54,7 @@ __global__ void gs_cg_weights_kernel(const int* __restrict__ start, const int* _
 
 int gs_setup(GsMaps& gs, const int64_t* glo_num, int64_t n, int nx1, std::string& err) {
   gs_free(gs);
-  if (n >= (int64_t)INT32_MAX) {
+  if (n < 0 || n >= (int64_t)INT32_MAX) {
     err = "gs_setup: more than 2^31-1 local points";
     return -1;
   }
@@ -71,8 +71,9 @@ int gs_setup(GsMaps& gs, const int64_t* glo_num, int64_t n, int nx1, std::string
         gmax = std::max(gmax, glo_num[i]);
       }
     pr.resize((size_t)cnt_n);
-    if (cnt_n && gmax - gmin < 4 * n) {
-      std::vector<int> bucket((size_t)(gmax - gmin + 2), 0);
+    const uint64_t span = cnt_n ? (uint64_t)gmax - (uint64_t)gmin : 0;
+    if (cnt_n && span < (uint64_t)(4 * n)) {
+      std::vector<int> bucket((size_t)span + 2, 0);
       for (int64_t i = 0; i < n; ++i)
         if (glo_num[i] != 0) ++bucket[(size_t)(glo_num[i] - gmin + 1)];
       for (size_t b = 1; b < bucket.size(); ++b) bucket[b] += bucket[b - 1];

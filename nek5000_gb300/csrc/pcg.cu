@@ -643,8 +643,6 @@ template <typename T>
 PcgResult pcg_solve(Handle& h, const OpData<T>& op, PcgWork<T>& wk, T* x, const T* f,
                     const Coef<T>& c, const T* mask, const T* mult, const T* binv, double tin,
                     int maxiter, int istep, bool exact, const T* dpre) {
-  Mesh& m = h.mesh;
-  cudaStream_t s = h.stream;
   bool trivial = false;
   PcgResult res = pcg_prepare<T>(h, wk, x, f, c, mask, mult, tin, maxiter, istep, dpre, &trivial);
   if (res.status || trivial) return res;
