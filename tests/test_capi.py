@@ -58,3 +58,13 @@ def test_init_without_gpu_fails_cleanly(lib):
     h = C.c_int64(0)
     rc = lib.nekgpu_init(C.byref(C.c_int(0)), C.byref(h))
     assert rc in (-3, -1)
+
+
+def test_integration_bindings_name_declared_entry_points():
+    """Every bind(C) name of the Fortran interface module in INTEGRATION.md is
+    an entry point the headers declare (the binding a maintainer copies must
+    link)."""
+    doc = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    names = set(re.findall(r'bind\(C,\s*name="(\w+)"\)', doc))
+    assert names, "no bind(C) names found"
+    assert names <= set(declared_symbols()), sorted(names - set(declared_symbols()))
