@@ -68,3 +68,16 @@ def test_integration_bindings_name_declared_entry_points():
     names = set(re.findall(r'bind\(C,\s*name="(\w+)"\)', doc))
     assert names, "no bind(C) names found"
     assert names <= set(declared_symbols()), sorted(names - set(declared_symbols()))
+
+
+def test_documented_entry_points_exist():
+    """Every nekgpu_* / nekmesh_* name the design doc and INTEGRATION.md mention
+    is declared (names ending in '_' stand for a family)."""
+    syms = set(declared_symbols())
+    for f in ("DESIGN.md", "INTEGRATION.md"):
+        text = open(os.path.join(ROOT, f)).read()
+        for name in set(re.findall(r"\b(nek(?:gpu|mesh)_[a-z0-9_]+)\b", text)):
+            if name.endswith("_"):
+                assert any(s.startswith(name) for s in syms), (f, name)
+            else:
+                assert name in syms, (f, name)
