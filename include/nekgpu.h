@@ -110,6 +110,18 @@ int nekgpu_hmh_gmres_dev(const int64_t *handle, double *res, const double *h1, c
                          const double *wt, const double *mask, const double *tol,
                          const int *maxit, const int *kmax, const int *null_space, int *niter,
                          double *div0, double *rnorm);
+/* The pressure solve's other Krylov method, hmh_flex_cg (core/hmholtz.f:
+ * 2164-2289, param(42) = 2): flexible (Polak-Ribiere) preconditioned CG on
+ * the same operator, weights, stopping test, null-space handling and Jacobi
+ * stand-in preconditioner as nekgpu_hmh_gmres_dev.  A zero right-hand side
+ * returns x = 0 after no iteration. */
+int nekgpu_hmh_flex_cg_dev(const int64_t *handle, double *res, const double *h1,
+                           const double *h2, const double *wt, const double *mask,
+                           const double *tol, const int *maxit, const int *null_space,
+                           int *niter, double *div0, double *rnorm);
+int nekgpu_hmh_flex_cg(const int64_t *handle, double *res, const double *h1, const double *h2,
+                       const double *wt, const double *mask, const double *tol, const int *maxit,
+                       const int *null_space, int *niter, double *div0, double *rnorm);
 /* The same on host arrays (copied in and out inside the call). */
 int nekgpu_hmh_gmres(const int64_t *handle, double *res, const double *h1, const double *h2,
                      const double *wt, const double *mask, const double *tol, const int *maxit,

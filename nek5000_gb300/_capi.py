@@ -62,6 +62,8 @@ SIGNATURES = {
     "nekgpu_setup": [_I64P, _IP, _IP, _P, _P, _P, _P, _P, _P, _P, _P, _P],
     "nekgpu_hmh_gmres_dev": [_I64P, _P, _P, _P, _P, _P, _DP, _IP, _IP, _IP, _IP, _DP, _DP],
     "nekgpu_hmh_gmres": [_I64P, _P, _P, _P, _P, _P, _DP, _IP, _IP, _IP, _IP, _DP, _DP],
+    "nekgpu_hmh_flex_cg_dev": [_I64P, _P, _P, _P, _P, _P, _DP, _IP, _IP, _IP, _DP, _DP],
+    "nekgpu_hmh_flex_cg": [_I64P, _P, _P, _P, _P, _P, _DP, _IP, _IP, _IP, _DP, _DP],
     "nekgpu_setup_xyz": [_I64P, _IP, _IP, _P, _P, _P, _P, _P, _P],
     "nekgpu_geom_update_dev": [_I64P, _P, _P, _P, _P],
     "nekgpu_geometry": [_I64P, _P, _P, _P, _P, _P, _P, _P],

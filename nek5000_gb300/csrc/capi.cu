@@ -744,6 +744,31 @@ int nekgpu_hmh_gmres(const int64_t* handle, double* res, const double* h1, const
   return rc2 ? rc2 : rc;
 }
 
+int nekgpu_hmh_flex_cg_dev(const int64_t* handle, double* res, const double* h1,
+                           const double* h2, const double* wt, const double* mask,
+                           const double* tol, const int* maxit, const int* null_space,
+                           int* niter, double* div0, double* rnorm);
+
+int nekgpu_hmh_flex_cg(const int64_t* handle, double* res, const double* h1, const double* h2,
+                       const double* wt, const double* mask, const double* tol, const int* maxit,
+                       const int* null_space, int* niter, double* div0, double* rnorm) {
+  GET_HANDLE(handle);
+  NEED_MESH();
+  if (check_n(H, res) || check_n(H, h1) || check_n(H, h2) || check_n(H, wt) || check_n(H, mask))
+    return NEKGPU_EINVAL;
+  const int64_t n = H->mesh.n;
+  int rc;
+  if ((rc = h2d(H, H->io0, res, n)) || (rc = h2d(H, H->io1, h1, n)) ||
+      (rc = h2d(H, H->io2, h2, n)) || (rc = h2d(H, H->io4, wt, n)) ||
+      (rc = h2d(H, H->io7, mask, n)))
+    return rc;
+  rc = nekgpu_hmh_flex_cg_dev(handle, H->io0.ptr, H->io1.ptr, H->io2.ptr, H->io4.ptr,
+                              H->io7.ptr, tol, maxit, null_space, niter, div0, rnorm);
+  if (rc && rc != NEKGPU_ENOTCONV) return rc;
+  const int rc2 = d2h(H, res, H->io0.ptr, n);
+  return rc2 ? rc2 : rc;
+}
+
 int nekgpu_cggo_mixed_dev(const int64_t* handle, double* x, const double* f, const double* h1,
                           const double* h2, const double* mask, const double* mult,
                           const int* imsh, const double* tin, const int* maxit, const int* isd,

@@ -188,6 +188,71 @@ __global__ void resid_kernel(double* __restrict__ r, const double* __restrict__ 
     r[i] = __dadd_rn(res[i], -w[i]);
 }
 
+// Flexible CG (hmh_flex_cg): z = M r; t = r1 - r (sub2); partial sums
+// (z wt) r and (z wt) t; then r1 = r (the lagged residual)
+__global__ void __launch_bounds__(kT) fcg_rho_kernel(double* __restrict__ z,
+                                                     const double* __restrict__ d,
+                                                     const double* __restrict__ r,
+                                                     double* __restrict__ r1,
+                                                     const double* __restrict__ wt, int64_t n,
+                                                     double* __restrict__ partial) {
+  __shared__ double red[kT / 32][2];
+  double a = 0.0, b = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)kT + threadIdx.x; i < n; i += (int64_t)gridDim.x * kT) {
+    const double ri = r[i];
+    const double zz = __dmul_rn(d[i], ri);
+    const double t = __dsub_rn(r1[i], ri);
+    const double zw = __dmul_rn(zz, wt[i]);
+    a += __dmul_rn(zw, ri);
+    b += __dmul_rn(zw, t);
+    z[i] = zz;
+    r1[i] = ri;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+    b += __shfl_xor_sync(0xffffffffu, b, o);
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) {
+    red[wid][0] = a;
+    red[wid][1] = b;
+  }
+  __syncthreads();
+  if (threadIdx.x < 2) {
+    double s = 0.0;
+    for (int q = 0; q < kT / 32; ++q) s += red[q][threadIdx.x];
+    partial[(int64_t)blockIdx.x * 2 + threadIdx.x] = s;
+  }
+}
+
+// p = beta p + z (add2s1)
+__global__ void fcg_p_kernel(double* __restrict__ p, const double* __restrict__ z, double beta,
+                             int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = __dadd_rn(__dmul_rn(beta, p[i]), z[i]);
+}
+
+// x += alpha p; r -= alpha w; partial = sum (r r) wt
+__global__ void __launch_bounds__(kT) fcg_xr_kernel(double* __restrict__ x,
+                                                    double* __restrict__ r,
+                                                    const double* __restrict__ p,
+                                                    const double* __restrict__ w, double alpha,
+                                                    const double* __restrict__ wt, int64_t n,
+                                                    double* __restrict__ partial) {
+  __shared__ double red[kT / 32];
+  double s = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)kT + threadIdx.x; i < n; i += (int64_t)gridDim.x * kT) {
+    x[i] = __dadd_rn(x[i], __dmul_rn(alpha, p[i]));
+    const double rr = __dsub_rn(r[i], __dmul_rn(alpha, w[i]));
+    r[i] = rr;
+    s += __dmul_rn(__dmul_rn(rr, rr), wt[i]);
+  }
+  s = block_reduce(s, red);
+  if (threadIdx.x == 0) partial[blockIdx.x] = s;
+}
+
 struct Gm {
   Handle& h;
   cudaStream_t s;
@@ -372,6 +437,101 @@ int gmres_solve(Handle& h, double* res, const double* h1, const double* h2, cons
   return 0;
 }
 
+// hmh_flex_cg (core/hmholtz.f:2164-2289) with the Jacobi preconditioner:
+// flexible (Polak-Ribiere) PCG on the same operator and weights as
+// gmres_solve.  res: in the right-hand side, out the solution.  Returns 0,
+// -3, -4 or -5 as gmres_solve.
+int flex_cg_solve(Handle& h, double* res, const double* h1, const double* h2, const double* wt,
+                  const double* mask, double tol, int maxit, bool null_space, int* niter,
+                  double* div0_out, double* rnorm_out) {
+  Mesh& msh = h.mesh;
+  const int64_t n = msh.n;
+  cudaStream_t s = h.stream;
+  Gm g{h, s, n, nblocks(n), {}};
+  const int nb = g.nb;
+  // r, r1 (lagged residual), p, z, w: work vectors of the GMRES pool
+  if (h.gm_Z.ensure((size_t)3 * n) || h.gm_r.ensure(n) || h.gm_w.ensure(n) || h.gm_d.ensure(n) ||
+      h.red.ensure((size_t)nb * kDots)) {
+    set_error(h, "flex cg: device allocation failed");
+    return -4;
+  }
+  Coef<double> c;
+  if (detect_coef<double>(h, h1, h2, n, c)) {
+    set_error(h, "flex cg: coefficient scan failed");
+    return -3;
+  }
+  if (setprec_f64(h, h.gm_d.ptr, c)) {
+    set_error(h, "flex cg: setprec failed");
+    return -3;
+  }
+  double *r = h.gm_r.ptr, *w = h.gm_w.ptr, *r1 = h.gm_Z.ptr, *p = r1 + n, *z = r1 + 2 * n;
+  const double* d = h.gm_d.ptr;
+  cudaMemcpyAsync(r, res, n * sizeof(double), cudaMemcpyDeviceToDevice, s);
+  cudaMemsetAsync(res, 0, n * sizeof(double), s);
+  cudaMemsetAsync(r1, 0, 2 * n * sizeof(double), s);  // r1 and p
+  count_launch();
+  wdot_kernel<<<nb, kT, 0, s>>>(r, wt, r, n, h.red.ptr);  // glsc3(r, wt, r)
+  double t = 0.0;
+  if (g.sums(1, 1, &t)) return -3;
+  const double div0 = std::sqrt(t / msh.vol);
+  const double tolpss = tol < 0 ? std::fabs(tol) * div0 : std::fabs(tol);
+  double rho1 = 1.0, rnorm = div0;
+  int iter = 0;
+  // a zero right-hand side is solved by x = 0 (the reference's loop would
+  // divide 0 by 0)
+  for (int k = 1; k <= maxit && div0 != 0.0; ++k) {
+    count_launch();
+    fcg_rho_kernel<<<nb, kT, 0, s>>>(z, d, r, r1, wt, n, h.red.ptr);
+    double rr[2];
+    if (g.sums(2, 2, rr)) return -3;
+    const double rho0 = rho1;
+    rho1 = rr[0];
+    const double beta = -rr[1] / rho0;
+    count_launch();
+    fcg_p_kernel<<<nb, kT, 0, s>>>(p, z, beta, n);
+    cudaError_t e = h.exact ? launch_axhelm<double, true>(msh, msh.f64, w, p, c, s)
+                            : launch_axhelm<double, false>(msh, msh.f64, w, p, c, s);
+    if (e != cudaSuccess) {
+      set_error(h, std::string("flex cg: operator launch: ") + cudaGetErrorString(e));
+      return -3;
+    }
+    gs_op<double>(msh.gs, w, 0, s);
+    count_launch(2);
+    mask_kernel<<<nb, kT, 0, s>>>(w, mask, n);
+    wdot_kernel<<<nb, kT, 0, s>>>(w, wt, p, n, h.red.ptr);  // glsc3(w, wt, p)
+    double den = 0.0;
+    if (g.sums(1, 1, &den)) return -3;
+    const double alpha = rho1 / den;
+    count_launch();
+    fcg_xr_kernel<<<nb, kT, 0, s>>>(res, r, p, w, alpha, wt, n, h.red.ptr);
+    double rn = 0.0;
+    if (g.sums(1, 1, &rn)) return -3;
+    rnorm = std::sqrt(rn / msh.vol);
+    ++iter;
+    if (rnorm < tolpss) break;
+  }
+  if (null_space) {  // ortho on the solution
+    count_launch();
+    sum_kernel<<<nb, kT, 0, s>>>(res, n, h.red.ptr);
+    double sm = 0.0;
+    if (g.sums(1, 1, &sm)) return -3;
+    count_launch();
+    cadd_kernel<<<nb, kT, 0, s>>>(res, -(sm / (double)n), n);
+  }
+  if (cudaStreamSynchronize(s) != cudaSuccess) {
+    set_error(h, std::string("flex cg: ") + cudaGetErrorString(cudaGetLastError()));
+    return -3;
+  }
+  *niter = iter;
+  *div0_out = div0;
+  *rnorm_out = rnorm;
+  if (!(rnorm < tolpss) && div0 != 0.0) {
+    set_error(h, "flex cg: iteration cap reached above the tolerance");
+    return -5;
+  }
+  return 0;
+}
+
 }  // namespace nekgpu
 
 // ---------------------------------------------------------------------------
@@ -405,5 +565,26 @@ extern "C" int nekgpu_hmh_gmres_dev(const int64_t* handle, double* res, const do
   if (rc == -5) return handle_fail(H, NEKGPU_ENOTCONV, H->err);
   if (rc) return handle_fail(H, rc == -4 ? NEKGPU_ENOMEM : NEKGPU_ECUDA,
                              H->err.empty() ? "gmres failed" : H->err);
+  return NEKGPU_OK;
+}
+
+extern "C" int nekgpu_hmh_flex_cg_dev(const int64_t* handle, double* res, const double* h1,
+                                      const double* h2, const double* wt, const double* mask,
+                                      const double* tol, const int* maxit, const int* null_space,
+                                      int* niter, double* div0, double* rnorm) {
+  Handle* H = handle_lookup(handle);
+  if (!H) return handle_fail(nullptr, NEKGPU_EHANDLE, "unknown handle");
+  if (cudaSetDevice(H->device) != cudaSuccess)
+    return handle_fail(H, NEKGPU_ECUDA, "cudaSetDevice failed");
+  if (!H->has_mesh) return handle_fail(H, NEKGPU_ENOSETUP, "mesh not set up (nekgpu_setup)");
+  if (!res || !h1 || !h2 || !wt || !mask || !tol || !maxit || !niter || !div0 || !rnorm)
+    return handle_fail(H, NEKGPU_EINVAL, "null argument");
+  if (*maxit < 1) return handle_fail(H, NEKGPU_EINVAL, "maxit must be positive");
+  H->err.clear();
+  const int rc = flex_cg_solve(*H, res, h1, h2, wt, mask, *tol, *maxit,
+                               null_space && *null_space != 0, niter, div0, rnorm);
+  if (rc == -5) return handle_fail(H, NEKGPU_ENOTCONV, H->err);
+  if (rc) return handle_fail(H, rc == -4 ? NEKGPU_ENOMEM : NEKGPU_ECUDA,
+                             H->err.empty() ? "flex cg failed" : H->err);
   return NEKGPU_OK;
 }

@@ -224,6 +224,10 @@ PcgResult pcg_prepare(Handle& h, PcgWork<T>& wk, T* x, const T* f, const Coef<T>
                       const T* mask, const T* mult, double tin, int maxiter, int istep,
                       const T* dpre, bool* trivial);
 int pcg_vec_blocks(int64_t n);
+// hmh_flex_cg with the Jacobi preconditioner (gmres.cu); 0, -3, -4 or -5.
+int flex_cg_solve(Handle& h, double* res, const double* h1, const double* h2, const double* wt,
+                  const double* mask, double tol, int maxit, bool null_space, int* niter,
+                  double* div0, double* rnorm);
 // hmh_gmres with the Jacobi preconditioner (gmres.cu); 0, -3, -4 or -5.
 int gmres_solve(Handle& h, double* res, const double* h1, const double* h2, const double* wt,
                 const double* mask, double tol, int maxit, int m, bool null_space, int* niter,

@@ -176,6 +176,20 @@ class NekGpu:
         self._check(rc, allow=(_capi.ENOTCONV,))
         return it.value, d0.value, rn.value, rc
 
+    def hmh_flex_cg(self, res, h1, h2, wt, mask, tol, maxit=10 ** 6, null_space=False):
+        """The pressure solve's flexible CG (res: rhs in, solution out; all
+        device or all host arrays).  Returns (iterations, div0, rnorm, status)."""
+        dev = [_is_dev(t) for t in (res, h1, h2, wt, mask)]
+        if any(dev) and not all(dev):
+            raise TypeError("hmh_flex_cg takes all device or all host arrays")
+        fn = self._L.nekgpu_hmh_flex_cg_dev if dev[0] else self._L.nekgpu_hmh_flex_cg
+        it, d0, rn = _cint(0), _cdouble(0), _cdouble(0)
+        rc = fn(C.byref(self._h), _ptr(res), _ptr(h1), _ptr(h2), _ptr(wt), _ptr(mask),
+                C.byref(_cdouble(tol)), C.byref(_cint(int(maxit))),
+                C.byref(_cint(int(bool(null_space)))), C.byref(it), C.byref(d0), C.byref(rn))
+        self._check(rc, allow=(_capi.ENOTCONV,))
+        return it.value, d0.value, rn.value, rc
+
     def setup_xyz(self, lx1: int, nel: int, D, w, x, y, z, glo_num):
         """setup with G1..G6 and bm1 computed on the GPU from the GLL
         coordinates x, y, z ((n,) numpy each) and the GLL weights w (lx1)."""

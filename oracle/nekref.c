@@ -1577,3 +1577,66 @@ int ref_gmres(const ref_ops *ops, double *res, const double *h1, const double *h
   free(gam);
   return iter;
 }
+
+/* ========================================================================
+ * hmh_flex_cg -- core/hmholtz.f:2164-2289 (see nekref.h), M = diag
+ * ====================================================================== */
+int ref_flex_cg(const ref_ops *ops, double *res, const double *h1, const double *h2,
+                const double *wt, const double *mask, double tol, int maxit, int null_space,
+                double *div0_out, double *rnorm_out) {
+  const int64_t n = ops->n;
+  double *d = (double *)malloc(sizeof(double) * n);
+  double *r = (double *)malloc(sizeof(double) * n);
+  double *r1 = (double *)calloc((size_t)n, sizeof(double));
+  double *p = (double *)calloc((size_t)n, sizeof(double));
+  double *z = (double *)malloc(sizeof(double) * n);
+  double *w = (double *)malloc(sizeof(double) * n);
+  ref_setprec(ops, d, h1, h2);
+  for (int64_t i = 0; i < n; ++i) {
+    r[i] = res[i];
+    res[i] = 0.0;
+  }
+  double rho1 = 1.0, t;
+  GLOBAL_SUM(ops, t, r[i] * wt[i] * r[i]); /* glsc3(r, wt, r) */
+  const double div0 = sqrt(t / ops->vol);
+  const double tolpss = tol < 0 ? fabs(tol) * div0 : fabs(tol);
+  double rnorm = div0;
+  int iter = 0;
+  /* a zero right-hand side is solved by x = 0 after no iteration (the
+     reference's loop would form 0/0 there) */
+  for (int k = 1; k <= maxit && div0 != 0.0; ++k) {
+    for (int64_t i = 0; i < n; ++i) z[i] = d[i] * r[i]; /* z = M r */
+    for (int64_t i = 0; i < n; ++i) r1[i] = r1[i] - r[i]; /* sub2 */
+    const double rho0 = rho1;
+    GLOBAL_SUM(ops, rho1, z[i] * wt[i] * r[i]);
+    double rho2;
+    GLOBAL_SUM(ops, rho2, z[i] * wt[i] * r1[i]);
+    rho2 = -rho2;
+    const double beta = rho2 / rho0;
+    for (int64_t i = 0; i < n; ++i) r1[i] = r[i];
+    for (int64_t i = 0; i < n; ++i) p[i] = beta * p[i] + z[i]; /* add2s1 */
+    gm_ax(ops, w, p, h1, h2, mask);
+    double den;
+    GLOBAL_SUM(ops, den, w[i] * wt[i] * p[i]);
+    const double alpha = rho1 / den;
+    for (int64_t i = 0; i < n; ++i) {
+      res[i] = res[i] + alpha * p[i];
+      r[i] = r[i] - alpha * w[i];
+    }
+    double rn;
+    GLOBAL_SUM(ops, rn, r[i] * r[i] * wt[i]);
+    rnorm = sqrt(rn / ops->vol);
+    ++iter;
+    if (rnorm < tolpss) break;
+  }
+  gm_ortho(ops, res, null_space);
+  if (div0_out) *div0_out = div0;
+  if (rnorm_out) *rnorm_out = rnorm;
+  free(d);
+  free(r);
+  free(r1);
+  free(p);
+  free(z);
+  free(w);
+  return iter;
+}

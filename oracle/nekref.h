@@ -122,6 +122,16 @@ int ref_gmres(const ref_ops *ops, double *res, const double *h1, const double *h
               const double *wt, const double *mask, double tol, int maxit, int m, int null_space,
               double *div0, double *rnorm);
 
+/* hmh_flex_cg (hmholtz.f:2164-2289): the pressure solve's flexible
+ * (Polak-Ribiere) preconditioned CG, param(42) = 2, on the same ax() and
+ * weights as ref_gmres, with the same Jacobi stand-in for the reference's
+ * multigrid preconditioner; ortho() on the result when null_space is set.
+ * res: in the right-hand side, out the solution.  tol as ref_gmres.
+ * Returns the iteration count. */
+int ref_flex_cg(const ref_ops *ops, double *res, const double *h1, const double *h2,
+                const double *wt, const double *mask, double tol, int maxit, int null_space,
+                double *div0, double *rnorm);
+
 /* local_grad3 (navier5.f:428) / local_grad3_t (navier1.f:4669), one element */
 void ref_local_grad3(double *ur, double *us, double *ut, const double *u, int N,
                      const double *d, const double *dt);

@@ -92,6 +92,9 @@ def lib():
             L.ref_gmres.argtypes = [_vp, _dp, _dp, _dp, _dp, _dp, C.c_double, C.c_int, C.c_int,
                                     C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
             L.ref_gmres.restype = C.c_int
+            L.ref_flex_cg.argtypes = [_vp, _dp, _dp, _dp, _dp, _dp, C.c_double, C.c_int, C.c_int,
+                                      C.POINTER(C.c_double), C.POINTER(C.c_double)]
+            L.ref_flex_cg.restype = C.c_int
             L.ref_local_grad3.argtypes = [_dp, _dp, _dp, _dp, C.c_int, _dp, _dp]
             L.ref_local_grad3_t.argtypes = [_dp, _dp, _dp, _dp, C.c_int, _dp, _dp, _dp]
             L.ref_mxm.argtypes = [_dp, C.c_int, _dp, C.c_int, _dp, C.c_int]
@@ -251,6 +254,15 @@ class Ops:
         d0, rn = C.c_double(0), C.c_double(0)
         it = lib().ref_gmres(self.h, x, _c(h1), _c(h2), _c(wt), _c(mask), float(tol),
                              int(maxit), int(m), int(bool(null_space)), C.byref(d0), C.byref(rn))
+        return x, it, d0.value, rn.value
+
+    def flex_cg(self, rhs, h1, h2, wt, mask, tol, maxit=10 ** 6, null_space=False):
+        """hmh_flex_cg with the Jacobi stand-in preconditioner (nekref.h).
+        Returns (x, iterations, div0, rnorm)."""
+        x = np.array(rhs, dtype=np.float64, copy=True)
+        d0, rn = C.c_double(0), C.c_double(0)
+        it = lib().ref_flex_cg(self.h, x, _c(h1), _c(h2), _c(wt), _c(mask), float(tol),
+                               int(maxit), int(bool(null_space)), C.byref(d0), C.byref(rn))
         return x, it, d0.value, rn.value
 
     def hmholtz(self, rhs, h1, h2, mask, mult, binv, tli, maxit=10 ** 9, maxcg=900, istep=0):

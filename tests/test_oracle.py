@@ -277,3 +277,30 @@ def test_gmres_restatement_solves_the_system(oracle):
     xq, itq, d0q, rnq = oq.gmres(g, np.ones(nq), np.zeros(nq), Q["mult"], Q["mask"], -1e-10,
                                  maxit=4000, null_space=True)
     assert rnq < 1e-10 * d0q and abs(np.mean(xq)) < 1e-14
+
+
+def test_flex_cg_restatement_solves_the_system(oracle):
+    """hmh_flex_cg restated (Jacobi stand-in preconditioner): its residual
+    norm is the true weighted residual, it agrees with GMRES on the same
+    system, the null-space case returns a zero-mean solution and a zero
+    right-hand side gives x = 0 after no iteration."""
+    from conftest import rng_unit_vector
+    P = oracle.box_problem(5, 3, 2, 2, v=rng_unit_vector(63))
+    n, ops = P["n"], P["ops"]
+    h1, h2 = np.ones(n), np.full(n, 2.0)
+    f = ops.dssum(P["bm1"] * np.random.default_rng(63).standard_normal(n)) * P["mask"]
+    x, it, d0, rn = ops.flex_cg(f, h1, h2, P["mult"], P["mask"], -1e-10)
+    r = f - ops.dssum(ops.axhelm(x, h1, h2)) * P["mask"]
+    true = np.sqrt(np.sum(r * r * P["mult"]) / np.sum(P["bm1"]))
+    assert rn < 1e-10 * d0 and abs(true - rn) <= 1e-3 * rn
+    xg, _, _, _ = ops.gmres(f, h1, h2, P["mult"], P["mask"], -1e-10, m=30)
+    assert np.linalg.norm(xg - x) <= 1e-8 * np.linalg.norm(x)
+    Q = oracle.box_problem(5, 2, 2, 2, dirichlet=(False,) * 6, v=rng_unit_vector(64))
+    nq, oq = Q["n"], Q["ops"]
+    g = oq.dssum(Q["bm1"] * np.random.default_rng(64).standard_normal(nq))
+    g = g - np.sum(g * Q["mult"]) / np.sum(Q["mult"])
+    xq, itq, d0q, rnq = oq.flex_cg(g, np.ones(nq), np.zeros(nq), Q["mult"], Q["mask"], -1e-10,
+                                   maxit=4000, null_space=True)
+    assert rnq < 1e-10 * d0q and abs(np.mean(xq)) < 1e-14
+    x0, it0, d00, _ = ops.flex_cg(np.zeros(n), h1, h2, P["mult"], P["mask"], -1e-10)
+    assert it0 == 0 and d00 == 0.0 and not np.any(x0)
