@@ -893,8 +893,9 @@ def run_velocity3(args):
 def run_pressure(args):
     """The pressure solve's Krylov method (hmh_gmres, restart 30) on the
     E=k^3, N Poisson problem (all-Dirichlet box, h1 = 1, h2 = 0, seed 0), to
-    1e-10 of the initial residual norm, beside FP64 Jacobi-PCG (cggo) on the
-    same system; both with the Jacobi preconditioner."""
+    1e-10 of the initial residual norm, beside FP64 Jacobi-PCG (cggo) and the
+    flexible CG (hmh_flex_cg) on the same system; all with the Jacobi
+    preconditioner."""
     import torch
     ws, rank, local, pg = dist_setup(args.gpus)
     torch.cuda.set_device(local)
@@ -917,8 +918,12 @@ def run_pressure(args):
         x = torch.zeros(n, dtype=torch.float64, device=f"cuda:{local}")
         return lib.cggo(x, f, h1, h2, mask, mult, 1, -args.tol, 10 ** 6, 1, binv, maxcg=10 ** 6)
 
+    def flex():
+        x = f.clone()
+        return lib.hmh_flex_cg(x, h1, h2, mult, mask, -args.tol, maxit=10 ** 6)
+
     out = {}
-    for name, fn in (("gmres", gmres), ("cggo", cg)):
+    for name, fn in (("gmres", gmres), ("cggo", cg), ("flex_cg", flex)):
         for _ in range(args.warmup):
             r = fn()
         torch.cuda.synchronize()
@@ -940,6 +945,7 @@ def run_pressure(args):
                                                                     N=args.N)),
                        "n_points": n, "tol": f"{args.tol:g} x initial rnorm"},
             "gmres": out["gmres"], "cggo_same_system": out["cggo"],
+            "flex_cg_same_system": out["flex_cg"],
             "clocks": out["gmres"]["clocks"]}
     if rank == 0 and ws == 1 and not args.no_cpu:
         from oracle import nekref
