@@ -800,6 +800,9 @@ struct ref_ops {
 };
 
 const ref_gs *ref_ops_gs(const ref_ops *ops) { return ops->gs; }
+int ref_ops_nx1(const ref_ops *ops) { return ops->nx1; }
+int ref_ops_nel(const ref_ops *ops) { return ops->nel; }
+int64_t ref_ops_n(const ref_ops *ops) { return ops->n; }
 
 /* Global sum of a per-point expression, formed as contiguous element-block
  * partial sums in block order (the P-rank gop pattern).  EXPR(i) must be the
@@ -1461,9 +1464,9 @@ static void gm_ortho(const ref_ops *ops, double *z, int null_space) {
   for (int64_t i = 0; i < ops->n; ++i) z[i] = z[i] + (-rlam);
 }
 
-int ref_gmres(const ref_ops *ops, double *res, const double *h1, const double *h2,
-              const double *wt, const double *mask, double tol, int maxit, int m, int null_space,
-              double *div0_out, double *rnorm_out) {
+static int gmres_body(const ref_ops *ops, const ref_h1mg *mg, double *res, const double *h1,
+                      const double *h2, const double *wt, const double *mask, double tol,
+                      int maxit, int m, int null_space, double *div0_out, double *rnorm_out) {
   const int64_t n = ops->n;
   if (m < 1) m = 1;
   double *d = (double *)malloc(sizeof(double) * n);
@@ -1502,7 +1505,12 @@ int ref_gmres(const ref_ops *ops, double *res, const double *h1, const double *h
     for (j = 0; j < m; ++j) {
       ++iter;
       double *zj = Z + (size_t)n * j, *vj = V + (size_t)n * j;
-      for (int64_t i = 0; i < n; ++i) zj[i] = d[i] * (1.0 * vj[i]); /* M (mu v_j) */
+      if (mg) { /* h1mg_solve(z_j, w = mu v_j); w is masked in place, then overwritten */
+        for (int64_t i = 0; i < n; ++i) w[i] = 1.0 * vj[i];
+        ref_h1mg_solve(mg, zj, w);
+      } else {
+        for (int64_t i = 0; i < n; ++i) zj[i] = d[i] * (1.0 * vj[i]); /* M (mu v_j) */
+      }
       gm_ortho(ops, zj, null_space);
       gm_ax(ops, w, zj, h1, h2, mask);
       for (int iv = 0; iv <= j; ++iv) { /* h_ij = vlsc3(w, v_i, wt) */
@@ -1578,12 +1586,26 @@ int ref_gmres(const ref_ops *ops, double *res, const double *h1, const double *h
   return iter;
 }
 
+int ref_gmres(const ref_ops *ops, double *res, const double *h1, const double *h2,
+              const double *wt, const double *mask, double tol, int maxit, int m, int null_space,
+              double *div0_out, double *rnorm_out) {
+  return gmres_body(ops, NULL, res, h1, h2, wt, mask, tol, maxit, m, null_space, div0_out,
+                    rnorm_out);
+}
+
+int ref_gmres_h1mg(const ref_ops *ops, const ref_h1mg *mg, double *res, const double *h1,
+                   const double *h2, const double *wt, const double *mask, double tol, int maxit,
+                   int m, int null_space, double *div0_out, double *rnorm_out) {
+  return gmres_body(ops, mg, res, h1, h2, wt, mask, tol, maxit, m, null_space, div0_out,
+                    rnorm_out);
+}
+
 /* ========================================================================
  * hmh_flex_cg -- core/hmholtz.f:2164-2289 (see nekref.h), M = diag
  * ====================================================================== */
-int ref_flex_cg(const ref_ops *ops, double *res, const double *h1, const double *h2,
-                const double *wt, const double *mask, double tol, int maxit, int null_space,
-                double *div0_out, double *rnorm_out) {
+static int flex_body(const ref_ops *ops, const ref_h1mg *mg, double *res, const double *h1,
+                     const double *h2, const double *wt, const double *mask, double tol,
+                     int maxit, int null_space, double *div0_out, double *rnorm_out) {
   const int64_t n = ops->n;
   double *d = (double *)malloc(sizeof(double) * n);
   double *r = (double *)malloc(sizeof(double) * n);
@@ -1605,7 +1627,10 @@ int ref_flex_cg(const ref_ops *ops, double *res, const double *h1, const double 
   /* a zero right-hand side is solved by x = 0 after no iteration (the
      reference's loop would form 0/0 there) */
   for (int k = 1; k <= maxit && div0 != 0.0; ++k) {
-    for (int64_t i = 0; i < n; ++i) z[i] = d[i] * r[i]; /* z = M r */
+    if (mg) /* h1mg_solve(z, r): r is masked in place */
+      ref_h1mg_solve(mg, z, r);
+    else
+      for (int64_t i = 0; i < n; ++i) z[i] = d[i] * r[i]; /* z = M r */
     for (int64_t i = 0; i < n; ++i) r1[i] = r1[i] - r[i]; /* sub2 */
     const double rho0 = rho1;
     GLOBAL_SUM(ops, rho1, z[i] * wt[i] * r[i]);
@@ -1639,4 +1664,16 @@ int ref_flex_cg(const ref_ops *ops, double *res, const double *h1, const double 
   free(z);
   free(w);
   return iter;
+}
+
+int ref_flex_cg(const ref_ops *ops, double *res, const double *h1, const double *h2,
+                const double *wt, const double *mask, double tol, int maxit, int null_space,
+                double *div0_out, double *rnorm_out) {
+  return flex_body(ops, NULL, res, h1, h2, wt, mask, tol, maxit, null_space, div0_out, rnorm_out);
+}
+
+int ref_flex_cg_h1mg(const ref_ops *ops, const ref_h1mg *mg, double *res, const double *h1,
+                     const double *h2, const double *wt, const double *mask, double tol,
+                     int maxit, int null_space, double *div0_out, double *rnorm_out) {
+  return flex_body(ops, mg, res, h1, h2, wt, mask, tol, maxit, null_space, div0_out, rnorm_out);
 }

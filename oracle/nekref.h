@@ -144,6 +144,37 @@ void ref_mxm(const double *a, int n1, const double *b, int n2, double *c, int n3
 /* threads actually used by the OpenMP loops (1 without OpenMP) */
 int ref_max_threads(void);
 
+/* ---- the pressure preconditioner h1mg_solve (h1mg.c; core/hsmg.f) ------- */
+typedef struct ref_h1mg ref_h1mg;
+/* x, y, z: fine GLL coordinates; fbc: 6 face types per element (r-, r+, s-,
+ * s+, t-, t+; 0 shared, 1 Dirichlet, 2 Neumann); vertex: 8 vertex ids per
+ * element (tensor corner order).  NULL when lx1 < 3 or the coarse matrix is
+ * not positive definite. */
+ref_h1mg *ref_h1mg_create(const ref_ops *ops, const double *x, const double *y, const double *z,
+                          const int *fbc, const int64_t *vertex, int null_space);
+void ref_h1mg_free(ref_h1mg *mg);
+int ref_h1mg_levels(int lx1, int *order);
+/* z = M rhs (h1mg_solve, if_hybrid = .false.); rhs is masked in place */
+void ref_h1mg_solve(const ref_h1mg *mg, double *z, double *rhs);
+int ref_h1mg_nlev(const ref_h1mg *mg);
+int ref_h1mg_nx(const ref_h1mg *mg, int l);
+int64_t ref_h1mg_ncoarse(const ref_h1mg *mg);
+void ref_h1mg_level(const ref_h1mg *mg, int l, double *mask, double *rwt, double *swt);
+void ref_h1mg_schwarz(const ref_h1mg *mg, int l, double *e, double *r);
+void ref_h1mg_coarse(const ref_h1mg *mg, double *e, const double *r);
+/* hmh_gmres / hmh_flex_cg preconditioned by h1mg_solve */
+int ref_gmres_h1mg(const ref_ops *ops, const ref_h1mg *mg, double *res, const double *h1,
+                   const double *h2, const double *wt, const double *mask, double tol, int maxit,
+                   int m, int null_space, double *div0_out, double *rnorm_out);
+int ref_flex_cg_h1mg(const ref_ops *ops, const ref_h1mg *mg, double *res, const double *h1,
+                     const double *h2, const double *wt, const double *mask, double tol,
+                     int maxit, int null_space, double *div0_out, double *rnorm_out);
+
+/* sizes of an operator state */
+int ref_ops_nx1(const ref_ops *ops);
+int ref_ops_nel(const ref_ops *ops);
+int64_t ref_ops_n(const ref_ops *ops);
+
 #ifdef __cplusplus
 }
 #endif

@@ -58,6 +58,25 @@ def lib():
             L.ref_gs_nidx.restype = C.c_int64
             L.ref_gs_maps.argtypes = [_vp, _ip, _ip, _ip]
             L.ref_ops_create.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp, _dp, _ip, C.c_int]
+            _i32 = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+            L.ref_h1mg_create.argtypes = [_vp, _dp, _dp, _dp, _i32, _ip, C.c_int]
+            L.ref_h1mg_create.restype = _vp
+            L.ref_h1mg_free.argtypes = [_vp]
+            L.ref_h1mg_solve.argtypes = [_vp, _dp, _dp]
+            L.ref_h1mg_nlev.argtypes = [_vp]
+            L.ref_h1mg_nx.argtypes = [_vp, C.c_int]
+            L.ref_h1mg_ncoarse.argtypes = [_vp]
+            L.ref_h1mg_ncoarse.restype = C.c_int64
+            L.ref_h1mg_level.argtypes = [_vp, C.c_int, _vp, _vp, _vp]
+            L.ref_h1mg_schwarz.argtypes = [_vp, C.c_int, _dp, _dp]
+            L.ref_h1mg_coarse.argtypes = [_vp, _dp, _dp]
+            L.ref_h1mg_levels.argtypes = [C.c_int, _i32]
+            L.ref_gmres_h1mg.argtypes = [_vp, _vp, _dp, _dp, _dp, _dp, _dp, C.c_double, C.c_int,
+                                         C.c_int, C.c_int, C.POINTER(C.c_double),
+                                         C.POINTER(C.c_double)]
+            L.ref_flex_cg_h1mg.argtypes = [_vp, _vp, _dp, _dp, _dp, _dp, _dp, C.c_double, C.c_int,
+                                           C.c_int, C.POINTER(C.c_double),
+                                           C.POINTER(C.c_double)]
             L.ref_ops_create.restype = _vp
             L.ref_ops_free.argtypes = [_vp]
             L.ref_ops_gs.argtypes = [_vp]
@@ -247,22 +266,33 @@ class Ops:
                             _c(binv), C.byref(r0), C.byref(r2))
         return x, it, r0.value, r2.value
 
-    def gmres(self, rhs, h1, h2, wt, mask, tol, maxit=10 ** 6, m=30, null_space=False):
-        """hmh_gmres with the Jacobi stand-in preconditioner (nekref.h).
-        Returns (x, iterations, div0, rnorm)."""
+    def gmres(self, rhs, h1, h2, wt, mask, tol, maxit=10 ** 6, m=30, null_space=False, mg=None):
+        """hmh_gmres with the Jacobi stand-in preconditioner, or h1mg_solve
+        when mg (an H1mg) is given.  Returns (x, iterations, div0, rnorm)."""
         x = np.array(rhs, dtype=np.float64, copy=True)
         d0, rn = C.c_double(0), C.c_double(0)
-        it = lib().ref_gmres(self.h, x, _c(h1), _c(h2), _c(wt), _c(mask), float(tol),
-                             int(maxit), int(m), int(bool(null_space)), C.byref(d0), C.byref(rn))
+        if mg is None:
+            it = lib().ref_gmres(self.h, x, _c(h1), _c(h2), _c(wt), _c(mask), float(tol),
+                                 int(maxit), int(m), int(bool(null_space)), C.byref(d0),
+                                 C.byref(rn))
+        else:
+            it = lib().ref_gmres_h1mg(self.h, mg.h, x, _c(h1), _c(h2), _c(wt), _c(mask),
+                                      float(tol), int(maxit), int(m), int(bool(null_space)),
+                                      C.byref(d0), C.byref(rn))
         return x, it, d0.value, rn.value
 
-    def flex_cg(self, rhs, h1, h2, wt, mask, tol, maxit=10 ** 6, null_space=False):
-        """hmh_flex_cg with the Jacobi stand-in preconditioner (nekref.h).
-        Returns (x, iterations, div0, rnorm)."""
+    def flex_cg(self, rhs, h1, h2, wt, mask, tol, maxit=10 ** 6, null_space=False, mg=None):
+        """hmh_flex_cg with the Jacobi stand-in preconditioner, or h1mg_solve
+        when mg (an H1mg) is given.  Returns (x, iterations, div0, rnorm)."""
         x = np.array(rhs, dtype=np.float64, copy=True)
         d0, rn = C.c_double(0), C.c_double(0)
-        it = lib().ref_flex_cg(self.h, x, _c(h1), _c(h2), _c(wt), _c(mask), float(tol),
-                               int(maxit), int(bool(null_space)), C.byref(d0), C.byref(rn))
+        if mg is None:
+            it = lib().ref_flex_cg(self.h, x, _c(h1), _c(h2), _c(wt), _c(mask), float(tol),
+                                   int(maxit), int(bool(null_space)), C.byref(d0), C.byref(rn))
+        else:
+            it = lib().ref_flex_cg_h1mg(self.h, mg.h, x, _c(h1), _c(h2), _c(wt), _c(mask),
+                                        float(tol), int(maxit), int(bool(null_space)),
+                                        C.byref(d0), C.byref(rn))
         return x, it, d0.value, rn.value
 
     def hmholtz(self, rhs, h1, h2, mask, mult, binv, tli, maxit=10 ** 9, maxcg=900, istep=0):
@@ -274,6 +304,86 @@ class Ops:
                                int(min(maxit, 2 ** 31 - 1)), int(min(maxcg, 2 ** 31 - 1)),
                                int(istep), _c(binv), C.byref(r0), C.byref(r2))
         return u, rhs, it, r0.value, r2.value
+
+
+def face_types(nx1, nel, glo_num, mask):
+    """Face types per element (r-, r+, s-, s+, t-, t+) as get_fast_bc gives
+    them for the pressure (core/fast3d.f:802-870), read from the numbering
+    and the mask: 0 where the face's point (1, 1) is shared with another
+    element (interior or periodic face), else 1 where it is masked
+    (Dirichlet), else 2 (Neumann)."""
+    g = np.asarray(glo_num).reshape(nel, nx1, nx1, nx1)  # [e, k, j, i]
+    m = np.asarray(mask).reshape(nel, nx1, nx1, nx1)
+    _, inv, cnt = np.unique(g.reshape(-1), return_inverse=True, return_counts=True)
+    shared = (cnt[inv] > 1).reshape(g.shape)
+    n2 = nx1 - 1
+    pts = [(slice(None), 1, 1, 0), (slice(None), 1, 1, n2), (slice(None), 1, 0, 1),
+           (slice(None), 1, n2, 1), (slice(None), 0, 1, 1), (slice(None), n2, 1, 1)]
+    fbc = np.empty((nel, 6), dtype=np.int32)
+    for f, p in enumerate(pts):
+        fbc[:, f] = np.where(shared[p], 0, np.where(m[p] == 0.0, 1, 2))
+    return fbc
+
+
+class H1mg:
+    """The pressure preconditioner h1mg_solve (h1mg.c) on an Ops mesh:
+    x, y, z the fine GLL coordinates, fbc the face types (face_types),
+    vertex the 8 vertex ids per element (tensor corner order)."""
+
+    def __init__(self, ops, x, y, z, fbc, vertex, null_space=False):
+        self.ops = ops
+        self._keep = [_c(x), _c(y), _c(z)]
+        self.h = lib().ref_h1mg_create(ops.h, self._keep[0], self._keep[1], self._keep[2],
+                                       np.ascontiguousarray(fbc, dtype=np.int32).reshape(-1),
+                                       _c(vertex, np.int64).reshape(-1), int(bool(null_space)))
+        if not self.h:
+            raise ValueError("h1mg setup failed (lx1 < 3 or a singular coarse matrix)")
+
+    def __del__(self):
+        try:
+            lib().ref_h1mg_free(self.h)
+        except Exception:
+            pass
+
+    @property
+    def levels(self):
+        return [lib().ref_h1mg_nx(self.h, l) for l in range(lib().ref_h1mg_nlev(self.h))]
+
+    @property
+    def ncoarse(self):
+        return lib().ref_h1mg_ncoarse(self.h)
+
+    def level(self, l):
+        """(mask, rwt, swt) of level l (0 = coarsest; swt zero there)."""
+        n = self.levels[l] ** 3 * self.ops.nel
+        out = [np.zeros(n) for _ in range(3)]
+        lib().ref_h1mg_level(self.h, l, *[o.ctypes.data_as(C.c_void_p) for o in out])
+        return tuple(out)
+
+    def solve(self, rhs):
+        """z = M rhs; returns (z, rhs masked as the reference leaves it)."""
+        r = np.array(rhs, dtype=np.float64, copy=True)
+        z = np.zeros_like(r)
+        lib().ref_h1mg_solve(self.h, z, r)
+        return z, r
+
+    def schwarz(self, l, r):
+        r = np.array(r, dtype=np.float64, copy=True)
+        e = np.zeros_like(r)
+        lib().ref_h1mg_schwarz(self.h, l, e, r)
+        return e
+
+    def coarse(self, r):
+        r = np.ascontiguousarray(r, dtype=np.float64)
+        e = np.zeros_like(r)
+        lib().ref_h1mg_coarse(self.h, e, r)
+        return e
+
+
+def h1mg_levels(lx1):
+    o = np.zeros(4, dtype=np.int32)
+    lmax = lib().ref_h1mg_levels(int(lx1), o)
+    return [int(v) for v in o[:lmax]]
 
 
 class Projection:
