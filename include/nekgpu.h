@@ -122,6 +122,28 @@ int nekgpu_hmh_flex_cg_dev(const int64_t *handle, double *res, const double *h1,
 int nekgpu_hmh_flex_cg(const int64_t *handle, double *res, const double *h1, const double *h2,
                        const double *wt, const double *mask, const double *tol, const int *maxit,
                        const int *null_space, int *niter, double *div0, double *rnorm);
+/* The pressure preconditioner h1mg_solve (core/hsmg.f:1855-1949, with
+ * if_hybrid = .false. as hmh_gmres and hmh_flex_cg call it; setup h1mg_setup
+ * :2234-2270 and set_up_h1_crs, core/navier8.f:83-238): additive multilevel
+ * overlapping Schwarz on polynomial orders N, min(3, ...) and 1, with
+ * fast-diagonalisation local solves on elements extended by one layer and
+ * a Galerkin coarse solve on the vertices (exact: a dense inverse, so at
+ * most 12288 coarse unknowns).  Host arrays: x, y, z the GLL coordinates
+ * (xm1, ym1, zm1), glo_num the numbering given to nekgpu_setup, and either
+ * fbc (6 face types per element, r-, r+, s-, s+, t-, t+: 0 interior or
+ * periodic, 1 Dirichlet ('O'), 2 Neumann (wall); get_fast_bc,
+ * core/fast3d.f:802) or, with fbc null, the pressure mask they are read
+ * from (nekmesh_face_types).  *null_space != 0 when the pressure has a null
+ * space (no outflow): the coarse solve pins one vertex and removes the mean.
+ * Once set up, nekgpu_hmh_gmres(_dev) and nekgpu_hmh_flex_cg(_dev) use it
+ * instead of the Jacobi diagonal; nekgpu_h1mg_free returns to Jacobi; a new
+ * mesh drops it.  3 <= lx1 <= 12. */
+int nekgpu_h1mg_setup(const int64_t *handle, const double *x, const double *y, const double *z,
+                      const double *mask, const int64_t *glo_num, const int *fbc,
+                      const int *null_space);
+int nekgpu_h1mg_free(const int64_t *handle);
+/* z = M rhs on device arrays; rhs is masked in place, as h1mg_solve leaves it. */
+int nekgpu_h1mg_apply_dev(const int64_t *handle, double *z, double *rhs);
 /* The same on host arrays (copied in and out inside the call). */
 int nekgpu_hmh_gmres(const int64_t *handle, double *res, const double *h1, const double *h2,
                      const double *wt, const double *mask, const double *tol, const int *maxit,

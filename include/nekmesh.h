@@ -133,6 +133,32 @@ int nekmesh_genxyz(const int *nx, const int *nel, const double *zgll, const doub
                    const int *side, const double *curve, const char *ccurve, double *x, double *y,
                    double *z);
 
+/* ---- pressure preconditioner setup data (core/hsmg.f; host only) -------- */
+/* Level orders of h1mg_setup_mg_nx (:2272-2338): order[0..lmax-1], coarsest
+ * first; returns lmax (2 or 3) or NEKGPU_EINVAL (3 <= lx1 <= 12). */
+int nekmesh_h1mg_levels(const int *lx1, int *order);
+/* Face types as get_fast_bc gives them for the pressure, read from the
+ * numbering and mask: per element r-, r+, s-, s+, t-, t+; 0 when the face's
+ * point (1, 1) is shared with another element, else 1 when masked, else 2. */
+int nekmesh_face_types(const int *nx, const int *nel, const int64_t *glo_num, const double *mask,
+                       int *fbc);
+/* The setup nekgpu_h1mg_setup computes for level *level (0 = coarsest):
+ * *nx its points per direction; its mask, restriction weights (1 /
+ * multiplicity) and Schwarz weights (1 / overlap count; 0 on level 0), each
+ * nx^3 nel; lengths (may be null): per element the widths of the
+ * neighbours and of the element (swap_lengths, core/fast3d.f:1542), 9 per
+ * element: left r s t, middle r s t, right r s t. */
+int nekmesh_h1mg_level(const int *nx1, const int *nel, const int64_t *glo_num, const double *x,
+                       const double *y, const double *z, const double *mask, const int *fbc,
+                       const int *level, int *nx, double *lmask, double *rwt, double *swt,
+                       double *lengths);
+/* One 1-D fast-diagonalisation operator of order n (hsmg_setup_fast1d,
+ * core/hsmg.f:783-881) for face types lbc, rbc and widths ll, lm, lr: s the
+ * (n+3)^2 eigenvectors (column-major, column j = vector j, rows of excluded
+ * points zeroed), lam the n+3 eigenvalues ascending. */
+int nekmesh_fdm1d(const int *n, const int *lbc, const int *rbc, const double *ll,
+                  const double *lm, const double *lr, double *s, double *lam);
+
 #ifdef __cplusplus
 }
 #endif

@@ -64,6 +64,13 @@ SIGNATURES = {
     "nekgpu_hmh_gmres": [_I64P, _P, _P, _P, _P, _P, _DP, _IP, _IP, _IP, _IP, _DP, _DP],
     "nekgpu_hmh_flex_cg_dev": [_I64P, _P, _P, _P, _P, _P, _DP, _IP, _IP, _IP, _DP, _DP],
     "nekgpu_hmh_flex_cg": [_I64P, _P, _P, _P, _P, _P, _DP, _IP, _IP, _IP, _DP, _DP],
+    "nekgpu_h1mg_setup": [_I64P, _P, _P, _P, _P, _P, _P, _IP],
+    "nekgpu_h1mg_free": [_I64P],
+    "nekgpu_h1mg_apply_dev": [_I64P, _P, _P],
+    "nekmesh_h1mg_levels": [_IP, _P],
+    "nekmesh_face_types": [_IP, _IP, _P, _P, _P],
+    "nekmesh_h1mg_level": [_IP, _IP, _P, _P, _P, _P, _P, _P, _IP, _IP, _P, _P, _P, _P],
+    "nekmesh_fdm1d": [_IP, _IP, _IP, _DP, _DP, _DP, _P, _P],
     "nekgpu_setup_xyz": [_I64P, _IP, _IP, _P, _P, _P, _P, _P, _P],
     "nekgpu_geom_update_dev": [_I64P, _P, _P, _P, _P],
     "nekgpu_geometry": [_I64P, _P, _P, _P, _P, _P, _P, _P],

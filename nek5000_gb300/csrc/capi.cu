@@ -215,6 +215,7 @@ int handle_open(Handle& H, int device, cudaStream_t shared, std::string& err) {
 void handle_close(Handle& H) {
   cudaSetDevice(H.device);
   if (H.stream) cudaStreamSynchronize(H.stream);
+  H.mg.reset();
   gs_free(H.mesh.gs);
   H.mesh.f64.release();
   H.mesh.f32.release();
@@ -256,6 +257,7 @@ static int mesh_prepare(Handle& H, int lx1, int nel, const double* dxm1, std::st
   m.has_f32 = false;
   m.ax_sel[0] = m.ax_sel[1] = AxShapeSel();
   H.proj.clear();  // projection spaces belong to the old mesh
+  H.mg.reset();    // and so does the pressure preconditioner
   H.has_mesh = false;
   if (H.gexec) cudaGraphExecDestroy(H.gexec);
   H.gexec = nullptr;

@@ -10,11 +10,11 @@
 // arithmetic is rounded as the reference's (no fused multiply-adds); the
 // dot products are block sums added on the host in block order.
 //
-// The reference preconditions with hybrid Schwarz multigrid or FDM local
-// solves plus an XXT / AMG coarse solve (gmres.f:447-470); here M is the
-// Jacobi diagonal of setprec, the one preconditioner this library has, so
-// the iteration counts are this method's, not the reference's; the solution
-// is the same linear system's to the tolerance.
+// The reference preconditions with h1mg_solve (gmres.f:407-411), the
+// multilevel Schwarz method of h1mg.cu; M is that once nekgpu_h1mg_setup
+// has run on the handle, else the Jacobi diagonal of setprec (iteration
+// counts then are that method's; the solution is the same linear system's
+// to the tolerance).
 #include <cmath>
 #include <string>
 #include <vector>
@@ -200,12 +200,12 @@ __global__ void __launch_bounds__(kT) fcg_rho_kernel(double* __restrict__ z,
   double a = 0.0, b = 0.0;
   for (int64_t i = blockIdx.x * (int64_t)kT + threadIdx.x; i < n; i += (int64_t)gridDim.x * kT) {
     const double ri = r[i];
-    const double zz = __dmul_rn(d[i], ri);
+    const double zz = d ? __dmul_rn(d[i], ri) : z[i];  // d null: z = M r already formed
     const double t = __dsub_rn(r1[i], ri);
     const double zw = __dmul_rn(zz, wt[i]);
     a += __dmul_rn(zw, ri);
     b += __dmul_rn(zw, t);
-    z[i] = zz;
+    if (d) z[i] = zz;
     r1[i] = ri;
   }
 #pragma unroll
@@ -366,9 +366,15 @@ int gmres_solve(Handle& h, double* res, const double* h1, const double* h2, cons
       ++iter;
       double* zj = Z + (size_t)n * j;
       const double* vj = V + (size_t)n * j;
-      count_launch();
-      prec_kernel<<<nb, kT, 0, s>>>(zj, d, vj, n, null_space ? h.red.ptr : nullptr);
-      if (ortho(zj, null_space ? h.red.ptr : nullptr)) return -3;
+      if (h.mg) {  // h1mg_solve(z_j, w = mu v_j); w is masked in place, then overwritten
+        cudaMemcpyAsync(w, vj, n * sizeof(double), cudaMemcpyDeviceToDevice, s);
+        if (h1mg_apply(h, zj, w)) return -3;
+        if (ortho(zj, nullptr)) return -3;
+      } else {
+        count_launch();
+        prec_kernel<<<nb, kT, 0, s>>>(zj, d, vj, n, null_space ? h.red.ptr : nullptr);
+        if (ortho(zj, null_space ? h.red.ptr : nullptr)) return -3;
+      }
       if (apply_A(w, zj)) return -3;
       // h_ij = (w, v_i), i <= j, eight vectors per pass
       for (int i0 = 0; i0 <= j; i0 += kDots) {
@@ -480,8 +486,9 @@ int flex_cg_solve(Handle& h, double* res, const double* h1, const double* h2, co
   // a zero right-hand side is solved by x = 0 (the reference's loop would
   // divide 0 by 0)
   for (int k = 1; k <= maxit && div0 != 0.0; ++k) {
+    if (h.mg && h1mg_apply(h, z, r)) return -3;  // h1mg_solve(z, r): r masked in place
     count_launch();
-    fcg_rho_kernel<<<nb, kT, 0, s>>>(z, d, r, r1, wt, n, h.red.ptr);
+    fcg_rho_kernel<<<nb, kT, 0, s>>>(z, h.mg ? nullptr : d, r, r1, wt, n, h.red.ptr);
     double rr[2];
     if (g.sums(2, 2, rr)) return -3;
     const double rho0 = rho1;

@@ -112,6 +112,12 @@ struct MultiField {
   ~MultiField() { cudaFreeHost(cg_host); }
 };
 
+// The pressure preconditioner h1mg_solve on the device (h1mg.cu).
+struct MgDev;
+struct MgDevDeleter {
+  void operator()(MgDev* p) const;
+};
+
 struct Handle {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -166,6 +172,9 @@ struct Handle {
   DevBuf<double> mpartialA, mpartialB, mpartialC;
   DevBuf<unsigned int> mcounter;
   DevBuf<CgScalars> cg_tune;  // scalars of the tuning launches (beta = 0, not done)
+  // pressure preconditioner of hmh_gmres / hmh_flex_cg: h1mg_solve once set
+  // up (nekgpu_h1mg_setup), else the Jacobi diagonal
+  std::unique_ptr<MgDev, MgDevDeleter> mg;
 };
 
 // ---- operator entry points (axhelm_*.cu) ---------------------------------
@@ -224,6 +233,13 @@ PcgResult pcg_prepare(Handle& h, PcgWork<T>& wk, T* x, const T* f, const Coef<T>
                       const T* mask, const T* mult, double tin, int maxiter, int istep,
                       const T* dpre, bool* trivial);
 int pcg_vec_blocks(int64_t n);
+// h1mg.cu: z = M rhs with the set-up preconditioner (rhs masked in place,
+// as h1mg_solve leaves it); 0, -3 or -6 (not set up).  Setup from host
+// coordinates, mask or face types, and the fine numbering; 0 or NEKGPU_E*.
+int h1mg_apply(Handle& h, double* z, double* rhs);
+int h1mg_setup(Handle& h, const double* x, const double* y, const double* z, const double* mask,
+               const int64_t* glo, const int* fbc, bool null_space);
+
 // hmh_flex_cg with the Jacobi preconditioner (gmres.cu); 0, -3, -4 or -5.
 int flex_cg_solve(Handle& h, double* res, const double* h1, const double* h2, const double* wt,
                   const double* mask, double tol, int maxit, bool null_space, int* niter,

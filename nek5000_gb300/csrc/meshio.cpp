@@ -385,6 +385,11 @@ bool repair_faces(std::vector<int64_t>& cell, int64_t nel) {
 
 }  // namespace
 
+namespace nekgpu {
+// the message nekmesh_last_error returns, from the other host-only entry points
+int mesh_fail(int code, const std::string& msg) { return fail(code, msg); }
+}  // namespace nekgpu
+
 // =============================================================================
 // C ABI
 extern "C" {

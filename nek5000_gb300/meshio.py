@@ -142,6 +142,59 @@ def setvert3d(nx: int, vertex):
     return glo, ngv.value
 
 
+def h1mg_levels(lx1: int):
+    """Polynomial orders of the pressure preconditioner's levels, coarsest
+    first (h1mg_setup_mg_nx, core/hsmg.f:2272)."""
+    o = np.zeros(4, dtype=np.int32)
+    lmax = _lib().nekmesh_h1mg_levels(C.byref(C.c_int(int(lx1))), _p(o))
+    if lmax < 0:
+        _check(lmax)
+    return [int(v) for v in o[:lmax]]
+
+
+def face_types(nx: int, glo, mask):
+    """Pressure face types (6 per element: 0 shared, 1 Dirichlet, 2 Neumann)
+    read from a numbering and mask (nekmesh_face_types)."""
+    glo = np.ascontiguousarray(glo, dtype=np.int64).reshape(-1)
+    mask = np.ascontiguousarray(mask, dtype=np.float64).reshape(-1)
+    nel = glo.size // nx ** 3
+    fbc = np.zeros(6 * nel, dtype=np.int32)
+    _check(_lib().nekmesh_face_types(C.byref(C.c_int(nx)), C.byref(C.c_int(nel)), _p(glo),
+                                     _p(mask), _p(fbc)))
+    return fbc.reshape(nel, 6)
+
+
+def h1mg_level(nx1: int, glo, x, y, z, level: int, mask=None, fbc=None):
+    """The preconditioner's setup of one level (nekmesh_h1mg_level): returns
+    (nx, mask, rwt, swt, lengths[nel, 3, 3])."""
+    glo = np.ascontiguousarray(glo, dtype=np.int64).reshape(-1)
+    nel = glo.size // nx1 ** 3
+    f64 = lambda a: None if a is None else np.ascontiguousarray(a, dtype=np.float64).reshape(-1)
+    xs, ys, zs, m = f64(x), f64(y), f64(z), f64(mask)
+    fb = None if fbc is None else np.ascontiguousarray(fbc, dtype=np.int32).reshape(-1)
+    nx = C.c_int(0)
+    npt = nx1 ** 3 * nel  # large enough for every level
+    out = [np.zeros(npt) for _ in range(3)]
+    lengths = np.zeros(9 * nel)
+    _check(_lib().nekmesh_h1mg_level(C.byref(C.c_int(nx1)), C.byref(C.c_int(nel)), _p(glo),
+                                     _p(xs), _p(ys), _p(zs), _p(m), _p(fb),
+                                     C.byref(C.c_int(int(level))), C.byref(nx), *[_p(o) for o in out],
+                                     _p(lengths)))
+    k = nx.value ** 3 * nel
+    return nx.value, out[0][:k], out[1][:k], out[2][:k], lengths.reshape(nel, 3, 3)
+
+
+def fdm1d(n: int, lbc: int, rbc: int, ll: float, lm: float, lr: float):
+    """One 1-D fast-diagonalisation operator (nekmesh_fdm1d): (S, lam)."""
+    nl = n + 3
+    s = np.zeros(nl * nl)
+    lam = np.zeros(nl)
+    _check(_lib().nekmesh_fdm1d(C.byref(C.c_int(n)), C.byref(C.c_int(lbc)), C.byref(C.c_int(rbc)),
+                                C.byref(C.c_double(ll)), C.byref(C.c_double(lm)),
+                                C.byref(C.c_double(lr)), _p(s), _p(lam)))
+    return s.reshape(nl, nl).T.copy(), lam  # S[i, j]: component i of vector j
+
+
 def check_p_bc(nx: int, cbc, glo):
     """Single-element periodicity ('p  ' on two opposite faces of an element:
     core/navier8.f check_p_bc), applied to glo in place."""

@@ -190,6 +190,31 @@ class NekGpu:
         self._check(rc, allow=(_capi.ENOTCONV,))
         return it.value, d0.value, rn.value, rc
 
+    def h1mg_setup(self, x, y, z, glo_num, mask=None, fbc=None, null_space=False):
+        """The pressure preconditioner h1mg_solve (nekgpu_h1mg_setup): host
+        numpy coordinates, the numbering given to setup, and the pressure
+        mask or the face types (6 per element).  The pressure solves of this
+        handle use it until h1mg_free."""
+        f64 = lambda a: np.ascontiguousarray(a, dtype=np.float64).reshape(-1)
+        xs, ys, zs = f64(x), f64(y), f64(z)
+        glo = np.ascontiguousarray(glo_num, dtype=np.int64).reshape(-1)
+        m = None if mask is None else f64(mask)
+        fb = None if fbc is None else np.ascontiguousarray(fbc, dtype=np.int32).reshape(-1)
+        if m is None and fb is None:
+            raise TypeError("h1mg_setup needs the mask or the face types")
+        rc = self._L.nekgpu_h1mg_setup(C.byref(self._h), _ptr(xs), _ptr(ys), _ptr(zs), _ptr(m),
+                                       _ptr(glo), _ptr(fb), C.byref(_cint(int(bool(null_space)))))
+        self._check(rc)
+
+    def h1mg_free(self):
+        self._check(self._L.nekgpu_h1mg_free(C.byref(self._h)))
+
+    def h1mg_apply(self, z, rhs):
+        """z = M rhs on device tensors; rhs is masked in place."""
+        if not (_is_dev(z) and _is_dev(rhs)):
+            raise TypeError("h1mg_apply takes device arrays")
+        self._check(self._L.nekgpu_h1mg_apply_dev(C.byref(self._h), _ptr(z), _ptr(rhs)))
+
     def setup_xyz(self, lx1: int, nel: int, D, w, x, y, z, glo_num):
         """setup with G1..G6 and bm1 computed on the GPU from the GLL
         coordinates x, y, z ((n,) numpy each) and the GLL weights w (lx1)."""

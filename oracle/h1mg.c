@@ -68,6 +68,7 @@ struct ref_h1mg {
   int64_t nsolve;        /* unknowns in the factor (nc, or nc - 1 pinned) */
   double *vmult;         /* fine 1/multiplicity (dsavg) */
   double *ext0, *ext1, *ext2; /* scratch: extended arrays (finest) */
+  double *len;           /* per element: left r s t, middle r s t, right r s t */
 };
 
 /* ---- Fornberg weights ---------------------------------------------------- */
@@ -538,6 +539,13 @@ ref_h1mg *ref_h1mg_create(const ref_ops *ops, const double *x, const double *y, 
     free(B);
   }
   free(vr);
+  mg->len = (double *)malloc(sizeof(double) * 9 * nel);
+  for (int e = 0; e < nel; ++e)
+    for (int d = 0; d < 3; ++d) {
+      mg->len[9 * e + d] = lenl[3 * e + d];
+      mg->len[9 * e + 3 + d] = lenm[3 * e + d];
+      mg->len[9 * e + 6 + d] = lenr[3 * e + d];
+    }
   free(lw);
   /* coarse unknowns and the Galerkin matrix (set_up_h1_crs, core/navier8.f:83-238) */
   {
@@ -633,6 +641,7 @@ void ref_h1mg_free(ref_h1mg *mg) {
     free(L->dinv);
   }
   free(mg->cid);
+  free(mg->len);
   free(mg->L);
   free(mg->vmult);
   free(mg->ext0);
@@ -791,3 +800,29 @@ void ref_h1mg_level(const ref_h1mg *mg, int l, double *mask, double *rwt, double
 /* the Schwarz solve of one level alone (tests) */
 void ref_h1mg_schwarz(const ref_h1mg *mg, int l, double *e, double *r) { schwarz(mg, l, e, r); }
 void ref_h1mg_coarse(const ref_h1mg *mg, double *e, const double *r) { coarse_solve(mg, e, r); }
+
+/* One 1-D fast-diagonalisation operator of order n (tests): s (column j =
+ * vector j, excluded rows zeroed) and lam ascending, nl = n + 3. */
+void ref_fdm1d(int n, int lbc, int rbc, double ll, double lm, double lr, double *s, double *lam) {
+  const int nx = n + 1;
+  double z[16], w[16], c[64], D[256], ah[256];
+  ref_zwgll(z, w, nx);
+  for (int i = 0; i <= n; ++i) {
+    fd_weights(z[i], z, n, 1, c);
+    for (int j = 0; j <= n; ++j) D[i + nx * j] = c[j + nx];
+  }
+  for (int j = 0; j <= n; ++j)
+    for (int i = 0; i <= n; ++i) {
+      double a = 0.0;
+      for (int k = 0; k <= n; ++k) a = a + D[k + nx * i] * w[k] * D[k + nx * j];
+      ah[i + nx * j] = a;
+    }
+  double *tmp = (double *)malloc(sizeof(double) * 2 * (n + 3) * (n + 3));
+  fast1d(tmp, lam, lbc, rbc, ll, lm, lr, ah, w, n);
+  memcpy(s, tmp, sizeof(double) * (n + 3) * (n + 3));
+  free(tmp);
+}
+
+void ref_h1mg_lengths(const ref_h1mg *mg, double *out) {
+  memcpy(out, mg->len, sizeof(double) * 9 * mg->nel);
+}

@@ -162,6 +162,8 @@ int64_t ref_h1mg_ncoarse(const ref_h1mg *mg);
 void ref_h1mg_level(const ref_h1mg *mg, int l, double *mask, double *rwt, double *swt);
 void ref_h1mg_schwarz(const ref_h1mg *mg, int l, double *e, double *r);
 void ref_h1mg_coarse(const ref_h1mg *mg, double *e, const double *r);
+void ref_h1mg_lengths(const ref_h1mg *mg, double *out);
+void ref_fdm1d(int n, int lbc, int rbc, double ll, double lm, double lr, double *s, double *lam);
 /* hmh_gmres / hmh_flex_cg preconditioned by h1mg_solve */
 int ref_gmres_h1mg(const ref_ops *ops, const ref_h1mg *mg, double *res, const double *h1,
                    const double *h2, const double *wt, const double *mask, double tol, int maxit,

@@ -71,6 +71,9 @@ def lib():
             L.ref_h1mg_schwarz.argtypes = [_vp, C.c_int, _dp, _dp]
             L.ref_h1mg_coarse.argtypes = [_vp, _dp, _dp]
             L.ref_h1mg_levels.argtypes = [C.c_int, _i32]
+            L.ref_h1mg_lengths.argtypes = [_vp, _dp]
+            L.ref_fdm1d.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
+                                    _dp, _dp]
             L.ref_gmres_h1mg.argtypes = [_vp, _vp, _dp, _dp, _dp, _dp, _dp, C.c_double, C.c_int,
                                          C.c_int, C.c_int, C.POINTER(C.c_double),
                                          C.POINTER(C.c_double)]
@@ -360,6 +363,12 @@ class H1mg:
         lib().ref_h1mg_level(self.h, l, *[o.ctypes.data_as(C.c_void_p) for o in out])
         return tuple(out)
 
+    def lengths(self):
+        """per element (3, 3): left, middle, right widths in r, s, t"""
+        out = np.zeros(9 * self.ops.nel)
+        lib().ref_h1mg_lengths(self.h, out)
+        return out.reshape(self.ops.nel, 3, 3)
+
     def solve(self, rhs):
         """z = M rhs; returns (z, rhs masked as the reference leaves it)."""
         r = np.array(rhs, dtype=np.float64, copy=True)
@@ -378,6 +387,15 @@ class H1mg:
         e = np.zeros_like(r)
         lib().ref_h1mg_coarse(self.h, e, r)
         return e
+
+
+def fdm1d(n, lbc, rbc, ll, lm, lr):
+    """(S, lam) of one 1-D fast-diagonalisation operator; S[i, j] is
+    component i of eigenvector j."""
+    nl = n + 3
+    s, lam = np.zeros(nl * nl), np.zeros(nl)
+    lib().ref_fdm1d(int(n), int(lbc), int(rbc), float(ll), float(lm), float(lr), s, lam)
+    return s.reshape(nl, nl).T.copy(), lam
 
 
 def h1mg_levels(lx1):
