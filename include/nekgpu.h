@@ -127,8 +127,8 @@ int nekgpu_hmh_flex_cg(const int64_t *handle, double *res, const double *h1, con
  * :2234-2270 and set_up_h1_crs, core/navier8.f:83-238): additive multilevel
  * overlapping Schwarz on polynomial orders N, min(3, ...) and 1, with
  * fast-diagonalisation local solves on elements extended by one layer and
- * a Galerkin coarse solve on the vertices (exact: a dense inverse, so at
- * most 12288 coarse unknowns).  Host arrays: x, y, z the GLL coordinates
+ * a Galerkin coarse solve on the vertices (exact: A^-1 = X X^T with X sparse
+ * in nested-dissection order, as crs_xxt factors it).  Host arrays: x, y, z the GLL coordinates
  * (xm1, ym1, zm1), glo_num the numbering given to nekgpu_setup, and either
  * fbc (6 face types per element, r-, r+, s-, s+, t-, t+: 0 interior or
  * periodic, 1 Dirichlet ('O'), 2 Neumann (wall); get_fast_bc,

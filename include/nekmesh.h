@@ -159,6 +159,16 @@ int nekmesh_h1mg_level(const int *nx1, const int *nel, const int64_t *glo_num, c
 int nekmesh_fdm1d(const int *n, const int *lbc, const int *rbc, const double *ll,
                   const double *lm, const double *lr, double *s, double *lam);
 
+/* The coarse solve's factor A^-1 = X X^T (crs_xxt's form, core/crs_xxt.c:
+ * 863): A symmetric positive definite, n x n in CSR (ptr n+1, idx, val,
+ * both triangles), its unknowns at xyz (3 each) for the nested-dissection
+ * order.  *nnz = the entries of X; with the outputs non-null: perm (n, the
+ * unknown numbered k), and X by columns in that order (cptr n+1, cidx and
+ * cval nnz: rows of column j). */
+int nekmesh_xxt_factor(const int64_t *n, const int64_t *ptr, const int *idx, const double *val,
+                       const double *xyz, int64_t *nnz, int *perm, int64_t *cptr, int *cidx,
+                       double *cval);
+
 #ifdef __cplusplus
 }
 #endif

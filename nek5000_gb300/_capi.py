@@ -71,6 +71,7 @@ SIGNATURES = {
     "nekmesh_face_types": [_IP, _IP, _P, _P, _P],
     "nekmesh_h1mg_level": [_IP, _IP, _P, _P, _P, _P, _P, _P, _IP, _IP, _P, _P, _P, _P],
     "nekmesh_fdm1d": [_IP, _IP, _IP, _DP, _DP, _DP, _P, _P],
+    "nekmesh_xxt_factor": [_I64P, _P, _P, _P, _P, _I64P, _P, _P, _P, _P],
     "nekgpu_setup_xyz": [_I64P, _IP, _IP, _P, _P, _P, _P, _P, _P],
     "nekgpu_geom_update_dev": [_I64P, _P, _P, _P, _P],
     "nekgpu_geometry": [_I64P, _P, _P, _P, _P, _P, _P, _P],

@@ -8,8 +8,9 @@
 //
 //   top level  : Schwarz (mask, extend, exchange, FDM, sum back, dssum, W)
 //   each level : restrict (1/mult weights, J^T (x) J^T (x) J^T, dssum), Schwarz
-//   coarse     : restrict without dssum, gather by vertex, x = A_c^-1 b (dense
-//                inverse, one warp per row), null-space pin and mean, scatter
+//   coarse     : restrict without dssum, gather by vertex, x = X (X^T b) with
+//                the sparse factor A_c^-1 = X X^T (xxt.cpp; two row-parallel
+//                sparse products), null-space pin and mean, scatter
 //   unwind     : e_l += J e_{l-1}; z += J e_top-1; dsavg
 //
 // All FP64.  Sums are formed in a fixed order (no atomics), so the result
@@ -38,7 +39,11 @@ struct MgDev {
   DevBuf<double> A, E, rtop, vmult;
   int64_t nc = 0, ns = 0;
   DevBuf<int> cstart, cidx, cid;
-  DevBuf<double> ainv, cv, cy;
+  DevBuf<double> cv, cy;
+  // coarse factor A^-1 = X X^T in nested-dissection order (xxt.cpp)
+  DevBuf<int> xperm, xcidx, xridx;
+  DevBuf<int64_t> xcptr, xrptr;
+  DevBuf<double> xcval, xrval, xb, xy;
   ~MgDev() {
     for (auto& L : lev) {
       gs_free(L.gs);
@@ -295,18 +300,35 @@ __global__ void mg_cgather_kernel(double* __restrict__ v, const double* __restri
   v[c] = s;
 }
 
-// y[i] = sum_j Ainv[i][j] v[j], i < ns; one warp per row
-__global__ void mg_gemv_kernel(double* __restrict__ y, const double* __restrict__ Ainv,
-                               const double* __restrict__ v, int64_t ns) {
+// out[r] = sum over the row's entries val * in[idx], r < nrows; one warp per
+// row, lanes strided, then a fixed shuffle tree (the same order every run)
+__global__ void mg_spmv_kernel(double* __restrict__ out, const int64_t* __restrict__ ptr,
+                               const int* __restrict__ idx, const double* __restrict__ val,
+                               const double* __restrict__ in, int64_t nrows) {
   const int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
-  if (row >= ns) return;
-  const double* a = Ainv + row * ns;
+  if (row >= nrows) return;
   double acc = 0.0;
-  for (int64_t j = lane; j < ns; j += 32) acc += a[j] * v[j];
+  for (int64_t q = ptr[row] + lane; q < ptr[row + 1]; q += 32) acc += val[q] * in[idx[q]];
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-  if (lane == 0) y[row] = acc;
+  if (lane == 0) out[row] = acc;
+}
+
+// b[k] = v[perm[k]] (into the factor's order), k < n
+__global__ void mg_perm_gather_kernel(double* __restrict__ b, const double* __restrict__ v,
+                                      const int* __restrict__ perm, int64_t n) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+       k += (int64_t)gridDim.x * blockDim.x)
+    b[k] = v[perm[k]];
+}
+
+// v[perm[k]] = x[k] (back to the unknowns' order), k < n
+__global__ void mg_perm_scatter_kernel(double* __restrict__ v, const double* __restrict__ x,
+                                       const int* __restrict__ perm, int64_t n) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+       k += (int64_t)gridDim.x * blockDim.x)
+    v[perm[k]] = x[k];
 }
 
 // null space: the pinned unknown is 0, then the mean over all unknowns is
@@ -417,9 +439,16 @@ int h1mg_apply(Handle& h, double* z, double* rhs) {
   count_launch(3);
   mg_cgather_kernel<<<(int)((m.nc + 255) / 256), 256, 0, s>>>(m.cv.ptr, L0.r.ptr, m.cstart.ptr,
                                                              m.cidx.ptr, m.nc);
-  if (m.ns > 0)
-    mg_gemv_kernel<<<(int)((m.ns * 32 + 255) / 256), 256, 0, s>>>(m.cy.ptr, m.ainv.ptr, m.cv.ptr,
-                                                                  m.ns);
+  if (m.ns > 0) {  // cy = X (X^T cv) on the first ns unknowns
+    const int gw = (int)((m.ns * 32 + 255) / 256);
+    count_launch(4);
+    mg_perm_gather_kernel<<<grid_for(m.ns), kMgT, 0, s>>>(m.xb.ptr, m.cv.ptr, m.xperm.ptr, m.ns);
+    mg_spmv_kernel<<<gw, 256, 0, s>>>(m.xy.ptr, m.xcptr.ptr, m.xcidx.ptr, m.xcval.ptr, m.xb.ptr,
+                                      m.ns);
+    mg_spmv_kernel<<<gw, 256, 0, s>>>(m.xb.ptr, m.xrptr.ptr, m.xridx.ptr, m.xrval.ptr, m.xy.ptr,
+                                      m.ns);
+    mg_perm_scatter_kernel<<<grid_for(m.ns), kMgT, 0, s>>>(m.cy.ptr, m.xb.ptr, m.xperm.ptr, m.ns);
+  }
   if (m.null_space && m.nc > 0) {
     count_launch();
     mg_cmean_kernel<<<1, 1024, 0, s>>>(m.cy.ptr, m.nc);
@@ -545,9 +574,14 @@ int h1mg_setup(Handle& h, const double* x, const double* y, const double* z, con
     std::vector<int> fill(start.begin(), start.end() - 1);
     for (int64_t i = 0; i < n0; ++i)
       if (p.cid[i] >= 0) idx[fill[p.cid[i]]++] = (int)i;
+    const XxtFactor& X = p.xxt;
     if (upload(m->cstart, start, s) || upload(m->cidx, idx, s) || upload(m->cid, cid, s) ||
-        upload(m->ainv, p.ainv, s) || m->cv.ensure(std::max<int64_t>(p.nc, 1)) ||
-        m->cy.ensure(std::max<int64_t>(p.nc, 1))) {
+        upload(m->xperm, X.perm, s) || upload(m->xcptr, X.cptr, s) ||
+        upload(m->xcidx, X.cidx, s) || upload(m->xcval, X.cval, s) ||
+        upload(m->xrptr, X.rptr, s) || upload(m->xridx, X.ridx, s) ||
+        upload(m->xrval, X.rval, s) || m->xb.ensure(std::max<int64_t>(p.nsolve, 1)) ||
+        m->xy.ensure(std::max<int64_t>(p.nsolve, 1)) ||
+        m->cv.ensure(std::max<int64_t>(p.nc, 1)) || m->cy.ensure(std::max<int64_t>(p.nc, 1))) {
       set_error(h, "h1mg: device upload failed");
       return NEKGPU_ENOMEM;
     }

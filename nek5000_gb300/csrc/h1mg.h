@@ -11,7 +11,23 @@
 namespace nekgpu {
 
 constexpr int kMgMaxLev = 4;
-constexpr int kMgMaxCoarse = 12288;  // dense coarse inverse: at most 1.2 GB
+
+// A^-1 = X X^T in nested-dissection order (xxt.cpp): perm[k] = the unknown
+// numbered k; X by columns (cptr/cidx/cval: rows i of column j) and by rows
+// (rptr/ridx/rval: columns j of row i, ascending), both in that order.
+struct XxtFactor {
+  int64_t n = 0;
+  std::vector<int> perm;
+  std::vector<int64_t> cptr, rptr;
+  std::vector<int> cidx, ridx;
+  std::vector<double> cval, rval;
+};
+
+// Factor the symmetric positive definite n x n matrix (CSR, both triangles)
+// whose unknowns sit at xyz (3 per unknown).  Returns 0 or NEKGPU_EINVAL.
+int xxt_factor(XxtFactor& f, int64_t n, const std::vector<int64_t>& ptr,
+               const std::vector<int>& idx, const std::vector<double>& val, const double* xyz,
+               std::string& err);
 
 struct MgLevelPlan {
   int nx = 0;                         // points per direction (order + 1)
@@ -36,7 +52,8 @@ struct MgPlan {
   std::vector<double> lenl, lenm, lenr;  // element widths [3 e + d]
   int64_t nc = 0, nsolve = 0;  // coarse unknowns, and those in the inverse
   std::vector<int64_t> cid;    // per level-0 point: coarse unknown or -1
-  std::vector<double> ainv;    // nsolve x nsolve inverse of the coarse matrix
+  std::vector<double> ccoord;  // coordinates of the coarse unknowns (3 each)
+  XxtFactor xxt;               // of the first nsolve unknowns
 };
 
 // Level orders of h1mg_setup_mg_nx (core/hsmg.f:2272-2338) in 3-D; returns lmax.
@@ -59,7 +76,7 @@ int h1mg_plan(MgPlan& p, int nx1, int nel, const int64_t* glo, const double* x, 
 // GLL points (gen_crs_basis, core/navier8.f:1689-1731): 8 nx1^3 values.
 void h1mg_coarse_basis(int nx1, std::vector<double>& b);
 
-// Coarse inverse from the element matrices a[e][i + 8 j] = b_i^T A_e b_j
+// Coarse factor from the element matrices a[e][i + 8 j] = b_i^T A_e b_j
 // (get_local_crs_galerkin, core/navier8.f:1648-1687).  Returns 0 or an error.
 int h1mg_plan_coarse(MgPlan& p, const double* elem, std::string& err);
 

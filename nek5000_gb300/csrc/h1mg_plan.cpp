@@ -8,13 +8,12 @@
 // eigenvectors and inverse eigenvalue sums of every element
 // (hsmg_setup_fast :701-781) from the element widths (swap_lengths,
 // core/fast3d.f:1542-1617), the interpolation matrices (hsmg_setup_intp
-// :83-120), and the dense inverse of the coarse Galerkin matrix (the
-// single-rank equivalent of crs_setup's XXT factor, core/crs_xxt.c:863).
+// :83-120), and the coarse Galerkin matrix with its X X^T factor (xxt.cpp;
+// crs_setup, core/crs_xxt.c:863).
 // Compiled without fused multiply-adds (x86 and aarch64 hosts round alike).
 #include <algorithm>
 #include <cmath>
 #include <cstring>
-#include <thread>
 
 #include "h1mg.h"
 #include "nekgpu.h"
@@ -22,24 +21,6 @@
 
 namespace nekgpu {
 namespace {
-
-template <typename F>
-void parallel_rows(int64_t lo, int64_t hi, F&& f) {  // f(i) for i in [lo, hi), strided
-  const int64_t cnt = hi - lo;
-  if (cnt <= 0) return;
-  unsigned nt = std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
-  if (cnt < 64) nt = 1;
-  if (nt == 1) {
-    for (int64_t i = lo; i < hi; ++i) f(i);
-    return;
-  }
-  std::vector<std::thread> th;
-  for (unsigned t = 0; t < nt; ++t)
-    th.emplace_back([&, t]() {
-      for (int64_t i = lo + t; i < hi; i += nt) f(i);
-    });
-  for (auto& x : th) x.join();
-}
 
 // Fornberg's weights (B. Fornberg, SIAM Review 40 (1998) 685-691), the
 // recursion fd_weights_full (core/fast3d.f:1294) evaluates: c[j + (n+1) k]
@@ -528,102 +509,60 @@ int h1mg_plan(MgPlan& p, int nx1, int nel, const int64_t* glo, const double* x, 
   ids.erase(std::unique(ids.begin(), ids.end()), ids.end());
   p.nc = (int64_t)ids.size();
   p.nsolve = (null_space && p.nc > 0) ? p.nc - 1 : p.nc;
-  if (p.nsolve > kMgMaxCoarse) {
-    err = "h1mg: coarse problem above " + std::to_string(kMgMaxCoarse) +
-          " unknowns (the dense coarse inverse is limited to that size)";
+  if (p.nc >= (int64_t)1 << 31) {
+    err = "h1mg: more than 2^31 - 1 coarse unknowns";
     return NEKGPU_EINVAL;
   }
   p.cid.assign(C.n, -1);
+  p.ccoord.assign(3 * (size_t)p.nc, 0.0);
   for (int64_t i = 0; i < C.n; ++i)
-    if (C.mask[i] >= 0.1)
-      p.cid[i] = std::lower_bound(ids.begin(), ids.end(), C.glo[i]) - ids.begin();
+    if (C.mask[i] >= 0.1) {
+      const int64_t c = std::lower_bound(ids.begin(), ids.end(), C.glo[i]) - ids.begin();
+      p.cid[i] = c;
+      const int64_t e = i / 8, cr = i % 8;  // level-0 point = element corner cr
+      const int64_t q = e * nxyz + (cr & 1) * (nx1 - 1) + nx1 * (((cr >> 1) & 1) * (nx1 - 1)) +
+                        (int64_t)nx1 * nx1 * ((cr >> 2) * (nx1 - 1));
+      p.ccoord[3 * c] = x[q];
+      p.ccoord[3 * c + 1] = y[q];
+      p.ccoord[3 * c + 2] = z[q];
+    }
   return NEKGPU_OK;
 }
 
 int h1mg_plan_coarse(MgPlan& p, const double* elem, std::string& err) {
-  const int64_t nc = p.nc, ns = p.nsolve;
-  // assemble the unpinned unknowns (row-major, full)
-  std::vector<double> A((size_t)ns * ns, 0.0);
+  const int64_t ns = p.nsolve;
+  // assemble the unknowns below nsolve (the pinned one left out) by rows
+  std::vector<std::vector<std::pair<int, double>>> rows((size_t)ns);
   for (int e = 0; e < p.nel; ++e)
     for (int j = 0; j < 8; ++j)
       for (int i = 0; i < 8; ++i) {
         const int64_t ci = p.cid[8 * e + i], cj = p.cid[8 * e + j];
-        if (ci >= 0 && cj >= 0 && ci < ns && cj < ns) A[ci * ns + cj] += elem[64 * e + i + 8 * j];
+        if (ci >= 0 && cj >= 0 && ci < ns && cj < ns)
+          rows[ci].push_back({(int)cj, elem[64 * (size_t)e + i + 8 * j]});
       }
-  (void)nc;
-  // blocked right-looking Cholesky A = L L^T (lower triangle, row-major)
-  constexpr int64_t BS = 64;
-  bool bad = false;
-  for (int64_t k0 = 0; k0 < ns && !bad; k0 += BS) {
-    const int64_t k1 = std::min(ns, k0 + BS);
-    for (int64_t j = k0; j < k1 && !bad; ++j) {  // the diagonal block
-      double d = A[j * ns + j];
-      for (int64_t k = k0; k < j; ++k) d -= A[j * ns + k] * A[j * ns + k];
-      if (!(d > 0.0)) {
-        bad = true;
-        break;
-      }
-      d = std::sqrt(d);
-      A[j * ns + j] = d;
-      for (int64_t i = j + 1; i < k1; ++i) {
-        double s = A[i * ns + j];
-        for (int64_t k = k0; k < j; ++k) s -= A[i * ns + k] * A[j * ns + k];
-        A[i * ns + j] = s / d;
-      }
+  std::vector<int64_t> ptr((size_t)ns + 1, 0);
+  std::vector<int> idx;
+  std::vector<double> val;
+  for (int64_t r = 0; r < ns; ++r) {
+    auto& v = rows[r];
+    std::stable_sort(v.begin(), v.end(),
+                     [](const std::pair<int, double>& a, const std::pair<int, double>& b) {
+                       return a.first < b.first;
+                     });
+    for (size_t q = 0; q < v.size();) {  // duplicates summed in element order
+      double a = 0.0;
+      const int c = v[q].first;
+      for (; q < v.size() && v[q].first == c; ++q) a += v[q].second;
+      idx.push_back(c);
+      val.push_back(a);
     }
-    if (bad) break;
-    parallel_rows(k1, ns, [&](int64_t i) {  // the panel below
-      double* ri = &A[i * ns];
-      for (int64_t j = k0; j < k1; ++j) {
-        double s = ri[j];
-        const double* rj = &A[j * ns];
-        for (int64_t k = k0; k < j; ++k) s -= ri[k] * rj[k];
-        ri[j] = s / rj[j];
-      }
-    });
-    parallel_rows(k1, ns, [&](int64_t i) {  // trailing update of row i, columns k1..i
-      double* ri = &A[i * ns];
-      for (int64_t j = k1; j <= i; ++j) {
-        const double* rj = &A[j * ns];
-        double s = 0.0;
-        for (int64_t k = k0; k < k1; ++k) s += ri[k] * rj[k];
-        ri[j] -= s;
-      }
-    });
+    ptr[r + 1] = (int64_t)idx.size();
+    std::vector<std::pair<int, double>>().swap(v);
   }
-  if (bad) {
+  const int rc = xxt_factor(p.xxt, ns, ptr, idx, val, p.ccoord.data(), err);
+  if (rc && err.find("positive") != std::string::npos)
     err = "h1mg: the coarse matrix is not positive definite (a null space without null_space?)";
-    return NEKGPU_EINVAL;
-  }
-  // L^-1 column by column (row-major lower W), then A^-1 = W^T W
-  std::vector<double> W((size_t)ns * ns, 0.0);
-  parallel_rows(0, ns, [&](int64_t c) {
-    W[c * ns + c] = 1.0 / A[c * ns + c];
-    for (int64_t i = c + 1; i < ns; ++i) {
-      double s = 0.0;
-      const double* ri = &A[i * ns];
-      for (int64_t k = c; k < i; ++k) s += ri[k] * W[k * ns + c];
-      W[i * ns + c] = -s / ri[i];
-    }
-  });
-  std::vector<double> WT((size_t)ns * ns, 0.0);  // WT[i][k] = W[k][i], nonzero for k >= i
-  for (int64_t k = 0; k < ns; ++k)
-    for (int64_t i = 0; i <= k; ++i) WT[i * ns + k] = W[k * ns + i];
-  W.clear();
-  W.shrink_to_fit();
-  p.ainv.assign((size_t)ns * ns, 0.0);
-  parallel_rows(0, ns, [&](int64_t i) {
-    const double* ti = &WT[i * ns];
-    for (int64_t j = 0; j <= i; ++j) {
-      const double* tj = &WT[j * ns];
-      double s = 0.0;
-      for (int64_t k = i; k < ns; ++k) s += ti[k] * tj[k];
-      p.ainv[i * ns + j] = s;
-    }
-  });
-  for (int64_t i = 0; i < ns; ++i)
-    for (int64_t j = i + 1; j < ns; ++j) p.ainv[i * ns + j] = p.ainv[j * ns + i];
-  return NEKGPU_OK;
+  return rc;
 }
 
 }  // namespace nekgpu

@@ -195,6 +195,32 @@ def fdm1d(n: int, lbc: int, rbc: int, ll: float, lm: float, lr: float):
     return s.reshape(nl, nl).T.copy(), lam  # S[i, j]: component i of vector j
 
 
+def xxt_factor(A, xyz):
+    """X with A^-1 = X X^T for a symmetric positive definite scipy/numpy
+    matrix A whose unknowns sit at xyz (n, 3) (nekmesh_xxt_factor); returns
+    (perm, X) with X dense, rows and columns in the nested-dissection order
+    perm (perm[k] = the unknown numbered k)."""
+    import scipy.sparse as sp
+    A = sp.csr_matrix(A)
+    n = A.shape[0]
+    ptr = np.ascontiguousarray(A.indptr, dtype=np.int64)
+    idx = np.ascontiguousarray(A.indices, dtype=np.int32)
+    val = np.ascontiguousarray(A.data, dtype=np.float64)
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1)
+    nnz = C.c_int64(0)
+    args = [C.byref(C.c_int64(n)), _p(ptr), _p(idx), _p(val), _p(xyz), C.byref(nnz)]
+    _check(_lib().nekmesh_xxt_factor(*args, None, None, None, None))
+    perm = np.zeros(n, dtype=np.int32)
+    cptr = np.zeros(n + 1, dtype=np.int64)
+    cidx = np.zeros(nnz.value, dtype=np.int32)
+    cval = np.zeros(nnz.value)
+    _check(_lib().nekmesh_xxt_factor(*args, _p(perm), _p(cptr), _p(cidx), _p(cval)))
+    X = np.zeros((n, n))
+    for j in range(n):
+        X[cidx[cptr[j]:cptr[j + 1]], j] = cval[cptr[j]:cptr[j + 1]]
+    return perm, X
+
+
 def check_p_bc(nx: int, cbc, glo):
     """Single-element periodicity ('p  ' on two opposite faces of an element:
     core/navier8.f check_p_bc), applied to glo in place."""

@@ -63,3 +63,33 @@ def test_fdm1d_matches(oracle, n, lbc, rbc):
     M = S @ np.diag(inv(lam)) @ S.T  # the zero mode of a floating 1-D block left out
     Mo = So @ np.diag(inv(lamo)) @ So.T
     assert np.allclose(M, Mo, rtol=0, atol=1e-11 * np.abs(Mo).max())
+
+
+def test_xxt_factor_inverts_and_stays_sparse():
+    """X X^T = A^-1 for the 27-point vertex operator of a 12^3 box (random
+    SPD element matrices), and X has far fewer entries than n^2 with the
+    nested-dissection order (columns non-zero only on their subtree)."""
+    sp = pytest.importorskip("scipy.sparse")
+    k = 11  # vertices 12^3
+    nv = (k + 1) ** 3
+    rng = np.random.default_rng(7)
+    g = np.arange(nv).reshape(k + 1, k + 1, k + 1)
+    rows, cols, vals = [], [], []
+    for ez in range(k):
+        for ey in range(k):
+            for ex in range(k):
+                ids = np.array([g[ez + (c >> 2), ey + ((c >> 1) & 1), ex + (c & 1)] for c in range(8)])
+                B = rng.standard_normal((8, 8))
+                Ae = B @ B.T + 8 * np.eye(8)
+                rows.append(np.repeat(ids, 8))
+                cols.append(np.tile(ids, 8))
+                vals.append(Ae.reshape(-1))
+    A = sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))),
+                      shape=(nv, nv))
+    zz, yy, xx = np.meshgrid(*(np.arange(k + 1.0),) * 3, indexing="ij")
+    xyz = np.stack([xx.reshape(-1), yy.reshape(-1), zz.reshape(-1)], axis=1)
+    perm, X = meshio.xxt_factor(A, xyz)
+    assert sorted(perm.tolist()) == list(range(nv))
+    Ap = A.toarray()[np.ix_(perm, perm)]
+    assert np.allclose(X @ X.T @ Ap, np.eye(nv), atol=1e-10)
+    assert np.count_nonzero(X) < 0.4 * nv * nv
