@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <thread>
 
 #include "h1mg.h"
 #include "nekgpu.h"
@@ -21,6 +22,26 @@
 
 namespace nekgpu {
 namespace {
+
+// f(e) for every element, elements split into contiguous chunks over the
+// host's threads (each element's output is its own)
+template <typename F>
+void parallel_elements(int nel, F&& f) {
+  unsigned nt = std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
+  if (nel < 64) nt = 1;
+  if (nt == 1) {
+    for (int e = 0; e < nel; ++e) f(e);
+    return;
+  }
+  std::vector<std::thread> th;
+  const int chunk = (nel + (int)nt - 1) / (int)nt;
+  for (unsigned t = 0; t < nt; ++t)
+    th.emplace_back([&, t]() {
+      const int e1 = std::min(nel, (int)(t + 1) * chunk);
+      for (int e = (int)t * chunk; e < e1; ++e) f(e);
+    });
+  for (auto& x : th) x.join();
+}
 
 // Fornberg's weights (B. Fornberg, SIAM Review 40 (1998) 685-691), the
 // recursion fd_weights_full (core/fast3d.f:1294) evaluates: c[j + (n+1) k]
@@ -463,7 +484,7 @@ int h1mg_plan(MgPlan& p, int nx1, int nel, const int64_t* glo, const double* x, 
     // fast diagonalisation of every element's extended operator
     L.S.assign((size_t)nel * 3 * nl * nl, 0.0);
     L.dinv.assign((size_t)nn * nel, 0.0);
-    for (int e = 0; e < nel; ++e) {
+    parallel_elements(nel, [&](int e) {
       double lam[3][32];
       for (int d = 0; d < 3; ++d)
         h1mg_fast1d(L.S.data() + ((size_t)e * 3 + d) * nl * nl, lam[d], p.fbc[6 * e + 2 * d],
@@ -483,7 +504,7 @@ int h1mg_plan(MgPlan& p, int nx1, int nel, const int64_t* glo, const double* x, 
             const double diag = lam[0][i] + lam[1][j] + lam[2][k];
             de[il++] = diag > eps ? 1.0 / diag : 0.0;
           }
-    }
+    });
     // Schwarz weights: 1 / the number of extended subdomains over a point
     std::vector<double> A((size_t)nn * nel, 0.0), B((size_t)nn * nel, 1.0);
     extrude(A.data(), 0, 0.0, B.data(), 0, 1.0, nl, nel);
