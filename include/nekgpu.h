@@ -144,6 +144,45 @@ int nekgpu_h1mg_setup(const int64_t *handle, const double *x, const double *y, c
 int nekgpu_h1mg_free(const int64_t *handle);
 /* z = M rhs on device arrays; rhs is masked in place, as h1mg_solve leaves it. */
 int nekgpu_h1mg_apply_dev(const int64_t *handle, double *z, double *rhs);
+/* ---- a solve split over element shards ----------------------------------
+ * The reference splits the mesh over MPI ranks; each rank's solve runs its
+ * local operator and gather-scatter, exchanges the sums at the points it
+ * shares with other ranks (inside gs_op), and adds its local dot products
+ * over the ranks (gop, core/comm_mpi.f:216).  These device entry points are
+ * the local pieces a caller's loop needs between its own exchanges (MPI,
+ * NCCL or torch.distributed); all arrays are the handle's n local points.
+ *   col2   a = a b           (core/math.f:563)
+ *   col3   a = b c           (core/math.f:597)
+ *   add2s1 a = c1 a + b      (core/math.f:677)
+ *   add2s2 a = a + c2 b      (core/math.f:689)
+ *   vlsc3  *out = local sum of a b c        (core/navier4.f:323)
+ *   vlsc32 *out = local sum of b c a^2      (core/hmholtz.f:848)
+ *   invcol1 a = 1/a          (core/math.f:61)
+ *   vlmax  *out = local max |a| (*mode 0), max a (1) or min a (2) */
+int nekgpu_col2_dev(const int64_t *handle, double *a, const double *b);
+int nekgpu_col3_dev(const int64_t *handle, double *a, const double *b, const double *c);
+int nekgpu_add2s1_dev(const int64_t *handle, double *a, const double *b, const double *c1);
+int nekgpu_add2s2_dev(const int64_t *handle, double *a, const double *b, const double *c2);
+int nekgpu_vlsc3_dev(const int64_t *handle, const double *a, const double *b, const double *c,
+                     double *out);
+int nekgpu_vlsc32_dev(const int64_t *handle, const double *a, const double *b, const double *c,
+                      double *out);
+int nekgpu_invcol1_dev(const int64_t *handle, double *a);
+int nekgpu_vlmax_dev(const int64_t *handle, const double *a, const int *mode, double *out);
+/* setprec's element-local diagonal (core/hmholtz.f:380-524 before its dssum
+ * and reciprocal): a shard sums it locally (nekgpu_dssum_dev), across its
+ * interfaces, then inverts. */
+int nekgpu_setprec_local_dev(const int64_t *handle, double *diag, const double *h1,
+                             const double *h2);
+/* Interface points shared with other shards: point k has the local copies
+ * pos[start[k] .. start[k+1]-1] (host arrays, start has nk+1 entries).
+ * gather: buf[k] = u at point k's first copy (after the local dssum all
+ * copies agree); scatter: every copy of point k = buf[k]. */
+int nekgpu_iface_setup(const int64_t *handle, const int64_t *nk, const int64_t *start,
+                       const int64_t *pos);
+int nekgpu_iface_gather_dev(const int64_t *handle, double *buf, const double *u);
+int nekgpu_iface_scatter_dev(const int64_t *handle, double *u, const double *buf);
+
 /* The same on host arrays (copied in and out inside the call). */
 int nekgpu_hmh_gmres(const int64_t *handle, double *res, const double *h1, const double *h2,
                      const double *wt, const double *mask, const double *tol, const int *maxit,

@@ -64,6 +64,18 @@ SIGNATURES = {
     "nekgpu_hmh_gmres": [_I64P, _P, _P, _P, _P, _P, _DP, _IP, _IP, _IP, _IP, _DP, _DP],
     "nekgpu_hmh_flex_cg_dev": [_I64P, _P, _P, _P, _P, _P, _DP, _IP, _IP, _IP, _DP, _DP],
     "nekgpu_hmh_flex_cg": [_I64P, _P, _P, _P, _P, _P, _DP, _IP, _IP, _IP, _DP, _DP],
+    "nekgpu_col2_dev": [_I64P, _P, _P],
+    "nekgpu_col3_dev": [_I64P, _P, _P, _P],
+    "nekgpu_add2s1_dev": [_I64P, _P, _P, _DP],
+    "nekgpu_add2s2_dev": [_I64P, _P, _P, _DP],
+    "nekgpu_vlsc3_dev": [_I64P, _P, _P, _P, _DP],
+    "nekgpu_vlsc32_dev": [_I64P, _P, _P, _P, _DP],
+    "nekgpu_invcol1_dev": [_I64P, _P],
+    "nekgpu_vlmax_dev": [_I64P, _P, _IP, _DP],
+    "nekgpu_setprec_local_dev": [_I64P, _P, _P, _P],
+    "nekgpu_iface_setup": [_I64P, _I64P, _P, _P],
+    "nekgpu_iface_gather_dev": [_I64P, _P, _P],
+    "nekgpu_iface_scatter_dev": [_I64P, _P, _P],
     "nekgpu_h1mg_setup": [_I64P, _P, _P, _P, _P, _P, _P, _IP],
     "nekgpu_h1mg_free": [_I64P],
     "nekgpu_h1mg_apply_dev": [_I64P, _P, _P],

@@ -216,6 +216,7 @@ void handle_close(Handle& H) {
   cudaSetDevice(H.device);
   if (H.stream) cudaStreamSynchronize(H.stream);
   H.mg.reset();
+  H.iface.reset();
   gs_free(H.mesh.gs);
   H.mesh.f64.release();
   H.mesh.f32.release();
@@ -258,6 +259,7 @@ static int mesh_prepare(Handle& H, int lx1, int nel, const double* dxm1, std::st
   m.ax_sel[0] = m.ax_sel[1] = AxShapeSel();
   H.proj.clear();  // projection spaces belong to the old mesh
   H.mg.reset();    // and so does the pressure preconditioner
+  H.iface.reset();  // and the shard's interface maps
   H.has_mesh = false;
   if (H.gexec) cudaGraphExecDestroy(H.gexec);
   H.gexec = nullptr;

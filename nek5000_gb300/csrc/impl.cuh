@@ -112,6 +112,12 @@ struct MultiField {
   ~MultiField() { cudaFreeHost(cg_host); }
 };
 
+// Interface exchange maps of an element shard (vecops.cu).
+struct ShardIface;
+struct ShardIfaceDeleter {
+  void operator()(ShardIface* p) const;
+};
+
 // The pressure preconditioner h1mg_solve on the device (h1mg.cu).
 struct MgDev;
 struct MgDevDeleter {
@@ -175,6 +181,8 @@ struct Handle {
   // pressure preconditioner of hmh_gmres / hmh_flex_cg: h1mg_solve once set
   // up (nekgpu_h1mg_setup), else the Jacobi diagonal
   std::unique_ptr<MgDev, MgDevDeleter> mg;
+  // interface points shared with other shards (nekgpu_iface_setup)
+  std::unique_ptr<ShardIface, ShardIfaceDeleter> iface;
 };
 
 // ---- operator entry points (axhelm_*.cu) ---------------------------------
@@ -209,6 +217,8 @@ template <typename T>
 int detect_coef(Handle& h, const T* h1, const T* h2, int64_t n, Coef<T>& c);
 template <typename T>
 cudaError_t setprec(Handle& h, const OpData<T>& op, T* d, const Coef<T>& c);
+// element-local Jacobi diagonal, before dssum and reciprocal (pcg.cu)
+int setprec_local_f64(Handle& h, double* d, const Coef<double>& c);
 int setprec_f64(Handle& h, double* d, const Coef<double>& c);
 double device_sum(Handle& h, int kind, const double* a, const double* b, const double* c,
                   int64_t n, int* status);

@@ -285,6 +285,37 @@ static void launch_setprec_nx(Handle& h, double* d, const Coef<double>& c) {
 }
 
 // d = 1/dssum(diag)  (setprec, hmholtz.f:380-524), FP64
+// The element-local diagonal alone (before dssum and the reciprocal): what a
+// sharded solve sums across its shards' interfaces first.
+int setprec_local_f64(Handle& h, double* d, const Coef<double>& c) {
+  cudaError_t pre = cudaGetLastError();
+  if (pre != cudaSuccess) {
+    set_error(h, std::string("setprec: error pending from an earlier call: ") +
+                     cudaGetErrorString(pre));
+    return -3;
+  }
+  switch (h.mesh.nx1) {
+    case 2: launch_setprec_nx<2>(h, d, c); break;
+    case 3: launch_setprec_nx<3>(h, d, c); break;
+    case 4: launch_setprec_nx<4>(h, d, c); break;
+    case 5: launch_setprec_nx<5>(h, d, c); break;
+    case 6: launch_setprec_nx<6>(h, d, c); break;
+    case 7: launch_setprec_nx<7>(h, d, c); break;
+    case 8: launch_setprec_nx<8>(h, d, c); break;
+    case 9: launch_setprec_nx<9>(h, d, c); break;
+    case 10: launch_setprec_nx<10>(h, d, c); break;
+    case 11: launch_setprec_nx<11>(h, d, c); break;
+    case 12: launch_setprec_nx<12>(h, d, c); break;
+    default: return -1;
+  }
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_error(h, std::string("setprec kernel: ") + cudaGetErrorString(e));
+    return -3;
+  }
+  return 0;
+}
+
 int setprec_f64(Handle& h, double* d, const Coef<double>& c) {
   cudaError_t pre = cudaGetLastError();
   if (pre != cudaSuccess) {

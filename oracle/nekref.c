@@ -927,7 +927,8 @@ void ref_axhelm(const ref_ops *ops, double *au, const double *u, const double *h
 }
 
 /* ---- setprec (hmholtz.f:380-524), 3-D deformed ------------------------- */
-void ref_setprec(const ref_ops *ops, double *dpcm1, const double *helm1, const double *helm2) {
+static void setprec_body(const ref_ops *ops, double *dpcm1, const double *helm1, const double *helm2,
+                         int local) {
   const int nx = ops->nx1, nxyz = nx * nx * nx;
   const int64_t ntot = ops->n;
   const double *dxtm1 = ops->dt; /* dytm1 = dztm1 = dxtm1 */
@@ -988,9 +989,20 @@ void ref_setprec(const ref_ops *ops, double *dpcm1, const double *helm1, const d
   for (int64_t i = 0; i < ntot; ++i) dpcm1[i] = dpcm1[i] * helm1[i];                 /* COL2 */
   PFOR
   for (int64_t i = 0; i < ntot; ++i) dpcm1[i] = dpcm1[i] + helm2[i] * ops->bm1[i];  /* ADDCOL3 */
+  if (local) return; /* the element-local diagonal alone */
   ref_dssum(ops, dpcm1);
   PFOR
   for (int64_t i = 0; i < ntot; ++i) dpcm1[i] = 1.0 / dpcm1[i];                     /* INVCOL1 */
+}
+
+void ref_setprec(const ref_ops *ops, double *dpcm1, const double *helm1, const double *helm2) {
+  setprec_body(ops, dpcm1, helm1, helm2, 0);
+}
+
+/* setprec's element-local diagonal, before its dssum and reciprocal */
+void ref_setprec_local(const ref_ops *ops, double *diag, const double *helm1,
+                       const double *helm2) {
+  setprec_body(ops, diag, helm1, helm2, 1);
 }
 
 /* ---- chktcg1 (hmholtz.f:527-609); EIGAA = 0 so ACONDNO = 10 ----------- */

@@ -71,6 +71,7 @@ void ref_axhelm(const ref_ops *ops, double *au, const double *u, const double *h
 void ref_dssum(const ref_ops *ops, double *u);                       /* dssum.f:33    */
 void ref_dsop(const ref_ops *ops, double *u, int op);                 /* dssum.f:100   */
 void ref_setprec(const ref_ops *ops, double *d, const double *h1, const double *h2); /* :380 */
+void ref_setprec_local(const ref_ops *ops, double *d, const double *h1, const double *h2);
 double ref_glsc3(const ref_ops *ops, const double *a, const double *b, const double *m);
 void ref_chktcg1(const ref_ops *ops, double *tol, const double *res, const double *h1,
                  const double *h2, const double *mask, const double *mult,

@@ -88,6 +88,7 @@ def lib():
             L.ref_dssum.argtypes = [_vp, _dp]
             L.ref_dsop.argtypes = [_vp, _dp, C.c_int]
             L.ref_setprec.argtypes = [_vp, _dp, _dp, _dp]
+            L.ref_setprec_local.argtypes = [_vp, _dp, _dp, _dp]
             L.ref_glsc3.argtypes = [_vp, _dp, _dp, _dp]
             L.ref_glsc3.restype = C.c_double
             L.ref_chktcg1.argtypes = [_vp, C.POINTER(C.c_double), _dp, _dp, _dp, _dp, _dp, _dp]
@@ -251,6 +252,12 @@ class Ops:
     def setprec(self, h1, h2):
         d = np.zeros(self.n)
         lib().ref_setprec(self.h, d, _c(h1), _c(h2))
+        return d
+
+    def setprec_local(self, h1, h2):
+        """setprec's element-local diagonal (before dssum and reciprocal)"""
+        d = np.zeros(self.n)
+        lib().ref_setprec_local(self.h, d, _c(h1), _c(h2))
         return d
 
     def glsc3(self, a, b, m):
