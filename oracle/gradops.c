@@ -1,0 +1,134 @@
+/*
+ * gradops.c -- CPU restatement of the gradient-type operators of the PN-PN
+ * splitting step (TEST INFRASTRUCTURE ONLY: the oracle the device operators
+ * are checked against; never linked into the product).  Arithmetic in the
+ * reference's order (mxm sums over the inner index left to right, products
+ * and sums unfused: built with -ffp-contract=off).
+ *
+ *   wgradm1  core/navier1.f:4170-4230  weak gradient (opgrad for PN-PN)
+ *   cdtp     core/navier1.f:330-470    D^T x, the PN-PN (ifsplit) 3-D branch
+ *   dudxyz   core/navier1.f:1156-1220  strong derivative du/dx_isd
+ *   op_curl  core/plan4.f:368-430      curl, averaged when ifavg
+ *
+ * rst: the metric terms rxm1..tzm1 as nine arrays of n (rx ry rz sx sy sz tx
+ * ty tz, ref_geom_rst); jac: jacm1.
+ */
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "nekref.h"
+
+void ref_zwgll(double *z, double *w, int np);
+void ref_dgll(double *d, double *dt, const double *zin, int nz);
+
+static void dmat(int nx1, double *d, double *dt, double *w3) {
+  double z[32], w[32];
+  ref_zwgll(z, w, nx1);
+  ref_dgll(d, dt, z, nx1);
+  if (w3)
+    for (int k = 0; k < nx1; ++k)
+      for (int j = 0; j < nx1; ++j)
+        for (int i = 0; i < nx1; ++i) w3[i + nx1 * (j + nx1 * k)] = w[i] * w[j] * w[k];
+}
+
+void ref_wgradm1(int nx1, int nel, double *ux, double *uy, double *uz, const double *u,
+                 const double *rst) {
+  const int nxyz = nx1 * nx1 * nx1;
+  const int64_t n = (int64_t)nxyz * nel;
+  double d[1024], dt[1024];
+  double *w3 = (double *)malloc(sizeof(double) * nxyz);
+  double *ur = (double *)malloc(sizeof(double) * 3 * nxyz), *us = ur + nxyz, *ut = us + nxyz;
+  dmat(nx1, d, dt, w3);
+  const double *rx = rst, *ry = rst + n, *rz = rst + 2 * n, *sx = rst + 3 * n, *sy = rst + 4 * n,
+               *sz = rst + 5 * n, *tx = rst + 6 * n, *ty = rst + 7 * n, *tz = rst + 8 * n;
+  for (int e = 0; e < nel; ++e) {
+    const int64_t o = (int64_t)nxyz * e;
+    ref_local_grad3(ur, us, ut, u + o, nx1 - 1, d, dt);
+    for (int i = 0; i < nxyz; ++i) {
+      const int64_t p = o + i;
+      ux[p] = w3[i] * (ur[i] * rx[p] + us[i] * sx[p] + ut[i] * tx[p]);
+      uy[p] = w3[i] * (ur[i] * ry[p] + us[i] * sy[p] + ut[i] * ty[p]);
+      uz[p] = w3[i] * (ur[i] * rz[p] + us[i] * sz[p] + ut[i] * tz[p]);
+    }
+  }
+  free(w3);
+  free(ur);
+}
+
+/* isd = 1, 2, 3: the metric terms of x, y or z (rm2 = rxm1 ... as cdtp's
+ * callers pass them) */
+void ref_cdtp(int nx1, int nel, double *dtx, const double *x, const double *rst,
+              const double *jac, const double *bm1, int isd) {
+  const int nxyz = nx1 * nx1 * nx1;
+  const int64_t n = (int64_t)nxyz * nel;
+  double d[1024], dt[1024];
+  double *wx = (double *)malloc(sizeof(double) * 5 * nxyz);
+  double *ta = wx + nxyz, *tb = ta + nxyz, *tc = tb + nxyz, *wk = tc + nxyz;
+  dmat(nx1, d, dt, NULL);
+  const double *rm = rst + (int64_t)(isd - 1) * n, *sm = rst + (int64_t)(isd + 2) * n,
+               *tm = rst + (int64_t)(isd + 5) * n;
+  for (int e = 0; e < nel; ++e) {
+    const int64_t o = (int64_t)nxyz * e;
+    for (int i = 0; i < nxyz; ++i) {
+      wx[i] = bm1[o + i] * x[o + i]; /* col3 */
+      wx[i] = wx[i] / jac[o + i];    /* invcol2 */
+    }
+    for (int i = 0; i < nxyz; ++i) {
+      ta[i] = wx[i] * rm[o + i];
+      tb[i] = wx[i] * sm[o + i];
+      tc[i] = wx[i] * tm[o + i];
+    }
+    ref_local_grad3_t(dtx + o, ta, tb, tc, nx1 - 1, d, dt, wk);
+  }
+  free(wx);
+}
+
+void ref_dudxyz(int nx1, int nel, double *du, const double *u, const double *rst,
+                const double *jac, int isd) {
+  const int nxyz = nx1 * nx1 * nx1;
+  const int64_t n = (int64_t)nxyz * nel;
+  double d[1024], dt[1024];
+  double *ur = (double *)malloc(sizeof(double) * 3 * nxyz), *us = ur + nxyz, *ut = us + nxyz;
+  dmat(nx1, d, dt, NULL);
+  const double *rm = rst + (int64_t)(isd - 1) * n, *sm = rst + (int64_t)(isd + 2) * n,
+               *tm = rst + (int64_t)(isd + 5) * n;
+  for (int e = 0; e < nel; ++e) {
+    const int64_t o = (int64_t)nxyz * e;
+    ref_local_grad3(ur, us, ut, u + o, nx1 - 1, d, dt);
+    for (int i = 0; i < nxyz; ++i) {
+      double v = ur[i] * rm[o + i];    /* col2 */
+      v = v + us[i] * sm[o + i];       /* addcol3 */
+      v = v + ut[i] * tm[o + i];       /* addcol3 */
+      const double jacmi = 1.0 / jac[o + i];
+      du[o + i] = v * jacmi;           /* col2 by jacmi */
+    }
+  }
+  free(ur);
+}
+
+void ref_op_curl(const ref_ops *ops, double *w1, double *w2, double *w3, const double *u1,
+                 const double *u2, const double *u3, int ifavg, const double *rst,
+                 const double *jac, const double *bm1, const double *binv) {
+  const int nx1 = ref_ops_nx1(ops), nel = ref_ops_nel(ops);
+  const int64_t n = ref_ops_n(ops);
+  double *a = (double *)malloc(sizeof(double) * 2 * n), *b = a + n;
+  ref_dudxyz(nx1, nel, a, u3, rst, jac, 2);
+  ref_dudxyz(nx1, nel, b, u2, rst, jac, 3);
+  for (int64_t i = 0; i < n; ++i) w1[i] = a[i] - b[i];
+  ref_dudxyz(nx1, nel, a, u1, rst, jac, 3);
+  ref_dudxyz(nx1, nel, b, u3, rst, jac, 1);
+  for (int64_t i = 0; i < n; ++i) w2[i] = a[i] - b[i];
+  ref_dudxyz(nx1, nel, a, u2, rst, jac, 1);
+  ref_dudxyz(nx1, nel, b, u1, rst, jac, 2);
+  for (int64_t i = 0; i < n; ++i) w3[i] = a[i] - b[i];
+  if (ifavg) {
+    double *w[3] = {w1, w2, w3};
+    for (int c = 0; c < 3; ++c) {
+      for (int64_t i = 0; i < n; ++i) w[c][i] = w[c][i] * bm1[i];
+      ref_dssum(ops, w[c]);
+      for (int64_t i = 0; i < n; ++i) w[c][i] = w[c][i] * binv[i];
+    }
+  }
+  free(a);
+}

@@ -354,8 +354,23 @@ void ref_box_mesh(int nx1, int kx, int ky, int kz, int periodic_y, int periodic_
  * Geometry -- core/coef.f xyzrst (:879-926), glmapm1 (:555-631),
  * geodat1 (:633-784), genwz W3M1 (:263-267)
  * ====================================================================== */
+static void geom_body(int nx1, int nel, const double *xm1, const double *ym1, const double *zm1,
+                      double *g6, double *bm1, double *jacm1, double *rst);
+
 void ref_geom(int nx1, int nel, const double *xm1, const double *ym1, const double *zm1,
               double *g6, double *bm1, double *jacm1) {
+  geom_body(nx1, nel, xm1, ym1, zm1, g6, bm1, jacm1, NULL);
+}
+
+/* The same, with the metric terms rxm1..tzm1 (glmapm1's cofactors, nine
+ * arrays of n in the order rx ry rz sx sy sz tx ty tz) and jacm1. */
+void ref_geom_rst(int nx1, int nel, const double *xm1, const double *ym1, const double *zm1,
+                  double *g6, double *bm1, double *jacm1, double *rst) {
+  geom_body(nx1, nel, xm1, ym1, zm1, g6, bm1, jacm1, rst);
+}
+
+static void geom_body(int nx1, int nel, const double *xm1, const double *ym1, const double *zm1,
+                      double *g6, double *bm1, double *jacm1, double *rst) {
   const int nxyz = nx1 * nx1 * nx1, nxy = nx1 * nx1;
   const int64_t n = (int64_t)nxyz * nel;
   double z[32], w[32], d[32 * 32], dt[32 * 32];
@@ -428,6 +443,10 @@ void ref_geom(int nx1, int nel, const double *xm1, const double *ym1, const doub
         g6_[o + i] = a6 * w3[i];
         bm1[o + i] = jac * w3[i];
         if (jacm1) jacm1[o + i] = jac;
+        if (rst) {
+          const double m9[9] = {rx, ry, rz, sx, sy, sz, tx, ty, tz};
+          for (int q = 0; q < 9; ++q) rst[(int64_t)q * n + o + i] = m9[q];
+        }
       }
     }
     free(buf);

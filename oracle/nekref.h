@@ -173,6 +173,19 @@ int ref_flex_cg_h1mg(const ref_ops *ops, const ref_h1mg *mg, double *res, const 
                      const double *h2, const double *wt, const double *mask, double tol,
                      int maxit, int null_space, double *div0_out, double *rnorm_out);
 
+/* ---- gradient-type operators of the splitting step (gradops.c) --------- */
+void ref_geom_rst(int nx1, int nel, const double *xm1, const double *ym1, const double *zm1,
+                  double *g6, double *bm1, double *jacm1, double *rst);
+void ref_wgradm1(int nx1, int nel, double *ux, double *uy, double *uz, const double *u,
+                 const double *rst);
+void ref_cdtp(int nx1, int nel, double *dtx, const double *x, const double *rst,
+              const double *jac, const double *bm1, int isd);
+void ref_dudxyz(int nx1, int nel, double *du, const double *u, const double *rst,
+                const double *jac, int isd);
+void ref_op_curl(const ref_ops *ops, double *w1, double *w2, double *w3, const double *u1,
+                 const double *u2, const double *u3, int ifavg, const double *rst,
+                 const double *jac, const double *bm1, const double *binv);
+
 /* sizes of an operator state */
 int ref_ops_nx1(const ref_ops *ops);
 int ref_ops_nel(const ref_ops *ops);

@@ -72,6 +72,12 @@ def lib():
             L.ref_h1mg_coarse.argtypes = [_vp, _dp, _dp]
             L.ref_h1mg_levels.argtypes = [C.c_int, _i32]
             L.ref_h1mg_lengths.argtypes = [_vp, _dp]
+            L.ref_geom_rst.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
+            L.ref_wgradm1.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp]
+            L.ref_cdtp.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp, C.c_int]
+            L.ref_dudxyz.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp, _dp, C.c_int]
+            L.ref_op_curl.argtypes = [_vp, _dp, _dp, _dp, _dp, _dp, _dp, C.c_int, _dp, _dp, _dp,
+                                      _dp]
             L.ref_fdm1d.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
                                     _dp, _dp]
             L.ref_gmres_h1mg.argtypes = [_vp, _vp, _dp, _dp, _dp, _dp, _dp, C.c_double, C.c_int,
@@ -403,6 +409,40 @@ def fdm1d(n, lbc, rbc, ll, lm, lr):
     s, lam = np.zeros(nl * nl), np.zeros(nl)
     lib().ref_fdm1d(int(n), int(lbc), int(rbc), float(ll), float(lm), float(lr), s, lam)
     return s.reshape(nl, nl).T.copy(), lam
+
+
+def geom_rst(nx1, nel, x, y, z):
+    """(rst (9, n): rx ry rz sx sy sz tx ty tz, jac (n)) of glmapm1."""
+    n = nx1 ** 3 * nel
+    g, bm1, jac, rst = np.zeros(6 * n), np.zeros(n), np.zeros(n), np.zeros(9 * n)
+    lib().ref_geom_rst(int(nx1), int(nel), _c(x), _c(y), _c(z), g, bm1, jac, rst)
+    return rst.reshape(9, n), jac
+
+
+def wgradm1(nx1, nel, u, rst):
+    n = nx1 ** 3 * nel
+    out = [np.zeros(n) for _ in range(3)]
+    lib().ref_wgradm1(int(nx1), int(nel), *out, _c(u), _c(rst))
+    return out
+
+
+def cdtp(nx1, nel, x, rst, jac, bm1, isd):
+    out = np.zeros(nx1 ** 3 * nel)
+    lib().ref_cdtp(int(nx1), int(nel), out, _c(x), _c(rst), _c(jac), _c(bm1), int(isd))
+    return out
+
+
+def dudxyz(nx1, nel, u, rst, jac, isd):
+    out = np.zeros(nx1 ** 3 * nel)
+    lib().ref_dudxyz(int(nx1), int(nel), out, _c(u), _c(rst), _c(jac), int(isd))
+    return out
+
+
+def op_curl(ops, u1, u2, u3, rst, jac, bm1, binv, ifavg=True):
+    out = [np.zeros(ops.n) for _ in range(3)]
+    lib().ref_op_curl(ops.h, *out, _c(u1), _c(u2), _c(u3), int(bool(ifavg)), _c(rst), _c(jac),
+                      _c(bm1), _c(binv))
+    return out
 
 
 def h1mg_levels(lx1):

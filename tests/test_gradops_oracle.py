@@ -1,0 +1,48 @@
+"""The oracle's gradient-type operators (oracle/gradops.c) on a deformed
+box, through identities a correct restatement must satisfy: linear fields
+are exact in the GLL interpolant, so the strong derivative is the constant
+gradient, the weak gradient is bm1 times it, the curl of (-y, x, 0) is
+(0, 0, 2), and cdtp is the transpose of bm1 * dudxyz."""
+import numpy as np
+
+from conftest import rng_unit_vector
+
+
+def _mesh(oracle):
+    P = oracle.box_problem(6, 3, 2, 2, v=rng_unit_vector(141))
+    rst, jac = oracle.geom_rst(P["nx1"], P["nel"], P["x"], P["y"], P["z"])
+    assert np.allclose(jac, P["jac"], rtol=0, atol=0)
+    return P, rst, jac
+
+
+def test_linear_fields_are_differentiated_exactly(oracle):
+    P, rst, jac = _mesh(oracle)
+    nx1, nel = P["nx1"], P["nel"]
+    a = np.array([0.3, -1.2, 2.5])
+    u = a[0] * P["x"] + a[1] * P["y"] + a[2] * P["z"]
+    for isd in (1, 2, 3):
+        du = oracle.dudxyz(nx1, nel, u, rst, jac, isd)
+        assert np.allclose(du, a[isd - 1], rtol=0, atol=1e-11)
+    ux, uy, uz = oracle.wgradm1(nx1, nel, u, rst)
+    for c, g in enumerate((ux, uy, uz)):
+        assert np.allclose(g, a[c] * P["bm1"], rtol=1e-11, atol=1e-14)
+
+
+def test_curl_of_a_rotation(oracle):
+    P, rst, jac = _mesh(oracle)
+    ops = P["ops"]
+    w1, w2, w3 = oracle.op_curl(ops, -P["y"], P["x"], np.zeros(P["n"]), rst, jac, P["bm1"],
+                                P["binv"], ifavg=True)
+    assert np.abs(w1).max() < 1e-11 and np.abs(w2).max() < 1e-11
+    assert np.allclose(w3, 2.0, rtol=0, atol=1e-11)
+
+
+def test_cdtp_is_the_transpose_of_the_weighted_derivative(oracle):
+    P, rst, jac = _mesh(oracle)
+    nx1, nel, n = P["nx1"], P["nel"], P["n"]
+    rng = np.random.default_rng(142)
+    x, v = rng.standard_normal(n), rng.standard_normal(n)
+    for isd in (1, 2, 3):
+        lhs = np.dot(v, oracle.cdtp(nx1, nel, x, rst, jac, P["bm1"], isd))
+        rhs = np.dot(x, P["bm1"] * oracle.dudxyz(nx1, nel, v, rst, jac, isd))
+        assert abs(lhs - rhs) <= 1e-12 * (abs(lhs) + abs(rhs))
