@@ -144,6 +144,26 @@ int nekgpu_h1mg_setup(const int64_t *handle, const double *x, const double *y, c
 int nekgpu_h1mg_free(const int64_t *handle);
 /* z = M rhs on device arrays; rhs is masked in place, as h1mg_solve leaves it. */
 int nekgpu_h1mg_apply_dev(const int64_t *handle, double *z, double *rhs);
+/* ---- gradient-type operators of the splitting step (plan4) --------------
+ * On device arrays of the handle's n points, in the reference's arithmetic
+ * order (bit-identical to its unfused FP64 evaluation).  They need the metric
+ * terms rxm1..tzm1 and jacm1, which the library keeps when the geometry comes
+ * from coordinates (nekgpu_setup_xyz, nekgpu_geom_update_dev); NEKGPU_ENOSETUP
+ * otherwise.  isd = 1, 2, 3 selects x, y, z.
+ *   wgradm1  u_x,y,z = w3m1 (u_r r_x + u_s s_x + u_t t_x), ...
+ *            (opgrad for PN-PN, core/navier1.f:4170)
+ *   dudxyz   du = (u_r r_isd + u_s s_isd + u_t t_isd) / jacm1 (:1156)
+ *   cdtp     dtx = D^T (bm1 x / jacm1 times r_isd, s_isd, t_isd) (:330)
+ *   op_curl  w = curl u from dudxyz; with *ifavg != 0 averaged as
+ *            w = binv dssum(bm1 w) (core/plan4.f:368-430) */
+int nekgpu_wgradm1_dev(const int64_t *handle, double *ux, double *uy, double *uz,
+                       const double *u);
+int nekgpu_dudxyz_dev(const int64_t *handle, double *du, const double *u, const int *isd);
+int nekgpu_cdtp_dev(const int64_t *handle, double *dtx, const double *x, const int *isd);
+int nekgpu_op_curl_dev(const int64_t *handle, double *w1, double *w2, double *w3,
+                       const double *u1, const double *u2, const double *u3, const int *ifavg,
+                       const double *binv);
+
 /* ---- a solve split over element shards ----------------------------------
  * The reference splits the mesh over MPI ranks; each rank's solve runs its
  * local operator and gather-scatter, exchanges the sums at the points it

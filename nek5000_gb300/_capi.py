@@ -64,6 +64,10 @@ SIGNATURES = {
     "nekgpu_hmh_gmres": [_I64P, _P, _P, _P, _P, _P, _DP, _IP, _IP, _IP, _IP, _DP, _DP],
     "nekgpu_hmh_flex_cg_dev": [_I64P, _P, _P, _P, _P, _P, _DP, _IP, _IP, _IP, _DP, _DP],
     "nekgpu_hmh_flex_cg": [_I64P, _P, _P, _P, _P, _P, _DP, _IP, _IP, _IP, _DP, _DP],
+    "nekgpu_wgradm1_dev": [_I64P, _P, _P, _P, _P],
+    "nekgpu_dudxyz_dev": [_I64P, _P, _P, _IP],
+    "nekgpu_cdtp_dev": [_I64P, _P, _P, _IP],
+    "nekgpu_op_curl_dev": [_I64P, _P, _P, _P, _P, _P, _P, _IP, _P],
     "nekgpu_col2_dev": [_I64P, _P, _P],
     "nekgpu_col3_dev": [_I64P, _P, _P, _P],
     "nekgpu_add2s1_dev": [_I64P, _P, _P, _DP],

@@ -257,6 +257,7 @@ static int mesh_prepare(Handle& H, int lx1, int nel, const double* dxm1, std::st
   m.f32.release();
   m.has_f32 = false;
   m.ax_sel[0] = m.ax_sel[1] = AxShapeSel();
+  m.has_rst = false;  // metric terms only come with coordinates (geom.cu)
   H.proj.clear();  // projection spaces belong to the old mesh
   H.mg.reset();    // and so does the pressure preconditioner
   H.iface.reset();  // and the shard's interface maps

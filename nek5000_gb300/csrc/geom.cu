@@ -22,7 +22,9 @@ __global__ void __launch_bounds__(NX* NX) geom_kernel(const double* __restrict__
                                                       const double* __restrict__ D,
                                                       const double* __restrict__ w,
                                                       double* __restrict__ G,
-                                                      double* __restrict__ bm1, int* bad) {
+                                                      double* __restrict__ bm1, int* bad,
+                                                      double* __restrict__ rst,
+                                                      double* __restrict__ jacm1, int64_t n) {
   constexpr int P = NX * NX * NX, NXY = NX * NX;
   __shared__ double sx[P], sy[P], sz[P], sD[NXY], sw[NX];
   const int e = blockIdx.x, tid = threadIdx.x;
@@ -87,15 +89,22 @@ __global__ void __launch_bounds__(NX* NX) geom_kernel(const double* __restrict__
 #pragma unroll
     for (int q = 0; q < 6; ++q) Ge[q * P + pt] = __dmul_rn(__dmul_rn(a[q], wj), w3);
     bm1[eo + pt] = __dmul_rn(jac, w3);
+    if (rst) {  // the metric terms and the Jacobian themselves
+      const double m9[9] = {rx, ry, rz, sxv, syv, szv, tx, ty, tz};
+#pragma unroll
+      for (int q = 0; q < 9; ++q) rst[(int64_t)q * n + eo + pt] = m9[q];
+      jacm1[eo + pt] = jac;
+    }
     if (!(jac > 0.0)) atomicOr(bad, 1);
   }
 }
 
 template <int NX>
 void launch_nx(int nel, const double* x, const double* y, const double* z, const double* D,
-               const double* w, double* G, double* bm1, int* bad, cudaStream_t s) {
+               const double* w, double* G, double* bm1, int* bad, double* rst, double* jac,
+               int64_t n, cudaStream_t s) {
   count_launch();
-  geom_kernel<NX><<<nel, NX * NX, 0, s>>>(x, y, z, D, w, G, bm1, bad);
+  geom_kernel<NX><<<nel, NX * NX, 0, s>>>(x, y, z, D, w, G, bm1, bad, rst, jac, n);
 }
 
 }  // namespace
@@ -108,15 +117,27 @@ int geom_from_xyz(Handle& H, const double* x, const double* y, const double* z, 
   Mesh& m = H.mesh;
   const int64_t n = m.n;
   DevBuf<double> wd;
-  if (wd.ensure(m.nx1)) {
+  const int64_t nxyz = (int64_t)m.nx1 * m.nx1 * m.nx1;
+  if (wd.ensure(m.nx1) || m.rst.ensure((size_t)9 * n) || m.jac.ensure(n) || m.w3.ensure(nxyz)) {
     err = "geometry: allocation failed";
     return NEKGPU_ENOMEM;
   }
   cudaMemcpyAsync(wd.ptr, w, m.nx1 * sizeof(double), cudaMemcpyHostToDevice, H.stream);
+  {  // w3m1 = w(i) w(j) w(k), in that order (genwz)
+    std::vector<double> w3((size_t)nxyz);
+    for (int k = 0; k < m.nx1; ++k)
+      for (int j = 0; j < m.nx1; ++j)
+        for (int i = 0; i < m.nx1; ++i) w3[i + m.nx1 * (j + (int64_t)m.nx1 * k)] = w[i] * w[j] * w[k];
+    cudaMemcpyAsync(m.w3.ptr, w3.data(), nxyz * sizeof(double), cudaMemcpyHostToDevice, H.stream);
+    cudaStreamSynchronize(H.stream);  // w3 is a host temporary
+  }
   cudaMemsetAsync(H.flag, 0, sizeof(int), H.stream);
   switch (m.nx1) {
 #define NEKGPU_GEOM_CASE(N) \
-  case N: launch_nx<N>(m.nel, x, y, z, m.f64.D, wd.ptr, m.f64.G, m.f64.bm1, H.flag, H.stream); break;
+  case N:                                                                                    \
+    launch_nx<N>(m.nel, x, y, z, m.f64.D, wd.ptr, m.f64.G, m.f64.bm1, H.flag, m.rst.ptr, m.jac.ptr, \
+                 n, H.stream);                                                                  \
+    break;
     NEKGPU_GEOM_CASE(2)
     NEKGPU_GEOM_CASE(3)
     NEKGPU_GEOM_CASE(4)
@@ -149,6 +170,7 @@ int geom_from_xyz(Handle& H, const double* x, const double* y, const double* z, 
   double vol = 0.0;
   for (int64_t i = 0; i < n; ++i) vol = vol + hb[(size_t)i];
   m.vol = vol;
+  m.has_rst = true;
   // the FP32 copy of the operator data no longer matches
   m.f32.release();
   m.has_f32 = false;

@@ -74,6 +74,11 @@ struct Mesh {
   // (threads, groups-per-thread shift) and its launch time
   int gs_gshift[2] = {0, 0};
   float gs_ms[2] = {0.f, 0.f};
+  // metric terms rxm1..tzm1 (nine arrays of n: rx ry rz sx sy sz tx ty tz),
+  // jacm1 and w3m1 (nx1^3), kept when the geometry is formed from
+  // coordinates (geom.cu); the gradient-type operators need them (gradops.cu)
+  DevBuf<double> rst, jac, w3;
+  bool has_rst = false;
 };
 
 // Coefficient descriptor after uniformity detection.
@@ -243,6 +248,12 @@ PcgResult pcg_prepare(Handle& h, PcgWork<T>& wk, T* x, const T* f, const Coef<T>
                       const T* mask, const T* mult, double tin, int maxiter, int istep,
                       const T* dpre, bool* trivial);
 int pcg_vec_blocks(int64_t n);
+// gradops.cu: op 0 wgradm1 (o1..o3 <- i1), 1 dudxyz (o1 <- i1, m = isd - 1),
+// 2 cdtp (o1 <- i1, m, bm1), 3 curl (o1..o3 <- i1..i3); 0 or -1 (lx1).
+int launch_gradop(Handle& h, int op, double* o1, double* o2, double* o3, const double* i1,
+                  const double* i2, const double* i3, int m, const double* bm1);
+void launch_mul_by(Handle& h, double* a, const double* b);
+
 // h1mg.cu: z = M rhs with the set-up preconditioner (rhs masked in place,
 // as h1mg_solve leaves it); 0, -3 or -6 (not set up).  Setup from host
 // coordinates, mask or face types, and the fine numbering; 0 or NEKGPU_E*.

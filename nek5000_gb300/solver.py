@@ -190,6 +190,24 @@ class NekGpu:
         self._check(rc, allow=(_capi.ENOTCONV,))
         return it.value, d0.value, rn.value, rc
 
+    # ---- gradient-type operators of the splitting step (device arrays) --------
+    def wgradm1(self, ux, uy, uz, u):
+        self._check(self._L.nekgpu_wgradm1_dev(C.byref(self._h), _ptr(ux), _ptr(uy), _ptr(uz),
+                                               _ptr(u)))
+
+    def dudxyz(self, du, u, isd: int):
+        self._check(self._L.nekgpu_dudxyz_dev(C.byref(self._h), _ptr(du), _ptr(u),
+                                              C.byref(_cint(isd))))
+
+    def cdtp(self, dtx, x, isd: int):
+        self._check(self._L.nekgpu_cdtp_dev(C.byref(self._h), _ptr(dtx), _ptr(x),
+                                            C.byref(_cint(isd))))
+
+    def op_curl(self, w1, w2, w3, u1, u2, u3, ifavg=True, binv=None):
+        self._check(self._L.nekgpu_op_curl_dev(C.byref(self._h), _ptr(w1), _ptr(w2), _ptr(w3),
+                                               _ptr(u1), _ptr(u2), _ptr(u3),
+                                               C.byref(_cint(int(bool(ifavg)))), _ptr(binv)))
+
     def h1mg_setup(self, x, y, z, glo_num, mask=None, fbc=None, null_space=False):
         """The pressure preconditioner h1mg_solve (nekgpu_h1mg_setup): host
         numpy coordinates, the numbering given to setup, and the pressure

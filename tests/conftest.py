@@ -13,11 +13,12 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300) and the built libnekgpu.so")
 
 
-# Files whose code builds on the rest (the pressure preconditioner and the
-# element shards run on the operator, gather-scatter and Krylov solves the
-# other files test) run after them, so that a failure there is reported
-# after, not instead of, the results of what it builds on.
-_BUILT_ON_THE_REST = ("test_gpu_h1mg.py", "test_gpu_shard.py")
+# Files whose code builds on the rest (the splitting step's gradient
+# operators on the geometry, the pressure preconditioner and the element
+# shards on the operator, gather-scatter and Krylov solves the other files
+# test) run after them, so that a failure there is reported after, not
+# instead of, the results of what it builds on.
+_BUILT_ON_THE_REST = ("test_gpu_gradops.py", "test_gpu_h1mg.py", "test_gpu_shard.py")
 
 
 def pytest_collection_modifyitems(session, config, items):

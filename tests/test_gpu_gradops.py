@@ -1,0 +1,59 @@
+"""The gradient-type operators of the splitting step on the device
+(nekgpu_wgradm1_dev, _dudxyz_dev, _cdtp_dev, _op_curl_dev) against the
+oracle's restatement (oracle/gradops.c): both evaluate the reference's
+arithmetic in its order without fused multiply-adds, so they must agree bit
+for bit, on a deformed box and on a periodic one."""
+import numpy as np
+import pytest
+
+from conftest import rng_unit_vector
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("case", ["box", "periodic"])
+def test_gradops_match_the_oracle_bit_for_bit(gpu_lib, oracle, case):
+    torch = pytest.importorskip("torch")
+    if case == "box":
+        P = oracle.box_problem(7, 3, 2, 2, v=rng_unit_vector(151))
+    else:
+        P = oracle.box_problem(6, 3, 3, 3, periodic=(False, True, True), v=rng_unit_vector(152))
+    nx1, nel, n = P["nx1"], P["nel"], P["n"]
+    rst, jac = oracle.geom_rst(nx1, nel, P["x"], P["y"], P["z"])
+    lib = gpu_lib(0)
+    lib.setup_xyz(nx1, nel, P["D"], P["wgll"], P["x"], P["y"], P["z"], P["glo_num"])
+    rng = np.random.default_rng(153)
+    u1, u2, u3 = (rng.standard_normal(n) for _ in range(3))
+    dev = lambda a: torch.tensor(np.ascontiguousarray(a), device="cuda")
+    zeros = lambda: torch.zeros(n, dtype=torch.float64, device="cuda")
+    host = lambda t: t.cpu().numpy()
+    # weak gradient
+    g = [zeros() for _ in range(3)]
+    lib.wgradm1(*g, dev(u1))
+    for a, b in zip(g, oracle.wgradm1(nx1, nel, u1, rst)):
+        assert np.array_equal(host(a), b)
+    for isd in (1, 2, 3):
+        du = zeros()
+        lib.dudxyz(du, dev(u2), isd)
+        assert np.array_equal(host(du), oracle.dudxyz(nx1, nel, u2, rst, jac, isd)), isd
+        dt = zeros()
+        lib.cdtp(dt, dev(u3), isd)
+        assert np.array_equal(host(dt), oracle.cdtp(nx1, nel, u3, rst, jac, P["bm1"], isd)), isd
+    for ifavg in (False, True):
+        w = [zeros() for _ in range(3)]
+        lib.op_curl(*w, dev(u1), dev(u2), dev(u3), ifavg=ifavg, binv=dev(P["binv"]))
+        want = oracle.op_curl(P["ops"], u1, u2, u3, rst, jac, P["bm1"], P["binv"], ifavg=ifavg)
+        for a, b in zip(w, want):
+            assert np.array_equal(host(a), b), ifavg
+
+
+def test_gradops_need_coordinates(gpu_lib, oracle):
+    torch = pytest.importorskip("torch")
+    from nek5000_gb300 import _capi
+    P = oracle.box_problem(5, 2, 2, 2, v=rng_unit_vector(154))
+    lib = gpu_lib(0)
+    lib.setup(P["nx1"], P["nel"], P["D"], P["g"], P["bm1"], P["glo_num"])
+    u = torch.zeros(P["n"], dtype=torch.float64, device="cuda")
+    with pytest.raises(_capi.NekGpuError) as ei:
+        lib.dudxyz(u.clone(), u, 1)
+    assert ei.value.code == _capi.ENOSETUP
