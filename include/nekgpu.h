@@ -164,6 +164,28 @@ int nekgpu_op_curl_dev(const int64_t *handle, double *w1, double *w2, double *w3
                        const double *u1, const double *u2, const double *u3, const int *ifavg,
                        const double *binv);
 
+/* The splitting step's explicit right-hand sides (plan4, core/plan4.f), on
+ * device arrays, PN-PN without the stress formulation.  Same setup needs as
+ * the operators above; with NEKGPU_OPT_EXACT set they are the reference's
+ * unfused FP64 values bit for bit.
+ *   cresvsp  (:264-306) r = -A(h1, h2) v - opgrad(pr - vdiff qtl / 3) + bf
+ *   crespsp  (:99-230)  the pressure right-hand side (curl curl of the
+ *            extrapolated velocity, opgrad qtl, A(1/vtrans, 0) pr, the
+ *            forcing, qtl bm1 bd(1)/dt; the mean removed when *null_space).
+ *            The reference adds face terms on inflow ('v', 'V', 'MV', 'mv',
+ *            'shl') and 'SYM' faces; these are not formed here, so the mesh
+ *            must have none (walls, outflow and periodic faces are fine). */
+int nekgpu_cresvsp_dev(const int64_t *handle, double *r1, double *r2, double *r3,
+                       const double *vx, const double *vy, const double *vz, const double *h1,
+                       const double *h2, const double *vdiff, const double *qtl,
+                       const double *pr, const double *bfx, const double *bfy,
+                       const double *bfz);
+int nekgpu_crespsp_dev(const int64_t *handle, double *respr, const double *vxe,
+                       const double *vye, const double *vze, const double *pr,
+                       const double *qtl, const double *vdiff, const double *vtrans,
+                       const double *bfx, const double *bfy, const double *bfz,
+                       const double *binv, const double *dtbd, const int *null_space);
+
 /* ---- a solve split over element shards ----------------------------------
  * The reference splits the mesh over MPI ranks; each rank's solve runs its
  * local operator and gather-scatter, exchanges the sums at the points it

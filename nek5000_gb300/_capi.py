@@ -68,6 +68,8 @@ SIGNATURES = {
     "nekgpu_dudxyz_dev": [_I64P, _P, _P, _IP],
     "nekgpu_cdtp_dev": [_I64P, _P, _P, _IP],
     "nekgpu_op_curl_dev": [_I64P, _P, _P, _P, _P, _P, _P, _IP, _P],
+    "nekgpu_cresvsp_dev": [_I64P] + [_P] * 14,
+    "nekgpu_crespsp_dev": [_I64P] + [_P] * 12 + [_DP, _IP],
     "nekgpu_col2_dev": [_I64P, _P, _P],
     "nekgpu_col3_dev": [_I64P, _P, _P, _P],
     "nekgpu_add2s1_dev": [_I64P, _P, _P, _DP],

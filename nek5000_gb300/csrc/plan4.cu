@@ -1,0 +1,254 @@
+// plan4.cu -- the explicit right-hand sides of the PN-PN splitting step
+// (plan4, core/plan4.f) on the device, composed from the library's
+// operator (axhelm), gradient-type operators (gradops.cu) and gather-scatter:
+//
+//   cresvsp  core/plan4.f:264-306  velocity residual
+//            resv = -A(h1, h2) v - opgrad(pr - vdiff qtl / 3) + bf
+//   crespsp  core/plan4.f:99-230   pressure right-hand side from the
+//            curl-curl of the extrapolated velocity, qtl, the pressure's own
+//            operator and the forcing
+//
+// Pointwise steps are rounded one by one in the reference's order; with the
+// handle's exact option the operator is too, and both residuals are then the
+// reference's unfused FP64 values bit for bit.  Not served: the stress
+// formulation (ifstrs) and crespsp's face terms, which the reference adds
+// only on inflow ('v', 'V', 'MV', 'mv', 'shl') and 'SYM' faces -- the caller
+// states that the mesh has none.
+#include <string>
+#include <vector>
+
+#include "impl.cuh"
+
+namespace nekgpu {
+namespace {
+
+int pblocks(int64_t n) { return (int)std::min<int64_t>((n + 255) / 256, 152 * 8); }
+
+#define PFOR(i, n) \
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+
+// ta = scale (vdiff qtl) + pr   (col3, add2s1)
+__global__ void p4_ta4_kernel(double* __restrict__ ta, const double* __restrict__ vdiff,
+                              const double* __restrict__ qtl, const double* __restrict__ pr,
+                              double scale, int64_t n) {
+  PFOR(i, n) ta[i] = __dadd_rn(__dmul_rn(scale, __dmul_rn(vdiff[i], qtl[i])), pr[i]);
+}
+
+// r = ((-r) - t) + bf   (opchsgn, opsub2, opadd2)
+__global__ void p4_resv_kernel(double* __restrict__ r, const double* __restrict__ t,
+                               const double* __restrict__ bf, int64_t n) {
+  PFOR(i, n) r[i] = __dadd_rn(__dsub_rn(-r[i], t[i]), bf[i]);
+}
+
+// wa = (wa bm1 + ta scale) (vdiff / vtrans)   (opcolv, opadd2cm, invcol3, opcolv)
+__global__ void p4_wa_kernel(double* __restrict__ wa, const double* __restrict__ ta,
+                             const double* __restrict__ bm1, const double* __restrict__ vdiff,
+                             const double* __restrict__ vtrans, double scale, int64_t n) {
+  PFOR(i, n) {
+    const double w = __dadd_rn(__dmul_rn(wa[i], bm1[i]), __dmul_rn(ta[i], scale));
+    wa[i] = __dmul_rn(w, __ddiv_rn(vdiff[i], vtrans[i]));
+  }
+}
+
+// h1 = 1 / vtrans, h2 = 0   (invers2, rzero)
+__global__ void p4_h_kernel(double* __restrict__ h1, double* __restrict__ h2,
+                            const double* __restrict__ vtrans, int64_t n) {
+  PFOR(i, n) {
+    h1[i] = __ddiv_rn(1.0, vtrans[i]);
+    h2[i] = 0.0;
+  }
+}
+
+// ta = bf / vtrans - wa
+__global__ void p4_tb_kernel(double* __restrict__ ta, const double* __restrict__ bf,
+                             const double* __restrict__ vtrans, const double* __restrict__ wa,
+                             int64_t n) {
+  PFOR(i, n) ta[i] = __dsub_rn(__ddiv_rn(bf[i], vtrans[i]), wa[i]);
+}
+
+// respr = (((-respr) + wa1 + wa2 + wa3) + (qtl bm1) dtbd)   (chsign, sum, admcol3)
+__global__ void p4_respr_kernel(double* __restrict__ respr, const double* __restrict__ w1,
+                                const double* __restrict__ w2, const double* __restrict__ w3,
+                                const double* __restrict__ qtl, const double* __restrict__ bm1,
+                                double dtbd, int64_t n) {
+  PFOR(i, n) {
+    double r = __dadd_rn(__dadd_rn(__dadd_rn(-respr[i], w1[i]), w2[i]), w3[i]);
+    respr[i] = __dadd_rn(r, __dmul_rn(__dmul_rn(qtl[i], bm1[i]), dtbd));
+  }
+}
+
+// partial[blk] = sum over the block's points (the ortho mean)
+__global__ void __launch_bounds__(256) p4_sum_kernel(const double* __restrict__ a, int64_t n,
+                                                     double* __restrict__ partial) {
+  __shared__ double red[8];
+  double s = 0.0;
+  PFOR(i, n) s += a[i];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int q = 0; q < 8; ++q) t += red[q];
+    partial[blockIdx.x] = t;
+  }
+}
+
+__global__ void p4_cadd_kernel(double* __restrict__ a, double c, int64_t n) {
+  PFOR(i, n) a[i] = __dadd_rn(a[i], c);
+}
+
+#undef PFOR
+
+int axhelm_any(Handle& h, double* au, const double* u, const Coef<double>& c) {
+  const cudaError_t e = h.exact ? launch_axhelm<double, true>(h.mesh, h.mesh.f64, au, u, c, h.stream)
+                                : launch_axhelm<double, false>(h.mesh, h.mesh.f64, au, u, c, h.stream);
+  return e == cudaSuccess ? 0 : -3;
+}
+
+}  // namespace
+}  // namespace nekgpu
+
+// ---------------------------------------------------------------------------
+// C ABI
+namespace nekgpu {
+Handle* handle_lookup(const int64_t* h);
+int handle_fail(Handle* H, int code, const std::string& msg);
+}  // namespace nekgpu
+
+using namespace nekgpu;
+
+namespace {
+
+Handle* p4_handle(const int64_t* handle, int* rc) {
+  Handle* H = handle_lookup(handle);
+  if (!H) {
+    *rc = handle_fail(nullptr, NEKGPU_EHANDLE, "unknown handle");
+    return nullptr;
+  }
+  if (cudaSetDevice(H->device) != cudaSuccess) {
+    *rc = handle_fail(H, NEKGPU_ECUDA, "cudaSetDevice failed");
+    return nullptr;
+  }
+  if (!H->has_mesh || !H->mesh.has_rst) {
+    *rc = handle_fail(H, NEKGPU_ENOSETUP,
+                      "metric terms not set up (the geometry must come from coordinates)");
+    return nullptr;
+  }
+  *rc = 0;
+  return H;
+}
+
+int p4_done(Handle* H, int rc, const char* what) {
+  const cudaError_t e = cudaGetLastError();
+  if (rc || e != cudaSuccess)
+    return handle_fail(H, NEKGPU_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
+  return NEKGPU_OK;
+}
+
+}  // namespace
+
+extern "C" int nekgpu_cresvsp_dev(const int64_t* handle, double* r1, double* r2, double* r3,
+                                  const double* vx, const double* vy, const double* vz,
+                                  const double* h1, const double* h2, const double* vdiff,
+                                  const double* qtl, const double* pr, const double* bfx,
+                                  const double* bfy, const double* bfz) {
+  int rc;
+  Handle* H = p4_handle(handle, &rc);
+  if (!H) return rc;
+  if (!r1 || !r2 || !r3 || !vx || !vy || !vz || !h1 || !h2 || !vdiff || !qtl || !pr || !bfx ||
+      !bfy || !bfz)
+    return handle_fail(H, NEKGPU_EINVAL, "null argument");
+  const int64_t n = H->mesh.n;
+  cudaStream_t s = H->stream;
+  if (H->io0.ensure(n) || H->io1.ensure(n) || H->io2.ensure(n) || H->io3.ensure(n))
+    return handle_fail(H, NEKGPU_ENOMEM, "device allocation failed");
+  Coef<double> c;
+  if (detect_coef<double>(*H, h1, h2, n, c))
+    return handle_fail(H, NEKGPU_ECUDA, "coefficient scan failed");
+  double* r[3] = {r1, r2, r3};
+  const double* v[3] = {vx, vy, vz};
+  const double* bf[3] = {bfx, bfy, bfz};
+  for (int k = 0; k < 3; ++k)  // ophx
+    if (axhelm_any(*H, r[k], v[k], c)) return p4_done(H, -3, "cresvsp operator");
+  double *ta = H->io0.ptr, *t[3] = {H->io1.ptr, H->io2.ptr, H->io3.ptr};
+  count_launch();
+  p4_ta4_kernel<<<pblocks(n), 256, 0, s>>>(ta, vdiff, qtl, pr, -1. / 3., n);
+  if (launch_gradop(*H, 0, t[0], t[1], t[2], ta, nullptr, nullptr, 0, nullptr))
+    return handle_fail(H, NEKGPU_EINVAL, "cresvsp: lx1 out of range");
+  for (int k = 0; k < 3; ++k) {
+    count_launch();
+    p4_resv_kernel<<<pblocks(n), 256, 0, s>>>(r[k], t[k], bf[k], n);
+  }
+  return p4_done(H, 0, "cresvsp");
+}
+
+extern "C" int nekgpu_crespsp_dev(const int64_t* handle, double* respr, const double* vxe,
+                                  const double* vye, const double* vze, const double* pr,
+                                  const double* qtl, const double* vdiff, const double* vtrans,
+                                  const double* bfx, const double* bfy, const double* bfz,
+                                  const double* binv, const double* dtbd, const int* null_space) {
+  int rc;
+  Handle* H = p4_handle(handle, &rc);
+  if (!H) return rc;
+  if (!respr || !vxe || !vye || !vze || !pr || !qtl || !vdiff || !vtrans || !bfx || !bfy ||
+      !bfz || !binv || !dtbd)
+    return handle_fail(H, NEKGPU_EINVAL, "null argument");
+  const int64_t n = H->mesh.n;
+  cudaStream_t s = H->stream;
+  if (H->io0.ensure(n) || H->io1.ensure(n) || H->io2.ensure(n) || H->io3.ensure(n) ||
+      H->io4.ensure(n) || H->io5.ensure(n) || H->io6.ensure(n) || H->io7.ensure(n) ||
+      H->red.ensure(152 * 8))
+    return handle_fail(H, NEKGPU_ENOMEM, "device allocation failed");
+  const double* bm1 = H->mesh.f64.bm1;
+  double *ta[3] = {H->io0.ptr, H->io1.ptr, H->io2.ptr}, *wa[3] = {H->io3.ptr, H->io4.ptr, H->io5.ptr};
+  double *hh1 = H->io6.ptr, *hh2 = H->io7.ptr;
+  const double* bf[3] = {bfx, bfy, bfz};
+  // curl curl of the extrapolated velocity, both curls averaged
+  if (launch_gradop(*H, 3, ta[0], ta[1], ta[2], vxe, vye, vze, 0, nullptr))
+    return handle_fail(H, NEKGPU_EINVAL, "crespsp: lx1 out of range");
+  for (double* w : ta) {
+    launch_mul_by(*H, w, bm1);
+    gs_op<double>(H->mesh.gs, w, 0, s);
+    launch_mul_by(*H, w, binv);
+  }
+  launch_gradop(*H, 3, wa[0], wa[1], wa[2], ta[0], ta[1], ta[2], 0, nullptr);
+  for (double* w : wa) {
+    launch_mul_by(*H, w, bm1);
+    gs_op<double>(H->mesh.gs, w, 0, s);
+    launch_mul_by(*H, w, binv);
+  }
+  launch_gradop(*H, 0, ta[0], ta[1], ta[2], qtl, nullptr, nullptr, 0, nullptr);  // opgrad(qtl)
+  for (int k = 0; k < 3; ++k) {
+    count_launch();
+    p4_wa_kernel<<<pblocks(n), 256, 0, s>>>(wa[k], ta[k], bm1, vdiff, vtrans, -4. / 3., n);
+  }
+  count_launch();
+  p4_h_kernel<<<pblocks(n), 256, 0, s>>>(hh1, hh2, vtrans, n);
+  Coef<double> c;
+  if (detect_coef<double>(*H, hh1, hh2, n, c))
+    return handle_fail(H, NEKGPU_ECUDA, "coefficient scan failed");
+  if (axhelm_any(*H, respr, pr, c)) return p4_done(H, -3, "crespsp operator");
+  for (int k = 0; k < 3; ++k) {
+    count_launch();
+    p4_tb_kernel<<<pblocks(n), 256, 0, s>>>(ta[k], bf[k], vtrans, wa[k], n);
+    gs_op<double>(H->mesh.gs, ta[k], 0, s);
+    launch_mul_by(*H, ta[k], binv);
+    launch_gradop(*H, 2, wa[k], nullptr, nullptr, ta[k], nullptr, nullptr, k, bm1);  // cdtp
+  }
+  count_launch();
+  p4_respr_kernel<<<pblocks(n), 256, 0, s>>>(respr, wa[0], wa[1], wa[2], qtl, bm1, *dtbd, n);
+  if (null_space && *null_space) {  // ortho
+    const int nb = pblocks(n);
+    count_launch();
+    p4_sum_kernel<<<nb, 256, 0, s>>>(respr, n, H->red.ptr);
+    std::vector<double> part((size_t)nb);
+    cudaMemcpyAsync(part.data(), H->red.ptr, nb * sizeof(double), cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return p4_done(H, -3, "crespsp ortho");
+    double sum = 0.0;
+    for (double v : part) sum += v;
+    count_launch();
+    p4_cadd_kernel<<<pblocks(n), 256, 0, s>>>(respr, -(sum / (double)n), n);
+  }
+  return p4_done(H, 0, "crespsp");
+}

@@ -208,6 +208,22 @@ class NekGpu:
                                                _ptr(u1), _ptr(u2), _ptr(u3),
                                                C.byref(_cint(int(bool(ifavg)))), _ptr(binv)))
 
+    def cresvsp(self, r, v, h1, h2, vdiff, qtl, pr, bf):
+        """velocity residual of the splitting step (r, v, bf: 3 device arrays each)"""
+        self._check(self._L.nekgpu_cresvsp_dev(C.byref(self._h), *[_ptr(a) for a in r],
+                                               *[_ptr(a) for a in v], _ptr(h1), _ptr(h2),
+                                               _ptr(vdiff), _ptr(qtl), _ptr(pr),
+                                               *[_ptr(a) for a in bf]))
+
+    def crespsp(self, respr, ve, pr, qtl, vdiff, vtrans, bf, binv, dtbd, null_space=False):
+        """pressure right-hand side of the splitting step (no inflow/SYM faces)"""
+        self._check(self._L.nekgpu_crespsp_dev(C.byref(self._h), _ptr(respr),
+                                               *[_ptr(a) for a in ve], _ptr(pr), _ptr(qtl),
+                                               _ptr(vdiff), _ptr(vtrans),
+                                               *[_ptr(a) for a in bf], _ptr(binv),
+                                               C.byref(_cdouble(dtbd)),
+                                               C.byref(_cint(int(bool(null_space))))))
+
     def h1mg_setup(self, x, y, z, glo_num, mask=None, fbc=None, null_space=False):
         """The pressure preconditioner h1mg_solve (nekgpu_h1mg_setup): host
         numpy coordinates, the numbering given to setup, and the pressure

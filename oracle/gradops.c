@@ -132,3 +132,88 @@ void ref_op_curl(const ref_ops *ops, double *w1, double *w2, double *w3, const d
   }
   free(a);
 }
+
+/* ---- the splitting step's residuals ---------------------------------------- */
+
+/* cresvsp (core/plan4.f:264-306), PN-PN without the stress formulation:
+ * resv = -A(h1, h2) v - wgradm1(pr - vdiff qtl / 3) + bf, per component. */
+void ref_cresvsp(const ref_ops *ops, double *r1, double *r2, double *r3, const double *vx,
+                 const double *vy, const double *vz, const double *h1, const double *h2,
+                 const double *vdiff, const double *qtl, const double *pr, const double *bfx,
+                 const double *bfy, const double *bfz, const double *rst) {
+  const int nx1 = ref_ops_nx1(ops), nel = ref_ops_nel(ops);
+  const int64_t n = ref_ops_n(ops);
+  double *ta = (double *)malloc(sizeof(double) * 4 * n), *t1 = ta + n, *t2 = t1 + n, *t3 = t2 + n;
+  double *r[3] = {r1, r2, r3};
+  const double *v[3] = {vx, vy, vz}, *bf[3] = {bfx, bfy, bfz};
+  for (int c = 0; c < 3; ++c) ref_axhelm(ops, r[c], v[c], h1, h2); /* ophx */
+  for (int c = 0; c < 3; ++c)
+    for (int64_t i = 0; i < n; ++i) r[c][i] = -r[c][i];             /* opchsgn */
+  const double scale = -1. / 3.;
+  for (int64_t i = 0; i < n; ++i) {
+    ta[i] = vdiff[i] * qtl[i];       /* col3 */
+    ta[i] = scale * ta[i] + pr[i];   /* add2s1 */
+  }
+  ref_wgradm1(nx1, nel, t1, t2, t3, ta, rst); /* opgrad */
+  const double *t[3] = {t1, t2, t3};
+  for (int c = 0; c < 3; ++c)
+    for (int64_t i = 0; i < n; ++i) {
+      r[c][i] = r[c][i] - t[c][i];   /* opsub2 */
+      r[c][i] = r[c][i] + bf[c][i];  /* opadd2 */
+    }
+  free(ta);
+}
+
+/* crespsp (core/plan4.f:99-230), PN-PN without the stress formulation and
+ * without the face terms (meshes with no 'v', 'V', 'MV', 'mv', 'shl' or
+ * 'SYM' face, where the reference adds none): the pressure right-hand side
+ * from the curl-curl of the extrapolated velocity, qtl, the pressure's own
+ * operator, the forcing, and dtbd = bd(1)/dt; the mean removed when
+ * null_space (ortho). */
+void ref_crespsp(const ref_ops *ops, double *respr, const double *vxe, const double *vye,
+                 const double *vze, const double *pr, const double *qtl, const double *vdiff,
+                 const double *vtrans, const double *bfx, const double *bfy, const double *bfz,
+                 const double *bm1, const double *binv, double dtbd, int null_space,
+                 const double *rst, const double *jac) {
+  const int nx1 = ref_ops_nx1(ops), nel = ref_ops_nel(ops);
+  const int64_t n = ref_ops_n(ops);
+  double *buf = (double *)malloc(sizeof(double) * 9 * n);
+  double *ta[3] = {buf, buf + n, buf + 2 * n}, *wa[3] = {buf + 3 * n, buf + 4 * n, buf + 5 * n};
+  double *w1 = buf + 6 * n, *w2 = buf + 7 * n, *w3 = buf + 8 * n;
+  const double *bf[3] = {bfx, bfy, bfz};
+  ref_op_curl(ops, ta[0], ta[1], ta[2], vxe, vye, vze, 1, rst, jac, bm1, binv);
+  ref_op_curl(ops, wa[0], wa[1], wa[2], ta[0], ta[1], ta[2], 1, rst, jac, bm1, binv);
+  for (int c = 0; c < 3; ++c)
+    for (int64_t i = 0; i < n; ++i) wa[c][i] = wa[c][i] * bm1[i]; /* opcolv */
+  ref_wgradm1(nx1, nel, ta[0], ta[1], ta[2], qtl, rst);            /* opgrad */
+  const double scale = -4. / 3.;
+  for (int c = 0; c < 3; ++c)
+    for (int64_t i = 0; i < n; ++i) wa[c][i] = wa[c][i] + ta[c][i] * scale; /* opadd2cm */
+  for (int64_t i = 0; i < n; ++i) w1[i] = vdiff[i] / vtrans[i];              /* invcol3 */
+  for (int c = 0; c < 3; ++c)
+    for (int64_t i = 0; i < n; ++i) wa[c][i] = wa[c][i] * w1[i];            /* opcolv */
+  for (int64_t i = 0; i < n; ++i) {
+    ta[0][i] = 1.0 / vtrans[i]; /* invers2 */
+    ta[1][i] = 0.0;
+  }
+  ref_axhelm(ops, respr, pr, ta[0], ta[1]);
+  for (int64_t i = 0; i < n; ++i) respr[i] = -respr[i]; /* chsign */
+  for (int c = 0; c < 3; ++c)
+    for (int64_t i = 0; i < n; ++i) ta[c][i] = bf[c][i] / vtrans[i] - wa[c][i];
+  for (int c = 0; c < 3; ++c) {
+    ref_dssum(ops, ta[c]); /* opdssum */
+    for (int64_t i = 0; i < n; ++i) ta[c][i] = ta[c][i] * binv[i];
+  }
+  for (int c = 0; c < 3; ++c) ref_cdtp(nx1, nel, wa[c], ta[c], rst, jac, bm1, c + 1);
+  for (int64_t i = 0; i < n; ++i) respr[i] = respr[i] + wa[0][i] + wa[1][i] + wa[2][i];
+  for (int64_t i = 0; i < n; ++i) respr[i] = respr[i] + qtl[i] * bm1[i] * dtbd; /* admcol3 */
+  if (null_space) { /* ortho: the mean over all points removed */
+    double s = 0.0;
+    for (int64_t i = 0; i < n; ++i) s = s + respr[i];
+    const double m = s / (double)n;
+    for (int64_t i = 0; i < n; ++i) respr[i] = respr[i] - m;
+  }
+  (void)w2;
+  (void)w3;
+  free(buf);
+}

@@ -186,6 +186,16 @@ void ref_op_curl(const ref_ops *ops, double *w1, double *w2, double *w3, const d
                  const double *u2, const double *u3, int ifavg, const double *rst,
                  const double *jac, const double *bm1, const double *binv);
 
+void ref_cresvsp(const ref_ops *ops, double *r1, double *r2, double *r3, const double *vx,
+                 const double *vy, const double *vz, const double *h1, const double *h2,
+                 const double *vdiff, const double *qtl, const double *pr, const double *bfx,
+                 const double *bfy, const double *bfz, const double *rst);
+void ref_crespsp(const ref_ops *ops, double *respr, const double *vxe, const double *vye,
+                 const double *vze, const double *pr, const double *qtl, const double *vdiff,
+                 const double *vtrans, const double *bfx, const double *bfy, const double *bfz,
+                 const double *bm1, const double *binv, double dtbd, int null_space,
+                 const double *rst, const double *jac);
+
 /* sizes of an operator state */
 int ref_ops_nx1(const ref_ops *ops);
 int ref_ops_nel(const ref_ops *ops);

@@ -78,6 +78,8 @@ def lib():
             L.ref_dudxyz.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp, _dp, C.c_int]
             L.ref_op_curl.argtypes = [_vp, _dp, _dp, _dp, _dp, _dp, _dp, C.c_int, _dp, _dp, _dp,
                                       _dp]
+            L.ref_cresvsp.argtypes = [_vp] + [_dp] * 15
+            L.ref_crespsp.argtypes = [_vp] + [_dp] * 13 + [C.c_double, C.c_int, _dp, _dp]
             L.ref_fdm1d.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
                                     _dp, _dp]
             L.ref_gmres_h1mg.argtypes = [_vp, _vp, _dp, _dp, _dp, _dp, _dp, C.c_double, C.c_int,
@@ -442,6 +444,23 @@ def op_curl(ops, u1, u2, u3, rst, jac, bm1, binv, ifavg=True):
     out = [np.zeros(ops.n) for _ in range(3)]
     lib().ref_op_curl(ops.h, *out, _c(u1), _c(u2), _c(u3), int(bool(ifavg)), _c(rst), _c(jac),
                       _c(bm1), _c(binv))
+    return out
+
+
+def cresvsp(ops, v, h1, h2, vdiff, qtl, pr, bf, rst):
+    """velocity residual of the splitting step; v, bf: 3 components"""
+    out = [np.zeros(ops.n) for _ in range(3)]
+    lib().ref_cresvsp(ops.h, *out, *[_c(a) for a in v], _c(h1), _c(h2), _c(vdiff), _c(qtl),
+                      _c(pr), *[_c(a) for a in bf], _c(rst))
+    return out
+
+
+def crespsp(ops, ve, pr, qtl, vdiff, vtrans, bf, bm1, binv, dtbd, null_space, rst, jac):
+    """pressure right-hand side of the splitting step (no inflow/SYM faces)"""
+    out = np.zeros(ops.n)
+    lib().ref_crespsp(ops.h, out, *[_c(a) for a in ve], _c(pr), _c(qtl), _c(vdiff), _c(vtrans),
+                      *[_c(a) for a in bf], _c(bm1), _c(binv), float(dtbd),
+                      int(bool(null_space)), _c(rst), _c(jac))
     return out
 
 

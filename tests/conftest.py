@@ -18,7 +18,8 @@ def pytest_configure(config):
 # shards on the operator, gather-scatter and Krylov solves the other files
 # test) run after them, so that a failure there is reported after, not
 # instead of, the results of what it builds on.
-_BUILT_ON_THE_REST = ("test_gpu_gradops.py", "test_gpu_h1mg.py", "test_gpu_shard.py")
+_BUILT_ON_THE_REST = ("test_gpu_gradops.py", "test_gpu_h1mg.py", "test_gpu_plan4.py",
+                      "test_gpu_shard.py")
 
 
 def pytest_collection_modifyitems(session, config, items):

@@ -1,0 +1,49 @@
+"""The splitting step's right-hand sides on the device (nekgpu_cresvsp_dev,
+nekgpu_crespsp_dev) against the oracle (oracle/gradops.c): bit for bit with
+the handle's exact option (every product and sum rounded in the reference's
+order), to 1e-12 with the default fused operator; the null-space mean of
+crespsp is a block-order sum, so that case is compared to 1e-13."""
+import numpy as np
+import pytest
+
+from conftest import rng_unit_vector
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("exact", [True, False])
+def test_residuals_match_the_oracle(gpu_lib, oracle, exact):
+    torch = pytest.importorskip("torch")
+    P = oracle.box_problem(6, 3, 2, 2, v=rng_unit_vector(161))
+    nx1, nel, n, ops = P["nx1"], P["nel"], P["n"], P["ops"]
+    rst, jac = oracle.geom_rst(nx1, nel, P["x"], P["y"], P["z"])
+    rng = np.random.default_rng(162)
+    rnd = lambda: rng.standard_normal(n)
+    v, bf = [rnd() for _ in range(3)], [rnd() for _ in range(3)]
+    h1, h2 = 1.0 + 0.1 * np.abs(rnd()), np.abs(rnd())
+    vdiff, qtl, pr = 1.0 + 0.1 * np.abs(rnd()), rnd(), rnd()
+    vtrans = 1.0 + 0.2 * np.abs(rnd())
+    lib = gpu_lib(0)
+    lib.setup_xyz(nx1, nel, P["D"], P["wgll"], P["x"], P["y"], P["z"], P["glo_num"])
+    lib.set_exact(exact)
+    dev = lambda a: torch.tensor(np.ascontiguousarray(a), device="cuda")
+    zeros = lambda: torch.zeros(n, dtype=torch.float64, device="cuda")
+    cmp = (lambda a, b: np.array_equal(a, b)) if exact else \
+        (lambda a, b: np.allclose(a, b, rtol=0, atol=1e-12 * np.abs(b).max()))
+    r = [zeros() for _ in range(3)]
+    lib.cresvsp(r, [dev(a) for a in v], dev(h1), dev(h2), dev(vdiff), dev(qtl), dev(pr),
+                [dev(a) for a in bf])
+    want = oracle.cresvsp(ops, v, h1, h2, vdiff, qtl, pr, bf, rst)
+    for a, b in zip(r, want):
+        assert cmp(a.cpu().numpy(), b)
+    for null in (False, True):
+        respr = zeros()
+        lib.crespsp(respr, [dev(a) for a in v], dev(pr), dev(qtl), dev(vdiff), dev(vtrans),
+                    [dev(a) for a in bf], dev(P["binv"]), 1.5, null_space=null)
+        want = oracle.crespsp(ops, v, pr, qtl, vdiff, vtrans, bf, P["bm1"], P["binv"], 1.5,
+                              null, rst, jac)
+        got = respr.cpu().numpy()
+        if null:
+            assert np.allclose(got, want, rtol=0, atol=1e-13 * np.abs(want).max())
+        else:
+            assert cmp(got, want)

@@ -46,3 +46,23 @@ def test_cdtp_is_the_transpose_of_the_weighted_derivative(oracle):
         lhs = np.dot(v, oracle.cdtp(nx1, nel, x, rst, jac, P["bm1"], isd))
         rhs = np.dot(x, P["bm1"] * oracle.dudxyz(nx1, nel, v, rst, jac, isd))
         assert abs(lhs - rhs) <= 1e-12 * (abs(lhs) + abs(rhs))
+
+
+def test_splitting_residuals_on_known_fields(oracle):
+    """cresvsp with v = 0, qtl = 0: r = bf - bm1 grad(pr), exact for a linear
+    pr; crespsp with a rigid rotation (curl curl = 0), bf = 0 and qtl = 0:
+    respr = -A(1/vtrans, 0) pr."""
+    P, rst, jac = _mesh(oracle)
+    n, ops = P["n"], P["ops"]
+    z0 = np.zeros(n)
+    pr = 0.7 * P["x"] - 0.2 * P["z"]
+    bf = [np.full(n, 0.1), np.full(n, -0.3), np.full(n, 0.5)]
+    r = oracle.cresvsp(ops, [z0, z0, z0], np.ones(n), z0, np.ones(n), z0, pr, bf, rst)
+    for c, g in enumerate((0.7, 0.0, -0.2)):
+        assert np.allclose(r[c], bf[c] - g * P["bm1"], rtol=0, atol=1e-11)
+    vtrans = np.full(n, 2.0)
+    ve = [-P["y"], P["x"], z0]
+    respr = oracle.crespsp(ops, ve, pr, z0, np.ones(n), vtrans, [z0, z0, z0], P["bm1"],
+                           P["binv"], 1.5, False, rst, jac)
+    want = -ops.axhelm(pr, 1.0 / vtrans, z0)
+    assert np.allclose(respr, want, rtol=0, atol=1e-10 * np.abs(want).max())
