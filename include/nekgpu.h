@@ -163,6 +163,13 @@ int nekgpu_cdtp_dev(const int64_t *handle, double *dtx, const double *x, const i
 int nekgpu_op_curl_dev(const int64_t *handle, double *w1, double *w2, double *w3,
                        const double *u1, const double *u2, const double *u3, const int *ifavg,
                        const double *binv);
+/* The convective term without dealiasing (conv1, core/navier1.f:3276; what
+ * convop uses when dealiasing is off): du = (v . grad) u, and advab
+ * (:1516): bf_c -= bm1 (v . grad) v_c for the three components. */
+int nekgpu_conv1_dev(const int64_t *handle, double *du, const double *u, const double *vx,
+                     const double *vy, const double *vz);
+int nekgpu_advab_dev(const int64_t *handle, double *bfx, double *bfy, double *bfz,
+                     const double *vx, const double *vy, const double *vz);
 
 /* The splitting step's explicit right-hand sides (plan4, core/plan4.f), on
  * device arrays, PN-PN without the stress formulation.  Same setup needs as

@@ -180,6 +180,44 @@ __global__ void __launch_bounds__(NX* NX) curl_kernel(double* __restrict__ w1,
   }
 }
 
+// du = (1/J) (vx (rx u_r + sx u_s + tx u_t) + vy (...) + vz (...))   (conv1)
+template <int NX>
+__global__ void __launch_bounds__(NX* NX) conv1_kernel(double* __restrict__ du,
+                                                       const double* __restrict__ u,
+                                                       const double* __restrict__ vx,
+                                                       const double* __restrict__ vy,
+                                                       const double* __restrict__ vz,
+                                                       const double* __restrict__ rst,
+                                                       const double* __restrict__ jac,
+                                                       const double* __restrict__ D, int64_t n) {
+  constexpr int P = NX * NX * NX;
+  __shared__ double su[P], sD[NX * NX];
+  const int64_t eo = (int64_t)blockIdx.x * P;
+  const int tid = threadIdx.x;
+  for (int q = tid; q < P; q += NX * NX) su[q] = u[eo + q];
+  for (int q = tid; q < NX * NX; q += NX * NX) sD[q] = D[q];
+  __syncthreads();
+  const int i = tid % NX, j = tid / NX;
+  for (int k = 0; k < NX; ++k) {
+    const int64_t g = eo + i + NX * (j + NX * k);
+    double ur, us, ut;
+    grad_at<NX>(su, sD, i, j, k, ur, us, ut);
+    const double a = dot3(rst[g], ur, rst[3 * n + g], us, rst[6 * n + g], ut);
+    const double b = dot3(rst[n + g], ur, rst[4 * n + g], us, rst[7 * n + g], ut);
+    const double c = dot3(rst[2 * n + g], ur, rst[5 * n + g], us, rst[8 * n + g], ut);
+    const double sum = dot3(vx[g], a, vy[g], b, vz[g], c);
+    du[g] = __dmul_rn(__ddiv_rn(1.0, jac[g]), sum);
+  }
+}
+
+// bf = bf - bm1 ta   (subcol3)
+__global__ void subcol3_kernel(double* __restrict__ bf, const double* __restrict__ bm1,
+                               const double* __restrict__ ta, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    bf[i] = __dsub_rn(bf[i], __dmul_rn(bm1[i], ta[i]));
+}
+
 __global__ void mul_by_kernel(double* __restrict__ a, const double* __restrict__ b, int64_t n) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
@@ -226,6 +264,40 @@ int launch_gradop(Handle& h, int op, double* o1, double* o2, double* o3, const d
       return -1;
   }
   return 0;
+}
+
+int launch_conv1(Handle& h, double* du, const double* u, const double* vx, const double* vy,
+                 const double* vz) {
+  Mesh& M = h.mesh;
+  const int64_t n = M.n;
+  count_launch();
+  switch (M.nx1) {
+#define NEKGPU_CONV_CASE(N)                                                                      \
+  case N:                                                                                        \
+    conv1_kernel<N><<<M.nel, N * N, 0, h.stream>>>(du, u, vx, vy, vz, M.rst.ptr, M.jac.ptr,      \
+                                                   M.f64.D, n);                                  \
+    break;
+    NEKGPU_CONV_CASE(2)
+    NEKGPU_CONV_CASE(3)
+    NEKGPU_CONV_CASE(4)
+    NEKGPU_CONV_CASE(5)
+    NEKGPU_CONV_CASE(6)
+    NEKGPU_CONV_CASE(7)
+    NEKGPU_CONV_CASE(8)
+    NEKGPU_CONV_CASE(9)
+    NEKGPU_CONV_CASE(10)
+    NEKGPU_CONV_CASE(11)
+    NEKGPU_CONV_CASE(12)
+#undef NEKGPU_CONV_CASE
+    default:
+      return -1;
+  }
+  return 0;
+}
+
+void launch_subcol3(Handle& h, double* bf, const double* ta) {
+  count_launch();
+  subcol3_kernel<<<nblk(h.mesh.n), 256, 0, h.stream>>>(bf, h.mesh.f64.bm1, ta, h.mesh.n);
 }
 
 void launch_mul_by(Handle& h, double* a, const double* b) {
@@ -327,4 +399,30 @@ extern "C" int nekgpu_op_curl_dev(const int64_t* handle, double* w1, double* w2,
     launch_mul_by(*H, c, binv);
   }
   return grad_done(H, 0, "op_curl average");
+}
+
+extern "C" int nekgpu_conv1_dev(const int64_t* handle, double* du, const double* u,
+                                const double* vx, const double* vy, const double* vz) {
+  int rc;
+  Handle* H = grad_handle(handle, &rc);
+  if (!H) return rc;
+  if (!du || !u || !vx || !vy || !vz) return handle_fail(H, NEKGPU_EINVAL, "null argument");
+  return grad_done(H, launch_conv1(*H, du, u, vx, vy, vz), "conv1");
+}
+
+extern "C" int nekgpu_advab_dev(const int64_t* handle, double* bfx, double* bfy, double* bfz,
+                                const double* vx, const double* vy, const double* vz) {
+  int rc;
+  Handle* H = grad_handle(handle, &rc);
+  if (!H) return rc;
+  if (!bfx || !bfy || !bfz || !vx || !vy || !vz)
+    return handle_fail(H, NEKGPU_EINVAL, "null argument");
+  if (H->io0.ensure(H->mesh.n)) return handle_fail(H, NEKGPU_ENOMEM, "device allocation failed");
+  double* bf[3] = {bfx, bfy, bfz};
+  const double* v[3] = {vx, vy, vz};
+  for (int c = 0; c < 3; ++c) {
+    if (launch_conv1(*H, H->io0.ptr, v[c], vx, vy, vz)) return grad_done(H, -1, "advab");
+    launch_subcol3(*H, bf[c], H->io0.ptr);
+  }
+  return grad_done(H, 0, "advab");
 }

@@ -208,6 +208,16 @@ class NekGpu:
                                                _ptr(u1), _ptr(u2), _ptr(u3),
                                                C.byref(_cint(int(bool(ifavg)))), _ptr(binv)))
 
+    def conv1(self, du, u, v):
+        """du = (v . grad) u without dealiasing (device arrays; v: 3 components)"""
+        self._check(self._L.nekgpu_conv1_dev(C.byref(self._h), _ptr(du), _ptr(u),
+                                             *[_ptr(a) for a in v]))
+
+    def advab(self, bf, v):
+        """bf_c -= bm1 (v . grad) v_c (device arrays, 3 components each)"""
+        self._check(self._L.nekgpu_advab_dev(C.byref(self._h), *[_ptr(a) for a in bf],
+                                             *[_ptr(a) for a in v]))
+
     def cresvsp(self, r, v, h1, h2, vdiff, qtl, pr, bf):
         """velocity residual of the splitting step (r, v, bf: 3 device arrays each)"""
         self._check(self._L.nekgpu_cresvsp_dev(C.byref(self._h), *[_ptr(a) for a in r],

@@ -217,3 +217,44 @@ void ref_crespsp(const ref_ops *ops, double *respr, const double *vxe, const dou
   (void)w3;
   free(buf);
 }
+
+/* conv1 (core/navier1.f:3276-3330): du = jacmi (vx (rx u_r + sx u_s + tx u_t)
+ * + vy (ry u_r + ...) + vz (rz u_r + ...)), the convective term without
+ * dealiasing (convop with ifdeal false, :3138) */
+void ref_conv1(int nx1, int nel, double *du, const double *u, const double *vx, const double *vy,
+               const double *vz, const double *rst, const double *jac) {
+  const int nxyz = nx1 * nx1 * nx1;
+  const int64_t n = (int64_t)nxyz * nel;
+  double d[1024], dt[1024];
+  double *ur = (double *)malloc(sizeof(double) * 3 * nxyz), *us = ur + nxyz, *ut = us + nxyz;
+  dmat(nx1, d, dt, NULL);
+  const double *rx = rst, *ry = rst + n, *rz = rst + 2 * n, *sx = rst + 3 * n, *sy = rst + 4 * n,
+               *sz = rst + 5 * n, *tx = rst + 6 * n, *ty = rst + 7 * n, *tz = rst + 8 * n;
+  for (int e = 0; e < nel; ++e) {
+    const int64_t o = (int64_t)nxyz * e;
+    ref_local_grad3(ur, us, ut, u + o, nx1 - 1, d, dt);
+    for (int i = 0; i < nxyz; ++i) {
+      const int64_t p = o + i;
+      const double jacmi = 1.0 / jac[p];
+      du[p] = jacmi * (vx[p] * (rx[p] * ur[i] + sx[p] * us[i] + tx[p] * ut[i]) +
+                       vy[p] * (ry[p] * ur[i] + sy[p] * us[i] + ty[p] * ut[i]) +
+                       vz[p] * (rz[p] * ur[i] + sz[p] * us[i] + tz[p] * ut[i]));
+    }
+  }
+  free(ur);
+}
+
+/* advab (core/navier1.f:1516-1546): bf -= bm1 conv(v_c), per component */
+void ref_advab(int nx1, int nel, double *bfx, double *bfy, double *bfz, const double *vx,
+               const double *vy, const double *vz, const double *bm1, const double *rst,
+               const double *jac) {
+  const int64_t n = (int64_t)nx1 * nx1 * nx1 * nel;
+  double *ta = (double *)malloc(sizeof(double) * n);
+  double *bf[3] = {bfx, bfy, bfz};
+  const double *v[3] = {vx, vy, vz};
+  for (int c = 0; c < 3; ++c) {
+    ref_conv1(nx1, nel, ta, v[c], vx, vy, vz, rst, jac);
+    for (int64_t i = 0; i < n; ++i) bf[c][i] = bf[c][i] - bm1[i] * ta[i]; /* subcol3 */
+  }
+  free(ta);
+}

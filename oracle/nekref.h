@@ -196,6 +196,12 @@ void ref_crespsp(const ref_ops *ops, double *respr, const double *vxe, const dou
                  const double *bm1, const double *binv, double dtbd, int null_space,
                  const double *rst, const double *jac);
 
+void ref_conv1(int nx1, int nel, double *du, const double *u, const double *vx, const double *vy,
+               const double *vz, const double *rst, const double *jac);
+void ref_advab(int nx1, int nel, double *bfx, double *bfy, double *bfz, const double *vx,
+               const double *vy, const double *vz, const double *bm1, const double *rst,
+               const double *jac);
+
 /* sizes of an operator state */
 int ref_ops_nx1(const ref_ops *ops);
 int ref_ops_nel(const ref_ops *ops);

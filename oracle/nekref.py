@@ -78,6 +78,8 @@ def lib():
             L.ref_dudxyz.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp, _dp, C.c_int]
             L.ref_op_curl.argtypes = [_vp, _dp, _dp, _dp, _dp, _dp, _dp, C.c_int, _dp, _dp, _dp,
                                       _dp]
+            L.ref_conv1.argtypes = [C.c_int, C.c_int] + [_dp] * 7
+            L.ref_advab.argtypes = [C.c_int, C.c_int] + [_dp] * 9
             L.ref_cresvsp.argtypes = [_vp] + [_dp] * 15
             L.ref_crespsp.argtypes = [_vp] + [_dp] * 13 + [C.c_double, C.c_int, _dp, _dp]
             L.ref_fdm1d.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
@@ -444,6 +446,18 @@ def op_curl(ops, u1, u2, u3, rst, jac, bm1, binv, ifavg=True):
     out = [np.zeros(ops.n) for _ in range(3)]
     lib().ref_op_curl(ops.h, *out, _c(u1), _c(u2), _c(u3), int(bool(ifavg)), _c(rst), _c(jac),
                       _c(bm1), _c(binv))
+    return out
+
+
+def conv1(nx1, nel, u, v, rst, jac):
+    out = np.zeros(nx1 ** 3 * nel)
+    lib().ref_conv1(int(nx1), int(nel), out, _c(u), *[_c(a) for a in v], _c(rst), _c(jac))
+    return out
+
+
+def advab(nx1, nel, bf, v, bm1, rst, jac):
+    out = [np.array(a, dtype=np.float64, copy=True) for a in bf]
+    lib().ref_advab(int(nx1), int(nel), *out, *[_c(a) for a in v], _c(bm1), _c(rst), _c(jac))
     return out
 
 

@@ -57,3 +57,24 @@ def test_gradops_need_coordinates(gpu_lib, oracle):
     with pytest.raises(_capi.NekGpuError) as ei:
         lib.dudxyz(u.clone(), u, 1)
     assert ei.value.code == _capi.ENOSETUP
+
+
+def test_convection_matches_the_oracle_bit_for_bit(gpu_lib, oracle):
+    torch = pytest.importorskip("torch")
+    P = oracle.box_problem(7, 3, 2, 2, v=rng_unit_vector(155))
+    nx1, nel, n = P["nx1"], P["nel"], P["n"]
+    rst, jac = oracle.geom_rst(nx1, nel, P["x"], P["y"], P["z"])
+    lib = gpu_lib(0)
+    lib.setup_xyz(nx1, nel, P["D"], P["wgll"], P["x"], P["y"], P["z"], P["glo_num"])
+    rng = np.random.default_rng(156)
+    v = [rng.standard_normal(n) for _ in range(3)]
+    u = rng.standard_normal(n)
+    dev = lambda a: torch.tensor(np.ascontiguousarray(a), device="cuda")
+    du = torch.zeros(n, dtype=torch.float64, device="cuda")
+    lib.conv1(du, dev(u), [dev(a) for a in v])
+    assert np.array_equal(du.cpu().numpy(), oracle.conv1(nx1, nel, u, v, rst, jac))
+    bf = [rng.standard_normal(n) for _ in range(3)]
+    bfd = [dev(a) for a in bf]
+    lib.advab(bfd, [dev(a) for a in v])
+    for a, b in zip(bfd, oracle.advab(nx1, nel, bf, v, P["bm1"], rst, jac)):
+        assert np.array_equal(a.cpu().numpy(), b)

@@ -66,3 +66,21 @@ def test_splitting_residuals_on_known_fields(oracle):
                            P["binv"], 1.5, False, rst, jac)
     want = -ops.axhelm(pr, 1.0 / vtrans, z0)
     assert np.allclose(respr, want, rtol=0, atol=1e-10 * np.abs(want).max())
+
+
+def test_convection_of_a_linear_field(oracle):
+    """conv1 of u = a.x in the velocity field v: v.a, exact for linear u;
+    advab subtracts bm1 times it from the forcing."""
+    P, rst, jac = _mesh(oracle)
+    nx1, nel, n = P["nx1"], P["nel"], P["n"]
+    rng = np.random.default_rng(143)
+    v = [rng.standard_normal(n) for _ in range(3)]
+    a = np.array([0.5, -0.25, 1.5])
+    u = a[0] * P["x"] + a[1] * P["y"] + a[2] * P["z"]
+    c = oracle.conv1(nx1, nel, u, v, rst, jac)
+    assert np.allclose(c, a[0] * v[0] + a[1] * v[1] + a[2] * v[2], rtol=0, atol=1e-10)
+    bf = [np.ones(n), np.zeros(n), -np.ones(n)]
+    out = oracle.advab(nx1, nel, bf, v, P["bm1"], rst, jac)
+    for k in range(3):
+        ck = oracle.conv1(nx1, nel, v[k], v, rst, jac)
+        assert np.array_equal(out[k], bf[k] - P["bm1"] * ck)
