@@ -193,6 +193,24 @@ int nekgpu_crespsp_dev(const int64_t *handle, double *respr, const double *vxe,
                        const double *bfx, const double *bfy, const double *bfz,
                        const double *binv, const double *dtbd, const int *null_space);
 
+/* The step's time-integration bookkeeping, one velocity component per call
+ * (fixed geometry, constant-density flow):
+ *   makeabf (core/navier1.f:1597) extrapolated forcing: ta = ab1 abx1 +
+ *           ab2 abx2; abx2 = abx1; abx1 = bf; bf = (ab0 bf + ta) vtrans
+ *           (ab: the 3 coefficients of setab3)
+ *   makebdf (:1548) bf += (v bm1 bd(2) + sum over the lags of vlag bm1
+ *           bd(l+1)) vtrans / dt; bd: nbd + 1 coefficients (1 <= nbd <= 3);
+ *           vlag: nbd - 1 lagged fields of n, back to back
+ *   sumab   (core/plan4.f:525) v = ab0 vv + ab1 vvlag_1 (+ ab2 vvlag_2 when
+ *           nab = 3); vvlag: the lagged fields back to back */
+int nekgpu_makeabf_dev(const int64_t *handle, double *bf, double *abx1, double *abx2,
+                       const double *vtrans, const double *ab);
+int nekgpu_makebdf_dev(const int64_t *handle, double *bf, const double *v, const double *vlag,
+                       const double *vtrans, const double *bd, const int *nbd,
+                       const double *dt);
+int nekgpu_sumab_dev(const int64_t *handle, double *v, const double *vv, const double *vvlag,
+                     const double *ab, const int *nab);
+
 /* ---- a solve split over element shards ----------------------------------
  * The reference splits the mesh over MPI ranks; each rank's solve runs its
  * local operator and gather-scatter, exchanges the sums at the points it

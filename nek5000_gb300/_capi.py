@@ -70,6 +70,9 @@ SIGNATURES = {
     "nekgpu_op_curl_dev": [_I64P, _P, _P, _P, _P, _P, _P, _IP, _P],
     "nekgpu_conv1_dev": [_I64P] + [_P] * 5,
     "nekgpu_advab_dev": [_I64P] + [_P] * 6,
+    "nekgpu_makeabf_dev": [_I64P, _P, _P, _P, _P, _P],
+    "nekgpu_makebdf_dev": [_I64P, _P, _P, _P, _P, _P, _IP, _DP],
+    "nekgpu_sumab_dev": [_I64P, _P, _P, _P, _P, _IP],
     "nekgpu_cresvsp_dev": [_I64P] + [_P] * 14,
     "nekgpu_crespsp_dev": [_I64P] + [_P] * 12 + [_DP, _IP],
     "nekgpu_col2_dev": [_I64P, _P, _P],

@@ -98,6 +98,51 @@ __global__ void p4_cadd_kernel(double* __restrict__ a, double c, int64_t n) {
   PFOR(i, n) a[i] = __dadd_rn(a[i], c);
 }
 
+// makeabf, one component: ta = ab1 abx1 + ab2 abx2; abx2 = abx1; abx1 = bf;
+// bf = (ab0 bf + ta) vtrans
+__global__ void p4_makeabf_kernel(double* __restrict__ bf, double* __restrict__ abx1,
+                                  double* __restrict__ abx2, const double* __restrict__ vtrans,
+                                  double ab0, double ab1, double ab2, int64_t n) {
+  PFOR(i, n) {
+    const double a1 = abx1[i];
+    const double ta = __dadd_rn(__dmul_rn(ab1, a1), __dmul_rn(ab2, abx2[i]));
+    const double b = bf[i];
+    abx2[i] = a1;
+    abx1[i] = b;
+    bf[i] = __dmul_rn(__dadd_rn(__dmul_rn(ab0, b), ta), vtrans[i]);
+  }
+}
+
+struct Bd {
+  double c[4];
+};
+
+// makebdf, one component: bf += (v bm1 bd1 + sum_l vlag_l bm1 bd_{l+1}) (vtrans / dt)
+__global__ void p4_makebdf_kernel(double* __restrict__ bf, const double* __restrict__ v,
+                                  const double* __restrict__ vlag, int nlag,
+                                  const double* __restrict__ bm1,
+                                  const double* __restrict__ vtrans, Bd bd, double cnst,
+                                  int64_t n) {
+  PFOR(i, n) {
+    const double h2 = __dmul_rn(vtrans[i], cnst);
+    double tb = __dmul_rn(__dmul_rn(v[i], bm1[i]), bd.c[1]);
+    for (int l = 0; l < nlag; ++l)
+      tb = __dadd_rn(tb, __dmul_rn(__dmul_rn(vlag[(int64_t)l * n + i], bm1[i]), bd.c[l + 2]));
+    bf[i] = __dadd_rn(bf[i], __dmul_rn(tb, h2));
+  }
+}
+
+// sumab: v = ab0 vv + ab1 vvlag_1 (+ ab2 vvlag_2)
+__global__ void p4_sumab_kernel(double* __restrict__ v, const double* __restrict__ vv,
+                                const double* __restrict__ vvlag, double ab0, double ab1,
+                                double ab2, int nab, int64_t n) {
+  PFOR(i, n) {
+    double a = __dadd_rn(__dmul_rn(ab0, vv[i]), __dmul_rn(ab1, vvlag[i]));
+    if (nab == 3) a = __dadd_rn(a, __dmul_rn(ab2, vvlag[n + i]));
+    v[i] = a;
+  }
+}
+
 #undef PFOR
 
 int axhelm_any(Handle& h, double* au, const double* u, const Coef<double>& c) {
@@ -251,4 +296,70 @@ extern "C" int nekgpu_crespsp_dev(const int64_t* handle, double* respr, const do
     p4_cadd_kernel<<<pblocks(n), 256, 0, s>>>(respr, -(sum / (double)n), n);
   }
   return p4_done(H, 0, "crespsp");
+}
+
+namespace {
+
+Handle* p4_mesh_handle(const int64_t* handle, int* rc) {
+  Handle* H = handle_lookup(handle);
+  if (!H) {
+    *rc = handle_fail(nullptr, NEKGPU_EHANDLE, "unknown handle");
+    return nullptr;
+  }
+  if (cudaSetDevice(H->device) != cudaSuccess) {
+    *rc = handle_fail(H, NEKGPU_ECUDA, "cudaSetDevice failed");
+    return nullptr;
+  }
+  if (!H->has_mesh) {
+    *rc = handle_fail(H, NEKGPU_ENOSETUP, "mesh not set up (nekgpu_setup)");
+    return nullptr;
+  }
+  *rc = 0;
+  return H;
+}
+
+}  // namespace
+
+extern "C" int nekgpu_makeabf_dev(const int64_t* handle, double* bf, double* abx1, double* abx2,
+                                  const double* vtrans, const double* ab) {
+  int rc;
+  Handle* H = p4_mesh_handle(handle, &rc);
+  if (!H) return rc;
+  if (!bf || !abx1 || !abx2 || !vtrans || !ab) return handle_fail(H, NEKGPU_EINVAL, "null argument");
+  const int64_t n = H->mesh.n;
+  count_launch();
+  p4_makeabf_kernel<<<pblocks(n), 256, 0, H->stream>>>(bf, abx1, abx2, vtrans, ab[0], ab[1],
+                                                      ab[2], n);
+  return p4_done(H, 0, "makeabf");
+}
+
+extern "C" int nekgpu_makebdf_dev(const int64_t* handle, double* bf, const double* v,
+                                  const double* vlag, const double* vtrans, const double* bd,
+                                  const int* nbd, const double* dt) {
+  int rc;
+  Handle* H = p4_mesh_handle(handle, &rc);
+  if (!H) return rc;
+  if (!bf || !v || !vtrans || !bd || !nbd || !dt || *nbd < 1 || *nbd > 3 || (*nbd > 1 && !vlag))
+    return handle_fail(H, NEKGPU_EINVAL, "bad argument (1 <= nbd <= 3, lags for nbd > 1)");
+  const int64_t n = H->mesh.n;
+  Bd c{{0.0, 0.0, 0.0, 0.0}};
+  for (int q = 0; q <= *nbd; ++q) c.c[q] = bd[q];
+  count_launch();
+  p4_makebdf_kernel<<<pblocks(n), 256, 0, H->stream>>>(bf, v, vlag, *nbd - 1, H->mesh.f64.bm1,
+                                                      vtrans, c, 1. / *dt, n);
+  return p4_done(H, 0, "makebdf");
+}
+
+extern "C" int nekgpu_sumab_dev(const int64_t* handle, double* v, const double* vv,
+                                const double* vvlag, const double* ab, const int* nab) {
+  int rc;
+  Handle* H = p4_mesh_handle(handle, &rc);
+  if (!H) return rc;
+  if (!v || !vv || !vvlag || !ab || !nab || *nab < 2 || *nab > 3)
+    return handle_fail(H, NEKGPU_EINVAL, "bad argument (nab 2 or 3)");
+  const int64_t n = H->mesh.n;
+  count_launch();
+  p4_sumab_kernel<<<pblocks(n), 256, 0, H->stream>>>(v, vv, vvlag, ab[0], ab[1],
+                                                    *nab == 3 ? ab[2] : 0.0, *nab, n);
+  return p4_done(H, 0, "sumab");
 }

@@ -218,6 +218,23 @@ class NekGpu:
         self._check(self._L.nekgpu_advab_dev(C.byref(self._h), *[_ptr(a) for a in bf],
                                              *[_ptr(a) for a in v]))
 
+    def makeabf(self, bf, abx1, abx2, vtrans, ab):
+        a = np.ascontiguousarray(ab, dtype=np.float64)
+        self._check(self._L.nekgpu_makeabf_dev(C.byref(self._h), _ptr(bf), _ptr(abx1), _ptr(abx2),
+                                               _ptr(vtrans), C.c_void_p(a.ctypes.data)))
+
+    def makebdf(self, bf, v, vlag, vtrans, bd, nbd: int, dt: float):
+        """vlag: one device array holding the nbd - 1 lagged fields back to back"""
+        b = np.ascontiguousarray(bd, dtype=np.float64)
+        self._check(self._L.nekgpu_makebdf_dev(C.byref(self._h), _ptr(bf), _ptr(v), _ptr(vlag),
+                                               _ptr(vtrans), C.c_void_p(b.ctypes.data),
+                                               C.byref(_cint(nbd)), C.byref(_cdouble(dt))))
+
+    def sumab(self, v, vv, vvlag, ab, nab: int):
+        a = np.ascontiguousarray(ab, dtype=np.float64)
+        self._check(self._L.nekgpu_sumab_dev(C.byref(self._h), _ptr(v), _ptr(vv), _ptr(vvlag),
+                                             C.c_void_p(a.ctypes.data), C.byref(_cint(nab))))
+
     def cresvsp(self, r, v, h1, h2, vdiff, qtl, pr, bf):
         """velocity residual of the splitting step (r, v, bf: 3 device arrays each)"""
         self._check(self._L.nekgpu_cresvsp_dev(C.byref(self._h), *[_ptr(a) for a in r],

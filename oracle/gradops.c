@@ -258,3 +258,41 @@ void ref_advab(int nx1, int nel, double *bfx, double *bfy, double *bfz, const do
   }
   free(ta);
 }
+
+/* ---- time-integration bookkeeping of the step (core/navier1.f, plan4.f) ---- */
+
+/* makeabf (core/navier1.f:1597-1640, iflomach false), one component:
+ * ta = ab1 abx1 + ab2 abx2; abx2 = abx1; abx1 = bf; bf = (ab0 bf + ta) vtrans */
+void ref_makeabf(int64_t n, double *bf, double *abx1, double *abx2, const double *vtrans,
+                 const double *ab) {
+  for (int64_t i = 0; i < n; ++i) {
+    const double ta = ab[1] * abx1[i] + ab[2] * abx2[i]; /* add3s2 */
+    abx2[i] = abx1[i];
+    abx1[i] = bf[i];
+    bf[i] = ab[0] * bf[i] + ta; /* add2s1 */
+    bf[i] = bf[i] * vtrans[i];  /* col2 */
+  }
+}
+
+/* makebdf (core/navier1.f:1548-1595, fixed geometry, iflomach false), one
+ * component: tb = v bm1 bd[1] + sum over lags l = 1..nbd-1 of vlag_l bm1
+ * bd[l+1]; bf += tb (vtrans / dt).  vlag: nbd - 1 arrays of n. */
+void ref_makebdf(int64_t n, double *bf, const double *v, const double *vlag, const double *bm1,
+                 const double *vtrans, const double *bd, int nbd, double dt) {
+  const double cnst = 1. / dt;
+  for (int64_t i = 0; i < n; ++i) {
+    const double h2 = vtrans[i] * cnst; /* cmult2 */
+    double tb = v[i] * bm1[i] * bd[1]; /* opcolv3c */
+    for (int l = 2; l <= nbd; ++l) tb = tb + vlag[(int64_t)(l - 2) * n + i] * bm1[i] * bd[l];
+    bf[i] = bf[i] + tb * h2; /* opadd2col */
+  }
+}
+
+/* sumab (core/plan4.f:525-540): v = ab0 vv + ab1 vvlag_1 (+ ab2 vvlag_2) */
+void ref_sumab(int64_t n, double *v, const double *vv, const double *vvlag, const double *ab,
+               int nab) {
+  for (int64_t i = 0; i < n; ++i) {
+    v[i] = ab[0] * vv[i] + ab[1] * vvlag[i]; /* add3s2 */
+    if (nab == 3) v[i] = v[i] + ab[2] * vvlag[n + i]; /* add2s2 */
+  }
+}

@@ -202,6 +202,13 @@ void ref_advab(int nx1, int nel, double *bfx, double *bfy, double *bfz, const do
                const double *vy, const double *vz, const double *bm1, const double *rst,
                const double *jac);
 
+void ref_makeabf(int64_t n, double *bf, double *abx1, double *abx2, const double *vtrans,
+                 const double *ab);
+void ref_makebdf(int64_t n, double *bf, const double *v, const double *vlag, const double *bm1,
+                 const double *vtrans, const double *bd, int nbd, double dt);
+void ref_sumab(int64_t n, double *v, const double *vv, const double *vvlag, const double *ab,
+               int nab);
+
 /* sizes of an operator state */
 int ref_ops_nx1(const ref_ops *ops);
 int ref_ops_nel(const ref_ops *ops);

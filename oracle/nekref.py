@@ -80,6 +80,10 @@ def lib():
                                       _dp]
             L.ref_conv1.argtypes = [C.c_int, C.c_int] + [_dp] * 7
             L.ref_advab.argtypes = [C.c_int, C.c_int] + [_dp] * 9
+            L.ref_makeabf.argtypes = [C.c_int64, _dp, _dp, _dp, _dp, _dp]
+            L.ref_makebdf.argtypes = [C.c_int64, _dp, _dp, _dp, _dp, _dp, _dp, C.c_int,
+                                      C.c_double]
+            L.ref_sumab.argtypes = [C.c_int64, _dp, _dp, _dp, _dp, C.c_int]
             L.ref_cresvsp.argtypes = [_vp] + [_dp] * 15
             L.ref_crespsp.argtypes = [_vp] + [_dp] * 13 + [C.c_double, C.c_int, _dp, _dp]
             L.ref_fdm1d.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
@@ -459,6 +463,27 @@ def advab(nx1, nel, bf, v, bm1, rst, jac):
     out = [np.array(a, dtype=np.float64, copy=True) for a in bf]
     lib().ref_advab(int(nx1), int(nel), *out, *[_c(a) for a in v], _c(bm1), _c(rst), _c(jac))
     return out
+
+
+def makeabf(bf, abx1, abx2, vtrans, ab):
+    """returns (bf, abx1, abx2) after makeabf (one component)"""
+    bf, a1, a2 = (np.array(a, dtype=np.float64, copy=True) for a in (bf, abx1, abx2))
+    lib().ref_makeabf(bf.size, bf, a1, a2, _c(vtrans), _c(ab))
+    return bf, a1, a2
+
+
+def makebdf(bf, v, vlag, bm1, vtrans, bd, nbd, dt):
+    bf = np.array(bf, dtype=np.float64, copy=True)
+    lag = _c(np.concatenate([np.asarray(a, dtype=np.float64) for a in vlag])) if vlag else \
+        np.zeros(1)
+    lib().ref_makebdf(bf.size, bf, _c(v), lag, _c(bm1), _c(vtrans), _c(bd), int(nbd), float(dt))
+    return bf
+
+
+def sumab(vv, vvlag, ab, nab):
+    v = np.zeros(len(vv))
+    lib().ref_sumab(v.size, v, _c(vv), _c(np.concatenate(vvlag)), _c(ab), int(nab))
+    return v
 
 
 def cresvsp(ops, v, h1, h2, vdiff, qtl, pr, bf, rst):

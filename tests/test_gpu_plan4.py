@@ -47,3 +47,30 @@ def test_residuals_match_the_oracle(gpu_lib, oracle, exact):
             assert np.allclose(got, want, rtol=0, atol=1e-13 * np.abs(want).max())
         else:
             assert cmp(got, want)
+
+
+def test_time_integration_bookkeeping_bit_for_bit(gpu_lib, oracle):
+    torch = pytest.importorskip("torch")
+    P = oracle.box_problem(5, 2, 2, 2, v=rng_unit_vector(163))
+    n = P["n"]
+    lib = gpu_lib(0)
+    lib.setup(P["nx1"], P["nel"], P["D"], P["g"], P["bm1"], P["glo_num"])
+    rng = np.random.default_rng(164)
+    r = lambda: rng.standard_normal(n)
+    dev = lambda a: torch.tensor(np.ascontiguousarray(a), device="cuda")
+    host = lambda t: t.cpu().numpy()
+    bf, a1, a2, vt = r(), r(), r(), 1.0 + np.abs(r())
+    ab = [1.8, -1.0, 0.2]
+    bfd, a1d, a2d = dev(bf), dev(a1), dev(a2)
+    lib.makeabf(bfd, a1d, a2d, dev(vt), ab)
+    for got, want in zip((bfd, a1d, a2d), oracle.makeabf(bf, a1, a2, vt, np.array(ab))):
+        assert np.array_equal(host(got), want)
+    v, l1, l2 = r(), r(), r()
+    bd = [11 / 6, 3.0, -1.5, 1 / 3]
+    bfd = dev(bf)
+    lib.makebdf(bfd, dev(v), dev(np.concatenate([l1, l2])), dev(vt), bd, 3, 0.01)
+    assert np.array_equal(host(bfd), oracle.makebdf(bf, v, [l1, l2], P["bm1"], vt,
+                                                    np.array(bd), 3, 0.01))
+    out = torch.zeros(n, dtype=torch.float64, device="cuda")
+    lib.sumab(out, dev(v), dev(np.concatenate([l1, l2])), ab, 3)
+    assert np.array_equal(host(out), oracle.sumab(v, [l1, l2], np.array(ab), 3))

@@ -84,3 +84,26 @@ def test_convection_of_a_linear_field(oracle):
     for k in range(3):
         ck = oracle.conv1(nx1, nel, v[k], v, rst, jac)
         assert np.array_equal(out[k], bf[k] - P["bm1"] * ck)
+
+
+def test_time_integration_bookkeeping(oracle):
+    """makeabf, makebdf and sumab restated: equal, bit for bit, to the same
+    formulas evaluated by numpy in the reference's order."""
+    rng = np.random.default_rng(144)
+    n = 1000
+    r = lambda: rng.standard_normal(n)
+    bf, a1, a2, vt, bm1 = r(), r(), r(), 1.0 + np.abs(r()), np.abs(r())
+    ab = np.array([1.8, -1.0, 0.2])
+    b, n1, n2 = oracle.makeabf(bf, a1, a2, vt, ab)
+    ta = ab[1] * a1 + ab[2] * a2
+    assert np.array_equal(b, (ab[0] * bf + ta) * vt)
+    assert np.array_equal(n1, bf) and np.array_equal(n2, a1)
+    v, l1, l2 = r(), r(), r()
+    bd = np.array([11 / 6, 3.0, -1.5, 1 / 3])
+    got = oracle.makebdf(bf, v, [l1, l2], bm1, vt, bd, 3, 0.01)
+    tb = v * bm1 * bd[1]
+    tb = tb + l1 * bm1 * bd[2]
+    tb = tb + l2 * bm1 * bd[3]
+    assert np.array_equal(got, bf + tb * (vt * (1.0 / 0.01)))
+    s = oracle.sumab(v, [l1, l2], ab, 3)
+    assert np.array_equal(s, (ab[0] * v + ab[1] * l1) + ab[2] * l2)
