@@ -163,6 +163,18 @@ int nekgpu_cdtp_dev(const int64_t *handle, double *dtx, const double *x, const i
 int nekgpu_op_curl_dev(const int64_t *handle, double *w1, double *w2, double *w3,
                        const double *u1, const double *u2, const double *u3, const int *ifavg,
                        const double *binv);
+/* The convective term with dealiasing (convop with param(99) = 4,
+ * core/navier1.f:3196 -> convect_new, core/convect.f:639): after
+ * nekgpu_dealias_setup(lxd) (lx1 <= lxd <= 18, typically 3 lx1 / 2) the
+ * field and velocity are interpolated to lxd Gauss points per direction,
+ * the product formed there with the Gauss-weighted metric terms, projected
+ * back and divided by bm1.  nekgpu_convop_dev is convop: dealiased once set
+ * up, conv1 otherwise; nekgpu_advab_dev follows the same choice.  Agrees
+ * with the reference to rounding (not bit for bit).  A moved geometry
+ * (nekgpu_geom_update_dev) rebuilds the fine metric terms. */
+int nekgpu_dealias_setup(const int64_t *handle, const int *lxd);
+int nekgpu_convop_dev(const int64_t *handle, double *conv, const double *u, const double *vx,
+                      const double *vy, const double *vz);
 /* The convective term without dealiasing (conv1, core/navier1.f:3276; what
  * convop uses when dealiasing is off): du = (v . grad) u, and advab
  * (:1516): bf_c -= bm1 (v . grad) v_c for the three components. */

@@ -68,6 +68,8 @@ SIGNATURES = {
     "nekgpu_dudxyz_dev": [_I64P, _P, _P, _IP],
     "nekgpu_cdtp_dev": [_I64P, _P, _P, _IP],
     "nekgpu_op_curl_dev": [_I64P, _P, _P, _P, _P, _P, _P, _IP, _P],
+    "nekgpu_dealias_setup": [_I64P, _IP],
+    "nekgpu_convop_dev": [_I64P] + [_P] * 5,
     "nekgpu_conv1_dev": [_I64P] + [_P] * 5,
     "nekgpu_advab_dev": [_I64P] + [_P] * 6,
     "nekgpu_makeabf_dev": [_I64P, _P, _P, _P, _P, _P],

@@ -217,6 +217,7 @@ void handle_close(Handle& H) {
   if (H.stream) cudaStreamSynchronize(H.stream);
   H.mg.reset();
   H.iface.reset();
+  H.dealias.reset();
   gs_free(H.mesh.gs);
   H.mesh.f64.release();
   H.mesh.f32.release();
@@ -261,6 +262,7 @@ static int mesh_prepare(Handle& H, int lx1, int nel, const double* dxm1, std::st
   H.proj.clear();  // projection spaces belong to the old mesh
   H.mg.reset();    // and so does the pressure preconditioner
   H.iface.reset();  // and the shard's interface maps
+  H.dealias.reset();  // and the dealiasing grid
   H.has_mesh = false;
   if (H.gexec) cudaGraphExecDestroy(H.gexec);
   H.gexec = nullptr;

@@ -171,6 +171,11 @@ int geom_from_xyz(Handle& H, const double* x, const double* y, const double* z, 
   for (int64_t i = 0; i < n; ++i) vol = vol + hb[(size_t)i];
   m.vol = vol;
   m.has_rst = true;
+  if (H.dealias) {  // the fine-grid metric terms follow the moved geometry
+    const int md = dealias_lxd(H);
+    const int rc = dealias_setup(H, md, err);
+    if (rc) return rc;
+  }
   // the FP32 copy of the operator data no longer matches
   m.f32.release();
   m.has_f32 = false;

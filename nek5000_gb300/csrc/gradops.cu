@@ -420,8 +420,10 @@ extern "C" int nekgpu_advab_dev(const int64_t* handle, double* bfx, double* bfy,
   if (H->io0.ensure(H->mesh.n)) return handle_fail(H, NEKGPU_ENOMEM, "device allocation failed");
   double* bf[3] = {bfx, bfy, bfz};
   const double* v[3] = {vx, vy, vz};
-  for (int c = 0; c < 3; ++c) {
-    if (launch_conv1(*H, H->io0.ptr, v[c], vx, vy, vz)) return grad_done(H, -1, "advab");
+  for (int c = 0; c < 3; ++c) {  // convop: dealiased once nekgpu_dealias_setup has run
+    const int rc2 = H->dealias ? convop_dealias(*H, H->io0.ptr, v[c], vx, vy, vz)
+                               : launch_conv1(*H, H->io0.ptr, v[c], vx, vy, vz);
+    if (rc2) return grad_done(H, -1, "advab");
     launch_subcol3(*H, bf[c], H->io0.ptr);
   }
   return grad_done(H, 0, "advab");

@@ -123,6 +123,12 @@ struct ShardIfaceDeleter {
   void operator()(ShardIface* p) const;
 };
 
+// Matrices and fine-grid metric terms of the dealiased convective term (dealias.cu).
+struct Dealias;
+struct DealiasDeleter {
+  void operator()(Dealias* p) const;
+};
+
 // The pressure preconditioner h1mg_solve on the device (h1mg.cu).
 struct MgDev;
 struct MgDevDeleter {
@@ -188,6 +194,8 @@ struct Handle {
   std::unique_ptr<MgDev, MgDevDeleter> mg;
   // interface points shared with other shards (nekgpu_iface_setup)
   std::unique_ptr<ShardIface, ShardIfaceDeleter> iface;
+  // the dealiased convective term once nekgpu_dealias_setup has run
+  std::unique_ptr<Dealias, DealiasDeleter> dealias;
 };
 
 // ---- operator entry points (axhelm_*.cu) ---------------------------------
@@ -253,6 +261,15 @@ int pcg_vec_blocks(int64_t n);
 int launch_gradop(Handle& h, int op, double* o1, double* o2, double* o3, const double* i1,
                   const double* i2, const double* i3, int m, const double* bm1);
 void launch_mul_by(Handle& h, double* a, const double* b);
+int launch_conv1(Handle& h, double* du, const double* u, const double* vx, const double* vy,
+                 const double* vz);
+void launch_subcol3(Handle& h, double* bf, const double* ta);
+// dealias.cu: fine-grid matrices and metric terms for lxd points; the
+// dealiased convective term conv = convect_new(u) / bm1.  0 or an error.
+int dealias_setup(Handle& h, int lxd, std::string& err);
+int dealias_lxd(const Handle& h);
+int convop_dealias(Handle& h, double* conv, const double* u, const double* vx, const double* vy,
+                   const double* vz);
 
 // h1mg.cu: z = M rhs with the set-up preconditioner (rhs masked in place,
 // as h1mg_solve leaves it); 0, -3 or -6 (not set up).  Setup from host

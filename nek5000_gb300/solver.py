@@ -208,6 +208,14 @@ class NekGpu:
                                                _ptr(u1), _ptr(u2), _ptr(u3),
                                                C.byref(_cint(int(bool(ifavg)))), _ptr(binv)))
 
+    def dealias_setup(self, lxd: int):
+        self._check(self._L.nekgpu_dealias_setup(C.byref(self._h), C.byref(_cint(lxd))))
+
+    def convop(self, conv, u, v):
+        """convop: dealiased once dealias_setup has run, conv1 otherwise"""
+        self._check(self._L.nekgpu_convop_dev(C.byref(self._h), _ptr(conv), _ptr(u),
+                                              *[_ptr(a) for a in v]))
+
     def conv1(self, du, u, v):
         """du = (v . grad) u without dealiasing (device arrays; v: 3 components)"""
         self._check(self._L.nekgpu_conv1_dev(C.byref(self._h), _ptr(du), _ptr(u),

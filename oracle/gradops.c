@@ -13,6 +13,7 @@
  * rst: the metric terms rxm1..tzm1 as nine arrays of n (rx ry rz sx sy sz tx
  * ty tz, ref_geom_rst); jac: jacm1.
  */
+#include <math.h>
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
@@ -295,4 +296,122 @@ void ref_sumab(int64_t n, double *v, const double *vv, const double *vvlag, cons
     v[i] = ab[0] * vv[i] + ab[1] * vvlag[i]; /* add3s2 */
     if (nab == 3) v[i] = v[i] + ab[2] * vvlag[n + i]; /* add2s2 */
   }
+}
+
+/* ---- the dealiased convective term (core/convect.f) --------------------------- */
+
+void ref_fd_weights(double xx, const double *x, int n, int m, double *c);
+
+/* Gauss-Legendre points and weights (zwgl): roots of P_m by Newton from the
+ * Chebyshev guesses, weights 2 / ((1 - x^2) P'_m(x)^2). */
+static void gauss_points(int m, double *z, double *w) {
+  for (int i = 0; i < m; ++i) {
+    double x = -cos(3.14159265358979323846 * (i + 0.75) / (m + 0.5)), dp = 1.0;
+    for (int it = 0; it < 100; ++it) {
+      double p0 = 1.0, p1 = x;
+      for (int k = 1; k < m; ++k) {
+        const double p2 = ((2 * k + 1) * x * p1 - k * p0) / (k + 1);
+        p0 = p1;
+        p1 = p2;
+      }
+      dp = m * (x * p1 - p0) / (x * x - 1.0);
+      const double dx = p1 / dp;
+      x -= dx;
+      if (fabs(dx) < 1e-16) break;
+    }
+    z[i] = x;
+    w[i] = 2.0 / ((1.0 - x * x) * dp * dp);
+  }
+}
+
+/* v (nb^3) = [A (x) A (x) A] u (na^3), A nb x na column-major */
+static void tensor3(double *v, int nb, const double *u, int na, const double *A, double *w1,
+                    double *w2) {
+  for (int k = 0; k < na; ++k) /* r */
+    for (int j = 0; j < na; ++j)
+      for (int i = 0; i < nb; ++i) {
+        double s = 0.0;
+        for (int l = 0; l < na; ++l) s += A[i + nb * l] * u[l + na * (j + na * k)];
+        w1[i + nb * (j + na * k)] = s;
+      }
+  for (int k = 0; k < na; ++k) /* s */
+    for (int j = 0; j < nb; ++j)
+      for (int i = 0; i < nb; ++i) {
+        double s = 0.0;
+        for (int l = 0; l < na; ++l) s += A[j + nb * l] * w1[i + nb * (l + na * k)];
+        w2[i + nb * (j + nb * k)] = s;
+      }
+  for (int k = 0; k < nb; ++k) /* t */
+    for (int j = 0; j < nb; ++j)
+      for (int i = 0; i < nb; ++i) {
+        double s = 0.0;
+        for (int l = 0; l < na; ++l) s += A[k + nb * l] * w2[i + nb * (j + nb * l)];
+        v[i + nb * (j + nb * k)] = s;
+      }
+}
+
+/* convop with dealiasing (param(99) = 4, core/navier1.f:3196-3204): conv =
+ * convect_new(u; vx, vy, vz) / bm1 (core/convect.f:639-725, set_dealias_rx
+ * core/convect2.f:120-175) on lxd Gauss points per direction. */
+void ref_convect_new(int nx1, int nel, int lxd, double *conv, const double *u, const double *vx,
+                     const double *vy, const double *vz, const double *rst, const double *bm1) {
+  const int mx = nx1, md = lxd;
+  const int64_t n1 = (int64_t)mx * mx * mx, nd = (int64_t)md * md * md, n = n1 * nel;
+  double zg[32], wg[32], zd[32], wd[32], c[128];
+  ref_zwgll(zg, wg, mx);
+  gauss_points(md, zd, wd);
+  double *J = (double *)malloc(sizeof(double) * md * mx), *Jt = (double *)malloc(sizeof(double) * md * mx);
+  double *Dd = (double *)malloc(sizeof(double) * md * md);
+  for (int i = 0; i < md; ++i) {
+    ref_fd_weights(zd[i], zg, mx - 1, 0, c);
+    for (int j = 0; j < mx; ++j) J[i + md * j] = c[j];
+    ref_fd_weights(zd[i], zd, md - 1, 1, c);
+    for (int j = 0; j < md; ++j) Dd[i + md * j] = c[j + md];
+  }
+  for (int i = 0; i < md; ++i)
+    for (int j = 0; j < mx; ++j) Jt[j + mx * i] = J[i + md * j];
+  double *buf = (double *)malloc(sizeof(double) * nd * 20);
+  double *fx = buf, *fy = fx + nd, *fz = fy + nd, *uf = fz + nd, *ur = uf + nd, *us = ur + nd,
+         *ut = us + nd, *w1 = ut + nd, *w2 = w1 + nd, *rxd = w2 + nd; /* rxd: 9 nd */
+  double *out = rxd + 9 * nd;
+  for (int e = 0; e < nel; ++e) {
+    const int64_t o = n1 * e;
+    for (int q = 0; q < 9; ++q) { /* set_dealias_rx */
+      tensor3(rxd + q * nd, md, rst + (int64_t)q * n + o, mx, J, w1, w2);
+      for (int k = 0; k < md; ++k)
+        for (int j = 0; j < md; ++j)
+          for (int i = 0; i < md; ++i)
+            rxd[q * nd + i + md * (j + md * k)] *= wd[i] * wd[j] * wd[k];
+    }
+    tensor3(fx, md, vx + o, mx, J, w1, w2);
+    tensor3(fy, md, vy + o, mx, J, w1, w2);
+    tensor3(fz, md, vz + o, mx, J, w1, w2);
+    tensor3(uf, md, u + o, mx, J, w1, w2);
+    for (int k = 0; k < md; ++k) /* grad_rst on the Gauss grid */
+      for (int j = 0; j < md; ++j)
+        for (int i = 0; i < md; ++i) {
+          double a = 0.0, b = 0.0, t = 0.0;
+          for (int l = 0; l < md; ++l) {
+            a += Dd[i + md * l] * uf[l + md * (j + md * k)];
+            b += Dd[j + md * l] * uf[i + md * (l + md * k)];
+            t += Dd[k + md * l] * uf[i + md * (j + md * l)];
+          }
+          const int64_t p = i + md * (j + md * k);
+          ur[p] = a;
+          us[p] = b;
+          ut[p] = t;
+        }
+    for (int64_t p = 0; p < nd; ++p) {
+      const double t1 = rxd[p] * fx[p] + rxd[nd + p] * fy[p] + rxd[2 * nd + p] * fz[p];
+      const double t2 = rxd[3 * nd + p] * fx[p] + rxd[4 * nd + p] * fy[p] + rxd[5 * nd + p] * fz[p];
+      const double t3 = rxd[6 * nd + p] * fx[p] + rxd[7 * nd + p] * fy[p] + rxd[8 * nd + p] * fz[p];
+      uf[p] = t1 * ur[p] + t2 * us[p] + t3 * ut[p];
+    }
+    tensor3(out, mx, uf, md, Jt, w1, w2); /* project back: J^T */
+    for (int64_t p = 0; p < n1; ++p) conv[o + p] = out[p] / bm1[o + p];
+  }
+  free(J);
+  free(Jt);
+  free(Dd);
+  free(buf);
 }

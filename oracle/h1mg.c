@@ -76,7 +76,7 @@ struct ref_h1mg {
  * from the n+1 nodes x[0..n] (B. Fornberg, "Calculation of weights in finite
  * difference formulas", SIAM Review 40 (1998) 685-691), the recursion
  * fd_weights_full (core/fast3d.f:1294) evaluates. */
-static void fd_weights(double xx, const double *x, int n, int m, double *c) {
+void ref_fd_weights(double xx, const double *x, int n, int m, double *c) {
   const int ld = n + 1;
   for (int k = 0; k <= m; ++k)
     for (int j = 0; j <= n; ++j) c[j + ld * k] = 0.0;
@@ -453,7 +453,7 @@ ref_h1mg *ref_h1mg_create(const ref_ops *ops, const double *x, const double *y, 
     /* semhat: D from the Fornberg weights, a = D^T diag(w) D */
     double c[64], D[256];
     for (int i = 0; i <= N; ++i) {
-      fd_weights(L->z[i], L->z, N, 1, c);
+      ref_fd_weights(L->z[i], L->z, N, 1, c);
       for (int j = 0; j <= N; ++j) D[i + nx * j] = c[j + nx];
     }
     for (int j = 0; j <= N; ++j)
@@ -466,7 +466,7 @@ ref_h1mg *ref_h1mg_create(const ref_ops *ops, const double *x, const double *y, 
       const mglev *C = &mg->lev[l - 1];
       const int nc = C->nx;
       for (int i = 0; i < nx; ++i) {
-        fd_weights(L->z[i], C->z, nc - 1, 1, c);
+        ref_fd_weights(L->z[i], C->z, nc - 1, 1, c);
         for (int j = 0; j < nc; ++j) L->jh[i + nx * j] = c[j];
       }
       for (int i = 0; i < nx; ++i)
@@ -808,7 +808,7 @@ void ref_fdm1d(int n, int lbc, int rbc, double ll, double lm, double lr, double 
   double z[16], w[16], c[64], D[256], ah[256];
   ref_zwgll(z, w, nx);
   for (int i = 0; i <= n; ++i) {
-    fd_weights(z[i], z, n, 1, c);
+    ref_fd_weights(z[i], z, n, 1, c);
     for (int j = 0; j <= n; ++j) D[i + nx * j] = c[j + nx];
   }
   for (int j = 0; j <= n; ++j)

@@ -209,6 +209,9 @@ void ref_makebdf(int64_t n, double *bf, const double *v, const double *vlag, con
 void ref_sumab(int64_t n, double *v, const double *vv, const double *vvlag, const double *ab,
                int nab);
 
+void ref_convect_new(int nx1, int nel, int lxd, double *conv, const double *u, const double *vx,
+                     const double *vy, const double *vz, const double *rst, const double *bm1);
+
 /* sizes of an operator state */
 int ref_ops_nx1(const ref_ops *ops);
 int ref_ops_nel(const ref_ops *ops);

@@ -84,6 +84,7 @@ def lib():
             L.ref_makebdf.argtypes = [C.c_int64, _dp, _dp, _dp, _dp, _dp, _dp, C.c_int,
                                       C.c_double]
             L.ref_sumab.argtypes = [C.c_int64, _dp, _dp, _dp, _dp, C.c_int]
+            L.ref_convect_new.argtypes = [C.c_int, C.c_int, C.c_int] + [_dp] * 7
             L.ref_cresvsp.argtypes = [_vp] + [_dp] * 15
             L.ref_crespsp.argtypes = [_vp] + [_dp] * 13 + [C.c_double, C.c_int, _dp, _dp]
             L.ref_fdm1d.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
@@ -484,6 +485,14 @@ def sumab(vv, vvlag, ab, nab):
     v = np.zeros(len(vv))
     lib().ref_sumab(v.size, v, _c(vv), _c(np.concatenate(vvlag)), _c(ab), int(nab))
     return v
+
+
+def convect_new(nx1, nel, lxd, u, v, rst, bm1):
+    """convop with dealiasing on lxd Gauss points: convect_new(u) / bm1"""
+    out = np.zeros(nx1 ** 3 * nel)
+    lib().ref_convect_new(int(nx1), int(nel), int(lxd), out, _c(u), *[_c(a) for a in v],
+                          _c(rst), _c(bm1))
+    return out
 
 
 def cresvsp(ops, v, h1, h2, vdiff, qtl, pr, bf, rst):

@@ -78,3 +78,32 @@ def test_convection_matches_the_oracle_bit_for_bit(gpu_lib, oracle):
     lib.advab(bfd, [dev(a) for a in v])
     for a, b in zip(bfd, oracle.advab(nx1, nel, bf, v, P["bm1"], rst, jac)):
         assert np.array_equal(a.cpu().numpy(), b)
+
+
+@pytest.mark.parametrize("nx1,lxd", [(6, 9), (8, 12)])
+def test_dealiased_convection_matches_the_oracle(gpu_lib, oracle, nx1, lxd):
+    """convop with dealiasing on the device against the oracle's
+    convect_new / bm1 (to 1e-12: both sum the tensor steps in their own
+    order); advab follows the dealiased path once it is set up."""
+    torch = pytest.importorskip("torch")
+    P = oracle.box_problem(nx1, 3, 2, 2, v=rng_unit_vector(157))
+    nel, n = P["nel"], P["n"]
+    rst, jac = oracle.geom_rst(nx1, nel, P["x"], P["y"], P["z"])
+    lib = gpu_lib(0)
+    lib.setup_xyz(nx1, nel, P["D"], P["wgll"], P["x"], P["y"], P["z"], P["glo_num"])
+    lib.dealias_setup(lxd)
+    rng = np.random.default_rng(158)
+    v = [rng.standard_normal(n) for _ in range(3)]
+    u = rng.standard_normal(n)
+    dev = lambda a: torch.tensor(np.ascontiguousarray(a), device="cuda")
+    c = torch.zeros(n, dtype=torch.float64, device="cuda")
+    lib.convop(c, dev(u), [dev(a) for a in v])
+    want = oracle.convect_new(nx1, nel, lxd, u, v, rst, P["bm1"])
+    assert np.allclose(c.cpu().numpy(), want, rtol=0, atol=1e-12 * np.abs(want).max())
+    bf = [rng.standard_normal(n) for _ in range(3)]
+    bfd = [dev(a) for a in bf]
+    lib.advab(bfd, [dev(a) for a in v])
+    for k in range(3):
+        ck = oracle.convect_new(nx1, nel, lxd, v[k], v, rst, P["bm1"])
+        want = bf[k] - P["bm1"] * ck
+        assert np.allclose(bfd[k].cpu().numpy(), want, rtol=0, atol=1e-12 * np.abs(want).max())
