@@ -188,12 +188,14 @@ int nekgpu_advab_dev(const int64_t *handle, double *bfx, double *bfy, double *bf
  * the operators above; with NEKGPU_OPT_EXACT set they are the reference's
  * unfused FP64 values bit for bit.
  *   cresvsp  (:264-306) r = -A(h1, h2) v - opgrad(pr - vdiff qtl / 3) + bf
- *   crespsp  (:99-230)  the pressure right-hand side (curl curl of the
+ *   crespsp  (:99-260)  the pressure right-hand side (curl curl of the
  *            extrapolated velocity, opgrad qtl, A(1/vtrans, 0) pr, the
- *            forcing, qtl bm1 bd(1)/dt; the mean removed when *null_space).
- *            The reference adds face terms on inflow ('v', 'V', 'MV', 'mv',
- *            'shl') and 'SYM' faces; these are not formed here, so the mesh
- *            must have none (walls, outflow and periodic faces are fine). */
+ *            forcing, qtl bm1 bd(1)/dt, the face terms; the mean removed when
+ *            *null_space).  fbc (host, 6 per element in the preprocessor
+ *            face order of cbc; may be null for none): 0 no face term, 1
+ *            'V', 'v', 'MV', 'mv' (the current velocity vx, vy, vz through
+ *            the face, times bd(1)/dt), 2 'shl' (the same, unscaled), 3
+ *            'SYM'. */
 int nekgpu_cresvsp_dev(const int64_t *handle, double *r1, double *r2, double *r3,
                        const double *vx, const double *vy, const double *vz, const double *h1,
                        const double *h2, const double *vdiff, const double *qtl,
@@ -203,7 +205,8 @@ int nekgpu_crespsp_dev(const int64_t *handle, double *respr, const double *vxe,
                        const double *vye, const double *vze, const double *pr,
                        const double *qtl, const double *vdiff, const double *vtrans,
                        const double *bfx, const double *bfy, const double *bfz,
-                       const double *binv, const double *dtbd, const int *null_space);
+                       const double *binv, const double *dtbd, const int *null_space,
+                       const double *vx, const double *vy, const double *vz, const int *fbc);
 
 /* The step's time-integration bookkeeping, one velocity component per call
  * (fixed geometry, constant-density flow):

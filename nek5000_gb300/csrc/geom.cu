@@ -118,11 +118,13 @@ int geom_from_xyz(Handle& H, const double* x, const double* y, const double* z, 
   const int64_t n = m.n;
   DevBuf<double> wd;
   const int64_t nxyz = (int64_t)m.nx1 * m.nx1 * m.nx1;
-  if (wd.ensure(m.nx1) || m.rst.ensure((size_t)9 * n) || m.jac.ensure(n) || m.w3.ensure(nxyz)) {
+  if (wd.ensure(m.nx1) || m.rst.ensure((size_t)9 * n) || m.jac.ensure(n) || m.w3.ensure(nxyz) ||
+      m.w1.ensure(m.nx1)) {
     err = "geometry: allocation failed";
     return NEKGPU_ENOMEM;
   }
   cudaMemcpyAsync(wd.ptr, w, m.nx1 * sizeof(double), cudaMemcpyHostToDevice, H.stream);
+  cudaMemcpyAsync(m.w1.ptr, w, m.nx1 * sizeof(double), cudaMemcpyHostToDevice, H.stream);
   {  // w3m1 = w(i) w(j) w(k), in that order (genwz)
     std::vector<double> w3((size_t)nxyz);
     for (int k = 0; k < m.nx1; ++k)

@@ -77,7 +77,7 @@ struct Mesh {
   // metric terms rxm1..tzm1 (nine arrays of n: rx ry rz sx sy sz tx ty tz),
   // jacm1 and w3m1 (nx1^3), kept when the geometry is formed from
   // coordinates (geom.cu); the gradient-type operators need them (gradops.cu)
-  DevBuf<double> rst, jac, w3;
+  DevBuf<double> rst, jac, w3, w1;  // w1: the nx1 GLL weights
   bool has_rst = false;
 };
 
@@ -196,6 +196,7 @@ struct Handle {
   std::unique_ptr<ShardIface, ShardIfaceDeleter> iface;
   // the dealiased convective term once nekgpu_dealias_setup has run
   std::unique_ptr<Dealias, DealiasDeleter> dealias;
+  DevBuf<int> p4_fbc;  // crespsp's face types, staged per call
 };
 
 // ---- operator entry points (axhelm_*.cu) ---------------------------------

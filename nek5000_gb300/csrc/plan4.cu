@@ -11,9 +11,7 @@
 // Pointwise steps are rounded one by one in the reference's order; with the
 // handle's exact option the operator is too, and both residuals are then the
 // reference's unfused FP64 values bit for bit.  Not served: the stress
-// formulation (ifstrs) and crespsp's face terms, which the reference adds
-// only on inflow ('v', 'V', 'MV', 'mv', 'shl') and 'SYM' faces -- the caller
-// states that the mesh has none.
+// formulation (ifstrs).
 #include <string>
 #include <vector>
 
@@ -143,6 +141,67 @@ __global__ void p4_sumab_kernel(double* __restrict__ v, const double* __restrict
   }
 }
 
+// crespsp's face terms (core/plan4.f:219-258), one block per element, the
+// six faces in preprocessor order one after another (edge points of two
+// marked faces take both subtractions in that order).  Face f's outward
+// normal is +-(the r, s or t cofactor triple) / its length and its area
+// that length times the two GLL weights (area3 / unitvec, core/coef.f:
+// 1354-1445).  Types: 1 velocity times dtbd, 2 velocity ('shl'), 3 'SYM'
+// (the fields s1..s3).
+__global__ void p4_face_kernel(double* __restrict__ respr, const double* __restrict__ v1,
+                               const double* __restrict__ v2, const double* __restrict__ v3,
+                               const double* __restrict__ s1, const double* __restrict__ s2,
+                               const double* __restrict__ s3, const int* __restrict__ fbc,
+                               const double* __restrict__ rst, const double* __restrict__ w,
+                               double dtbd, int nx1, int64_t n) {
+  const int64_t e = blockIdx.x, eo = e * (int64_t)nx1 * nx1 * nx1;
+  const int N = nx1 - 1;
+  for (int f = 1; f <= 6; ++f) {
+    const int t = fbc[6 * e + f - 1];  // the same for the whole block
+    if (t >= 1 && t <= 3) {
+      const int d = (f == 2 || f == 4) ? 0 : (f == 1 || f == 3) ? 1 : 2;
+      const double sg = (f == 1 || f == 4 || f == 5) ? -1.0 : 1.0;
+      const double *b1 = t == 3 ? s1 : v1, *b2 = t == 3 ? s2 : v2, *b3 = t == 3 ? s3 : v3;
+      for (int q = threadIdx.x; q < nx1 * nx1; q += blockDim.x) {
+        const int a = q % nx1, b = q / nx1;
+        int i, j, k;
+        if (d == 0) {
+          i = f == 2 ? N : 0;
+          j = a;
+          k = b;
+        } else if (d == 1) {
+          i = a;
+          j = f == 3 ? N : 0;
+          k = b;
+        } else {
+          i = a;
+          j = b;
+          k = f == 6 ? N : 0;
+        }
+        const int64_t p = eo + i + nx1 * (j + nx1 * k);
+        const double c1 = rst[(int64_t)(3 * d) * n + p], c2 = rst[(int64_t)(3 * d + 1) * n + p],
+                     c3 = rst[(int64_t)(3 * d + 2) * n + p];
+        const double len =
+            __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(c1, c1), __dmul_rn(c2, c2)), __dmul_rn(c3, c3)));
+        double nx = sg * c1, ny = sg * c2, nz = sg * c3;
+        if (len != 0.0) {
+          nx = __ddiv_rn(nx, len);
+          ny = __ddiv_rn(ny, len);
+          nz = __ddiv_rn(nz, len);
+        }
+        const double area = __dmul_rn(len, __dmul_rn(w[a], w[b]));
+        double v = __dmul_rn(b1[p], nx);
+        v = __dadd_rn(v, __dmul_rn(b2[p], ny));
+        v = __dadd_rn(v, __dmul_rn(b3[p], nz));
+        v = __dmul_rn(v, area);
+        if (t == 1) v = __dmul_rn(v, dtbd);
+        respr[p] = __dsub_rn(respr[p], v);
+      }
+    }
+    __syncthreads();
+  }
+}
+
 #undef PFOR
 
 int axhelm_any(Handle& h, double* au, const double* u, const Coef<double>& c) {
@@ -232,7 +291,9 @@ extern "C" int nekgpu_crespsp_dev(const int64_t* handle, double* respr, const do
                                   const double* vye, const double* vze, const double* pr,
                                   const double* qtl, const double* vdiff, const double* vtrans,
                                   const double* bfx, const double* bfy, const double* bfz,
-                                  const double* binv, const double* dtbd, const int* null_space) {
+                                  const double* binv, const double* dtbd, const int* null_space,
+                                  const double* vx, const double* vy, const double* vz,
+                                  const int* fbc) {
   int rc;
   Handle* H = p4_handle(handle, &rc);
   if (!H) return rc;
@@ -283,6 +344,23 @@ extern "C" int nekgpu_crespsp_dev(const int64_t* handle, double* respr, const do
   }
   count_launch();
   p4_respr_kernel<<<pblocks(n), 256, 0, s>>>(respr, wa[0], wa[1], wa[2], qtl, bm1, *dtbd, n);
+  if (fbc) {  // face terms on velocity and symmetry faces
+    bool vel = false;
+    for (int q = 0; q < 6 * H->mesh.nel; ++q) {
+      if (fbc[q] < 0 || fbc[q] > 3) return handle_fail(H, NEKGPU_EINVAL, "face types are 0..3");
+      vel = vel || fbc[q] == 1 || fbc[q] == 2;
+    }
+    if (vel && (!vx || !vy || !vz))
+      return handle_fail(H, NEKGPU_EINVAL, "velocity faces need vx, vy, vz");
+    if (H->p4_fbc.ensure((size_t)6 * H->mesh.nel))
+      return handle_fail(H, NEKGPU_ENOMEM, "device allocation failed");
+    cudaMemcpyAsync(H->p4_fbc.ptr, fbc, (size_t)6 * H->mesh.nel * sizeof(int),
+                    cudaMemcpyHostToDevice, s);
+    count_launch();
+    p4_face_kernel<<<H->mesh.nel, 64, 0, s>>>(respr, vx, vy, vz, ta[0], ta[1], ta[2],
+                                              H->p4_fbc.ptr, H->mesh.rst.ptr, H->mesh.w1.ptr,
+                                              *dtbd, H->mesh.nx1, n);
+  }
   if (null_space && *null_space) {  // ortho
     const int nb = pblocks(n);
     count_launch();

@@ -250,14 +250,21 @@ class NekGpu:
                                                _ptr(vdiff), _ptr(qtl), _ptr(pr),
                                                *[_ptr(a) for a in bf]))
 
-    def crespsp(self, respr, ve, pr, qtl, vdiff, vtrans, bf, binv, dtbd, null_space=False):
-        """pressure right-hand side of the splitting step (no inflow/SYM faces)"""
+    def crespsp(self, respr, ve, pr, qtl, vdiff, vtrans, bf, binv, dtbd, null_space=False,
+                v=None, fbc=None):
+        """pressure right-hand side of the splitting step; fbc: host (nel, 6)
+        face types (0 none, 1 velocity times dtbd, 2 'shl', 3 'SYM'), v the
+        current velocity (3 device arrays) for types 1 and 2"""
+        fb = None if fbc is None else np.ascontiguousarray(fbc, dtype=np.int32).reshape(-1)
+        vv = v if v is not None else [None] * 3
         self._check(self._L.nekgpu_crespsp_dev(C.byref(self._h), _ptr(respr),
                                                *[_ptr(a) for a in ve], _ptr(pr), _ptr(qtl),
                                                _ptr(vdiff), _ptr(vtrans),
                                                *[_ptr(a) for a in bf], _ptr(binv),
                                                C.byref(_cdouble(dtbd)),
-                                               C.byref(_cint(int(bool(null_space))))))
+                                               C.byref(_cint(int(bool(null_space)))),
+                                               *[_ptr(a) for a in vv],
+                                               None if fb is None else C.c_void_p(fb.ctypes.data)))
 
     def h1mg_setup(self, x, y, z, glo_num, mask=None, fbc=None, null_space=False):
         """The pressure preconditioner h1mg_solve (nekgpu_h1mg_setup): host

@@ -165,17 +165,59 @@ void ref_cresvsp(const ref_ops *ops, double *r1, double *r2, double *r3, const d
   free(ta);
 }
 
-/* crespsp (core/plan4.f:99-230), PN-PN without the stress formulation and
- * without the face terms (meshes with no 'v', 'V', 'MV', 'mv', 'shl' or
- * 'SYM' face, where the reference adds none): the pressure right-hand side
+/* crespsp (core/plan4.f:99-260), PN-PN without the stress formulation: the
+ * face terms on the faces fbc marks (6 per element, preprocessor order: 0
+ * none, 1 'V'/'v'/'MV'/'mv', 2 'shl', 3 'SYM'; fbc null: none); the pressure right-hand side
  * from the curl-curl of the extrapolated velocity, qtl, the pressure's own
  * operator, the forcing, and dtbd = bd(1)/dt; the mean removed when
  * null_space (ortho). */
+/* The face term of crespsp (core/plan4.f:219-258) on face f (preprocessor
+ * order 1..6) of element e: w = (b1 unx + b2 uny + b3 unz) area (times dtbd
+ * for type 1) subtracted at the face points.  Normals and areas as area3 and
+ * unitvec form them (core/coef.f:1354-1445): the cross product of the face's
+ * tangent derivatives is the r-, s- or t-cofactor triple up to its sign
+ * (outward: - on faces 1, 4, 5, + on 2, 3, 6), its length times the two
+ * GLL weights is the area, the triple over its length the unit normal. */
+static void face_term(int nx1, int64_t n, int64_t e, int f, int type, double *respr,
+                      const double *b1, const double *b2, const double *b3, const double *rst,
+                      const double *w, double dtbd) {
+  const int N = nx1 - 1;
+  const int64_t eo = e * (int64_t)nx1 * nx1 * nx1;
+  const int d = (f == 2 || f == 4) ? 0 : (f == 1 || f == 3) ? 1 : 2; /* r, s, t */
+  const double sg = (f == 1 || f == 4 || f == 5) ? -1.0 : 1.0;
+  for (int b = 0; b < nx1; ++b)
+    for (int a = 0; a < nx1; ++a) {
+      int i, j, k;
+      double wt;
+      if (d == 0) { i = f == 2 ? N : 0; j = a; k = b; wt = w[a] * w[b]; }
+      else if (d == 1) { i = a; j = f == 3 ? N : 0; k = b; wt = w[a] * w[b]; }
+      else { i = a; j = b; k = f == 6 ? N : 0; wt = w[a] * w[b]; }
+      const int64_t p = eo + i + nx1 * (j + nx1 * k);
+      const double c1 = rst[(int64_t)(3 * d) * n + p], c2 = rst[(int64_t)(3 * d + 1) * n + p],
+                   c3 = rst[(int64_t)(3 * d + 2) * n + p];
+      const double len = sqrt(c1 * c1 + c2 * c2 + c3 * c3);
+      double nx = sg * c1, ny = sg * c2, nz = sg * c3;
+      if (len != 0.0) {
+        nx = nx / len;
+        ny = ny / len;
+        nz = nz / len;
+      }
+      const double area = len * wt;
+      double v = b1[p] * nx;      /* faccl3 */
+      v = v + b2[p] * ny;         /* add2 */
+      v = v + b3[p] * nz;
+      v = v * area;               /* faccl2 */
+      if (type == 1) v = v * dtbd; /* cmult */
+      respr[p] = respr[p] - v;    /* sub2 */
+    }
+}
+
 void ref_crespsp(const ref_ops *ops, double *respr, const double *vxe, const double *vye,
                  const double *vze, const double *pr, const double *qtl, const double *vdiff,
                  const double *vtrans, const double *bfx, const double *bfy, const double *bfz,
                  const double *bm1, const double *binv, double dtbd, int null_space,
-                 const double *rst, const double *jac) {
+                 const double *rst, const double *jac, const double *vx, const double *vy,
+                 const double *vz, const int *fbc, const double *w) {
   const int nx1 = ref_ops_nx1(ops), nel = ref_ops_nel(ops);
   const int64_t n = ref_ops_n(ops);
   double *buf = (double *)malloc(sizeof(double) * 9 * n);
@@ -208,6 +250,13 @@ void ref_crespsp(const ref_ops *ops, double *respr, const double *vxe, const dou
   for (int c = 0; c < 3; ++c) ref_cdtp(nx1, nel, wa[c], ta[c], rst, jac, bm1, c + 1);
   for (int64_t i = 0; i < n; ++i) respr[i] = respr[i] + wa[0][i] + wa[1][i] + wa[2][i];
   for (int64_t i = 0; i < n; ++i) respr[i] = respr[i] + qtl[i] * bm1[i] * dtbd; /* admcol3 */
+  if (fbc) /* face terms: velocity (types 1, 2) or symmetry (3) faces */
+    for (int e = 0; e < nel; ++e)
+      for (int f = 1; f <= 6; ++f) {
+        const int t = fbc[6 * e + f - 1];
+        if (t == 1 || t == 2) face_term(nx1, n, e, f, t, respr, vx, vy, vz, rst, w, dtbd);
+        else if (t == 3) face_term(nx1, n, e, f, t, respr, ta[0], ta[1], ta[2], rst, w, dtbd);
+      }
   if (null_space) { /* ortho: the mean over all points removed */
     double s = 0.0;
     for (int64_t i = 0; i < n; ++i) s = s + respr[i];

@@ -194,7 +194,8 @@ void ref_crespsp(const ref_ops *ops, double *respr, const double *vxe, const dou
                  const double *vze, const double *pr, const double *qtl, const double *vdiff,
                  const double *vtrans, const double *bfx, const double *bfy, const double *bfz,
                  const double *bm1, const double *binv, double dtbd, int null_space,
-                 const double *rst, const double *jac);
+                 const double *rst, const double *jac, const double *vx, const double *vy,
+                 const double *vz, const int *fbc, const double *w);
 
 void ref_conv1(int nx1, int nel, double *du, const double *u, const double *vx, const double *vy,
                const double *vz, const double *rst, const double *jac);

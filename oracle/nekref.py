@@ -86,7 +86,8 @@ def lib():
             L.ref_sumab.argtypes = [C.c_int64, _dp, _dp, _dp, _dp, C.c_int]
             L.ref_convect_new.argtypes = [C.c_int, C.c_int, C.c_int] + [_dp] * 7
             L.ref_cresvsp.argtypes = [_vp] + [_dp] * 15
-            L.ref_crespsp.argtypes = [_vp] + [_dp] * 13 + [C.c_double, C.c_int, _dp, _dp]
+            L.ref_crespsp.argtypes = [_vp] + [_dp] * 13 + [C.c_double, C.c_int, _dp, _dp, _dp, _dp,
+                                                           _dp, _vp, _dp]
             L.ref_fdm1d.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
                                     _dp, _dp]
             L.ref_gmres_h1mg.argtypes = [_vp, _vp, _dp, _dp, _dp, _dp, _dp, C.c_double, C.c_int,
@@ -503,12 +504,19 @@ def cresvsp(ops, v, h1, h2, vdiff, qtl, pr, bf, rst):
     return out
 
 
-def crespsp(ops, ve, pr, qtl, vdiff, vtrans, bf, bm1, binv, dtbd, null_space, rst, jac):
-    """pressure right-hand side of the splitting step (no inflow/SYM faces)"""
+def crespsp(ops, ve, pr, qtl, vdiff, vtrans, bf, bm1, binv, dtbd, null_space, rst, jac,
+            v=None, fbc=None):
+    """pressure right-hand side of the splitting step; fbc (nel, 6) face
+    types (0 none, 1 velocity scaled by dtbd, 2 'shl', 3 'SYM') with v the
+    current velocity"""
     out = np.zeros(ops.n)
+    z, w = zwgll(ops.nx1)
+    vv = v if v is not None else [np.zeros(ops.n)] * 3
+    fb = None if fbc is None else np.ascontiguousarray(fbc, dtype=np.int32).reshape(-1)
     lib().ref_crespsp(ops.h, out, *[_c(a) for a in ve], _c(pr), _c(qtl), _c(vdiff), _c(vtrans),
                       *[_c(a) for a in bf], _c(bm1), _c(binv), float(dtbd),
-                      int(bool(null_space)), _c(rst), _c(jac))
+                      int(bool(null_space)), _c(rst), _c(jac), *[_c(a) for a in vv],
+                      None if fb is None else fb.ctypes.data_as(C.c_void_p), _c(w))
     return out
 
 

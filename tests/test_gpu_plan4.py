@@ -36,12 +36,15 @@ def test_residuals_match_the_oracle(gpu_lib, oracle, exact):
     want = oracle.cresvsp(ops, v, h1, h2, vdiff, qtl, pr, bf, rst)
     for a, b in zip(r, want):
         assert cmp(a.cpu().numpy(), b)
-    for null in (False, True):
+    vc = [rnd() for _ in range(3)]  # the current velocity (face terms)
+    fbc = rng.integers(0, 4, size=(nel, 6)).astype(np.int32)  # all four face kinds
+    for null, faces in ((False, None), (True, None), (False, fbc)):
         respr = zeros()
         lib.crespsp(respr, [dev(a) for a in v], dev(pr), dev(qtl), dev(vdiff), dev(vtrans),
-                    [dev(a) for a in bf], dev(P["binv"]), 1.5, null_space=null)
+                    [dev(a) for a in bf], dev(P["binv"]), 1.5, null_space=null,
+                    v=[dev(a) for a in vc], fbc=faces)
         want = oracle.crespsp(ops, v, pr, qtl, vdiff, vtrans, bf, P["bm1"], P["binv"], 1.5,
-                              null, rst, jac)
+                              null, rst, jac, v=vc, fbc=faces)
         got = respr.cpu().numpy()
         if null:
             assert np.allclose(got, want, rtol=0, atol=1e-13 * np.abs(want).max())

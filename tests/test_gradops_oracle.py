@@ -129,3 +129,29 @@ def test_dealiased_convection(oracle):
     c2 = oracle.convect_new(nx1, nel, lxd, u2, v2, rst, P["bm1"])
     c1 = oracle.conv1(nx1, nel, u2, v2, rst, jac)
     assert np.allclose(c2, c1, rtol=0, atol=1e-10)
+
+
+def test_crespsp_face_terms_close_over_the_boundary(oracle):
+    """With every boundary face an 'shl' velocity face, a constant velocity
+    and nothing else, crespsp is minus the flux c . n dA at the face points,
+    which sums to zero over a closed boundary; one face alone gives minus the
+    flux through it (here the plane face x = 0 of an undeformed box)."""
+    P = oracle.box_problem(5, 3, 2, 2, amp=0.0, v=rng_unit_vector(146))
+    nx1, nel, n, ops = P["nx1"], P["nel"], P["n"], P["ops"]
+    rst, jac = oracle.geom_rst(nx1, nel, P["x"], P["y"], P["z"])
+    fb = oracle.face_types(nx1, nel, P["glo_num"], P["mask"])  # r-, r+, s-, s+, t-, t+
+    pre = np.zeros((nel, 6), dtype=np.int32)  # preprocessor order 1..6: s- r+ s+ r- t- t+
+    for f_pre, f_fast in ((0, 2), (1, 1), (2, 3), (3, 0), (4, 4), (5, 5)):
+        pre[:, f_pre] = np.where(fb[:, f_fast] != 0, 2, 0)
+    z0 = np.zeros(n)
+    c = np.array([0.3, -1.1, 0.7])
+    v = [np.full(n, c[0]), np.full(n, c[1]), np.full(n, c[2])]
+    args = (ops, [z0] * 3, z0, z0, np.ones(n), np.ones(n), [z0] * 3, P["bm1"], P["binv"], 1.5,
+            False, rst, jac)
+    r = oracle.crespsp(*args, v=v, fbc=pre)
+    assert abs(r.sum()) < 1e-12 * np.abs(r).sum() and np.abs(r).sum() > 0.1
+    one = np.zeros_like(pre)
+    one[:, 3] = pre[:, 3]  # the x = 0 faces (r-, preprocessor face 4) only
+    r1 = oracle.crespsp(*args, v=v, fbc=one)
+    area = (P["y"].max() - P["y"].min()) * (P["z"].max() - P["z"].min())
+    assert abs(r1.sum() - c[0] * area) < 1e-12
