@@ -81,3 +81,37 @@ def test_documented_entry_points_exist():
                 assert any(s.startswith(name) for s in syms), (f, name)
             else:
                 assert name in syms, (f, name)
+
+
+def _prototypes(path):
+    """name -> parameter list of every int-returning entry point of a header"""
+    import re
+    text = open(path).read()
+    text = re.sub(r"/\*.*?\*/", " ", text, flags=re.S)
+    out = {}
+    for m in re.finditer(r"\bint\s+(nek(?:gpu|mesh)_\w+)\s*\(([^)]*)\)\s*;", text):
+        params = [p.strip() for p in m.group(2).split(",") if p.strip() and p.strip() != "void"]
+        out[m.group(1)] = params
+    return out
+
+
+def test_ctypes_signatures_match_the_headers():
+    """Every ctypes declaration has as many arguments as the header's
+    prototype, pointers where the prototype has pointers and ints/doubles
+    passed by reference where it has pointers to them: a mismatch would
+    hand the library wrong addresses."""
+    import ctypes as C
+    from nek5000_gb300 import _capi
+    protos = {}
+    for h in ("nekgpu.h", "nekmesh.h"):
+        protos.update(_prototypes(os.path.join(ROOT, "include", h)))
+    missing = [n for n in _capi.SIGNATURES if n not in protos]
+    assert not missing, missing
+    for name, args in _capi.SIGNATURES.items():
+        params = protos[name]
+        assert len(args) == len(params), (name, len(args), len(params))
+        for a, p in zip(args, params):
+            is_ptr = "*" in p
+            ctype_is_ptr = a is C.c_void_p or a is C.c_char_p or (
+                isinstance(a, type) and issubclass(a, C._Pointer))
+            assert is_ptr == ctype_is_ptr, (name, p, a)
