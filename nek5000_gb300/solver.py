@@ -279,7 +279,9 @@ class NekGpu:
         if m is None and fb is None:
             raise TypeError("h1mg_setup needs the mask or the face types")
         rc = self._L.nekgpu_h1mg_setup(C.byref(self._h), _ptr(xs), _ptr(ys), _ptr(zs), _ptr(m),
-                                       _ptr(glo), _ptr(fb), C.byref(_cint(int(bool(null_space)))))
+                                       C.c_void_p(glo.ctypes.data),
+                                       None if fb is None else C.c_void_p(fb.ctypes.data),
+                                       C.byref(_cint(int(bool(null_space)))))
         self._check(rc)
 
     def h1mg_free(self):

@@ -115,3 +115,84 @@ def test_ctypes_signatures_match_the_headers():
             ctype_is_ptr = a is C.c_void_p or a is C.c_char_p or (
                 isinstance(a, type) and issubclass(a, C._Pointer))
             assert is_ptr == ctype_is_ptr, (name, p, a)
+
+
+class _FakeDev:
+    """Stands in for a CUDA tensor in a call that must stop at the handle
+    check: the library rejects an unknown handle before it reads any array."""
+    is_cuda = True
+    dtype = "torch.float64"
+
+    def is_contiguous(self):
+        return True
+
+    def data_ptr(self):
+        return 0
+
+
+def test_python_wrappers_reach_the_library(lib):
+    """Every wrapper of the pressure preconditioner, the shard primitives and
+    the splitting-step operators passes the library the argument list its
+    ctypes declaration expects: called on an unknown handle each one ends
+    in the library's EHANDLE status, not in a ctypes or Python error."""
+    import ctypes as C
+    import numpy as np
+    from nek5000_gb300 import _capi
+    from nek5000_gb300.solver import NekGpu
+    g = NekGpu.__new__(NekGpu)
+    g._L, g._h = lib, C.c_int64(987654321)
+    d, h = _FakeDev(), np.zeros(8)
+    gl = np.arange(8, dtype=np.int64)
+    calls = [
+        lambda: g.hmh_flex_cg(d, d, d, d, d, -1e-10),
+        lambda: g.hmh_flex_cg(h, h, h, h, h, -1e-10),
+        lambda: g.h1mg_setup(h, h, h, gl, mask=h),
+        lambda: g.h1mg_free(),
+        lambda: g.h1mg_apply(d, d),
+        lambda: g.wgradm1(d, d, d, d),
+        lambda: g.dudxyz(d, d, 1),
+        lambda: g.cdtp(d, d, 2),
+        lambda: g.op_curl(d, d, d, d, d, d, ifavg=True, binv=d),
+        lambda: g.conv1(d, d, [d, d, d]),
+        lambda: g.advab([d, d, d], [d, d, d]),
+        lambda: g.dealias_setup(12),
+        lambda: g.convop(d, d, [d, d, d]),
+        lambda: g.cresvsp([d, d, d], [d, d, d], d, d, d, d, d, [d, d, d]),
+        lambda: g.crespsp(d, [d, d, d], d, d, d, d, [d, d, d], d, 1.5, True, v=[d, d, d],
+                          fbc=np.zeros((1, 6), dtype=np.int32)),
+        lambda: g.makeabf(d, d, d, d, [1.0, 0.0, 0.0]),
+        lambda: g.makebdf(d, d, d, d, [1.0, 1.0, 0.0, 0.0], 2, 0.1),
+        lambda: g.sumab(d, d, d, [1.0, 0.0, 0.0], 2),
+    ]
+    for k, call in enumerate(calls):
+        with pytest.raises(_capi.NekGpuError) as ei:
+            call()
+        assert ei.value.code == _capi.EHANDLE, k
+
+
+def test_device_shard_calls_reach_the_library(lib):
+    """The element-shard backend's library calls (shard.DeviceShard) pass
+    their arguments as the declarations expect: on an unknown handle each
+    ends in EHANDLE."""
+    import ctypes as C
+    import numpy as np
+    from nek5000_gb300 import _capi
+    from nek5000_gb300.shard import DeviceShard, Interface
+    from nek5000_gb300.solver import NekGpu
+    g = NekGpu.__new__(NekGpu)
+    g._L, g._h = lib, C.c_int64(987654321)
+    s = DeviceShard.__new__(DeviceShard)
+    s.lib = g
+    d = _FakeDev()
+    calls = [
+        lambda: s.dssum(d), lambda: s.axhelm(d, d, d, d), lambda: s.setprec_local(d, d, d),
+        lambda: s.col2(d, d), lambda: s.col3(d, d, d), lambda: s.add2s1(d, d, 0.5),
+        lambda: s.add2s2(d, d, -0.5), lambda: s.invcol1(d), lambda: s.vlsc3(d, d, d),
+        lambda: s.vlsc32(d, d, d), lambda: s.vlmax(d, 0),
+        lambda: s.iface_setup(Interface(np.array([1, 2, 2, 0]), [np.array([1, 2]),
+                                                                  np.array([2, 3])])),
+    ]
+    for k, call in enumerate(calls):
+        with pytest.raises(_capi.NekGpuError) as ei:
+            call()
+        assert ei.value.code == _capi.EHANDLE, k
