@@ -436,9 +436,12 @@ int h1mg_apply(Handle& h, double* z, double* rhs) {
     rc = C.r.ptr;
   }
   MgDevLevel& L0 = m.lev[0];
-  count_launch(3);
-  mg_cgather_kernel<<<(int)((m.nc + 255) / 256), 256, 0, s>>>(m.cv.ptr, L0.r.ptr, m.cstart.ptr,
-                                                             m.cidx.ptr, m.nc);
+  count_launch(2);
+  if (m.nc > 0) {  // no coarse unknown (every vertex Dirichlet): the coarse correction is 0
+    count_launch();
+    mg_cgather_kernel<<<(int)((m.nc + 255) / 256), 256, 0, s>>>(m.cv.ptr, L0.r.ptr, m.cstart.ptr,
+                                                               m.cidx.ptr, m.nc);
+  }
   if (m.ns > 0) {  // cy = X (X^T cv) on the first ns unknowns
     const int gw = (int)((m.ns * 32 + 255) / 256);
     count_launch(4);
