@@ -175,6 +175,11 @@ int nekgpu_op_curl_dev(const int64_t *handle, double *w1, double *w2, double *w3
 int nekgpu_dealias_setup(const int64_t *handle, const int *lxd);
 int nekgpu_convop_dev(const int64_t *handle, double *conv, const double *u, const double *vx,
                       const double *vy, const double *vz);
+/* The conservative form on the same Gauss grid (convop with param(99) = 5,
+ * convect_cons, core/convect.f:729): conv = div(v u) in weak form / bm1;
+ * needs nekgpu_dealias_setup. */
+int nekgpu_convect_cons_dev(const int64_t *handle, double *conv, const double *u,
+                            const double *vx, const double *vy, const double *vz);
 /* The convective term without dealiasing (conv1, core/navier1.f:3276; what
  * convop uses when dealiasing is off): du = (v . grad) u, and advab
  * (:1516): bf_c -= bm1 (v . grad) v_c for the three components. */

@@ -168,6 +168,48 @@ __global__ void __launch_bounds__(256) conv_fine_kernel(double* __restrict__ uo,
   }
 }
 
+// conservative form on the Gauss grid: cu = sum_d (D_r p_d rxd(d) + D_s p_d
+// rxd(d+3) + D_t p_d rxd(d+6)), p_d = f_d uf (convect_cons).  smem:
+// 3 md^3 + md^2 doubles.
+__global__ void __launch_bounds__(256) conv_cons_fine_kernel(double* __restrict__ cu,
+                                                             const double* __restrict__ uf,
+                                                             const double* __restrict__ fx,
+                                                             const double* __restrict__ fy,
+                                                             const double* __restrict__ fz,
+                                                             const double* __restrict__ rxd,
+                                                             const double* __restrict__ Dd,
+                                                             int md, int64_t nd) {
+  extern __shared__ __align__(128) unsigned char dl_smem[];
+  const int md3 = md * md * md;
+  double* sp = reinterpret_cast<double*>(dl_smem);  // [d][md^3]
+  double* sD = sp + 3 * md3;
+  const int64_t e = blockIdx.x, eo = e * md3;
+  for (int q = threadIdx.x; q < md3; q += blockDim.x) {
+    const double u = uf[eo + q];
+    sp[q] = fx[eo + q] * u;
+    sp[md3 + q] = fy[eo + q] * u;
+    sp[2 * md3 + q] = fz[eo + q] * u;
+  }
+  for (int q = threadIdx.x; q < md * md; q += blockDim.x) sD[q] = Dd[q];
+  __syncthreads();
+  for (int q = threadIdx.x; q < md3; q += blockDim.x) {
+    const int i = q % md, j = (q / md) % md, k = q / (md * md);
+    const int64_t g = eo + q;
+    double acc = 0.0;
+    for (int d = 0; d < 3; ++d) {
+      const double* p = sp + d * md3;
+      double a = 0.0, b = 0.0, t = 0.0;
+      for (int l = 0; l < md; ++l) {
+        a += sD[i + md * l] * p[l + md * (j + md * k)];
+        b += sD[j + md * l] * p[i + md * (l + md * k)];
+        t += sD[k + md * l] * p[i + md * (j + md * l)];
+      }
+      acc = acc + a * rxd[d * nd + g] + b * rxd[(d + 3) * nd + g] + t * rxd[(d + 6) * nd + g];
+    }
+    cu[g] = acc;
+  }
+}
+
 __global__ void div_by_kernel(double* __restrict__ a, const double* __restrict__ b, int64_t n) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
@@ -225,6 +267,8 @@ int dealias_setup(Handle& h, int lxd, std::string& err) {
                        (int)t3_smem(18, 18));
   cudaFuncSetAttribute(conv_fine_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)(sizeof(double) * (18 * 18 * 18 + 18 * 18)));
+  cudaFuncSetAttribute(conv_cons_fine_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)(sizeof(double) * (3 * 18 * 18 * 18 + 18 * 18)));
   for (int q = 0; q < 9; ++q) {  // set_dealias_rx
     count_launch(2);
     tensor3_kernel<<<M.nel, 256, sm, s>>>(d->rxd.ptr + q * nd, M.rst.ptr + (int64_t)q * M.n,
@@ -241,6 +285,26 @@ int dealias_setup(Handle& h, int lxd, std::string& err) {
 }
 
 int dealias_lxd(const Handle& h) { return h.dealias ? h.dealias->md : 0; }
+
+int convect_cons_dealias(Handle& h, double* conv, const double* u, const double* vx,
+                         const double* vy, const double* vz) {
+  Mesh& M = h.mesh;
+  Dealias& d = *h.dealias;
+  const int mx = M.nx1, md = d.md;
+  const int64_t nd = (int64_t)md * md * md * M.nel;
+  cudaStream_t s = h.stream;
+  const size_t sf = t3_smem(mx, md), sb = t3_smem(md, mx);
+  count_launch(7);
+  tensor3_kernel<<<M.nel, 256, sf, s>>>(d.uf.ptr, u, d.J.ptr, mx, md);
+  tensor3_kernel<<<M.nel, 256, sf, s>>>(d.fx.ptr, vx, d.J.ptr, mx, md);
+  tensor3_kernel<<<M.nel, 256, sf, s>>>(d.fy.ptr, vy, d.J.ptr, mx, md);
+  tensor3_kernel<<<M.nel, 256, sf, s>>>(d.fz.ptr, vz, d.J.ptr, mx, md);
+  conv_cons_fine_kernel<<<M.nel, 256, sizeof(double) * (3 * (size_t)md * md * md + md * md), s>>>(
+      d.uo.ptr, d.uf.ptr, d.fx.ptr, d.fy.ptr, d.fz.ptr, d.rxd.ptr, d.Dd.ptr, md, nd);
+  tensor3_kernel<<<M.nel, 256, sb, s>>>(conv, d.uo.ptr, d.Jt.ptr, md, mx);
+  div_by_kernel<<<vgrid(M.n), 256, 0, s>>>(conv, M.f64.bm1, M.n);
+  return cudaGetLastError() == cudaSuccess ? 0 : -3;
+}
 
 int convop_dealias(Handle& h, double* conv, const double* u, const double* vx, const double* vy,
                    const double* vz) {
@@ -302,5 +366,21 @@ extern "C" int nekgpu_convop_dev(const int64_t* handle, double* conv, const doub
   const cudaError_t e = cudaGetLastError();
   if (rc || e != cudaSuccess)
     return handle_fail(H, NEKGPU_ECUDA, std::string("convop: ") + cudaGetErrorString(e));
+  return NEKGPU_OK;
+}
+
+extern "C" int nekgpu_convect_cons_dev(const int64_t* handle, double* conv, const double* u,
+                                       const double* vx, const double* vy, const double* vz) {
+  Handle* H = handle_lookup(handle);
+  if (!H) return handle_fail(nullptr, NEKGPU_EHANDLE, "unknown handle");
+  if (cudaSetDevice(H->device) != cudaSuccess)
+    return handle_fail(H, NEKGPU_ECUDA, "cudaSetDevice failed");
+  if (!H->has_mesh || !H->dealias)
+    return handle_fail(H, NEKGPU_ENOSETUP, "dealiasing not set up (nekgpu_dealias_setup)");
+  if (!conv || !u || !vx || !vy || !vz) return handle_fail(H, NEKGPU_EINVAL, "null argument");
+  const int rc = convect_cons_dealias(*H, conv, u, vx, vy, vz);
+  const cudaError_t e = cudaGetLastError();
+  if (rc || e != cudaSuccess)
+    return handle_fail(H, NEKGPU_ECUDA, std::string("convect_cons: ") + cudaGetErrorString(e));
   return NEKGPU_OK;
 }

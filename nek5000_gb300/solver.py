@@ -216,6 +216,11 @@ class NekGpu:
         self._check(self._L.nekgpu_convop_dev(C.byref(self._h), _ptr(conv), _ptr(u),
                                               *[_ptr(a) for a in v]))
 
+    def convect_cons(self, conv, u, v):
+        """the conservative dealiased form div(v u) / bm1 (needs dealias_setup)"""
+        self._check(self._L.nekgpu_convect_cons_dev(C.byref(self._h), _ptr(conv), _ptr(u),
+                                                    *[_ptr(a) for a in v]))
+
     def conv1(self, du, u, v):
         """du = (v . grad) u without dealiasing (device arrays; v: 3 components)"""
         self._check(self._L.nekgpu_conv1_dev(C.byref(self._h), _ptr(du), _ptr(u),

@@ -464,3 +464,66 @@ void ref_convect_new(int nx1, int nel, int lxd, double *conv, const double *u, c
   free(Dd);
   free(buf);
 }
+
+/* convop with the conservative form on the Gauss grid (param(99) = 5,
+ * core/navier1.f:3205-3207 -> convect_cons, core/convect.f:729-800):
+ * conv = J^T [sum_i (D_r (c_i u) rx_i + D_s (c_i u) sx_i + D_t (c_i u) tx_i)]
+ * / bm1 with the Gauss-weighted fine metric terms. */
+void ref_convect_cons(int nx1, int nel, int lxd, double *conv, const double *u,
+                      const double *vx, const double *vy, const double *vz, const double *rst,
+                      const double *bm1) {
+  const int mx = nx1, md = lxd;
+  const int64_t n1 = (int64_t)mx * mx * mx, nd = (int64_t)md * md * md, n = n1 * nel;
+  double zg[32], wg[32], zd[32], wd[32], c[128];
+  ref_zwgll(zg, wg, mx);
+  gauss_points(md, zd, wd);
+  double *J = (double *)malloc(sizeof(double) * md * mx), *Jt = (double *)malloc(sizeof(double) * md * mx);
+  double *Dd = (double *)malloc(sizeof(double) * md * md);
+  for (int i = 0; i < md; ++i) {
+    ref_fd_weights(zd[i], zg, mx - 1, 0, c);
+    for (int j = 0; j < mx; ++j) J[i + md * j] = c[j];
+    ref_fd_weights(zd[i], zd, md - 1, 1, c);
+    for (int j = 0; j < md; ++j) Dd[i + md * j] = c[j + md];
+  }
+  for (int i = 0; i < md; ++i)
+    for (int j = 0; j < mx; ++j) Jt[j + mx * i] = J[i + md * j];
+  double *buf = (double *)malloc(sizeof(double) * nd * 16);
+  double *uf = buf, *cf = uf + nd, *cu = cf + nd, *w1 = cu + nd, *w2 = w1 + nd, *rxd = w2 + nd;
+  double *out = rxd + 9 * nd;
+  const double *cv[3] = {vx, vy, vz};
+  for (int e = 0; e < nel; ++e) {
+    const int64_t o = n1 * e;
+    for (int q = 0; q < 9; ++q) {
+      tensor3(rxd + q * nd, md, rst + (int64_t)q * n + o, mx, J, w1, w2);
+      for (int k = 0; k < md; ++k)
+        for (int j = 0; j < md; ++j)
+          for (int i = 0; i < md; ++i)
+            rxd[q * nd + i + md * (j + md * k)] *= wd[i] * wd[j] * wd[k];
+    }
+    tensor3(uf, md, u + o, mx, J, w1, w2);
+    for (int64_t p = 0; p < nd; ++p) cu[p] = 0.0;
+    for (int d = 0; d < 3; ++d) {
+      tensor3(cf, md, cv[d] + o, mx, J, w1, w2);
+      for (int64_t p = 0; p < nd; ++p) cf[p] = cf[p] * uf[p];
+      for (int k = 0; k < md; ++k)
+        for (int j = 0; j < md; ++j)
+          for (int i = 0; i < md; ++i) {
+            double a = 0.0, b = 0.0, t = 0.0;
+            for (int l = 0; l < md; ++l) {
+              a += Dd[i + md * l] * cf[l + md * (j + md * k)];
+              b += Dd[j + md * l] * cf[i + md * (l + md * k)];
+              t += Dd[k + md * l] * cf[i + md * (j + md * l)];
+            }
+            const int64_t p = i + md * (j + md * k);
+            cu[p] = cu[p] + a * rxd[d * nd + p] + b * rxd[(d + 3) * nd + p] +
+                    t * rxd[(d + 6) * nd + p];
+          }
+    }
+    tensor3(out, mx, cu, md, Jt, w1, w2);
+    for (int64_t p = 0; p < n1; ++p) conv[o + p] = out[p] / bm1[o + p];
+  }
+  free(J);
+  free(Jt);
+  free(Dd);
+  free(buf);
+}

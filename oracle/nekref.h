@@ -213,6 +213,10 @@ void ref_sumab(int64_t n, double *v, const double *vv, const double *vvlag, cons
 void ref_convect_new(int nx1, int nel, int lxd, double *conv, const double *u, const double *vx,
                      const double *vy, const double *vz, const double *rst, const double *bm1);
 
+void ref_convect_cons(int nx1, int nel, int lxd, double *conv, const double *u,
+                      const double *vx, const double *vy, const double *vz, const double *rst,
+                      const double *bm1);
+
 /* sizes of an operator state */
 int ref_ops_nx1(const ref_ops *ops);
 int ref_ops_nel(const ref_ops *ops);

@@ -85,6 +85,7 @@ def lib():
                                       C.c_double]
             L.ref_sumab.argtypes = [C.c_int64, _dp, _dp, _dp, _dp, C.c_int]
             L.ref_convect_new.argtypes = [C.c_int, C.c_int, C.c_int] + [_dp] * 7
+            L.ref_convect_cons.argtypes = [C.c_int, C.c_int, C.c_int] + [_dp] * 7
             L.ref_cresvsp.argtypes = [_vp] + [_dp] * 15
             L.ref_crespsp.argtypes = [_vp] + [_dp] * 13 + [C.c_double, C.c_int, _dp, _dp, _dp, _dp,
                                                            _dp, _vp, _dp]
@@ -493,6 +494,14 @@ def convect_new(nx1, nel, lxd, u, v, rst, bm1):
     out = np.zeros(nx1 ** 3 * nel)
     lib().ref_convect_new(int(nx1), int(nel), int(lxd), out, _c(u), *[_c(a) for a in v],
                           _c(rst), _c(bm1))
+    return out
+
+
+def convect_cons(nx1, nel, lxd, u, v, rst, bm1):
+    """convop with the conservative form on lxd Gauss points: div(v u) / bm1"""
+    out = np.zeros(nx1 ** 3 * nel)
+    lib().ref_convect_cons(int(nx1), int(nel), int(lxd), out, _c(u), *[_c(a) for a in v],
+                           _c(rst), _c(bm1))
     return out
 
 

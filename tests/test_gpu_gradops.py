@@ -107,3 +107,22 @@ def test_dealiased_convection_matches_the_oracle(gpu_lib, oracle, nx1, lxd):
         ck = oracle.convect_new(nx1, nel, lxd, v[k], v, rst, P["bm1"])
         want = bf[k] - P["bm1"] * ck
         assert np.allclose(bfd[k].cpu().numpy(), want, rtol=0, atol=1e-12 * np.abs(want).max())
+
+
+def test_conservative_convection_matches_the_oracle(gpu_lib, oracle):
+    torch = pytest.importorskip("torch")
+    nx1, lxd = 6, 9
+    P = oracle.box_problem(nx1, 3, 2, 2, v=rng_unit_vector(159))
+    nel, n = P["nel"], P["n"]
+    rst, jac = oracle.geom_rst(nx1, nel, P["x"], P["y"], P["z"])
+    lib = gpu_lib(0)
+    lib.setup_xyz(nx1, nel, P["D"], P["wgll"], P["x"], P["y"], P["z"], P["glo_num"])
+    lib.dealias_setup(lxd)
+    rng = np.random.default_rng(160)
+    v = [rng.standard_normal(n) for _ in range(3)]
+    u = rng.standard_normal(n)
+    dev = lambda a: torch.tensor(np.ascontiguousarray(a), device="cuda")
+    c = torch.zeros(n, dtype=torch.float64, device="cuda")
+    lib.convect_cons(c, dev(u), [dev(a) for a in v])
+    want = oracle.convect_cons(nx1, nel, lxd, u, v, rst, P["bm1"])
+    assert np.allclose(c.cpu().numpy(), want, rtol=0, atol=1e-12 * np.abs(want).max())

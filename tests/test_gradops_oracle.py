@@ -155,3 +155,19 @@ def test_crespsp_face_terms_close_over_the_boundary(oracle):
     r1 = oracle.crespsp(*args, v=v, fbc=one)
     area = (P["y"].max() - P["y"].min()) * (P["z"].max() - P["z"].min())
     assert abs(r1.sum() - c[0] * area) < 1e-12
+
+
+def test_conservative_convection(oracle):
+    """The conservative form div(v u) equals the advective one v . grad u
+    for a divergence-free velocity (a rigid rotation) when both are exact
+    (u linear, affine mesh)."""
+    P = oracle.box_problem(6, 3, 2, 2, amp=0.0, v=rng_unit_vector(147))
+    nx1, nel, n = P["nx1"], P["nel"], P["n"]
+    rst, jac = oracle.geom_rst(nx1, nel, P["x"], P["y"], P["z"])
+    lxd = (3 * nx1) // 2
+    u = 0.4 * P["x"] - 0.9 * P["y"] + 0.2 * P["z"]
+    v = [-P["y"], P["x"], np.zeros(n)]
+    cc = oracle.convect_cons(nx1, nel, lxd, u, v, rst, P["bm1"])
+    ca = oracle.convect_new(nx1, nel, lxd, u, v, rst, P["bm1"])
+    assert np.allclose(cc, ca, rtol=0, atol=1e-11)
+    assert np.allclose(ca, -P["y"] * 0.4 + P["x"] * (-0.9), rtol=0, atol=1e-11)
