@@ -61,9 +61,9 @@ def test_init_without_gpu_fails_cleanly(lib):
 
 
 def test_integration_bindings_name_declared_entry_points():
-    """Every bind(C) name of the Fortran interface module in INTEGRATION.md is
-    an entry point the headers declare (the binding a maintainer copies must
-    link)."""
+    """Every bind(C) name of the Fortran interface module in the integration
+    notes is an entry point the headers declare (the binding a maintainer
+    copies must link)."""
     doc = open(os.path.join(ROOT, "INTEGRATION.md")).read()
     names = set(re.findall(r'bind\(C,\s*name="(\w+)"\)', doc))
     assert names, "no bind(C) names found"
@@ -71,8 +71,8 @@ def test_integration_bindings_name_declared_entry_points():
 
 
 def test_documented_entry_points_exist():
-    """Every nekgpu_* / nekmesh_* name the design doc and INTEGRATION.md mention
-    is declared (names ending in '_' stand for a family)."""
+    """Every nekgpu_* / nekmesh_* name the design and integration notes
+    mention is declared (names ending in '_' stand for a family)."""
     syms = set(declared_symbols())
     for f in ("DESIGN.md", "INTEGRATION.md"):
         text = open(os.path.join(ROOT, f)).read()
