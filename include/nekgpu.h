@@ -175,6 +175,16 @@ int nekgpu_op_curl_dev(const int64_t *handle, double *w1, double *w2, double *w3
 int nekgpu_dealias_setup(const int64_t *handle, const int *lxd);
 int nekgpu_convop_dev(const int64_t *handle, double *conv, const double *u, const double *vx,
                       const double *vy, const double *vz);
+/* conv2 (core/navier1.f:1288): dtfi = D^T (w3 (rst v) fi) / bm1, the
+ * transposed (weak) convective operator; and the skew-symmetric form
+ * (convopo with param(86) != 0, :1221): conv1 and conv2 of fi masked by
+ * cmask (:1390), whose ofc flags (host, 6 per element, preprocessor face
+ * order; null for none) mark the outflow ('O', 'o') faces.  Bit-identical to
+ * the reference's unfused FP64 arithmetic. */
+int nekgpu_conv2_dev(const int64_t *handle, double *dtfi, const double *fi, const double *vx,
+                     const double *vy, const double *vz);
+int nekgpu_convopo_dev(const int64_t *handle, double *conv, const double *fi, const double *vx,
+                       const double *vy, const double *vz, const int *ofc);
 /* The conservative form on the same Gauss grid (convop with param(99) = 5,
  * convect_cons, core/convect.f:729): conv = div(v u) in weak form / bm1;
  * needs nekgpu_dealias_setup. */

@@ -71,6 +71,8 @@ SIGNATURES = {
     "nekgpu_dealias_setup": [_I64P, _IP],
     "nekgpu_convop_dev": [_I64P] + [_P] * 5,
     "nekgpu_convect_cons_dev": [_I64P] + [_P] * 5,
+    "nekgpu_conv2_dev": [_I64P] + [_P] * 5,
+    "nekgpu_convopo_dev": [_I64P] + [_P] * 6,
     "nekgpu_conv1_dev": [_I64P] + [_P] * 5,
     "nekgpu_advab_dev": [_I64P] + [_P] * 6,
     "nekgpu_makeabf_dev": [_I64P, _P, _P, _P, _P, _P],

@@ -210,6 +210,84 @@ __global__ void __launch_bounds__(NX* NX) conv1_kernel(double* __restrict__ du,
   }
 }
 
+// dtfi = (D_r^T t_r + D_s^T t_s + D_t^T t_t) / bm1, t_q = w3 (((m_qx vx) fi +
+// (m_qy vy) fi) + (m_qz vz) fi)   (conv2, core/navier1.f:1288-1388)
+template <int NX>
+__global__ void __launch_bounds__(NX* NX) conv2_kernel(double* __restrict__ dtfi,
+                                                       const double* __restrict__ fi,
+                                                       const double* __restrict__ vx,
+                                                       const double* __restrict__ vy,
+                                                       const double* __restrict__ vz,
+                                                       const double* __restrict__ rst,
+                                                       const double* __restrict__ w3,
+                                                       const double* __restrict__ bm1,
+                                                       const double* __restrict__ D, int64_t n) {
+  constexpr int P = NX * NX * NX;
+  __shared__ double ta[P], tb[P], tc[P], sD[NX * NX];
+  const int64_t eo = (int64_t)blockIdx.x * P;
+  const int tid = threadIdx.x;
+  double* t3[3] = {ta, tb, tc};
+  for (int q = tid; q < P; q += NX * NX) {
+    const int64_t g = eo + q;
+    const double f = fi[g], a1 = vx[g], a2 = vy[g], a3 = vz[g];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      double a = __dmul_rn(__dmul_rn(rst[(int64_t)(3 * d) * n + g], a1), f);
+      a = __dadd_rn(a, __dmul_rn(__dmul_rn(rst[(int64_t)(3 * d + 1) * n + g], a2), f));
+      a = __dadd_rn(a, __dmul_rn(__dmul_rn(rst[(int64_t)(3 * d + 2) * n + g], a3), f));
+      t3[d][q] = __dmul_rn(a, w3[q]);
+    }
+  }
+  for (int q = tid; q < NX * NX; q += NX * NX) sD[q] = D[q];
+  __syncthreads();
+  const int i = tid % NX, j = tid / NX;
+  for (int k = 0; k < NX; ++k) {
+    double r = __dmul_rn(sD[i], ta[NX * (j + NX * k)]);
+    double s = __dmul_rn(tb[i + NX * NX * k], sD[j]);
+    double t = __dmul_rn(tc[i + NX * j], sD[k]);
+#pragma unroll
+    for (int l = 1; l < NX; ++l) {
+      r = __dadd_rn(r, __dmul_rn(sD[l * NX + i], ta[l + NX * (j + NX * k)]));
+      s = __dadd_rn(s, __dmul_rn(tb[i + NX * (l + NX * k)], sD[l * NX + j]));
+      t = __dadd_rn(t, __dmul_rn(tc[i + NX * (j + NX * l)], sD[l * NX + k]));
+    }
+    const int64_t g = eo + i + NX * (j + NX * k);
+    dtfi[g] = __ddiv_rn(__dadd_rn(__dadd_rn(r, s), t), bm1[g]);
+  }
+}
+
+// cmask (core/navier1.f:1390): c1 = 0, c2 = 1 on the points of flagged
+// (outflow) faces, else 1 and 0; element-local
+__global__ void cmask_kernel(double* __restrict__ c1, double* __restrict__ c2,
+                             const int* __restrict__ ofc, int nx1) {
+  const int64_t e = blockIdx.x, nxyz = (int64_t)nx1 * nx1 * nx1;
+  const int N = nx1 - 1;
+  const int* of = ofc + 6 * e;
+  for (int q = threadIdx.x; q < nxyz; q += blockDim.x) {
+    const int i = q % nx1, j = (q / nx1) % nx1, k = q / (nx1 * nx1);
+    const bool on = (of[0] && j == 0) || (of[1] && i == N) || (of[2] && j == N) ||
+                    (of[3] && i == 0) || (of[4] && k == 0) || (of[5] && k == N);
+    c1[e * nxyz + q] = on ? 0.0 : 1.0;
+    c2[e * nxyz + q] = on ? 1.0 : 0.0;
+  }
+}
+
+// a = b c   (col3)
+__global__ void col3_kernel(double* __restrict__ a, const double* __restrict__ b,
+                            const double* __restrict__ c, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    a[i] = __dmul_rn(b[i], c[i]);
+}
+
+// conv = conv + coef (dm cmask)   (col3 then add2s2 / add2)
+__global__ void acc_kernel(double* __restrict__ conv, const double* __restrict__ dm,
+                           const double* __restrict__ cm, double coef, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    conv[i] = __dadd_rn(conv[i], __dmul_rn(coef, __dmul_rn(dm[i], cm[i])));
+}
+
 // bf = bf - bm1 ta   (subcol3)
 __global__ void subcol3_kernel(double* __restrict__ bf, const double* __restrict__ bm1,
                                const double* __restrict__ ta, int64_t n) {
@@ -289,6 +367,35 @@ int launch_conv1(Handle& h, double* du, const double* u, const double* vx, const
     NEKGPU_CONV_CASE(11)
     NEKGPU_CONV_CASE(12)
 #undef NEKGPU_CONV_CASE
+    default:
+      return -1;
+  }
+  return 0;
+}
+
+int launch_conv2(Handle& h, double* dtfi, const double* fi, const double* vx, const double* vy,
+                 const double* vz) {
+  Mesh& M = h.mesh;
+  const int64_t n = M.n;
+  count_launch();
+  switch (M.nx1) {
+#define NEKGPU_CONV2_CASE(N)                                                                     \
+  case N:                                                                                        \
+    conv2_kernel<N><<<M.nel, N * N, 0, h.stream>>>(dtfi, fi, vx, vy, vz, M.rst.ptr, M.w3.ptr,    \
+                                                   M.f64.bm1, M.f64.D, n);                       \
+    break;
+    NEKGPU_CONV2_CASE(2)
+    NEKGPU_CONV2_CASE(3)
+    NEKGPU_CONV2_CASE(4)
+    NEKGPU_CONV2_CASE(5)
+    NEKGPU_CONV2_CASE(6)
+    NEKGPU_CONV2_CASE(7)
+    NEKGPU_CONV2_CASE(8)
+    NEKGPU_CONV2_CASE(9)
+    NEKGPU_CONV2_CASE(10)
+    NEKGPU_CONV2_CASE(11)
+    NEKGPU_CONV2_CASE(12)
+#undef NEKGPU_CONV2_CASE
     default:
       return -1;
   }
@@ -427,4 +534,56 @@ extern "C" int nekgpu_advab_dev(const int64_t* handle, double* bfx, double* bfy,
     launch_subcol3(*H, bf[c], H->io0.ptr);
   }
   return grad_done(H, 0, "advab");
+}
+
+extern "C" int nekgpu_conv2_dev(const int64_t* handle, double* dtfi, const double* fi,
+                                const double* vx, const double* vy, const double* vz) {
+  int rc;
+  Handle* H = grad_handle(handle, &rc);
+  if (!H) return rc;
+  if (!dtfi || !fi || !vx || !vy || !vz) return handle_fail(H, NEKGPU_EINVAL, "null argument");
+  return grad_done(H, launch_conv2(*H, dtfi, fi, vx, vy, vz), "conv2");
+}
+
+extern "C" int nekgpu_convopo_dev(const int64_t* handle, double* conv, const double* fi,
+                                  const double* vx, const double* vy, const double* vz,
+                                  const int* ofc) {
+  int rc;
+  Handle* H = grad_handle(handle, &rc);
+  if (!H) return rc;
+  if (!conv || !fi || !vx || !vy || !vz) return handle_fail(H, NEKGPU_EINVAL, "null argument");
+  const int64_t n = H->mesh.n;
+  const int nel = H->mesh.nel;
+  cudaStream_t s = H->stream;
+  if (H->io0.ensure(n) || H->io1.ensure(n) || H->io2.ensure(n) || H->io3.ensure(n) ||
+      H->p4_fbc.ensure((size_t)6 * nel))
+    return handle_fail(H, NEKGPU_ENOMEM, "device allocation failed");
+  double *c1 = H->io0.ptr, *c2 = H->io1.ptr, *mfi = H->io2.ptr, *dm = H->io3.ptr;
+  if (ofc) {
+    cudaMemcpyAsync(H->p4_fbc.ptr, ofc, (size_t)6 * nel * sizeof(int), cudaMemcpyHostToDevice, s);
+  } else {
+    cudaMemsetAsync(H->p4_fbc.ptr, 0, (size_t)6 * nel * sizeof(int), s);
+  }
+  count_launch(2);
+  cmask_kernel<<<nel, 128, 0, s>>>(c1, c2, H->p4_fbc.ptr, H->mesh.nx1);
+  cudaMemsetAsync(conv, 0, n * sizeof(double), s);
+  const int nb = nblk(n);
+  auto acc = [&](const double* cm, double coef) {
+    count_launch();
+    acc_kernel<<<nb, 256, 0, s>>>(conv, dm, cm, coef, n);
+  };
+  col3_kernel<<<nb, 256, 0, s>>>(mfi, fi, c1, n);
+  if (launch_conv1(*H, dm, mfi, vx, vy, vz)) return grad_done(H, -1, "convopo");
+  acc(c1, 0.5);
+  acc(c2, 1.0);
+  launch_conv2(*H, dm, mfi, vx, vy, vz);
+  acc(c1, -0.5);
+  count_launch();
+  col3_kernel<<<nb, 256, 0, s>>>(mfi, fi, c2, n);
+  launch_conv1(*H, dm, mfi, vx, vy, vz);
+  acc(c2, 0.5);
+  launch_conv2(*H, dm, mfi, vx, vy, vz);
+  acc(c1, -1.0);
+  acc(c2, 0.5);
+  return grad_done(H, 0, "convopo");
 }

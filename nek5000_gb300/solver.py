@@ -216,6 +216,17 @@ class NekGpu:
         self._check(self._L.nekgpu_convop_dev(C.byref(self._h), _ptr(conv), _ptr(u),
                                               *[_ptr(a) for a in v]))
 
+    def conv2(self, dtfi, fi, v):
+        self._check(self._L.nekgpu_conv2_dev(C.byref(self._h), _ptr(dtfi), _ptr(fi),
+                                             *[_ptr(a) for a in v]))
+
+    def convopo(self, conv, fi, v, ofc=None):
+        """skew-symmetric convective form; ofc: host (nel, 6) outflow-face flags"""
+        of = None if ofc is None else np.ascontiguousarray(ofc, dtype=np.int32).reshape(-1)
+        self._check(self._L.nekgpu_convopo_dev(C.byref(self._h), _ptr(conv), _ptr(fi),
+                                               *[_ptr(a) for a in v],
+                                               None if of is None else C.c_void_p(of.ctypes.data)))
+
     def convect_cons(self, conv, u, v):
         """the conservative dealiased form div(v u) / bm1 (needs dealias_setup)"""
         self._check(self._L.nekgpu_convect_cons_dev(C.byref(self._h), _ptr(conv), _ptr(u),

@@ -527,3 +527,97 @@ void ref_convect_cons(int nx1, int nel, int lxd, double *conv, const double *u,
   free(Dd);
   free(buf);
 }
+
+/* conv2 (core/navier1.f:1288-1388, 3-D): dtfi = (D_r^T (w3 (rx vx + ry vy
+ * + rz vz) fi) + D_s^T (...) + D_t^T (...)) / bm1, each col4 product
+ * (m v) fi and the sums in the reference's order */
+void ref_conv2(int nx1, int nel, double *dtfi, const double *fi, const double *vx,
+               const double *vy, const double *vz, const double *rst, const double *bm1) {
+  const int nxyz = nx1 * nx1 * nx1;
+  const int64_t n = (int64_t)nxyz * nel;
+  double d[1024], dt[1024];
+  double *w3 = (double *)malloc(sizeof(double) * nxyz);
+  double *ta = (double *)malloc(sizeof(double) * 4 * nxyz), *tb = ta + nxyz, *tc = tb + nxyz,
+         *wk = tc + nxyz;
+  dmat(nx1, d, dt, w3);
+  for (int e = 0; e < nel; ++e) {
+    const int64_t o = (int64_t)nxyz * e;
+    double *t[3] = {ta, tb, tc};
+    for (int q = 0; q < 3; ++q) { /* r, s, t */
+      const double *mx = rst + (int64_t)(3 * q) * n, *my = rst + (int64_t)(3 * q + 1) * n,
+                   *mz = rst + (int64_t)(3 * q + 2) * n;
+      for (int i = 0; i < nxyz; ++i) {
+        const int64_t p = o + i;
+        double a = mx[p] * vx[p] * fi[p];
+        a = a + my[p] * vy[p] * fi[p];
+        a = a + mz[p] * vz[p] * fi[p];
+        t[q][i] = a * w3[i];
+      }
+    }
+    ref_local_grad3_t(dtfi + o, ta, tb, tc, nx1 - 1, d, dt, wk);
+    for (int i = 0; i < nxyz; ++i) dtfi[o + i] = dtfi[o + i] / bm1[o + i];
+  }
+  free(w3);
+  free(ta);
+}
+
+/* convopo with param(86) != 0 (core/navier1.f:1221-1286): the
+ * skew-symmetric form, with cmask1 = 0 / cmask2 = 1 on the points of
+ * outflow faces (cmask, :1390; ofc: 6 flags per element, preprocessor face
+ * order) and 1 / 0 elsewhere. */
+void ref_convopo(int nx1, int nel, double *conv, const double *fi, const double *vx,
+                 const double *vy, const double *vz, const double *rst, const double *jac,
+                 const double *bm1, const int *ofc) {
+  const int nxyz = nx1 * nx1 * nx1, N = nx1 - 1;
+  const int64_t n = (int64_t)nxyz * nel;
+  double *c1 = (double *)malloc(sizeof(double) * 5 * n), *c2 = c1 + n, *mfi = c2 + n,
+         *dm = mfi + n, *md = dm + n;
+  for (int64_t i = 0; i < n; ++i) {
+    c1[i] = 1.0;
+    c2[i] = 0.0;
+    conv[i] = 0.0;
+  }
+  for (int e = 0; e < nel; ++e)
+    for (int f = 1; f <= 6; ++f) {
+      if (!ofc[6 * e + f - 1]) continue;
+      for (int k = 0; k < nx1; ++k)
+        for (int j = 0; j < nx1; ++j)
+          for (int i = 0; i < nx1; ++i) {
+            const int on = (f == 1 && j == 0) || (f == 2 && i == N) || (f == 3 && j == N) ||
+                           (f == 4 && i == 0) || (f == 5 && k == 0) || (f == 6 && k == N);
+            if (!on) continue;
+            const int64_t p = (int64_t)nxyz * e + i + nx1 * (j + nx1 * k);
+            c1[p] = 0.0;
+            c2[p] = 1.0;
+          }
+    }
+  const double *v[3] = {vx, vy, vz};
+  (void)v;
+  for (int64_t i = 0; i < n; ++i) mfi[i] = fi[i] * c1[i];
+  ref_conv1(nx1, nel, dm, mfi, vx, vy, vz, rst, jac);
+  for (int64_t i = 0; i < n; ++i) {
+    md[i] = dm[i] * c1[i];
+    conv[i] = conv[i] + 0.5 * md[i];
+    md[i] = dm[i] * c2[i];
+    conv[i] = conv[i] + md[i];
+  }
+  ref_conv2(nx1, nel, dm, mfi, vx, vy, vz, rst, bm1);
+  for (int64_t i = 0; i < n; ++i) {
+    md[i] = dm[i] * c1[i];
+    conv[i] = conv[i] + -0.5 * md[i];
+  }
+  for (int64_t i = 0; i < n; ++i) mfi[i] = fi[i] * c2[i];
+  ref_conv1(nx1, nel, dm, mfi, vx, vy, vz, rst, jac);
+  for (int64_t i = 0; i < n; ++i) {
+    md[i] = dm[i] * c2[i];
+    conv[i] = conv[i] + 0.5 * md[i];
+  }
+  ref_conv2(nx1, nel, dm, mfi, vx, vy, vz, rst, bm1);
+  for (int64_t i = 0; i < n; ++i) {
+    md[i] = dm[i] * c1[i];
+    conv[i] = conv[i] + -1. * md[i];
+    md[i] = dm[i] * c2[i];
+    conv[i] = conv[i] + 0.5 * md[i];
+  }
+  free(c1);
+}

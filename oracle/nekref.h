@@ -217,6 +217,12 @@ void ref_convect_cons(int nx1, int nel, int lxd, double *conv, const double *u,
                       const double *vx, const double *vy, const double *vz, const double *rst,
                       const double *bm1);
 
+void ref_conv2(int nx1, int nel, double *dtfi, const double *fi, const double *vx,
+               const double *vy, const double *vz, const double *rst, const double *bm1);
+void ref_convopo(int nx1, int nel, double *conv, const double *fi, const double *vx,
+                 const double *vy, const double *vz, const double *rst, const double *jac,
+                 const double *bm1, const int *ofc);
+
 /* sizes of an operator state */
 int ref_ops_nx1(const ref_ops *ops);
 int ref_ops_nel(const ref_ops *ops);

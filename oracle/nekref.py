@@ -86,6 +86,8 @@ def lib():
             L.ref_sumab.argtypes = [C.c_int64, _dp, _dp, _dp, _dp, C.c_int]
             L.ref_convect_new.argtypes = [C.c_int, C.c_int, C.c_int] + [_dp] * 7
             L.ref_convect_cons.argtypes = [C.c_int, C.c_int, C.c_int] + [_dp] * 7
+            L.ref_conv2.argtypes = [C.c_int, C.c_int] + [_dp] * 7
+            L.ref_convopo.argtypes = [C.c_int, C.c_int] + [_dp] * 8 + [_vp]
             L.ref_cresvsp.argtypes = [_vp] + [_dp] * 15
             L.ref_crespsp.argtypes = [_vp] + [_dp] * 13 + [C.c_double, C.c_int, _dp, _dp, _dp, _dp,
                                                            _dp, _vp, _dp]
@@ -502,6 +504,21 @@ def convect_cons(nx1, nel, lxd, u, v, rst, bm1):
     out = np.zeros(nx1 ** 3 * nel)
     lib().ref_convect_cons(int(nx1), int(nel), int(lxd), out, _c(u), *[_c(a) for a in v],
                            _c(rst), _c(bm1))
+    return out
+
+
+def conv2(nx1, nel, fi, v, rst, bm1):
+    out = np.zeros(nx1 ** 3 * nel)
+    lib().ref_conv2(int(nx1), int(nel), out, _c(fi), *[_c(a) for a in v], _c(rst), _c(bm1))
+    return out
+
+
+def convopo(nx1, nel, fi, v, rst, jac, bm1, ofc):
+    """the skew-symmetric convective form; ofc (nel, 6) outflow-face flags"""
+    out = np.zeros(nx1 ** 3 * nel)
+    of = np.ascontiguousarray(ofc, dtype=np.int32).reshape(-1)
+    lib().ref_convopo(int(nx1), int(nel), out, _c(fi), *[_c(a) for a in v], _c(rst), _c(jac),
+                      _c(bm1), of.ctypes.data_as(C.c_void_p))
     return out
 
 

@@ -158,6 +158,8 @@ def test_python_wrappers_reach_the_library(lib):
         lambda: g.dealias_setup(12),
         lambda: g.convop(d, d, [d, d, d]),
         lambda: g.convect_cons(d, d, [d, d, d]),
+        lambda: g.conv2(d, d, [d, d, d]),
+        lambda: g.convopo(d, d, [d, d, d], ofc=np.zeros((2, 6), dtype=np.int32)),
         lambda: g.cresvsp([d, d, d], [d, d, d], d, d, d, d, d, [d, d, d]),
         lambda: g.crespsp(d, [d, d, d], d, d, d, d, [d, d, d], d, 1.5, True, v=[d, d, d],
                           fbc=np.zeros((1, 6), dtype=np.int32)),

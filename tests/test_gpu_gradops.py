@@ -126,3 +126,23 @@ def test_conservative_convection_matches_the_oracle(gpu_lib, oracle):
     lib.convect_cons(c, dev(u), [dev(a) for a in v])
     want = oracle.convect_cons(nx1, nel, lxd, u, v, rst, P["bm1"])
     assert np.allclose(c.cpu().numpy(), want, rtol=0, atol=1e-12 * np.abs(want).max())
+
+
+def test_conv2_and_skew_symmetric_form_bit_for_bit(gpu_lib, oracle):
+    torch = pytest.importorskip("torch")
+    P = oracle.box_problem(6, 3, 2, 2, v=rng_unit_vector(165))
+    nx1, nel, n = P["nx1"], P["nel"], P["n"]
+    rst, jac = oracle.geom_rst(nx1, nel, P["x"], P["y"], P["z"])
+    lib = gpu_lib(0)
+    lib.setup_xyz(nx1, nel, P["D"], P["wgll"], P["x"], P["y"], P["z"], P["glo_num"])
+    rng = np.random.default_rng(166)
+    v = [rng.standard_normal(n) for _ in range(3)]
+    fi = rng.standard_normal(n)
+    dev = lambda a: torch.tensor(np.ascontiguousarray(a), device="cuda")
+    out = torch.zeros(n, dtype=torch.float64, device="cuda")
+    lib.conv2(out, dev(fi), [dev(a) for a in v])
+    assert np.array_equal(out.cpu().numpy(), oracle.conv2(nx1, nel, fi, v, rst, P["bm1"]))
+    ofc = rng.integers(0, 2, size=(nel, 6)).astype(np.int32)
+    lib.convopo(out, dev(fi), [dev(a) for a in v], ofc=ofc)
+    want = oracle.convopo(nx1, nel, fi, v, rst, jac, P["bm1"], ofc)
+    assert np.array_equal(out.cpu().numpy(), want)

@@ -171,3 +171,25 @@ def test_conservative_convection(oracle):
     ca = oracle.convect_new(nx1, nel, lxd, u, v, rst, P["bm1"])
     assert np.allclose(cc, ca, rtol=0, atol=1e-11)
     assert np.allclose(ca, -P["y"] * 0.4 + P["x"] * (-0.9), rtol=0, atol=1e-11)
+
+
+def test_conv2_is_the_transpose_of_conv1(oracle):
+    """sum bm1 psi conv2(phi) = sum bm1 phi conv1(psi) on every element
+    (conv2 is the weak transposed form); with no outflow face the
+    skew-symmetric form is (conv1 - conv2) / 2 and is skew:
+    sum bm1 phi convopo(phi) = 0."""
+    P = oracle.box_problem(5, 3, 2, 2, v=rng_unit_vector(148))
+    nx1, nel, n = P["nx1"], P["nel"], P["n"]
+    rst, jac = oracle.geom_rst(nx1, nel, P["x"], P["y"], P["z"])
+    rng = np.random.default_rng(149)
+    v = [rng.standard_normal(n) for _ in range(3)]
+    phi, psi = rng.standard_normal(n), rng.standard_normal(n)
+    lhs = np.sum(P["bm1"] * psi * oracle.conv2(nx1, nel, phi, v, rst, P["bm1"]))
+    rhs = np.sum(P["bm1"] * phi * oracle.conv1(nx1, nel, psi, v, rst, jac))
+    assert abs(lhs - rhs) <= 1e-11 * (abs(lhs) + abs(rhs))
+    none = np.zeros((nel, 6), dtype=np.int32)
+    c = oracle.convopo(nx1, nel, phi, v, rst, jac, P["bm1"], none)
+    want = 0.5 * oracle.conv1(nx1, nel, phi, v, rst, jac) - 0.5 * oracle.conv2(nx1, nel, phi, v, rst, P["bm1"])
+    assert np.allclose(c, want, rtol=0, atol=1e-12 * np.abs(want).max())
+    skew = np.sum(P["bm1"] * phi * c)
+    assert abs(skew) <= 1e-11 * np.sum(np.abs(P["bm1"] * phi * c))
