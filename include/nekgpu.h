@@ -20,6 +20,16 @@
  * device pointers (cudaMalloc'ed, or torch tensors' data_ptr) and copy
  * nothing; they run on the handle's stream and return when the work is
  * complete.
+ *
+ * Ordering with the caller's own GPU work: the handle's stream is created
+ * non-blocking, so every call first makes it wait for all work already
+ * queued on the legacy default stream (stream 0: torch's default stream,
+ * cudaMemcpy, kernels launched without a stream), and every call waits for
+ * the handle's stream before it returns.  Inputs written by such work are
+ * therefore complete when the call's kernels read them, and outputs may be
+ * read from any stream once the call has returned.  Work the caller queued
+ * on a non-blocking stream of its own must be finished (or synchronized
+ * with stream 0) before the call.
  */
 #ifndef NEKGPU_H
 #define NEKGPU_H
@@ -375,10 +385,13 @@ int nekgpu_hmholtz_dev(const int64_t *handle, double *u, double *rhs, const doub
  * doubles (64 KiB) that every GPU loading this library holds until the
  * process exits, and makes no device allocation itself.  Meshes of more than
  * NEKGPU_NOALLOC_MAX_POINTS local points are rejected with NEKGPU_EINVAL.
- * The first call on a device looks up that array's device address, so make
- * it before any stream capture.  Calls share the array: calls that overlap on
- * the GPU (from several threads or handles at once) race on it; each call
- * writes every slot it reads, so nothing needs clearing between calls. */
+ * Like every call here it waits for its own kernels before it returns.  The
+ * first call on a device also looks up that array's device address (with
+ * the device current); make that first call before any stream capture.
+ * Calls share the array: calls that overlap on the GPU (from several threads
+ * or handles at once) race on it; each call writes every slot it reads, so
+ * nothing needs clearing between calls.  With NEKGPU_OPT_TIMING on it
+ * records the scan and the operator together, as nekgpu_axhelm_dev does. */
 #define NEKGPU_NOALLOC_MAX_POINTS 4194304
 int nekgpu_axhelm_dev_noalloc(const int64_t *handle, double *au, const double *u,
                               const double *h1, const double *h2, const int *imesh,

@@ -869,6 +869,10 @@ int nekgpu_batch_solve_dev(const int64_t* batch, const int* nprob, double* const
       return bfail(B, NEKGPU_EINVAL, "null array for problem " + std::to_string(p));
   cudaSetDevice(B->device);
   B->err.clear();
+  // The problems' handles share the batch's stream: waiting once makes the
+  // batch's kernels start after the caller's queued work (handle_enter).
+  if (np > 0 && nekgpu::handle_enter(*B->probs[0]) != cudaSuccess)
+    return bfail(B, NEKGPU_ECUDA, "call entry failed");
   int rc;
   if (mixed && *mixed) {
     if (*mixed != 1 && *mixed != 2) return bfail(B, NEKGPU_EINVAL, "mixed must be 0, 1 or 2");
@@ -886,8 +890,10 @@ int nekgpu_batch_solve_dev(const int64_t* batch, const int* nprob, double* const
     if (nouter)
       for (int p = 0; p < np; ++p) nouter[p] = 0;
   }
+  const cudaError_t le = cudaStreamSynchronize(B->stream);  // finished before the call returns
   if (rc) return bfail(B, rc == -4 ? NEKGPU_ENOMEM : NEKGPU_ECUDA,
                        B->err.empty() ? "batch solve failed" : B->err);
+  if (le != cudaSuccess) return bfail(B, NEKGPU_ECUDA, std::string("batch solve: ") + cudaGetErrorString(le));
   for (int p = 0; p < np; ++p)
     if (status[p] && status[p] != NEKGPU_ENOTCONV && B->err.empty())
       B->err = "problem " + std::to_string(p) + ": " + B->probs[p]->err;

@@ -37,11 +37,24 @@ int cuda_fail(Handle* H, cudaError_t e, const char* where) {
   return fail(H, NEKGPU_ECUDA, std::string(where) + ": " + cudaGetErrorString(e));
 }
 
+// Every call on a handle: look it up, wait for the caller's queued work
+// (handle_enter), and wait for the handle's stream when the call returns, on
+// every return path, so that no kernel of the call is still running then.
+// The paths that read results back already synchronize and report errors;
+// the guard only makes the completion promise hold on all of them.
+struct LeaveGuard {
+  Handle* h;
+  ~LeaveGuard() {
+    if (h && h->stream) cudaStreamSynchronize(h->stream);
+  }
+};
+
 #define GET_HANDLE(hp)                                                   \
   Handle* H = get(hp);                                                   \
   if (!H) return fail(nullptr, NEKGPU_EHANDLE, "unknown handle");        \
-  if (cudaSetDevice(H->device) != cudaSuccess)                           \
-    return fail(H, NEKGPU_ECUDA, "cudaSetDevice failed");
+  if (cudaError_t e_ = handle_enter(*H))                                 \
+    return cuda_fail(H, e_, "call entry");                               \
+  LeaveGuard leave_guard_{H};
 
 #define NEED_MESH()                                                      \
   if (!H->has_mesh) return fail(H, NEKGPU_ENOSETUP, "mesh not set up (nekgpu_setup)");
@@ -209,7 +222,25 @@ int handle_open(Handle& H, int device, cudaStream_t shared, std::string& err) {
   cudaEventCreate(&H.ev1);
   cudaEventCreate(&H.evt0);
   cudaEventCreate(&H.evt1);
+  if ((e = cudaEventCreateWithFlags(&H.ev_enter, cudaEventDisableTiming)) != cudaSuccess) {
+    err = std::string("event: ") + cudaGetErrorString(e);
+    return -3;
+  }
   return 0;
+}
+
+cudaError_t handle_enter(Handle& H) {
+  cudaError_t e = cudaSetDevice(H.device);
+  if (e != cudaSuccess) return e;
+  e = cudaEventRecord(H.ev_enter, cudaStreamLegacy);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(H.stream, H.ev_enter, 0);
+  return e;
+}
+
+cudaError_t handle_leave(Handle& H) {
+  cudaError_t e = cudaStreamSynchronize(H.stream);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  return e;
 }
 
 void handle_close(Handle& H) {
@@ -237,6 +268,8 @@ void handle_close(Handle& H) {
   cudaEventDestroy(H.ev1);
   cudaEventDestroy(H.evt0);
   cudaEventDestroy(H.evt1);
+  if (H.ev_enter) cudaEventDestroy(H.ev_enter);
+  H.ev_enter = nullptr;
   if (H.own_stream && H.stream) cudaStreamDestroy(H.stream);
   H.stream = nullptr;
 }

@@ -340,8 +340,8 @@ using namespace nekgpu;
 extern "C" int nekgpu_dealias_setup(const int64_t* handle, const int* lxd) {
   Handle* H = handle_lookup(handle);
   if (!H) return handle_fail(nullptr, NEKGPU_EHANDLE, "unknown handle");
-  if (cudaSetDevice(H->device) != cudaSuccess)
-    return handle_fail(H, NEKGPU_ECUDA, "cudaSetDevice failed");
+  if (handle_enter(*H) != cudaSuccess)
+    return handle_fail(H, NEKGPU_ECUDA, "call entry failed");
   if (!H->has_mesh || !H->mesh.has_rst)
     return handle_fail(H, NEKGPU_ENOSETUP,
                        "metric terms not set up (the geometry must come from coordinates)");
@@ -355,17 +355,18 @@ extern "C" int nekgpu_convop_dev(const int64_t* handle, double* conv, const doub
                                  const double* vx, const double* vy, const double* vz) {
   Handle* H = handle_lookup(handle);
   if (!H) return handle_fail(nullptr, NEKGPU_EHANDLE, "unknown handle");
-  if (cudaSetDevice(H->device) != cudaSuccess)
-    return handle_fail(H, NEKGPU_ECUDA, "cudaSetDevice failed");
+  if (handle_enter(*H) != cudaSuccess)
+    return handle_fail(H, NEKGPU_ECUDA, "call entry failed");
   if (!H->has_mesh || !H->mesh.has_rst)
     return handle_fail(H, NEKGPU_ENOSETUP,
                        "metric terms not set up (the geometry must come from coordinates)");
   if (!conv || !u || !vx || !vy || !vz) return handle_fail(H, NEKGPU_EINVAL, "null argument");
   const int rc = H->dealias ? convop_dealias(*H, conv, u, vx, vy, vz)
                             : launch_conv1(*H, conv, u, vx, vy, vz);
-  const cudaError_t e = cudaGetLastError();
-  if (rc || e != cudaSuccess)
+  const cudaError_t e = handle_leave(*H);  // finished before the call returns
+  if (e != cudaSuccess)
     return handle_fail(H, NEKGPU_ECUDA, std::string("convop: ") + cudaGetErrorString(e));
+  if (rc) return handle_fail(H, NEKGPU_ECUDA, "convop failed");
   return NEKGPU_OK;
 }
 
@@ -373,14 +374,15 @@ extern "C" int nekgpu_convect_cons_dev(const int64_t* handle, double* conv, cons
                                        const double* vx, const double* vy, const double* vz) {
   Handle* H = handle_lookup(handle);
   if (!H) return handle_fail(nullptr, NEKGPU_EHANDLE, "unknown handle");
-  if (cudaSetDevice(H->device) != cudaSuccess)
-    return handle_fail(H, NEKGPU_ECUDA, "cudaSetDevice failed");
+  if (handle_enter(*H) != cudaSuccess)
+    return handle_fail(H, NEKGPU_ECUDA, "call entry failed");
   if (!H->has_mesh || !H->dealias)
     return handle_fail(H, NEKGPU_ENOSETUP, "dealiasing not set up (nekgpu_dealias_setup)");
   if (!conv || !u || !vx || !vy || !vz) return handle_fail(H, NEKGPU_EINVAL, "null argument");
   const int rc = convect_cons_dealias(*H, conv, u, vx, vy, vz);
-  const cudaError_t e = cudaGetLastError();
-  if (rc || e != cudaSuccess)
+  const cudaError_t e = handle_leave(*H);  // finished before the call returns
+  if (e != cudaSuccess)
     return handle_fail(H, NEKGPU_ECUDA, std::string("convect_cons: ") + cudaGetErrorString(e));
+  if (rc) return handle_fail(H, NEKGPU_ECUDA, "convect_cons failed");
   return NEKGPU_OK;
 }

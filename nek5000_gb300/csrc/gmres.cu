@@ -557,8 +557,8 @@ extern "C" int nekgpu_hmh_gmres_dev(const int64_t* handle, double* res, const do
                                     double* rnorm) {
   Handle* H = handle_lookup(handle);
   if (!H) return handle_fail(nullptr, NEKGPU_EHANDLE, "unknown handle");
-  if (cudaSetDevice(H->device) != cudaSuccess)
-    return handle_fail(H, NEKGPU_ECUDA, "cudaSetDevice failed");
+  if (handle_enter(*H) != cudaSuccess)
+    return handle_fail(H, NEKGPU_ECUDA, "call entry failed");
   if (!H->has_mesh) return handle_fail(H, NEKGPU_ENOSETUP, "mesh not set up (nekgpu_setup)");
   if (!res || !h1 || !h2 || !wt || !mask || !tol || !maxit || !niter || !div0 || !rnorm)
     return handle_fail(H, NEKGPU_EINVAL, "null argument");
@@ -569,6 +569,7 @@ extern "C" int nekgpu_hmh_gmres_dev(const int64_t* handle, double* res, const do
   H->err.clear();
   const int rc = gmres_solve(*H, res, h1, h2, wt, mask, *tol, *maxit, m,
                              null_space && *null_space != 0, niter, div0, rnorm);
+  handle_leave(*H);  // no kernel of the call runs after it returns
   if (rc == -5) return handle_fail(H, NEKGPU_ENOTCONV, H->err);
   if (rc) return handle_fail(H, rc == -4 ? NEKGPU_ENOMEM : NEKGPU_ECUDA,
                              H->err.empty() ? "gmres failed" : H->err);
@@ -581,8 +582,8 @@ extern "C" int nekgpu_hmh_flex_cg_dev(const int64_t* handle, double* res, const 
                                       int* niter, double* div0, double* rnorm) {
   Handle* H = handle_lookup(handle);
   if (!H) return handle_fail(nullptr, NEKGPU_EHANDLE, "unknown handle");
-  if (cudaSetDevice(H->device) != cudaSuccess)
-    return handle_fail(H, NEKGPU_ECUDA, "cudaSetDevice failed");
+  if (handle_enter(*H) != cudaSuccess)
+    return handle_fail(H, NEKGPU_ECUDA, "call entry failed");
   if (!H->has_mesh) return handle_fail(H, NEKGPU_ENOSETUP, "mesh not set up (nekgpu_setup)");
   if (!res || !h1 || !h2 || !wt || !mask || !tol || !maxit || !niter || !div0 || !rnorm)
     return handle_fail(H, NEKGPU_EINVAL, "null argument");
@@ -590,6 +591,7 @@ extern "C" int nekgpu_hmh_flex_cg_dev(const int64_t* handle, double* res, const 
   H->err.clear();
   const int rc = flex_cg_solve(*H, res, h1, h2, wt, mask, *tol, *maxit,
                                null_space && *null_space != 0, niter, div0, rnorm);
+  handle_leave(*H);  // no kernel of the call runs after it returns
   if (rc == -5) return handle_fail(H, NEKGPU_ENOTCONV, H->err);
   if (rc) return handle_fail(H, rc == -4 ? NEKGPU_ENOMEM : NEKGPU_ECUDA,
                              H->err.empty() ? "flex cg failed" : H->err);

@@ -431,8 +431,8 @@ Handle* grad_handle(const int64_t* handle, int* rc) {
     *rc = handle_fail(nullptr, NEKGPU_EHANDLE, "unknown handle");
     return nullptr;
   }
-  if (cudaSetDevice(H->device) != cudaSuccess) {
-    *rc = handle_fail(H, NEKGPU_ECUDA, "cudaSetDevice failed");
+  if (handle_enter(*H) != cudaSuccess) {
+    *rc = handle_fail(H, NEKGPU_ECUDA, "call entry failed");
     return nullptr;
   }
   if (!H->has_mesh || !H->mesh.has_rst) {
@@ -445,9 +445,11 @@ Handle* grad_handle(const int64_t* handle, int* rc) {
   return H;
 }
 
+// End of a gradient-type call: the kernels must have finished before the
+// call returns (the caller may read the outputs from another stream).
 int grad_done(Handle* H, int rc, const char* what) {
+  const cudaError_t e = handle_leave(*H);
   if (rc) return handle_fail(H, NEKGPU_EINVAL, std::string(what) + ": lx1 out of range");
-  const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return handle_fail(H, NEKGPU_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
   return NEKGPU_OK;
 }

@@ -625,14 +625,15 @@ extern "C" int nekgpu_h1mg_setup(const int64_t* handle, const double* x, const d
                                  const int* fbc, const int* null_space) {
   Handle* H = handle_lookup(handle);
   if (!H) return handle_fail(nullptr, NEKGPU_EHANDLE, "unknown handle");
-  if (cudaSetDevice(H->device) != cudaSuccess)
-    return handle_fail(H, NEKGPU_ECUDA, "cudaSetDevice failed");
+  if (handle_enter(*H) != cudaSuccess)
+    return handle_fail(H, NEKGPU_ECUDA, "call entry failed");
   if (!H->has_mesh) return handle_fail(H, NEKGPU_ENOSETUP, "mesh not set up (nekgpu_setup)");
   if (!x || !y || !z || !glo_num || (!mask && !fbc))
     return handle_fail(H, NEKGPU_EINVAL, "null argument");
   H->err.clear();
   H->mg.reset();
   const int rc = h1mg_setup(*H, x, y, z, mask, glo_num, fbc, null_space && *null_space != 0);
+  handle_leave(*H);  // no kernel of the call runs after it returns
   if (rc) return handle_fail(H, rc, H->err.empty() ? "h1mg setup failed" : H->err);
   return NEKGPU_OK;
 }
@@ -640,8 +641,8 @@ extern "C" int nekgpu_h1mg_setup(const int64_t* handle, const double* x, const d
 extern "C" int nekgpu_h1mg_free(const int64_t* handle) {
   Handle* H = handle_lookup(handle);
   if (!H) return handle_fail(nullptr, NEKGPU_EHANDLE, "unknown handle");
-  if (cudaSetDevice(H->device) != cudaSuccess)
-    return handle_fail(H, NEKGPU_ECUDA, "cudaSetDevice failed");
+  if (handle_enter(*H) != cudaSuccess)
+    return handle_fail(H, NEKGPU_ECUDA, "call entry failed");
   cudaStreamSynchronize(H->stream);
   H->mg.reset();
   return NEKGPU_OK;
@@ -650,8 +651,8 @@ extern "C" int nekgpu_h1mg_free(const int64_t* handle) {
 extern "C" int nekgpu_h1mg_apply_dev(const int64_t* handle, double* z, double* rhs) {
   Handle* H = handle_lookup(handle);
   if (!H) return handle_fail(nullptr, NEKGPU_EHANDLE, "unknown handle");
-  if (cudaSetDevice(H->device) != cudaSuccess)
-    return handle_fail(H, NEKGPU_ECUDA, "cudaSetDevice failed");
+  if (handle_enter(*H) != cudaSuccess)
+    return handle_fail(H, NEKGPU_ECUDA, "call entry failed");
   if (!H->mg) return handle_fail(H, NEKGPU_ENOSETUP, "h1mg not set up (nekgpu_h1mg_setup)");
   if (!z || !rhs) return handle_fail(H, NEKGPU_EINVAL, "null argument");
   H->err.clear();

@@ -158,6 +158,7 @@ struct Handle {
   // timing
   bool timing = false;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, evt0 = nullptr, evt1 = nullptr;
+  cudaEvent_t ev_enter = nullptr;  // handle_enter's marker on the legacy default stream
   std::vector<cudaEvent_t> ax_ev;  // per-launch operator timing pool
   double ms_total = 0.0, ms_axhelm = 0.0, ms_gs = 0.0, ms_update = 0.0;
   int n_axhelm = 0;
@@ -356,6 +357,15 @@ void set_error(Handle& h, const std::string& msg);
 // handle use that stream instead of creating one.
 int handle_open(Handle& h, int device, cudaStream_t shared, std::string& err);
 void handle_close(Handle& h);
+// Start of every call on a handle: make the handle's device current and make
+// the handle's stream wait for all work already queued on the legacy default
+// stream (torch's default stream, cudaMemcpy, kernels launched on stream 0).
+// The handle's stream is non-blocking, so without this wait a kernel of the
+// call could read an input the caller's last kernel has not finished writing.
+cudaError_t handle_enter(Handle& h);
+// End of every call: wait for the handle's stream and report the first error
+// it met, so that the caller may read the outputs from any stream.
+cudaError_t handle_leave(Handle& h);
 int handle_setup(Handle& h, int lx1, int nel, const double* dxm1, const double* const* g6,
                  const double* bm1, const int64_t* glo_num, std::string& err);
 

@@ -723,8 +723,8 @@ extern "C" int nekgpu_cggo_mixed_multi_dev(const int64_t* handle, const int* nfi
   (void)isd;
   Handle* H = handle_lookup(handle);
   if (!H) return handle_fail(nullptr, NEKGPU_EHANDLE, "unknown handle");
-  if (cudaSetDevice(H->device) != cudaSuccess)
-    return handle_fail(H, NEKGPU_ECUDA, "cudaSetDevice failed");
+  if (handle_enter(*H) != cudaSuccess)
+    return handle_fail(H, NEKGPU_ECUDA, "call entry failed");
   if (!H->has_mesh) return handle_fail(H, NEKGPU_ENOSETUP, "mesh not set up (nekgpu_setup)");
   if (!nfield || !x || !f || !h1 || !h2 || !mask || !mult || !binv || !tin || !maxit ||
       !niter_outer || !niter_inner || !rbn0 || !rbn2 || !status)
@@ -742,6 +742,7 @@ extern "C" int nekgpu_cggo_mixed_multi_dev(const int64_t* handle, const int* nfi
   if (H->timing) cudaEventRecord(H->evt0, H->stream);
   const int rc = mixed_multi_solve(*H, nc, x, f, h1, h2, mask, mult, binv, *tin, *maxit, itol,
                                    niter_outer, niter_inner, rbn0, rbn2, status);
+  handle_leave(*H);  // no kernel of the call runs after it returns
   if (H->timing) {
     cudaEventRecord(H->evt1, H->stream);
     cudaEventSynchronize(H->evt1);

@@ -115,8 +115,8 @@ extern "C" int nekgpu_axhelm_dev_noalloc(const int64_t* handle, double* au, cons
   (void)isd;
   Handle* H = handle_lookup(handle);
   if (!H) return handle_fail(nullptr, NEKGPU_EHANDLE, "unknown handle");
-  if (cudaSetDevice(H->device) != cudaSuccess)
-    return handle_fail(H, NEKGPU_ECUDA, "cudaSetDevice failed");
+  if (handle_enter(*H) != cudaSuccess)
+    return handle_fail(H, NEKGPU_ECUDA, "call entry failed");
   if (!H->has_mesh) return handle_fail(H, NEKGPU_ENOSETUP, "mesh not set up (nekgpu_setup)");
   if (!au || !u || !h1 || !h2) return handle_fail(H, NEKGPU_EINVAL, "null array argument");
   const int64_t n = H->mesh.n;
@@ -130,9 +130,11 @@ extern "C" int nekgpu_axhelm_dev_noalloc(const int64_t* handle, double* au, cons
   int rc = scratch_address(H->device, &scratch, err);
   if (rc) return handle_fail(H, rc, err);
   const int nb = (int)((n + kPointsPerBlock - 1) / kPointsPerBlock);
+  if (H->timing) cudaEventRecord(H->evt0, H->stream);
   count_launch();
   coef_scan_kernel<<<nb, kScanThreads, 0, H->stream>>>(h1, h2, n, scratch);
-  double part[4 * kScanMaxBlocks];
+  // host copy of the partials: per thread, not on the stack (64 KiB)
+  static thread_local double part[4 * kScanMaxBlocks];
   cudaError_t e = cudaMemcpyAsync(part, scratch, 4 * (size_t)nb * sizeof(double),
                                   cudaMemcpyDeviceToHost, H->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(H->stream);
@@ -166,8 +168,16 @@ extern "C" int nekgpu_axhelm_dev_noalloc(const int64_t* handle, double* au, cons
   }
   e = H->exact ? launch_axhelm<double, true>(H->mesh, H->mesh.f64, au, u, c, H->stream)
                : launch_axhelm<double, false>(H->mesh, H->mesh.f64, au, u, c, H->stream);
+  if (e == cudaSuccess && H->timing) e = cudaEventRecord(H->evt1, H->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(H->stream);
   if (e != cudaSuccess)
     return handle_fail(H, NEKGPU_ECUDA, std::string("axhelm_dev_noalloc: ") + cudaGetErrorString(e));
+  if (H->timing) {  // as nekgpu_axhelm_dev: scan and operator together
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, H->evt0, H->evt1);
+    H->ms_total = ms;
+    H->ms_axhelm = ms;
+    H->n_axhelm = 1;
+  }
   return NEKGPU_OK;
 }

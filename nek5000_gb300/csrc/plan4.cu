@@ -230,8 +230,8 @@ Handle* p4_handle(const int64_t* handle, int* rc) {
     *rc = handle_fail(nullptr, NEKGPU_EHANDLE, "unknown handle");
     return nullptr;
   }
-  if (cudaSetDevice(H->device) != cudaSuccess) {
-    *rc = handle_fail(H, NEKGPU_ECUDA, "cudaSetDevice failed");
+  if (handle_enter(*H) != cudaSuccess) {
+    *rc = handle_fail(H, NEKGPU_ECUDA, "call entry failed");
     return nullptr;
   }
   if (!H->has_mesh || !H->mesh.has_rst) {
@@ -243,10 +243,15 @@ Handle* p4_handle(const int64_t* handle, int* rc) {
   return H;
 }
 
+// End of a splitting-step call: the kernels must have finished before the
+// call returns (the caller may read the outputs from another stream).  A
+// nonzero rc is a failure the call detected itself (an allocation or a
+// launch); its message names the call, not the CUDA status.
 int p4_done(Handle* H, int rc, const char* what) {
-  const cudaError_t e = cudaGetLastError();
-  if (rc || e != cudaSuccess)
+  const cudaError_t e = handle_leave(*H);
+  if (e != cudaSuccess)
     return handle_fail(H, NEKGPU_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
+  if (rc) return handle_fail(H, rc < 0 ? rc : NEKGPU_ECUDA, std::string(what) + " failed");
   return NEKGPU_OK;
 }
 
@@ -384,8 +389,8 @@ Handle* p4_mesh_handle(const int64_t* handle, int* rc) {
     *rc = handle_fail(nullptr, NEKGPU_EHANDLE, "unknown handle");
     return nullptr;
   }
-  if (cudaSetDevice(H->device) != cudaSuccess) {
-    *rc = handle_fail(H, NEKGPU_ECUDA, "cudaSetDevice failed");
+  if (handle_enter(*H) != cudaSuccess) {
+    *rc = handle_fail(H, NEKGPU_ECUDA, "call entry failed");
     return nullptr;
   }
   if (!H->has_mesh) {

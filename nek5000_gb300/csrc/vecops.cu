@@ -156,8 +156,8 @@ Handle* vec_handle(const int64_t* handle, int* rc) {
     *rc = handle_fail(nullptr, NEKGPU_EHANDLE, "unknown handle");
     return nullptr;
   }
-  if (cudaSetDevice(H->device) != cudaSuccess) {
-    *rc = handle_fail(H, NEKGPU_ECUDA, "cudaSetDevice failed");
+  if (handle_enter(*H) != cudaSuccess) {
+    *rc = handle_fail(H, NEKGPU_ECUDA, "call entry failed");
     return nullptr;
   }
   if (!H->has_mesh) {
@@ -168,8 +168,10 @@ Handle* vec_handle(const int64_t* handle, int* rc) {
   return H;
 }
 
+// End of a vector call: the kernels must have finished before the call
+// returns (the caller may read the outputs from another stream).
 int vec_done(Handle* H, const char* what) {
-  const cudaError_t e = cudaGetLastError();
+  const cudaError_t e = handle_leave(*H);
   if (e != cudaSuccess) return handle_fail(H, NEKGPU_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
   return NEKGPU_OK;
 }
@@ -286,7 +288,7 @@ extern "C" int nekgpu_setprec_local_dev(const int64_t* handle, double* diag, con
   if (detect_coef<double>(*H, h1, h2, n, c))
     return handle_fail(H, NEKGPU_ECUDA, "coefficient scan failed");
   if (setprec_local_f64(*H, diag, c)) return handle_fail(H, NEKGPU_ECUDA, H->err);
-  return NEKGPU_OK;
+  return vec_done(H, "setprec_local");
 }
 
 extern "C" int nekgpu_iface_setup(const int64_t* handle, const int64_t* nk, const int64_t* start,

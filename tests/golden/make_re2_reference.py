@@ -3,9 +3,10 @@ short_tests/lpm_one/uniform.re2 from the reference tree, check it against
 the box its uniform.box describes (element counts, uniform spacing on the
 given ranges, x fastest, preprocessor corner order, the given wall type on
 every outside face), and write the figures tests/test_meshio.py compares
-(re2_reference.json).  Run in a tree where the reference is present:
+(re2_reference.json).  Run where a Nek5000 source tree is present, naming
+its root on the command line or in NEK5000_REFERENCE:
 
-    python tests/golden/make_re2_reference.py /root/reference
+    python tests/golden/make_re2_reference.py <path to the Nek5000 tree>
 """
 import json
 import os
@@ -58,4 +59,7 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("NEK5000_REFERENCE")
+    if not root:
+        sys.exit("name the Nek5000 source tree: an argument or NEK5000_REFERENCE")
+    main(root)

@@ -60,29 +60,6 @@ def test_init_without_gpu_fails_cleanly(lib):
     assert rc in (-3, -1)
 
 
-def test_integration_bindings_name_declared_entry_points():
-    """Every bind(C) name of the Fortran interface module in the integration
-    notes is an entry point the headers declare (the binding a maintainer
-    copies must link)."""
-    doc = open(os.path.join(ROOT, "INTEGRATION.md")).read()
-    names = set(re.findall(r'bind\(C,\s*name="(\w+)"\)', doc))
-    assert names, "no bind(C) names found"
-    assert names <= set(declared_symbols()), sorted(names - set(declared_symbols()))
-
-
-def test_documented_entry_points_exist():
-    """Every nekgpu_* / nekmesh_* name the design and integration notes
-    mention is declared (names ending in '_' stand for a family)."""
-    syms = set(declared_symbols())
-    for f in ("DESIGN.md", "INTEGRATION.md"):
-        text = open(os.path.join(ROOT, f)).read()
-        for name in set(re.findall(r"\b(nek(?:gpu|mesh)_[a-z0-9_]+)\b", text)):
-            if name.endswith("_"):
-                assert any(s.startswith(name) for s in syms), (f, name)
-            else:
-                assert name in syms, (f, name)
-
-
 def _prototypes(path):
     """name -> parameter list of every int-returning entry point of a header"""
     import re

@@ -17,7 +17,10 @@ from re2_util import box_elements, rotate_elements, same_partition, write_re2
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 GOLDEN = os.path.join(ROOT, "tests", "golden", "re2_reference.json")
-REF_RE2 = "/root/reference/short_tests/lpm_one/uniform.re2"
+# the reference's Nek5000 source tree, when the environment names it
+_REF_ROOT = os.environ.get("NEK5000_REFERENCE", "")
+REF_RE2 = (os.path.join(_REF_ROOT, "short_tests", "lpm_one", "uniform.re2") if _REF_ROOT
+           else "")
 
 
 @pytest.fixture(scope="module")
@@ -76,8 +79,9 @@ def test_reference_genbox_file(mio):
     elements of 0.2, x fastest, corners in preprocessor order, W on every
     outside face (150 records) and E inside."""
     ref = json.load(open(GOLDEN))["uniform.re2"]
-    if not os.path.exists(REF_RE2):
-        pytest.skip("reference tree not present (golden digest checked by its generator)")
+    if not REF_RE2 or not os.path.exists(REF_RE2):
+        pytest.skip("NEK5000_REFERENCE does not name a Nek5000 tree (the golden digest was "
+                    "checked by its generator)")
     R = mio.read_re2(REF_RE2)
     assert (R["nelgt"], R["ndim"], R["nelgv"], R["wdsize"]) == tuple(ref["header"])
     xc, yc, zc, _, bcs = box_elements(5, 5, 5)
