@@ -52,6 +52,9 @@ def parse():
     ap.add_argument("--tol", type=float, default=1e-10)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-parity", action="store_true",
+                    help="skip the oracle's full solve (the FP64 and mixed solutions' error "
+                         "against the CPU restatement of the reference at the bench's size)")
     ap.add_argument("--cpu-iters", type=int, default=0, help="oracle PCG iterations per sample")
     ap.add_argument("--inner-tol", type=float, default=None,
                     help="mixed: inner FP32 tolerance (default: the library's for the mode)")
@@ -240,6 +243,20 @@ def allsum(pg, v):
 
 
 # ---------------------------------------------------------------------------
+def cpu_model():
+    """The host CPU's model name as lscpu reports it (aarch64 hosts have no
+    'model name' line in /proc/cpuinfo)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    import platform
+    return platform.processor() or platform.machine()
+
+
 def cpu_sample(M, nthreads, iters):
     """Oracle (CPU restatement of the reference) PCG iterations on the full problem."""
     from oracle import nekref
@@ -278,6 +295,28 @@ def run_reference(args):
             "e2e": {"value": value, "unit": "DOF-iters/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def oracle_parity(M, x64, xmx, it64, tol, nthreads):
+    """The oracle's own FP64 Jacobi-PCG on the same full problem, to the same
+    relative tolerance: its iteration count and the relative 2-norm error of
+    the GPU's FP64 and mixed solutions against its solution.  The oracle sums
+    its dot products over `nthreads` element ranges, as that many ranks of
+    the reference would."""
+    from oracle import nekref
+    ops = nekref.Ops(M["lx1"], M["nel"], M["D"], M["g"], M["bm1"], M["glo_num"], nthreads)
+    t0 = time.perf_counter()
+    xr, it, r0, r2 = ops.cggo(M["f"], M["h1"], M["h2"], M["mask"], M["mult"], M["binv"], -tol,
+                              maxcg=10 ** 6)
+    dt = time.perf_counter() - t0
+    nr = float(np.linalg.norm(xr))
+    return {"oracle_iterations": int(it), "fp64_iterations": int(it64),
+            "rel_error_fp64_vs_oracle": float(np.linalg.norm(x64 - xr)) / nr,
+            "rel_error_mixed_vs_oracle": float(np.linalg.norm(xmx - xr)) / nr,
+            "oracle_rbn2_over_rbn0": r2 / r0 if r0 else None,
+            "oracle_threads": nthreads, "oracle_seconds": dt,
+            "note": "oracle = C restatement of cggo (core/hmholtz.f:611-846), FP64, "
+                    "summation over element ranges as that many ranks would"}
 
 
 def run_gpu(args):
@@ -360,7 +399,9 @@ def run_gpu(args):
                    "avg_launch_ms": r64["ms_ax"],
                    "GB/s": b64 * n / (r64["ms_ax"] * 1e-3) / 1e9, "bytes_per_point": b64,
                    "fp64_tflops": flops_pt * n / (r64["ms_ax"] * 1e-3) / 1e12,
-                   "ncu_fp64_pipe_active_pct": (ns64 or {}).get("fp64_pipe_active_pct")},
+                   "ncu_fp64_pipe_active_pct": (ns64 or {}).get("fp64_pipe_active_pct"),
+                   "ncu_source": (f"{ns64['source']}: committed ncu capture at E=20^3 "
+                                  "(not measured in this run)") if ns64 else None},
         "per_iteration_ms": r64.get("per_iter_ms"),
         "gpu_launches": r64["launches"], "clocks": r64["clocks"]}
     x64 = x.clone() if not args.only_mixed else None
@@ -401,7 +442,10 @@ def run_gpu(args):
                          "peak_source": peak_src, "bytes_per_point": b32,
                          "avg_launch_ms": rmx["ms_ax"], "launches_timed": rmx["n_ax"],
                          "inner_iteration_ms": rmx["per_iter_ms"],
-                         "traffic": ns32["dram_bytes_per_point"] * n if ns32 else None},
+                         "traffic": ns32["dram_bytes_per_point"] * n if ns32 else None,
+                         "traffic_source": (f"{ns32['source']}: DRAM bytes per point of a "
+                                            "committed ncu capture at E=20^3, times this n "
+                                            "(not measured in this run)") if ns32 else None},
             "gpu_launches": rmx["launches"],
             "clocks": rmx["clocks"]}
     # ---- end to end through the host entry points -------------------------------
@@ -441,9 +485,17 @@ def run_gpu(args):
         nth = os.cpu_count() or 1
         iters_cpu = args.cpu_iters or 200
         v, it, dt = cpu_sample(M, nth, iters_cpu)
+        v1, it1, dt1 = cpu_sample(M, 1, max(2, iters_cpu // 10))
         line["cpu_baseline"] = {"value": v, "unit": "DOF-iters/s", "cores": nth, "kind": "port",
+                                "cpu_model": cpu_model(),
                                 "sample": f"{it} Jacobi-PCG iterations of the full problem "
-                                          f"({dt:.1f} s), C restatement of the reference, FP64"}
+                                          f"({dt:.1f} s), C restatement of the reference, FP64",
+                                "one_core": {"value": v1, "unit": "DOF-iters/s", "cores": 1,
+                                             "sample": f"{it1} iterations ({dt1:.1f} s)"}}
+    # ---- parity against the oracle at this size (outside every timed region) ----
+    if rank == 0 and ws == 1 and not args.no_parity and x64 is not None:
+        line["parity"] = oracle_parity(M, x64.cpu().numpy(), x.cpu().numpy(), it64,
+                                       args.tol, os.cpu_count() or 1)
     if rank == 0:
         print(json.dumps(line), flush=True)
     lib.close()

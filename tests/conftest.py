@@ -19,7 +19,7 @@ def pytest_configure(config):
 # test) run after them, so that a failure there is reported after, not
 # instead of, the results of what it builds on.
 _BUILT_ON_THE_REST = ("test_gpu_gradops.py", "test_gpu_h1mg.py", "test_gpu_plan4.py",
-                      "test_gpu_shard.py")
+                      "test_gpu_plan4_step.py", "test_gpu_shard.py")
 
 
 def pytest_collection_modifyitems(session, config, items):
