@@ -52,6 +52,11 @@ def parse():
     ap.add_argument("--tol", type=float, default=1e-10)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--split", action="store_true",
+                    help="mixed solve: FP32 vectors in the assembled-boundary layout "
+                         "(NEKGPU_OPT_SPLIT 1) instead of element-local ones")
+    ap.add_argument("--no-df", action="store_true",
+                    help="skip the FP64 solve with the double-float operator")
     ap.add_argument("--no-parity", action="store_true",
                     help="skip the oracle's full solve (the FP64 and mixed solutions' error "
                          "against the CPU restatement of the reference at the bench's size)")
@@ -74,6 +79,9 @@ def parse():
                          "ingest: .re2 mesh ingestion on the host; "
                          "pressure: the pressure solve's GMRES")
     ap.add_argument("--batch-problems", type=int, default=61)
+    ap.add_argument("--persistent-batch", action="store_true",
+                    help="batch: one persistent cooperative launch per segment instead of "
+                         "three graph-replayed launches per iteration")
     ap.add_argument("--fp64-shape", default=None,
                     help="pin the FP64 operator launch shape 'kind,epb' instead of autotuning")
     ap.add_argument("--gs-shape", default=None,
@@ -297,7 +305,16 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def oracle_parity(M, x64, xmx, it64, tol, nthreads):
+def boundary_nodes(glo_num, lx1):
+    """Global nodes on element boundaries: the distinct ids of the
+    element-boundary points (the boundary groups of the gather-scatter)."""
+    g = np.asarray(glo_num).reshape(-1, lx1, lx1, lx1)
+    inner = np.zeros((lx1, lx1, lx1), dtype=bool)
+    inner[1:-1, 1:-1, 1:-1] = True
+    return int(np.unique(g[:, ~inner]).size)
+
+
+def oracle_parity(M, x64, xmx, it64, tol, nthreads, xdf=None):
     """The oracle's own FP64 Jacobi-PCG on the same full problem, to the same
     relative tolerance: its iteration count and the relative 2-norm error of
     the GPU's FP64 and mixed solutions against its solution.  The oracle sums
@@ -313,6 +330,8 @@ def oracle_parity(M, x64, xmx, it64, tol, nthreads):
     return {"oracle_iterations": int(it), "fp64_iterations": int(it64),
             "rel_error_fp64_vs_oracle": float(np.linalg.norm(x64 - xr)) / nr,
             "rel_error_mixed_vs_oracle": float(np.linalg.norm(xmx - xr)) / nr,
+            "rel_error_fp64_df_vs_oracle": (None if xdf is None
+                                            else float(np.linalg.norm(xdf - xr)) / nr),
             "oracle_rbn2_over_rbn0": r2 / r0 if r0 else None,
             "oracle_threads": nthreads, "oracle_seconds": dt,
             "note": "oracle = C restatement of cggo (core/hmholtz.f:611-846), FP64, "
@@ -337,6 +356,7 @@ def run_gpu(args):
     big = 10 ** 6
     lib.set_option(2, 1)  # timing: solve-total and per-launch operator events
     lib.set_option(7, args.mixed_mode)
+    lib.set_option(9, 1 if args.split else 0)
     for prec, spec in ((0, args.fp64_shape), (1, args.fp32_shape)):
         if spec:
             kind, epb = (int(v) for v in spec.split(","))
@@ -405,6 +425,27 @@ def run_gpu(args):
         "per_iteration_ms": r64.get("per_iter_ms"),
         "gpu_launches": r64["launches"], "clocks": r64["clocks"]}
     x64 = x.clone() if not args.only_mixed else None
+    # the same FP64 solve with the double-float operator (NEKGPU_OPT_DF)
+    df_block = None
+    if not args.only_mixed and not args.no_df:
+        lib.set_option(10, 1)
+        rdf = timed(fp64)
+        lib.set_option(10, 0)
+        vdf = allsum(pg, n * sum(rdf["iters"])) / rdf["T"]
+        df_block = {
+            "value": vdf, "unit": "DOF-iters/s", "iterations": rdf["iters"],
+            "ms_per_solve": 1e3 * rdf["T"] / args.steps,
+            "axhelm": {"kernel": f"axhelm_df_kernel<{M['lx1']},fused> (double-float contractions "
+                                 "on the FP32 pipe, FP64 in/out)",
+                       "avg_launch_ms": rdf["ms_ax"],
+                       "GB/s": b64 * n / (rdf["ms_ax"] * 1e-3) / 1e9, "bytes_per_point": b64,
+                       "frac_of_hbm_peak": b64 * n / (rdf["ms_ax"] * 1e-3) / 1e9 / peak,
+                       "speedup_vs_fp64_operator": r64["ms_ax"] / rdf["ms_ax"]},
+            "per_iteration_ms": rdf.get("per_iter_ms"),
+            "rel_error_vs_fp64_operator_solution":
+                float(torch.linalg.norm(x - x64) / torch.linalg.norm(x64)),
+            "gpu_launches": rdf["launches"], "clocks": rdf["clocks"]}
+        x_df = x.clone()
     rmx = timed(mixed)
     err64 = (float(torch.linalg.norm(x - x64) / torch.linalg.norm(x64))
              if x64 is not None else None)
@@ -412,9 +453,24 @@ def run_gpu(args):
     inner = [i for o, i in rmx["iters"]]
     # time to solution, counted with the FP64 solve's iteration count
     vmx = allsum(pg, n * (it64 or sum(inner) // len(inner)) * args.steps) / rmx["T"]
-    b32 = 4 * 12
+    # The FP32 operator of the inner solve.  Element-local form: r, d, p_old,
+    # G1..G6, bm1 in, p and w out (12 words per point).  Assembled-boundary
+    # form (even lx1, mixed mode 1): G1..G6 and bm1 per point, r, d, p_old once
+    # per global node (interior per element, boundary per node), the 4-byte
+    # group index of every element-boundary point, w out once per point.
+    lx1 = M["lx1"]
+    split = (args.split and args.mixed_mode == 1 and lx1 % 2 == 0 and lx1 >= 4)
+    if split:
+        ni = (lx1 - 2) ** 3
+        nb_nodes = boundary_nodes(M["glo_num"], lx1)
+        b32 = (4 * (6 + (1 if M["h2"][0] != 0 else 0) + 1)
+               + 12.0 * (ni * M["nel"] + nb_nodes) / n + 4.0 * (lx1 ** 3 - ni) / lx1 ** 3)
+        kname = f"split_ax_kernel<{lx1},1> (fp32 operator, assembled-boundary layout)"
+    else:
+        b32 = 4 * 12
+        kname = f"fused fp32 operator lx1={lx1} (inner solve)"
     ax_gbs = b32 * n / (rmx["ms_ax"] * 1e-3) / 1e9
-    ns32 = ncu_summary("axhelm_fused_f32_n7")
+    ns32 = ncu_summary("split_ax_f32_n7" if split else "axhelm_fused_f32_n7")
     line = {"metric": METRIC, "value": vmx, "unit": "DOF-iters/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * rmx["T"] / args.steps, "higher_is_better": True,
@@ -435,8 +491,9 @@ def run_gpu(args):
                                                   "autotuned on the first solve"},
                        "l2": "inputs larger than L2", "parallelism": f"replicas{ws}"},
             "fp64": fp64_block,
+            "fp64_df": df_block,
             "speedup_mixed_vs_fp64": vmx / v64 if v64 > 0 else None,
-            "roofline": {"kernel": f"fused fp32 operator lx1={M['lx1']} (inner solve)",
+            "roofline": {"kernel": kname,
                          "bound": "hbm",
                          "achieved": ax_gbs, "peak": peak, "unit": "GB/s", "frac": ax_gbs / peak,
                          "peak_source": peak_src, "bytes_per_point": b32,
@@ -495,7 +552,8 @@ def run_gpu(args):
     # ---- parity against the oracle at this size (outside every timed region) ----
     if rank == 0 and ws == 1 and not args.no_parity and x64 is not None:
         line["parity"] = oracle_parity(M, x64.cpu().numpy(), x.cpu().numpy(), it64,
-                                       args.tol, os.cpu_count() or 1)
+                                       args.tol, os.cpu_count() or 1,
+                                       None if df_block is None else x_df.cpu().numpy())
     if rank == 0:
         print(json.dumps(line), flush=True)
     lib.close()
@@ -540,6 +598,7 @@ def run_batch(args):
     nb.build()
     probs = batch_workload(args.batch_problems)
     B = NekGpuBatch(local)
+    B.set_persistent(args.persistent_batch)
     for M in probs:
         B.add(M["lx1"], M["nel"], M["D"], M["g"], M["bm1"], M["glo_num"])
         M.pop("g")
@@ -592,7 +651,12 @@ def run_batch(args):
                                  ("fp64 residual replacement, search direction kept"
                                   if args.mixed_mode == 1 else "restarted per outer step"),
                        "operator_block_threads": {"fp64": B.shape(0)[0], "fp32": B.shape(1)[0],
-                                                  "note": "autotuned on the first solve"},
+                                                  "note": "autotuned on the first solve "
+                                                          "(graph form); 256 in the "
+                                                          "persistent form"},
+                       "launch_form": ("one persistent cooperative launch per segment"
+                                       if args.persistent_batch else
+                                       "three launches per iteration, graph-replayed"),
                        "parallelism": f"replicas{ws}"},
             "fp64": {"value": v64, "unit": "DOF-iters/s",
                      "ms_per_step": 1e3 * out[False]["T"] / args.steps},

@@ -70,6 +70,27 @@ extern "C" {
                                 a precision, time the operator's launch shapes
                                 and keep the fastest (nekgpu_autotune); 0: the
                                 built-in shapes.  Setting it forgets the picks. */
+#define NEKGPU_OPT_SPLIT 9    /* mixed solve, residual-replacement mode: 1
+                                keep the FP32 inner PCG's vectors once per
+                                global node on element boundaries and once per
+                                element inside (two kernels per iteration; even
+                                lx1 >= 4 with the TMA operator); 0 (default)
+                                the element-local form of the FP64 solver    */
+#define NEKGPU_OPT_DF 10     /* 1: the FP64 operator (fused multiply-add form)
+                                forms its tensor contractions in double-float
+                                arithmetic -- pairs of FP32 values, 48
+                                significant bits, compensated products and
+                                sums -- on the FP32 pipe; FP64 in and out, the
+                                mass term and the PCG's vector algebra in FP64.
+                                0 (default): FP64 contractions            */
+#define NEKGPU_OPT_FACE_ORDER 11  /* mixed solve, residual-replacement mode: 1
+                                store each element's points of the FP32 inner
+                                vectors face by face (face interiors, edges,
+                                vertices, then the element interior), so that
+                                the direct-stiffness sum reads and writes whole
+                                memory sectors; 0 (default) the reference's
+                                x-fastest order.  Results agree to FP32
+                                rounding.                                    */
 #define NEKGPU_OPT_MIXED_MODE 7  /* mixed solve: 1 (default) one FP32 PCG whose
                                 residual is replaced by the FP64 one each time
                                 it drops by inner_tol, search direction kept;
@@ -499,6 +520,17 @@ int nekgpu_batch_solve_dev(const int64_t *batch, const int *nprob, double *const
  * reference counterpart.  A 128-thread block is a candidate only when every
  * problem's lx1^2 <= 128. */
 int nekgpu_batch_shape(const int64_t *batch, const int *precision, int *threads, double *ms);
+/* *on = 1: each batch segment -- the iterations until every
+ * problem has stopped, or until every problem's FP32 residual has dropped by
+ * inner_tol in the mixed form -- is one persistent cooperative launch whose
+ * resident blocks run the operator, boundary-group and update phases of all
+ * problems with grid-wide barriers between them (bounded waits: a barrier
+ * that does not complete within seconds fails the solve with NEKGPU_ECUDA
+ * and leaves the GPU usable).  Its block size is 256 threads.  *on = 0
+ * (default): three launches per iteration, replayed as a captured CUDA
+ * graph, with the operator block size tuned as nekgpu_batch_shape says.  Both
+ * forms give identical results.  No reference counterpart. */
+int nekgpu_batch_set_persistent(const int64_t *batch, const int *on);
 int nekgpu_batch_set_shape(const int64_t *batch, const int *precision, const int *threads);
 int nekgpu_batch_last_error(const int64_t *batch, char *buf, const int *buflen);
 int nekgpu_batch_destroy(int64_t *batch);

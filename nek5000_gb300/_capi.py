@@ -18,6 +18,9 @@ EINVAL, EHANDLE, ECUDA, ENOMEM, ENOTCONV, ENOSETUP, ENAN, EIO = -1, -2, -3, -4, 
 OPT_EXACT, OPT_TIMING, OPT_CHUNK, OPT_ISTEP, OPT_TMA, OPT_GRAPH, OPT_MIXED_MODE = (
     1, 2, 3, 4, 5, 6, 7)
 OPT_AUTOTUNE = 8
+OPT_SPLIT = 9
+OPT_DF = 10
+OPT_FACE_ORDER = 11
 MAX_LX1 = 12
 NOALLOC_MAX_POINTS = 4194304
 PROJ_SPACES, PROJ_MAX, PROJ_DEFAULT = 16, 16, 8
@@ -132,6 +135,7 @@ SIGNATURES = {
                                     _DP, _IP, _IP, _DP, _DP, _IP],
     "nekgpu_proj_count": [_I64P, _IP, _IP],
     "nekgpu_batch_set_shape": [_I64P, _IP, _IP],
+    "nekgpu_batch_set_persistent": [_I64P, _IP],
     "nekgpu_ax_shape": [_I64P, _IP, _IP, _IP, _DP],
     "nekgpu_gs_shape": [_I64P, _IP, _IP, _IP, _DP],
     "nekgpu_set_gs_shape": [_I64P, _IP, _IP],

@@ -61,6 +61,10 @@ struct AxArgs {
   // fields of a multi-field solve): staged with the default L2 policy so that
   // the later reads hit L2; 0: every input is read once (evict first).
   int shared_in;
+  // Fused form: the PCG vectors (r, d, p, w) store each element's points in
+  // the face order of perm.cu; perm[pt] is the position of natural point pt
+  // (G, bm1, h1, h2 stay natural).  nullptr: natural order.
+  const int* perm;
 };
 
 template <int NX>
@@ -205,10 +209,11 @@ __device__ __forceinline__ void axhelm_body(const AxArgs<T>& a, int blk, int tx,
     T v = T(0);
     if (act) {
       if constexpr (FUSED) {
-        T z = EXACT ? mul_x(a.r[eo + pt], a.d[eo + pt]) : a.r[eo + pt] * a.d[eo + pt];
+        const int q = a.perm ? __ldg(a.perm + pt) : pt;  // position in the vectors
+        T z = EXACT ? mul_x(a.r[eo + q], a.d[eo + q]) : a.r[eo + q] * a.d[eo + q];
         if (mcor) z = EXACT ? add_x(z, zmean) : z + zmean;  // cadd(z,rmean) (hmholtz.f:749)
-        v = madd<EXACT>(beta, a.u[eo + pt], z);  // add2s1: p = beta*p + z
-        a.p[eo + pt] = v;
+        v = madd<EXACT>(beta, a.u[eo + q], z);  // add2s1: p = beta*p + z
+        a.p[eo + q] = v;
       } else {
         v = a.u[eo + pt];
       }
@@ -324,8 +329,12 @@ __device__ __forceinline__ void axhelm_body(const AxArgs<T>& a, int blk, int tx,
         }
         s = EXACT ? add_x(s, mul_x(hb, ru[k])) : fma(hb, ru[k], s);
       }
-      if constexpr (FUSED && sizeof(T) == 4) st_hint(a.au + eo + pt, s, l2_policy_evict_last());
-      else a.au[eo + pt] = s;
+      if constexpr (FUSED && sizeof(T) == 4) {
+        const int q = a.perm ? __ldg(a.perm + pt) : pt;
+        st_hint(a.au + eo + q, s, l2_policy_evict_last());
+      } else {
+        a.au[eo + pt] = s;
+      }
       if constexpr (FUSED) {
         if (a.allrho || (i > 0 && i < NX - 1 && j > 0 && j < NX - 1 && k > 0 && k < NX - 1 &&
                          (!a.skip || !a.skip[eo + pt])))

@@ -69,6 +69,10 @@ static cudaError_t launch_ax(const Mesh& m, const AxArgs<T>& a, int* nparts, cud
       return launch_tma_f32(m, a, FUSED, sh.epb, nparts, s);
   }
   const int epb = sh.kind == 0 ? sh.epb : axhelm_epb(m.nx1);
+  if constexpr (!EXACT && sizeof(T) == 8) {
+    // NEKGPU_OPT_DF: contractions in double-float arithmetic on the FP32 pipe
+    if (m.use_df && m.has_df) return launch_axhelm_df(m, a, FUSED, epb, nparts, s);
+  }
   switch (m.nx1) {
     case 2: return launch_ax_nx<2, T, EXACT, FUSED>(m, a, epb, nparts, s);
     case 3: return launch_ax_nx<3, T, EXACT, FUSED>(m, a, epb, nparts, s);
@@ -104,6 +108,7 @@ static AxArgs<T> make_args(const Mesh& m, const OpData<T>& op, T* au, const T* u
   a.nel = m.nel;
   a.err = m.dev_err;
   a.skip = m.gs.skip;
+  a.perm = c.perm;
   return a;
 }
 

@@ -153,18 +153,42 @@ __device__ __forceinline__ void axhelm_tma_body(const AxArgs<T>& a, int blk,
   T beta = T(0);
   if constexpr (FUSED) beta = (T)a.cg->beta;
   T ru[NX];
+  int qp[NX];  // positions of the column's points in the vectors (face order or natural)
 #pragma unroll
   for (int k = 0; k < NX; ++k) {
     const int pt = k * NXY + j * NX + i;
-    T v = act ? sU[lo + pt] : T(0);
-    if constexpr (FUSED) {
+    qp[k] = (FUSED && a.perm) ? __ldg(a.perm + pt) : pt;
+  }
+  if (FUSED && a.perm) {
+    // face-ordered vectors: p at each position, then the slabs in natural order
+#pragma unroll
+    for (int k = 0; k < NX; ++k) {
+      const int q = qp[k];
+      T v = T(0);
       if (act) {
-        v = fma(beta, v, sR[lo + pt] * sDg[lo + pt]);  // add2s1: p = beta*p + r*d
-        sU[lo + pt] = v;
-        a.p[eo + pt] = v;
+        v = fma(beta, sU[lo + q], sR[lo + q] * sDg[lo + q]);  // add2s1: p = beta*p + r*d
+        a.p[eo + q] = v;
       }
+      ru[k] = v;
     }
-    ru[k] = v;
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < NX; ++k)
+      if (el < EPB) sU[lo + k * NXY + j * NX + i] = ru[k];
+  } else {
+#pragma unroll
+    for (int k = 0; k < NX; ++k) {
+      const int pt = k * NXY + j * NX + i;
+      T v = act ? sU[lo + pt] : T(0);
+      if constexpr (FUSED) {
+        if (act) {
+          v = fma(beta, v, sR[lo + pt] * sDg[lo + pt]);  // add2s1: p = beta*p + r*d
+          sU[lo + pt] = v;
+          a.p[eo + pt] = v;
+        }
+      }
+      ru[k] = v;
+    }
   }
   __syncthreads();
 
@@ -227,7 +251,7 @@ __device__ __forceinline__ void axhelm_tma_body(const AxArgs<T>& a, int blk,
         const T hv = hh2 ? sH2[lo + pt] : a.h2s;
         s = fma(hv * sB[lo + pt], ru[k], s);
       }
-      if constexpr (FUSED && sizeof(T) == 4) st_hint(a.au + eo + pt, s, keep);
+      if constexpr (FUSED && sizeof(T) == 4) st_hint(a.au + eo + qp[k], s, keep);
       else a.au[eo + pt] = s;
       if constexpr (FUSED) {
         if (a.allrho || (i > 0 && i < NX - 1 && j > 0 && j < NX - 1 && k > 0 && k < NX - 1 &&

@@ -120,6 +120,119 @@ __global__ void __launch_bounds__(kBatchThreads)
                                                  d->partialC, blk, d->nblkC, red, &am_last);
 }
 
+// ---- the persistent form: one cooperative launch runs whole iterations ----
+//
+// Every block of the launch stays resident (cudaLaunchCooperativeKernel
+// checks that they all fit at once) and walks the virtual blocks of the three
+// phases of an iteration -- the operator blocks of every problem, their
+// boundary-group blocks, their update blocks, with the same tables as the
+// three-launch form -- separated by grid-wide barriers.  It keeps iterating
+// until every problem has stopped or `kmax` iterations have run.  The
+// barrier is a counter and a generation word in global memory; its wait is
+// bounded (kBarrierLimit polls with a short sleep, seconds in all), after
+// which the block raises bit 2 of *err and every block leaves at the next
+// barrier, so that a lost block can never hold the GPU.
+constexpr unsigned int kBarrierLimit = 1u << 24;
+
+__device__ __forceinline__ bool grid_barrier(unsigned int* bar, unsigned int nblocks, int* err) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned int* gen = bar + 1;
+    const unsigned int g = *gen;
+    __threadfence();
+    const unsigned int t = atomicAdd(bar, 1u);
+    if (t == nblocks - 1) {
+      atomicExch(bar, 0u);
+      __threadfence();
+      atomicAdd(bar + 1, 1u);
+    } else {
+      unsigned int it = 0;
+      while (*gen == g) {
+        if (++it > kBarrierLimit) {
+          atomicOr(err, 2);
+          break;
+        }
+        __nanosleep(100);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return *reinterpret_cast<volatile int*>(err) == 0;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kBatchThreads, 2)
+    batch_persistent_kernel(const BDesc<T>* __restrict__ D, int np, const int* __restrict__ mapA,
+                            const int* __restrict__ baseA, int gridA, const int* __restrict__ mapB,
+                            const int* __restrict__ baseB, int gridB,
+                            const int* __restrict__ mapC, const int* __restrict__ baseC,
+                            int gridC, int kmax, unsigned int* bar, int* err) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ double red[32];
+  __shared__ int am_last;
+  __shared__ int all_done;
+  const unsigned int nb = gridDim.x;
+  for (int it = 0; it < kmax; ++it) {
+    for (int v = blockIdx.x; v < gridA; v += nb) {  // the operator
+      const int pi = mapA[v];
+      const BDesc<T>* d = D + pi;
+      if (d->cg->done) continue;
+      const AxArgs<T> a = d->ax;
+      const int blk = v - baseA[pi], epb = d->epb;
+      switch (d->nx1) {
+        case 2: batch_ax_nx<T, 2>(a, blk, epb, smem, red); break;
+        case 3: batch_ax_nx<T, 3>(a, blk, epb, smem, red); break;
+        case 4: batch_ax_nx<T, 4>(a, blk, epb, smem, red); break;
+        case 5: batch_ax_nx<T, 5>(a, blk, epb, smem, red); break;
+        case 6: batch_ax_nx<T, 6>(a, blk, epb, smem, red); break;
+        case 7: batch_ax_nx<T, 7>(a, blk, epb, smem, red); break;
+        case 8: batch_ax_nx<T, 8>(a, blk, epb, smem, red); break;
+        case 9: batch_ax_nx<T, 9>(a, blk, epb, smem, red); break;
+        case 10: batch_ax_nx<T, 10>(a, blk, epb, smem, red); break;
+        case 11: batch_ax_nx<T, 11>(a, blk, epb, smem, red); break;
+        default: batch_ax_nx<T, 12>(a, blk, epb, smem, red); break;
+      }
+      __syncthreads();  // the next virtual block reuses the shared memory
+    }
+    if (!grid_barrier(bar, nb, err)) return;
+    for (int v = blockIdx.x; v < gridB; v += nb) {  // the boundary groups
+      const int pi = mapB[v];
+      const BDesc<T>* d = D + pi;
+      if (d->cg->done) continue;
+      gs_cg_body<T>(d->ax.au, d->ax.p, d->bstart, d->bidx, d->cls, d->segmask, d->segmsum, d->cg,
+                    d->ax.partial, d->ax.nel, d->partialB, v - baseB[pi], d->nblkB, red,
+                    &am_last);
+      __syncthreads();
+    }
+    if (!grid_barrier(bar, nb, err)) return;
+    for (int v = blockIdx.x; v < gridC; v += nb) {  // the update
+      const int pi = mapC[v];
+      const BDesc<T>* d = D + pi;
+      if (d->cg->done) continue;
+      const int blk = v - baseC[pi];
+      if (d->vec)
+        cg_update_body<T, false, false, true, true>(d->x, const_cast<T*>(d->ax.r), d->ax.p,
+                                                    d->ax.au, d->md, d->mult, d->mb, d->n, d->cg,
+                                                    d->partialC, blk, d->nblkC, red, &am_last);
+      else
+        cg_update_body<T, false, false, false, true>(d->x, const_cast<T*>(d->ax.r), d->ax.p,
+                                                     d->ax.au, d->md, d->mult, d->mb, d->n,
+                                                     d->cg, d->partialC, blk, d->nblkC, red,
+                                                     &am_last);
+      __syncthreads();
+    }
+    if (!grid_barrier(bar, nb, err)) return;
+    if (threadIdx.x == 0) {  // every problem stopped: leave (the same answer in every block)
+      int all = 1;
+      for (int q = 0; q < np; ++q) all &= (*reinterpret_cast<volatile int*>(&D[q].cg->done) != 0);
+      all_done = all;
+    }
+    __syncthreads();
+    if (all_done) return;
+  }
+}
+
 // Shared memory of one operator block: epb elements of lx1 = nx.
 template <typename T>
 size_t batch_smem(int nx, int epb) {
@@ -166,6 +279,14 @@ struct Batch {
   std::vector<int64_t> gkey;
   int chunk = 16;
   bool use_graph = true;
+  // one cooperative launch per batch segment (batch_persistent_kernel)
+  // instead of three graph-replayed launches per iteration.  Off by default:
+  // on GB300 the fused kernel holds every phase's registers (one or two
+  // blocks per SM), and its memory-bound phases run slower than the separate
+  // launches (nekgpu_batch_set_persistent)
+  bool persistent = false;
+  DevBuf<unsigned int> bar;  // the persistent launch's barrier words
+  DevBuf<int> perr;          // and its error flag
   // operator block size per precision ([0] FP64, [1] FP32): picked by
   // batch_tune for the problem set in tkey, or pinned (pinned[prec] != 0)
   int threads[2] = {0, 0};
@@ -327,6 +448,10 @@ int batch_tune(Batch& B, const std::vector<int>& ids, const std::vector<Coef<T>>
     B.threads[prec] = B.pinned[prec];
     return 0;
   }
+  if (B.persistent) {  // the persistent launch runs every phase with 256 threads
+    B.threads[prec] = kBatchThreads;
+    return 0;
+  }
   std::vector<int64_t> key;
   int maxnxy = 0;
   for (size_t q = 0; q < ids.size(); ++q) {
@@ -389,6 +514,77 @@ int batch_tune(Batch& B, const std::vector<int>& ids, const std::vector<Coef<T>>
   return 0;
 }
 
+// The persistent form of batch_iterate's loop (after the iteration-1
+// check): cooperative launches of batch_persistent_kernel until every problem
+// has stopped.  Returns 0, a negative status, or 1 when the device cannot
+// take the cooperative launch (then the three-launch form runs).
+template <typename T>
+int batch_iterate_persistent(Batch& B, const std::vector<int>& ids, const BatchLaunch& L) {
+  const int np = (int)ids.size();
+  static bool configured = false;
+  if (!configured) {
+    if (cudaFuncSetAttribute(batch_persistent_kernel<T>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)batch_smem_max<T>()) != cudaSuccess)
+      return 1;
+    configured = true;
+  }
+  int dev = 0, coop = 0, nsm = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  if (!coop ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_persistent_kernel<T>,
+                                                    kBatchThreads, L.smem) != cudaSuccess ||
+      per_sm < 1) {
+    cudaGetLastError();
+    return 1;
+  }
+  const int grid = std::min(per_sm * nsm, std::max({L.gridA, L.gridB, L.gridC, 1}));
+  if (B.bar.ensure(2) || B.perr.ensure(1)) return -4;
+  const BDesc<T>* D = reinterpret_cast<const BDesc<T>*>(L.desc);
+  int gA = L.gridA, gB = L.gridB, gC = L.gridC, kmax = 1 << 30, npp = np;
+  unsigned int* bar = B.bar.ptr;
+  int* perr = B.perr.ptr;
+  const int *mA = L.mapA, *bA = L.baseA, *mB = L.mapB, *bB = L.baseB, *mC = L.mapC,
+            *bC = L.baseC;
+  void* args[] = {(void*)&D, &npp, (void*)&mA, (void*)&bA, &gA, (void*)&mB, (void*)&bB, &gB,
+                  (void*)&mC, (void*)&bC, &gC, &kmax, (void*)&bar, (void*)&perr};
+  for (;;) {
+    for (int q = 0; q < np; ++q)
+      cudaMemcpyAsync(&B.cg_host_all[q], B.probs[ids[q]]->cg, sizeof(CgScalars),
+                      cudaMemcpyDeviceToHost, B.stream);
+    if (cudaStreamSynchronize(B.stream) != cudaSuccess) {
+      B.err = std::string("batch: ") + cudaGetErrorString(cudaGetLastError());
+      return -3;
+    }
+    bool all = true;
+    for (int q = 0; q < np; ++q) all = all && B.cg_host_all[q].done;
+    if (all) break;
+    cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned int), B.stream);
+    cudaMemsetAsync(perr, 0, sizeof(int), B.stream);
+    count_launch();
+    cudaError_t e = cudaLaunchCooperativeKernel((const void*)batch_persistent_kernel<T>, grid,
+                                                kBatchThreads, args, L.smem, B.stream);
+    if (e != cudaSuccess) {
+      B.err = std::string("batch persistent launch: ") + cudaGetErrorString(e);
+      return -3;
+    }
+    int herr = 0;
+    cudaMemcpyAsync(&herr, perr, sizeof(int), cudaMemcpyDeviceToHost, B.stream);
+    if (cudaStreamSynchronize(B.stream) != cudaSuccess) {
+      B.err = std::string("batch: ") + cudaGetErrorString(cudaGetLastError());
+      return -3;
+    }
+    if (herr) {
+      B.err = "batch persistent launch: a grid barrier wait expired";
+      return -3;
+    }
+  }
+  for (int q = 0; q < np; ++q) *B.probs[ids[q]]->cg_host = B.cg_host_all[q];
+  return 0;
+}
+
 // first: run the iteration-1 check of freshly prepared problems first (not
 // after a residual replacement, which sets the scalars itself).
 template <typename T>
@@ -398,6 +594,15 @@ int batch_iterate(Batch& B, const std::vector<int>& ids, const BatchLaunch& L, b
   if (first) {
     count_launch();
     batch_update_kernel<T, true><<<L.gridC, kBatchThreads, 0, B.stream>>>(D, L.mapC, L.baseC);
+  }
+  if (B.cg_host_cap < (size_t)np) {
+    cudaFreeHost(B.cg_host_all);
+    if (cudaMallocHost(&B.cg_host_all, sizeof(CgScalars) * np) != cudaSuccess) return -4;
+    B.cg_host_cap = np;
+  }
+  if (B.persistent && L.threadsA == kBatchThreads) {
+    const int rc = batch_iterate_persistent<T>(B, ids, L);
+    if (rc != 1) return rc;  // 1: cooperative launch unavailable, the launches below run
   }
   bool graph = B.use_graph;
   std::vector<int64_t> key = {(int64_t)sizeof(T), L.gridA, L.gridB, L.gridC, (int64_t)L.smem,
@@ -422,11 +627,6 @@ int batch_iterate(Batch& B, const std::vector<int>& ids, const BatchLaunch& L, b
     } else {
       B.gkey = key;
     }
-  }
-  if (B.cg_host_cap < (size_t)np) {
-    cudaFreeHost(B.cg_host_all);
-    if (cudaMallocHost(&B.cg_host_all, sizeof(CgScalars) * np) != cudaSuccess) return -4;
-    B.cg_host_cap = np;
   }
   for (;;) {
     for (int q = 0; q < np; ++q)
@@ -920,6 +1120,14 @@ int nekgpu_batch_set_shape(const int64_t* batch, const int* precision, const int
   B->pinned[*precision] = *threads;
   B->threads[*precision] = 0;
   B->tkey[*precision].clear();
+  return NEKGPU_OK;
+}
+
+int nekgpu_batch_set_persistent(const int64_t* batch, const int* on) {
+  Batch* B = bget(batch);
+  if (!B) return bfail(nullptr, NEKGPU_EHANDLE, "unknown batch");
+  if (!on) return bfail(B, NEKGPU_EINVAL, "null argument");
+  B->persistent = (*on != 0);
   return NEKGPU_OK;
 }
 

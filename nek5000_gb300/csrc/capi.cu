@@ -247,6 +247,8 @@ void handle_close(Handle& H) {
   cudaSetDevice(H.device);
   if (H.stream) cudaStreamSynchronize(H.stream);
   H.mg.reset();
+  H.split.reset();
+  H.perm.reset();
   H.iface.reset();
   H.dealias.reset();
   gs_free(H.mesh.gs);
@@ -285,11 +287,14 @@ static int mesh_prepare(Handle& H, int lx1, int nel, const double* dxm1, std::st
     return NEKGPU_EINVAL;
   }
   cudaStreamSynchronize(H.stream);
+  H.split.reset();  // maps of the old mesh
+  H.perm.reset();
   Mesh& m = H.mesh;
   gs_free(m.gs);
   m.f64.release();
   m.f32.release();
   m.has_f32 = false;
+  m.has_df = false;
   m.ax_sel[0] = m.ax_sel[1] = AxShapeSel();
   m.has_rst = false;  // metric terms only come with coordinates (geom.cu)
   H.proj.clear();  // projection spaces belong to the old mesh
@@ -337,6 +342,10 @@ static int mesh_finish(Handle& H, const int64_t* glo_num, std::string& err) {
     return NEKGPU_ECUDA;
   }
   H.has_mesh = true;
+  if (m.use_df && build_df(H)) {
+    err = "setup: double-float geometric factors failed";
+    return NEKGPU_ECUDA;
+  }
   return 0;
 }
 
@@ -471,6 +480,17 @@ int nekgpu_set_option(const int64_t* handle, const int* key, const int* value) {
       H->mesh.gs_ms[0] = H->mesh.gs_ms[1] = 0.f;
       break;
     case NEKGPU_OPT_GRAPH: H->use_graph = (*value != 0); break;
+    case NEKGPU_OPT_SPLIT: H->use_split = (*value != 0); break;
+    case NEKGPU_OPT_FACE_ORDER: H->use_perm = (*value != 0); break;
+    case NEKGPU_OPT_DF:
+      H->mesh.use_df = (*value != 0);
+      if (H->mesh.use_df && H->has_mesh && !H->mesh.has_df && build_df(*H))
+        return fail(H, NEKGPU_ECUDA, "double-float geometric factors failed");
+      if (H->gexec) {  // captured FP64 iterations launch the other kernel now
+        cudaGraphExecDestroy(H->gexec);
+        H->gexec = nullptr;
+      }
+      break;
     case NEKGPU_OPT_MIXED_MODE:
       if (*value != 0 && *value != 1) return fail(H, NEKGPU_EINVAL, "mixed mode must be 0 or 1");
       H->mixed_mode = *value;
@@ -513,6 +533,7 @@ int nekgpu_geom_update_dev(const int64_t* handle, const double* wxm1, const doub
   std::string err;
   const int rc = geom_from_xyz(*H, xm1, ym1, zm1, wxm1, err);
   if (rc) return fail(H, rc, err);
+  if (H->mesh.use_df && build_df(*H)) return fail(H, NEKGPU_ECUDA, "double-float geometric factors failed");
   return NEKGPU_OK;
 }
 

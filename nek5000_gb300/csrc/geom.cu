@@ -181,6 +181,7 @@ int geom_from_xyz(Handle& H, const double* x, const double* y, const double* z, 
   // the FP32 copy of the operator data no longer matches
   m.f32.release();
   m.has_f32 = false;
+  m.has_df = false;
   return NEKGPU_OK;
 }
 

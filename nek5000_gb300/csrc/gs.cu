@@ -52,7 +52,8 @@ __global__ void gs_cg_weights_kernel(const int* __restrict__ start, const int* _
 
 }  // namespace
 
-int gs_setup(GsMaps& gs, const int64_t* glo_num, int64_t n, int nx1, std::string& err) {
+int gs_setup(GsMaps& gs, const int64_t* glo_num, int64_t n, int nx1, std::string& err,
+             const int* pos_pt) {
   gs_free(gs);
   if (n < 0 || n >= (int64_t)INT32_MAX) {
     err = "gs_setup: more than 2^31-1 local points";
@@ -93,7 +94,8 @@ int gs_setup(GsMaps& gs, const int64_t* glo_num, int64_t n, int nx1, std::string
   bix.reserve(pr.size());
   const int P = nx1 * nx1 * nx1;
   auto interior = [&](int64_t i) {
-    const int p = (int)(i % P), x = p % nx1, y = (p / nx1) % nx1, z = p / (nx1 * nx1);
+    const int q = (int)(i % P), p = pos_pt ? pos_pt[q] : q;
+    const int x = p % nx1, y = (p / nx1) % nx1, z = p / (nx1 * nx1);
     return x > 0 && x < nx1 - 1 && y > 0 && y < nx1 - 1 && z > 0 && z < nx1 - 1;
   };
   std::vector<unsigned char> skip;

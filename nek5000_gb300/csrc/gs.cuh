@@ -54,7 +54,12 @@ struct GsMaps {
 // Host: build maps from glo_num (sort by (id, local index)).  nx1 classifies
 // element-interior points: element-boundary points with id 0 join the PCG-form
 // maps as singletons (so that masks reach them).  Returns 0 or an error code.
-int gs_setup(GsMaps& gs, const int64_t* glo_num, int64_t n, int nx1, std::string& err);
+// pos_pt (optional, nx1^3 entries): the natural point (x fastest) held at
+// each position of an element when the vectors these maps serve store an
+// element's points in another order (the FP32 inner PCG's face-ordered
+// layout); nullptr: natural order.
+int gs_setup(GsMaps& gs, const int64_t* glo_num, int64_t n, int nx1, std::string& err,
+             const int* pos_pt = nullptr);
 void gs_free(GsMaps& gs);
 
 // u <- gs_op(u, op): op 0 '+', 1 '*', 2 max, 3 min

@@ -79,6 +79,10 @@ struct Mesh {
   // coordinates (geom.cu); the gradient-type operators need them (gradops.cu)
   DevBuf<double> rst, jac, w3, w1;  // w1: the nx1 GLL weights
   bool has_rst = false;
+  // double-float form of the FP64 operator (axhelm_df.cuh): (hi, lo) pairs
+  // of G1..G6 and D, kept while NEKGPU_OPT_DF is on
+  bool use_df = false, has_df = false;
+  DevBuf<float2> Gdf, Ddf;
 };
 
 // Coefficient descriptor after uniformity detection.
@@ -89,6 +93,7 @@ struct Coef {
   const T* h1 = nullptr;
   const T* h2 = nullptr;
   const T* hbm = nullptr;  // h2 * bm1 per point when a solve has formed it (AxArgs::hbm)
+  const int* perm = nullptr;  // FP32 inner PCG in face order: AxArgs::perm
 };
 
 // Work space of one PCG precision.
@@ -127,6 +132,18 @@ struct ShardIfaceDeleter {
 struct Dealias;
 struct DealiasDeleter {
   void operator()(Dealias* p) const;
+};
+
+// The FP32 inner PCG's face-ordered element layout (perm.cu).
+struct PermLayout;
+struct PermLayoutDeleter {
+  void operator()(PermLayout* p) const;
+};
+
+// The FP32 inner PCG's assembled-boundary layout (split.cu).
+struct SplitLayout;
+struct SplitLayoutDeleter {
+  void operator()(SplitLayout* p) const;
 };
 
 // The pressure preconditioner h1mg_solve on the device (h1mg.cu).
@@ -198,7 +215,25 @@ struct Handle {
   // the dealiased convective term once nekgpu_dealias_setup has run
   std::unique_ptr<Dealias, DealiasDeleter> dealias;
   DevBuf<int> p4_fbc;  // crespsp's face types, staged per call
+  // the mixed solve's FP32 inner PCG in the assembled-boundary layout
+  // (split.cu), built on first use per mesh when use_split is on
+  // (NEKGPU_OPT_SPLIT; off by default: slower than the element-local form
+  // on this GPU, see split.cu)
+  std::unique_ptr<SplitLayout, SplitLayoutDeleter> split;
+  bool use_split = false;
+  // the mixed solve's FP32 inner PCG with each element's points in face
+  // order (perm.cu), built on first use per mesh when use_perm is on
+  // (NEKGPU_OPT_FACE_ORDER; off by default, see perm.cu).  gs32: the maps the
+  // FP32 PCG uses while a solve runs in that layout (nullptr: the mesh's own)
+  std::unique_ptr<PermLayout, PermLayoutDeleter> perm;
+  bool use_perm = false;
+  const GsMaps* gs32 = nullptr;
 };
+
+// Double-float FP64 operator (axhelm_df.cu): the mesh's Gdf / Ddf pairs.
+cudaError_t launch_axhelm_df(const Mesh& m, const AxArgs<double>& a, bool fused, int epb,
+                             int* nparts, cudaStream_t s);
+int build_df(Handle& h);
 
 // ---- operator entry points (axhelm_*.cu) ---------------------------------
 // Plain operator: au = A u.  Returns cudaError_t of the launch.
@@ -328,7 +363,8 @@ int proj_project1(Handle& h, ProjSpace& P, double* b, const Coef<double>& c, con
 int proj_project2(Handle& h, ProjSpace& P, double* x, const Coef<double>& c, const double* msk,
                   const double* w);
 // Residual replacement into the running FP32 PCG (see mixed.cu).
-int mixed_replace(Handle& h, double& scale, double inner_tol, int* restarts);
+int mixed_replace(Handle& h, double& scale, double inner_tol, int* restarts,
+                  const int* perm = nullptr);
 // The same for any FP32 PCG: its vectors, the FP64 residual, its scalars.
 struct ReplaceTarget {
   float* r32;
@@ -340,6 +376,7 @@ struct ReplaceTarget {
   const double* r64;
   CgScalars* cg_dev;
   CgScalars* cg_host;
+  const int* perm = nullptr;  // face-ordered FP32 vectors (perm.cu): r32 cast through it
 };
 int mixed_replace_into(Handle& h, const ReplaceTarget& t, double& scale, double inner_tol,
                        int* restarts);
@@ -352,6 +389,28 @@ MixedResult mixed_solve(Handle& h, double* x, const double* f, const double* h1,
                         int mode = 0);
 
 void set_error(Handle& h, const std::string& msg);
+
+// ---- the FP32 inner PCG in the face-ordered element layout (perm.cu) -----
+std::vector<int> face_order(int nx);
+bool perm_eligible(const Handle& h);
+int perm_setup(Handle& h);
+const int* perm_pt_pos(const Handle& h);
+const GsMaps* perm_maps(const Handle& h);
+// o (face-ordered FP32) = scale * a (natural FP64); x (natural) += scale * e32
+void perm_cast(Handle& h, float* o, const double* a, double scale);
+void perm_axpy(Handle& h, double* x, const float* e32, double scale);
+
+// ---- the FP32 inner PCG in the assembled-boundary layout (split.cu) ------
+// Eligible meshes: even lx1 in 4..12, interior points private to their
+// element, the TMA-staged operator on.
+bool split_eligible(const Handle& h);
+int split_setup(Handle& h);
+int split_load(Handle& h, const double* r64, double inv_scale, const double* d64,
+               const double* binv64, const double* mask64);
+int split_first_check(Handle& h, const Coef<float>& c);
+PcgResult split_iterate(Handle& h, const Coef<float>& c);
+void split_axpy(Handle& h, double* x64, double scale);
+int split_replace(Handle& h, const double* r64, double& scale, double inner_tol, int* restarts);
 
 // Handle life cycle and mesh upload (capi.cu); `shared` != nullptr makes the
 // handle use that stream instead of creating one.

@@ -17,6 +17,7 @@
 // plain solve.
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 
 #include "impl.cuh"
 
@@ -194,10 +195,10 @@ double outer_residual(Handle& h, double* r, const double* f, const double* x,
 // counted in *restarts) when the true norm exceeds twice the recurrence norm,
 // i.e. FP32 drift dominates and p no longer fits r.  Returns 0, 1 when r is
 // zero (nothing to iterate on), or a negative status.
-int mixed_replace(Handle& h, double& scale, double inner_tol, int* restarts) {
+int mixed_replace(Handle& h, double& scale, double inner_tol, int* restarts, const int* perm) {
   PcgWork<float>& wk = h.w32;
   ReplaceTarget t{wk.r.ptr, wk.p.ptr, wk.x.ptr, wk.d.ptr, wk.mult.ptr, wk.binv.ptr,
-                  h.w64.r.ptr, h.cg, h.cg_host};
+                  h.w64.r.ptr, h.cg, h.cg_host, perm};
   return mixed_replace_into(h, t, scale, inner_tol, restarts);
 }
 
@@ -213,8 +214,9 @@ int mixed_replace_into(Handle& h, const ReplaceTarget& t, double& scale, double 
   if (amax == 0.0) return 1;
   const double s_new = std::ldexp(1.0, std::ilogb(amax));
   const double ratio = scale / s_new;
-  count_launch(3);
-  cast_scale_kernel<float, double><<<nb, kThreads, 0, s>>>(t.r32, t.r64, 1.0 / s_new, n);
+  count_launch(2);
+  if (t.perm) perm_cast(h, t.r32, t.r64, 1.0 / s_new);
+  else cast_scale_kernel<float, double><<<nb, kThreads, 0, s>>>(t.r32, t.r64, 1.0 / s_new, n);
   scale_kernel<<<nb, kThreads, 0, s>>>(t.p32, (float)ratio, n);
   cudaMemsetAsync(t.x32, 0, n * sizeof(float), s);
   rz_kernel<<<nb, kThreads, 0, s>>>(t.r32, t.d32, t.mult32, t.binv32, n, h.red.ptr);
@@ -243,6 +245,97 @@ int mixed_replace_into(Handle& h, const ReplaceTarget& t, double& scale, double 
   cudaMemcpyAsync(t.cg_dev, &c, sizeof(CgScalars), cudaMemcpyHostToDevice, s);
   scale = s_new;
   return 0;
+}
+
+// Residual-replacement mode with the FP32 inner PCG in the assembled-boundary
+// layout (split.cu): the same outer loop as the element-local form below, on
+// the layout's vectors.  h.w64.r holds r = f on entry, h.w64.d the FP64
+// Jacobi diagonal, h.w32 the FP32 mask and mult.
+MixedResult mixed_split(Handle& h, MixedResult res, double* x, const double* f,
+                        const Coef<double>& c64, const Coef<float>& c32, const double* mask,
+                        const double* mult, const double* binv, double tol, double rbn,
+                        int maxit, double inner_tol, double scale) {
+  Mesh& m = h.mesh;
+  const int64_t n = m.n;
+  cudaStream_t s = h.stream;
+  PcgWork<float>& wk = h.w32;
+  PcgWork<double>& w64 = h.w64;
+  // the element-local solver's checks: one mask value per shared node, mask
+  // and mult 1 inside the elements
+  if (wk.segmask.ensure(m.gs.nbseg) || wk.segmsum.ensure(m.gs.nbseg)) {
+    res.status = -4;
+    set_error(h, "mixed: device allocation failed");
+    return res;
+  }
+  cudaMemsetAsync(h.flag, 0, 2 * sizeof(int), s);
+  gs_cg_weights<float>(m.gs, wk.mask.ptr, wk.mult.ptr, wk.segmask.ptr, wk.segmsum.ptr, h.flag, s);
+  launch_interior_check(h, wk.mask.ptr, wk.mult.ptr, h.flag + 1);
+  int flags[2] = {0, 0};
+  cudaMemcpyAsync(flags, h.flag, 2 * sizeof(int), cudaMemcpyDeviceToHost, s);
+  if (split_load(h, w64.r.ptr, 1.0 / scale, w64.d.ptr, binv, mask)) {
+    res.status = -3;
+    return res;
+  }
+  CgScalars& hc = *h.cg_host;
+  memset(&hc, 0, sizeof(CgScalars));
+  hc.rtz1 = 1.0;
+  hc.tin = -inner_tol;
+  hc.tol = inner_tol;
+  hc.vol = m.vol;
+  hc.maxiter = maxit;
+  hc.istep = 0;
+  if (maxit < 1) {
+    hc.done = 1;
+    hc.niter = 0;
+  }
+  cudaMemcpyAsync(h.cg, &hc, sizeof(CgScalars), cudaMemcpyHostToDevice, s);
+  if (cudaStreamSynchronize(s) != cudaSuccess) {
+    res.status = -3;
+    set_error(h, std::string("mixed: ") + cudaGetErrorString(cudaGetLastError()));
+    return res;
+  }
+  if (flags[0] || flags[1]) {
+    res.status = -1;
+    set_error(h, flags[0] ? "pcg: mask differs between copies of a shared node (apply dsop '*' first)"
+                          : "pcg: an element-interior point has mask or multiplicity other than 1");
+    return res;
+  }
+  if (split_first_check(h, c32)) {
+    res.status = -3;
+    return res;
+  }
+  for (int upd = 1; upd <= 100000; ++upd) {
+    PcgResult pr = split_iterate(h, c32);
+    if (pr.status && pr.status != -5) {
+      res.status = pr.status;
+      return res;
+    }
+    res.outer = upd;
+    res.inner = h.cg_host->niter;
+    const bool capped = h.cg_host->iter > h.cg_host->maxiter;
+    split_axpy(h, x, scale);
+    const double rnew = outer_residual(h, w64.r.ptr, f, x, c64, mask, mult, binv, w64.w.ptr);
+    if (!(rnew >= 0.0) || !std::isfinite(rnew)) {
+      res.status = -7;
+      set_error(h, "mixed: non-finite outer residual");
+      return res;
+    }
+    const bool progress = rnew < rbn;
+    rbn = rnew;
+    if (rbn <= tol || capped || !progress) break;
+    const int rr = split_replace(h, w64.r.ptr, scale, inner_tol, &res.restarts);
+    if (rr < 0) {
+      res.status = rr;
+      return res;
+    }
+    if (rr == 1) break;
+  }
+  res.rbn2 = rbn;
+  if (!(rbn <= tol)) {
+    res.status = -5;
+    set_error(h, "mixed: defect correction did not reach the tolerance");
+  }
+  return res;
 }
 
 MixedResult mixed_solve(Handle& h, double* x, const double* f, const double* h1,
@@ -343,7 +436,39 @@ MixedResult mixed_solve(Handle& h, double* x, const double* f, const double* h1,
       return res;
     }
     double scale = std::ldexp(1.0, std::ilogb(amax));
-    cast(wk.f.ptr, w64.r.ptr, 1.0 / scale);
+    if (h.use_split && split_eligible(h)) {
+      const int sst = split_setup(h);
+      if (sst) {
+        res.status = sst;
+        return res;
+      }
+      return mixed_split(h, res, x, f, c64, c32, mask, mult, binv, tol, rbn, maxit, inner_tol,
+                         scale);
+    }
+    // face-ordered FP32 vectors (perm.cu): the maps, position map and the
+    // vectors cast in that order; the guard puts the mesh's maps back
+    struct Gs32Reset {
+      Handle& h;
+      ~Gs32Reset() { h.gs32 = nullptr; }
+    } gs32_reset{h};
+    const int* perm = nullptr;
+    if (perm_eligible(h)) {
+      const int pst = perm_setup(h);
+      if (pst) {
+        res.status = pst;
+        return res;
+      }
+      perm = perm_pt_pos(h);
+      h.gs32 = perm_maps(h);
+      c32.perm = perm;
+      perm_cast(h, wk.mask.ptr, mask, 1.0);
+      perm_cast(h, wk.mult.ptr, mult, 1.0);
+      perm_cast(h, wk.binv.ptr, binv, 1.0);
+      perm_cast(h, wk.d.ptr, w64.d.ptr, 1.0);
+      perm_cast(h, wk.f.ptr, w64.r.ptr, 1.0 / scale);
+    } else {
+      cast(wk.f.ptr, w64.r.ptr, 1.0 / scale);
+    }
     bool trivial = false;
     PcgResult pr = pcg_prepare<float>(h, wk, wk.x.ptr, wk.f.ptr, c32, wk.mask.ptr, wk.mult.ptr,
                                       -inner_tol, maxit, 0, wk.d.ptr, &trivial);
@@ -364,8 +489,12 @@ MixedResult mixed_solve(Handle& h, double* x, const double* f, const double* h1,
       res.outer = upd;
       res.inner = h.cg_host->niter;
       const bool capped = h.cg_host->iter > h.cg_host->maxiter;
-      count_launch();
-      axpy_kernel<<<nb, kThreads, 0, s>>>(x, wk.x.ptr, scale, n);
+      if (perm) {
+        perm_axpy(h, x, wk.x.ptr, scale);
+      } else {
+        count_launch();
+        axpy_kernel<<<nb, kThreads, 0, s>>>(x, wk.x.ptr, scale, n);
+      }
       const double rnew = outer_residual(h, w64.r.ptr, f, x, c64, mask, mult, binv, w64.w.ptr);
       if (!(rnew >= 0.0) || !std::isfinite(rnew)) {
         res.status = -7;
@@ -375,7 +504,7 @@ MixedResult mixed_solve(Handle& h, double* x, const double* f, const double* h1,
       const bool progress = rnew < rbn;
       rbn = rnew;
       if (rbn <= tol || capped || !progress) break;
-      const int rr = mixed_replace(h, scale, inner_tol, &res.restarts);
+      const int rr = mixed_replace(h, scale, inner_tol, &res.restarts, perm);
       if (rr < 0) {
         res.status = rr;
         return res;

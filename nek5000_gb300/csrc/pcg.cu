@@ -172,12 +172,15 @@ __global__ void sum_kernel(int kind, const double* __restrict__ a, const double*
 template <typename T>
 __global__ void interior_check_kernel(const T* __restrict__ mask, const T* __restrict__ mult,
                                       const unsigned char* __restrict__ skip, int nx1, int64_t n,
-                                      int* bad) {
-  const int P = nx1 * nx1 * nx1;
+                                      int* bad, bool face_order = false) {
+  const int P = nx1 * nx1 * nx1, m = nx1 - 2;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     const int p = (int)(i % P), x = p % nx1, y = (p / nx1) % nx1, z = p / (nx1 * nx1);
-    const bool in = x > 0 && x < nx1 - 1 && y > 0 && y < nx1 - 1 && z > 0 && z < nx1 - 1;
+    // face order (perm.cu): the element's interior points come last
+    const bool in = face_order ? (m > 0 && p >= P - m * m * m)
+                               : (x > 0 && x < nx1 - 1 && y > 0 && y < nx1 - 1 && z > 0 &&
+                                  z < nx1 - 1);
     if (in && !(skip && skip[i]) && (mask[i] != T(1) || mult[i] != T(1))) atomicOr(bad, 1);
   }
 }
@@ -470,11 +473,13 @@ PcgResult pcg_prepare(Handle& h, PcgWork<T>& wk, T* x, const T* f, const Coef<T>
   const int64_t n = m.n;
   cudaStream_t s = h.stream;
   const int nA = axhelm_blocks(m.nx1, m.nel);
+  // the FP32 solve in the face-ordered layout uses that layout's maps
+  const GsMaps& gs = (sizeof(T) == 4 && h.gs32) ? *h.gs32 : m.gs;
   const int nB = std::max(
-      std::max(gs_cg_blocks(m.gs), gs_cg_blocks(m.gs.cls_tuned[sizeof(T) == 4 ? 1 : 0])), 1);
+      std::max(gs_cg_blocks(gs), gs_cg_blocks(gs.cls_tuned[sizeof(T) == 4 ? 1 : 0])), 1);
   const int nC = vec_blocks(n);
   if (wk.r.ensure(n) || wk.w.ensure(n) || wk.p.ensure(n) || wk.d.ensure(n) ||
-      wk.segmask.ensure(m.gs.nbseg) || wk.segmsum.ensure(m.gs.nbseg) ||
+      wk.segmask.ensure(gs.nbseg) || wk.segmsum.ensure(gs.nbseg) ||
       h.partialA.ensure(nA) || h.partialB.ensure(nB) || h.partialC.ensure(4 * (size_t)nC)) {
     res.status = -4;
     set_error(h, "pcg: device allocation failed");
@@ -536,10 +541,10 @@ PcgResult pcg_prepare(Handle& h, PcgWork<T>& wk, T* x, const T* f, const Coef<T>
   }
   // boundary-group mask / multiplicity weights
   cudaMemsetAsync(h.flag, 0, 2 * sizeof(int), s);
-  gs_cg_weights<T>(m.gs, mask, mult, wk.segmask.ptr, wk.segmsum.ptr, h.flag, s);
+  gs_cg_weights<T>(gs, mask, mult, wk.segmask.ptr, wk.segmsum.ptr, h.flag, s);
   count_launch();
-  interior_check_kernel<T><<<vec_blocks(n), kVecThreads, 0, s>>>(mask, mult, m.gs.skip, m.nx1, n,
-                                                                 h.flag + 1);
+  interior_check_kernel<T><<<vec_blocks(n), kVecThreads, 0, s>>>(mask, mult, gs.skip, m.nx1, n,
+                                                                 h.flag + 1, &gs != &m.gs);
   int flags[2] = {0, 0};
   cudaMemcpyAsync(flags, h.flag, 2 * sizeof(int), cudaMemcpyDeviceToHost, s);
   // r = f, p = 0
@@ -694,6 +699,7 @@ PcgResult pcg_iterate(Handle& h, const OpData<T>& op, PcgWork<T>& wk, T* x, cons
   cudaStream_t s = h.stream;
   const T* f = wk.r.ptr;  // graph key only
   const T* mask = wk.segmask.ptr;
+  const GsMaps& gsm = (sizeof(T) == 4 && h.gs32) ? *h.gs32 : m.gs;
   // main loop: chunks of iterations, one host check per chunk.  With kernel
   // timing on, every fused-axhelm launch is bracketed by events; after the
   // chunk's check, the first (iterations completed in the chunk) of them are
@@ -717,8 +723,8 @@ PcgResult pcg_iterate(Handle& h, const OpData<T>& op, PcgWork<T>& wk, T* x, cons
       if (h.timing) cudaEventRecord(h.ax_ev[4 * q + 1], s);
       if (e != cudaSuccess) return e;
       // FP32: rho came whole from the operator (AxArgs::allrho)
-      gs_cg<T>(m.gs, wk.w.ptr, wk.p.ptr, wk.segmask.ptr, wk.segmsum.ptr, h.cg, h.partialA.ptr,
-               nAb, h.partialB.ptr, s, sizeof(T) != 4, &m.gs.cls_tuned[sizeof(T) == 4 ? 1 : 0]);
+      gs_cg<T>(gsm, wk.w.ptr, wk.p.ptr, wk.segmask.ptr, wk.segmsum.ptr, h.cg, h.partialA.ptr,
+               nAb, h.partialB.ptr, s, sizeof(T) != 4, &gsm.cls_tuned[sizeof(T) == 4 ? 1 : 0]);
       if (h.timing) cudaEventRecord(h.ax_ev[4 * q + 2], s);
       launch_C<T>(h, wk, x, mult, binv, exact, false);
       if (h.timing) cudaEventRecord(h.ax_ev[4 * q + 3], s);
@@ -732,13 +738,14 @@ PcgResult pcg_iterate(Handle& h, const OpData<T>& op, PcgWork<T>& wk, T* x, cons
     Handle::GraphKey key;
     const void* ptrs[15] = {x,        f,        mask,      mult,           binv, wk.r.ptr,
                             wk.w.ptr, wk.p.ptr, wk.d.ptr,  wk.md.ptr,      c.h1, c.h2,
-                            wk.mb.ptr, c.hbm,   wk.segmask.ptr};
+                            wk.mb.ptr, c.perm ? (const void*)gsm.bidx : (const void*)c.hbm,
+                            wk.segmask.ptr};
     for (int i = 0; i < 15; ++i) key.ptr[i] = ptrs[i];
     key.ints[0] = (int)sizeof(T);
     key.ints[1] = c.h1mode;
     key.ints[2] = c.h2mode + 8 * (int)h.mcor;
     const AxShapeSel& sh = m.ax_sel[sizeof(T) == 4 ? 1 : 0];
-    const GsClasses& gc = m.gs.cls_tuned[sizeof(T) == 4 ? 1 : 0];
+    const GsClasses& gc = gsm.cls_tuned[sizeof(T) == 4 ? 1 : 0];
     key.ints[3] = (int)exact + 4 * (int)m.use_tma + 8 * (sh.kind + 1) + 32 * sh.epb +
                   4096 * (gc.threads / 32) + 65536 * (m.gs_gshift[sizeof(T) == 4 ? 1 : 0] + 4);
     key.ints[4] = chunk;

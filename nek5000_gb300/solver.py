@@ -564,6 +564,13 @@ class NekGpuBatch:
         if rc:
             raise _capi.NekGpuError(rc, self.last_error())
 
+    def set_persistent(self, on: bool = True):
+        """One persistent cooperative launch per batch segment (default), or
+        three graph-replayed launches per iteration."""
+        rc = self._L.nekgpu_batch_set_persistent(C.byref(self._b), C.byref(_cint(int(bool(on)))))
+        if rc:
+            raise _capi.NekGpuError(rc, self.last_error())
+
     def close(self):
         if getattr(self, "_b", None) is not None and self._b.value:
             self._L.nekgpu_batch_destroy(C.byref(self._b))

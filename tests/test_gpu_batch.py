@@ -109,6 +109,7 @@ def test_batch_block_sizes_give_identical_solves(problems):
     out = {}
     for threads in (0, 128, 256):
         B = NekGpuBatch(0)
+        B.set_persistent(False)  # the block size is tuned for the three-launch form
         for P in problems:
             B.add(P["nx1"], P["nel"], P["D"], P["g"], P["bm1"], P["glo_num"])
         if threads:
@@ -129,3 +130,30 @@ def test_batch_block_sizes_give_identical_solves(problems):
         assert out[threads][0] == out[0][0]
         for a, b in zip(out[threads][1], out[0][1]):
             assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("mixed", [0, 1])
+def test_persistent_launch_equals_graph_launches(gpu_lib, oracle, problems, mixed):
+    """The persistent cooperative form (nekgpu_batch_set_persistent 1, the
+    default) and the three-launch graph form run the same per-problem
+    arithmetic: identical iteration counts, norms and solutions, bit for
+    bit, FP64 and mixed."""
+    torch = pytest.importorskip("torch")
+    from nek5000_gb300 import NekGpuBatch
+    col = lambda k: [_dev(torch, P[k]) for P in problems]
+    out = {}
+    for persistent in (True, False):
+        B = NekGpuBatch(0)
+        B.set_persistent(persistent)
+        for P in problems:
+            B.add(P["nx1"], P["nel"], P["D"], P["g"], P["bm1"], P["glo_num"])
+        xs = [torch.zeros(P["n"], dtype=torch.float64, device="cuda") for P in problems]
+        res = B.solve(xs, col("f"), col("h1v"), col("h2v"), col("mask"), col("mult"),
+                      col("binv"), tin=-1e-10, mixed=mixed)
+        assert res["status"] == [0] * len(problems), B.last_error()
+        out[persistent] = (res, [x.cpu().numpy() for x in xs])
+        B.close()
+    (ra, xa), (rb, xb) = out[True], out[False]
+    assert ra["niter"] == rb["niter"] and ra["rbn2"] == rb["rbn2"]
+    for a, b in zip(xa, xb):
+        assert np.array_equal(a, b)

@@ -85,3 +85,77 @@ def test_mixed_host_entry_point(gpu_lib, oracle):
     assert rc == 0
     assert np.array_equal(r, rhs_ref)
     assert fp64_residual_norm(P, u, rhs_ref, h1, h2) <= 1.05e-10 * r0_ref
+
+
+@pytest.mark.parametrize("nx1,k,periodic,h2", [
+    (8, (4, 3, 3), (False, True, True), 10.0),
+    (4, (5, 4, 3), (False, False, False), 0.0),
+    (7, (3, 3, 3), (False, False, False), 0.0),   # odd lx1: the element-local form runs
+])
+def test_assembled_boundary_layout_matches_element_local_form(gpu_lib, oracle, nx1, k, periodic,
+                                                              h2):
+    """The residual-replacement solve with its FP32 vectors stored once per
+    global node (NEKGPU_OPT_SPLIT 1, the default) and element-locally (0):
+    both meet the FP64 tolerance, and their FP32 iteration counts agree to a
+    few percent (the same PCG; only the order of its FP32 sums differs)."""
+    torch = pytest.importorskip("torch")
+    from nek5000_gb300 import _capi
+    P = oracle.box_problem(nx1, *k, periodic=periodic, v=rng_unit_vector(31))
+    n = P["n"]
+    rng = np.random.default_rng(31)
+    f = P["ops"].dssum(P["bm1"] * (P["ops"].dssum(rng.standard_normal(n)) * P["mult"])) * P["mask"]
+    h1, h2a = np.ones(n), np.full(n, h2)
+    lib = gpu_lib(0)
+    lib.setup(P["nx1"], P["nel"], P["D"], P["g"], P["bm1"], P["glo_num"])
+    dev = lambda a: torch.tensor(a, device="cuda")
+    out = {}
+    for split in (1, 0):
+        lib.set_option(_capi.OPT_SPLIT, split)
+        x = torch.zeros(n, dtype=torch.float64, device="cuda")
+        outer, inner, r0, r2, rc = lib.cggo_mixed(x, dev(f), dev(h1), dev(h2a), dev(P["mask"]),
+                                                  dev(P["mult"]), 1, -1e-10, 10 ** 6, 1,
+                                                  dev(P["binv"]), inner_tol=None)
+        assert rc == 0, lib.last_error()
+        xs = x.cpu().numpy()
+        assert fp64_residual_norm(P, xs, f, h1, h2a) <= 1.05e-10 * r0
+        out[split] = (inner, xs)
+    (i1, x1), (i0, x0) = out[1], out[0]
+    assert abs(i1 - i0) <= max(3, 0.03 * i0), (i1, i0)
+    assert np.linalg.norm(x1 - x0) <= 1e-8 * np.linalg.norm(x0)
+
+
+@pytest.mark.parametrize("nx1,k,periodic,h2", [
+    (8, (4, 3, 3), (False, True, True), 10.0),
+    (7, (3, 3, 2), (False, False, False), 0.0),
+    (10, (2, 3, 2), (False, False, False), 1500.0),
+])
+def test_face_ordered_layout_matches_natural_order(gpu_lib, oracle, nx1, k, periodic, h2):
+    """The residual-replacement solve with its FP32 vectors in the
+    face-ordered element layout (NEKGPU_OPT_FACE_ORDER 1, the default) and in
+    the natural order (0): both meet the FP64 tolerance and their FP32
+    iteration counts agree to a few percent (the same PCG; the FP32 sums run
+    in another order)."""
+    torch = pytest.importorskip("torch")
+    from nek5000_gb300 import _capi
+    P = oracle.box_problem(nx1, *k, periodic=periodic, v=rng_unit_vector(33))
+    n = P["n"]
+    rng = np.random.default_rng(33)
+    f = P["ops"].dssum(P["bm1"] * (P["ops"].dssum(rng.standard_normal(n)) * P["mult"])) * P["mask"]
+    h1, h2a = np.ones(n), np.full(n, h2)
+    lib = gpu_lib(0)
+    lib.setup(P["nx1"], P["nel"], P["D"], P["g"], P["bm1"], P["glo_num"])
+    dev = lambda a: torch.tensor(a, device="cuda")
+    out = {}
+    for fo in (1, 0):
+        lib.set_option(_capi.OPT_FACE_ORDER, fo)
+        x = torch.zeros(n, dtype=torch.float64, device="cuda")
+        outer, inner, r0, r2, rc = lib.cggo_mixed(x, dev(f), dev(h1), dev(h2a), dev(P["mask"]),
+                                                  dev(P["mult"]), 1, -1e-10, 10 ** 6, 1,
+                                                  dev(P["binv"]), inner_tol=None)
+        assert rc == 0, lib.last_error()
+        xs = x.cpu().numpy()
+        assert fp64_residual_norm(P, xs, f, h1, h2a) <= 1.05e-10 * r0
+        out[fo] = (inner, xs)
+    (i1, x1), (i0, x0) = out[1], out[0]
+    assert abs(i1 - i0) <= max(3, 0.03 * i0), (i1, i0)
+    assert np.linalg.norm(x1 - x0) <= 1e-8 * np.linalg.norm(x0)
