@@ -1068,6 +1068,20 @@ def run_pressure(args):
         lib.h1mg_free()
     except Exception as exc:  # reported in the line, the Jacobi rows stand
         h1mg["error"] = str(exc)
+    # the same with the coarse solve by algebraic multigrid (param(40) = 1)
+    h1amg = {}
+    try:
+        lib.set_option(12, 1)
+        t0 = time.perf_counter()
+        lib.h1mg_setup(M["x"], M["y"], M["z"], M["glo_num"], mask=M["mask"])
+        h1amg["setup_s"] = time.perf_counter() - t0
+        timed("gmres_h1mg_amg", gmres)
+        timed("flex_cg_h1mg_amg", flex)
+        h1amg.update(gmres=out["gmres_h1mg_amg"], flex_cg=out["flex_cg_h1mg_amg"])
+        lib.h1mg_free()
+        lib.set_option(12, 0)
+    except Exception as exc:
+        h1amg["error"] = str(exc)
     line = {"metric": f"pressure-solve GMRES (hmh_gmres, restart 30, Jacobi) DOF-iters/s, "
                       f"E={args.k}^3 N={args.N} Poisson",
             "value": out["gmres"]["dof_iters_per_s"], "unit": "DOF-iters/s", "n_gpus": ws,
@@ -1079,6 +1093,7 @@ def run_pressure(args):
                        "n_points": n, "tol": f"{args.tol:g} x initial rnorm"},
             "gmres": out["gmres"], "cggo_same_system": out["cggo"],
             "flex_cg_same_system": out["flex_cg"], "h1mg_preconditioned": h1mg,
+            "h1mg_amg_coarse_preconditioned": h1amg,
             "clocks": out["gmres"]["clocks"]}
     if rank == 0 and ws == 1 and not args.no_cpu:
         from oracle import nekref

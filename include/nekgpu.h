@@ -91,6 +91,12 @@ extern "C" {
                                 memory sectors; 0 (default) the reference's
                                 x-fastest order.  Results agree to FP32
                                 rounding.                                    */
+#define NEKGPU_OPT_COARSE 12  /* coarse solve of the pressure preconditioner
+                                set up by the next nekgpu_h1mg_setup: 0
+                                (default) the sparse X X^T factor (the
+                                reference's param(40) = 0, crs_xxt); 1 algebraic
+                                multigrid (param(40) = 1, crs_amg; see
+                                nekgpu_crs_amg_setup)                        */
 #define NEKGPU_OPT_MIXED_MODE 7  /* mixed solve: 1 (default) one FP32 PCG whose
                                 residual is replaced by the FP64 one each time
                                 it drops by inner_tol, search direction kept;
@@ -175,6 +181,18 @@ int nekgpu_h1mg_setup(const int64_t *handle, const double *x, const double *y, c
 int nekgpu_h1mg_free(const int64_t *handle);
 /* z = M rhs on device arrays; rhs is masked in place, as h1mg_solve leaves it. */
 int nekgpu_h1mg_apply_dev(const int64_t *handle, double *z, double *rhs);
+
+/* The coarse solve of the reference's crs_amg interface on a handle:
+ * crs_amg_setup (core/crs_amg.c:531: n unknowns, nz matrix entries in
+ * coordinate form ai, aj, av -- zero-based, duplicates summed -- and the
+ * null-space flag) and crs_amg_solve (:186: x = one AMG V-cycle applied to
+ * b, device arrays of n; with the null space the last unknown is pinned to 0
+ * during the cycle and the mean of x is removed afterwards, as crs_solve
+ * does).  The hierarchy is built on the host by the setup nekmesh_amg_setup
+ * describes (the reference reads it from files its setup tool writes). */
+int nekgpu_crs_amg_setup(const int64_t *handle, const int64_t *n, const int64_t *nz,
+                         const int *ai, const int *aj, const double *av, const int *null_space);
+int nekgpu_crs_amg_solve_dev(const int64_t *handle, double *x, const double *b);
 /* ---- gradient-type operators of the splitting step (plan4) --------------
  * On device arrays of the handle's n points, in the reference's arithmetic
  * order (bit-identical to its unfused FP64 evaluation).  They need the metric

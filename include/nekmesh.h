@@ -169,6 +169,32 @@ int nekmesh_xxt_factor(const int64_t *n, const int64_t *ptr, const int *idx, con
                        const double *xyz, int64_t *nnz, int *perm, int64_t *cptr, int *cidx,
                        double *cval);
 
+/* The algebraic multigrid hierarchy of a coarse matrix (the reference's
+ * crs_amg data, core/crs_amg.c:96-128, which its setup tool writes to amg*.dat
+ * files; built here without them): the same setup nekgpu_crs_amg_setup and
+ * the AMG coarse solve of the pressure preconditioner run.  A symmetric
+ * positive definite, n x n in CSR (ptr n+1, idx, val, both triangles,
+ * columns ascending); *plan receives an id for the calls below. */
+int nekmesh_amg_setup(const int64_t *n, const int64_t *ptr, const int *idx, const double *val,
+                      int64_t *plan);
+/* Levels (*nlev), level offsets off (nlev+1: level l holds its F points at
+ * [off[l], off[l+1]) of the plan's order) and perm (n: the unknown at each
+ * position), each when non-null. */
+int nekmesh_amg_layout(const int64_t *plan, int *nlev, int64_t *off, int64_t *perm);
+/* Level *lev: sizes[6] = nf, nc and the entries of W, W^T, AfP, A_FF (AfP =
+ * A_FF W + A_FC, the F rows of A P with P = [W; I], crs_amg's AfP);
+ * Chebyshev steps and radius; the scaled inverse diagonal dff (nf) and the
+ * four matrices in CSR (W and AfP: nf rows, W^T: nc rows, A_FF: nf rows),
+ * each array when non-null. */
+int nekmesh_amg_level(const int64_t *plan, const int *lev, int64_t *sizes, int *m, double *rho,
+                      double *dff, int64_t *w_ptr, int *w_idx, double *w_val, int64_t *wt_ptr,
+                      int *wt_idx, double *wt_val, int64_t *afp_ptr, int *afp_idx,
+                      double *afp_val, int64_t *aff_ptr, int *aff_idx, double *aff_val);
+/* One V-cycle (amg_exec, core/crs_amg.c:129-186) on the host, in the plan's
+ * order (x out, b overwritten). */
+int nekmesh_amg_apply(const int64_t *plan, double *x, double *b);
+int nekmesh_amg_free(int64_t *plan);
+
 #ifdef __cplusplus
 }
 #endif

@@ -21,6 +21,7 @@ OPT_AUTOTUNE = 8
 OPT_SPLIT = 9
 OPT_DF = 10
 OPT_FACE_ORDER = 11
+OPT_COARSE = 12
 MAX_LX1 = 12
 NOALLOC_MAX_POINTS = 4194304
 PROJ_SPACES, PROJ_MAX, PROJ_DEFAULT = 16, 16, 8
@@ -52,6 +53,11 @@ SIGNATURES = {
     "nekmesh_co2_read": [C.c_char_p, _IP, _IP, _IP, _P],
     "nekmesh_co2_write": [C.c_char_p, _IP, _IP, _IP, _P],
     "nekmesh_ma2_read": [C.c_char_p, _IP, _IP, _P, _P],
+    "nekmesh_amg_setup": [_I64P, _P, _P, _P, _I64P],
+    "nekmesh_amg_layout": [_I64P, _IP, _P, _P],
+    "nekmesh_amg_level": [_I64P, _IP, _P, _IP, _DP] + [_P] * 13,
+    "nekmesh_amg_apply": [_I64P, _P, _P],
+    "nekmesh_amg_free": [_I64P],
     "nekmesh_connect": [_IP, _IP, _P, _P, _P, _P, _P, _DP, _P, _I64P],
     "nekmesh_setvert3d": [_IP, _IP, _P, _P, _I64P],
     "nekmesh_check_p_bc": [_IP, _IP, C.c_char_p, _P],
@@ -136,6 +142,8 @@ SIGNATURES = {
     "nekgpu_proj_count": [_I64P, _IP, _IP],
     "nekgpu_batch_set_shape": [_I64P, _IP, _IP],
     "nekgpu_batch_set_persistent": [_I64P, _IP],
+    "nekgpu_crs_amg_setup": [_I64P, _I64P, _I64P, _P, _P, _P, _IP],
+    "nekgpu_crs_amg_solve_dev": [_I64P, _P, _P],
     "nekgpu_ax_shape": [_I64P, _IP, _IP, _IP, _DP],
     "nekgpu_gs_shape": [_I64P, _IP, _IP, _IP, _DP],
     "nekgpu_set_gs_shape": [_I64P, _IP, _IP],

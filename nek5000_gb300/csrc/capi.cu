@@ -249,6 +249,7 @@ void handle_close(Handle& H) {
   H.mg.reset();
   H.split.reset();
   H.perm.reset();
+  H.crs_amg.reset();
   H.iface.reset();
   H.dealias.reset();
   gs_free(H.mesh.gs);
@@ -482,6 +483,10 @@ int nekgpu_set_option(const int64_t* handle, const int* key, const int* value) {
     case NEKGPU_OPT_GRAPH: H->use_graph = (*value != 0); break;
     case NEKGPU_OPT_SPLIT: H->use_split = (*value != 0); break;
     case NEKGPU_OPT_FACE_ORDER: H->use_perm = (*value != 0); break;
+    case NEKGPU_OPT_COARSE:
+      if (*value != 0 && *value != 1) return fail(H, NEKGPU_EINVAL, "coarse must be 0 or 1");
+      H->coarse_amg = (*value == 1);
+      break;
     case NEKGPU_OPT_DF:
       H->mesh.use_df = (*value != 0);
       if (H->mesh.use_df && H->has_mesh && !H->mesh.has_df && build_df(*H))

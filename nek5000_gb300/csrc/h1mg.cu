@@ -44,6 +44,8 @@ struct MgDev {
   DevBuf<int> xperm, xcidx, xridx;
   DevBuf<int64_t> xcptr, xrptr;
   DevBuf<double> xcval, xrval, xb, xy;
+  // or the AMG hierarchy of the same unknowns (amg.cu), when set up so
+  std::unique_ptr<AmgDev, AmgDevDeleter> amg;
   ~MgDev() {
     for (auto& L : lev) {
       gs_free(L.gs);
@@ -442,7 +444,9 @@ int h1mg_apply(Handle& h, double* z, double* rhs) {
     mg_cgather_kernel<<<(int)((m.nc + 255) / 256), 256, 0, s>>>(m.cv.ptr, L0.r.ptr, m.cstart.ptr,
                                                                m.cidx.ptr, m.nc);
   }
-  if (m.ns > 0) {  // cy = X (X^T cv) on the first ns unknowns
+  if (m.ns > 0 && m.amg) {  // cy = one AMG V-cycle on cv (crs_amg_solve)
+    amg_apply_dev(*m.amg, m.cy.ptr, m.cv.ptr, s);
+  } else if (m.ns > 0) {  // cy = X (X^T cv) on the first ns unknowns
     const int gw = (int)((m.ns * 32 + 255) / 256);
     count_launch(4);
     mg_perm_gather_kernel<<<grid_for(m.ns), kMgT, 0, s>>>(m.xb.ptr, m.cv.ptr, m.xperm.ptr, m.ns);
@@ -527,6 +531,7 @@ int h1mg_setup(Handle& h, const double* x, const double* y, const double* z, con
         elem[64 * (size_t)e + i + 8 * j] = a;
       }
   }
+  p.use_amg = h.coarse_amg;
   rc = h1mg_plan_coarse(p, elem.data(), err);
   if (rc) {
     set_error(h, err);
@@ -588,6 +593,10 @@ int h1mg_setup(Handle& h, const double* x, const double* y, const double* z, con
       set_error(h, "h1mg: device upload failed");
       return NEKGPU_ENOMEM;
     }
+  }
+  if (p.use_amg && p.nsolve > 0 && amg_upload(p.amg, m->amg, s)) {
+    set_error(h, "h1mg: AMG upload failed");
+    return NEKGPU_ENOMEM;
   }
   if (m->A.ensure(nemax) || m->E.ensure(nemax) || m->rtop.ensure(n) || m->vmult.ensure(n)) {
     set_error(h, "h1mg: device allocation failed");

@@ -29,6 +29,36 @@ int xxt_factor(XxtFactor& f, int64_t n, const std::vector<int64_t>& ptr,
                const std::vector<int>& idx, const std::vector<double>& val, const double* xyz,
                std::string& err);
 
+// Algebraic multigrid of a coarse matrix (amg_plan.cpp): the reference's crs_amg
+// hierarchy (core/crs_amg.c), level l holding its F points at
+// [off[l], off[l+1]) of the plan's order (perm[k] = the unknown at position
+// k).  W: interpolation from the coarser points (nf x nc, CSR), WT its
+// transpose, AFP = AFF W + A_FC the F rows of A P (P = [W; I]; kept in the
+// afc_* arrays) and AFF the F-F block of the level's matrix,
+// dff the scaled inverse diagonal of AFF, cheb_m / cheb_rho the Chebyshev
+// smoother.  The last level has one unknown: x = dff b.
+struct AmgLevel {
+  int64_t nf = 0, nc = 0;
+  int cheb_m = 1;
+  double cheb_rho = 0.0;
+  std::vector<double> dff;
+  std::vector<int64_t> w_ptr, wt_ptr, afc_ptr, aff_ptr;
+  std::vector<int> w_idx, wt_idx, afc_idx, aff_idx;
+  std::vector<double> w_val, wt_val, afc_val, aff_val;
+};
+struct AmgPlan {
+  int64_t n = 0;
+  std::vector<int64_t> perm, off;
+  std::vector<AmgLevel> lev;
+};
+// Hierarchy of the symmetric positive definite n x n matrix (CSR, both
+// triangles, columns ascending).  Returns 0 or NEKGPU_EINVAL.
+int amg_setup(AmgPlan& p, int64_t n, const std::vector<int64_t>& ptr, const std::vector<int>& idx,
+              const std::vector<double>& val, std::string& err);
+// One V-cycle (amg_exec, core/crs_amg.c:129-186) in the plan's order; b is
+// overwritten.
+void amg_apply_host(const AmgPlan& p, double* x, double* b);
+
 struct MgLevelPlan {
   int nx = 0;                         // points per direction (order + 1)
   int64_t n = 0;                      // nx^3 nel
@@ -54,6 +84,8 @@ struct MgPlan {
   std::vector<int64_t> cid;    // per level-0 point: coarse unknown or -1
   std::vector<double> ccoord;  // coordinates of the coarse unknowns (3 each)
   XxtFactor xxt;               // of the first nsolve unknowns
+  bool use_amg = false;        // coarse solve by AMG (crs_amg) instead of X X^T
+  AmgPlan amg;                 // of the first nsolve unknowns, when use_amg
 };
 
 // Level orders of h1mg_setup_mg_nx (core/hsmg.f:2272-2338) in 3-D; returns lmax.

@@ -580,7 +580,8 @@ int h1mg_plan_coarse(MgPlan& p, const double* elem, std::string& err) {
     ptr[r + 1] = (int64_t)idx.size();
     std::vector<std::pair<int, double>>().swap(v);
   }
-  const int rc = xxt_factor(p.xxt, ns, ptr, idx, val, p.ccoord.data(), err);
+  const int rc = p.use_amg ? amg_setup(p.amg, ns, ptr, idx, val, err)
+                           : xxt_factor(p.xxt, ns, ptr, idx, val, p.ccoord.data(), err);
   if (rc && err.find("positive") != std::string::npos)
     err = "h1mg: the coarse matrix is not positive definite (a null space without null_space?)";
   return rc;

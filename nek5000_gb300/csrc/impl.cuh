@@ -134,6 +134,12 @@ struct DealiasDeleter {
   void operator()(Dealias* p) const;
 };
 
+// An algebraic multigrid hierarchy on the device (amg.cu).
+struct AmgDev;
+struct AmgDevDeleter {
+  void operator()(AmgDev* p) const;
+};
+
 // The FP32 inner PCG's face-ordered element layout (perm.cu).
 struct PermLayout;
 struct PermLayoutDeleter {
@@ -227,6 +233,14 @@ struct Handle {
   // FP32 PCG uses while a solve runs in that layout (nullptr: the mesh's own)
   std::unique_ptr<PermLayout, PermLayoutDeleter> perm;
   bool use_perm = false;
+  // coarse solve of the pressure preconditioner: X X^T (false, the
+  // reference's param(40) = 0) or AMG (true, param(40) = 1;
+  // NEKGPU_OPT_COARSE), read by nekgpu_h1mg_setup
+  bool coarse_amg = false;
+  // the crs_amg-style coarse solver of nekgpu_crs_amg_setup / _solve_dev
+  std::unique_ptr<AmgDev, AmgDevDeleter> crs_amg;
+  int64_t crs_n = 0;
+  bool crs_null = false;
   const GsMaps* gs32 = nullptr;
 };
 
@@ -389,6 +403,12 @@ MixedResult mixed_solve(Handle& h, double* x, const double* f, const double* h1,
                         int mode = 0);
 
 void set_error(Handle& h, const std::string& msg);
+
+// ---- algebraic multigrid on the device (amg.cu) ---------------------------
+struct AmgPlan;
+int amg_upload(const AmgPlan& p, std::unique_ptr<AmgDev, AmgDevDeleter>& out, cudaStream_t s);
+// y = one V-cycle applied to v (unknowns' order, n values each)
+void amg_apply_dev(AmgDev& a, double* y, const double* v, cudaStream_t s);
 
 // ---- the FP32 inner PCG in the face-ordered element layout (perm.cu) -----
 std::vector<int> face_order(int nx);
