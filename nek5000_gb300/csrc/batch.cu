@@ -3,10 +3,14 @@
 //
 // Every problem keeps its own mesh, work vectors, PCG scalars and partial
 // sums (one Handle each, all on the batch's stream).  One PCG iteration of
-// the whole batch is three launches -- the fused operator, the boundary-group
-// gather-scatter and the update -- each covering every problem: a per-block
-// table maps a block to its problem, and the block runs that problem's body
-// (the operator dispatches on the problem's lx1).  A problem that has
+// the whole batch is the fused operator, the boundary-group gather-scatter
+// and the update, each covering every problem: a per-block table maps a block
+// to its problem, and the block runs that problem's body.  The operator is
+// one launch per polynomial order present (the problems' blocks grouped by
+// lx1), each compiled for its order alone, so that a launch holds only the
+// registers its order needs (one kernel over every order would carry the
+// largest order's registers, about 145 for FP32, and run one 256-thread block
+// per SM).  A problem that has
 // converged makes its blocks return at once, so each one stops at its own
 // iteration count, exactly as if it were solved alone.  Chunks of iterations
 // are captured once as a CUDA graph and replayed.
@@ -59,30 +63,20 @@ __device__ __forceinline__ void batch_ax_nx(const AxArgs<T>& a, int blk, int epb
   axhelm_body<NX, T, false, true>(a, blk, threadIdx.x % NXY, threadIdx.x / NXY, epb, smem, red);
 }
 
-template <typename T>
+// The operator for the problems of one order: virtual blocks start ..
+// start + gridDim.x - 1 of the operator table (every one of lx1 = NX).
+template <typename T, int NX>
 __global__ void __launch_bounds__(kBatchThreads)
-    batch_axhelm_kernel(const BDesc<T>* __restrict__ D, const int* __restrict__ map,
-                        const int* __restrict__ base) {
+    batch_axhelm_nx_kernel(const BDesc<T>* __restrict__ D, const int* __restrict__ map,
+                           const int* __restrict__ base, int start) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ double red[32];
-  const int pi = map[blockIdx.x];
+  const int vb = start + (int)blockIdx.x;
+  const int pi = map[vb];
   const BDesc<T>* d = D + pi;
   if (d->cg->done) return;
   const AxArgs<T> a = d->ax;
-  const int blk = blockIdx.x - base[pi], epb = d->epb;
-  switch (d->nx1) {
-    case 2: batch_ax_nx<T, 2>(a, blk, epb, smem, red); break;
-    case 3: batch_ax_nx<T, 3>(a, blk, epb, smem, red); break;
-    case 4: batch_ax_nx<T, 4>(a, blk, epb, smem, red); break;
-    case 5: batch_ax_nx<T, 5>(a, blk, epb, smem, red); break;
-    case 6: batch_ax_nx<T, 6>(a, blk, epb, smem, red); break;
-    case 7: batch_ax_nx<T, 7>(a, blk, epb, smem, red); break;
-    case 8: batch_ax_nx<T, 8>(a, blk, epb, smem, red); break;
-    case 9: batch_ax_nx<T, 9>(a, blk, epb, smem, red); break;
-    case 10: batch_ax_nx<T, 10>(a, blk, epb, smem, red); break;
-    case 11: batch_ax_nx<T, 11>(a, blk, epb, smem, red); break;
-    default: batch_ax_nx<T, 12>(a, blk, epb, smem, red); break;
-  }
+  batch_ax_nx<T, NX>(a, vb - base[pi], d->epb, smem, red);
 }
 
 template <typename T>
@@ -300,7 +294,13 @@ namespace {
 struct BatchLaunch {
   int gridA = 0, gridB = 0, gridC = 0;
   int threadsA = kBatchThreads;  // operator block size
-  size_t smem = 0;
+  size_t smem = 0;               // largest operator block's shared memory
+  // operator launches, one per order present: lx1, first virtual block,
+  // blocks, shared memory per block
+  int ngrp = 0;
+  int gnx[NEKGPU_MAX_LX1 + 1] = {}, gstart[NEKGPU_MAX_LX1 + 1] = {},
+      gcount[NEKGPU_MAX_LX1 + 1] = {};
+  size_t gsmem[NEKGPU_MAX_LX1 + 1] = {};
   const void* desc = nullptr;
   const int *mapA, *mapB, *mapC, *baseA, *baseB, *baseC;
 };
@@ -373,12 +373,29 @@ int batch_tables(Batch& B, const std::vector<int>& ids, const std::vector<Coef<T
             al(d.mult) && al(d.mb);
     d.cg = h.cg;
     smem = std::max(smem, batch_smem<T>(m.nx1, d.epb));
-    baseA[q] = (int)mapA.size();
-    mapA.insert(mapA.end(), d.nblkA, q);
     baseB[q] = (int)mapB.size();
     mapB.insert(mapB.end(), d.nblkB, q);
     baseC[q] = (int)mapC.size();
     mapC.insert(mapC.end(), d.nblkC, q);
+  }
+  // operator blocks grouped by order (ascending lx1, problems in list order
+  // inside an order): one launch per group
+  L.ngrp = 0;
+  for (int nx = 2; nx <= NEKGPU_MAX_LX1; ++nx) {
+    const int g0 = (int)mapA.size();
+    size_t gs = 0;
+    for (int q = 0; q < np; ++q) {
+      if (hd[q].nx1 != nx) continue;
+      baseA[q] = (int)mapA.size();
+      mapA.insert(mapA.end(), hd[q].nblkA, q);
+      gs = std::max(gs, batch_smem<T>(nx, hd[q].epb));
+    }
+    if ((int)mapA.size() == g0) continue;
+    L.gnx[L.ngrp] = nx;
+    L.gstart[L.ngrp] = g0;
+    L.gcount[L.ngrp] = (int)mapA.size() - g0;
+    L.gsmem[L.ngrp] = gs;
+    ++L.ngrp;
   }
   const size_t dbytes = sizeof(BDesc<T>) * np;
   const size_t nmap = mapA.size() + mapB.size() + mapC.size();
@@ -412,20 +429,54 @@ int batch_tables(Batch& B, const std::vector<int>& ids, const std::vector<Coef<T
   return 0;
 }
 
-template <typename T>
-cudaError_t batch_enqueue(Batch& B, const BatchLaunch& L, int k) {
+// One order's operator launch.
+template <typename T, int NX>
+cudaError_t batch_ops_nx(const BDesc<T>* D, const BatchLaunch& L, int g, cudaStream_t s) {
   static bool configured = false;
   if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(batch_axhelm_kernel<T>,
+    cudaError_t e = cudaFuncSetAttribute(batch_axhelm_nx_kernel<T, NX>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)batch_smem_max<T>());
+                                         (int)batch_smem<T>(NX, batch_epb(NX, kBatchThreads)));
     if (e != cudaSuccess) return e;
     configured = true;
   }
+  batch_axhelm_nx_kernel<T, NX><<<L.gcount[g], L.threadsA, L.gsmem[g], s>>>(D, L.mapA, L.baseA,
+                                                                           L.gstart[g]);
+  return cudaSuccess;
+}
+
+// The operator of one batched iteration: one launch per order present.
+template <typename T>
+cudaError_t batch_ops(const BatchLaunch& L, cudaStream_t s) {
+  const BDesc<T>* D = reinterpret_cast<const BDesc<T>*>(L.desc);
+  for (int g = 0; g < L.ngrp; ++g) {
+    count_launch();
+    cudaError_t e = cudaSuccess;
+    switch (L.gnx[g]) {
+      case 2: e = batch_ops_nx<T, 2>(D, L, g, s); break;
+      case 3: e = batch_ops_nx<T, 3>(D, L, g, s); break;
+      case 4: e = batch_ops_nx<T, 4>(D, L, g, s); break;
+      case 5: e = batch_ops_nx<T, 5>(D, L, g, s); break;
+      case 6: e = batch_ops_nx<T, 6>(D, L, g, s); break;
+      case 7: e = batch_ops_nx<T, 7>(D, L, g, s); break;
+      case 8: e = batch_ops_nx<T, 8>(D, L, g, s); break;
+      case 9: e = batch_ops_nx<T, 9>(D, L, g, s); break;
+      case 10: e = batch_ops_nx<T, 10>(D, L, g, s); break;
+      case 11: e = batch_ops_nx<T, 11>(D, L, g, s); break;
+      default: e = batch_ops_nx<T, 12>(D, L, g, s); break;
+    }
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+template <typename T>
+cudaError_t batch_enqueue(Batch& B, const BatchLaunch& L, int k) {
   const BDesc<T>* D = reinterpret_cast<const BDesc<T>*>(L.desc);
   for (int q = 0; q < k; ++q) {
-    count_launch(3);
-    batch_axhelm_kernel<T><<<L.gridA, L.threadsA, L.smem, B.stream>>>(D, L.mapA, L.baseA);
+    cudaError_t e = batch_ops<T>(L, B.stream);
+    if (e != cudaSuccess) return e;
+    count_launch(2);
     batch_gs_kernel<T><<<L.gridB, kGsThreads, 0, B.stream>>>(D, L.mapB, L.baseB);
     batch_update_kernel<T, false><<<L.gridC, kBatchThreads, 0, B.stream>>>(D, L.mapC, L.baseC);
   }
@@ -479,13 +530,9 @@ int batch_tune(Batch& B, const std::vector<int>& ids, const std::vector<Coef<T>>
         cudaEventDestroy(e1);
         return rc;
       }
-      const BDesc<T>* D = reinterpret_cast<const BDesc<T>*>(L.desc);
-      cudaError_t e = batch_enqueue<T>(B, L, 0);  // sets the kernel's shared-memory limit
-      count_launch(4);
-      batch_axhelm_kernel<T><<<L.gridA, L.threadsA, L.smem, B.stream>>>(D, L.mapA, L.baseA);
+      cudaError_t e = batch_ops<T>(L, B.stream);  // warm-up
       cudaEventRecord(e0, B.stream);
-      for (int q = 0; q < 3; ++q)
-        batch_axhelm_kernel<T><<<L.gridA, L.threadsA, L.smem, B.stream>>>(D, L.mapA, L.baseA);
+      for (int q = 0; q < 3 && e == cudaSuccess; ++q) e = batch_ops<T>(L, B.stream);
       cudaEventRecord(e1, B.stream);
       if (e == cudaSuccess) e = cudaGetLastError();
       float ms = 0.f;
@@ -608,6 +655,8 @@ int batch_iterate(Batch& B, const std::vector<int>& ids, const BatchLaunch& L, b
   std::vector<int64_t> key = {(int64_t)sizeof(T), L.gridA, L.gridB, L.gridC, (int64_t)L.smem,
                               L.threadsA,
                               (int64_t)(uintptr_t)L.desc, (int64_t)(uintptr_t)L.mapA, B.chunk};
+  for (int g = 0; g < L.ngrp; ++g)  // the operator launches' shapes are baked into the graph
+    key.insert(key.end(), {L.gnx[g], L.gstart[g], L.gcount[g], (int64_t)L.gsmem[g]});
   if (graph && (!B.gexec || key != B.gkey)) {
     if (B.gexec) cudaGraphExecDestroy(B.gexec);
     B.gexec = nullptr;
@@ -641,7 +690,7 @@ int batch_iterate(Batch& B, const std::vector<int>& ids, const BatchLaunch& L, b
     if (all) break;
     cudaError_t e;
     if (graph) {
-      count_launch(3LL * B.chunk);
+      count_launch((2LL + L.ngrp) * B.chunk);
       e = cudaGraphLaunch(B.gexec, B.stream);
     } else {
       e = batch_enqueue<T>(B, L, B.chunk);

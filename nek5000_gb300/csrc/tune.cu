@@ -7,14 +7,19 @@
 // competes with the plain-load one.  On the first solve of a mesh in a
 // precision, tune_operator times every candidate shape of the fused PCG
 // operator on that mesh (CUDA events on the handle's stream, zeroed work
-// vectors as operands) and keeps the fastest.  Every shape computes the same
+// vectors as operands) and keeps the fastest.  The candidates are timed in
+// kRounds interleaved sweeps and each keeps its best sweep, so a clock that
+// is still ramping up, or another process's burst, during one sweep does not
+// decide the pick.  Every shape computes the same
 // numbers -- pointwise results do not depend on the block a point lands in,
 // and the rho partials are per element -- so the pick changes speed only.
 // A process-wide cache keyed by device, lx1, nel, precision and coefficient
 // modes lets later meshes of the same kind reuse a pick without timing.
+#include <algorithm>
 #include <map>
 #include <mutex>
 #include <tuple>
+#include <vector>
 
 #include "axhelm_launch.cuh"
 #include "impl.cuh"
@@ -63,7 +68,7 @@ std::mutex g_mu;
 std::map<Key, AxShapeSel> g_cache;
 std::map<Key, std::pair<int, int>> g_gs_cache;  // boundary-group kernel (threads, gshift)
 
-constexpr int kWarm = 2, kReps = 5;
+constexpr int kWarm = 2, kReps = 5, kRounds = 3;
 
 }  // namespace
 
@@ -108,40 +113,47 @@ int tune_operator(Handle& h, const OpData<T>& op, PcgWork<T>& wk, const Coef<T>&
     set_error(h, "autotune: cudaEventCreate failed");
     return -3;
   }
+  std::vector<float> tbest(cand.size(), 1e30f);
+  std::vector<char> usable(cand.size(), 1);
+  for (int round = 0; round < kRounds; ++round)
+    for (size_t ci = 0; ci < cand.size(); ++ci) {
+      if (!usable[ci]) continue;
+      m.ax_sel[prec] = cand[ci];
+      auto launch = [&]() {
+        int np = 0;
+        // d = r (zero): the operands' values do not change the launch's cost
+        return launch_axhelm_cg<T, false>(m, op, wk.w.ptr, wk.p.ptr, wk.r.ptr, wk.r.ptr, c,
+                                          h.cg_tune.ptr, h.partialA.ptr, &np, s);
+      };
+      cudaError_t e = cudaSuccess;
+      for (int q = 0; q < kWarm && e == cudaSuccess; ++q) e = launch();
+      cudaEventRecord(e0, s);
+      for (int q = 0; q < kReps && e == cudaSuccess; ++q) e = launch();
+      cudaEventRecord(e1, s);
+      if (e != cudaSuccess) {  // a shape this device cannot launch: skip it
+        cudaGetLastError();
+        cudaStreamSynchronize(s);
+        usable[ci] = 0;
+        continue;
+      }
+      float ms = 0.f;
+      if (cudaEventSynchronize(e1) != cudaSuccess ||
+          cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        m.ax_sel[prec] = AxShapeSel();
+        set_error(h, std::string("autotune: ") + cudaGetErrorString(cudaGetLastError()));
+        return -3;
+      }
+      tbest[ci] = std::min(tbest[ci], ms / kReps);
+    }
   AxShapeSel best;
   best.ms = 1e30f;
-  for (const AxShapeSel& sh : cand) {
-    m.ax_sel[prec] = sh;
-    auto launch = [&]() {
-      int np = 0;
-      // d = r (zero): the operands' values do not change the launch's cost
-      return launch_axhelm_cg<T, false>(m, op, wk.w.ptr, wk.p.ptr, wk.r.ptr, wk.r.ptr, c,
-                                        h.cg_tune.ptr, h.partialA.ptr, &np, s);
-    };
-    cudaError_t e = cudaSuccess;
-    for (int q = 0; q < kWarm && e == cudaSuccess; ++q) e = launch();
-    cudaEventRecord(e0, s);
-    for (int q = 0; q < kReps && e == cudaSuccess; ++q) e = launch();
-    cudaEventRecord(e1, s);
-    if (e != cudaSuccess) {  // a shape this device cannot launch: skip it
-      cudaGetLastError();
-      cudaStreamSynchronize(s);
-      continue;
+  for (size_t ci = 0; ci < cand.size(); ++ci)
+    if (usable[ci] && tbest[ci] < best.ms) {
+      best = cand[ci];
+      best.ms = tbest[ci];
     }
-    float ms = 0.f;
-    if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
-      cudaEventDestroy(e0);
-      cudaEventDestroy(e1);
-      m.ax_sel[prec] = AxShapeSel();
-      set_error(h, std::string("autotune: ") + cudaGetErrorString(cudaGetLastError()));
-      return -3;
-    }
-    ms /= kReps;
-    if (ms < best.ms) {
-      best = sh;
-      best.ms = ms;
-    }
-  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (best.kind < 0) {
@@ -192,12 +204,13 @@ int tune_gs(Handle& h, PcgWork<T>& wk) {
     set_error(h, "autotune: cudaEventCreate failed");
     return -3;
   }
-  float best = 1e30f;
-  GsClasses bestc = m.gs.cls;
-  int bestg = 0;
+  std::vector<std::pair<int, int>> shapes;
   for (int threads : {128, 256, 512})
-    for (int gshift : {-1, 0, 1}) {
-      const GsClasses c = gs_shape(m.gs.cls, threads, gshift);
+    for (int gshift : {-1, 0, 1}) shapes.emplace_back(threads, gshift);
+  std::vector<float> tbest(shapes.size(), 1e30f);
+  for (int round = 0; round < kRounds; ++round)
+    for (size_t si = 0; si < shapes.size(); ++si) {
+      const GsClasses c = gs_shape(m.gs.cls, shapes[si].first, shapes[si].second);
       if (h.partialB.ensure(gs_cg_blocks(c))) {
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
@@ -221,12 +234,16 @@ int tune_gs(Handle& h, PcgWork<T>& wk) {
         set_error(h, std::string("autotune: ") + cudaGetErrorString(e));
         return -3;
       }
-      ms /= kReps;
-      if (ms < best) {
-        best = ms;
-        bestc = c;
-        bestg = gshift;
-      }
+      tbest[si] = std::min(tbest[si], ms / kReps);
+    }
+  float best = 1e30f;
+  GsClasses bestc = m.gs.cls;
+  int bestg = 0;
+  for (size_t si = 0; si < shapes.size(); ++si)
+    if (tbest[si] < best) {
+      best = tbest[si];
+      bestc = gs_shape(m.gs.cls, shapes[si].first, shapes[si].second);
+      bestg = shapes[si].second;
     }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
