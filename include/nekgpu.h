@@ -545,9 +545,12 @@ int nekgpu_batch_shape(const int64_t *batch, const int *precision, int *threads,
  * problems with grid-wide barriers between them (bounded waits: a barrier
  * that does not complete within seconds fails the solve with NEKGPU_ECUDA
  * and leaves the GPU usable).  Its block size is 256 threads.  *on = 0
- * (default): three launches per iteration, replayed as a captured CUDA
- * graph, with the operator block size tuned as nekgpu_batch_shape says.  Both
- * forms give identical results.  No reference counterpart. */
+ * (default): per iteration one operator launch per polynomial order present
+ * (FP32: the TMA-staged body where it applies and times faster) plus the
+ * boundary-group and update launches, replayed as a captured CUDA graph, with
+ * the plain operator's block size tuned as nekgpu_batch_shape says.  Both
+ * forms give results within the FP64 tolerance of each other (FP64 solves:
+ * identical).  No reference counterpart. */
 int nekgpu_batch_set_persistent(const int64_t *batch, const int *on);
 int nekgpu_batch_set_shape(const int64_t *batch, const int *precision, const int *threads);
 int nekgpu_batch_last_error(const int64_t *batch, char *buf, const int *buflen);

@@ -67,6 +67,12 @@ struct AxArgs {
   const int* perm;
 };
 
+// Orders the TMA-staged FP32 kernel (axhelm_tma.cuh) serves: every even
+// lx1, and odd lx1 up to 9 in blocks of 4 elements.
+__host__ __device__ constexpr bool tma_lx1(int nx) {
+  return nx % 2 == 0 || (nx >= 3 && nx <= 9);
+}
+
 template <int NX>
 struct AxShape {
   static constexpr int R = NX + 1;           // padded row

@@ -65,7 +65,7 @@ static cudaError_t launch_ax(const Mesh& m, const AxArgs<T>& a, int* nparts, cud
   if constexpr (!EXACT && sizeof(T) == 4) {
     // FP64 is bound by the FP64 pipe, where the plain-load kernel (D in
     // shared memory, higher occupancy) is faster; the TMA form serves FP32.
-    if (sh.kind == 1 && m.use_tma && m.nx1 % 2 == 0 && tma_ok<T, FUSED>(a))
+    if (sh.kind == 1 && m.use_tma && tma_lx1(m.nx1) && tma_ok<T, FUSED>(a))
       return launch_tma_f32(m, a, FUSED, sh.epb, nparts, s);
   }
   const int epb = sh.kind == 0 ? sh.epb : axhelm_epb(m.nx1);

@@ -1,5 +1,5 @@
 // axhelm_tma.cu -- FP32 instantiations of the TMA-staged operator
-// (axhelm_tma.cuh), every even lx1 and every candidate block shape.
+// (axhelm_tma.cuh), every lx1 it serves and every candidate block shape.
 #include "axhelm_tma.cuh"
 #include "impl.cuh"
 
@@ -41,7 +41,11 @@ cudaError_t launch_fused(const Mesh& m, const AxArgs<float>& a, int epb, int* np
                          cudaStream_t s) {
   switch (m.nx1) {
     case 2: return launch_nx<2, FUSED>(m, a, epb, nparts, s);
+    case 3: return launch_nx<3, FUSED>(m, a, epb, nparts, s);
     case 4: return launch_nx<4, FUSED>(m, a, epb, nparts, s);
+    case 5: return launch_nx<5, FUSED>(m, a, epb, nparts, s);
+    case 7: return launch_nx<7, FUSED>(m, a, epb, nparts, s);
+    case 9: return launch_nx<9, FUSED>(m, a, epb, nparts, s);
     case 6: return launch_nx<6, FUSED>(m, a, epb, nparts, s);
     case 8: return launch_nx<8, FUSED>(m, a, epb, nparts, s);
     case 10: return launch_nx<10, FUSED>(m, a, epb, nparts, s);
@@ -62,7 +66,11 @@ cudaError_t launch_tma_f32(const Mesh& m, const AxArgs<float>& a, bool fused, in
 int tma_default_epb(int nx) {
   switch (nx) {
     case 2: return tma_epb<2>();
+    case 3: return tma_epb<3>();
     case 4: return tma_epb<4>();
+    case 5: return tma_epb<5>();
+    case 7: return tma_epb<7>();
+    case 9: return tma_epb<9>();
     case 6: return tma_epb<6>();
     case 8: return tma_epb<8>();
     case 10: return tma_epb<10>();
@@ -85,7 +93,11 @@ std::vector<int> tma_candidates(int nx) {
     for (int q = 0; q < 3; ++q) add(tma_epb_cand<N>(q));     \
     break;
     NEKGPU_TMA_CAND(2)
+    NEKGPU_TMA_CAND(3)
     NEKGPU_TMA_CAND(4)
+    NEKGPU_TMA_CAND(5)
+    NEKGPU_TMA_CAND(7)
+    NEKGPU_TMA_CAND(9)
     NEKGPU_TMA_CAND(6)
     NEKGPU_TMA_CAND(8)
     NEKGPU_TMA_CAND(10)

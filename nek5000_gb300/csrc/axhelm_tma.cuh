@@ -14,8 +14,14 @@
 //    16-byte vectors (warp broadcasts), columns as conflict-free scalars;
 //  * the t-direction transposed contraction accumulates in registers.
 //
-// Valid when lx1^3 * sizeof(T) is a multiple of 16 bytes (even lx1) and the
-// arrays are 16-byte aligned; otherwise axhelm.cuh's kernel is used.
+// Valid when the arrays are 16-byte aligned.  For even lx1 a block's slices
+// start and end on 16-byte boundaries (lx1^3 sizeof(T) is a multiple of 16).
+// For odd lx1 (FP32, lx1 <= 9) each slice is copied as the window of whole
+// 16-byte units that holds it -- up to 3 values before its first element and
+// after its last, never outside the array -- and the slice pointer is offset
+// into the window; a block whose window would reach past the end of an array
+// (the last block) stages its slices with plain loads instead.  Otherwise
+// axhelm.cuh's kernel is used.
 #pragma once
 #include "axhelm.cuh"
 #include "tma.cuh"
@@ -35,6 +41,15 @@ __host__ __device__ constexpr int tma_epb_cand(int q) {
                 : (q == 1 ? tma_epb<NX>() : 2 * tma_epb<NX>());
 }
 
+// Values of a staged slice of `len` values in shared memory: len when len
+// values are whole 16-byte units for every block (P sizeof(T) a multiple of
+// 16), else room for the 16-byte window around them.
+template <typename T>
+__host__ __device__ constexpr int tma_window(int len, bool whole) {
+  return whole ? len : ((len + 2 * (16 / (int)sizeof(T)) - 2) / (16 / (int)sizeof(T))) *
+                           (16 / (int)sizeof(T));
+}
+
 // Number of staged field slices (of EPB*P values) besides G and the work slabs.
 __host__ __device__ constexpr int tma_nslices(bool fused, int h1mode, int h2mode) {
   return 1 + (fused ? 2 : 0) + (h2mode ? 1 : 0) + (h1mode == 1 ? 1 : 0) + (h2mode == 2 ? 1 : 0);
@@ -45,9 +60,11 @@ __host__ __device__ constexpr int tma_nslices(bool fused, int h1mode, int h2mode
 template <int NX, typename T, int EPB>
 __host__ __device__ constexpr size_t tma_smem_bytes(bool fused, int h1mode, int h2mode) {
   constexpr int P = NX * NX * NX;
-  return 64 /* mbarrier + pad */ + (size_t)NX * NX * sizeof(T) /* D */ +
-         (size_t)EPB * P * sizeof(T) *
-             (tma_nslices(fused, h1mode, h2mode) + 6 + (fused ? 0 : 2));
+  constexpr bool whole = (P * sizeof(T)) % 16 == 0;
+  return 64 /* mbarrier + pad */ + ((size_t)NX * NX * sizeof(T) + 15) / 16 * 16 /* D */ +
+         sizeof(T) * ((size_t)tma_window<T>(EPB * P, whole) *
+                          (tma_nslices(fused, h1mode, h2mode) + (fused ? 0 : 2)) +
+                      tma_window<T>(6 * EPB * P, whole));
 }
 
 // Load NX consecutive values of T from shared memory with the widest aligned
@@ -89,51 +106,85 @@ template <int NX, typename T, bool FUSED, int EPB>
 __device__ __forceinline__ void axhelm_tma_body(const AxArgs<T>& a, int blk,
                                                 unsigned char* smem_raw) {
   constexpr int P = NX * NX * NX, NXY = NX * NX;
+  constexpr int U = 16 / (int)sizeof(T);  // values per 16-byte unit
+  constexpr bool whole = (P % U) == 0;     // every block's slices are whole units
+  constexpr int SL = tma_window<T>(EPB * P, whole), SLG = tma_window<T>(6 * EPB * P, whole);
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
   T* sD = reinterpret_cast<T*>(smem_raw + 64);  // D[i][l] row-major
-  // staged slices, each EPB*P values, 16-byte aligned (P*sizeof(T) % 16 == 0)
+  // staged slices (windows of SL values, 16-byte aligned), G's of SLG
   T* base = reinterpret_cast<T*>(smem_raw + 64 + ((NX * NX * sizeof(T) + 15) / 16) * 16);
   const int hb = a.h2mode ? 1 : 0, hh1 = a.h1mode == 1 ? 1 : 0, hh2 = a.h2mode == 2 ? 1 : 0;
-  T* sU = base;
-  T* sR = sU + EPB * P;
-  T* sDg = sR + (FUSED ? EPB * P : 0);
-  T* sB = sDg + (FUSED ? EPB * P : 0);
-  T* sH1 = sB + hb * EPB * P;
-  T* sH2 = sH1 + hh1 * EPB * P;
-  T* sG = sH2 + hh2 * EPB * P;
-  T* st1 = FUSED ? sR : sG + 6 * EPB * P;
-  T* st2 = FUSED ? sDg : sG + 7 * EPB * P;
+  const int e0 = blk * EPB;
+  const int ne = min(EPB, a.nel - e0);  // elements of this block
+  const size_t off = (size_t)e0 * P;
+  // values of the window before the block's first element (0 when whole)
+  const int du = whole ? 0 : (int)(off % U), dg = whole ? 0 : (int)((6 * off) % U);
+  T* wU = base;
+  T* wR = wU + SL;
+  T* wDg = wR + (FUSED ? SL : 0);
+  T* wB = wDg + (FUSED ? SL : 0);
+  T* wH1 = wB + hb * SL;
+  T* wH2 = wH1 + hh1 * SL;
+  T* wG = wH2 + hh2 * SL;
+  T* sU = wU + du;
+  T* sR = wR + du;
+  T* sDg = wDg + du;
+  T* sB = wB + du;
+  T* sH1 = wH1 + du;
+  T* sH2 = wH2 + du;
+  T* sG = wG + dg;
+  T* st1 = FUSED ? sR : wG + SLG;
+  T* st2 = FUSED ? sDg : wG + SLG + SL;
 
   if constexpr (FUSED) {
     if (a.cg->done) return;
   }
   const int tid = threadIdx.x + NXY * threadIdx.y;
-  const int e0 = blk * EPB;
-  const int ne = min(EPB, a.nel - e0);  // elements of this block
   if (tid == 0) {
     mbar_init(bar, 1);
     mbar_fence_init();
   }
   for (int q = tid; q < NXY; q += NXY * EPB) sD[q] = a.D[q];
   __syncthreads();
-  if (tid == 0) {
-    const uint32_t fb = (uint32_t)(ne * P * sizeof(T));
-    const size_t off = (size_t)e0 * P;
-    const uint32_t total = fb * (1 + (FUSED ? 2 : 0) + hb + hh1 + hh2 + 6);
+  // window lengths (whole 16-byte units) and whether they stay inside the
+  // arrays; if not (the last block of an odd order), plain loads of the same
+  // slices (block-uniform)
+  const int wl = whole ? ne * P : (du + ne * P + U - 1) / U * U;
+  const int wlg = whole ? 6 * ne * P : (dg + 6 * ne * P + U - 1) / U * U;
+  const size_t n = (size_t)a.nel * P;
+  const bool bulk = off - du + wl <= n && 6 * off - dg + wlg <= 6 * n;
+  if (!bulk) {
+    const int nv = ne * P, nt = NXY * EPB;
+    for (int q = tid; q < nv; q += nt) {
+      sU[q] = a.u[off + q];
+      if constexpr (FUSED) {
+        sR[q] = a.r[off + q];
+        sDg[q] = a.d[off + q];
+      }
+      if (hb) sB[q] = a.bm1[off + q];
+      if (hh1) sH1[q] = a.h1[off + q];
+      if (hh2) sH2[q] = a.h2[off + q];
+    }
+    for (int q = tid; q < 6 * nv; q += nt) sG[q] = a.G[6 * off + q];
+  }
+  if (tid == 0 && bulk) {
+    const uint32_t fb = (uint32_t)(wl * sizeof(T)), fg = (uint32_t)(wlg * sizeof(T));
+    const uint32_t total = fb * (1 + (FUSED ? 2 : 0) + hb + hh1 + hh2) + fg;
     mbar_expect_tx(bar, total);
     // every input is read once per apply: evict first, so that L2 keeps w
     // (operands shared by the fields of a multi-field solve: default policy)
     const uint64_t pol = l2_policy_evict_first();
     const uint64_t spol = a.shared_in ? l2_policy_evict_normal() : pol;
-    bulk_g2s_hint(sU, a.u + off, fb, bar, pol);
+    const size_t wo = off - du;
+    bulk_g2s_hint(wU, a.u + wo, fb, bar, pol);
     if constexpr (FUSED) {
-      bulk_g2s_hint(sR, a.r + off, fb, bar, pol);
-      bulk_g2s_hint(sDg, a.d + off, fb, bar, spol);
+      bulk_g2s_hint(wR, a.r + wo, fb, bar, pol);
+      bulk_g2s_hint(wDg, a.d + wo, fb, bar, spol);
     }
-    if (hb) bulk_g2s_hint(sB, a.bm1 + off, fb, bar, spol);
-    if (hh1) bulk_g2s_hint(sH1, a.h1 + off, fb, bar, spol);
-    if (hh2) bulk_g2s_hint(sH2, a.h2 + off, fb, bar, spol);
-    bulk_g2s_hint(sG, a.G + 6 * off, 6 * fb, bar, spol);
+    if (hb) bulk_g2s_hint(wB, a.bm1 + wo, fb, bar, spol);
+    if (hh1) bulk_g2s_hint(wH1, a.h1 + wo, fb, bar, spol);
+    if (hh2) bulk_g2s_hint(wH2, a.h2 + wo, fb, bar, spol);
+    bulk_g2s_hint(wG, a.G + (6 * off - dg), fg, bar, spol);
   }
   // D rows / columns of this thread while the copies fly
   const int i = threadIdx.x % NX, j = threadIdx.x / NX, el = threadIdx.y;
@@ -145,7 +196,9 @@ __device__ __forceinline__ void axhelm_tma_body(const AxArgs<T>& a, int blk,
     DTi[l] = a.D[l * NX + i];
     DTj[l] = a.D[l * NX + j];
   }
-  const bool ok = mbar_wait_bounded(bar, 0, a.err);
+  bool ok = true;
+  if (bulk) ok = mbar_wait_bounded(bar, 0, a.err);
+  else __syncthreads();
   const bool act = ok && el < ne;
   const int lo = el * P;  // element offset inside the staged slices
   const size_t eo = (size_t)(e0 + (el < ne ? el : 0)) * P;

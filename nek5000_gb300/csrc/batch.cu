@@ -10,7 +10,8 @@
 // lx1), each compiled for its order alone, so that a launch holds only the
 // registers its order needs (one kernel over every order would carry the
 // largest order's registers, about 145 for FP32, and run one 256-thread block
-// per SM).  A problem that has
+// per SM).  For FP32 and even lx1 the order's launch is the TMA-staged
+// operator body (axhelm_tma.cuh), as in a single solve.  A problem that has
 // converged makes its blocks return at once, so each one stops at its own
 // iteration count, exactly as if it were solved alone.  Chunks of iterations
 // are captured once as a CUDA graph and replayed.
@@ -23,6 +24,7 @@
 #include <map>
 #include <mutex>
 
+#include "axhelm_tma.cuh"
 #include "cg_kernels.cuh"
 #include "gs_kernels.cuh"
 #include "impl.cuh"
@@ -77,6 +79,29 @@ __global__ void __launch_bounds__(kBatchThreads)
   if (d->cg->done) return;
   const AxArgs<T> a = d->ax;
   batch_ax_nx<T, NX>(a, vb - base[pi], d->epb, smem, red);
+}
+
+// Elements per block of the batched TMA-staged FP32 operator: one for
+// lx1 >= 7 (what the single-solve autotuner picks there), else the built-in
+// count of about 128 threads.
+template <int NX>
+__host__ __device__ constexpr int batch_tma_epb() {
+  return NX >= 7 ? 1 : tma_epb<NX>();
+}
+
+// The TMA-staged FP32 operator for the problems of one order (blocks of
+// (NX*NX, EPB) threads; virtual blocks as batch_axhelm_nx_kernel).
+template <int NX, int EPB>
+__global__ void __launch_bounds__(NX* NX* EPB)
+    batch_axhelm_tma_kernel(const BDesc<float>* __restrict__ D, const int* __restrict__ map,
+                            const int* __restrict__ base, int start) {
+  extern __shared__ __align__(128) unsigned char smem_tma[];
+  const int vb = start + (int)blockIdx.x;
+  const int pi = map[vb];
+  const BDesc<float>* d = D + pi;
+  if (d->cg->done) return;
+  const AxArgs<float> a = d->ax;
+  axhelm_tma_body<NX, float, true, EPB>(a, vb - base[pi], smem_tma);
 }
 
 template <typename T>
@@ -257,6 +282,49 @@ size_t batch_smem_max() {
   return b;
 }
 
+// Elements per block and shared memory of the batched TMA operator
+// (tma_lx1(nx)).
+int batch_tma_epb_rt(int nx) {
+  switch (nx) {
+    case 2: return batch_tma_epb<2>();
+    case 3: return batch_tma_epb<3>();
+    case 4: return batch_tma_epb<4>();
+    case 5: return batch_tma_epb<5>();
+    case 7: return batch_tma_epb<7>();
+    case 9: return batch_tma_epb<9>();
+    case 6: return batch_tma_epb<6>();
+    case 8: return batch_tma_epb<8>();
+    case 10: return batch_tma_epb<10>();
+    default: return batch_tma_epb<12>();
+  }
+}
+
+size_t batch_tma_smem(int nx, int h1m, int h2m) {
+  switch (nx) {
+    case 2: return tma_smem_bytes<2, float, batch_tma_epb<2>()>(true, h1m, h2m);
+    case 3: return tma_smem_bytes<3, float, batch_tma_epb<3>()>(true, h1m, h2m);
+    case 4: return tma_smem_bytes<4, float, batch_tma_epb<4>()>(true, h1m, h2m);
+    case 5: return tma_smem_bytes<5, float, batch_tma_epb<5>()>(true, h1m, h2m);
+    case 7: return tma_smem_bytes<7, float, batch_tma_epb<7>()>(true, h1m, h2m);
+    case 9: return tma_smem_bytes<9, float, batch_tma_epb<9>()>(true, h1m, h2m);
+    case 6: return tma_smem_bytes<6, float, batch_tma_epb<6>()>(true, h1m, h2m);
+    case 8: return tma_smem_bytes<8, float, batch_tma_epb<8>()>(true, h1m, h2m);
+    case 10: return tma_smem_bytes<10, float, batch_tma_epb<10>()>(true, h1m, h2m);
+    default: return tma_smem_bytes<12, float, batch_tma_epb<12>()>(true, h1m, h2m);
+  }
+}
+
+// Every array the TMA body stages is 16-byte aligned.
+template <typename T>
+bool batch_tma_aligned(const AxArgs<T>& a) {
+  auto al = [](const void* p) { return ((uintptr_t)p & 15u) == 0; };
+  bool ok = al(a.u) && al(a.G) && al(a.D) && al(a.r) && al(a.d);
+  if (a.h2mode) ok = ok && al(a.bm1);
+  if (a.h1mode == 1) ok = ok && al(a.h1);
+  if (a.h2mode == 2) ok = ok && al(a.h2);
+  return ok;
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -287,6 +355,9 @@ struct Batch {
   int pinned[2] = {0, 0};
   std::vector<int64_t> tkey[2];
   float tune_ms[2] = {0.f, 0.f};
+  // FP32 orders (bit lx1) whose operator launch keeps the plain body although
+  // the TMA-staged one applies: batch_tune found it faster there
+  unsigned tma_off = 0u;
 };
 
 namespace {
@@ -299,7 +370,7 @@ struct BatchLaunch {
   // blocks, shared memory per block
   int ngrp = 0;
   int gnx[NEKGPU_MAX_LX1 + 1] = {}, gstart[NEKGPU_MAX_LX1 + 1] = {},
-      gcount[NEKGPU_MAX_LX1 + 1] = {};
+      gcount[NEKGPU_MAX_LX1 + 1] = {}, gtma[NEKGPU_MAX_LX1 + 1] = {};
   size_t gsmem[NEKGPU_MAX_LX1 + 1] = {};
   const void* desc = nullptr;
   const int *mapA, *mapB, *mapC, *baseA, *baseB, *baseC;
@@ -367,7 +438,14 @@ int batch_tables(Batch& B, const std::vector<int>& ids, const std::vector<Coef<T
     d.mb = wk.mb.ptr;
     d.n = m.n;
     d.partialC = h.partialC.ptr;
-    d.nblkC = pcg_vec_blocks(m.n);
+    // FP64: the single solve's block count (the same FP64 sums, so that a
+    // batched FP64 problem returns exactly what its solve alone returns);
+    // FP32: at least 8 vector steps per thread, so that the small problems'
+    // blocks are not mostly reduction
+    d.nblkC = std::is_same<T, double>::value
+                  ? pcg_vec_blocks(m.n)
+                  : (int)std::min<int64_t>(std::max<int64_t>((m.n + 8191) / 8192, 1),
+                                           pcg_vec_blocks(m.n));
     auto al = [](const void* p) { return ((uintptr_t)p & 15u) == 0; };
     d.vec = al(d.x) && al(wk.r.ptr) && al(wk.p.ptr) && al(wk.w.ptr) && al(d.md) &&
             al(d.mult) && al(d.mb);
@@ -380,21 +458,40 @@ int batch_tables(Batch& B, const std::vector<int>& ids, const std::vector<Coef<T
   }
   // operator blocks grouped by order (ascending lx1, problems in list order
   // inside an order): one launch per group
+  // (FP32, an order the TMA-staged body serves, every array aligned and the
+  // order not in tma_off: that body, as in a single solve; the persistent
+  // form keeps the plain body in every phase)
   L.ngrp = 0;
   for (int nx = 2; nx <= NEKGPU_MAX_LX1; ++nx) {
+    bool any = false;
+    bool tma = std::is_same<T, float>::value && !B.persistent && tma_lx1(nx) &&
+               !((B.tma_off >> nx) & 1u);
+    for (int q = 0; q < np; ++q) {
+      if (hd[q].nx1 != nx) continue;
+      any = true;
+      tma = tma && B.probs[ids[q]]->mesh.use_tma && batch_tma_aligned(hd[q].ax);
+    }
+    if (!any) continue;
     const int g0 = (int)mapA.size();
     size_t gs = 0;
     for (int q = 0; q < np; ++q) {
-      if (hd[q].nx1 != nx) continue;
+      BDesc<T>& d = hd[q];
+      if (d.nx1 != nx) continue;
+      if (tma) {
+        d.epb = batch_tma_epb_rt(nx);
+        d.nblkA = (d.ax.nel + d.epb - 1) / d.epb;
+        gs = std::max(gs, batch_tma_smem(nx, d.ax.h1mode, d.ax.h2mode));
+      } else {
+        gs = std::max(gs, batch_smem<T>(nx, d.epb));
+      }
       baseA[q] = (int)mapA.size();
-      mapA.insert(mapA.end(), hd[q].nblkA, q);
-      gs = std::max(gs, batch_smem<T>(nx, hd[q].epb));
+      mapA.insert(mapA.end(), d.nblkA, q);
     }
-    if ((int)mapA.size() == g0) continue;
     L.gnx[L.ngrp] = nx;
     L.gstart[L.ngrp] = g0;
     L.gcount[L.ngrp] = (int)mapA.size() - g0;
     L.gsmem[L.ngrp] = gs;
+    L.gtma[L.ngrp] = tma ? 1 : 0;
     ++L.ngrp;
   }
   const size_t dbytes = sizeof(BDesc<T>) * np;
@@ -429,9 +526,31 @@ int batch_tables(Batch& B, const std::vector<int>& ids, const std::vector<Coef<T
   return 0;
 }
 
+// One even order's TMA-staged FP32 operator launch.
+template <int NX>
+cudaError_t batch_tma_nx(const BDesc<float>* D, const BatchLaunch& L, int g, cudaStream_t s) {
+  constexpr int EPB = batch_tma_epb<NX>();
+  static bool configured = false;  // room for the largest slice set
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(batch_axhelm_tma_kernel<NX, EPB>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)tma_smem_bytes<NX, float, EPB>(true, 1, 2));
+    if (e != cudaSuccess) return e;
+    cudaFuncSetAttribute(batch_axhelm_tma_kernel<NX, EPB>,
+                         cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    configured = true;
+  }
+  batch_axhelm_tma_kernel<NX, EPB><<<L.gcount[g], dim3(NX * NX, EPB), L.gsmem[g], s>>>(
+      D, L.mapA, L.baseA, L.gstart[g]);
+  return cudaSuccess;
+}
+
 // One order's operator launch.
 template <typename T, int NX>
 cudaError_t batch_ops_nx(const BDesc<T>* D, const BatchLaunch& L, int g, cudaStream_t s) {
+  if constexpr (std::is_same<T, float>::value && tma_lx1(NX)) {
+    if (L.gtma[g]) return batch_tma_nx<NX>(D, L, g, s);
+  }
   static bool configured = false;
   if (!configured) {
     cudaError_t e = cudaFuncSetAttribute(batch_axhelm_nx_kernel<T, NX>,
@@ -445,26 +564,31 @@ cudaError_t batch_ops_nx(const BDesc<T>* D, const BatchLaunch& L, int g, cudaStr
   return cudaSuccess;
 }
 
+// Operator launch g of a batched iteration (one order's problems).
+template <typename T>
+cudaError_t batch_op_group(const BatchLaunch& L, int g, cudaStream_t s) {
+  const BDesc<T>* D = reinterpret_cast<const BDesc<T>*>(L.desc);
+  count_launch();
+  switch (L.gnx[g]) {
+    case 2: return batch_ops_nx<T, 2>(D, L, g, s);
+    case 3: return batch_ops_nx<T, 3>(D, L, g, s);
+    case 4: return batch_ops_nx<T, 4>(D, L, g, s);
+    case 5: return batch_ops_nx<T, 5>(D, L, g, s);
+    case 6: return batch_ops_nx<T, 6>(D, L, g, s);
+    case 7: return batch_ops_nx<T, 7>(D, L, g, s);
+    case 8: return batch_ops_nx<T, 8>(D, L, g, s);
+    case 9: return batch_ops_nx<T, 9>(D, L, g, s);
+    case 10: return batch_ops_nx<T, 10>(D, L, g, s);
+    case 11: return batch_ops_nx<T, 11>(D, L, g, s);
+    default: return batch_ops_nx<T, 12>(D, L, g, s);
+  }
+}
+
 // The operator of one batched iteration: one launch per order present.
 template <typename T>
 cudaError_t batch_ops(const BatchLaunch& L, cudaStream_t s) {
-  const BDesc<T>* D = reinterpret_cast<const BDesc<T>*>(L.desc);
   for (int g = 0; g < L.ngrp; ++g) {
-    count_launch();
-    cudaError_t e = cudaSuccess;
-    switch (L.gnx[g]) {
-      case 2: e = batch_ops_nx<T, 2>(D, L, g, s); break;
-      case 3: e = batch_ops_nx<T, 3>(D, L, g, s); break;
-      case 4: e = batch_ops_nx<T, 4>(D, L, g, s); break;
-      case 5: e = batch_ops_nx<T, 5>(D, L, g, s); break;
-      case 6: e = batch_ops_nx<T, 6>(D, L, g, s); break;
-      case 7: e = batch_ops_nx<T, 7>(D, L, g, s); break;
-      case 8: e = batch_ops_nx<T, 8>(D, L, g, s); break;
-      case 9: e = batch_ops_nx<T, 9>(D, L, g, s); break;
-      case 10: e = batch_ops_nx<T, 10>(D, L, g, s); break;
-      case 11: e = batch_ops_nx<T, 11>(D, L, g, s); break;
-      default: e = batch_ops_nx<T, 12>(D, L, g, s); break;
-    }
+    const cudaError_t e = batch_op_group<T>(L, g, s);
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
@@ -483,7 +607,54 @@ cudaError_t batch_enqueue(Batch& B, const BatchLaunch& L, int k) {
   return cudaGetLastError();
 }
 
-// Runs the batched PCG for the listed problems until each has stopped.
+// FP32: per order, the TMA-staged body or the plain one, whichever times
+// faster on this problem set (3 launches of the order's operator each; the
+// two bodies compute the same numbers).  Sets B.tma_off.
+template <typename T>
+int batch_tune_tma(Batch& B, const std::vector<int>& ids, const std::vector<Coef<T>>& coef,
+                   const std::vector<T*>& xs, const std::vector<const T*>& mults,
+                   const std::vector<const T*>& binvs) {
+  float t[2][NEKGPU_MAX_LX1 + 1];
+  int tma_at[NEKGPU_MAX_LX1 + 1] = {};
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return -3;
+  const unsigned masks[2] = {0u, ~0u};  // TMA wherever it applies / nowhere
+  for (int v = 0; v < 2; ++v) {
+    for (int nx = 0; nx <= NEKGPU_MAX_LX1; ++nx) t[v][nx] = 1e30f;
+    B.tma_off = masks[v];
+    BatchLaunch L;
+    int rc = batch_tables<T>(B, ids, coef, xs, mults, binvs, L);
+    cudaError_t e = cudaSuccess;
+    for (int g = 0; g < L.ngrp && !rc && e == cudaSuccess; ++g) {
+      if (v == 0) tma_at[L.gnx[g]] = L.gtma[g];
+      if (!tma_at[L.gnx[g]]) continue;  // one body only: nothing to compare
+      e = batch_op_group<T>(L, g, B.stream);  // warm-up
+      cudaEventRecord(e0, B.stream);
+      for (int q = 0; q < 3 && e == cudaSuccess; ++q) e = batch_op_group<T>(L, g, B.stream);
+      cudaEventRecord(e1, B.stream);
+      if (e == cudaSuccess) e = cudaGetLastError();
+      float ms = 0.f;
+      if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+      t[v][L.gnx[g]] = ms;
+    }
+    if (rc || e != cudaSuccess) {
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      B.tma_off = 0u;
+      if (!rc) B.err = std::string("batch autotune: ") + cudaGetErrorString(e);
+      return rc ? rc : -3;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  unsigned off = 0u;
+  for (int nx = 0; nx <= NEKGPU_MAX_LX1; ++nx)
+    if (tma_at[nx] && t[1][nx] < t[0][nx]) off |= 1u << nx;
+  B.tma_off = off;
+  return 0;
+}
+
 // Picks the operator block size for a problem set: times a batched operator
 // launch for every candidate (128 or 256 threads; 128 only when every
 // element slab fits) and keeps the fastest, once per problem set and
@@ -557,6 +728,10 @@ int batch_tune(Batch& B, const std::vector<int>& ids, const std::vector<Coef<T>>
   }
   B.threads[prec] = best;
   B.tune_ms[prec] = best_ms;
+  if (prec == 1) {
+    const int rc = batch_tune_tma<T>(B, ids, coef, xs, mults, binvs);
+    if (rc) return rc;
+  }
   B.tkey[prec] = key;
   return 0;
 }
@@ -656,7 +831,7 @@ int batch_iterate(Batch& B, const std::vector<int>& ids, const BatchLaunch& L, b
                               L.threadsA,
                               (int64_t)(uintptr_t)L.desc, (int64_t)(uintptr_t)L.mapA, B.chunk};
   for (int g = 0; g < L.ngrp; ++g)  // the operator launches' shapes are baked into the graph
-    key.insert(key.end(), {L.gnx[g], L.gstart[g], L.gcount[g], (int64_t)L.gsmem[g]});
+    key.insert(key.end(), {L.gnx[g], L.gstart[g], L.gcount[g], (int64_t)L.gsmem[g], L.gtma[g]});
   if (graph && (!B.gexec || key != B.gkey)) {
     if (B.gexec) cudaGraphExecDestroy(B.gexec);
     B.gexec = nullptr;

@@ -43,7 +43,7 @@ std::vector<AxShapeSel> ax_candidates(int nx, int prec, bool tma) {
     s.epb = emax;
     v.push_back(s);
   }
-  if (prec == 1 && tma && nx % 2 == 0)
+  if (prec == 1 && tma && tma_lx1(nx))
     for (int e : tma_candidates(nx)) {
       AxShapeSel s;
       s.kind = 1;
@@ -63,7 +63,7 @@ AxShapeSel ax_shape_in_use(const Mesh& m, int prec) {
 
 namespace {
 
-using Key = std::tuple<int, int, int, int, int, int, int>;  // dev, nx, nel, prec, h1m, h2m, tma
+using Key = std::tuple<int, int, int, int, int, int, int>;  // dev, nx, nel, prec, h1m, h2m, form
 std::mutex g_mu;
 std::map<Key, AxShapeSel> g_cache;
 std::map<Key, std::pair<int, int>> g_gs_cache;  // boundary-group kernel (threads, gshift)
@@ -80,7 +80,9 @@ int tune_operator(Handle& h, const OpData<T>& op, PcgWork<T>& wk, const Coef<T>&
   Mesh& m = h.mesh;
   const int prec = sizeof(T) == 4 ? 1 : 0;
   if (!h.autotune || m.ax_sel[prec].kind >= 0) return 0;
-  const Key key{h.device, m.nx1, m.nel, prec, c.h1mode, c.h2mode, (int)m.use_tma};
+  // FP32 launches depend on the TMA option, FP64 ones on the double-float one
+  const int form = prec ? (int)m.use_tma : (int)(m.use_df && m.has_df);
+  const Key key{h.device, m.nx1, m.nel, prec, c.h1mode, c.h2mode, form};
   {
     std::lock_guard<std::mutex> lk(g_mu);
     auto it = g_cache.find(key);

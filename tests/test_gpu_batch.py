@@ -16,7 +16,7 @@ CASES = [  # (lx1, kx, ky, kz, periodic, h2)
     (6, 2, 3, 2, (False, False, False), 0.0),
     (8, 3, 2, 2, (False, True, True), 10.0),
     (10, 2, 2, 2, (False, False, False), 1500.0),
-    (7, 2, 2, 3, (False, False, False), 0.0),
+    (7, 3, 3, 2, (False, False, False), 0.0),  # 18 elements: a ragged block of 4
     (9, 2, 2, 2, (False, False, False), 1.0),
     (8, 2, 2, 2, (False, False, False), 0.0),  # zero right-hand side
 ]
@@ -134,8 +134,8 @@ def test_batch_block_sizes_give_identical_solves(problems):
 
 @pytest.mark.parametrize("mixed", [0, 1])
 def test_persistent_launch_equals_graph_launches(gpu_lib, oracle, problems, mixed):
-    """The persistent cooperative form (nekgpu_batch_set_persistent 1, the
-    default) and the three-launch graph form run the same per-problem
+    """The persistent cooperative form (nekgpu_batch_set_persistent 1) and
+    the graph-replayed launches (the default) run the same per-problem
     arithmetic: identical iteration counts, norms and solutions, bit for
     bit, FP64 and mixed."""
     torch = pytest.importorskip("torch")

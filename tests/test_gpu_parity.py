@@ -82,13 +82,16 @@ def test_axhelm_exact_bitwise_all_orders(gpu_lib, oracle, nx1):
         assert np.array_equal(au, P["ops"].axhelm(u, h1, h2))
 
 
+@pytest.mark.parametrize("df", [1, 0])
 @pytest.mark.parametrize("tma", [1, 0])
 @pytest.mark.parametrize("nx1", [2, 3, 4, 6, 8, 9, 10, 12])
-def test_axhelm_fma_within_tolerance(gpu_lib, oracle, nx1, tma):
-    """Default (fused multiply-add) operator, TMA-staged (even lx1) or plain loads."""
+def test_axhelm_fma_within_tolerance(gpu_lib, oracle, nx1, tma, df):
+    """Default (fused multiply-add) operator, TMA-staged (even lx1) or plain
+    loads, with double-float contractions (the default) or FP64 ones."""
     P = oracle.box_problem(nx1, 3, 2, 2, v=rng_unit_vector(20 + nx1))
     lib = _setup(gpu_lib, P)
     lib.set_option(5, tma)
+    lib.set_option(10, df)
     n = P["n"]
     rng = np.random.default_rng(11)
     u = rng.standard_normal(n)

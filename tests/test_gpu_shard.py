@@ -1,8 +1,9 @@
 """The solve split over element shards on the device: two DeviceShards
 (two library handles on disjoint element slabs) in one process, their
 interface sums exchanged in shard order (LocalExchange; no kernel waits on
-another shard's), against the library's single-domain cggo on the same
-problem: iterations to +-1, solutions to 1e-9 relative."""
+another shard's), against the oracle's cggo (core/hmholtz.f:611-846) and the
+library's single-domain cggo on the same problem: iterations to +-1,
+solutions to 1e-9 relative."""
 import numpy as np
 import pytest
 
@@ -45,5 +46,9 @@ def test_two_device_shards_match_the_single_domain(gpu_lib, oracle, case):
     for i, xi in zip(idxs, x):
         xs[i] = xi.cpu().numpy()
     xh = xf.cpu().numpy()
+    x_ref, it_ref, _, _ = P["ops"].cggo(f, h1, h2, P["mask"], P["mult"], P["binv"], -1e-10,
+                                        maxcg=10 ** 5)
+    assert abs(it - it_ref) <= 1, (it, it_ref)
+    assert np.linalg.norm(xs - x_ref) <= 1e-9 * np.linalg.norm(x_ref)
     assert abs(it - itf) <= 1, (it, itf)
     assert np.linalg.norm(xs - xh) <= 1e-9 * np.linalg.norm(xh)
