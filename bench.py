@@ -354,7 +354,6 @@ def run_gpu(args):
     mask, mult, binv = dev(M["mask"]), dev(M["mult"]), dev(M["binv"])
     x = torch.zeros(n, dtype=torch.float64, device=f"cuda:{local}")
     big = 10 ** 6
-    lib.set_option(2, 1)  # timing: solve-total and per-launch operator events
     lib.set_option(7, args.mixed_mode)
     lib.set_option(9, 1 if args.split else 0)
     for prec, spec in ((0, args.fp64_shape), (1, args.fp32_shape)):
@@ -375,32 +374,50 @@ def run_gpu(args):
         return (no, ni), rc
 
     def timed(solve):
+        """Warm-up, then the timed steps with the library's per-kernel timing
+        off (the PCG chunks replay as CUDA graphs): CUDA events on the calling
+        stream around each call (every call waits for that stream's earlier
+        work and returns with its own finished).  Then two more solves outside
+        the timed region with per-kernel timing on (direct launches bracketed
+        by events) for the kernel breakdown."""
+        lib.set_option(2, 0)
         for _ in range(args.warmup):
             solve()
         barrier(pg)
         torch.cuda.synchronize()
         l0 = lib.launch_count()
-        its, ms_tot, ms_ax, n_ax, ms_gs, ms_up = [], 0.0, 0.0, 0, 0.0, 0.0
+        its, ms_tot = [], 0.0
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(args.steps)]
         with Clocks(local) as ck:
-            for _ in range(args.steps):
+            for q in range(args.steps):
+                ev[q][0].record()
                 it, rc = solve()
+                ev[q][1].record()
                 if rc != 0:
                     raise RuntimeError(f"solve did not converge: {lib.last_error()}")
-                t_tot, t_ax, k_ax = lib.last_timing()
-                _, t_gs, t_up, _ = lib.last_kernel_times()
                 its.append(it)
-                ms_tot += t_tot
-                ms_ax += t_ax
-                n_ax += k_ax
-                ms_gs += t_gs
-                ms_up += t_up
-        torch.cuda.synchronize()
+            torch.cuda.synchronize()
+        launches = lib.launch_count() - l0
+        ms_tot = sum(a.elapsed_time(b) for a, b in ev)
         barrier(pg)
+        lib.set_option(2, 1)  # breakdown runs (not timed)
+        ms_ax = ms_gs = ms_up = 0.0
+        n_ax = 0
+        for _ in range(2):
+            solve()
+            _, t_ax, k_ax = lib.last_timing()
+            _, t_gs, t_up, _ = lib.last_kernel_times()
+            ms_ax += t_ax
+            n_ax += k_ax
+            ms_gs += t_gs
+            ms_up += t_up
+        lib.set_option(2, 0)
         k = max(n_ax, 1)
         return dict(iters=its, T=allmax(pg, ms_tot / 1e3), ms_ax=ms_ax / k, n_ax=n_ax,
                     per_iter_ms={"operator": ms_ax / k, "boundary_groups": ms_gs / k,
                                  "update": ms_up / k},
-                    launches=lib.launch_count() - l0, clocks=ck.summary())
+                    launches=launches, clocks=ck.summary())
 
     peak, peak_src = peaks()
     flops_pt = 12 * M["lx1"] + 25
@@ -518,28 +535,33 @@ def run_gpu(args):
         rhs = pin(M["rhs"])
         u = pin(np.zeros(n))
 
-        def e2e(call):
+        per_call = {}
+
+        def e2e(call, name):
             np.copyto(rhs, rhs0)
             call()  # warm the staging buffers
-            tot, cnt = 0.0, 0
+            tot, ms = 0.0, []
             barrier(pg)
             for _ in range(args.steps):
                 np.copyto(rhs, rhs0)
                 t0 = time.perf_counter()
                 call()
-                tot += time.perf_counter() - t0
-                cnt += 1
+                dt = time.perf_counter() - t0
+                tot += dt
+                ms.append(round(1e3 * dt, 2))
             barrier(pg)
+            per_call[name] = ms
             return allmax(pg, tot)
 
         tm = e2e(lambda: lib.hmholtz_mixed("TEMP", u, rhs, hb["h1"], hb["h2"], hb["mask"],
                                            hb["mult"], 1, -args.tol, big, 1, hb["binv"],
-                                           inner_tol=args.inner_tol))
+                                           inner_tol=args.inner_tol), "mixed")
         t6 = e2e(lambda: lib.hmholtz("TEMP", u, rhs, hb["h1"], hb["h2"], hb["mask"], hb["mult"], 1,
-                                     -args.tol, big, 1, hb["binv"], maxcg=big))
+                                     -args.tol, big, 1, hb["binv"], maxcg=big), "fp64")
         line["e2e"] = {"value": allsum(pg, n * it64 * args.steps) / tm, "unit": "DOF-iters/s",
                        "h2d_bytes_per_step": 6 * 8 * n, "d2h_bytes_per_step": 2 * 8 * n,
-                       "api": "nekgpu_hmholtz_mixed (host arrays, pinned)"}
+                       "api": "nekgpu_hmholtz_mixed (host arrays, pinned)",
+                       "ms_per_call": per_call["mixed"]}
         fp64_block["e2e"] = {"value": allsum(pg, n * it64 * args.steps) / t6,
                              "unit": "DOF-iters/s", "api": "nekgpu_hmholtz (host arrays, pinned)"}
     # ---- CPU baseline (oracle) on rank 0, N=1 only ------------------------------
@@ -619,7 +641,9 @@ def run_batch(args):
                        inner_tol=args.inner_tol)
 
     out = {}
-    for mixed in (False, True):
+    # --only-mixed (profiling runs): the FP64 leg is skipped, and the value is
+    # counted with the mixed solve's inner iterations
+    for mixed in ((True,) if args.only_mixed else (False, True)):
         for _ in range(args.warmup):
             solve(mixed)
         barrier(pg)
@@ -633,6 +657,8 @@ def run_batch(args):
         if any(s != 0 for s in res["status"]):
             raise RuntimeError(f"batch: status {res['status']}: {B.last_error()}")
         out[mixed] = dict(res=res, T=T, clocks=ck.summary())
+    if args.only_mixed:
+        out[False] = dict(res=out[True]["res"], T=float("nan"), clocks=None)
     it64 = np.array(out[False]["res"]["niter"], dtype=np.float64)
     v64 = allsum(pg, float((ns * it64).sum()) * args.steps) / out[False]["T"]
     vmx = allsum(pg, float((ns * it64).sum()) * args.steps) / out[True]["T"]
@@ -656,12 +682,14 @@ def run_batch(args):
                                  ("fp64 residual replacement, search direction kept"
                                   if args.mixed_mode == 1 else "restarted per outer step"),
                        "operator_block_threads": {"fp64": B.shape(0)[0], "fp32": B.shape(1)[0],
-                                                  "note": "autotuned on the first solve "
-                                                          "(graph form); 256 in the "
-                                                          "persistent form"},
+                                                  "note": "plain operator body, autotuned on "
+                                                          "the first solve (graph form); 256 "
+                                                          "in the persistent form"},
                        "launch_form": ("one persistent cooperative launch per segment"
                                        if args.persistent_batch else
-                                       "three launches per iteration, graph-replayed"),
+                                       "per iteration one operator launch per order (FP32: "
+                                       "TMA-staged or plain body, tuned per order) + "
+                                       "boundary-group + update, graph-replayed"),
                        "parallelism": f"replicas{ws}"},
             "fp64": {"value": v64, "unit": "DOF-iters/s",
                      "ms_per_step": 1e3 * out[False]["T"] / args.steps},

@@ -19,9 +19,10 @@
 //   * the element-local result hi + lo is formed in FP64, where the mass
 //     term h2 B p, the PCG's p update and its rho dot product stay.
 //
-// Per point this leaves about ten FP64 operations (the p update, the split,
-// the recombination, the mass term) against 121 in the FP64 kernel; the rest
-// runs on the FP32 pipe.  The result differs from the FP64 operator by a few
+// Per point this leaves about six FP64 operations (the p update, the
+// recombination, the mass term, the rho dot) against 121 in the FP64 kernel;
+// the conversions of the split and the recombination are integer operations
+// (df_split_int, df_widen), the rest runs on the FP32 pipe.  The result differs from the FP64 operator by a few
 // units in 2^-48 of the magnitude of the summed terms.
 #pragma once
 #include "axhelm.cuh"
@@ -38,6 +39,48 @@ __device__ __forceinline__ DfPair df_split(double v) {
 }
 
 __device__ __forceinline__ double df_join(float h, float l) { return (double)h + (double)l; }
+
+// The same split and join with the conversions done by integer operations.
+// On GB300 FP32 <-> FP64 conversions issue on the FP64 pipe (2 results per
+// clock per SM); split and join took about five of them per point, more pipe
+// time than the operator's FP64 arithmetic.
+//
+// Split: |v|'s bit pattern rounded at bit 29 (half away from zero; a carry
+// runs into the exponent, as the value does) is hi's significand and
+// exponent; |v| - |hi| is the integer difference of the two patterns in units
+// of ulp(v) (at most 2^28 in magnitude), so lo = fl32(that integer) * ulp(v)
+// is fl32(v - hi) exactly.  hi equals fl32(v) except at exact ties, where it
+// is the other neighbour and lo keeps the pair exact.  Outside
+// 2^-74 <= |v| < 2^126 (ulp(v) or hi out of the FP32 normal range), and for
+// infinities and NaN, the FP64 form runs.
+__device__ __forceinline__ DfPair df_split_int(double v) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  const unsigned long long a = b & 0x7FFFFFFFFFFFFFFFull;
+  const float sgn = (b >> 63) ? -1.0f : 1.0f;
+  if (a == 0ull) return {sgn * 0.0f, 0.0f};
+  const int E = (int)(a >> 52);
+  if (E < 949 || E > 1149) return df_split(v);
+  const unsigned long long r = (a + (1ull << 28)) & ~((1ull << 29) - 1ull);
+  const float h = __uint_as_float((unsigned int)((r >> 29) - (896ull << 23)));
+  const int rem = (int)(long long)(a - r);
+  const float l = __int2float_rn(rem) * __int_as_float((E - 948) << 23);
+  return {sgn * h, sgn * l};
+}
+
+// (double)f by assembling the FP64 bit pattern (normal f and zeros; others
+// convert).
+__device__ __forceinline__ double df_widen(float f) {
+  const unsigned int u = __float_as_uint(f);
+  const unsigned int e = (u >> 23) & 0xFFu;
+  if (e == 0u && (u & 0x7FFFFFu) == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
+  if (e == 0u || e == 0xFFu) return (double)f;
+  const unsigned int hi = (u & 0x80000000u) | ((e + 896u) << 20) | ((u >> 3) & 0xFFFFFu);
+  return __hiloint2double((int)hi, (int)(u << 29));
+}
+
+__device__ __forceinline__ double df_join_int(float h, float l) {
+  return df_widen(h) + df_widen(l);
+}
 
 // (sh, sl) += (ah, al) * (bh, bl): TwoProduct of the high parts, the cross
 // products into its error, TwoSum into the running sum; sl gathers the
@@ -82,7 +125,10 @@ __device__ __forceinline__ void df_add(float& sh, float& sl, float ah, float al)
 }
 
 // Shared memory of the kernel: D and D^T pairs (padded rows), then three
-// padded slabs of pairs per element.
+// padded slabs of pairs per element.  (Staging the block's G pairs in shared
+// memory as well, by one bulk copy, measured slower on GB300: 1.25 against
+// 0.87 ms per launch at E=32^3 N=7, the larger blocks halving the resident
+// warps.)
 template <int NX>
 __host__ __device__ constexpr size_t axhelm_df_smem_bytes(int epb) {
   return (size_t)(2 * NX * (NX + 1) + epb * 3 * AxShape<NX>::LP) * sizeof(float2);
@@ -149,7 +195,7 @@ __device__ __forceinline__ void axhelm_df_body(const DfArgs& A, int blk, int tx,
       }
     }
     ru64[k] = v;
-    const DfPair s = df_split(v);
+    const DfPair s = df_split_int(v);
     ruh[k] = s.h;
     rul[k] = s.l;
     if (ty < epb) su[k * NX * R + j * R + i] = make_float2(s.h, s.l);
@@ -158,8 +204,19 @@ __device__ __forceinline__ void axhelm_df_body(const DfArgs& A, int blk, int tx,
 
   float rauh[NX], raul[NX];
   const float2* __restrict__ g = A.Gdf + (size_t)(act ? e : 0) * 6 * P;
+  // G pairs of plane k are loaded one plane ahead, so that their latency
+  // hides behind plane k - 1's contractions
+  float2 gn[6];
+  auto load_g = [&](int k) {
+    const int pt = k * NXY + j * NX + i;
+#pragma unroll
+    for (int q = 0; q < 6; ++q) gn[q] = act ? __ldg(g + q * P + pt) : make_float2(0.f, 0.f);
+  };
+  load_g(0);
 #pragma unroll
   for (int k = 0; k < NX; ++k) {
+    const float2 g1 = gn[0], g2 = gn[1], g3 = gn[2], g4 = gn[3], g5 = gn[4], g6 = gn[5];
+    if (k + 1 < NX) load_g(k + 1);
     const float2* slab = su + k * NX * R;
     float urh, url, ush, usl, uth, utl;
     {
@@ -195,17 +252,8 @@ __device__ __forceinline__ void axhelm_df_body(const DfArgs& A, int blk, int tx,
       df_norm(uth, utl);
     }
     const int pt = k * NXY + j * NX + i;
-    float2 g1 = make_float2(0.f, 0.f), g2 = g1, g3 = g1, g4 = g1, g5 = g1, g6 = g1;
     DfPair h = h1c;
-    if (act) {
-      g1 = __ldg(g + pt);
-      g2 = __ldg(g + P + pt);
-      g3 = __ldg(g + 2 * P + pt);
-      g4 = __ldg(g + 3 * P + pt);
-      g5 = __ldg(g + 4 * P + pt);
-      g6 = __ldg(g + 5 * P + pt);
-      if (a.h1mode) h = df_split(__ldg(a.h1 + eo + pt));
-    }
+    if (act && a.h1mode) h = df_split_int(__ldg(a.h1 + eo + pt));
     // col3 / addcol3 order of hmholtz.f:199-206
     float t1h, t1l, t2h, t2l, t3h, t3l;
     df_mul(t1h, t1l, urh, url, g1.x, g1.y);
@@ -271,7 +319,7 @@ __device__ __forceinline__ void axhelm_df_body(const DfArgs& A, int blk, int tx,
     // au = (tm1 + tm2) + tm3  (:215-217)
     df_add(ah, al, bh, bl);
     df_add(ah, al, rauh[k], raul[k]);
-    double s = df_join(ah, al);
+    double s = df_join_int(ah, al);
     const int pt = k * NXY + j * NX + i;
     if (act) {
       if (a.h2mode) {  // addcol4(au,helm2,bm1,u) (:225), in FP64

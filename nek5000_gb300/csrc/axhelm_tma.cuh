@@ -152,7 +152,7 @@ __device__ __forceinline__ void axhelm_tma_body(const AxArgs<T>& a, int blk,
   const int wl = whole ? ne * P : (du + ne * P + U - 1) / U * U;
   const int wlg = whole ? 6 * ne * P : (dg + 6 * ne * P + U - 1) / U * U;
   const size_t n = (size_t)a.nel * P;
-  const bool bulk = off - du + wl <= n && 6 * off - dg + wlg <= 6 * n;
+  const bool bulk = whole || (off - du + wl <= n && 6 * off - dg + wlg <= 6 * n);
   if (!bulk) {
     const int nv = ne * P, nt = NXY * EPB;
     for (int q = tid; q < nv; q += nt) {
