@@ -322,8 +322,16 @@ __device__ __forceinline__ void axhelm_tma_body(const AxArgs<T>& a, int blk,
   if (tid == 0 && ok) mbar_inval(bar);
 }
 
+// lx1 = 10, one element per block: at least 5 resident blocks (96 registers,
+// 20 warps per SM) instead of the 4 that 128 registers allow.
+template <int NX, int EPB>
+__host__ __device__ constexpr int tma_min_blocks() {
+  return (NX == 10 && EPB == 1) ? 5 : 1;
+}
+
 template <int NX, typename T, bool FUSED, int EPB>
-__global__ void __launch_bounds__(NX* NX* EPB) axhelm_tma_kernel(const AxArgs<T> a) {
+__global__ void __launch_bounds__(NX* NX* EPB, tma_min_blocks<NX, EPB>())
+    axhelm_tma_kernel(const AxArgs<T> a) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   axhelm_tma_body<NX, T, FUSED, EPB>(a, blockIdx.x, smem_raw);
 }

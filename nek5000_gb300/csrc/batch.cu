@@ -92,7 +92,7 @@ __host__ __device__ constexpr int batch_tma_epb() {
 // The TMA-staged FP32 operator for the problems of one order (blocks of
 // (NX*NX, EPB) threads; virtual blocks as batch_axhelm_nx_kernel).
 template <int NX, int EPB>
-__global__ void __launch_bounds__(NX* NX* EPB)
+__global__ void __launch_bounds__(NX* NX* EPB, tma_min_blocks<NX, EPB>())
     batch_axhelm_tma_kernel(const BDesc<float>* __restrict__ D, const int* __restrict__ map,
                             const int* __restrict__ base, int start) {
   extern __shared__ __align__(128) unsigned char smem_tma[];
@@ -356,8 +356,13 @@ struct Batch {
   std::vector<int64_t> tkey[2];
   float tune_ms[2] = {0.f, 0.f};
   // FP32 orders (bit lx1) whose operator launch keeps the plain body although
-  // the TMA-staged one applies: batch_tune found it faster there
+  // the TMA-staged one applies: batch_tune found it faster there.  tma_pick
+  // keeps each order's verdict (-1 not timed yet, 0 plain, 1 TMA) for the
+  // life of the batch, so that the subsets of problems a mixed solve runs as
+  // others converge do not re-decide it on fewer blocks.
   unsigned tma_off = 0u;
+  int tma_pick[NEKGPU_MAX_LX1 + 1];
+  Batch() { std::fill(tma_pick, tma_pick + NEKGPU_MAX_LX1 + 1, -1); }
 };
 
 namespace {
@@ -608,49 +613,67 @@ cudaError_t batch_enqueue(Batch& B, const BatchLaunch& L, int k) {
 }
 
 // FP32: per order, the TMA-staged body or the plain one, whichever times
-// faster on this problem set (3 launches of the order's operator each; the
-// two bodies compute the same numbers).  Sets B.tma_off.
+// faster (the two bodies compute the same numbers).  An order is timed the
+// first time it appears in a problem set, in three interleaved rounds of 3
+// launches of its operator per body, each body keeping its best round; the
+// verdict sticks (Batch::tma_pick).  Sets B.tma_off.
 template <typename T>
 int batch_tune_tma(Batch& B, const std::vector<int>& ids, const std::vector<Coef<T>>& coef,
                    const std::vector<T*>& xs, const std::vector<const T*>& mults,
                    const std::vector<const T*>& binvs) {
   float t[2][NEKGPU_MAX_LX1 + 1];
   int tma_at[NEKGPU_MAX_LX1 + 1] = {};
-  cudaEvent_t e0 = nullptr, e1 = nullptr;
-  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return -3;
-  const unsigned masks[2] = {0u, ~0u};  // TMA wherever it applies / nowhere
-  for (int v = 0; v < 2; ++v) {
+  for (int v = 0; v < 2; ++v)
     for (int nx = 0; nx <= NEKGPU_MAX_LX1; ++nx) t[v][nx] = 1e30f;
-    B.tma_off = masks[v];
+  bool undecided = false;
+  {  // orders present where the TMA body applies and no verdict exists yet
+    B.tma_off = 0u;
     BatchLaunch L;
-    int rc = batch_tables<T>(B, ids, coef, xs, mults, binvs, L);
-    cudaError_t e = cudaSuccess;
-    for (int g = 0; g < L.ngrp && !rc && e == cudaSuccess; ++g) {
-      if (v == 0) tma_at[L.gnx[g]] = L.gtma[g];
-      if (!tma_at[L.gnx[g]]) continue;  // one body only: nothing to compare
-      e = batch_op_group<T>(L, g, B.stream);  // warm-up
-      cudaEventRecord(e0, B.stream);
-      for (int q = 0; q < 3 && e == cudaSuccess; ++q) e = batch_op_group<T>(L, g, B.stream);
-      cudaEventRecord(e1, B.stream);
-      if (e == cudaSuccess) e = cudaGetLastError();
-      float ms = 0.f;
-      if (e == cudaSuccess) e = cudaEventSynchronize(e1);
-      if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
-      t[v][L.gnx[g]] = ms;
-    }
-    if (rc || e != cudaSuccess) {
-      cudaEventDestroy(e0);
-      cudaEventDestroy(e1);
-      B.tma_off = 0u;
-      if (!rc) B.err = std::string("batch autotune: ") + cudaGetErrorString(e);
-      return rc ? rc : -3;
+    const int rc = batch_tables<T>(B, ids, coef, xs, mults, binvs, L);
+    if (rc) return rc;
+    for (int g = 0; g < L.ngrp; ++g) {
+      tma_at[L.gnx[g]] = L.gtma[g] && B.tma_pick[L.gnx[g]] < 0;
+      undecided = undecided || tma_at[L.gnx[g]];
     }
   }
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
+  if (undecided) {
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return -3;
+    const unsigned masks[2] = {0u, ~0u};  // TMA wherever it applies / nowhere
+    for (int round = 0; round < 3; ++round)
+      for (int v = 0; v < 2; ++v) {
+        B.tma_off = masks[v];
+        BatchLaunch L;
+        int rc = batch_tables<T>(B, ids, coef, xs, mults, binvs, L);
+        cudaError_t e = cudaSuccess;
+        for (int g = 0; g < L.ngrp && !rc && e == cudaSuccess; ++g) {
+          if (!tma_at[L.gnx[g]]) continue;
+          e = batch_op_group<T>(L, g, B.stream);  // warm-up
+          cudaEventRecord(e0, B.stream);
+          for (int q = 0; q < 3 && e == cudaSuccess; ++q) e = batch_op_group<T>(L, g, B.stream);
+          cudaEventRecord(e1, B.stream);
+          if (e == cudaSuccess) e = cudaGetLastError();
+          float ms = 0.f;
+          if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+          if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+          t[v][L.gnx[g]] = std::min(t[v][L.gnx[g]], ms);
+        }
+        if (rc || e != cudaSuccess) {
+          cudaEventDestroy(e0);
+          cudaEventDestroy(e1);
+          B.tma_off = 0u;
+          if (!rc) B.err = std::string("batch autotune: ") + cudaGetErrorString(e);
+          return rc ? rc : -3;
+        }
+      }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    for (int nx = 0; nx <= NEKGPU_MAX_LX1; ++nx)
+      if (tma_at[nx]) B.tma_pick[nx] = t[1][nx] < t[0][nx] ? 0 : 1;
+  }
   unsigned off = 0u;
   for (int nx = 0; nx <= NEKGPU_MAX_LX1; ++nx)
-    if (tma_at[nx] && t[1][nx] < t[0][nx]) off |= 1u << nx;
+    if (B.tma_pick[nx] == 0) off |= 1u << nx;
   B.tma_off = off;
   return 0;
 }
