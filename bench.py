@@ -685,6 +685,8 @@ def run_batch(args):
                                                   "note": "plain operator body, autotuned on "
                                                           "the first solve (graph form); 256 "
                                                           "in the persistent form"},
+                       "fp32_operator_form_by_lx1": {str(k): ("tma" if v else "plain")
+                                                     for k, v in B.operator_forms().items()},
                        "launch_form": ("one persistent cooperative launch per segment"
                                        if args.persistent_batch else
                                        "per iteration one operator launch per order (FP32: "

@@ -553,6 +553,12 @@ int nekgpu_batch_shape(const int64_t *batch, const int *precision, int *threads,
  * identical).  No reference counterpart. */
 int nekgpu_batch_set_persistent(const int64_t *batch, const int *on);
 int nekgpu_batch_set_shape(const int64_t *batch, const int *precision, const int *threads);
+/* The FP32 operator body each polynomial order runs in the batch:
+ * forms[lx1] (NEKGPU_MAX_LX1 + 1 entries) is 1 for the TMA-staged body, 0
+ * for the plain one, -1 where no order lx1 has been timed yet (the first
+ * mixed solve times every order present where the TMA body applies, and the
+ * verdict stays for the batch).  No reference counterpart. */
+int nekgpu_batch_operator_forms(const int64_t *batch, int *forms);
 int nekgpu_batch_last_error(const int64_t *batch, char *buf, const int *buflen);
 int nekgpu_batch_destroy(int64_t *batch);
 

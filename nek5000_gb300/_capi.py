@@ -131,6 +131,7 @@ SIGNATURES = {
     "nekgpu_launch_count": [_I64P],
     "nekgpu_autotune": [_I64P, _IP, _IP, _IP, _IP, _IP, _DP],
     "nekgpu_batch_shape": [_I64P, _IP, _IP, _DP],
+    "nekgpu_batch_operator_forms": [_I64P, _IP],
     "nekgpu_last_kernel_times": [_I64P, _DP, _DP, _DP, _IP],
     "nekgpu_hsolve_dev": [_I64P, _IP, _P, _P, _P, _P, _P, _P, _IP, _DP, _IP, _IP, _P, _IP, _IP,
                           _DP, _DP, _IP],

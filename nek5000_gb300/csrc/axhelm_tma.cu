@@ -6,23 +6,30 @@
 namespace nekgpu {
 namespace {
 
+// The kernel of a shape (lx1 = 10 with one element per block has its own
+// register bound).
+template <int NX, bool FUSED, int EPB>
+constexpr auto tma_kernel() {
+  if constexpr (NX == 10 && EPB == 1) return axhelm_tma_kernel_10x1<float, FUSED>;
+  else return axhelm_tma_kernel<NX, float, FUSED, EPB>;
+}
+
 template <int NX, bool FUSED, int EPB>
 cudaError_t launch_one(const Mesh& m, const AxArgs<float>& a, int* nparts, cudaStream_t s) {
   const size_t smem = tma_smem_bytes<NX, float, EPB>(FUSED, a.h1mode, a.h2mode);
+  auto kern = tma_kernel<NX, FUSED, EPB>();
   static bool configured = false;  // per instantiation: room for the largest slice set
   if (!configured) {
     const int maxb = (int)tma_smem_bytes<NX, float, EPB>(true, 1, 2);
-    cudaError_t e = cudaFuncSetAttribute(axhelm_tma_kernel<NX, float, FUSED, EPB>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, maxb);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, maxb);
     if (e != cudaSuccess) return e;
-    cudaFuncSetAttribute(axhelm_tma_kernel<NX, float, FUSED, EPB>,
-                         cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     configured = true;
   }
   const int nb = (m.nel + EPB - 1) / EPB;
   if (nparts) *nparts = m.nel;
   count_launch();
-  axhelm_tma_kernel<NX, float, FUSED, EPB><<<nb, dim3(NX * NX, EPB), smem, s>>>(a);
+  kern<<<nb, dim3(NX * NX, EPB), smem, s>>>(a);
   return cudaGetLastError();
 }
 

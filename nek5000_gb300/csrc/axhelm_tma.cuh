@@ -322,18 +322,21 @@ __device__ __forceinline__ void axhelm_tma_body(const AxArgs<T>& a, int blk,
   if (tid == 0 && ok) mbar_inval(bar);
 }
 
-// lx1 = 10, one element per block: at least 5 resident blocks (96 registers,
-// 20 warps per SM) instead of the 4 that 128 registers allow.
-template <int NX, int EPB>
-__host__ __device__ constexpr int tma_min_blocks() {
-  return (NX == 10 && EPB == 1) ? 5 : 1;
-}
-
 template <int NX, typename T, bool FUSED, int EPB>
-__global__ void __launch_bounds__(NX* NX* EPB, tma_min_blocks<NX, EPB>())
-    axhelm_tma_kernel(const AxArgs<T> a) {
+__global__ void __launch_bounds__(NX* NX* EPB) axhelm_tma_kernel(const AxArgs<T> a) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   axhelm_tma_body<NX, T, FUSED, EPB>(a, blockIdx.x, smem_raw);
+}
+
+// lx1 = 10 with one element per block: at least 5 resident blocks (96
+// registers, 20 warps per SM) instead of the 4 that the 128 registers of the
+// kernel above allow.  (A minimum-blocks bound on every shape is not
+// neutral: with a minimum of 1 ptxas gives the lx1 = 8 kernel 191 registers
+// instead of 96.)
+template <typename T, bool FUSED>
+__global__ void __launch_bounds__(100, 5) axhelm_tma_kernel_10x1(const AxArgs<T> a) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  axhelm_tma_body<10, T, FUSED, 1>(a, blockIdx.x, smem_raw);
 }
 
 }  // namespace nekgpu

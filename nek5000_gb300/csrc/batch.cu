@@ -92,7 +92,7 @@ __host__ __device__ constexpr int batch_tma_epb() {
 // The TMA-staged FP32 operator for the problems of one order (blocks of
 // (NX*NX, EPB) threads; virtual blocks as batch_axhelm_nx_kernel).
 template <int NX, int EPB>
-__global__ void __launch_bounds__(NX* NX* EPB, tma_min_blocks<NX, EPB>())
+__global__ void __launch_bounds__(NX* NX* EPB)
     batch_axhelm_tma_kernel(const BDesc<float>* __restrict__ D, const int* __restrict__ map,
                             const int* __restrict__ base, int start) {
   extern __shared__ __align__(128) unsigned char smem_tma[];
@@ -681,7 +681,7 @@ int batch_tune_tma(Batch& B, const std::vector<int>& ids, const std::vector<Coef
 // Picks the operator block size for a problem set: times a batched operator
 // launch for every candidate (128 or 256 threads; 128 only when every
 // element slab fits) and keeps the fastest, once per problem set and
-// precision.  Runs on freshly prepared problems only (beta = 0, p = 0), where
+// precision (a subset of a tuned set keeps its pick).  Runs on freshly prepared problems only (beta = 0, p = 0), where
 // the launches it times change nothing the first iteration reads.  Every
 // size gives the same results (per-element rho partials).
 template <typename T>
@@ -697,16 +697,20 @@ int batch_tune(Batch& B, const std::vector<int>& ids, const std::vector<Coef<T>>
     B.threads[prec] = kBatchThreads;
     return 0;
   }
+  // (problem, coefficient modes), sorted: a set already tuned, or a subset of
+  // one (the problems a mixed solve still runs as others converge), keeps
+  // the pick
   std::vector<int64_t> key;
   int maxnxy = 0;
   for (size_t q = 0; q < ids.size(); ++q) {
     const Mesh& m = B.probs[ids[q]]->mesh;
-    key.push_back(m.nx1);
-    key.push_back(m.nel);
-    key.push_back(coef[q].h1mode * 4 + coef[q].h2mode);
+    key.push_back((int64_t)ids[q] * 16 + coef[q].h1mode * 4 + coef[q].h2mode);
     maxnxy = std::max(maxnxy, m.nx1 * m.nx1);
   }
-  if (B.threads[prec] && key == B.tkey[prec]) return 0;
+  std::sort(key.begin(), key.end());
+  if (B.threads[prec] &&
+      std::includes(B.tkey[prec].begin(), B.tkey[prec].end(), key.begin(), key.end()))
+    return 0;  // (a subset's orders all have their TMA verdicts: tma_off stands)
   std::vector<int> cand;
   for (int t : {128, 256})
     if (t >= maxnxy) cand.push_back(t);
@@ -1354,6 +1358,14 @@ int nekgpu_batch_shape(const int64_t* batch, const int* precision, int* threads,
     return bfail(B, NEKGPU_EINVAL, "precision must be 0 or 1");
   if (threads) *threads = B->threads[*precision];
   if (ms) *ms = B->tune_ms[*precision];
+  return NEKGPU_OK;
+}
+
+int nekgpu_batch_operator_forms(const int64_t* batch, int* forms) {
+  Batch* B = bget(batch);
+  if (!B) return bfail(nullptr, NEKGPU_EHANDLE, "unknown batch");
+  if (!forms) return bfail(B, NEKGPU_EINVAL, "null argument");
+  for (int nx = 0; nx <= NEKGPU_MAX_LX1; ++nx) forms[nx] = B->tma_pick[nx];
   return NEKGPU_OK;
 }
 

@@ -557,6 +557,15 @@ class NekGpuBatch:
             raise _capi.NekGpuError(rc, self.last_error())
         return t.value, ms.value
 
+    def operator_forms(self):
+        """FP32 operator body per order: {lx1: 1 TMA-staged, 0 plain} for the
+        orders timed so far."""
+        forms = (C.c_int * (_capi.MAX_LX1 + 1))()
+        rc = self._L.nekgpu_batch_operator_forms(C.byref(self._b), forms)
+        if rc:
+            raise _capi.NekGpuError(rc, self.last_error())
+        return {nx: v for nx, v in enumerate(forms) if v >= 0}
+
     def set_shape(self, precision: int, threads: int):
         """Pin the operator block size (128 or 256; 0 returns to tuning)."""
         rc = self._L.nekgpu_batch_set_shape(C.byref(self._b), C.byref(_cint(precision)),
