@@ -265,6 +265,20 @@ int nekgpu_cresvsp_dev(const int64_t *handle, double *r1, double *r2, double *r3
                        const double *h2, const double *vdiff, const double *qtl,
                        const double *pr, const double *bfx, const double *bfy,
                        const double *bfz);
+/* cresvsp_weak (core/plan4.f:308-361), the velocity residual of plan4's
+ * stress-formulation branch (:84-86, ifstrs and not ifaxis):
+ *   r = -A(h1, h2) v - (opgrad(scale vdiff qtl) - cdtp(pr)) + bf
+ * per component, the pressure through its weak gradient (cdtp per
+ * direction with the mesh's mass and metric terms), scale = 2/3 when
+ * *stress, else -1/3.  Same setup needs and exact-mode behaviour as
+ * nekgpu_cresvsp_dev.  The traction boundary terms that the reference adds
+ * before it (bcneutr) and the coupled stress operator the velocity solve
+ * then uses (ophinv with ifstrs) are not part of this library. */
+int nekgpu_cresvsp_weak_dev(const int64_t *handle, double *r1, double *r2, double *r3,
+                            const double *vx, const double *vy, const double *vz,
+                            const double *h1, const double *h2, const double *vdiff,
+                            const double *qtl, const double *pr, const double *bfx,
+                            const double *bfy, const double *bfz, const int *stress);
 int nekgpu_crespsp_dev(const int64_t *handle, double *respr, const double *vxe,
                        const double *vye, const double *vze, const double *pr,
                        const double *qtl, const double *vdiff, const double *vtrans,

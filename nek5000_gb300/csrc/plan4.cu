@@ -3,6 +3,8 @@
 // operator (axhelm), gradient-type operators (gradops.cu) and gather-scatter:
 //
 //   cresvsp  core/plan4.f:264-306  velocity residual
+//   cresvsp_weak  core/plan4.f:308-361  the same with the weak pressure
+//            gradient (the stress formulation's branch, plan4.f:84-86)
 //            resv = -A(h1, h2) v - opgrad(pr - vdiff qtl / 3) + bf
 //   crespsp  core/plan4.f:99-230   pressure right-hand side from the
 //            curl-curl of the extrapolated velocity, qtl, the pressure's own
@@ -36,6 +38,17 @@ __global__ void p4_ta4_kernel(double* __restrict__ ta, const double* __restrict_
 __global__ void p4_resv_kernel(double* __restrict__ r, const double* __restrict__ t,
                                const double* __restrict__ bf, int64_t n) {
   PFOR(i, n) r[i] = __dadd_rn(__dsub_rn(-r[i], t[i]), bf[i]);
+}
+
+// ta = (vdiff qtl) scale   (col3, cmult)
+__global__ void p4_ta4w_kernel(double* __restrict__ ta, const double* __restrict__ vdiff,
+                               const double* __restrict__ qtl, double scale, int64_t n) {
+  PFOR(i, n) ta[i] = __dmul_rn(__dmul_rn(vdiff[i], qtl[i]), scale);
+}
+
+// t = t - wa   (sub2)
+__global__ void p4_sub_kernel(double* __restrict__ t, const double* __restrict__ wa, int64_t n) {
+  PFOR(i, n) t[i] = __dsub_rn(t[i], wa[i]);
 }
 
 // wa = (wa bm1 + ta scale) (vdiff / vtrans)   (opcolv, opadd2cm, invcol3, opcolv)
@@ -290,6 +303,47 @@ extern "C" int nekgpu_cresvsp_dev(const int64_t* handle, double* r1, double* r2,
     p4_resv_kernel<<<pblocks(n), 256, 0, s>>>(r[k], t[k], bf[k], n);
   }
   return p4_done(H, 0, "cresvsp");
+}
+
+extern "C" int nekgpu_cresvsp_weak_dev(const int64_t* handle, double* r1, double* r2, double* r3,
+                                       const double* vx, const double* vy, const double* vz,
+                                       const double* h1, const double* h2, const double* vdiff,
+                                       const double* qtl, const double* pr, const double* bfx,
+                                       const double* bfy, const double* bfz, const int* stress) {
+  int rc;
+  Handle* H = p4_handle(handle, &rc);
+  if (!H) return rc;
+  if (!r1 || !r2 || !r3 || !vx || !vy || !vz || !h1 || !h2 || !vdiff || !qtl || !pr || !bfx ||
+      !bfy || !bfz || !stress)
+    return handle_fail(H, NEKGPU_EINVAL, "null argument");
+  const int64_t n = H->mesh.n;
+  cudaStream_t s = H->stream;
+  if (H->io0.ensure(n) || H->io1.ensure(n) || H->io2.ensure(n) || H->io3.ensure(n) ||
+      H->io4.ensure(n))
+    return handle_fail(H, NEKGPU_ENOMEM, "device allocation failed");
+  Coef<double> c;
+  if (detect_coef<double>(*H, h1, h2, n, c))
+    return handle_fail(H, NEKGPU_ECUDA, "coefficient scan failed");
+  double* r[3] = {r1, r2, r3};
+  const double* v[3] = {vx, vy, vz};
+  const double* bf[3] = {bfx, bfy, bfz};
+  for (int k = 0; k < 3; ++k)  // ophx
+    if (axhelm_any(*H, r[k], v[k], c)) return p4_done(H, -3, "cresvsp_weak operator");
+  double *ta = H->io0.ptr, *t[3] = {H->io1.ptr, H->io2.ptr, H->io3.ptr}, *wa = H->io4.ptr;
+  count_launch();
+  p4_ta4w_kernel<<<pblocks(n), 256, 0, s>>>(ta, vdiff, qtl, *stress ? 2. / 3. : -1. / 3., n);
+  if (launch_gradop(*H, 0, t[0], t[1], t[2], ta, nullptr, nullptr, 0, nullptr))  // opgrad
+    return handle_fail(H, NEKGPU_EINVAL, "cresvsp_weak: lx1 out of range");
+  for (int k = 0; k < 3; ++k) {
+    launch_gradop(*H, 2, wa, nullptr, nullptr, pr, nullptr, nullptr, k, H->mesh.f64.bm1);  // cdtp
+    count_launch();
+    p4_sub_kernel<<<pblocks(n), 256, 0, s>>>(t[k], wa, n);
+  }
+  for (int k = 0; k < 3; ++k) {
+    count_launch();
+    p4_resv_kernel<<<pblocks(n), 256, 0, s>>>(r[k], t[k], bf[k], n);
+  }
+  return p4_done(H, 0, "cresvsp_weak");
 }
 
 extern "C" int nekgpu_crespsp_dev(const int64_t* handle, double* respr, const double* vxe,

@@ -266,6 +266,15 @@ class NekGpu:
                                                _ptr(vdiff), _ptr(qtl), _ptr(pr),
                                                *[_ptr(a) for a in bf]))
 
+    def cresvsp_weak(self, r, v, h1, h2, vdiff, qtl, pr, bf, stress=True):
+        """velocity residual with the weak pressure gradient (the stress
+        formulation's branch of the splitting step; 3 device arrays each)"""
+        self._check(self._L.nekgpu_cresvsp_weak_dev(C.byref(self._h), *[_ptr(a) for a in r],
+                                                    *[_ptr(a) for a in v], _ptr(h1), _ptr(h2),
+                                                    _ptr(vdiff), _ptr(qtl), _ptr(pr),
+                                                    *[_ptr(a) for a in bf],
+                                                    C.byref(_cint(1 if stress else 0))))
+
     def crespsp(self, respr, ve, pr, qtl, vdiff, vtrans, bf, binv, dtbd, null_space=False,
                 v=None, fbc=None):
         """pressure right-hand side of the splitting step; fbc: host (nel, 6)

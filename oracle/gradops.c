@@ -165,6 +165,44 @@ void ref_cresvsp(const ref_ops *ops, double *r1, double *r2, double *r3, const d
   free(ta);
 }
 
+/* cresvsp_weak (core/plan4.f:308-361), the velocity residual of the stress
+ * formulation's branch of plan4 (:84-86): the pressure enters through its
+ * weak gradient (cdtp of pr per direction) instead of the strong one,
+ * resv = -A(h1, h2) v - (wgradm1(scale vdiff qtl) - cdtp(pr)) + bf, per
+ * component, with scale = 2/3 (stress formulation) or -1/3. */
+void ref_cresvsp_weak(const ref_ops *ops, double *r1, double *r2, double *r3, const double *vx,
+                      const double *vy, const double *vz, const double *h1, const double *h2,
+                      const double *vdiff, const double *qtl, const double *pr,
+                      const double *bfx, const double *bfy, const double *bfz,
+                      const double *rst, const double *jac, const double *bm1, int stress) {
+  const int nx1 = ref_ops_nx1(ops), nel = ref_ops_nel(ops);
+  const int64_t n = ref_ops_n(ops);
+  double *ta = (double *)malloc(sizeof(double) * 5 * n), *t1 = ta + n, *t2 = t1 + n,
+         *t3 = t2 + n, *wa = t3 + n;
+  double *r[3] = {r1, r2, r3};
+  const double *v[3] = {vx, vy, vz}, *bf[3] = {bfx, bfy, bfz};
+  for (int c = 0; c < 3; ++c) ref_axhelm(ops, r[c], v[c], h1, h2); /* ophx */
+  for (int c = 0; c < 3; ++c)
+    for (int64_t i = 0; i < n; ++i) r[c][i] = -r[c][i];             /* opchsgn */
+  const double scale = stress ? 2. / 3. : -1. / 3.;
+  for (int64_t i = 0; i < n; ++i) {
+    ta[i] = vdiff[i] * qtl[i]; /* col3 */
+    ta[i] = ta[i] * scale;     /* cmult */
+  }
+  ref_wgradm1(nx1, nel, t1, t2, t3, ta, rst); /* opgrad */
+  double *t[3] = {t1, t2, t3};
+  for (int c = 0; c < 3; ++c) {
+    ref_cdtp(nx1, nel, wa, pr, rst, jac, bm1, c + 1);           /* cdtp(wa, pr, r/s/t x|y|z m1) */
+    for (int64_t i = 0; i < n; ++i) t[c][i] = t[c][i] - wa[i];  /* sub2 */
+  }
+  for (int c = 0; c < 3; ++c)
+    for (int64_t i = 0; i < n; ++i) {
+      r[c][i] = r[c][i] - t[c][i];   /* opsub2 */
+      r[c][i] = r[c][i] + bf[c][i];  /* opadd2 */
+    }
+  free(ta);
+}
+
 /* crespsp (core/plan4.f:99-260), PN-PN without the stress formulation: the
  * face terms on the faces fbc marks (6 per element, preprocessor order: 0
  * none, 1 'V'/'v'/'MV'/'mv', 2 'shl', 3 'SYM'; fbc null: none); the pressure right-hand side

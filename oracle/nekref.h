@@ -190,6 +190,11 @@ void ref_cresvsp(const ref_ops *ops, double *r1, double *r2, double *r3, const d
                  const double *vy, const double *vz, const double *h1, const double *h2,
                  const double *vdiff, const double *qtl, const double *pr, const double *bfx,
                  const double *bfy, const double *bfz, const double *rst);
+void ref_cresvsp_weak(const ref_ops *ops, double *r1, double *r2, double *r3, const double *vx,
+                      const double *vy, const double *vz, const double *h1, const double *h2,
+                      const double *vdiff, const double *qtl, const double *pr,
+                      const double *bfx, const double *bfy, const double *bfz,
+                      const double *rst, const double *jac, const double *bm1, int stress);
 void ref_crespsp(const ref_ops *ops, double *respr, const double *vxe, const double *vye,
                  const double *vze, const double *pr, const double *qtl, const double *vdiff,
                  const double *vtrans, const double *bfx, const double *bfy, const double *bfz,

@@ -30,8 +30,10 @@ _vp = C.c_void_p
 
 def build(force: bool = False) -> str:
     """Compile the oracle with its Makefile (gcc, OpenMP, -ffp-contract=off)."""
-    src = os.path.join(_HERE, "nekref.c")
-    if force or not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < os.path.getmtime(src):
+    srcs = [os.path.join(_HERE, f) for f in ("nekref.c", "h1mg.c", "gradops.c", "nekref.h",
+                                              "Makefile")]
+    if force or not os.path.exists(_LIB_PATH) or \
+            os.path.getmtime(_LIB_PATH) < max(os.path.getmtime(f) for f in srcs):
         subprocess.run(["make", "-s", "-C", _HERE], check=True)
     return _LIB_PATH
 
@@ -89,6 +91,7 @@ def lib():
             L.ref_conv2.argtypes = [C.c_int, C.c_int] + [_dp] * 7
             L.ref_convopo.argtypes = [C.c_int, C.c_int] + [_dp] * 8 + [_vp]
             L.ref_cresvsp.argtypes = [_vp] + [_dp] * 15
+            L.ref_cresvsp_weak.argtypes = [_vp] + [_dp] * 17 + [C.c_int]
             L.ref_crespsp.argtypes = [_vp] + [_dp] * 13 + [C.c_double, C.c_int, _dp, _dp, _dp, _dp,
                                                            _dp, _vp, _dp]
             L.ref_fdm1d.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
@@ -527,6 +530,16 @@ def cresvsp(ops, v, h1, h2, vdiff, qtl, pr, bf, rst):
     out = [np.zeros(ops.n) for _ in range(3)]
     lib().ref_cresvsp(ops.h, *out, *[_c(a) for a in v], _c(h1), _c(h2), _c(vdiff), _c(qtl),
                       _c(pr), *[_c(a) for a in bf], _c(rst))
+    return out
+
+
+def cresvsp_weak(ops, v, h1, h2, vdiff, qtl, pr, bf, rst, jac, bm1, stress=True):
+    """velocity residual of the stress formulation's branch of the splitting
+    step (weak pressure gradient); v, bf: 3 components"""
+    out = [np.zeros(ops.n) for _ in range(3)]
+    lib().ref_cresvsp_weak(ops.h, *out, *[_c(a) for a in v], _c(h1), _c(h2), _c(vdiff),
+                           _c(qtl), _c(pr), *[_c(a) for a in bf], _c(rst), _c(jac), _c(bm1),
+                           1 if stress else 0)
     return out
 
 

@@ -1,5 +1,5 @@
 """The splitting step's right-hand sides on the device (nekgpu_cresvsp_dev,
-nekgpu_crespsp_dev) against the oracle (oracle/gradops.c): bit for bit with
+nekgpu_cresvsp_weak_dev, nekgpu_crespsp_dev) against the oracle (oracle/gradops.c): bit for bit with
 the handle's exact option (every product and sum rounded in the reference's
 order), to 1e-12 with the default fused operator; the null-space mean of
 crespsp is a block-order sum, so that case is compared to 1e-13."""
@@ -36,6 +36,14 @@ def test_residuals_match_the_oracle(gpu_lib, oracle, exact):
     want = oracle.cresvsp(ops, v, h1, h2, vdiff, qtl, pr, bf, rst)
     for a, b in zip(r, want):
         assert cmp(a.cpu().numpy(), b)
+    for stress in (True, False):  # the weak-gradient form (plan4.f:308)
+        r = [zeros() for _ in range(3)]
+        lib.cresvsp_weak(r, [dev(a) for a in v], dev(h1), dev(h2), dev(vdiff), dev(qtl),
+                         dev(pr), [dev(a) for a in bf], stress=stress)
+        want = oracle.cresvsp_weak(ops, v, h1, h2, vdiff, qtl, pr, bf, rst, jac, P["bm1"],
+                                   stress=stress)
+        for a, b in zip(r, want):
+            assert cmp(a.cpu().numpy(), b), stress
     vc = [rnd() for _ in range(3)]  # the current velocity (face terms)
     fbc = rng.integers(0, 4, size=(nel, 6)).astype(np.int32)  # all four face kinds
     for null, faces in ((False, None), (True, None), (False, fbc)):
