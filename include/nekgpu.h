@@ -279,6 +279,30 @@ int nekgpu_cresvsp_weak_dev(const int64_t *handle, double *r1, double *r2, doubl
                             const double *h1, const double *h2, const double *vdiff,
                             const double *qtl, const double *pr, const double *bfx,
                             const double *bfy, const double *bfz, const int *stress);
+/* The stress formulation's coupled velocity operator and solve (device
+ * arrays; FP64, products and sums rounded in the reference's order; the
+ * geometry must come from coordinates, nekgpu_setup_xyz):
+ *   axhmsf  core/subs1.f:1240-1315 for a fluid (matmod = 0) in 3-D, its
+ *           default path axsf_e_3d (:2031-2116):
+ *           au_i = sum_j D^T (h1 w3 / J) (du_i/dx_j + du_j/dx_i) + h2 B u_i
+ *   hmhzsf  core/subs1.f:1093-1147 without the projection onto previous
+ *           solutions (param(94) = 0): r masked by m1, m2, m3 (the volume
+ *           masks of rmask) and dssum'ed in place, u = 0, chktcgs's
+ *           tolerance floor, then cggosf (:2-165): Jacobi-PCG on the coupled
+ *           system, preconditioned by the sum of the three setprec
+ *           diagonals, at most 200 iterations (the reference fixes that cap;
+ *           NEKGPU_ENOTCONV when reached).  *tol: absolute tolerance on
+ *           sqrt(sum binv mult |r|^2 / vol).  The face, edge and corner
+ *           masks of qmask (symmetry and other mixed conditions) are not
+ *           applied. */
+int nekgpu_axhmsf_dev(const int64_t *handle, double *au1, double *au2, double *au3,
+                      const double *u1, const double *u2, const double *u3, const double *h1,
+                      const double *h2);
+int nekgpu_hmhzsf_dev(const int64_t *handle, double *u1, double *u2, double *u3, double *r1,
+                      double *r2, double *r3, const double *h1, const double *h2,
+                      const double *m1, const double *m2, const double *m3, const double *mult,
+                      const double *binv, const double *tol, int *niter, double *rbn0,
+                      double *rbn2);
 int nekgpu_crespsp_dev(const int64_t *handle, double *respr, const double *vxe,
                        const double *vye, const double *vze, const double *pr,
                        const double *qtl, const double *vdiff, const double *vtrans,

@@ -89,6 +89,8 @@ SIGNATURES = {
     "nekgpu_sumab_dev": [_I64P, _P, _P, _P, _P, _IP],
     "nekgpu_cresvsp_dev": [_I64P] + [_P] * 14,
     "nekgpu_cresvsp_weak_dev": [_I64P] + [_P] * 14 + [_IP],
+    "nekgpu_axhmsf_dev": [_I64P] + [_P] * 8,
+    "nekgpu_hmhzsf_dev": [_I64P] + [_P] * 13 + [_DP, _IP, _DP, _DP],
     "nekgpu_crespsp_dev": [_I64P] + [_P] * 12 + [_DP, _IP, _P, _P, _P, _P],
     "nekgpu_col2_dev": [_I64P, _P, _P],
     "nekgpu_col3_dev": [_I64P, _P, _P, _P],

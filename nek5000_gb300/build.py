@@ -13,7 +13,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libnekgpu.so")
-SOURCES = ["axhelm_f64.cu", "axhelm_f32.cu", "axhelm_tma.cu", "axhelm_df.cu", "tune.cu", "gs.cu", "pcg.cu", "mixed.cu", "split.cu", "perm.cu", "batch.cu", "adjoint.cu", "proj.cu", "multi.cu", "noalloc.cu", "geom.cu", "gmres.cu", "h1mg.cu", "amg.cu", "vecops.cu", "gradops.cu", "plan4.cu", "dealias.cu", "capi.cu",
+SOURCES = ["axhelm_f64.cu", "axhelm_f32.cu", "axhelm_tma.cu", "axhelm_df.cu", "tune.cu", "gs.cu", "pcg.cu", "mixed.cu", "split.cu", "perm.cu", "batch.cu", "adjoint.cu", "proj.cu", "multi.cu", "noalloc.cu", "geom.cu", "gmres.cu", "h1mg.cu", "amg.cu", "vecops.cu", "gradops.cu", "plan4.cu", "stress.cu", "dealias.cu", "capi.cu",
            "meshio.cpp", "h1mg_plan.cpp", "xxt.cpp", "amg_plan.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",

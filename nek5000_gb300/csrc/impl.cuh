@@ -176,6 +176,9 @@ struct Handle {
   PcgWork<double> w64;
   PcgWork<float> w32;
   DevBuf<double> io0, io1, io2, io3, io4, io5, io6, io7, io8;  // host-path staging
+  // the stress formulation's solve (stress.cu): dpc, p, pp, ap (3 each), and
+  // the reductions' block partials
+  DevBuf<double> sfw[10], sf_part;
   bool exact = false;  // unfused FP64 arithmetic in the reference's order
   int istep = 0;       // reference time-step index (cggo's "at least one iteration" rule)
   // timing

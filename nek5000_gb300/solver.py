@@ -275,6 +275,24 @@ class NekGpu:
                                                     *[_ptr(a) for a in bf],
                                                     C.byref(_cint(1 if stress else 0))))
 
+    def axhmsf(self, au, u, h1, h2):
+        """the stress formulation's coupled operator (au, u: 3 device arrays)"""
+        self._check(self._L.nekgpu_axhmsf_dev(C.byref(self._h), *[_ptr(a) for a in au],
+                                              *[_ptr(a) for a in u], _ptr(h1), _ptr(h2)))
+
+    def hmhzsf(self, u, r, h1, h2, masks, mult, binv, tol):
+        """the stress formulation's coupled solve (u, r, masks: 3 device
+        arrays each; r is masked and dssum'ed in place).  Returns
+        (iterations, rbn0, rbn2, status)."""
+        it, r0, r2 = _cint(0), _cdouble(0), _cdouble(0)
+        rc = self._L.nekgpu_hmhzsf_dev(C.byref(self._h), *[_ptr(a) for a in u],
+                                       *[_ptr(a) for a in r], _ptr(h1), _ptr(h2),
+                                       *[_ptr(a) for a in masks], _ptr(mult), _ptr(binv),
+                                       C.byref(_cdouble(tol)), C.byref(it), C.byref(r0),
+                                       C.byref(r2))
+        self._check(rc, allow=(_capi.ENOTCONV,))
+        return it.value, r0.value, r2.value, rc
+
     def crespsp(self, respr, ve, pr, qtl, vdiff, vtrans, bf, binv, dtbd, null_space=False,
                 v=None, fbc=None):
         """pressure right-hand side of the splitting step; fbc: host (nel, 6)

@@ -203,6 +203,184 @@ void ref_cresvsp_weak(const ref_ops *ops, double *r1, double *r2, double *r3, co
   free(ta);
 }
 
+/* ---- the stress formulation's coupled velocity operator and solve --------- */
+
+/* axsf_e_3d over every element (core/subs1.f:2031-2116, the default "fast"
+ * path of axhmsf, :1240-1315, for a fluid, matmod = 0): the velocity gradient
+ * from local_grad3 and the metric terms, the symmetric strain times
+ * h1 w3 / J, contracted back with the metric terms and local_grad3_t, plus
+ * h2 B u per component. */
+void ref_axsf(const ref_ops *ops, double *au, double *av, double *aw, const double *u,
+              const double *v, const double *w, const double *h1, const double *h2,
+              const double *rst, const double *jac, const double *bm1) {
+  const int nx1 = ref_ops_nx1(ops), nel = (int)(ref_ops_n(ops) / ((int64_t)nx1 * nx1 * nx1));
+  const int nxyz = nx1 * nx1 * nx1;
+  const int64_t n = ref_ops_n(ops);
+  double d[1024], dt[1024];
+  double *w3 = (double *)malloc(sizeof(double) * nxyz);
+  double *ur = (double *)malloc(sizeof(double) * 10 * nxyz); /* ur(i, 3, 3) + work */
+  double *wk = ur + 9 * nxyz;
+  dmat(nx1, d, dt, w3);
+  const double *rx = rst, *ry = rst + n, *rz = rst + 2 * n, *sx = rst + 3 * n, *sy = rst + 4 * n,
+               *sz = rst + 5 * n, *tx = rst + 6 * n, *ty = rst + 7 * n, *tz = rst + 8 * n;
+#define UR(i, a, b) ur[(i) + nxyz * ((a) + 3 * (b))]
+  for (int e = 0; e < nel; ++e) {
+    const int64_t o = (int64_t)nxyz * e;
+    ref_local_grad3(&UR(0, 0, 0), &UR(0, 1, 0), &UR(0, 2, 0), u + o, nx1 - 1, d, dt);
+    ref_local_grad3(&UR(0, 0, 1), &UR(0, 1, 1), &UR(0, 2, 1), v + o, nx1 - 1, d, dt);
+    ref_local_grad3(&UR(0, 0, 2), &UR(0, 1, 2), &UR(0, 2, 2), w + o, nx1 - 1, d, dt);
+    for (int i = 0; i < nxyz; ++i) {
+      const int64_t q = o + i;
+      const double u1 = UR(i, 0, 0) * rx[q] + UR(i, 1, 0) * sx[q] + UR(i, 2, 0) * tx[q];
+      const double u2 = UR(i, 0, 0) * ry[q] + UR(i, 1, 0) * sy[q] + UR(i, 2, 0) * ty[q];
+      const double u3 = UR(i, 0, 0) * rz[q] + UR(i, 1, 0) * sz[q] + UR(i, 2, 0) * tz[q];
+      const double v1 = UR(i, 0, 1) * rx[q] + UR(i, 1, 1) * sx[q] + UR(i, 2, 1) * tx[q];
+      const double v2 = UR(i, 0, 1) * ry[q] + UR(i, 1, 1) * sy[q] + UR(i, 2, 1) * ty[q];
+      const double v3 = UR(i, 0, 1) * rz[q] + UR(i, 1, 1) * sz[q] + UR(i, 2, 1) * tz[q];
+      const double w1 = UR(i, 0, 2) * rx[q] + UR(i, 1, 2) * sx[q] + UR(i, 2, 2) * tx[q];
+      const double w2 = UR(i, 0, 2) * ry[q] + UR(i, 1, 2) * sy[q] + UR(i, 2, 2) * ty[q];
+      const double ww3 = UR(i, 0, 2) * rz[q] + UR(i, 1, 2) * sz[q] + UR(i, 2, 2) * tz[q];
+      const double dj = h1[q] * w3[i] * (1.0 / jac[q]);
+      const double s11 = dj * (u1 + u1), s12 = dj * (u2 + v1), s13 = dj * (u3 + w1);
+      const double s21 = dj * (v1 + u2), s22 = dj * (v2 + v2), s23 = dj * (v3 + w2);
+      const double s31 = dj * (w1 + u3), s32 = dj * (w2 + v3), s33 = dj * (ww3 + ww3);
+      UR(i, 0, 0) = rx[q] * s11 + ry[q] * s12 + rz[q] * s13;
+      UR(i, 1, 0) = sx[q] * s11 + sy[q] * s12 + sz[q] * s13;
+      UR(i, 2, 0) = tx[q] * s11 + ty[q] * s12 + tz[q] * s13;
+      UR(i, 0, 1) = rx[q] * s21 + ry[q] * s22 + rz[q] * s23;
+      UR(i, 1, 1) = sx[q] * s21 + sy[q] * s22 + sz[q] * s23;
+      UR(i, 2, 1) = tx[q] * s21 + ty[q] * s22 + tz[q] * s23;
+      UR(i, 0, 2) = rx[q] * s31 + ry[q] * s32 + rz[q] * s33;
+      UR(i, 1, 2) = sx[q] * s31 + sy[q] * s32 + sz[q] * s33;
+      UR(i, 2, 2) = tx[q] * s31 + ty[q] * s32 + tz[q] * s33;
+    }
+    ref_local_grad3_t(au + o, &UR(0, 0, 0), &UR(0, 1, 0), &UR(0, 2, 0), nx1 - 1, d, dt, wk);
+    ref_local_grad3_t(av + o, &UR(0, 0, 1), &UR(0, 1, 1), &UR(0, 2, 1), nx1 - 1, d, dt, wk);
+    ref_local_grad3_t(aw + o, &UR(0, 0, 2), &UR(0, 1, 2), &UR(0, 2, 2), nx1 - 1, d, dt, wk);
+    for (int i = 0; i < nxyz; ++i) {
+      const int64_t q = o + i;
+      au[q] = au[q] + h2[q] * bm1[q] * u[q];
+      av[q] = av[q] + h2[q] * bm1[q] * v[q];
+      aw[q] = aw[q] + h2[q] * bm1[q] * w[q];
+    }
+  }
+#undef UR
+  free(w3);
+  free(ur);
+}
+
+/* hmhzsf (core/subs1.f:1093-1147) without the projection onto previous
+ * solutions (param(94) = 0): rmask (the volume masks of qmask, :1800-1860),
+ * opdssum, u = 0, chktcgs (:1149-1238), then cggosf (:2-165): Jacobi-PCG on
+ * the coupled system with dpc the sum of the three setprec diagonals and the
+ * loop capped at 200 iterations, as the reference sets it.  tol is the
+ * absolute tolerance on sqrt(sum binv mult |r|^2 / vol).  Sums run serially
+ * over the points.  Returns the iteration count (-1: the cap was reached). */
+static double sf_wdot(int64_t n, const double *a1, const double *a2, const double *a3,
+                      const double *b1, const double *b2, const double *b3, const double *wt) {
+  double s = 0.0;
+  for (int64_t i = 0; i < n; ++i) s = s + wt[i] * (a1[i] * b1[i] + a2[i] * b2[i] + a3[i] * b3[i]);
+  return s;
+}
+
+int ref_hmhzsf(const ref_ops *ops, double *u1, double *u2, double *u3, double *r1, double *r2,
+               double *r3, const double *h1, const double *h2, const double *m1,
+               const double *m2, const double *m3, const double *mult, const double *binv,
+               const double *rst, const double *jac, const double *bm1, double vol, double tin,
+               double *rbn0, double *rbn2) {
+  const int64_t n = ref_ops_n(ops);
+  double *r[3] = {r1, r2, r3}, *u[3] = {u1, u2, u3};
+  const double *m[3] = {m1, m2, m3};
+  double *buf = (double *)malloc(sizeof(double) * 11 * n);
+  double *dpc = buf, *wa = buf + n, *p[3] = {buf + 2 * n, buf + 3 * n, buf + 4 * n},
+         *pp[3] = {buf + 5 * n, buf + 6 * n, buf + 7 * n},
+         *ap[3] = {buf + 8 * n, buf + 9 * n, buf + 10 * n};
+  for (int c = 0; c < 3; ++c) {
+    for (int64_t i = 0; i < n; ++i) r[c][i] = r[c][i] * m[c][i]; /* rmask */
+    ref_dssum(ops, r[c]);                                          /* opdssum */
+    for (int64_t i = 0; i < n; ++i) u[c][i] = 0.0;
+  }
+  /* chktcgs (EIGAA = 0: ACONDNO = 10; FP64: EPS = 1e-13) */
+  double tol = tin;
+  {
+    for (int64_t i = 0; i < n; ++i) wa[i] = r1[i] * r1[i] + r2[i] * r2[i] + r3[i] * r3[i];
+    double s = 0.0;
+    for (int64_t i = 0; i < n; ++i) s = s + wa[i] * binv[i] * mult[i];
+    const double rmin = 1e-13 * sqrt(s / vol);
+    if (tol < rmin) tol = rmin;
+    double b1 = 0.0, b2 = 0.0;
+    for (int64_t i = 0; i < n; ++i) {
+      wa[i] = m1[i] + m2[i] + m3[i];
+      b1 = b1 + wa[i] * mult[i];
+      b2 = b2 + mult[i];
+    }
+    if (fabs(b1 - 3.0 * b2) < 0.1) {
+      double o = 0.0;
+      for (int64_t i = 0; i < n; ++i) o = o + (r1[i] + r2[i] + r3[i]) * mult[i];
+      const double tolmin = fabs(o / 3.0) * 10.0;
+      if (tol < tolmin) tol = tolmin;
+    }
+  }
+  /* cggosf */
+  int iters = -1;
+  double rbnorm;
+  {
+    for (int64_t i = 0; i < n; ++i) wa[i] = r1[i] * r1[i] + r2[i] * r2[i] + r3[i] * r3[i];
+    double s = 0.0;
+    for (int64_t i = 0; i < n; ++i) s = s + wa[i] * binv[i] * mult[i];
+    rbnorm = sqrt(s / vol);
+  }
+  *rbn0 = rbnorm;
+  if (rbnorm < tol * tol) {
+    *rbn2 = rbnorm;
+    free(buf);
+    return 0;
+  }
+  ref_setprec(ops, dpc, h1, h2);
+  for (int64_t i = 0; i < n; ++i) dpc[i] = (dpc[i] + dpc[i]) + dpc[i]; /* isd = 1, 2, 3 */
+  for (int c = 0; c < 3; ++c)
+    for (int64_t i = 0; i < n; ++i) {
+      pp[c][i] = dpc[i] * r[c][i];
+      p[c][i] = 0.0 + pp[c][i];
+    }
+  double rpp1 = sf_wdot(n, p[0], p[1], p[2], r1, r2, r3, mult);
+  for (int iter = 1; iter <= 200; ++iter) {
+    ref_axsf(ops, ap[0], ap[1], ap[2], p[0], p[1], p[2], h1, h2, rst, jac, bm1);
+    for (int c = 0; c < 3; ++c) {
+      for (int64_t i = 0; i < n; ++i) ap[c][i] = ap[c][i] * m[c][i]; /* rmask */
+      ref_dssum(ops, ap[c]);                                            /* opdssum */
+    }
+    const double pap = sf_wdot(n, p[0], p[1], p[2], ap[0], ap[1], ap[2], mult);
+    const double alpha = rpp1 / pap;
+    for (int c = 0; c < 3; ++c)
+      for (int64_t i = 0; i < n; ++i) {
+        u[c][i] = u[c][i] + alpha * p[c][i];
+        r[c][i] = r[c][i] + (-alpha) * ap[c][i];
+      }
+    for (int64_t i = 0; i < n; ++i) wa[i] = r1[i] * r1[i] + r2[i] * r2[i] + r3[i] * r3[i];
+    double s = 0.0;
+    for (int64_t i = 0; i < n; ++i) s = s + wa[i] * binv[i] * mult[i];
+    rbnorm = sqrt(s / vol);
+    if (iter == 1) *rbn0 = rbnorm;
+    if (rbnorm < tol) {
+      iters = iter;
+      break;
+    }
+    for (int c = 0; c < 3; ++c)
+      for (int64_t i = 0; i < n; ++i) pp[c][i] = dpc[i] * r[c][i];
+    for (int64_t i = 0; i < n; ++i) wa[i] = r1[i] * pp[0][i] + r2[i] * pp[1][i] + r3[i] * pp[2][i];
+    const double rpp2 = rpp1;
+    rpp1 = 0.0;
+    for (int64_t i = 0; i < n; ++i) rpp1 = rpp1 + wa[i] * mult[i];
+    const double beta = rpp1 / rpp2;
+    for (int c = 0; c < 3; ++c)
+      for (int64_t i = 0; i < n; ++i) p[c][i] = beta * p[c][i] + pp[c][i];
+  }
+  *rbn2 = rbnorm;
+  free(buf);
+  return iters;
+}
+
 /* crespsp (core/plan4.f:99-260), PN-PN without the stress formulation: the
  * face terms on the faces fbc marks (6 per element, preprocessor order: 0
  * none, 1 'V'/'v'/'MV'/'mv', 2 'shl', 3 'SYM'; fbc null: none); the pressure right-hand side

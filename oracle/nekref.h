@@ -195,6 +195,14 @@ void ref_cresvsp_weak(const ref_ops *ops, double *r1, double *r2, double *r3, co
                       const double *vdiff, const double *qtl, const double *pr,
                       const double *bfx, const double *bfy, const double *bfz,
                       const double *rst, const double *jac, const double *bm1, int stress);
+void ref_axsf(const ref_ops *ops, double *au, double *av, double *aw, const double *u,
+              const double *v, const double *w, const double *h1, const double *h2,
+              const double *rst, const double *jac, const double *bm1);
+int ref_hmhzsf(const ref_ops *ops, double *u1, double *u2, double *u3, double *r1, double *r2,
+               double *r3, const double *h1, const double *h2, const double *m1,
+               const double *m2, const double *m3, const double *mult, const double *binv,
+               const double *rst, const double *jac, const double *bm1, double vol, double tin,
+               double *rbn0, double *rbn2);
 void ref_crespsp(const ref_ops *ops, double *respr, const double *vxe, const double *vye,
                  const double *vze, const double *pr, const double *qtl, const double *vdiff,
                  const double *vtrans, const double *bfx, const double *bfy, const double *bfz,

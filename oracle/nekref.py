@@ -92,6 +92,11 @@ def lib():
             L.ref_convopo.argtypes = [C.c_int, C.c_int] + [_dp] * 8 + [_vp]
             L.ref_cresvsp.argtypes = [_vp] + [_dp] * 15
             L.ref_cresvsp_weak.argtypes = [_vp] + [_dp] * 17 + [C.c_int]
+            L.ref_axsf.argtypes = [_vp] + [_dp] * 11
+            L.ref_hmhzsf.argtypes = [_vp] + [_dp] * 16 + [C.c_double, C.c_double,
+                                                           C.POINTER(C.c_double),
+                                                           C.POINTER(C.c_double)]
+            L.ref_hmhzsf.restype = C.c_int
             L.ref_crespsp.argtypes = [_vp] + [_dp] * 13 + [C.c_double, C.c_int, _dp, _dp, _dp, _dp,
                                                            _dp, _vp, _dp]
             L.ref_fdm1d.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
@@ -541,6 +546,25 @@ def cresvsp_weak(ops, v, h1, h2, vdiff, qtl, pr, bf, rst, jac, bm1, stress=True)
                            _c(qtl), _c(pr), *[_c(a) for a in bf], _c(rst), _c(jac), _c(bm1),
                            1 if stress else 0)
     return out
+
+
+def axsf(ops, u, h1, h2, rst, jac, bm1):
+    """the stress formulation's coupled operator (axsf_e_3d); u: 3 components"""
+    out = [np.zeros(ops.n) for _ in range(3)]
+    lib().ref_axsf(ops.h, *out, *[_c(a) for a in u], _c(h1), _c(h2), _c(rst), _c(jac), _c(bm1))
+    return out
+
+
+def hmhzsf(ops, r, h1, h2, masks, mult, binv, rst, jac, bm1, vol, tol):
+    """the stress formulation's coupled solve (hmhzsf without projection);
+    returns (u, r after, iterations (-1: 200 reached), rbn0, rbn2)"""
+    u = [np.zeros(ops.n) for _ in range(3)]
+    rr = [np.array(a, dtype=np.float64, copy=True) for a in r]
+    r0, r2 = C.c_double(0), C.c_double(0)
+    it = lib().ref_hmhzsf(ops.h, *u, *rr, _c(h1), _c(h2), *[_c(m) for m in masks], _c(mult),
+                          _c(binv), _c(rst), _c(jac), _c(bm1), float(vol), float(tol),
+                          C.byref(r0), C.byref(r2))
+    return u, rr, it, r0.value, r2.value
 
 
 def crespsp(ops, ve, pr, qtl, vdiff, vtrans, bf, bm1, binv, dtbd, null_space, rst, jac,
