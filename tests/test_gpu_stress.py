@@ -38,22 +38,6 @@ def test_stress_operator_bit_for_bit(gpu_lib, oracle, nx1):
         assert np.array_equal(a.cpu().numpy(), b)
 
 
-def test_stress_operator_is_symmetric(gpu_lib, oracle):
-    """(v, A u) = (u, A v) over the assembled space: the coupled operator of
-    the weak form is symmetric (checked on the oracle's own numbers)."""
-    P, rst, jac, _ = _setup(gpu_lib, oracle, 6, (2, 2, 2), 173)
-    n, ops = P["n"], P["ops"]
-    rng = np.random.default_rng(174)
-    cont = lambda: ops.dssum(rng.standard_normal(n) * P["mult"])  # continuous fields
-    u, v = [cont() for _ in range(3)], [cont() for _ in range(3)]
-    h1, h2 = np.ones(n), np.full(n, 2.0)
-    au = oracle.axsf(ops, u, h1, h2, rst, jac, P["bm1"])
-    av = oracle.axsf(ops, v, h1, h2, rst, jac, P["bm1"])
-    a = sum(np.dot(v[c], au[c]) for c in range(3))
-    b = sum(np.dot(u[c], av[c]) for c in range(3))
-    assert abs(a - b) <= 1e-12 * abs(a)
-
-
 @pytest.mark.parametrize("case", ["walls", "mixed"])
 def test_stress_solve_matches_the_oracle(gpu_lib, oracle, case):
     torch = pytest.importorskip("torch")
