@@ -10,15 +10,18 @@ reference's order, each a call through the C ABI on device arrays:
                   h2 = 0; ctolspl; hsolve('PRES') with projection; pr += dpr;
                   ortho(pr); cresvsp; ophinv (one hmholtz per component,
                   core/induct.f:1063-1073); v += dv
+  stress=True     the stress formulation's branch (core/plan4.f:84-86):
+                  cresvsp_weak, then ophinv's coupled hmhzsf
+                  (core/induct.f:1057-1061); walls need no bcneutr terms
 
 The coefficients of the BDF/extrapolation pair follow setbd / setabbd
 (core/navier1.f:1662, :1735) for a constant time step, ramping the order up
 over the first steps as setordbd does.  Velocity walls are homogeneous
 Dirichlet (bcdirvc then multiplies by the mask); the pressure is the
 all-Neumann one of a closed box when `null_space` (ortho removes its mean and
-the pressure solve applies cggo's null-space correction).  Not covered: the
-stress formulation (cresvsp_weak), moving geometry, variable density and
-characteristics (the `ifchar` branches of makef).
+the pressure solve applies cggo's null-space correction).  Not covered:
+traction boundaries of the stress formulation (bcneutr), moving geometry,
+variable density and characteristics (the `ifchar` branches of makef).
 """
 from __future__ import annotations
 
@@ -48,7 +51,8 @@ class SplittingStep:
 
     def __init__(self, lib, bm1, binvm1, vmask, pmask, vmult, vtrans, vdiff, qtl, dt,
                  tolhv=1e-10, tolpdf=1e-10, order=3, null_space=True, nmxv=1000,
-                 nmxp=1000, proj_space=0, mmx=8, convection=True, tolps=1e-8, prelax=1e-3):
+                 nmxp=1000, proj_space=0, mmx=8, convection=True, tolps=1e-8, prelax=1e-3,
+                 stress=False):
         import torch
         self.torch, self.lib = torch, lib
         t = lambda a: torch.as_tensor(np.ascontiguousarray(a, dtype=np.float64),
@@ -59,7 +63,7 @@ class SplittingStep:
         self.n = self.bm1.numel()
         self.dt, self.tolhv, self.tolpdf, self.order = float(dt), tolhv, tolpdf, order
         self.null_space, self.nmxv, self.nmxp = null_space, nmxv, nmxp
-        self.space, self.convection = proj_space, convection
+        self.space, self.convection, self.stress = proj_space, convection, stress
         self.tolps, self.prelax = tolps, prelax  # param(21) and 0.1 tolrel (drive2.f:238)
         z = lambda: torch.zeros(self.n, dtype=torch.float64, device="cuda")
         self.ones = z() + 1.0
@@ -164,8 +168,17 @@ class SplittingStep:
         self.h1v.copy_(self.vdiff)
         self.h2v.zero_()
         self._c("nekgpu_add2s2_dev", self.h2v, self.vtrans, dtbd)
-        lib.cresvsp(self.res, self.v, self.h1v, self.h2v, self.vdiff, self.qtl, self.pr, self.bf)
         itv = []
+        if self.stress:  # cresvsp_weak; ophinv -> hmhzsf, the components coupled
+            lib.cresvsp_weak(self.res, self.v, self.h1v, self.h2v, self.vdiff, self.qtl, self.pr,
+                             self.bf, stress=True)
+            it = lib.hmhzsf(self.dv, self.res, self.h1v, self.h2v, [self.vmask] * 3, self.vmult,
+                            self.binvm1, self.tolhv)[0]
+            for c in range(3):
+                self._c("nekgpu_add2s2_dev", self.v[c], self.dv[c], 1.0)
+            self.stats.append((itp, [it]))
+            return itp, [it]
+        lib.cresvsp(self.res, self.v, self.h1v, self.h2v, self.vdiff, self.qtl, self.pr, self.bf)
         for c in range(3):  # ophinv: hmholtz per component
             itv.append(lib.hmholtz("VEL", self.dv[c], self.res[c], self.h1v, self.h2v,
                                    self.vmask, self.vmult, 1, self.tolhv, self.nmxv, c + 1,

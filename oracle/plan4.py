@@ -13,6 +13,9 @@ infrastructure only: the GPU path never calls it.
             cresvsp (core/plan4.f:264, h1 = vdiff, h2 = vtrans bd(1)/dt from
             sethlm, core/subs1.f:1013); ophinv (core/induct.f:1022: hmholtz
             per component); v += dv
+  stress    the stress formulation's branch (core/plan4.f:84-86):
+            cresvsp_weak (:308) and hmhzsf (core/induct.f:1057-1061,
+            core/subs1.f:1093) for the three components together
 
 Coefficients: the same constant-step BDF / extrapolation pairs as the device
 driver (setbd / setabbd, core/navier1.f:1662-1800, with setordbd's ramp).
@@ -30,7 +33,7 @@ _AB = {1: [1.0, 0.0, 0.0], 2: [2.0, -1.0, 0.0], 3: [3.0, -3.0, 1.0]}
 class SplittingStepOracle:
     def __init__(self, P, vmask, pmask, vtrans, vdiff, qtl, dt, tolhv=1e-10, tolpdf=1e-10,
                  order=3, null_space=True, nmxv=1000, nmxp=1000, mmx=8, convection=True,
-                 tolps=1e-8, prelax=1e-3):
+                 tolps=1e-8, prelax=1e-3, stress=False):
         self.P = P
         self.ops = P["ops"]
         self.nx1, self.nel, self.n = P["nx1"], P["nel"], P["n"]
@@ -41,6 +44,7 @@ class SplittingStepOracle:
         self.dt, self.tolhv, self.tolpdf, self.order = float(dt), tolhv, tolpdf, order
         self.null_space, self.nmxv, self.nmxp = null_space, nmxv, nmxp
         self.convection, self.tolps, self.prelax = convection, tolps, prelax
+        self.stress = stress
         self.proj = nekref.Projection(self.ops, mmx)
         n = self.n
         self.v = [np.zeros(n) for _ in range(3)]
@@ -84,6 +88,15 @@ class SplittingStepOracle:
         if self.null_space:
             self.pr = self.pr - np.sum(self.pr) / n
         h1v, h2v = self.vdiff.copy(), self.vtrans * dtbd
+        if self.stress:
+            res = nekref.cresvsp_weak(self.ops, self.v, h1v, h2v, self.vdiff, self.qtl, self.pr,
+                                      bf, self.rst, self.jac, self.bm1, stress=True)
+            dv, _, it, _, _ = nekref.hmhzsf(self.ops, res, h1v, h2v, [self.vmask] * 3, self.mult,
+                                            self.binv, self.rst, self.jac, self.bm1,
+                                            self.volvm1, self.tolhv)
+            for c in range(3):
+                self.v[c] = self.v[c] + dv[c]
+            return itp, [it]
         res = nekref.cresvsp(self.ops, self.v, h1v, h2v, self.vdiff, self.qtl, self.pr, bf,
                              self.rst)
         itv = []

@@ -1,7 +1,8 @@
 """The whole splitting step (plan4, core/plan4.f:2-97) on the device:
 nek5000_gb300.plan4.SplittingStep strings the library's entry points together
 in the reference's order (makef, sumab, lagvel, bcdirvc, crespsp, the
-projected pressure solve, ortho, cresvsp, ophinv) and is compared after every
+projected pressure solve, ortho, cresvsp, ophinv; with the stress
+formulation cresvsp_weak and the coupled hmhzsf) and is compared after every
 one of six steps (the BDF/extrapolation order ramping from 1 to 3) with the
 oracle's restatement of the same step (oracle/plan4.py), on a deformed box
 with walls on every face and a divergence-free initial field that vanishes on
@@ -25,8 +26,8 @@ def _initial(P):
     return [vx * P["mask"], vy * P["mask"], np.zeros(P["n"])]
 
 
-@pytest.mark.parametrize("convection", [True, False])
-def test_splitting_step_matches_the_oracle(gpu_lib, oracle, convection):
+@pytest.mark.parametrize("convection,stress", [(True, False), (False, False), (True, True)])
+def test_splitting_step_matches_the_oracle(gpu_lib, oracle, convection, stress):
     torch = pytest.importorskip("torch")
     from oracle.plan4 import SplittingStepOracle
     from nek5000_gb300.plan4 import SplittingStep
@@ -35,7 +36,7 @@ def test_splitting_step_matches_the_oracle(gpu_lib, oracle, convection):
     lib = gpu_lib(0)
     lib.setup_xyz(P["nx1"], P["nel"], P["D"], P["wgll"], P["x"], P["y"], P["z"], P["glo_num"])
     vtrans, vdiff, qtl = np.ones(n), np.full(n, 0.01), np.zeros(n)
-    kw = dict(dt=1e-3, tolhv=1e-10, tolpdf=1e-10, convection=convection)
+    kw = dict(dt=1e-3, tolhv=1e-10, tolpdf=1e-10, convection=convection, stress=stress)
     ref = SplittingStepOracle(P, P["mask"], np.ones(n), vtrans, vdiff, qtl, **kw)
     dev = SplittingStep(lib, P["bm1"], P["binv"], P["mask"], np.ones(n), P["mult"], vtrans,
                         vdiff, qtl, **kw)
