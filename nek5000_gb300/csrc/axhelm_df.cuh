@@ -222,7 +222,7 @@ __device__ __forceinline__ void axhelm_df_body(const DfArgs& A, int blk, int tx,
     {
       float2 dd = sD[i * R], uu = slab[j * R];
       df_mul(urh, url, dd.x, dd.y, uu.x, uu.y);
-#pragma unroll
+#pragma unroll 2
       for (int l = 1; l < NX; ++l) {
         dd = sD[i * R + l];
         uu = slab[j * R + l];
@@ -233,7 +233,7 @@ __device__ __forceinline__ void axhelm_df_body(const DfArgs& A, int blk, int tx,
     {
       float2 uu = slab[i], dd = sD[j * R];
       df_mul(ush, usl, uu.x, uu.y, dd.x, dd.y);
-#pragma unroll
+#pragma unroll 2
       for (int l = 1; l < NX; ++l) {
         uu = slab[l * R + i];
         dd = sD[j * R + l];
@@ -299,7 +299,7 @@ __device__ __forceinline__ void axhelm_df_body(const DfArgs& A, int blk, int tx,
     {  // tm1(i,jk) = sum_l D(l,i) tmp1(l,jk)
       float2 dd = sDT[i * R], tt = s1[j * R];
       df_mul(ah, al, dd.x, dd.y, tt.x, tt.y);
-#pragma unroll
+#pragma unroll 2
       for (int l = 1; l < NX; ++l) {
         dd = sDT[i * R + l];
         tt = s1[j * R + l];
@@ -309,7 +309,7 @@ __device__ __forceinline__ void axhelm_df_body(const DfArgs& A, int blk, int tx,
     {  // tm2(i,j,k) = sum_l tmp2(i,l,k) D(l,j)
       float2 tt = s2[i], dd = sDT[j * R];
       df_mul(bh, bl, tt.x, tt.y, dd.x, dd.y);
-#pragma unroll
+#pragma unroll 2
       for (int l = 1; l < NX; ++l) {
         tt = s2[l * R + i];
         dd = sDT[j * R + l];
