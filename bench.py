@@ -72,7 +72,7 @@ def parse():
                              "adjoint", "velocity3", "ingest", "pressure"],
                     help="helmholtz: E=32^3 N=7 (default); poisson-n9: E=24^3 N=9 Poisson; "
                          "batch: 3 velocity solves + 61 uneven Poisson problems in one batch; "
-                         "axhelm-sweep: in-solve operator bandwidth at N=5,7,9, E=32^3; "
+                         "axhelm-sweep: in-solve operator bandwidth at N=5..9, E=32^3; "
                          "hsolve: a sequence of solves with projection onto previous solutions; "
                          "adjoint: dJ/dh1 through the adjoint solve, E=16^3 N=7; "
                          "velocity3: 3 velocity components in one fused mixed solve; "
@@ -703,7 +703,7 @@ def run_batch(args):
 
 
 def run_sweep(args):
-    """In-solve fused operator at N = 5, 7, 9 on the E=32^3 Helmholtz box:
+    """In-solve fused operator at N = 5...9 on the E=32^3 Helmholtz box:
     60 PCG iterations per precision, every operator launch timed with CUDA
     events; bytes per point are the fused operator's algorithmic 12 words."""
     import torch
@@ -715,7 +715,7 @@ def run_sweep(args):
     peak, peak_src = peaks()
     rows = []
     l0 = None
-    for N in (5, 7, 9):
+    for N in (5, 6, 7, 8, 9):
         M = workload(args.k, N)
         n = M["n"]
         lib = NekGpu(local)
@@ -745,7 +745,7 @@ def run_sweep(args):
         del a, binv, x, M
         torch.cuda.empty_cache()
     if rank == 0:
-        print(json.dumps({"metric": "fused operator HBM GB/s in the PCG, N=5,7,9",
+        print(json.dumps({"metric": "fused operator HBM GB/s in the PCG, N=5..9",
                           "unit": "GB/s", "peak": peak, "peak_source": peak_src,
                           "workload": f"helmholtz E={args.k}^3 h1=1 h2=10, 60 iterations",
                           "bytes_per_point": {"fp64": 96, "fp32": 48},
