@@ -45,12 +45,14 @@ def test_fp64_shapes_give_identical_solves(gpu_lib, oracle, nx1):
         assert np.array_equal(x, sols[0][2])
 
 
-@pytest.mark.parametrize("nx1", [8, 7, 9])
+@pytest.mark.parametrize("nx1", [8, 7, 9, 10])
 def test_fp32_shapes_give_identical_inner_solves(gpu_lib, oracle, nx1):
-    """Odd orders: 27 elements, so that the TMA-staged kernel's last block of
-    4 elements holds 3 and stages them with plain loads."""
+    """27 elements at lx1 = 7, 8, 9, so that the last block of every
+    multi-element shape is ragged (at odd lx1 the TMA-staged kernel's last
+    block of 4 elements holds 3 and stages them with plain loads), and 20 at
+    lx1 = 10 (the one-element kernel with its own register bound)."""
     torch = pytest.importorskip("torch")
-    P, f, h1, h2 = _problem(oracle, nx1, (3, 3, 4) if nx1 % 2 == 0 else (3, 3, 3), 10.0, 22)
+    P, f, h1, h2 = _problem(oracle, nx1, (5, 2, 2) if nx1 == 10 else (3, 3, 3), 10.0, 22)
     lib = gpu_lib(0)
     lib.setup(P["nx1"], P["nel"], P["D"], P["g"], P["bm1"], P["glo_num"])
     dev = lambda a: torch.tensor(a, device="cuda")
@@ -61,6 +63,7 @@ def test_fp32_shapes_give_identical_inner_solves(gpu_lib, oracle, nx1):
     by_kind = {}
     for kind, epb in cands:
         lib.set_ax_shape(1, kind, epb)
+        assert lib.ax_shape(1)[:2] == (kind, epb)
         x = torch.zeros(P["n"], dtype=torch.float64, device="cuda")
         no, ni, r0, r2, rc = lib.cggo_mixed(x, *args, 1, -1e-10, 10 ** 6, 1, dev(P["binv"]))
         assert rc == 0
