@@ -421,6 +421,40 @@ def run_gpu(args):
 
     peak, peak_src = peaks()
     flops_pt = 12 * M["lx1"] + 25
+    # ---- end to end through the host entry points ---------------------------------
+    # Each solver is timed on device arrays and then, right after, through its
+    # host entry point (pinned host arrays, the copies inside the timed region):
+    # the mixed solve first, then the FP64 ones.
+    per_call = {}
+    if not args.no_e2e:
+        pin = lambda a: torch.tensor(a).pin_memory().numpy()
+        rhs0 = pin(M["rhs"])
+        hb = {k: pin(M[k]) for k in ("h1", "h2", "mask", "mult", "binv")}
+        rhs = pin(M["rhs"])
+        u = pin(np.zeros(n))
+
+    def e2e(call, name):
+        np.copyto(rhs, rhs0)
+        call()  # warm the staging buffers
+        tot, ms = 0.0, []
+        barrier(pg)
+        for _ in range(args.steps):
+            np.copyto(rhs, rhs0)
+            t0 = time.perf_counter()
+            call()
+            dt = time.perf_counter() - t0
+            tot += dt
+            ms.append(round(1e3 * dt, 2))
+        barrier(pg)
+        per_call[name] = ms
+        return allmax(pg, tot)
+
+    rmx = timed(mixed)
+    x_mx = x.clone()
+    if not args.no_e2e:
+        tm = e2e(lambda: lib.hmholtz_mixed("TEMP", u, rhs, hb["h1"], hb["h2"], hb["mask"],
+                                           hb["mult"], 1, -args.tol, big, 1, hb["binv"],
+                                           inner_tol=args.inner_tol), "mixed")
     if args.only_mixed:  # profiling runs: iteration count of the FP64 solve not measured
         r64 = dict(iters=[0], T=1.0, ms_ax=float("nan"), launches=0, clocks=None)
     else:
@@ -468,8 +502,7 @@ def run_gpu(args):
                 float(torch.linalg.norm(x - x64) / torch.linalg.norm(x64)),
             "gpu_launches": rdf["launches"], "clocks": rdf["clocks"]}
         x_df = x.clone()
-    rmx = timed(mixed)
-    err64 = (float(torch.linalg.norm(x - x64) / torch.linalg.norm(x64))
+    err64 = (float(torch.linalg.norm(x_mx - x64) / torch.linalg.norm(x64))
              if x64 is not None else None)
     outer = [o for o, i in rmx["iters"]]
     inner = [i for o, i in rmx["iters"]]
@@ -527,41 +560,15 @@ def run_gpu(args):
                                             "(not measured in this run)") if ns32 else None},
             "gpu_launches": rmx["launches"],
             "clocks": rmx["clocks"]}
-    # ---- end to end through the host entry points -------------------------------
     if not args.no_e2e:
-        pin = lambda a: torch.tensor(a).pin_memory().numpy()
-        rhs0 = pin(M["rhs"])
-        hb = {k: pin(M[k]) for k in ("h1", "h2", "mask", "mult", "binv")}
-        rhs = pin(M["rhs"])
-        u = pin(np.zeros(n))
-
-        per_call = {}
-
-        def e2e(call, name):
-            np.copyto(rhs, rhs0)
-            call()  # warm the staging buffers
-            tot, ms = 0.0, []
-            barrier(pg)
-            for _ in range(args.steps):
-                np.copyto(rhs, rhs0)
-                t0 = time.perf_counter()
-                call()
-                dt = time.perf_counter() - t0
-                tot += dt
-                ms.append(round(1e3 * dt, 2))
-            barrier(pg)
-            per_call[name] = ms
-            return allmax(pg, tot)
-
-        tm = e2e(lambda: lib.hmholtz_mixed("TEMP", u, rhs, hb["h1"], hb["h2"], hb["mask"],
-                                           hb["mult"], 1, -args.tol, big, 1, hb["binv"],
-                                           inner_tol=args.inner_tol), "mixed")
         t6 = e2e(lambda: lib.hmholtz("TEMP", u, rhs, hb["h1"], hb["h2"], hb["mask"], hb["mult"], 1,
                                      -args.tol, big, 1, hb["binv"], maxcg=big), "fp64")
         line["e2e"] = {"value": allsum(pg, n * it64 * args.steps) / tm, "unit": "DOF-iters/s",
                        "h2d_bytes_per_step": 6 * 8 * n, "d2h_bytes_per_step": 2 * 8 * n,
                        "api": "nekgpu_hmholtz_mixed (host arrays, pinned)",
-                       "ms_per_call": per_call["mixed"]}
+                       "ms_per_call": per_call["mixed"],
+                       "measured": "right after the device-timed mixed solve, before the FP64 "
+                                   "solves"}
         fp64_block["e2e"] = {"value": allsum(pg, n * it64 * args.steps) / t6,
                              "unit": "DOF-iters/s", "api": "nekgpu_hmholtz (host arrays, pinned)"}
     # ---- CPU baseline (oracle) on rank 0, N=1 only ------------------------------
@@ -578,7 +585,7 @@ def run_gpu(args):
                                              "sample": f"{it1} iterations ({dt1:.1f} s)"}}
     # ---- parity against the oracle at this size (outside every timed region) ----
     if rank == 0 and ws == 1 and not args.no_parity and x64 is not None:
-        line["parity"] = oracle_parity(M, x64.cpu().numpy(), x.cpu().numpy(), it64,
+        line["parity"] = oracle_parity(M, x64.cpu().numpy(), x_mx.cpu().numpy(), it64,
                                        args.tol, os.cpu_count() or 1,
                                        None if df_block is None else x_df.cpu().numpy())
     if rank == 0:
