@@ -46,6 +46,27 @@ __device__ __forceinline__ void w_store(T* w, int i, T v, uint64_t pol) {
   else w[i] = v;
 }
 
+// Sum of a[q] for q = q0, q0 + st, ... < q1 (one lane's share of a fold),
+// with eight loads in flight: accumulator c takes terms c, c + 8, ... of the
+// sequence, and the eight are added in order (a fixed order for fixed
+// arguments).
+__device__ __forceinline__ double strided_sum_cg(const double* __restrict__ a, int q0, int q1,
+                                                 int st) {
+  double acc[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  int q = q0;
+  for (; q + 7 * st < q1; q += 8 * st) {
+#pragma unroll
+    for (int c = 0; c < 8; ++c) acc[c] += __ldcg(a + q + c * st);
+  }
+#pragma unroll
+  for (int c = 0; c < 7; ++c)
+    if (q + c * st < q1) acc[c] += __ldcg(a + q + c * st);
+  double s = acc[0];
+#pragma unroll
+  for (int c = 1; c < 8; ++c) s += acc[c];
+  return s;
+}
+
 template <typename T, int C, int G, bool RHO>
 __device__ __forceinline__ void gs_groups(const int* __restrict__ cidx, int s0, int step, int cnt,
                                           int goff, T* __restrict__ w, const T* __restrict__ p,
@@ -149,8 +170,7 @@ __device__ __forceinline__ void gs_cg_body(T* __restrict__ w, const T* __restric
     constexpr int kFoldChunk = 1024;
     double pa = 0.0;
     for (int c0 = blk * kFoldChunk; c0 < nA; c0 += nblk * kFoldChunk)
-      for (int q = c0 + threadIdx.x; q < min(c0 + kFoldChunk, nA); q += 32)
-        pa += __ldcg(partialA + q);
+      pa += strided_sum_cg(partialA, c0 + (int)threadIdx.x, min(c0 + kFoldChunk, nA), 32);
     pa = warp_sum(pa);
     unsigned int last = 0;
     if (threadIdx.x == 0) {
@@ -162,8 +182,7 @@ __device__ __forceinline__ void gs_cg_body(T* __restrict__ w, const T* __restric
     last = __shfl_sync(0xffffffffu, last, 0);
     if (!last) return;
     __threadfence();
-    double pb = 0.0;
-    for (int q = threadIdx.x; q < nblk; q += 32) pb += __ldcg(partialB + q);
+    double pb = strided_sum_cg(partialB, threadIdx.x, nblk, 32);
     pb = warp_sum(pb);
     if (threadIdx.x == 0) {
       cg->rho = pb;
