@@ -75,12 +75,12 @@ cudaError_t launch_adjoint(const Mesh& m, double* gh1, const double* lam, const 
   constexpr int P = NX * NX * NX;
   const int epb = axhelm_epb(NX);
   const size_t smem = (size_t)(NX * (NX + 1) + epb * 2 * P) * sizeof(double);
-  static bool configured = false;
-  if (!configured) {
+  static std::atomic<uint32_t> configured{0};  // per device
+  if (first_on_device(configured)) {
     cudaError_t e = cudaFuncSetAttribute(adjoint_h1_kernel<NX>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    configured = true;
+    mark_device(configured);
   }
   count_launch();
   adjoint_h1_kernel<NX><<<(m.nel + epb - 1) / epb, dim3(NX * NX, epb), smem, s>>>(

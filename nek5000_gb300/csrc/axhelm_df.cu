@@ -18,13 +18,13 @@ __global__ void split_pairs_kernel(float2* __restrict__ o, const double* __restr
 template <int NX, bool FUSED>
 cudaError_t launch_nx(const Mesh& m, const DfArgs& A, int epb, cudaStream_t s) {
   if (epb < 1 || epb * NX * NX > 256) epb = axhelm_epb(NX);
-  static bool configured = false;
-  if (!configured) {
+  static std::atomic<uint32_t> configured{0};  // per device
+  if (first_on_device(configured)) {
     cudaError_t e = cudaFuncSetAttribute(axhelm_df_kernel<NX, FUSED>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)axhelm_df_smem_bytes<NX>(axhelm_epb(NX)));
     if (e != cudaSuccess) return e;
-    configured = true;
+    mark_device(configured);
   }
   const int nb = (m.nel + epb - 1) / epb;
   count_launch();

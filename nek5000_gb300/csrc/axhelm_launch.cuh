@@ -19,13 +19,14 @@ static cudaError_t launch_ax_nx(const Mesh& m, const AxArgs<T>& a, int epb, int*
                                 cudaStream_t s) {
   if (epb < 1 || epb * NX * NX > 256) epb = axhelm_epb(NX);
   const size_t smem = axhelm_smem_bytes<NX, T>(epb);
-  static bool configured = false;  // per instantiation: room for the largest shape
-  if (!configured) {
+  // per instantiation and device: room for the largest shape
+  static std::atomic<uint32_t> configured{0};
+  if (first_on_device(configured)) {
     cudaError_t e = cudaFuncSetAttribute(axhelm_kernel<NX, T, EXACT, FUSED>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)axhelm_smem_bytes<NX, T>(axhelm_epb(NX)));
     if (e != cudaSuccess) return e;
-    configured = true;
+    mark_device(configured);
   }
   const int nb = (m.nel + epb - 1) / epb;
   if (nparts) *nparts = m.nel;

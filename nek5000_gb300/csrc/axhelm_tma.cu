@@ -18,13 +18,14 @@ template <int NX, bool FUSED, int EPB>
 cudaError_t launch_one(const Mesh& m, const AxArgs<float>& a, int* nparts, cudaStream_t s) {
   const size_t smem = tma_smem_bytes<NX, float, EPB>(FUSED, a.h1mode, a.h2mode);
   auto kern = tma_kernel<NX, FUSED, EPB>();
-  static bool configured = false;  // per instantiation: room for the largest slice set
-  if (!configured) {
+  // per instantiation and device: room for the largest slice set
+  static std::atomic<uint32_t> configured{0};
+  if (first_on_device(configured)) {
     const int maxb = (int)tma_smem_bytes<NX, float, EPB>(true, 1, 2);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, maxb);
     if (e != cudaSuccess) return e;
     cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-    configured = true;
+    mark_device(configured);
   }
   const int nb = (m.nel + EPB - 1) / EPB;
   if (nparts) *nparts = m.nel;

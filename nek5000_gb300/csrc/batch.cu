@@ -535,15 +535,16 @@ int batch_tables(Batch& B, const std::vector<int>& ids, const std::vector<Coef<T
 template <int NX>
 cudaError_t batch_tma_nx(const BDesc<float>* D, const BatchLaunch& L, int g, cudaStream_t s) {
   constexpr int EPB = batch_tma_epb<NX>();
-  static bool configured = false;  // room for the largest slice set
-  if (!configured) {
+  // room for the largest slice set, per device
+  static std::atomic<uint32_t> configured{0};
+  if (first_on_device(configured)) {
     cudaError_t e = cudaFuncSetAttribute(batch_axhelm_tma_kernel<NX, EPB>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)tma_smem_bytes<NX, float, EPB>(true, 1, 2));
     if (e != cudaSuccess) return e;
     cudaFuncSetAttribute(batch_axhelm_tma_kernel<NX, EPB>,
                          cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-    configured = true;
+    mark_device(configured);
   }
   batch_axhelm_tma_kernel<NX, EPB><<<L.gcount[g], dim3(NX * NX, EPB), L.gsmem[g], s>>>(
       D, L.mapA, L.baseA, L.gstart[g]);
@@ -556,13 +557,13 @@ cudaError_t batch_ops_nx(const BDesc<T>* D, const BatchLaunch& L, int g, cudaStr
   if constexpr (std::is_same<T, float>::value && tma_lx1(NX)) {
     if (L.gtma[g]) return batch_tma_nx<NX>(D, L, g, s);
   }
-  static bool configured = false;
-  if (!configured) {
+  static std::atomic<uint32_t> configured{0};  // per device
+  if (first_on_device(configured)) {
     cudaError_t e = cudaFuncSetAttribute(batch_axhelm_nx_kernel<T, NX>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)batch_smem<T>(NX, batch_epb(NX, kBatchThreads)));
     if (e != cudaSuccess) return e;
-    configured = true;
+    mark_device(configured);
   }
   batch_axhelm_nx_kernel<T, NX><<<L.gcount[g], L.threadsA, L.gsmem[g], s>>>(D, L.mapA, L.baseA,
                                                                            L.gstart[g]);
@@ -770,13 +771,13 @@ int batch_tune(Batch& B, const std::vector<int>& ids, const std::vector<Coef<T>>
 template <typename T>
 int batch_iterate_persistent(Batch& B, const std::vector<int>& ids, const BatchLaunch& L) {
   const int np = (int)ids.size();
-  static bool configured = false;
-  if (!configured) {
+  static std::atomic<uint32_t> configured{0};  // per device
+  if (first_on_device(configured)) {
     if (cudaFuncSetAttribute(batch_persistent_kernel<T>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)batch_smem_max<T>()) != cudaSuccess)
       return 1;
-    configured = true;
+    mark_device(configured);
   }
   int dev = 0, coop = 0, nsm = 0, per_sm = 0;
   cudaGetDevice(&dev);

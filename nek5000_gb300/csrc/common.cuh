@@ -32,6 +32,20 @@ inline void count_launch(long long k = 1) {
   if (!capturing()) launch_counter().fetch_add(k, std::memory_order_relaxed);
 }
 
+// Function attributes (the dynamic shared-memory limit, the carveout) belong
+// to a kernel on one device: a launch site sets them once per device it
+// launches on, recorded in a per-site mask of device bits.
+inline bool first_on_device(const std::atomic<uint32_t>& mask) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  return (mask.load(std::memory_order_relaxed) & (1u << (dev & 31))) == 0;
+}
+inline void mark_device(std::atomic<uint32_t>& mask) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  mask.fetch_or(1u << (dev & 31), std::memory_order_relaxed);
+}
+
 // ---- reductions: deterministic (fixed tree, no floating-point atomics) ----
 template <typename T>
 __device__ __forceinline__ T warp_sum(T v) {

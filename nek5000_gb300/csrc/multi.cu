@@ -330,15 +330,15 @@ __global__ void fold_kernel(float* __restrict__ md, float* __restrict__ mb,
 template <int NX>
 cudaError_t launch_op_nx(const MultiTmaArgs& m, cudaStream_t s) {
   const size_t smem = tma_smem_bytes<NX, float, 1>(true, m.base.h1mode, m.base.h2mode);
-  static bool configured = false;
-  if (!configured) {
+  static std::atomic<uint32_t> configured{0};  // per device
+  if (first_on_device(configured)) {
     const int maxb = (int)tma_smem_bytes<NX, float, 1>(true, 1, 2);
     cudaError_t e = cudaFuncSetAttribute(multi_op_kernel<NX>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, maxb);
     if (e != cudaSuccess) return e;
     cudaFuncSetAttribute(multi_op_kernel<NX>, cudaFuncAttributePreferredSharedMemoryCarveout,
                          100);
-    configured = true;
+    mark_device(configured);
   }
   count_launch();
   multi_op_kernel<NX><<<m.base.nel * m.nc, NX * NX, smem, s>>>(m);

@@ -634,15 +634,15 @@ inline int grid_for(int64_t n) {
 template <int NX, int EPB>
 cudaError_t launch_k1_nx(const SplitArgs& a, int nblk, cudaStream_t s) {
   const int hb = a.h2mode ? 1 : 0, hh1 = a.h1mode == 1 ? 1 : 0, hh2 = a.h2mode == 2 ? 1 : 0;
-  static bool configured = false;
-  if (!configured) {
+  static std::atomic<uint32_t> configured{0};  // per device
+  if (first_on_device(configured)) {
     const int maxb = (int)split_smem_bytes<NX, EPB>(1, 1, 1);
     cudaError_t e = cudaFuncSetAttribute(split_ax_kernel<NX, EPB>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, maxb);
     if (e != cudaSuccess) return e;
     cudaFuncSetAttribute(split_ax_kernel<NX, EPB>, cudaFuncAttributePreferredSharedMemoryCarveout,
                          100);
-    configured = true;
+    mark_device(configured);
   }
   count_launch();
   split_ax_kernel<NX, EPB><<<nblk, dim3(NX * NX, EPB), split_smem_bytes<NX, EPB>(hb, hh1, hh2), s>>>(a);

@@ -153,13 +153,13 @@ template <int NX>
 cudaError_t launch_axsf_nx(const Mesh& m, double* au, double* av, double* aw, const double* u,
                            const double* v, const double* w, const double* h1, const double* h2,
                            cudaStream_t s) {
-  static bool configured = false;
-  if (!configured) {
+  static std::atomic<uint32_t> configured{0};  // per device
+  if (first_on_device(configured)) {
     cudaError_t e = cudaFuncSetAttribute(axsf_kernel<NX>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)axsf_smem_bytes<NX>());
     if (e != cudaSuccess) return e;
-    configured = true;
+    mark_device(configured);
   }
   count_launch();
   axsf_kernel<NX><<<m.nel, NX * NX, axsf_smem_bytes<NX>(), s>>>(
