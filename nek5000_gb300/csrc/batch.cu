@@ -800,7 +800,8 @@ int batch_iterate_persistent(Batch& B, const std::vector<int>& ids, const BatchL
             *bC = L.baseC;
   void* args[] = {(void*)&D, &npp, (void*)&mA, (void*)&bA, &gA, (void*)&mB, (void*)&bB, &gB,
                   (void*)&mC, (void*)&bC, &gC, &kmax, (void*)&bar, (void*)&perr};
-  for (;;) {
+  std::vector<char> running(np, 0);
+  for (int round = 0;; ++round) {
     for (int q = 0; q < np; ++q)
       cudaMemcpyAsync(&B.cg_host_all[q], B.probs[ids[q]]->cg, sizeof(CgScalars),
                       cudaMemcpyDeviceToHost, B.stream);
@@ -808,9 +809,14 @@ int batch_iterate_persistent(Batch& B, const std::vector<int>& ids, const BatchL
       B.err = std::string("batch: ") + cudaGetErrorString(cudaGetLastError());
       return -3;
     }
-    bool all = true;
-    for (int q = 0; q < np; ++q) all = all && B.cg_host_all[q].done;
-    if (all) break;
+    bool all = true, stopped = false;
+    for (int q = 0; q < np; ++q) {
+      const bool done = B.cg_host_all[q].done != 0;
+      all = all && done;
+      if (round == 0) running[q] = !done;
+      else stopped = stopped || (running[q] && done);
+    }
+    if (all || (any && stopped)) break;
     cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned int), B.stream);
     cudaMemsetAsync(perr, 0, sizeof(int), B.stream);
     count_launch();
@@ -838,7 +844,10 @@ int batch_iterate_persistent(Batch& B, const std::vector<int>& ids, const BatchL
 // first: run the iteration-1 check of freshly prepared problems first (not
 // after a residual replacement, which sets the scalars itself).
 template <typename T>
-int batch_iterate(Batch& B, const std::vector<int>& ids, const BatchLaunch& L, bool first = true) {
+// Runs chunks of batched iterations until every problem has stopped, or with
+// `any` until at least one problem that was running on entry has stopped.
+int batch_iterate(Batch& B, const std::vector<int>& ids, const BatchLaunch& L, bool first = true,
+                  bool any = false) {
   const int np = (int)ids.size();
   const BDesc<T>* D = reinterpret_cast<const BDesc<T>*>(L.desc);
   if (first) {
@@ -880,7 +889,8 @@ int batch_iterate(Batch& B, const std::vector<int>& ids, const BatchLaunch& L, b
       B.gkey = key;
     }
   }
-  for (;;) {
+  std::vector<char> running(np, 0);
+  for (int round = 0;; ++round) {
     for (int q = 0; q < np; ++q)
       cudaMemcpyAsync(&B.cg_host_all[q], B.probs[ids[q]]->cg, sizeof(CgScalars),
                       cudaMemcpyDeviceToHost, B.stream);
@@ -888,9 +898,14 @@ int batch_iterate(Batch& B, const std::vector<int>& ids, const BatchLaunch& L, b
       B.err = std::string("batch: ") + cudaGetErrorString(cudaGetLastError());
       return -3;
     }
-    bool all = true;
-    for (int q = 0; q < np; ++q) all = all && B.cg_host_all[q].done;
-    if (all) break;
+    bool all = true, stopped = false;
+    for (int q = 0; q < np; ++q) {
+      const bool done = B.cg_host_all[q].done != 0;
+      all = all && done;
+      if (round == 0) running[q] = !done;
+      else stopped = stopped || (running[q] && done);
+    }
+    if (all || (any && stopped)) break;
     cudaError_t e;
     if (graph) {
       count_launch((2LL + L.ngrp) * B.chunk);
@@ -1110,52 +1125,89 @@ int batch_solve_mixed(Batch& B, int np, double* const* x, const double* const* f
       const int rc = batch_tune<float>(B, ids, coefs, xs, ms, bs);
       if (rc) return rc;
     }
+    // Each problem gets its FP64 residual and replacement as soon as its own
+    // FP32 PCG stops (checked after every chunk), and runs on while the
+    // others do; a problem that has converged stays in the tables, its
+    // blocks returning at once, until the stopped problems hold a quarter of
+    // the tables' points -- then the tables (and the captured chunk) are
+    // rebuilt without them.
     bool first = true;
-    for (int upd = 1; !ids.empty() && upd <= 100000; ++upd) {
-      BatchLaunch L;
-      int rc = batch_tables<float>(B, ids, coefs, xs, ms, bs, L);
-      if (rc) return rc;
-      rc = batch_iterate<float>(B, ids, L, first);
+    std::vector<char> live(ids.size(), 1);
+    int64_t tab_pts = 0, dead_pts = 0;
+    for (int p : ids) tab_pts += B.probs[p]->mesh.n;
+    BatchLaunch L;
+    bool rebuild = true;
+    for (int round = 1; !ids.empty() && round <= 100000; ++round) {
+      if (rebuild) {
+        const int rc = batch_tables<float>(B, ids, coefs, xs, ms, bs, L);
+        if (rc) return rc;
+        rebuild = false;
+      }
+      int rc = batch_iterate<float>(B, ids, L, first, true);
       if (rc) return rc;
       first = false;
-      std::vector<int> keep;
-      std::vector<Coef<float>> kc;
-      std::vector<float*> kx;
-      std::vector<const float*> km, kb;
+      int nlive = 0;
       for (size_t q = 0; q < ids.size(); ++q) {
+        if (!live[q]) continue;
         const int p = ids[q];
         Handle& h = *B.probs[p];
+        if (!h.cg_host->done) {
+          ++nlive;
+          continue;
+        }
         const int64_t n = h.mesh.n;
         const bool capped = h.cg_host->iter > h.cg_host->maxiter;
         niter[p] = h.cg_host->niter;
-        nouter[p] = upd;
+        ++nouter[p];
         axpy_f32(h, x[p], h.w32.x.ptr, scale[p], n);
         const double rnew = outer_residual(h, h.w64.r.ptr, f[p], x[p], c64[p], mask[p], mult[p],
                                            binv[p], h.w64.w.ptr);
+        bool stop = false;
         if (!(rnew >= 0.0) || !std::isfinite(rnew)) {
           status[p] = NEKGPU_ENAN;
-          continue;
+          stop = true;
+        } else {
+          const bool progress = rnew < rbn[p];
+          rbn[p] = rbn2[p] = rnew;
+          if (rnew <= tol[p] || capped || !progress) {
+            stop = true;
+          } else {
+            const int rr = mixed_replace(h, scale[p], inner_tol, nullptr);
+            if (rr < 0) status[p] = NEKGPU_ECUDA;
+            stop = rr != 0;
+          }
         }
-        const bool progress = rnew < rbn[p];
-        rbn[p] = rbn2[p] = rnew;
-        if (rnew <= tol[p] || capped || !progress) continue;
-        const int rr = mixed_replace(h, scale[p], inner_tol, nullptr);
-        if (rr < 0) {
-          status[p] = NEKGPU_ECUDA;
-          continue;
+        if (stop) {
+          live[q] = 0;
+          dead_pts += n;
+        } else {
+          ++nlive;
         }
-        if (rr == 1) continue;
-        keep.push_back(p);
-        kc.push_back(coefs[q]);
-        kx.push_back(xs[q]);
-        km.push_back(ms[q]);
-        kb.push_back(bs[q]);
       }
-      ids.swap(keep);
-      coefs.swap(kc);
-      xs.swap(kx);
-      ms.swap(km);
-      bs.swap(kb);
+      if (nlive == 0) break;
+      if (4 * dead_pts > tab_pts) {
+        std::vector<int> keep;
+        std::vector<Coef<float>> kc;
+        std::vector<float*> kx;
+        std::vector<const float*> km, kb;
+        for (size_t q = 0; q < ids.size(); ++q) {
+          if (!live[q]) continue;
+          keep.push_back(ids[q]);
+          kc.push_back(coefs[q]);
+          kx.push_back(xs[q]);
+          km.push_back(ms[q]);
+          kb.push_back(bs[q]);
+        }
+        ids.swap(keep);
+        coefs.swap(kc);
+        xs.swap(kx);
+        ms.swap(km);
+        bs.swap(kb);
+        live.assign(ids.size(), 1);
+        tab_pts -= dead_pts;
+        dead_pts = 0;
+        rebuild = true;
+      }
     }
   }
   for (int outer = 1; mode != 1 && outer <= kMaxOuter; ++outer) {
