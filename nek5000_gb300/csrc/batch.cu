@@ -58,6 +58,18 @@ namespace {
 
 constexpr int kBatchThreads = 256;
 
+// Every problem's PCG scalars into one array (one warp per problem), so that
+// the host reads them with one copy after a chunk.
+template <typename T>
+__global__ void __launch_bounds__(256)
+    batch_gather_cg_kernel(const BDesc<T>* __restrict__ D, int np, CgScalars* __restrict__ out) {
+  const int q = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+  if (q >= np) return;
+  const unsigned int* src = reinterpret_cast<const unsigned int*>(D[q].cg);
+  unsigned int* dst = reinterpret_cast<unsigned int*>(out + q);
+  for (int w = threadIdx.x % 32; w < (int)(sizeof(CgScalars) / 4); w += 32) dst[w] = __ldcg(src + w);
+}
+
 template <typename T, int NX>
 __device__ __forceinline__ void batch_ax_nx(const AxArgs<T>& a, int blk, int epb,
                                             unsigned char* smem, double* red) {
@@ -349,6 +361,7 @@ struct Batch {
   bool persistent = false;
   DevBuf<unsigned int> bar;  // the persistent launch's barrier words
   DevBuf<int> perr;          // and its error flag
+  DevBuf<CgScalars> cg_all;  // the problems' scalars gathered after a chunk
   // operator block size per precision ([0] FP64, [1] FP32): picked by
   // batch_tune for the problem set in tkey, or pinned (pinned[prec] != 0)
   int threads[2] = {0, 0};
@@ -800,23 +813,19 @@ int batch_iterate_persistent(Batch& B, const std::vector<int>& ids, const BatchL
             *bC = L.baseC;
   void* args[] = {(void*)&D, &npp, (void*)&mA, (void*)&bA, &gA, (void*)&mB, (void*)&bB, &gB,
                   (void*)&mC, (void*)&bC, &gC, &kmax, (void*)&bar, (void*)&perr};
-  std::vector<char> running(np, 0);
-  for (int round = 0;; ++round) {
-    for (int q = 0; q < np; ++q)
-      cudaMemcpyAsync(&B.cg_host_all[q], B.probs[ids[q]]->cg, sizeof(CgScalars),
-                      cudaMemcpyDeviceToHost, B.stream);
+  if (B.cg_all.ensure(np)) return -4;
+  for (;;) {
+    count_launch();
+    batch_gather_cg_kernel<T><<<(np + 7) / 8, 256, 0, B.stream>>>(D, np, B.cg_all.ptr);
+    cudaMemcpyAsync(B.cg_host_all, B.cg_all.ptr, sizeof(CgScalars) * np, cudaMemcpyDeviceToHost,
+                    B.stream);
     if (cudaStreamSynchronize(B.stream) != cudaSuccess) {
       B.err = std::string("batch: ") + cudaGetErrorString(cudaGetLastError());
       return -3;
     }
-    bool all = true, stopped = false;
-    for (int q = 0; q < np; ++q) {
-      const bool done = B.cg_host_all[q].done != 0;
-      all = all && done;
-      if (round == 0) running[q] = !done;
-      else stopped = stopped || (running[q] && done);
-    }
-    if (all || (any && stopped)) break;
+    bool all = true;
+    for (int q = 0; q < np; ++q) all = all && B.cg_host_all[q].done;
+    if (all) break;  // (one launch runs until every problem has stopped)
     cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned int), B.stream);
     cudaMemsetAsync(perr, 0, sizeof(int), B.stream);
     count_launch();
@@ -843,9 +852,9 @@ int batch_iterate_persistent(Batch& B, const std::vector<int>& ids, const BatchL
 
 // first: run the iteration-1 check of freshly prepared problems first (not
 // after a residual replacement, which sets the scalars itself).
-template <typename T>
 // Runs chunks of batched iterations until every problem has stopped, or with
 // `any` until at least one problem that was running on entry has stopped.
+template <typename T>
 int batch_iterate(Batch& B, const std::vector<int>& ids, const BatchLaunch& L, bool first = true,
                   bool any = false) {
   const int np = (int)ids.size();
@@ -890,10 +899,12 @@ int batch_iterate(Batch& B, const std::vector<int>& ids, const BatchLaunch& L, b
     }
   }
   std::vector<char> running(np, 0);
+  if (B.cg_all.ensure(np)) return -4;
   for (int round = 0;; ++round) {
-    for (int q = 0; q < np; ++q)
-      cudaMemcpyAsync(&B.cg_host_all[q], B.probs[ids[q]]->cg, sizeof(CgScalars),
-                      cudaMemcpyDeviceToHost, B.stream);
+    count_launch();
+    batch_gather_cg_kernel<T><<<(np + 7) / 8, 256, 0, B.stream>>>(D, np, B.cg_all.ptr);
+    cudaMemcpyAsync(B.cg_host_all, B.cg_all.ptr, sizeof(CgScalars) * np, cudaMemcpyDeviceToHost,
+                    B.stream);
     if (cudaStreamSynchronize(B.stream) != cudaSuccess) {
       B.err = std::string("batch: ") + cudaGetErrorString(cudaGetLastError());
       return -3;
