@@ -157,3 +157,32 @@ def test_persistent_launch_equals_graph_launches(gpu_lib, oracle, problems, mixe
     assert ra["niter"] == rb["niter"] and ra["rbn2"] == rb["rbn2"]
     for a, b in zip(xa, xb):
         assert np.array_equal(a, b)
+
+
+def test_batch_mixed_problem_independent_of_the_others(gpu_lib, oracle, problems):
+    """Residual replacement runs per problem as soon as its FP32 PCG stops,
+    while the others go on, and the launch tables drop converged problems
+    now and then: a problem's solve must not depend on that schedule.  Each
+    problem solved in a batch of its own gives the batched result bit for
+    bit (outer steps, inner iterations, norms, x)."""
+    torch = pytest.importorskip("torch")
+    from nek5000_gb300 import NekGpuBatch
+    col = lambda ps, k: [_dev(torch, P[k]) for P in ps]
+
+    def run(ps):
+        B = NekGpuBatch(0)
+        for P in ps:
+            B.add(P["nx1"], P["nel"], P["D"], P["g"], P["bm1"], P["glo_num"])
+        xs = [torch.zeros(P["n"], dtype=torch.float64, device="cuda") for P in ps]
+        res = B.solve(xs, col(ps, "f"), col(ps, "h1v"), col(ps, "h2v"), col(ps, "mask"),
+                      col(ps, "mult"), col(ps, "binv"), tin=-1e-10, mixed=1)
+        B.close()
+        return res, [x.cpu().numpy() for x in xs]
+
+    res, xs = run(problems)
+    assert res["status"] == [0] * len(problems)
+    for q, P in enumerate(problems):
+        r1, x1 = run([P])
+        for key in ("status", "niter", "nouter", "rbn0", "rbn2"):
+            assert r1[key][0] == res[key][q], (q, key, r1[key][0], res[key][q])
+        assert np.array_equal(x1[0], xs[q]), q
